@@ -1,0 +1,462 @@
+// extern "C" entry points of include/ib_gpu.h.
+#include <cstring>
+#include <string>
+
+#include "ctx.cuh"
+
+using ib::Ctx;
+
+static thread_local std::string g_err;
+
+static int fail(int rc, const char* what) {
+  g_err = what;
+  return rc;
+}
+
+struct IbCtx {
+  Ctx* c;
+};
+
+namespace {
+
+bool is_device(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Resolves an argument array to device memory: device pointers are used in
+// place, host arrays are copied into (and, for outputs, back from) one of the
+// context's staging buffers.
+struct Staging {
+  Ctx* c;
+  int next = 0;
+  struct Out { double* dev; double* host; size_t n; };
+  Out outs[8];
+  int nout = 0;
+  int rc = IB_OK;
+  explicit Staging(Ctx* cc) : c(cc) {}
+  double* in(const double* p, size_t n) {
+    if (!p) { rc = IB_ERR_ARG; return nullptr; }
+    if (is_device(p)) return const_cast<double*>(p);
+    if (next >= 8 || n > c->stage_n) { rc = IB_ERR_ARG; return nullptr; }
+    double* d = c->stage[next++];
+    if (cudaMemcpyAsync(d, p, 8 * n, cudaMemcpyHostToDevice, c->st) != cudaSuccess) rc = IB_ERR_CUDA;
+    return d;
+  }
+  double* out(double* p, size_t n, bool copy_in) {
+    if (!p) { rc = IB_ERR_ARG; return nullptr; }
+    if (is_device(p)) return p;
+    if (next >= 8 || n > c->stage_n) { rc = IB_ERR_ARG; return nullptr; }
+    double* d = c->stage[next++];
+    if (copy_in && cudaMemcpyAsync(d, p, 8 * n, cudaMemcpyHostToDevice, c->st) != cudaSuccess) rc = IB_ERR_CUDA;
+    outs[nout++] = {d, p, n};
+    return d;
+  }
+  int finish(int op_rc) {
+    if (op_rc != IB_OK) { cudaStreamSynchronize(c->st); return op_rc; }
+    for (int i = 0; i < nout; ++i)
+      if (cudaMemcpyAsync(outs[i].host, outs[i].dev, 8 * outs[i].n, cudaMemcpyDeviceToHost, c->st) != cudaSuccess)
+        return IB_ERR_CUDA;
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) return IB_ERR_CUDA;
+    return IB_OK;
+  }
+};
+
+#define CTX_OR_FAIL(h)                                             \
+  if (!(h) || !(h)->c) return fail(IB_ERR_ARG, "null context");    \
+  Ctx* c = (h)->c;
+
+#define STAGE_CHECK(S) \
+  if ((S).rc != IB_OK) return fail((S).rc, "bad array argument");
+
+int op_result(int rc, const char* what) {
+  if (rc != IB_OK) {
+    cudaError_t e = cudaGetLastError();
+    std::string m = what;
+    if (e != cudaSuccess) m += std::string(": ") + cudaGetErrorString(e);
+    return fail(rc, m.c_str());
+  }
+  return IB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ib_last_error(void) { return g_err.c_str(); }
+int ib_version(void) { return 1; }
+
+int ib_create(const IbParams* p, const IbBody* bodies, int nbody, IbCtx** out) {
+  if (!p || !out) return fail(IB_ERR_ARG, "null argument");
+  std::string msg;
+  Ctx* c = nullptr;
+  int rc = ib::ctx_create(p, bodies, nbody, &c, &msg);
+  if (rc != IB_OK) return fail(rc, msg.c_str());
+  *out = new IbCtx{c};
+  return IB_OK;
+}
+
+int ib_destroy(IbCtx* h) {
+  if (!h) return IB_OK;
+  ib::ctx_destroy(h->c);
+  delete h;
+  return IB_OK;
+}
+
+int ib_synchronize(IbCtx* h) {
+  CTX_OR_FAIL(h);
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  return IB_OK;
+}
+
+int ib_advance(IbCtx* h, int* itime) {
+  CTX_OR_FAIL(h);
+  int rc = ib::op_advance(c);
+  if (itime) *itime = c->itime;
+  return op_result(rc, "advance failed");
+}
+
+static int field_ptr(Ctx* c, int field, int level, double** p, size_t* n) {
+  if (level < 0 || level >= c->L) return IB_ERR_ARG;
+  switch (field) {
+    case IB_FIELD_OMEGA: *p = c->omega[level]; *n = c->g.ns; break;
+    case IB_FIELD_S: *p = c->s[level]; *n = c->g.ns; break;
+    case IB_FIELD_QX: *p = c->qx[level]; *n = c->g.nu; break;
+    case IB_FIELD_QY: *p = c->qy[level]; *n = c->g.nv; break;
+    case IB_FIELD_RHS_OLD: *p = c->rhs_old[level]; *n = c->g.ns; break;
+    case IB_FIELD_Q0X: *p = c->q0x[level]; *n = c->g.nu; break;
+    case IB_FIELD_Q0Y: *p = c->q0y[level]; *n = c->g.nv; break;
+    default: return IB_ERR_ARG;
+  }
+  return IB_OK;
+}
+
+int ib_get_field(IbCtx* h, int field, int level, double* out) {
+  CTX_OR_FAIL(h);
+  double* p; size_t n;
+  if (!out || field_ptr(c, field, level, &p, &n)) return fail(IB_ERR_ARG, "bad field or level");
+  if (cudaMemcpyAsync(out, p, 8 * n, cudaMemcpyDefault, c->st) != cudaSuccess ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  return IB_OK;
+}
+
+int ib_set_field(IbCtx* h, int field, int level, const double* in) {
+  CTX_OR_FAIL(h);
+  double* p; size_t n;
+  if (!in || field_ptr(c, field, level, &p, &n)) return fail(IB_ERR_ARG, "bad field or level");
+  if (cudaMemcpyAsync(p, in, 8 * n, cudaMemcpyDefault, c->st) != cudaSuccess ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  return IB_OK;
+}
+
+static double* vec_ptr(Ctx* c, int which) {
+  switch (which) {
+    case IB_VEC_F: return c->f;
+    case IB_VEC_F_RDST: return c->f_rdst;
+    case IB_VEC_XB: return c->xb;
+    case IB_VEC_YB: return c->yb;
+    default: return nullptr;
+  }
+}
+
+int ib_get_vector(IbCtx* h, int which, double* out) {
+  CTX_OR_FAIL(h);
+  double* p = vec_ptr(c, which);
+  if (!p || !out) return fail(IB_ERR_ARG, "bad vector");
+  if (c->nf == 0) return IB_OK;
+  if (cudaMemcpyAsync(out, p, 8 * (size_t)c->nf, cudaMemcpyDefault, c->st) != cudaSuccess ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  return IB_OK;
+}
+
+int ib_set_vector(IbCtx* h, int which, const double* in) {
+  CTX_OR_FAIL(h);
+  double* p = vec_ptr(c, which);
+  if (!p || !in) return fail(IB_ERR_ARG, "bad vector");
+  if (c->nf == 0) return IB_OK;
+  if (cudaMemcpyAsync(p, in, 8 * (size_t)c->nf, cudaMemcpyDefault, c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  int rc = IB_OK;
+  if (which == IB_VEC_XB || which == IB_VEC_YB) rc = ib::op_reg_prep(c);
+  if (rc == IB_OK) rc = ib::check_err(c);
+  return op_result(rc, "set_vector failed");
+}
+
+int ib_get_forces(IbCtx* h, double* cx, double* cy) {
+  CTX_OR_FAIL(h);
+  if (!cx || !cy) return fail(IB_ERR_ARG, "null output");
+  if (c->nbody == 0) return IB_OK;
+  int rc = ib::launch_force_coeffs(c->nf, c->nbody, c->comp, c->bid, c->f, c->p.dt, c->delta, c->forces, c->st);
+  if (rc) return op_result(rc, "force coefficients failed");
+  if (cudaMemcpyAsync(cx, c->forces, 8 * (size_t)c->nbody, cudaMemcpyDefault, c->st) != cudaSuccess ||
+      cudaMemcpyAsync(cy, c->forces + c->nbody, 8 * (size_t)c->nbody, cudaMemcpyDefault, c->st) != cudaSuccess ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  return IB_OK;
+}
+
+int ib_get_body_state(IbCtx* h, double* theta, double* thetad, double* thetadd) {
+  CTX_OR_FAIL(h);
+  if (c->nt == 0) return IB_OK;
+  size_t n = 8 * (size_t)c->nt;
+  if ((theta && cudaMemcpyAsync(theta, c->ts.theta, n, cudaMemcpyDefault, c->st) != cudaSuccess) ||
+      (thetad && cudaMemcpyAsync(thetad, c->ts.thetad, n, cudaMemcpyDefault, c->st) != cudaSuccess) ||
+      (thetadd && cudaMemcpyAsync(thetadd, c->ts.thetadd, n, cudaMemcpyDefault, c->st) != cudaSuccess) ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  return IB_OK;
+}
+
+int ib_get_counters(IbCtx* h, int* ksp_iter, int* fsi_iter) {
+  CTX_OR_FAIL(h);
+  if (ksp_iter) *ksp_iter = c->ksp_iter;
+  if (fsi_iter) *fsi_iter = c->fsi_iter;
+  return IB_OK;
+}
+
+int ib_get_dims(IbCtx* h, int* nf, int* nbc, int* ns, int* nu, int* nv) {
+  CTX_OR_FAIL(h);
+  if (nf) *nf = c->nf;
+  if (nbc) *nbc = c->g.nbc;
+  if (ns) *ns = c->g.ns;
+  if (nu) *nu = c->g.nu;
+  if (nv) *nv = c->g.nv;
+  return IB_OK;
+}
+
+// ------------------------------------------------------------ operators
+int ib_nonlinear(IbCtx* h, const double* omega, const double* qx, const double* qy, const double* bc, double* nlx,
+                 double* nly) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* o = S.in(omega, c->g.ns);
+  const double* x = S.in(qx, c->g.nu);
+  const double* y = S.in(qy, c->g.nv);
+  const double* r = S.in(bc, c->g.nbc);
+  double* a = S.out(nlx, c->g.nu, false);
+  double* b = S.out(nly, c->g.nv, false);
+  STAGE_CHECK(S);
+  int rc = ib::launch_nonlinear(c->g, o, r, x, nullptr, y, nullptr, a, b, c->st);
+  return op_result(S.finish(rc), "nonlinear failed");
+}
+
+int ib_rot(IbCtx* h, const double* hx, const double* hy, double* vort) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* x = S.in(hx, c->g.nu);
+  const double* y = S.in(hy, c->g.nv);
+  double* v = S.out(vort, c->g.ns, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::launch_rot(c->g, x, y, v, c->st)), "rot failed");
+}
+
+int ib_curl(IbCtx* h, const double* s, const double* sbc, double* qx, double* qy) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* sv = S.in(s, c->g.ns);
+  const double* r = S.in(sbc, c->g.nbc);
+  double* a = S.out(qx, c->g.nu, false);
+  double* b = S.out(qy, c->g.nv, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::launch_curl(c->g, sv, r, a, b, c->st)), "curl failed");
+}
+
+int ib_coarsify(IbCtx* h, const double* fine, double* coarse) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* f = S.in(fine, c->g.ns);
+  double* o = S.out(coarse, c->g.ns, true);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::launch_coarsify(c->g, f, o, c->st)), "coarsify failed");
+}
+
+int ib_get_bc(IbCtx* h, const double* s, double fac, double* ring) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* sv = S.in(s, c->g.ns);
+  double* r = S.out(ring, c->g.nbc, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::launch_get_bc(c->g, sv, fac, r, c->st)), "get_bc failed");
+}
+
+int ib_apply_bc(IbCtx* h, double* vort, const double* ring, double fac) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* r = S.in(ring, c->g.nbc);
+  double* v = S.out(vort, c->g.ns, true);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::launch_apply_bc(c->g, v, r, fac, c->st)), "apply_bc failed");
+}
+
+int ib_dst(IbCtx* h, const double* in, double* out) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* i = S.in(in, c->g.ns);
+  double* o = S.out(out, c->g.ns, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::op_dst(c, i, o)), "dst failed");
+}
+
+int ib_ctci(IbCtx* h, const double* vort, double* s) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* i = S.in(vort, c->g.ns);
+  double* o = S.out(s, c->g.ns, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::op_ctci(c, i, o, nullptr)), "ctci failed");
+}
+
+int ib_ainv(IbCtx* h, double* vort) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  double* v = S.out(vort, c->g.ns, true);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::op_ainv(c, v, v)), "ainv failed");
+}
+
+int ib_fluid_predictor(IbCtx* h, int level, double* omega, const double* rhs, const double* rhs_old,
+                       const double* rhsbc) {
+  CTX_OR_FAIL(h);
+  if (level < 0 || level >= c->L) return fail(IB_ERR_ARG, "bad level");
+  Staging S(c);
+  const double* a = S.in(rhs, c->g.ns);
+  const double* b = S.in(rhs_old, c->g.ns);
+  const double* r = S.in(rhsbc, c->g.ns);
+  double* o = S.out(omega, c->g.ns, true);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::op_predictor(c, level, o, a, b, r)), "fluid_predictor failed");
+}
+
+int ib_vort2flux(IbCtx* h, double* omega, double* s, double* qx, double* qy) {
+  CTX_OR_FAIL(h);
+  const int L = c->L;
+  Staging S(c);
+  double* w = S.out(omega, (size_t)L * c->g.ns, true);
+  double* sv = S.out(s, (size_t)L * c->g.ns, false);
+  double* a = S.out(qx, (size_t)L * c->g.nu, false);
+  double* b = S.out(qy, (size_t)L * c->g.nv, false);
+  STAGE_CHECK(S);
+  std::vector<double*> W(L), SS(L), QX(L), QY(L);
+  for (int k = 0; k < L; ++k) {
+    W[k] = w + (size_t)k * c->g.ns; SS[k] = sv + (size_t)k * c->g.ns;
+    QX[k] = a + (size_t)k * c->g.nu; QY[k] = b + (size_t)k * c->g.nv;
+  }
+  return op_result(S.finish(ib::op_vort2flux(c, W.data(), SS.data(), QX.data(), QY.data(), true)),
+                   "vort2flux failed");
+}
+
+int ib_reg_prep(IbCtx* h, const double* xb, const double* yb) {
+  CTX_OR_FAIL(h);
+  if (c->nf == 0) return IB_OK;
+  if (cudaMemcpyAsync(c->xb, xb, 8 * (size_t)c->nf, cudaMemcpyDefault, c->st) != cudaSuccess ||
+      cudaMemcpyAsync(c->yb, yb, 8 * (size_t)c->nf, cudaMemcpyDefault, c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  int rc = ib::op_reg_prep(c);
+  if (rc == IB_OK) rc = ib::check_err(c);
+  return op_result(rc, "reg_prep failed (stencil outside the grid?)");
+}
+
+int ib_reg(IbCtx* h, const double* h0, double* hx, double* hy) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* f = S.in(h0, c->nf);
+  double* a = S.out(hx, c->g.nu, false);
+  double* b = S.out(hy, c->g.nv, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::launch_reg(c->g, c->nf, f, c->reg, a, b, c->st)), "reg failed");
+}
+
+int ib_regT(IbCtx* h, const double* hx, const double* hy, double* h0) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* a = S.in(hx, c->g.nu);
+  const double* b = S.in(hy, c->g.nv);
+  double* o = S.out(h0, c->nf, true);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::launch_regT(c->g, c->nf, a, nullptr, b, nullptr, c->reg, o, o, c->st)),
+                   "regT failed");
+}
+
+int ib_redistribute(IbCtx* h, const double* f, double* frdst) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* a = S.in(f, c->nf);
+  double* o = S.out(frdst, c->nf, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::op_redistribute(c, a, o)), "redistribute failed");
+}
+
+int ib_schur_apply(IbCtx* h, const double* x, double* y) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* a = S.in(x, c->nf);
+  double* o = S.out(y, c->nf, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::op_schur(c, a, o, true)), "schur_apply failed");
+}
+
+int ib_schur_apply_fluid(IbCtx* h, const double* x, double* y) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* a = S.in(x, c->nf);
+  double* o = S.out(y, c->nf, false);
+  STAGE_CHECK(S);
+  return op_result(S.finish(ib::op_schur(c, a, o, false)), "schur_apply_fluid failed");
+}
+
+int ib_struct_btimes(IbCtx* h, const double* x, double* y) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* a = S.in(x, c->nf);
+  double* o = S.out(y, c->nf, false);
+  STAGE_CHECK(S);
+  int rc = cudaMemsetAsync(o, 0, 8 * (size_t)c->nf, c->st) == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+  if (rc == IB_OK) rc = ib::launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, a, o, c->st);
+  return op_result(S.finish(rc), "struct_btimes failed");
+}
+
+int ib_struct_rhs(IbCtx* h, double* y) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  double* o = S.out(y, c->nf, false);
+  STAGE_CHECK(S);
+  int rc = cudaMemsetAsync(o, 0, 8 * (size_t)c->nf, c->st) == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+  if (rc == IB_OK) rc = ib::launch_tors_rhs(c->nt, c->tb, c->ts, c->p.dt, c->delta, o, c->st);
+  return op_result(S.finish(rc), "struct_rhs failed");
+}
+
+int ib_struct_dx(IbCtx* h, const double* f, double* err) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* a = S.in(f, c->nf);
+  STAGE_CHECK(S);
+  int rc = ib::launch_tors_dx(c->nt, c->tb, c->ts, c->p.dt, c->delta, a, c->xb, c->yb, c->err_fsi, c->st);
+  if (rc == IB_OK && c->nt > 0) rc = ib::op_reg_prep(c);
+  rc = S.finish(rc);
+  if (rc == IB_OK && err) {
+    if (cudaMemcpy(err, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) rc = IB_ERR_CUDA;
+  }
+  if (rc == IB_OK) rc = ib::check_err(c);
+  return op_result(rc, "struct_dx failed");
+}
+
+int ib_schur_solve(IbCtx* h, const double* rhs, double* f, int* iterations) {
+  CTX_OR_FAIL(h);
+  Staging S(c);
+  const double* b = S.in(rhs, c->nf);
+  double* x = S.out(f, c->nf, true);
+  STAGE_CHECK(S);
+  int its = 0, reason = 0;
+  int rc = ib::op_gmres(c, b, x, &its, &reason);
+  if (iterations) *iterations = its;
+  return op_result(S.finish(rc), "schur_solve failed");
+}
+
+}  // extern "C"

@@ -1,0 +1,99 @@
+// Device-resident simulation context: all state of variables.F90 for one rank,
+// the spectral tables of myfft.F90, body data, Krylov workspace, and the stream
+// every kernel of this simulation runs on.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/ib_gpu.h"
+#include "dst.cuh"
+#include "kernels.cuh"
+
+namespace ib {
+
+// Bump allocator over one device allocation made at ib_create.
+struct DevPool {
+  char* base = nullptr;
+  size_t cap = 0, used = 0;
+  template <typename T>
+  T* take(size_t n) {
+    size_t bytes = ((n * sizeof(T) + 255) / 256) * 256;
+    if (used + bytes > cap) return nullptr;
+    T* p = reinterpret_cast<T*>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+struct Ctx {
+  IbParams p{};
+  GridDims g{};
+  int L = 0;
+  double delta = 0, normalize = 0;
+  cudaStream_t st = nullptr;
+  DevPool pool;
+
+  DstPlan px, py;
+  DstLaunch lx, ly_none, ly_diag, ly_pred;
+
+  // spectral tables (myfft.F90:125-148), each (n-1)(m-1)
+  double* laminv = nullptr;        // 1/lam/normalize
+  double* lam1i_n = nullptr;       // lam1i(:,:,1)/normalize (ainv)
+  std::vector<double*> lam1, lam1i;
+  std::vector<double> vfac, con1, con2;
+
+  // state per level
+  std::vector<double*> omega, s, qx, qy, q0x, q0y, rhs_old;
+  // Schur-operator scratch per level
+  std::vector<double*> mv_w, mv_s, mv_qx, mv_qy;
+  // work arrays
+  double *spec1 = nullptr, *spec2 = nullptr, *rhs = nullptr, *rhsbc = nullptr;
+  double *nlx = nullptr, *nly = nullptr, *hx = nullptr, *hy = nullptr, *vort = nullptr;
+  std::vector<double*> lastbc;
+  double *omegabc = nullptr, *sbc = nullptr, *zero_ring = nullptr;
+
+  // bodies
+  int nbody = 0, nb = 0, nf = 0, nt = 0;
+  std::vector<IbBody> bodies_h;
+  std::vector<int> comp_h, bid_h;
+  std::vector<TorsBody> tb_h;
+  double *f = nullptr, *f_rdst = nullptr, *xb = nullptr, *yb = nullptr;
+  double *rhsf = nullptr, *tmpf = nullptr, *tmpf2 = nullptr, *forces = nullptr;
+  int *comp = nullptr, *bid = nullptr;
+  RegDev reg{};
+  TorsBody* tb = nullptr;
+  TorsState ts{};
+  double* err_fsi = nullptr;       // [0] max |dtheta|, [1..nt] per body
+  GmresDev G{};
+  double* cholM = nullptr;         // nf x nf (num_stat)
+  bool chol_ready = false;
+
+  // host-visible status
+  int* d_err = nullptr;
+  int* h_ist = nullptr;            // pinned mirror of G.ist
+  double* h_scal = nullptr;        // pinned mirror of err_fsi[0]
+
+  // staging for host pointers passed to operator entry points
+  double* stage[8] = {nullptr};
+  size_t stage_n = 0;
+
+  int itime = 0, ksp_iter = 0, fsi_iter = 0;
+};
+
+// solver.cu
+int ctx_create(const IbParams* p, const IbBody* bodies, int nbody, Ctx** out, std::string* msg);
+void ctx_destroy(Ctx* c);
+int op_ctci(Ctx* c, const double* in, double* out, const double* ring);  // ring: apply_bc(fac 1) on a copy
+int op_ainv(Ctx* c, const double* in, double* out);
+int op_dst(Ctx* c, const double* in, double* out);
+int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs_old, const double* rhsbc);
+int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy,
+                 bool all_curls);
+int op_schur(Ctx* c, const double* x, double* y, bool with_b);
+int op_redistribute(Ctx* c, const double* f, double* frdst);
+int op_reg_prep(Ctx* c);
+int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason);
+int op_advance(Ctx* c);
+int check_err(Ctx* c);
+
+}  // namespace ib

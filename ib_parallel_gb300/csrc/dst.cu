@@ -1,0 +1,409 @@
+// Batched DST-I kernels (see dst.cuh for the algorithm).
+#include "dst.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace ib {
+
+// ---------------------------------------------------------------- tables
+// exp(-2 pi i num/den) evaluated in long double and rounded to double.
+static double2 twiddle(long long num, long long den) {
+  const long double PI_L = 3.141592653589793238462643383279502884L;
+  long long r = num % den;
+  if (r < 0) r += den;
+  long double a = 2.0L * PI_L * (long double)r / (long double)den;
+  return make_double2((double)cosl(a), (double)(-sinl(a)));
+}
+
+static bool factor_radices(int P, int* rad, int* nrad) {
+  // radix-5 and radix-3 stages first (no twiddles in the first stage), then 4, then 2.
+  int n = 0, q = P;
+  while (q % 5 == 0) { rad[n++] = 5; q /= 5; }
+  while (q % 3 == 0) { rad[n++] = 3; q /= 3; }
+  while (q % 4 == 0) { rad[n++] = 4; q /= 4; }
+  while (q % 2 == 0) { rad[n++] = 2; q /= 2; }
+  if (q != 1 || n > kMaxRadices) return false;
+  *nrad = n;
+  return true;
+}
+
+int dst_plan_create(DstPlan* p, int N) {
+  int M = N + 1;
+  if (N < 3 || M % 4 != 0) return IB_ERR_ARG;
+  p->N = N; p->M = M; p->P = M / 2;
+  if (!factor_radices(p->P, p->rad, &p->nrad)) return IB_ERR_ARG;
+  std::vector<double2> tw(p->P), uw(p->P / 2);
+  std::vector<double> sn(p->P + 1);
+  for (int t = 0; t < p->P; ++t) tw[t] = twiddle(t, p->P);
+  for (int k = 0; k < p->P / 2; ++k) uw[k] = twiddle(k, M);
+  const long double PI_L = 3.141592653589793238462643383279502884L;
+  for (int j = 0; j <= p->P; ++j) sn[j] = (double)sinl(PI_L * (long double)j / (long double)M);
+  if (cudaMalloc(&p->tw, sizeof(double2) * p->P) != cudaSuccess) return IB_ERR_NOMEM;
+  if (cudaMalloc(&p->uw, sizeof(double2) * (p->P / 2)) != cudaSuccess) return IB_ERR_NOMEM;
+  if (cudaMalloc(&p->sn, sizeof(double) * (p->P + 1)) != cudaSuccess) return IB_ERR_NOMEM;
+  IB_CUDA_CHECK(cudaMemcpy(p->tw, tw.data(), sizeof(double2) * p->P, cudaMemcpyHostToDevice));
+  IB_CUDA_CHECK(cudaMemcpy(p->uw, uw.data(), sizeof(double2) * (p->P / 2), cudaMemcpyHostToDevice));
+  IB_CUDA_CHECK(cudaMemcpy(p->sn, sn.data(), sizeof(double) * (p->P + 1), cudaMemcpyHostToDevice));
+  return IB_OK;
+}
+
+void dst_plan_destroy(DstPlan* p) {
+  if (p->tw) cudaFree(p->tw);
+  if (p->uw) cudaFree(p->uw);
+  if (p->sn) cudaFree(p->sn);
+  p->tw = p->uw = nullptr; p->sn = nullptr;
+}
+
+// ------------------------------------------------------- device helpers
+__device__ __forceinline__ double2 cmul(double2 a, double2 w) {
+  return make_double2(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+template <int R> struct Dft;
+template <> struct Dft<2> {
+  __device__ static void run(double2* v) {
+    double2 a = v[0], b = v[1];
+    v[0] = cadd(a, b); v[1] = csub(a, b);
+  }
+};
+template <> struct Dft<4> {
+  __device__ static void run(double2* v) {
+    double2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    double2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    // y1 = d02 - i d13, y3 = d02 + i d13
+    v[1] = make_double2(d02.x + d13.y, d02.y - d13.x);
+    v[3] = make_double2(d02.x - d13.y, d02.y + d13.x);
+  }
+};
+template <> struct Dft<3> {
+  __device__ static void run(double2* v) {
+    const double h = 0.86602540378443864676;  // sin(2 pi/3)
+    double2 t = cadd(v[1], v[2]);
+    double2 d = csub(v[1], v[2]);
+    double2 a = make_double2(fma(-0.5, t.x, v[0].x), fma(-0.5, t.y, v[0].y));
+    v[0] = cadd(v[0], t);
+    v[1] = make_double2(fma(h, d.y, a.x), fma(-h, d.x, a.y));
+    v[2] = make_double2(fma(-h, d.y, a.x), fma(h, d.x, a.y));
+  }
+};
+template <> struct Dft<5> {
+  __device__ static void run(double2* v) {
+    const double c1 = 0.30901699437494742410;   // cos(2 pi/5)
+    const double c2 = -0.80901699437494742410;  // cos(4 pi/5)
+    const double s1 = 0.95105651629515357212;   // sin(2 pi/5)
+    const double s2 = 0.58778525229247312917;   // sin(4 pi/5)
+    double2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+    double2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
+    double2 x0 = v[0];
+    double2 a1 = make_double2(fma(c2, t2.x, fma(c1, t1.x, x0.x)), fma(c2, t2.y, fma(c1, t1.y, x0.y)));
+    double2 a2 = make_double2(fma(c1, t2.x, fma(c2, t1.x, x0.x)), fma(c1, t2.y, fma(c2, t1.y, x0.y)));
+    double2 b1 = make_double2(fma(s2, d2.x, s1 * d1.x), fma(s2, d2.y, s1 * d1.y));
+    double2 b2 = make_double2(fma(-s1, d2.x, s2 * d1.x), fma(-s1, d2.y, s2 * d1.y));
+    v[0] = cadd(cadd(x0, t1), t2);
+    v[1] = make_double2(a1.x + b1.y, a1.y - b1.x);
+    v[4] = make_double2(a1.x - b1.y, a1.y + b1.x);
+    v[2] = make_double2(a2.x + b2.y, a2.y - b2.x);
+    v[3] = make_double2(a2.x - b2.y, a2.y + b2.x);
+  }
+};
+
+// One Stockham stage over B lines (line b at in + b*P).
+template <int R>
+__device__ __forceinline__ void stockham_stage(const double2* __restrict__ in, double2* __restrict__ out,
+                                               int P, int Ns, const double2* __restrict__ tw, int B,
+                                               int tid, int NT) {
+  const int nb = P / R;
+  const int total = B * nb;
+  const int twstep = P / (Ns * R);
+  for (int it = tid; it < total; it += NT) {
+    int b = it / nb;
+    int j = it - b * nb;
+    const double2* src = in + b * P;
+    double2* dst = out + b * P;
+    int k = j % Ns;
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * twstep]));
+    }
+    Dft<R>::run(v);
+    int idxD = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[idxD + r * Ns] = v[r];
+  }
+}
+
+struct DstDev {
+  int N, M, P, nrad;
+  int rad[kMaxRadices];
+  const double2* tw;
+  const double2* uw;
+  const double* sn;
+};
+
+static DstDev to_dev(const DstPlan& p) {
+  DstDev d;
+  d.N = p.N; d.M = p.M; d.P = p.P; d.nrad = p.nrad;
+  for (int i = 0; i < kMaxRadices; ++i) d.rad[i] = p.rad[i];
+  d.tw = p.tw; d.uw = p.uw; d.sn = p.sn;
+  return d;
+}
+
+// Transform B lines in place: line b holds x_1..x_N at xb[b*ldx + 0..N-1] and
+// receives Y_1..Y_N there.  zA, zB: B*P complex workspace each.
+__device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2* zA, double2* zB) {
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const int P = pl.P, M = pl.M;
+  // --- pre-processing: y (length M, real) written into zA viewed as doubles
+  for (int it = tid; it < B * P; it += NT) {
+    int b = it / P;
+    int t = it - b * P;
+    const double* x = xb + b * ldx;
+    double* y = reinterpret_cast<double*>(zA + b * P);
+    if (t == 0) {
+      double xp = x[P - 1];
+      y[0] = 0.0;
+      y[P] = xp + xp;
+    } else {
+      double xj = x[t - 1], xm = x[M - t - 1];
+      double a = xj + xm;
+      double h = 0.5 * (xj - xm);
+      double s = __ldg(&pl.sn[t]);
+      y[t] = fma(s, a, h);
+      y[M - t] = fma(s, a, -h);
+    }
+  }
+  __syncthreads();
+  // --- complex FFT of length P (Stockham, ping-pong zA <-> zB)
+  double2* cur = zA;
+  double2* nxt = zB;
+  int Ns = 1;
+  for (int s = 0; s < pl.nrad; ++s) {
+    int R = pl.rad[s];
+    switch (R) {
+      case 2: stockham_stage<2>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
+      case 3: stockham_stage<3>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
+      case 4: stockham_stage<4>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
+      default: stockham_stage<5>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
+    }
+    Ns *= R;
+    __syncthreads();
+    double2* t = cur; cur = nxt; nxt = t;
+  }
+  // --- unpack the real FFT: even outputs directly, odd increments in place
+  const int H = P / 2;
+  for (int it = tid; it < B * H; it += NT) {
+    int b = it / H;
+    int k = it - b * H;
+    const double2* Z = cur + b * P;
+    double* o = xb + b * ldx;
+    if (k == 0) {
+      double2 z0 = Z[0];
+      double2 zh = Z[H];
+      o[0] = z0.x + z0.y;     // D_1
+      o[P - 1] = zh.y + zh.y; // D_P
+      o[P] = zh.x + zh.x;     // Re(2Y_{P/2})
+    } else {
+      double2 zk = Z[k], zp = Z[P - k];
+      double2 E = make_double2(zk.x + zp.x, zk.y - zp.y);
+      double2 O = make_double2(zk.y + zp.y, zp.x - zk.x);
+      double2 T = cmul(O, __ldg(&pl.uw[k]));
+      o[2 * k - 1] = -E.y - T.y;
+      o[2 * k] = E.x + T.x;
+      o[2 * (P - k) - 1] = E.y - T.y;
+      o[2 * (P - k)] = E.x - T.x;
+    }
+  }
+  __syncthreads();
+  // --- inclusive prefix sum over positions 0,2,...,2(P-1): odd outputs
+  const int lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
+  const int c = (P + 31) >> 5;
+  for (int b = warp; b < B; b += nwarps) {
+    double* o = xb + b * ldx;
+    int s0 = lane * c;
+    int s1 = min(s0 + c, P);
+    double acc = 0.0;
+    for (int i = s0; i < s1; ++i) acc += o[2 * i];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      double v = __shfl_up_sync(0xffffffffu, acc, off);
+      if (lane >= off) acc += v;
+    }
+    double run = __shfl_up_sync(0xffffffffu, acc, 1);
+    if (lane == 0) run = 0.0;
+    for (int i = s0; i < s1; ++i) {
+      run += o[2 * i];
+      o[2 * i] = run;
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------- x pass
+template <int PRE>
+__global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, DstXArgs a, GridDims g, int B) {
+  extern __shared__ double2 smem2[];
+  const int ldx = pl.M;
+  double* xb = reinterpret_cast<double*>(smem2);
+  double2* zA = smem2 + (B * ldx) / 2;
+  double2* zB = zA + B * pl.P;
+  const int N = pl.N;
+  const int row0 = blockIdx.x * B;
+  for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
+    int b = it / N, j = it - b * N;
+    int row = row0 + b;
+    double v = 0.0;
+    if (row < nrows) {
+      size_t idx = (size_t)row * ld + j;
+      if (PRE == PRE_COPY) {
+        v = a.in[idx];
+      } else if (PRE == PRE_COMBINE) {
+        v = fma(a.cb, a.in2[idx], a.ca * a.in[idx]) + a.in3[idx];
+      } else {
+        // apply_bc (operators_fluid.F90:539-549): left, right, bottom, top
+        v = a.in[idx];
+        int I = j + 2, J = row + 2;
+        if (I == 2) v = v + a.fac * a.ring[g.left + J - 1];
+        if (I == g.m) v = v + a.fac * a.ring[g.right + J - 1];
+        if (J == 2) v = v + a.fac * a.ring[g.bottom + I - 1];
+        if (J == g.n) v = v + a.fac * a.ring[g.top + I - 1];
+      }
+    }
+    xb[b * ldx + j] = v;
+  }
+  __syncthreads();
+  dst_lines(pl, B, xb, ldx, zA, zB);
+  for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
+    int b = it / N, j = it - b * N;
+    int row = row0 + b;
+    if (row < nrows) a.out[(size_t)row * ld + j] = xb[b * ldx + j];
+  }
+}
+
+// ------------------------------------------------------------- y pass
+template <int MODE>
+__global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, DstYArgs a, int B) {
+  extern __shared__ double2 smem2[];
+  const int ldx = pl.M;
+  const int N = pl.N;
+  double* xa = reinterpret_cast<double*>(smem2);
+  double* xbb = xa + B * ldx;
+  double2* zA = reinterpret_cast<double2*>(MODE == YMODE_PRED ? xbb + B * ldx : xbb);
+  double2* zB = zA + B * pl.P;
+  const int col0 = blockIdx.x * B;
+  for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
+    int j = it / B, b = it - j * B;
+    int col = col0 + b;
+    double v = 0.0, w = 0.0;
+    if (col < ncols) {
+      size_t idx = (size_t)j * ld + col;
+      v = a.a[idx];
+      if (MODE == YMODE_PRED) w = a.b[idx];
+    }
+    xa[b * ldx + j] = v;
+    if (MODE == YMODE_PRED) xbb[b * ldx + j] = w;
+  }
+  __syncthreads();
+  dst_lines(pl, B, xa, ldx, zA, zB);
+  if (MODE == YMODE_PRED) dst_lines(pl, B, xbb, ldx, zA, zB);
+  if (MODE != YMODE_NONE) {
+    for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
+      int j = it / B, b = it - j * B;
+      int col = col0 + b;
+      if (col < ncols) {
+        size_t idx = (size_t)j * ld + col;
+        if (MODE == YMODE_DIAG) {
+          xa[b * ldx + j] = a.t1[idx] * xa[b * ldx + j];
+        } else {
+          // lam1i * (dst(rhs) + lam1 * dst(omega))   (operators_fluid.F90:657-661)
+          xa[b * ldx + j] = a.t1[idx] * fma(a.t2[idx], xbb[b * ldx + j], xa[b * ldx + j]);
+        }
+      }
+    }
+    __syncthreads();
+    dst_lines(pl, B, xa, ldx, zA, zB);
+  }
+  for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
+    int j = it / B, b = it - j * B;
+    int col = col0 + b;
+    if (col < ncols) a.a[(size_t)j * ld + col] = xa[b * ldx + j];
+  }
+}
+
+size_t dst_smem_x(const DstPlan& p, int B) { return (size_t)B * p.M * 8 * 3; }
+size_t dst_smem_y(const DstPlan& p, int B, DstYMode mode) {
+  return (size_t)B * p.M * 8 * (mode == YMODE_PRED ? 4 : 3);
+}
+
+template <typename K>
+static int launch_cfg(K kern, size_t smem) {
+  static_assert(sizeof(K) > 0, "");
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return IB_ERR_CUDA;
+  }
+  return IB_OK;
+}
+
+int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs& a, const GridDims& g,
+               const DstLaunch& L, cudaStream_t st) {
+  DstDev d = to_dev(px);
+  size_t smem = dst_smem_x(px, L.B);
+  dim3 grid(cdiv(nrows, L.B));
+  int rc = IB_OK;
+  switch (pre) {
+    case PRE_COPY:
+      rc = launch_cfg(k_dst_x<PRE_COPY>, smem);
+      if (rc) return rc;
+      k_dst_x<PRE_COPY><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      break;
+    case PRE_COMBINE:
+      rc = launch_cfg(k_dst_x<PRE_COMBINE>, smem);
+      if (rc) return rc;
+      k_dst_x<PRE_COMBINE><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      break;
+    default:
+      rc = launch_cfg(k_dst_x<PRE_APPLYBC>, smem);
+      if (rc) return rc;
+      k_dst_x<PRE_APPLYBC><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      break;
+  }
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int dst_pass_y(const DstPlan& py, int ncols, int ld, DstYMode mode, const DstYArgs& a, const DstLaunch& L,
+               cudaStream_t st) {
+  DstDev d = to_dev(py);
+  size_t smem = dst_smem_y(py, L.B, mode);
+  dim3 grid(cdiv(ncols, L.B));
+  int rc = IB_OK;
+  switch (mode) {
+    case YMODE_NONE:
+      rc = launch_cfg(k_dst_y<YMODE_NONE>, smem);
+      if (rc) return rc;
+      k_dst_y<YMODE_NONE><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
+      break;
+    case YMODE_DIAG:
+      rc = launch_cfg(k_dst_y<YMODE_DIAG>, smem);
+      if (rc) return rc;
+      k_dst_y<YMODE_DIAG><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
+      break;
+    default:
+      rc = launch_cfg(k_dst_y<YMODE_PRED>, smem);
+      if (rc) return rc;
+      k_dst_y<YMODE_PRED><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
+      break;
+  }
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+}  // namespace ib

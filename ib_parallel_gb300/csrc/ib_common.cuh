@@ -1,0 +1,73 @@
+// Common definitions for the GB300 immersed-boundary time step.
+//
+// Layouts follow the reference (nirmaljp6/IB_Parallel, one rank, natural
+// PETSc ordering, x fastest):
+//   vertex field (omega, s, rhs):  (n-1) rows x (m-1) cols, element (I,J) of the
+//       Fortran grid (I=2..m, J=2..n) at [(J-2)*(m-1) + (I-2)]   (grid.F90:186-203)
+//   u-face flux qx:  n rows x (m+1) cols, face (i,j) at [(j-1)*(m+1) + (i-1)]
+//   v-face flux qy:  (n+1) rows x m cols, face (i,j) at [(j-1)*m + (i-1)]
+//   boundary ring (nbc = 2(m+1)+2(n+1)): left[0..n], right[0..n], bottom[0..m],
+//       top[0..m]                                               (grid.F90:224-228)
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#define IB_OK 0
+#define IB_ERR_ARG 1
+#define IB_ERR_CUDA 2
+#define IB_ERR_NOMEM 3
+#define IB_ERR_GMRES 4
+#define IB_ERR_FSI 5
+#define IB_ERR_NONFINITE 6
+#define IB_ERR_DOMAIN 7
+#define IB_ERR_STATE 8
+
+namespace ib {
+
+struct GridDims {
+  int m, n;          // cells in x and y of one level
+  int nsx, nsy;      // vertex interior: m-1, n-1
+  int ns;            // (m-1)(n-1)
+  int nux, nuy;      // u-faces: m+1, n
+  int nu;
+  int nvx, nvy;      // v-faces: m, n+1
+  int nv;
+  int nbc;           // ring length
+  int left, right, bottom, top;
+  __host__ __device__ void init(int m_, int n_) {
+    m = m_; n = n_;
+    nsx = m - 1; nsy = n - 1; ns = nsx * nsy;
+    nux = m + 1; nuy = n; nu = nux * nuy;
+    nvx = m; nvy = n + 1; nv = nvx * nvy;
+    nbc = 2 * (m + 1) + 2 * (n + 1);
+    left = 0; right = n + 1; bottom = 2 * (n + 1); top = 2 * (n + 1) + m + 1;
+  }
+};
+
+// Ghosted vertex value at grid point (I,J), I=1..m+1, J=1..n+1: interior from the
+// field, edges from the ring with the precedence left, right, bottom, top
+// (later writes win at corners), as operators_fluid.F90:448-451 and 563-566 do.
+__device__ __forceinline__ double ghost_vertex(const double* __restrict__ f,
+                                               const double* __restrict__ ring,
+                                               const GridDims& g, int I, int J) {
+  if (J == 1) return ring[g.bottom + I - 1];
+  if (J == g.n + 1) return ring[g.top + I - 1];
+  if (I == 1) return ring[g.left + J - 1];
+  if (I == g.m + 1) return ring[g.right + J - 1];
+  return f[(J - 2) * g.nsx + (I - 2)];
+}
+
+inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace ib
+
+#define IB_CUDA_CHECK(expr)                                                     \
+  do {                                                                          \
+    cudaError_t _e = (expr);                                                    \
+    if (_e != cudaSuccess) {                                                    \
+      fprintf(stderr, "ib_gpu CUDA error %s at %s:%d\n", cudaGetErrorString(_e), \
+              __FILE__, __LINE__);                                              \
+      return IB_ERR_CUDA;                                                       \
+    }                                                                           \
+  } while (0)

@@ -1,0 +1,316 @@
+// Regularised delta-function transfer between body points and the finest grid:
+// E^T (reg, fsinterface.F90:14-47), E (regT, fsinterface.F90:51-80), the weights
+// (setup_reg, grid.F90:459-528; deltafnc, grid.F90:955-1003), force
+// redistribution (operators_struct.F90:735-834) and force coefficients
+// (write_force2, operators_struct.F90:711-731).
+//
+// reg is a face-major gather: for every face of the stencil bounding box the
+// contributing unknowns are listed in ascending order, so each face sums its
+// contributions in the same order as the reference's sequential scatter-add.
+#include "kernels.cuh"
+
+namespace ib {
+
+// Smoothed 6-point delta function.  Literals without a d exponent in the Fortran
+// source are default REAL, i.e. single precision: they appear as float literals.
+__device__ double deltafnc_dev(double x1, double x2, double dr) {
+  double r = fabs(x1 - x2);
+  double r1 = r / dr;
+  double r2 = r1 * r1;
+  double r3 = r2 * r1;
+  double r4 = r3 * r1;
+  const double s3 = sqrt(3.0);
+  double v;
+  if (r1 <= 1.0) {
+    double a5 = asin((1.0 / 2.0) * s3 * (2.0 * r1 - 1.0));
+    double a8 = sqrt(1.0 - 12.0 * r2 + 12.0 * r1);
+    v = 0.4166666667e-1 * r4 + ((double)(-.1388888889f) + 0.3472222222e-1 * a8) * r3 +
+        (-0.7121664902e-1 - 0.5208333333e-1 * a8 + (double)(0.2405626122f) * a5) * r2 +
+        (-(double)(.2405626122f) * a5 - (double)(.3792313933f) + (double)(.1012731481f) * a8) * r1 +
+        0.8018753741e-1 * a5 - 0.4195601852e-1 * a8 + (double)(.6485698427f);
+  } else if (r1 <= 2.0) {
+    double a6 = asin((1.0 / 2.0) * s3 * (-3.0 + 2.0 * r1));
+    double a9 = sqrt(-23.0 + 36.0 * r1 - 12.0 * r2);
+    v = -0.6250000000e-1 * r4 + ((double)(.4861111111f) - 0.1736111111e-1 * a9) * r3 +
+        ((double)(-1.143175026f) + 0.7812500000e-1 * a9 - (double)(.1202813061f) * a6) * r2 +
+        ((double)(.8751991178f) + (double)(.3608439183f) * a6 - (double)(.1548032407f) * a9) * r1 -
+        (double)(.2806563809f) * a6 + 0.822848104e-2 + (double)(.1150173611f) * a9;
+  } else if (r1 <= 3.0) {
+    double a1 = asin((1.0 / 2.0 * (2.0 * r1 - 5.0)) * s3);
+    double a7 = sqrt(-71.0 - 12.0 * r2 + 60.0 * r1);
+    v = 0.2083333333e-1 * r4 + (0.3472222222e-2 * a7 - (double)(.2638888889f)) * r3 +
+        ((double)(1.214391675f) - 0.2604166667e-1 * a7 + 0.2405626122e-1 * a1) * r2 +
+        (-(double)(.1202813061f) * a1 - (double)(2.449273192f) + 0.7262731481e-1 * a7) * r1 +
+        (double)(.1523563211f) * a1 + (double)(1.843201677f) - 0.7306134259e-1 * a7;
+  } else {
+    v = 0.0;
+  }
+  return v / dr;
+}
+
+// Per unknown: stencil origin and the 49 weights (l outer, p inner).
+__global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb, const double* __restrict__ yb,
+                              double d, double ox, double oy, const int* __restrict__ comp, int* ix, int* iy,
+                              double* w, int* err) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nf) return;
+  double xk = xb[k], yk = yb[k];
+  int cx = (int)((xk + ox) / d) + 1;   // Fortran INT truncates toward zero
+  int cy = (int)((yk + oy) / d) + 1;
+  ix[k] = cx;
+  iy[k] = cy;
+  const double d2 = 0.5 * d;
+  bool isx = comp[k] == 1;
+  // faces touched: u-face i in [1,m+1], j in [1,n]; v-face i in [1,m], j in [1,n+1]
+  int imax = isx ? g.m + 1 : g.m, jmax = isx ? g.n : g.n + 1;
+  if (cx - 3 < 1 || cx + 3 > imax || cy - 3 < 1 || cy + 3 > jmax) atomicExch(err, IB_ERR_DOMAIN);
+  double dx[7], dy[7];
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    int off = q - 3;
+    double x = d * (double)(cx - 1 + off) - ox;
+    double y = d * (double)(cy - 1 + off) - oy;
+    if (isx) y = y + d2; else x = x + d2;
+    dx[q] = deltafnc_dev(x, xk, d);
+    dy[q] = deltafnc_dev(y, yk, d);
+  }
+  double* wk = w + (size_t)k * 49;
+#pragma unroll
+  for (int l = 0; l < 7; ++l)
+#pragma unroll
+    for (int p = 0; p < 7; ++p) wk[l * 7 + p] = d * d * dx[p] * dy[l];
+}
+
+// Bounding box of all stencils (one CTA).
+__global__ void k_reg_bbox(int nf, const int* __restrict__ ix, const int* __restrict__ iy, int* bbox) {
+  __shared__ int s[4][32];
+  int imin = 1 << 30, jmin = 1 << 30, imax = -(1 << 30), jmax = -(1 << 30);
+  for (int k = threadIdx.x; k < nf; k += blockDim.x) {
+    imin = min(imin, ix[k]); imax = max(imax, ix[k]);
+    jmin = min(jmin, iy[k]); jmax = max(jmax, iy[k]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    imin = min(imin, __shfl_xor_sync(0xffffffffu, imin, o));
+    imax = max(imax, __shfl_xor_sync(0xffffffffu, imax, o));
+    jmin = min(jmin, __shfl_xor_sync(0xffffffffu, jmin, o));
+    jmax = max(jmax, __shfl_xor_sync(0xffffffffu, jmax, o));
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { s[0][wid] = imin; s[1][wid] = imax; s[2][wid] = jmin; s[3][wid] = jmax; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nw = blockDim.x >> 5;
+    for (int q = 1; q < nw; ++q) {
+      imin = min(imin, s[0][q]); imax = max(imax, s[1][q]);
+      jmin = min(jmin, s[2][q]); jmax = max(jmax, s[3][q]);
+    }
+    if (nf == 0) { imin = imax = jmin = jmax = 4; }
+    bbox[0] = imin - 3;
+    bbox[1] = jmin - 3;
+    bbox[2] = imax - imin + 7;
+    bbox[3] = jmax - jmin + 7;
+  }
+}
+
+// Count (fill=false) or list (fill=true) contributions per box face, ascending k.
+template <bool FILL>
+__global__ void k_reg_lists(int nf, const int* __restrict__ comp, const int* __restrict__ ix,
+                            const int* __restrict__ iy, const int* __restrict__ bbox, int* cnt_x, int* cnt_y,
+                            int* lst_x, int* lst_y, int max_faces) {
+  int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
+  int nface = ni * nj;
+  if (nface + 1 > max_faces) return;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * nface; t += gridDim.x * blockDim.x) {
+    int c = t < nface ? 1 : 2;
+    int fidx = t < nface ? t : t - nface;
+    int fi = i0 + fidx % ni, fj = j0 + fidx / ni;
+    int* cnt = c == 1 ? cnt_x : cnt_y;
+    int* lst = c == 1 ? lst_x : lst_y;
+    int pos = FILL ? cnt[fidx] : 0;
+    int n = 0;
+    for (int k = 0; k < nf; ++k) {
+      if (comp[k] != c) continue;
+      int p = fi - ix[k], l = fj - iy[k];
+      if (p >= -3 && p <= 3 && l >= -3 && l <= 3) {
+        if (FILL) lst[pos + n] = k * 49 + (l + 3) * 7 + (p + 3);
+        ++n;
+      }
+    }
+    if (!FILL) cnt[fidx] = n;
+  }
+}
+
+// Exclusive scan of both count arrays (one CTA, 1024 threads).
+__global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y, int max_faces) {
+  __shared__ int part[1024];
+  int nface = bbox[2] * bbox[3];
+  if (nface + 1 > max_faces) return;
+  for (int c = 0; c < 2; ++c) {
+    int* cnt = c == 0 ? cnt_x : cnt_y;
+    int per = (nface + blockDim.x - 1) / blockDim.x;
+    int s0 = threadIdx.x * per, s1 = min(s0 + per, nface);
+    int sum = 0;
+    for (int i = s0; i < s1; ++i) sum += cnt[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int run = 0;
+      for (int q = 0; q < (int)blockDim.x; ++q) { int v = part[q]; part[q] = run; run += v; }
+      cnt[nface] = run;
+    }
+    __syncthreads();
+    int run = part[threadIdx.x];
+    for (int i = s0; i < s1; ++i) { int v = cnt[i]; cnt[i] = run; run += v; }
+    __syncthreads();
+  }
+}
+
+int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
+                     double offy, RegDev& r, int* d_err, cudaStream_t st) {
+  if (nf == 0) return IB_OK;
+  k_reg_weights<<<cdiv(nf, 128), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w, d_err);
+  k_reg_bbox<<<1, 256, 0, st>>>(nf, r.ix, r.iy, r.bbox);
+  k_reg_lists<false><<<152 * 2, 128, 0, st>>>(nf, r.comp, r.ix, r.iy, r.bbox, r.cnt_x, r.cnt_y, nullptr,
+                                              nullptr, r.max_faces);
+  k_reg_scan<<<1, 1024, 0, st>>>(r.bbox, r.cnt_x, r.cnt_y, r.max_faces);
+  k_reg_lists<true><<<152 * 2, 128, 0, st>>>(nf, r.comp, r.ix, r.iy, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y,
+                                             r.max_faces);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+// E^T h0: every face of the box gets the ordered sum of weight*h0 over its list.
+__global__ void k_reg(GridDims g, const double* __restrict__ h0, const double* __restrict__ w,
+                      const int* __restrict__ bbox, const int* __restrict__ cnt_x, const int* __restrict__ cnt_y,
+                      const int* __restrict__ lst_x, const int* __restrict__ lst_y, double* hx, double* hy,
+                      int max_faces) {
+  int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
+  int nface = ni * nj;
+  if (nface + 1 > max_faces) return;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * nface; t += gridDim.x * blockDim.x) {
+    bool cx = t < nface;
+    int fidx = cx ? t : t - nface;
+    int fi = i0 + fidx % ni, fj = j0 + fidx / ni;
+    const int* cnt = cx ? cnt_x : cnt_y;
+    const int* lst = cx ? lst_x : lst_y;
+    int a = cnt[fidx], b = cnt[fidx + 1];
+    if (a == b) continue;
+    double acc = 0.0;
+    for (int q = a; q < b; ++q) {
+      int e = lst[q];
+      acc = acc + w[e] * h0[e / 49];
+    }
+    if (cx) hx[(fj - 1) * g.nux + (fi - 1)] = acc;
+    else hy[(fj - 1) * g.nvx + (fi - 1)] = acc;
+  }
+}
+
+int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, double* hx, double* hy,
+               cudaStream_t st) {
+  IB_CUDA_CHECK(cudaMemsetAsync(hx, 0, sizeof(double) * g.nu, st));
+  IB_CUDA_CHECK(cudaMemsetAsync(hy, 0, sizeof(double) * g.nv, st));
+  if (nf == 0) return IB_OK;
+  k_reg<<<152 * 2, 128, 0, st>>>(g, h0, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, hx, hy, r.max_faces);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+// E q: h0_out[k] = h0_in[k] + sum_slots w * q(face)  (sequential in slot order)
+__global__ void k_regT(GridDims g, int nf, const double* __restrict__ qx, const double* __restrict__ qx0,
+                       const double* __restrict__ qy, const double* __restrict__ qy0, const int* __restrict__ comp,
+                       const int* __restrict__ ix, const int* __restrict__ iy, const double* __restrict__ w,
+                       const double* __restrict__ h0_in, double* h0_out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nf) return;
+  bool isx = comp[k] == 1;
+  const double* q = isx ? qx : qy;
+  const double* q0 = isx ? qx0 : qy0;
+  int ld = isx ? g.nux : g.nvx;
+  int cx = ix[k], cy = iy[k];
+  const double* wk = w + (size_t)k * 49;
+  double vals[49];
+#pragma unroll
+  for (int l = 0; l < 7; ++l)
+#pragma unroll
+    for (int p = 0; p < 7; ++p) {
+      int idx = (cy + l - 3 - 1) * ld + (cx + p - 3 - 1);
+      vals[l * 7 + p] = q0 ? q[idx] + q0[idx] : q[idx];
+    }
+  double acc = h0_in ? h0_in[k] : 0.0;
+#pragma unroll
+  for (int s = 0; s < 49; ++s) acc = acc + wk[s] * vals[s];
+  h0_out[k] = acc;
+}
+
+int launch_regT(const GridDims& g, int nf, const double* qx, const double* qx0, const double* qy, const double* qy0,
+                const RegDev& r, const double* h0_in, double* h0_out, cudaStream_t st) {
+  if (nf == 0) return IB_OK;
+  k_regT<<<cdiv(nf, 64), 64, 0, st>>>(g, nf, qx, qx0, qy, qy0, r.comp, r.ix, r.iy, r.w, h0_in, h0_out);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+// finter = (1/E^T 1) * E^T f where E^T 1 > 1e-10, else 0 (redistribute2)
+__global__ void k_redist_field(GridDims g, const double* __restrict__ f, const double* __restrict__ w,
+                               const int* __restrict__ bbox, const int* __restrict__ cnt_x,
+                               const int* __restrict__ cnt_y, const int* __restrict__ lst_x,
+                               const int* __restrict__ lst_y, double* fx, double* fy, int max_faces) {
+  int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
+  int nface = ni * nj;
+  if (nface + 1 > max_faces) return;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * nface; t += gridDim.x * blockDim.x) {
+    bool cx = t < nface;
+    int fidx = cx ? t : t - nface;
+    int fi = i0 + fidx % ni, fj = j0 + fidx / ni;
+    const int* cnt = cx ? cnt_x : cnt_y;
+    const int* lst = cx ? lst_x : lst_y;
+    int a = cnt[fidx], b = cnt[fidx + 1];
+    if (a == b) continue;
+    double ws = 0.0, fs = 0.0;
+    for (int q = a; q < b; ++q) {
+      int e = lst[q];
+      ws = ws + w[e] * 1.0;
+      fs = fs + w[e] * f[e / 49];
+    }
+    double v = ws > 1.0e-10 ? 1.0 / ws * fs : 0.0;
+    if (cx) fx[(fj - 1) * g.nux + (fi - 1)] = v;
+    else fy[(fj - 1) * g.nvx + (fi - 1)] = v;
+  }
+}
+
+int launch_redistribute_field(const GridDims& g, int nf, const double* f, const RegDev& r, double* fx,
+                              double* fy, cudaStream_t st) {
+  IB_CUDA_CHECK(cudaMemsetAsync(fx, 0, sizeof(double) * g.nu, st));
+  IB_CUDA_CHECK(cudaMemsetAsync(fy, 0, sizeof(double) * g.nv, st));
+  if (nf == 0) return IB_OK;
+  k_redist_field<<<152 * 2, 128, 0, st>>>(g, f, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, fx, fy,
+                                          r.max_faces);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+// write_force2: out[b] = 2 delta sum_x f/dt, out[nbody+b] = 2 delta sum_y f/dt
+__global__ void k_force_coeffs(int nf, int nbody, const int* __restrict__ comp, const int* __restrict__ bid,
+                               const double* __restrict__ f, double dt, double delta, double* out) {
+  // one thread per body, sequential in unknown order
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbody) return;
+  double fx = 0.0, fy = 0.0;
+  for (int k = 0; k < nf; ++k) {
+    if (bid[k] != b) continue;
+    if (comp[k] == 1) fx = fx + f[k] / dt;
+    else fy = fy + f[k] / dt;
+  }
+  out[b] = 2.0 * delta * fx;
+  out[nbody + b] = 2.0 * delta * fy;
+}
+
+int launch_force_coeffs(int nf, int nbody, const int* comp, const int* bid, const double* f, double dt,
+                        double delta, double* out, cudaStream_t st) {
+  if (nbody == 0) return IB_OK;
+  k_force_coeffs<<<cdiv(nbody, 32), 32, 0, st>>>(nf, nbody, comp, bid, f, dt, delta, out);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+}  // namespace ib

@@ -1,0 +1,94 @@
+// Launchers of the grid, interface and structure kernels.
+#pragma once
+#include "ib_common.cuh"
+
+namespace ib {
+
+// stencil.cu -- operators_fluid.F90
+int launch_nonlinear(const GridDims& g, const double* om, const double* bc, const double* qx, const double* q0x,
+                     const double* qy, const double* q0y, double* nlx, double* nly, cudaStream_t st);
+int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vort, cudaStream_t st);
+int launch_curl(const GridDims& g, const double* s, const double* sbc, double* qx, double* qy, cudaStream_t st);
+int launch_coarsify(const GridDims& g, const double* fine, double* coarse, cudaStream_t st);
+int launch_get_bc(const GridDims& g, const double* s, double fac, double* ring, cudaStream_t st);
+int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st);
+int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st);
+int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st);
+int launch_sub(int n, const double* x, const double* y, double* z, cudaStream_t st);
+int launch_fill(int n, double v, double* z, cudaStream_t st);
+
+// ibm.cu -- fsinterface.F90, grid.F90:459-528, operators_struct.F90:711-834
+struct RegDev {
+  // per unknown k (nf): component (1 = x, 2 = y), stencil origin, 49 weights
+  const int* comp;
+  int* ix;
+  int* iy;
+  double* w;        // nf*49, slot = (l+3)*7 + (p+3)
+  // face-major contribution lists over the stencil bounding box, per component
+  int* bbox;        // [0..3] = i0, j0, ni, nj (same box for u- and v-faces)
+  int* cnt_x;       // bbox faces + 1 (exclusive offsets after the scan)
+  int* cnt_y;
+  int* lst_x;       // contributions: k*49 + slot, ascending k per face
+  int* lst_y;
+  int max_faces;    // capacity of cnt_* (faces)
+  int max_list;     // capacity of lst_*
+};
+
+int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
+                     double offy, RegDev& r, int* d_err, cudaStream_t st);
+// hx, hy must be zero outside the stencil box; this writes every face in the box.
+int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, double* hx, double* hy,
+               cudaStream_t st);
+// h0 (+)= E q   (accumulate=1 keeps the incoming h0, fsinterface.F90:51-80)
+int launch_regT(const GridDims& g, int nf, const double* qx, const double* qx0, const double* qy,
+                const double* qy0, const RegDev& r, const double* h0_in, double* h0_out, cudaStream_t st);
+// finter = E^T f / E^T 1 on faces with weight > 1e-10 (operators_struct.F90:810-834)
+int launch_redistribute_field(const GridDims& g, int nf, const double* f, const RegDev& r, double* fx,
+                              double* fy, cudaStream_t st);
+int launch_force_coeffs(int nf, int nbody, const int* comp, const int* bid, const double* f, double dt,
+                        double delta, double* out, cudaStream_t st);
+
+// structure.cu -- operators_struct.F90 (family 2, torsional bodies)
+struct TorsBody {
+  int off, npts;
+  double gamma0, itheta, ktheta, ctheta, deltas, xbf0, ybf0;
+};
+struct TorsState {  // device arrays of length nt
+  double *theta, *thetad, *thetadd, *theta0, *thetad0, *thetadd0;
+};
+int launch_tors_btimes(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, const double* x,
+                       double* y, cudaStream_t st);
+int launch_tors_rhs(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, double* y,
+                    cudaStream_t st);
+int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, const double* f,
+                   double* xb, double* yb, double* err, cudaStream_t st);
+int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta,
+                            const double* f, cudaStream_t st);
+int launch_tors_save(int nt, const TorsState& s, cudaStream_t st);
+
+// gmres.cu -- PETSc KSPGMRES as configured in variables.F90:565-574
+struct GmresDev {
+  int nf, restart;
+  double* V;       // (restart+1) * nf
+  double* H;       // (restart+1) * restart, column it at H + it*(restart+1)
+  double* cs;
+  double* sn;
+  double* g;       // restart+1
+  double* scal;    // [0]=ttol [1]=res [2]=bnorm [3]=rnorm
+  int* ist;        // [0]=its [1]=reason [2]=it (inner) [3]=active
+  double* xin;     // matvec input
+  double* Av;      // matvec output
+};
+int launch_gmres_init(const GmresDev& G, cudaStream_t st);
+int launch_gmres_start(const GmresDev& G, const double* b, const double* x, double rtol, double atol, int max_it,
+                       cudaStream_t st);
+int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st);
+int launch_gmres_update(const GmresDev& G, double* x, cudaStream_t st);
+
+// dense symmetric positive definite solve (stationary-body path)
+int launch_cholesky(int n, double* A, int* d_err, cudaStream_t st);
+int launch_chol_solve(int n, const double* Lf, const double* b, double* x, cudaStream_t st);
+int launch_copy_col(int n, const double* src, double* M, int col, cudaStream_t st);
+int launch_unit(int n, int i, double* e, cudaStream_t st);
+
+}  // namespace ib

@@ -1,0 +1,211 @@
+// Per-level grid stencils of operators_fluid.F90 (one rank, natural ordering).
+#include "kernels.cuh"
+
+namespace ib {
+
+// ------------------------------------------------------------ nonlinear
+// operators_fluid.F90:553-587.  omega ghosts come from the ring (bc); fluxes
+// outside the physical face grids are zero.  qx, qy are the total fluxes q+q0,
+// passed as q and q0 and summed on the fly.
+__global__ void k_nonlinear(GridDims g, const double* __restrict__ om, const double* __restrict__ bc,
+                            const double* __restrict__ qx, const double* __restrict__ q0x,
+                            const double* __restrict__ qy, const double* __restrict__ q0y,
+                            double* __restrict__ nlx, double* __restrict__ nly) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  auto QX = [&](int i, int j) -> double {  // i=1..m+1, j=0..n+1
+    if (j < 1 || j > g.n) return 0.0;
+    int idx = (j - 1) * g.nux + (i - 1);
+    return qx[idx] + (q0x ? q0x[idx] : 0.0);
+  };
+  auto QY = [&](int i, int j) -> double {  // i=0..m+1, j=1..n+1
+    if (i < 1 || i > g.m) return 0.0;
+    int idx = (j - 1) * g.nvx + (i - 1);
+    return qy[idx] + (q0y ? q0y[idx] : 0.0);
+  };
+  if (t < g.nu) {
+    int i = t % g.nux + 1, j = t / g.nux + 1;  // u-face (i,j), i=1..m+1, j=1..n
+    double v1 = 0.5 * (QY(i, j + 1) + QY(i - 1, j + 1));
+    double v0 = 0.5 * (QY(i, j) + QY(i - 1, j));
+    double w1 = ghost_vertex(om, bc, g, i, j + 1);
+    double w0 = ghost_vertex(om, bc, g, i, j);
+    nlx[t] = 0.5 * (v1 * w1 + v0 * w0);
+  } else if (t < g.nu + g.nv) {
+    int s = t - g.nu;
+    int i = s % g.nvx + 1, j = s / g.nvx + 1;  // v-face (i,j), i=1..m, j=1..n+1
+    double u1 = 0.5 * (QX(i + 1, j) + QX(i + 1, j - 1));
+    double u0 = 0.5 * (QX(i, j) + QX(i, j - 1));
+    double w1 = ghost_vertex(om, bc, g, i + 1, j);
+    double w0 = ghost_vertex(om, bc, g, i, j);
+    nly[s] = -0.5 * (u1 * w1 + u0 * w0);
+  }
+}
+
+// ------------------------------------------------------------------ rot
+// rot_int + rot_bc (operators_fluid.F90:203-233): the transpose of curl.
+__global__ void k_rot(GridDims g, const double* __restrict__ hx, const double* __restrict__ hy,
+                      double* __restrict__ vort) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.ns) return;
+  int I = t % g.nsx + 2, J = t / g.nsx + 2;
+  double a = hy[(J - 1) * g.nvx + (I - 1)];
+  double b = hy[(J - 1) * g.nvx + (I - 2)];
+  double c = hx[(J - 1) * g.nux + (I - 1)];
+  double d = hx[(J - 2) * g.nux + (I - 1)];
+  vort[t] = a - b - c + d;
+}
+
+// ----------------------------------------------------------------- curl
+// curl_int + curl_bc (operators_fluid.F90:423-471), s ghosts from the ring.
+__global__ void k_curl(GridDims g, const double* __restrict__ s, const double* __restrict__ sbc,
+                       double* __restrict__ qx, double* __restrict__ qy) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < g.nu) {
+    int i = t % g.nux + 1, j = t / g.nux + 1;
+    qx[t] = ghost_vertex(s, sbc, g, i, j + 1) - ghost_vertex(s, sbc, g, i, j);
+  } else if (t < g.nu + g.nv) {
+    int u = t - g.nu;
+    int i = u % g.nvx + 1, j = u / g.nvx + 1;
+    qy[u] = ghost_vertex(s, sbc, g, i, j) - ghost_vertex(s, sbc, g, i + 1, j);
+  }
+}
+
+// ------------------------------------------------------------- coarsify
+// operators_fluid.F90:381-419 with grid.F90:1061-1087: the full-weighting sum
+// at odd fine points I=3..m-1, J=3..n-1 overwrites coarse point
+// ((I-1)/2+m/4+1, (J-1)/2+n/4+1).
+__global__ void k_coarsify(GridDims g, const double* __restrict__ fine, double* __restrict__ coarse) {
+  int cx = g.m / 2 - 1, cy = g.n / 2 - 1;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cx * cy) return;
+  int a = t % cx, b = t / cx;
+  int I = 2 * a + 3, J = 2 * b + 3;
+  auto F = [&](int ii, int jj) { return fine[(jj - 2) * g.nsx + (ii - 2)]; };
+  double v = F(I, J) + 0.5 * (F(I + 1, J) + F(I, J + 1) + F(I - 1, J) + F(I, J - 1)) +
+             0.25 * (F(I + 1, J + 1) + F(I + 1, J - 1) + F(I - 1, J - 1) + F(I - 1, J + 1));
+  int Ic = (I - 1) / 2 + g.m / 4 + 1, Jc = (J - 1) / 2 + g.n / 4 + 1;
+  coarse[(Jc - 2) * g.nsx + (Ic - 2)] = v;
+}
+
+// --------------------------------------------------------------- get_bc
+// operators_fluid.F90:475-535 with grid.F90:1091-1140: coarse values on the
+// fine boundary; coincident points copied, midpoints averaged; times fac.
+__global__ void k_get_bc(GridDims g, const double* __restrict__ s, double fac, double* __restrict__ ring) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nbc) return;
+  auto S = [&](int I, int J) { return s[(J - 2) * g.nsx + (I - 2)]; };
+  double v;
+  if (t >= g.bottom) {  // bottom / top edges: p = 0..m
+    bool top = t >= g.top;
+    int p = t - (top ? g.top : g.bottom);
+    int J = top ? 3 * g.n / 4 + 1 : g.n / 4 + 1;
+    int I = g.m / 4 + 1 + p / 2;
+    v = (p & 1) ? 0.5 * (S(I, J) + S(I + 1, J)) : S(I, J);
+  } else {              // left / right edges: p = 0..n
+    bool right = t >= g.right;
+    int p = t - (right ? g.right : g.left);
+    int I = right ? 3 * g.m / 4 + 1 : g.m / 4 + 1;
+    int J = g.n / 4 + 1 + p / 2;
+    v = (p & 1) ? 0.5 * (S(I, J) + S(I, J + 1)) : S(I, J);
+  }
+  ring[t] = v * fac;
+}
+
+// ------------------------------------------------------------- apply_bc
+// operators_fluid.F90:539-549 in place: left, right, bottom, top.
+__global__ void k_apply_bc(GridDims g, double* __restrict__ v, const double* __restrict__ ring, double fac) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.ns) return;
+  int I = t % g.nsx + 2, J = t / g.nsx + 2;
+  if (I != 2 && I != g.m && J != 2 && J != g.n) return;
+  double x = v[t];
+  if (I == 2) x = x + fac * ring[g.left + J - 1];
+  if (I == g.m) x = x + fac * ring[g.right + J - 1];
+  if (J == 2) x = x + fac * ring[g.bottom + I - 1];
+  if (J == g.n) x = x + fac * ring[g.top + I - 1];
+  v[t] = x;
+}
+
+// rhsbc = 0; apply_bc(rhsbc, a, f); apply_bc(rhsbc, b, f)   (timestepper.F90:184-189)
+__global__ void k_rhsbc(GridDims g, double* __restrict__ v, const double* __restrict__ ra,
+                        const double* __restrict__ rb, double fac) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.ns) return;
+  int I = t % g.nsx + 2, J = t / g.nsx + 2;
+  double x = 0.0;
+  if (I == 2 || I == g.m || J == 2 || J == g.n) {
+    const double* rr[2] = {ra, rb};
+    for (int q = 0; q < 2; ++q) {
+      const double* r = rr[q];
+      if (!r) continue;
+      if (I == 2) x = x + fac * r[g.left + J - 1];
+      if (I == g.m) x = x + fac * r[g.right + J - 1];
+      if (J == 2) x = x + fac * r[g.bottom + I - 1];
+      if (J == g.n) x = x + fac * r[g.top + I - 1];
+    }
+  }
+  v[t] = x;
+}
+
+// -------------------------------------------------------- vector helpers
+__global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                        double* __restrict__ z) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) z[t] = a * x[t] + b * y[t];
+}
+__global__ void k_sub(int n, const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ z) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) z[t] = x[t] - y[t];
+}
+__global__ void k_fill(int n, double v, double* __restrict__ z) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) z[t] = v;
+}
+
+// ------------------------------------------------------------ launchers
+static inline int blocks(long long n, int nt = 256) { return (int)((n + nt - 1) / nt); }
+
+int launch_nonlinear(const GridDims& g, const double* om, const double* bc, const double* qx, const double* q0x,
+                     const double* qy, const double* q0y, double* nlx, double* nly, cudaStream_t st) {
+  k_nonlinear<<<blocks(g.nu + g.nv), 256, 0, st>>>(g, om, bc, qx, q0x, qy, q0y, nlx, nly);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vort, cudaStream_t st) {
+  k_rot<<<blocks(g.ns), 256, 0, st>>>(g, hx, hy, vort);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_curl(const GridDims& g, const double* s, const double* sbc, double* qx, double* qy, cudaStream_t st) {
+  k_curl<<<blocks(g.nu + g.nv), 256, 0, st>>>(g, s, sbc, qx, qy);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_coarsify(const GridDims& g, const double* fine, double* coarse, cudaStream_t st) {
+  int n = (g.m / 2 - 1) * (g.n / 2 - 1);
+  k_coarsify<<<blocks(n), 256, 0, st>>>(g, fine, coarse);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_get_bc(const GridDims& g, const double* s, double fac, double* ring, cudaStream_t st) {
+  k_get_bc<<<blocks(g.nbc), 256, 0, st>>>(g, s, fac, ring);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st) {
+  k_apply_bc<<<blocks(g.ns), 256, 0, st>>>(g, v, ring, fac);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st) {
+  k_rhsbc<<<blocks(g.ns), 256, 0, st>>>(g, v, ra, rb, fac);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st) {
+  k_axpby<<<blocks(n), 256, 0, st>>>(n, a, x, b, y, z);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_sub(int n, const double* x, const double* y, double* z, cudaStream_t st) {
+  k_sub<<<blocks(n), 256, 0, st>>>(n, x, y, z);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_fill(int n, double v, double* z, cudaStream_t st) {
+  if (n <= 0) return IB_OK;
+  k_fill<<<blocks(n), 256, 0, st>>>(n, v, z);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+
+}  // namespace ib

@@ -1,0 +1,171 @@
+// Torsional-body (family 2) structure operators of operators_struct.F90: a rigid
+// plate hinged at its first point on a torsional spring/damper, integrated with
+// the trapezoidal Newmark scheme.  Each body is handled by one CTA; the only
+// reduction is the BR . x dot product.  Gravity and pseudo-forces are zero in the
+// reference user hooks (user.F90:178-206) and are omitted.
+#include "kernels.cuh"
+
+namespace ib {
+
+// BR_build (operators_struct.F90:319-338): x-rows (j-1) ds sin(g0-th),
+// y-rows -(j-1) ds cos(g0-th).
+__device__ __forceinline__ double br_val(const TorsBody& b, double th, int j) {
+  if (j < b.npts) return (double)j * b.deltas * sin(b.gamma0 - th);
+  return -(double)(j - b.npts) * b.deltas * cos(b.gamma0 - th);
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+    red[0] = s;
+  }
+  __syncthreads();
+  s = red[0];
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ double keff(const TorsBody& b, double dt) {
+  return 4.0 / (dt * dt) * b.itheta + 2.0 / dt * b.ctheta + b.ktheta;
+}
+
+// b_times2 (operators_struct.F90:14-127): y += BR (BR . x)/K_eff * (delta^2/ds/dt)(2 ds/dt)
+__global__ void k_tors_btimes(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
+                              const double* __restrict__ x, double* __restrict__ y) {
+  TorsBody b = tb[blockIdx.x];
+  double th = s.theta[blockIdx.x];
+  double part = 0.0;
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, th, j) * x[b.off + j];
+  double dot = block_sum(part);
+  double scale = (delta * delta / b.deltas / dt) * (2.0 * b.deltas / dt);
+  double c = dot / keff(b, dt) * scale;
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = y[b.off + j] + br_val(b, th, j) * c;
+}
+
+// compute_rhs (operators_struct.F90:342-398): y = BR * delta*(r_theta - J r_phi - thetad)
+__global__ void k_tors_rhs(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
+                           double* __restrict__ y) {
+  int t = blockIdx.x;
+  TorsBody b = tb[t];
+  double th = s.theta[t], th0 = s.theta0[t], thd = s.thetad[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
+  double I = b.itheta, C = b.ctheta, K = b.ktheta;
+  double rth = thd0 + thd + 2.0 / dt * (th0 - th);
+  double jr = 2.0 / dt / (4.0 / (dt * dt) * I + 2.0 / dt * C + K) *
+              (I * (4.0 / (dt * dt) * th0 + 4.0 / dt * thd0 + thdd0) + C * (thd0 + 2.0 / dt * th0) -
+               (4.0 / (dt * dt) * I + 2.0 / dt * C + K) * th);
+  double c = delta * (rth - jr - thd);
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = br_val(b, th, j) * c;
+}
+
+// compute_dx + update_xb (operators_struct.F90:402-505, 600-620); err = max |dtheta|
+__global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
+                          const double* __restrict__ f, double* __restrict__ xb, double* __restrict__ yb,
+                          double* __restrict__ err_per_body) {
+  int t = blockIdx.x;
+  TorsBody b = tb[t];
+  double th = s.theta[t], th0 = s.theta0[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
+  double I = b.itheta, C = b.ctheta, K = b.ktheta;
+  double part = 0.0;
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, th, j) * f[b.off + j];
+  double brf = block_sum(part);
+  double jr = 1.0 / (4.0 / (dt * dt) * I + 2.0 / dt * C + K) *
+              (I * (4.0 / (dt * dt) * th0 + 4.0 / dt * thd0 + thdd0) + C * (thd0 + 2.0 / dt * th0) -
+               (4.0 / (dt * dt) * I + 2.0 / dt * C + K) * th);
+  brf = b.deltas / (4.0 / (dt * dt) * I + K) * brf * (delta / b.deltas / dt);
+  double dth = jr + brf;
+  double thn = th + dth;
+  if (threadIdx.x == 0) {
+    s.theta[t] = thn;
+    s.thetad[t] = -thd0 + 2.0 / dt * (thn - th0);
+    s.thetadd[t] = -thdd0 - 4.0 / dt * thd0 + 4.0 / (dt * dt) * (thn - th0);
+    err_per_body[t] = fabs(dth);
+  }
+  double g = b.gamma0 - thn;
+  double cg = cos(g), sg = sin(g);
+  for (int j = threadIdx.x; j < b.npts; j += blockDim.x) {
+    double px = b.xbf0 + (double)j * b.deltas * cg;
+    double py = b.ybf0 + (double)j * b.deltas * sg;
+    xb[b.off + j] = px; xb[b.off + b.npts + j] = px;
+    yb[b.off + j] = py; yb[b.off + b.npts + j] = py;
+  }
+}
+
+__global__ void k_max_reduce(int n, const double* __restrict__ v, double* out) {
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, v[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (threadIdx.x == 0) out[0] = m;
+}
+
+// initial_acc (operators_struct.F90:233-294)
+__global__ void k_tors_initial_acc(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
+                                   const double* __restrict__ f) {
+  int t = blockIdx.x;
+  TorsBody b = tb[t];
+  double th = s.theta[t];
+  double part = 0.0;
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, th, j) * f[b.off + j];
+  double brf = block_sum(part);
+  brf = brf * delta / b.deltas / dt;
+  if (threadIdx.x == 0) {
+    double ftint = b.ktheta * th;
+    s.thetadd[t] = 1.0 / b.itheta * (-b.ctheta * s.thetad[t] - ftint + brf * b.deltas);
+  }
+}
+
+__global__ void k_tors_save(int nt, TorsState s) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  s.theta0[t] = s.theta[t];
+  s.thetad0[t] = s.thetad[t];
+  s.thetadd0[t] = s.thetadd[t];
+}
+
+int launch_tors_btimes(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, const double* x,
+                       double* y, cudaStream_t st) {
+  if (nt == 0) return IB_OK;
+  k_tors_btimes<<<nt, 256, 0, st>>>(tb, s, dt, delta, x, y);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+int launch_tors_rhs(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, double* y,
+                    cudaStream_t st) {
+  if (nt == 0) return IB_OK;
+  k_tors_rhs<<<nt, 256, 0, st>>>(tb, s, dt, delta, y);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, const double* f,
+                   double* xb, double* yb, double* err, cudaStream_t st) {
+  if (nt == 0) {
+    IB_CUDA_CHECK(cudaMemsetAsync(err, 0, sizeof(double), st));
+    return IB_OK;
+  }
+  // err[1..nt] holds per-body |dtheta|, err[0] their maximum
+  k_tors_dx<<<nt, 256, 0, st>>>(tb, s, dt, delta, f, xb, yb, err + 1);
+  k_max_reduce<<<1, 32, 0, st>>>(nt, err + 1, err);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta,
+                            const double* f, cudaStream_t st) {
+  if (nt == 0) return IB_OK;
+  k_tors_initial_acc<<<nt, 256, 0, st>>>(tb, s, dt, delta, f);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+int launch_tors_save(int nt, const TorsState& s, cudaStream_t st) {
+  if (nt == 0) return IB_OK;
+  k_tors_save<<<cdiv(nt, 64), 64, 0, st>>>(nt, s);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+}  // namespace ib

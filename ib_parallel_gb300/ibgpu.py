@@ -1,0 +1,368 @@
+"""ctypes binding of ``libibgpu.so`` (the C ABI in ``include/ib_gpu.h``).
+
+This is the host-side mirror of the reference's Fortran module interface for
+the time step: ``Simulation.advance`` is ``timestepper::advance``
+(``src/timestepper.F90:18-556``) and the operator functions mirror
+``operators_fluid``, ``myfft``, ``fsinterface`` and ``operators_struct``.  Array
+arguments are numpy float64 arrays (host memory, staged by the library) or
+objects exposing ``data_ptr()`` (CUDA device memory, used in place).
+
+There is no CPU fallback: if the library cannot be loaded, or no GPU is
+present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_lib" / "libibgpu.so"
+
+IB_OK = 0
+ERRORS = {1: "IB_ERR_ARG", 2: "IB_ERR_CUDA", 3: "IB_ERR_NOMEM", 4: "IB_ERR_GMRES", 5: "IB_ERR_FSI",
+          6: "IB_ERR_NONFINITE", 7: "IB_ERR_DOMAIN", 8: "IB_ERR_STATE"}
+FIELDS = {"omega": 0, "s": 1, "qx": 2, "qy": 3, "rhs_old": 4, "q0x": 5, "q0y": 6}
+VECTORS = {"f": 0, "f_rdst": 1, "xb": 2, "yb": 3}
+
+# Every symbol include/ib_gpu.h declares (checked by the CPU tests).
+EXPORTS = [
+    "ib_last_error", "ib_version", "ib_create", "ib_destroy", "ib_synchronize", "ib_advance",
+    "ib_get_field", "ib_set_field", "ib_get_vector", "ib_set_vector", "ib_get_forces",
+    "ib_get_body_state", "ib_get_counters", "ib_get_dims", "ib_nonlinear", "ib_rot", "ib_curl",
+    "ib_coarsify", "ib_get_bc", "ib_apply_bc", "ib_dst", "ib_ctci", "ib_ainv", "ib_fluid_predictor",
+    "ib_vort2flux", "ib_reg_prep", "ib_reg", "ib_regT", "ib_redistribute", "ib_schur_apply",
+    "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
+]
+
+
+class IbError(RuntimeError):
+    pass
+
+
+class IbParams(C.Structure):
+    _fields_ = [("m", C.c_int), ("n", C.c_int), ("mgridlev", C.c_int),
+                ("dt", C.c_double), ("Re", C.c_double), ("len", C.c_double),
+                ("offsetx", C.c_double), ("offsety", C.c_double),
+                ("fsi_tol", C.c_double), ("atol", C.c_double), ("rtol", C.c_double),
+                ("num_stat", C.c_int), ("motion", C.c_double * 5),
+                ("gmres_restart", C.c_int), ("gmres_max_it", C.c_int), ("fsi_max_it", C.c_int),
+                ("autotune", C.c_int)]
+
+
+class IbBody(C.Structure):
+    _fields_ = [("npts", C.c_int), ("fam", C.c_int), ("gamma0_deg", C.c_double),
+                ("alpha0_deg", C.c_double), ("itheta", C.c_double), ("ktheta", C.c_double),
+                ("ctheta", C.c_double), ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double))]
+
+
+_lib = None
+
+
+def load(path: Optional[os.PathLike] = None):
+    """Load the library (building it first if it is missing)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        from . import build as _b
+        _b.build()
+    lib = C.CDLL(str(p))
+    P = C.c_void_p
+    D = C.POINTER(C.c_double)
+    I = C.POINTER(C.c_int)
+    sig = {
+        "ib_last_error": ([], C.c_char_p), "ib_version": ([], C.c_int),
+        "ib_create": ([C.POINTER(IbParams), C.POINTER(IbBody), C.c_int, C.POINTER(P)], C.c_int),
+        "ib_destroy": ([P], C.c_int), "ib_synchronize": ([P], C.c_int), "ib_advance": ([P, I], C.c_int),
+        "ib_get_field": ([P, C.c_int, C.c_int, P], C.c_int), "ib_set_field": ([P, C.c_int, C.c_int, P], C.c_int),
+        "ib_get_vector": ([P, C.c_int, P], C.c_int), "ib_set_vector": ([P, C.c_int, P], C.c_int),
+        "ib_get_forces": ([P, P, P], C.c_int), "ib_get_body_state": ([P, P, P, P], C.c_int),
+        "ib_get_counters": ([P, I, I], C.c_int), "ib_get_dims": ([P, I, I, I, I, I], C.c_int),
+        "ib_nonlinear": ([P, P, P, P, P, P, P], C.c_int), "ib_rot": ([P, P, P, P], C.c_int),
+        "ib_curl": ([P, P, P, P, P], C.c_int), "ib_coarsify": ([P, P, P], C.c_int),
+        "ib_get_bc": ([P, P, C.c_double, P], C.c_int), "ib_apply_bc": ([P, P, P, C.c_double], C.c_int),
+        "ib_dst": ([P, P, P], C.c_int), "ib_ctci": ([P, P, P], C.c_int), "ib_ainv": ([P, P], C.c_int),
+        "ib_fluid_predictor": ([P, C.c_int, P, P, P, P], C.c_int),
+        "ib_vort2flux": ([P, P, P, P, P], C.c_int), "ib_reg_prep": ([P, P, P], C.c_int),
+        "ib_reg": ([P, P, P, P], C.c_int), "ib_regT": ([P, P, P, P], C.c_int),
+        "ib_redistribute": ([P, P, P], C.c_int), "ib_schur_apply": ([P, P, P], C.c_int),
+        "ib_schur_apply_fluid": ([P, P, P], C.c_int), "ib_struct_btimes": ([P, P, P], C.c_int),
+        "ib_struct_rhs": ([P, P], C.c_int), "ib_struct_dx": ([P, P, P], C.c_int),
+        "ib_schur_solve": ([P, P, P, I], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(rc: int, what: str = ""):
+    if rc != IB_OK:
+        msg = load().ib_last_error().decode(errors="replace")
+        raise IbError(f"{what}: {ERRORS.get(rc, rc)}: {msg}")
+
+
+def _ptr(a):
+    """Pointer of a float64 numpy array (host) or a CUDA tensor (device)."""
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]):
+        raise TypeError("arrays must be C-contiguous float64 numpy arrays or CUDA tensors")
+    return C.c_void_p(a.ctypes.data)
+
+
+@dataclass
+class Body:
+    """One ``input/body.NNN.inp`` (grid.F90:252-288): fam 1 rigid, 2 torsional."""
+    x: np.ndarray
+    y: np.ndarray
+    fam: int = 1
+    gamma0_deg: float = 0.0
+    alpha0_deg: float = 0.0
+    itheta: float = 0.0
+    ktheta: float = 0.0
+    ctheta: float = 0.0
+
+    @property
+    def npts(self):
+        return len(self.x)
+
+
+@dataclass
+class Params:
+    """Namelist ``read_parameters`` (parameters.F90:55-59)."""
+    m: int
+    n: int
+    mgridlev: int
+    dt: float
+    Re: float
+    len: float
+    offsetx: float
+    offsety: float
+    fsi_tol: float = 1e-10
+    atol: float = 1e-10
+    rtol: float = 1e-10
+    num_stat: bool = False
+    motion: tuple = (-1.0, 0.0, 0.0, 0.0, 0.0)
+    gmres_restart: int = 30
+    gmres_max_it: int = 10000
+    fsi_max_it: int = 1000
+    autotune: bool = True
+
+    def to_c(self) -> IbParams:
+        p = IbParams()
+        for k in ("m", "n", "mgridlev", "gmres_restart", "gmres_max_it", "fsi_max_it"):
+            setattr(p, k, int(getattr(self, k)))
+        for k in ("dt", "Re", "len", "offsetx", "offsety", "fsi_tol", "atol", "rtol"):
+            setattr(p, k, float(getattr(self, k)))
+        p.num_stat = int(bool(self.num_stat))
+        p.autotune = int(bool(self.autotune))
+        for i in range(5):
+            p.motion[i] = float(self.motion[i])
+        return p
+
+
+class Simulation:
+    """One device-resident simulation (an ``IbCtx``)."""
+
+    def __init__(self, params: Params, bodies: Sequence[Body] = ()):
+        self.lib = load()
+        self.params = params
+        self._keep = []
+        cb = (IbBody * max(1, len(bodies)))()
+        for i, b in enumerate(bodies):
+            x = np.ascontiguousarray(b.x, dtype=np.float64)
+            y = np.ascontiguousarray(b.y, dtype=np.float64)
+            self._keep += [x, y]
+            cb[i].npts = len(x)
+            cb[i].fam = int(b.fam)
+            cb[i].gamma0_deg = float(b.gamma0_deg)
+            cb[i].alpha0_deg = float(b.alpha0_deg)
+            cb[i].itheta = float(b.itheta)
+            cb[i].ktheta = float(b.ktheta)
+            cb[i].ctheta = float(b.ctheta)
+            cb[i].x = x.ctypes.data_as(C.POINTER(C.c_double))
+            cb[i].y = y.ctypes.data_as(C.POINTER(C.c_double))
+        h = C.c_void_p()
+        cp = params.to_c()
+        _check(self.lib.ib_create(C.byref(cp), cb, len(bodies), C.byref(h)), "ib_create")
+        self.h = h
+        self.nbody = len(bodies)
+        self.ntors = sum(1 for b in bodies if b.fam == 2)
+        nf, nbc, ns, nu, nv = (C.c_int() for _ in range(5))
+        _check(self.lib.ib_get_dims(self.h, C.byref(nf), C.byref(nbc), C.byref(ns), C.byref(nu), C.byref(nv)))
+        self.nf, self.nbc, self.ns, self.nu, self.nv = nf.value, nbc.value, ns.value, nu.value, nv.value
+        m, n = params.m, params.n
+        self.shapes = {"omega": (n - 1, m - 1), "s": (n - 1, m - 1), "rhs_old": (n - 1, m - 1),
+                       "qx": (n, m + 1), "q0x": (n, m + 1), "qy": (n + 1, m), "q0y": (n + 1, m)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ib_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- stepping and state
+    def advance(self) -> int:
+        it = C.c_int()
+        _check(self.lib.ib_advance(self.h, C.byref(it)), "ib_advance")
+        return it.value
+
+    def get_field(self, name: str, level: int = 0) -> np.ndarray:
+        out = np.empty(self.shapes[name])
+        _check(self.lib.ib_get_field(self.h, FIELDS[name], level, _ptr(out)), "ib_get_field")
+        return out
+
+    def set_field(self, name: str, level: int, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64) if not hasattr(arr, "data_ptr") else arr
+        _check(self.lib.ib_set_field(self.h, FIELDS[name], level, _ptr(a)), "ib_set_field")
+
+    def get_vector(self, name: str) -> np.ndarray:
+        out = np.empty(self.nf)
+        _check(self.lib.ib_get_vector(self.h, VECTORS[name], _ptr(out)), "ib_get_vector")
+        return out
+
+    def set_vector(self, name: str, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        _check(self.lib.ib_set_vector(self.h, VECTORS[name], _ptr(a)), "ib_set_vector")
+
+    def forces(self):
+        cx = np.empty(max(1, self.nbody)); cy = np.empty(max(1, self.nbody))
+        _check(self.lib.ib_get_forces(self.h, _ptr(cx), _ptr(cy)), "ib_get_forces")
+        return cx[:self.nbody], cy[:self.nbody]
+
+    def body_state(self):
+        n = max(1, self.ntors)
+        a, b, c = np.zeros(n), np.zeros(n), np.zeros(n)
+        _check(self.lib.ib_get_body_state(self.h, _ptr(a), _ptr(b), _ptr(c)), "ib_get_body_state")
+        return a[:self.ntors], b[:self.ntors], c[:self.ntors]
+
+    def counters(self):
+        k, f = C.c_int(), C.c_int()
+        _check(self.lib.ib_get_counters(self.h, C.byref(k), C.byref(f)))
+        return k.value, f.value
+
+    def synchronize(self):
+        _check(self.lib.ib_synchronize(self.h), "ib_synchronize")
+
+    # ---- operators (mirror the Fortran routines)
+    def _o(self, shape):
+        return np.zeros(shape)
+
+    def nonlinear(self, omega, qx, qy, bc):
+        nlx = self._o(self.shapes["qx"]); nly = self._o(self.shapes["qy"])
+        _check(self.lib.ib_nonlinear(self.h, _ptr(omega), _ptr(qx), _ptr(qy), _ptr(bc), _ptr(nlx), _ptr(nly)),
+               "ib_nonlinear")
+        return nlx, nly
+
+    def rot(self, hx, hy):
+        v = self._o(self.shapes["omega"])
+        _check(self.lib.ib_rot(self.h, _ptr(hx), _ptr(hy), _ptr(v)), "ib_rot")
+        return v
+
+    def curl(self, s, sbc):
+        qx = self._o(self.shapes["qx"]); qy = self._o(self.shapes["qy"])
+        _check(self.lib.ib_curl(self.h, _ptr(s), _ptr(sbc), _ptr(qx), _ptr(qy)), "ib_curl")
+        return qx, qy
+
+    def coarsify(self, fine, coarse):
+        out = np.array(coarse, dtype=np.float64, copy=True)
+        _check(self.lib.ib_coarsify(self.h, _ptr(fine), _ptr(out)), "ib_coarsify")
+        return out
+
+    def get_bc(self, s, fac):
+        ring = np.zeros(self.nbc)
+        _check(self.lib.ib_get_bc(self.h, _ptr(s), C.c_double(fac), _ptr(ring)), "ib_get_bc")
+        return ring
+
+    def apply_bc(self, vort, ring, fac):
+        out = np.array(vort, dtype=np.float64, copy=True)
+        _check(self.lib.ib_apply_bc(self.h, _ptr(out), _ptr(ring), C.c_double(fac)), "ib_apply_bc")
+        return out
+
+    def dst(self, x):
+        out = self._o(self.shapes["omega"])
+        _check(self.lib.ib_dst(self.h, _ptr(np.ascontiguousarray(x)), _ptr(out)), "ib_dst")
+        return out
+
+    def ctci(self, x):
+        out = self._o(self.shapes["omega"])
+        _check(self.lib.ib_ctci(self.h, _ptr(np.ascontiguousarray(x)), _ptr(out)), "ib_ctci")
+        return out
+
+    def ainv(self, x):
+        out = np.array(x, dtype=np.float64, copy=True)
+        _check(self.lib.ib_ainv(self.h, _ptr(out)), "ib_ainv")
+        return out
+
+    def fluid_predictor(self, level, omega, rhs, rhs_old, rhsbc):
+        out = np.array(omega, dtype=np.float64, copy=True)
+        _check(self.lib.ib_fluid_predictor(self.h, level, _ptr(out), _ptr(rhs), _ptr(rhs_old), _ptr(rhsbc)),
+               "ib_fluid_predictor")
+        return out
+
+    def vort2flux(self, omega_levels):
+        L = self.params.mgridlev
+        w = np.ascontiguousarray(np.stack(omega_levels), dtype=np.float64).copy()
+        s = np.zeros_like(w)
+        qx = np.zeros((L,) + self.shapes["qx"]); qy = np.zeros((L,) + self.shapes["qy"])
+        _check(self.lib.ib_vort2flux(self.h, _ptr(w), _ptr(s), _ptr(qx), _ptr(qy)), "ib_vort2flux")
+        return list(w), list(s), list(qx), list(qy)
+
+    def reg_prep(self, xb, yb):
+        _check(self.lib.ib_reg_prep(self.h, _ptr(np.ascontiguousarray(xb, dtype=np.float64)),
+                                    _ptr(np.ascontiguousarray(yb, dtype=np.float64))), "ib_reg_prep")
+
+    def reg(self, h0):
+        hx = self._o(self.shapes["qx"]); hy = self._o(self.shapes["qy"])
+        _check(self.lib.ib_reg(self.h, _ptr(np.ascontiguousarray(h0, dtype=np.float64)), _ptr(hx), _ptr(hy)),
+               "ib_reg")
+        return hx, hy
+
+    def regT(self, hx, hy, h0=None):
+        out = np.zeros(self.nf) if h0 is None else np.array(h0, dtype=np.float64, copy=True)
+        _check(self.lib.ib_regT(self.h, _ptr(hx), _ptr(hy), _ptr(out)), "ib_regT")
+        return out
+
+    def redistribute(self, f):
+        out = np.zeros(self.nf)
+        _check(self.lib.ib_redistribute(self.h, _ptr(np.ascontiguousarray(f, dtype=np.float64)), _ptr(out)),
+               "ib_redistribute")
+        return out
+
+    def schur_apply(self, x, with_b=True):
+        out = np.zeros(self.nf)
+        fn = self.lib.ib_schur_apply if with_b else self.lib.ib_schur_apply_fluid
+        _check(fn(self.h, _ptr(np.ascontiguousarray(x, dtype=np.float64)), _ptr(out)), "ib_schur_apply")
+        return out
+
+    def struct_btimes(self, x):
+        out = np.zeros(self.nf)
+        _check(self.lib.ib_struct_btimes(self.h, _ptr(np.ascontiguousarray(x, dtype=np.float64)), _ptr(out)))
+        return out
+
+    def struct_rhs(self):
+        out = np.zeros(self.nf)
+        _check(self.lib.ib_struct_rhs(self.h, _ptr(out)), "ib_struct_rhs")
+        return out
+
+    def schur_solve(self, rhs, f0):
+        f = np.array(f0, dtype=np.float64, copy=True)
+        its = C.c_int()
+        _check(self.lib.ib_schur_solve(self.h, _ptr(np.ascontiguousarray(rhs, dtype=np.float64)), _ptr(f),
+                                       C.byref(its)), "ib_schur_solve")
+        return f, its.value

@@ -1,0 +1,142 @@
+/*
+ * C ABI of the GB300 immersed-boundary time step.
+ *
+ * Drop-in boundary for the Fortran modules of nirmaljp6/IB_Parallel
+ * (src/timestepper.F90, src/operators_fluid.F90, src/myfft.F90,
+ * src/fsinterface.F90, src/operators_struct.F90).  Every entry point returns an
+ * int status (IB_OK = 0); the message of the last failure on the calling thread
+ * is available from ib_last_error().
+ *
+ * Arrays cross the ABI in the reference's one-rank layout, x fastest:
+ *   vertex field (omega, s):  (n-1) x (m-1)   element (I,J) at (J-2)*(m-1)+(I-2)
+ *   u-face flux qx:           n x (m+1)       face (i,j) at (j-1)*(m+1)+(i-1)
+ *   v-face flux qy:           (n+1) x m       face (i,j) at (j-1)*m+(i-1)
+ *   boundary ring:            2(m+1)+2(n+1)   left[n+1] right[n+1] bottom[m+1] top[m+1]
+ *   body vectors (f, xb, yb): nf = 2*nb       per body: x-unknowns then y-unknowns
+ * Array pointers may be host or device memory: host arrays are staged through
+ * the context's device buffers, device arrays are used in place.  Calls are
+ * complete (the context's stream synchronised) when they return.
+ */
+#ifndef IB_GPU_H
+#define IB_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IB_OK 0
+#define IB_ERR_ARG 1
+#define IB_ERR_CUDA 2
+#define IB_ERR_NOMEM 3
+#define IB_ERR_GMRES 4
+#define IB_ERR_FSI 5
+#define IB_ERR_NONFINITE 6
+#define IB_ERR_DOMAIN 7
+#define IB_ERR_STATE 8
+
+/* Namelist read_parameters of parameters.F90:55-59 (the sub-domain and pressure
+ * keys are not part of this boundary).  motion = motion_grid of user.F90:13-31
+ * (frame u, v, angular velocity, centre x, y), constant in time. */
+typedef struct IbParams {
+  int m, n, mgridlev;
+  double dt, Re, len, offsetx, offsety;
+  double fsi_tol, atol, rtol;
+  int num_stat;
+  double motion[5];
+  int gmres_restart;  /* PETSc default 30 */
+  int gmres_max_it;   /* PETSc default 10000 */
+  int fsi_max_it;     /* timestepper.F90:318 iterates while fsi_count <= 1000 */
+  int autotune;       /* pick DST launch shapes by timing at ib_create */
+} IbParams;
+
+/* One input/body.NNN.inp (grid.F90:252-288).  fam: 1 rigid, 2 torsional.
+ * Rigid bodies must precede non-rigid ones (grid.F90:1226,1244). */
+typedef struct IbBody {
+  int npts, fam;
+  double gamma0_deg, alpha0_deg, itheta, ktheta, ctheta;
+  const double* x;
+  const double* y;
+} IbBody;
+
+typedef struct IbCtx IbCtx;
+
+enum { IB_FIELD_OMEGA = 0, IB_FIELD_S = 1, IB_FIELD_QX = 2, IB_FIELD_QY = 3, IB_FIELD_RHS_OLD = 4,
+       IB_FIELD_Q0X = 5, IB_FIELD_Q0Y = 6 };
+enum { IB_VEC_F = 0, IB_VEC_F_RDST = 1, IB_VEC_XB = 2, IB_VEC_YB = 3 };
+
+const char* ib_last_error(void);
+int ib_version(void);
+
+/* setup: grid.F90:117-234 setup, variables.F90:84-257 setup_variables,
+ * myfft.F90:96-157 setup_fft.  Initial condition variables.F90:262-295. */
+int ib_create(const IbParams* p, const IbBody* bodies, int nbody, IbCtx** out);
+int ib_destroy(IbCtx* ctx);
+int ib_synchronize(IbCtx* ctx);
+
+/* timestepper.F90:18-556 advance(itime): increments *itime and advances one step. */
+int ib_advance(IbCtx* ctx, int* itime);
+
+/* state access (the arrays of variables.F90:10-33) */
+int ib_get_field(IbCtx* ctx, int field, int level, double* out);
+int ib_set_field(IbCtx* ctx, int field, int level, const double* in);
+int ib_get_vector(IbCtx* ctx, int which, double* out);
+int ib_set_vector(IbCtx* ctx, int which, const double* in);
+/* write_force2 (operators_struct.F90:711-731): cx[nbody], cy[nbody] */
+int ib_get_forces(IbCtx* ctx, double* cx, double* cy);
+/* torsional state of family-2 bodies in file order (variables.F90:31-32) */
+int ib_get_body_state(IbCtx* ctx, double* theta, double* thetad, double* thetadd);
+/* ksp_iter, fsi_iter of the last step (timestepper.F90:365-366, 456) */
+int ib_get_counters(IbCtx* ctx, int* ksp_iter, int* fsi_iter);
+int ib_get_dims(IbCtx* ctx, int* nf, int* nbc, int* ns, int* nu, int* nv);
+
+/* ---- operator level (grid level 'level' is 0-based; tables of that level) ---- */
+/* operators_fluid.F90:553-587; qx, qy are the total fluxes q+q0 */
+int ib_nonlinear(IbCtx* ctx, const double* omega, const double* qx, const double* qy, const double* bc,
+                 double* nlx, double* nly);
+/* operators_fluid.F90:203-233 rot_int + rot_bc */
+int ib_rot(IbCtx* ctx, const double* hx, const double* hy, double* vort);
+/* operators_fluid.F90:423-471 curl_int + curl_bc */
+int ib_curl(IbCtx* ctx, const double* s, const double* sbc, double* qx, double* qy);
+/* operators_fluid.F90:381-419 (coarse modified in place, centre region only) */
+int ib_coarsify(IbCtx* ctx, const double* fine, double* coarse);
+/* operators_fluid.F90:475-535 */
+int ib_get_bc(IbCtx* ctx, const double* s, double fac, double* ring);
+/* operators_fluid.F90:539-549 (in place) */
+int ib_apply_bc(IbCtx* ctx, double* vort, const double* ring, double fac);
+/* myfft.F90:207-216 dst: unnormalised 2-D DST-I (FFTW RODFT00 x RODFT00) */
+int ib_dst(IbCtx* ctx, const double* in, double* out);
+/* myfft.F90:177-188 ctci */
+int ib_ctci(IbCtx* ctx, const double* vort, double* s);
+/* myfft.F90:161-173 ainv (in place) */
+int ib_ainv(IbCtx* ctx, double* vort);
+/* operators_fluid.F90:649-663 fluid_predictor (omega in place) */
+int ib_fluid_predictor(IbCtx* ctx, int level, double* omega, const double* rhs, const double* rhs_old,
+                       const double* rhsbc);
+/* operators_fluid.F90:237-377 vort2flux: omega, s: L*(n-1)(m-1); qx: L*n(m+1); qy: L*(n+1)m,
+ * levels contiguous; omega's coarse centres are overwritten as in the reference */
+int ib_vort2flux(IbCtx* ctx, double* omega, double* s, double* qx, double* qy);
+/* grid.F90:459-528 setup_reg / variables.F90:364-373 reg_prep for positions xb, yb (nf each) */
+int ib_reg_prep(IbCtx* ctx, const double* xb, const double* yb);
+/* fsinterface.F90:14-47 reg: hx, hy = E^T h0 (fields overwritten) */
+int ib_reg(IbCtx* ctx, const double* h0, double* hx, double* hy);
+/* fsinterface.F90:51-80 regT: h0 += E (hx, hy) */
+int ib_regT(IbCtx* ctx, const double* hx, const double* hy, double* h0);
+/* operators_struct.F90:735-834 */
+int ib_redistribute(IbCtx* ctx, const double* f, double* frdst);
+/* timestepper.F90:774-782 ab_times = operators_fluid.F90:14-120 a_times2 (+ b_times2) */
+int ib_schur_apply(IbCtx* ctx, const double* x, double* y);
+/* operators_fluid.F90:1020-1105 a_times (fluid part only) */
+int ib_schur_apply_fluid(IbCtx* ctx, const double* x, double* y);
+/* operators_struct.F90:14-127 b_times2 */
+int ib_struct_btimes(IbCtx* ctx, const double* x, double* y);
+/* operators_struct.F90:342-398 compute_rhs: y (nf) gets the structural rhs, zero elsewhere */
+int ib_struct_rhs(IbCtx* ctx, double* y);
+/* operators_struct.F90:402-505 compute_dx: updates theta and body positions; *err = max |dtheta| */
+int ib_struct_dx(IbCtx* ctx, const double* f, double* err);
+/* GMRES on the Schur operator (timestepper.F90:363-366): f updated in place */
+int ib_schur_solve(IbCtx* ctx, const double* rhs, double* f, int* iterations);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IB_GPU_H */

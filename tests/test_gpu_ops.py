@@ -1,0 +1,115 @@
+"""Operator-level parity of the CUDA path (through the C ABI) with the oracle."""
+import numpy as np
+import pytest
+
+import ib_oracle as O
+from helpers import PLATE, SMALL, pair, rel, small_cylinder, small_plate
+
+pytestmark = pytest.mark.gpu
+
+TOL_OP = 1e-13   # stencils and single transforms (FP64 round-off)
+
+
+@pytest.fixture(scope="module")
+def cyl():
+    o, g = pair(SMALL, [small_cylinder()])
+    yield o, g
+    g.close()
+
+
+def _rand(rng, shape):
+    return rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("mn", [(64, 32), (60, 40), (96, 48), (120, 36), (40, 200)])
+def test_dst_sizes(mn):
+    m, n = mn
+    kw = dict(SMALL, m=m, n=n, mgridlev=2)
+    o, g = pair(kw, [])
+    rng = np.random.default_rng(m * 1000 + n)
+    x = _rand(rng, (n - 1, m - 1))
+    assert rel(g.dst(x), o.dst(x)) < TOL_OP
+    assert rel(g.ctci(x), o.ctci(x)) < TOL_OP
+    assert rel(g.ainv(x), o.ainv(x)) < TOL_OP
+    g.close()
+
+
+def test_dst_involution(cyl):
+    o, g = cyl
+    rng = np.random.default_rng(1)
+    x = _rand(rng, (o.n - 1, o.m - 1))
+    y = g.dst(g.dst(x)) / o.normalize
+    assert rel(y, x) < 1e-13
+
+
+def test_stencils(cyl):
+    o, g = cyl
+    rng = np.random.default_rng(2)
+    m, n = o.m, o.n
+    om = _rand(rng, (n - 1, m - 1)); qx = _rand(rng, (n, m + 1)); qy = _rand(rng, (n + 1, m))
+    bc = _rand(rng, o.nbc)
+    nlx, nly = g.nonlinear(om, qx, qy, bc)
+    ex, ey = o.nonlinear(om, qx, qy, bc)
+    assert rel(nlx, ex) < TOL_OP and rel(nly, ey) < TOL_OP
+    assert rel(g.rot(qx, qy), o.rot(qx, qy)) < TOL_OP
+    cx, cy = g.curl(om, bc)
+    dx, dy = o.curl(om, bc)
+    assert rel(cx, dx) < TOL_OP and rel(cy, dy) < TOL_OP
+    coarse = _rand(rng, (n - 1, m - 1))
+    assert rel(g.coarsify(om, coarse), o.coarsify(om, coarse.copy())) < TOL_OP
+    for fac in (0.25, 1.0):
+        assert rel(g.get_bc(om, fac), o.get_bc(om, fac)) < TOL_OP
+        assert rel(g.apply_bc(om, bc, fac), o.apply_bc(om.copy(), bc, fac)) < TOL_OP
+
+
+def test_predictor(cyl):
+    o, g = cyl
+    rng = np.random.default_rng(3)
+    sh = (o.n - 1, o.m - 1)
+    om, r, ro, rb = (_rand(rng, sh) for _ in range(4))
+    for k in range(o.L):
+        assert rel(g.fluid_predictor(k, om, r, ro, rb), o.fluid_predictor(om, r, ro, rb, k)) < 1e-12
+
+
+def test_vort2flux(cyl):
+    o, g = cyl
+    rng = np.random.default_rng(4)
+    w = [_rand(rng, (o.n - 1, o.m - 1)) for _ in range(o.L)]
+    wg, sg, qxg, qyg = g.vort2flux([x.copy() for x in w])
+    wo = [x.copy() for x in w]
+    so, qxo, qyo = o.vort2flux(wo)
+    for k in range(o.L):
+        assert rel(wg[k], wo[k]) < TOL_OP
+        assert rel(sg[k], so[k]) < 1e-12
+        assert rel(qxg[k], qxo[k]) < 1e-12
+        assert rel(qyg[k], qyo[k]) < 1e-12
+
+
+def test_reg_regT_redistribute(cyl):
+    o, g = cyl
+    rng = np.random.default_rng(5)
+    f = _rand(rng, o.nf)
+    hx, hy = g.reg(f)
+    ex, ey = o.reg(f)
+    assert rel(hx, ex) < 1e-14 and rel(hy, ey) < 1e-14
+    qx = _rand(rng, (o.n, o.m + 1)); qy = _rand(rng, (o.n + 1, o.m))
+    h0 = _rand(rng, o.nf)
+    assert rel(g.regT(qx, qy, h0), o.regT(qx, qy, h0)) < 1e-14
+    assert rel(g.redistribute(f), o.redistribute(f)) < 1e-13
+
+
+def test_schur_matvec(cyl):
+    o, g = cyl
+    rng = np.random.default_rng(6)
+    x = _rand(rng, o.nf)
+    assert rel(g.schur_apply(x), o.a_times(x)) < 1e-12
+    assert rel(g.schur_apply(x, with_b=False), o.a_times(x, with_b=False)) < 1e-12
+
+
+def test_plate_struct_ops():
+    o, g = pair(PLATE, [small_plate()])
+    rng = np.random.default_rng(7)
+    x = _rand(rng, o.nf)
+    assert rel(g.struct_btimes(x), o.b_times(x)) < 1e-13
+    assert rel(g.schur_apply(x), o.a_times(x)) < 1e-12
+    g.close()
