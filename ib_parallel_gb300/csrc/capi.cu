@@ -459,4 +459,62 @@ int ib_schur_solve(IbCtx* h, const double* rhs, double* f, int* iterations) {
   return op_result(S.finish(rc), "schur_solve failed");
 }
 
+int ib_get_stream(IbCtx* h, void** stream) {
+  CTX_OR_FAIL(h);
+  if (!stream) return fail(IB_ERR_ARG, "null output");
+  *stream = (void*)c->st;
+  return IB_OK;
+}
+
+int ib_get_work(IbCtx* h, long long* matvecs, long long* passes4) {
+  CTX_OR_FAIL(h);
+  if (matvecs) *matvecs = c->n_matvec;
+  if (passes4)
+    for (int i = 0; i < 4; ++i) passes4[i] = c->n_pass[i];
+  return IB_OK;
+}
+
+long long ib_launch_count(void) { return ib::launch_count(); }
+
+int ib_measure_fp64_peak(double* tflops) {
+  if (!tflops) return fail(IB_ERR_ARG, "null output");
+  int rc = ib::probe_fp64(tflops);
+  return op_result(rc, "fp64 probe failed");
+}
+
+int ib_probe_throughput(int which, double* value) {
+  if (!value || which < 0 || which > 4) return fail(IB_ERR_ARG, "bad probe");
+  return op_result(ib::probe_throughput(which, value), "probe failed");
+}
+
+int ib_profile(IbCtx* h, int enable) {
+  CTX_OR_FAIL(h);
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "sync failed");
+  if (enable) c->prof_n = 0;
+  c->prof_on = enable != 0;
+  return IB_OK;
+}
+
+int ib_profile_read(IbCtx* h, int kind, int* count, double* total_ms, double* bytes) {
+  CTX_OR_FAIL(h);
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "sync failed");
+  int n = 0;
+  double t = 0.0, b = 0.0;
+  for (int i = 0; i < c->prof_n; ++i) {
+    if (c->prof_kind[i] != kind) continue;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->prof_ev[2 * i], c->prof_ev[2 * i + 1]) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    ++n;
+    t += ms;
+    b += c->prof_bytes[i];
+  }
+  if (count) *count = n;
+  if (total_ms) *total_ms = t;
+  if (bytes) *bytes = b;
+  return IB_OK;
+}
+
 }  // extern "C"

@@ -78,6 +78,26 @@ struct Ctx {
   size_t stage_n = 0;
 
   int itime = 0, ksp_iter = 0, fsi_iter = 0;
+
+  // work counters (host side): Schur matvecs and DST passes by kind
+  long long n_matvec = 0;
+  long long n_pass[4] = {0, 0, 0, 0};
+
+  // optional CUDA-event timing of DST passes (ib_profile)
+  static constexpr int kProfMax = 8192;
+  bool prof_on = false;
+  int prof_n = 0;
+  std::vector<cudaEvent_t> prof_ev;     // 2 per record
+  std::vector<int> prof_kind;
+  std::vector<double> prof_bytes;
+};
+
+// Wraps one DST pass launch in an event pair when profiling is on.
+struct ProfScope {
+  Ctx* c;
+  int slot = -1;
+  ProfScope(Ctx* cc, int kind, double bytes);
+  ~ProfScope();
 };
 
 // solver.cu

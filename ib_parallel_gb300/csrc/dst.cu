@@ -362,16 +362,19 @@ int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs&
     case PRE_COPY:
       rc = launch_cfg(k_dst_x<PRE_COPY>, smem);
       if (rc) return rc;
+      count_launch();
       k_dst_x<PRE_COPY><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
       break;
     case PRE_COMBINE:
       rc = launch_cfg(k_dst_x<PRE_COMBINE>, smem);
       if (rc) return rc;
+      count_launch();
       k_dst_x<PRE_COMBINE><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
       break;
     default:
       rc = launch_cfg(k_dst_x<PRE_APPLYBC>, smem);
       if (rc) return rc;
+      count_launch();
       k_dst_x<PRE_APPLYBC><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
       break;
   }
@@ -389,16 +392,19 @@ int dst_pass_y(const DstPlan& py, int ncols, int ld, DstYMode mode, const DstYAr
     case YMODE_NONE:
       rc = launch_cfg(k_dst_y<YMODE_NONE>, smem);
       if (rc) return rc;
+      count_launch();
       k_dst_y<YMODE_NONE><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
       break;
     case YMODE_DIAG:
       rc = launch_cfg(k_dst_y<YMODE_DIAG>, smem);
       if (rc) return rc;
+      count_launch();
       k_dst_y<YMODE_DIAG><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
       break;
     default:
       rc = launch_cfg(k_dst_y<YMODE_PRED>, smem);
       if (rc) return rc;
+      count_launch();
       k_dst_y<YMODE_PRED><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
       break;
   }

@@ -180,22 +180,26 @@ __global__ void k_gmres_update(GmresDev G, double* __restrict__ x) {
 }
 
 int launch_gmres_init(const GmresDev& G, cudaStream_t st) {
+  count_launch();
   k_gmres_init<<<1, 32, 0, st>>>(G);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
 int launch_gmres_start(const GmresDev& G, const double* b, const double* x, double rtol, double atol, int max_it,
                        cudaStream_t st) {
+  count_launch();
   k_gmres_start<<<1, kGmresThreads, 0, st>>>(G, b, x, rtol, atol, max_it);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
 int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st) {
+  count_launch();
   k_gmres_arnoldi<<<1, kGmresThreads, 0, st>>>(G, max_it);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
 int launch_gmres_update(const GmresDev& G, double* x, cudaStream_t st) {
+  count_launch();
   k_gmres_update<<<1, kGmresThreads, 0, st>>>(G, x);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
@@ -259,6 +263,7 @@ __global__ void k_unit(int n, int i, double* e) {
 }
 
 int launch_cholesky(int n, double* A, int* d_err, cudaStream_t st) {
+  count_launch();
   k_cholesky<<<1, 1024, 0, st>>>(n, A, d_err);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
@@ -268,16 +273,19 @@ int launch_chol_solve(int n, const double* Lf, const double* b, double* x, cudaS
   if (smem > 48 * 1024) {
     IB_CUDA_CHECK(cudaFuncSetAttribute(k_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
+  count_launch();
   k_chol_solve<<<1, 512, smem, st>>>(n, Lf, b, x);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
 int launch_copy_col(int n, const double* src, double* M, int col, cudaStream_t st) {
+  count_launch();
   k_copy_col<<<cdiv(n, 256), 256, 0, st>>>(n, src, M, col);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
 int launch_unit(int n, int i, double* e, cudaStream_t st) {
+  count_launch();
   k_unit<<<cdiv(n, 256), 256, 0, st>>>(n, i, e);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;

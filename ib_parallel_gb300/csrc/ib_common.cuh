@@ -60,6 +60,11 @@ __device__ __forceinline__ double ghost_vertex(const double* __restrict__ f,
 
 inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Number of kernels this library has launched (all contexts), for the benchmark's
+// launch count.  Defined in solver.cu.
+void count_launch();
+long long launch_count();
+
 }  // namespace ib
 
 #define IB_CUDA_CHECK(expr)                                                     \

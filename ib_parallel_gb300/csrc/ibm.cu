@@ -168,11 +168,16 @@ __global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y,
 int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
                      double offy, RegDev& r, int* d_err, cudaStream_t st) {
   if (nf == 0) return IB_OK;
+  count_launch();
   k_reg_weights<<<cdiv(nf, 128), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w, d_err);
+  count_launch();
   k_reg_bbox<<<1, 256, 0, st>>>(nf, r.ix, r.iy, r.bbox);
+  count_launch();
   k_reg_lists<false><<<152 * 2, 128, 0, st>>>(nf, r.comp, r.ix, r.iy, r.bbox, r.cnt_x, r.cnt_y, nullptr,
                                               nullptr, r.max_faces);
+  count_launch();
   k_reg_scan<<<1, 1024, 0, st>>>(r.bbox, r.cnt_x, r.cnt_y, r.max_faces);
+  count_launch();
   k_reg_lists<true><<<152 * 2, 128, 0, st>>>(nf, r.comp, r.ix, r.iy, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y,
                                              r.max_faces);
   IB_CUDA_CHECK(cudaGetLastError());
@@ -195,6 +200,9 @@ __global__ void k_reg(GridDims g, const double* __restrict__ h0, const double* _
     const int* lst = cx ? lst_x : lst_y;
     int a = cnt[fidx], b = cnt[fidx + 1];
     if (a == b) continue;
+    // faces outside the grid (a body too close to the edge, flagged as IB_ERR_DOMAIN
+    // when the weights were built) are skipped rather than written
+    if (fi < 1 || fj < 1 || fi > (cx ? g.nux : g.nvx) || fj > (cx ? g.nuy : g.nvy)) continue;
     double acc = 0.0;
     for (int q = a; q < b; ++q) {
       int e = lst[q];
@@ -210,6 +218,7 @@ int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, dou
   IB_CUDA_CHECK(cudaMemsetAsync(hx, 0, sizeof(double) * g.nu, st));
   IB_CUDA_CHECK(cudaMemsetAsync(hy, 0, sizeof(double) * g.nv, st));
   if (nf == 0) return IB_OK;
+  count_launch();
   k_reg<<<152 * 2, 128, 0, st>>>(g, h0, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, hx, hy, r.max_faces);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
@@ -226,6 +235,7 @@ __global__ void k_regT(GridDims g, int nf, const double* __restrict__ qx, const 
   const double* q = isx ? qx : qy;
   const double* q0 = isx ? qx0 : qy0;
   int ld = isx ? g.nux : g.nvx;
+  int ny = isx ? g.nuy : g.nvy;
   int cx = ix[k], cy = iy[k];
   const double* wk = w + (size_t)k * 49;
   double vals[49];
@@ -233,8 +243,12 @@ __global__ void k_regT(GridDims g, int nf, const double* __restrict__ qx, const 
   for (int l = 0; l < 7; ++l)
 #pragma unroll
     for (int p = 0; p < 7; ++p) {
-      int idx = (cy + l - 3 - 1) * ld + (cx + p - 3 - 1);
-      vals[l * 7 + p] = q0 ? q[idx] + q0[idx] : q[idx];
+      int fi = cx + p - 3, fj = cy + l - 3;
+      // stencil faces outside the grid (flagged as IB_ERR_DOMAIN) contribute nothing
+      bool in = fi >= 1 && fi <= ld && fj >= 1 && fj <= ny;
+      int idx = in ? (fj - 1) * ld + (fi - 1) : 0;
+      double v = q0 ? q[idx] + q0[idx] : q[idx];
+      vals[l * 7 + p] = in ? v : 0.0;
     }
   double acc = h0_in ? h0_in[k] : 0.0;
 #pragma unroll
@@ -245,6 +259,7 @@ __global__ void k_regT(GridDims g, int nf, const double* __restrict__ qx, const 
 int launch_regT(const GridDims& g, int nf, const double* qx, const double* qx0, const double* qy, const double* qy0,
                 const RegDev& r, const double* h0_in, double* h0_out, cudaStream_t st) {
   if (nf == 0) return IB_OK;
+  count_launch();
   k_regT<<<cdiv(nf, 64), 64, 0, st>>>(g, nf, qx, qx0, qy, qy0, r.comp, r.ix, r.iy, r.w, h0_in, h0_out);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
@@ -266,6 +281,7 @@ __global__ void k_redist_field(GridDims g, const double* __restrict__ f, const d
     const int* lst = cx ? lst_x : lst_y;
     int a = cnt[fidx], b = cnt[fidx + 1];
     if (a == b) continue;
+    if (fi < 1 || fj < 1 || fi > (cx ? g.nux : g.nvx) || fj > (cx ? g.nuy : g.nvy)) continue;
     double ws = 0.0, fs = 0.0;
     for (int q = a; q < b; ++q) {
       int e = lst[q];
@@ -283,6 +299,7 @@ int launch_redistribute_field(const GridDims& g, int nf, const double* f, const 
   IB_CUDA_CHECK(cudaMemsetAsync(fx, 0, sizeof(double) * g.nu, st));
   IB_CUDA_CHECK(cudaMemsetAsync(fy, 0, sizeof(double) * g.nv, st));
   if (nf == 0) return IB_OK;
+  count_launch();
   k_redist_field<<<152 * 2, 128, 0, st>>>(g, f, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, fx, fy,
                                           r.max_faces);
   IB_CUDA_CHECK(cudaGetLastError());
@@ -308,6 +325,7 @@ __global__ void k_force_coeffs(int nf, int nbody, const int* __restrict__ comp, 
 int launch_force_coeffs(int nf, int nbody, const int* comp, const int* bid, const double* f, double dt,
                         double delta, double* out, cudaStream_t st) {
   if (nbody == 0) return IB_OK;
+  count_launch();
   k_force_coeffs<<<cdiv(nbody, 32), 32, 0, st>>>(nf, nbody, comp, bid, f, dt, delta, out);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;

@@ -1,6 +1,7 @@
 // The time step of timestepper.F90:18-556 and the composite operators it calls,
 // orchestrated on one CUDA stream over device-resident state.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -15,6 +16,25 @@ namespace ib {
   } while (0)
 
 static const double kPi = 4.0 * std::atan(1.0);  // parameters.F90:61
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+ProfScope::ProfScope(Ctx* cc, int kind, double bytes) : c(cc) {
+  c->n_pass[kind] += 1;
+  if (!c->prof_on || c->prof_n >= Ctx::kProfMax) return;
+  slot = c->prof_n++;
+  c->prof_kind[slot] = kind;
+  c->prof_bytes[slot] = bytes;
+  cudaEventRecord(c->prof_ev[2 * slot], c->st);
+}
+ProfScope::~ProfScope() {
+  if (slot >= 0) cudaEventRecord(c->prof_ev[2 * slot + 1], c->st);
+}
+
+// algorithmic DRAM bytes of one pass: each input field read once, the output written once
+static double pass_bytes(const Ctx* c, int nin, int nout) { return 8.0 * c->g.ns * (nin + nout); }
 
 // ------------------------------------------------------------- DST tuning
 static int time_pass(Ctx* c, int which, const DstLaunch& L, float* ms) {
@@ -211,6 +231,11 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     *msg = "pinned allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM;
   }
 
+  c->prof_ev.resize(2 * Ctx::kProfMax);
+  c->prof_kind.resize(Ctx::kProfMax);
+  c->prof_bytes.resize(Ctx::kProfMax);
+  for (auto& e : c->prof_ev) IB_CUDA_CHECK(cudaEventCreate(&e));
+
   // spectral tables (myfft.F90:125-148)
   {
     std::vector<double> lam(ns), t1(ns), t2(ns);
@@ -292,6 +317,8 @@ void ctx_destroy(Ctx* c) {
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);
+  for (auto& e : c->prof_ev)
+    if (e) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -312,12 +339,19 @@ int check_err(Ctx* c) {
 static int ctci_like(Ctx* c, const double* in, double* out, const double* ring, const double* table) {
   DstXArgs a;
   a.in = in; a.out = c->spec1; a.ring = ring; a.fac = 1.0;
-  RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, ring ? PRE_APPLYBC : PRE_COPY, a, c->g, c->lx, c->st));
+  {
+    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, ring ? PRE_APPLYBC : PRE_COPY, a, c->g, c->lx, c->st));
+  }
   DstYArgs y;
   y.a = c->spec1; y.t1 = table;
-  RC(dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_DIAG, y, c->ly_diag, c->st));
+  {
+    ProfScope ps(c, 1, pass_bytes(c, 2, 1));
+    RC(dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_DIAG, y, c->ly_diag, c->st));
+  }
   DstXArgs b;
   b.in = c->spec1; b.out = out;
+  ProfScope ps(c, 0, pass_bytes(c, 1, 1));
   return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, b, c->g, c->lx, c->st);
 }
 
@@ -327,9 +361,13 @@ int op_ainv(Ctx* c, const double* in, double* out) { return ctci_like(c, in, out
 int op_dst(Ctx* c, const double* in, double* out) {
   DstXArgs a;
   a.in = in; a.out = out;
-  RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, a, c->g, c->lx, c->st));
+  {
+    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, a, c->g, c->lx, c->st));
+  }
   DstYArgs y;
   y.a = out;
+  ProfScope ps(c, 3, pass_bytes(c, 1, 1));
   return dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_NONE, y, c->ly_none, c->st);
 }
 
@@ -337,15 +375,25 @@ int op_dst(Ctx* c, const double* in, double* out) {
 int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs_old, const double* rhsbc) {
   DstXArgs a;
   a.in = rhs; a.in2 = rhs_old; a.in3 = rhsbc; a.ca = c->con1[k]; a.cb = c->con2[k]; a.out = c->spec1;
-  RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COMBINE, a, c->g, c->lx, c->st));
+  {
+    ProfScope ps(c, 0, pass_bytes(c, 3, 1));
+    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COMBINE, a, c->g, c->lx, c->st));
+  }
   DstXArgs b;
   b.in = om; b.out = c->spec2;
-  RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, b, c->g, c->lx, c->st));
+  {
+    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, b, c->g, c->lx, c->st));
+  }
   DstYArgs y;
   y.a = c->spec1; y.b = c->spec2; y.t1 = c->lam1i[k]; y.t2 = c->lam1[k];
-  RC(dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_PRED, y, c->ly_pred, c->st));
+  {
+    ProfScope ps(c, 2, pass_bytes(c, 4, 1));
+    RC(dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_PRED, y, c->ly_pred, c->st));
+  }
   DstXArgs d;
   d.in = c->spec1; d.out = om;
+  ProfScope ps(c, 0, pass_bytes(c, 1, 1));
   return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, d, c->g, c->lx, c->st);
 }
 
@@ -369,6 +417,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
 // ab_times / a_times2 (timestepper.F90:774-782, operators_fluid.F90:14-120)
 int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
   const GridDims& g = c->g;
+  c->n_matvec += 1;
   RC(launch_reg(g, c->nf, x, c->reg, c->hx, c->hy, c->st));
   RC(launch_rot(g, c->hx, c->hy, c->mv_w[0], c->st));
   RC(op_ainv(c, c->mv_w[0], c->mv_w[0]));

@@ -166,44 +166,54 @@ static inline int blocks(long long n, int nt = 256) { return (int)((n + nt - 1) 
 
 int launch_nonlinear(const GridDims& g, const double* om, const double* bc, const double* qx, const double* q0x,
                      const double* qy, const double* q0y, double* nlx, double* nly, cudaStream_t st) {
+  count_launch();
   k_nonlinear<<<blocks(g.nu + g.nv), 256, 0, st>>>(g, om, bc, qx, q0x, qy, q0y, nlx, nly);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vort, cudaStream_t st) {
+  count_launch();
   k_rot<<<blocks(g.ns), 256, 0, st>>>(g, hx, hy, vort);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_curl(const GridDims& g, const double* s, const double* sbc, double* qx, double* qy, cudaStream_t st) {
+  count_launch();
   k_curl<<<blocks(g.nu + g.nv), 256, 0, st>>>(g, s, sbc, qx, qy);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_coarsify(const GridDims& g, const double* fine, double* coarse, cudaStream_t st) {
   int n = (g.m / 2 - 1) * (g.n / 2 - 1);
+  count_launch();
   k_coarsify<<<blocks(n), 256, 0, st>>>(g, fine, coarse);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_get_bc(const GridDims& g, const double* s, double fac, double* ring, cudaStream_t st) {
+  count_launch();
   k_get_bc<<<blocks(g.nbc), 256, 0, st>>>(g, s, fac, ring);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st) {
+  count_launch();
   k_apply_bc<<<blocks(g.ns), 256, 0, st>>>(g, v, ring, fac);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st) {
+  count_launch();
   k_rhsbc<<<blocks(g.ns), 256, 0, st>>>(g, v, ra, rb, fac);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st) {
+  count_launch();
   k_axpby<<<blocks(n), 256, 0, st>>>(n, a, x, b, y, z);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_sub(int n, const double* x, const double* y, double* z, cudaStream_t st) {
+  count_launch();
   k_sub<<<blocks(n), 256, 0, st>>>(n, x, y, z);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_fill(int n, double v, double* z, cudaStream_t st) {
   if (n <= 0) return IB_OK;
+  count_launch();
   k_fill<<<blocks(n), 256, 0, st>>>(n, v, z);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }

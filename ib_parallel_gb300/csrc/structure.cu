@@ -131,6 +131,7 @@ __global__ void k_tors_save(int nt, TorsState s) {
 int launch_tors_btimes(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, const double* x,
                        double* y, cudaStream_t st) {
   if (nt == 0) return IB_OK;
+  count_launch();
   k_tors_btimes<<<nt, 256, 0, st>>>(tb, s, dt, delta, x, y);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
@@ -138,6 +139,7 @@ int launch_tors_btimes(int nt, const TorsBody* tb, const TorsState& s, double dt
 int launch_tors_rhs(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, double* y,
                     cudaStream_t st) {
   if (nt == 0) return IB_OK;
+  count_launch();
   k_tors_rhs<<<nt, 256, 0, st>>>(tb, s, dt, delta, y);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
@@ -149,7 +151,9 @@ int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, do
     return IB_OK;
   }
   // err[1..nt] holds per-body |dtheta|, err[0] their maximum
+  count_launch();
   k_tors_dx<<<nt, 256, 0, st>>>(tb, s, dt, delta, f, xb, yb, err + 1);
+  count_launch();
   k_max_reduce<<<1, 32, 0, st>>>(nt, err + 1, err);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
@@ -157,12 +161,14 @@ int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, do
 int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta,
                             const double* f, cudaStream_t st) {
   if (nt == 0) return IB_OK;
+  count_launch();
   k_tors_initial_acc<<<nt, 256, 0, st>>>(tb, s, dt, delta, f);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
 int launch_tors_save(int nt, const TorsState& s, cudaStream_t st) {
   if (nt == 0) return IB_OK;
+  count_launch();
   k_tors_save<<<cdiv(nt, 64), 64, 0, st>>>(nt, s);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;

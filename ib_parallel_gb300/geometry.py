@@ -38,13 +38,19 @@ def config_cylinder_400x200() -> tuple:
     return p, [cylinder(157)]
 
 
-def config_plate_800x400(seed: int = 0) -> tuple:
-    """Hinged flat plate (torsional analogue of the flexible plate): length 1, 201 points,
-    10 degrees incidence with a seeded 0.01 tip perturbation, Re=500, 800x400 on
-    [-1,7]x[-2,2], 5 levels, dt=1e-3, GMRES and FSI tolerance 1e-10."""
+def config_plate_800x400(seed: int = 0, npts: int = 51) -> tuple:
+    """Hinged flat plate (torsional analogue of the flexible plate): length 1, 10 degrees
+    incidence with a seeded 0.01 tip perturbation, Re=500, 800x400 on [-1,7]x[-2,2],
+    5 levels, dt=1e-3, GMRES and FSI tolerance 1e-10.
+
+    51 body points put the Lagrangian spacing at twice the grid spacing, the spacing the
+    reference's own inputs use.  At one or half a grid spacing (101 or 201 points) the
+    Schur operator is close to singular and GMRES(30) with classical Gram-Schmidt does not
+    reach 1e-10 (2000 iterations without convergence on the half-size grid), so the FSI
+    loop of timestepper.F90:318 never terminates."""
     rng = np.random.default_rng(seed)
     tip = 0.01 * rng.standard_normal()
     gamma0 = -10.0 + math.degrees(math.asin(max(-1.0, min(1.0, tip))))
     p = Params(m=800, n=400, mgridlev=5, dt=1e-3, Re=500.0, len=8.0, offsetx=1.0, offsety=2.0,
                fsi_tol=1e-10, atol=1e-10, rtol=1e-10)
-    return p, [torsional_plate(201, 1.0, gamma0, itheta=0.5 / 3.0, ktheta=1e-3)]
+    return p, [torsional_plate(npts, 1.0, gamma0, itheta=0.5 / 3.0, ktheta=1e-3)]

@@ -37,6 +37,8 @@ EXPORTS = [
     "ib_coarsify", "ib_get_bc", "ib_apply_bc", "ib_dst", "ib_ctci", "ib_ainv", "ib_fluid_predictor",
     "ib_vort2flux", "ib_reg_prep", "ib_reg", "ib_regT", "ib_redistribute", "ib_schur_apply",
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
+    "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
+    "ib_launch_count", "ib_probe_throughput",
 ]
 
 
@@ -95,6 +97,12 @@ def load(path: Optional[os.PathLike] = None):
         "ib_schur_apply_fluid": ([P, P, P], C.c_int), "ib_struct_btimes": ([P, P, P], C.c_int),
         "ib_struct_rhs": ([P, P], C.c_int), "ib_struct_dx": ([P, P, P], C.c_int),
         "ib_schur_solve": ([P, P, P, I], C.c_int),
+        "ib_get_stream": ([P, C.POINTER(P)], C.c_int), "ib_profile": ([P, C.c_int], C.c_int),
+        "ib_profile_read": ([P, C.c_int, I, D, D], C.c_int),
+        "ib_get_work": ([P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
+        "ib_measure_fp64_peak": ([D], C.c_int),
+        "ib_launch_count": ([], C.c_longlong),
+        "ib_probe_throughput": ([C.c_int, D], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -118,6 +126,25 @@ def _ptr(a):
     if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]):
         raise TypeError("arrays must be C-contiguous float64 numpy arrays or CUDA tensors")
     return C.c_void_p(a.ctypes.data)
+
+
+def launch_count() -> int:
+    """Kernels launched by libibgpu.so since it was loaded."""
+    return int(load().ib_launch_count())
+
+
+def probe_throughput(which: int) -> float:
+    """0 FP64 FMA, 1 FP64 FMA half lanes, 2 FP64 FMA one warp/SM, 3 FP32 FMA, 4 INT32 IMAD (T/s)."""
+    t = C.c_double()
+    _check(load().ib_probe_throughput(which, C.byref(t)), "ib_probe_throughput")
+    return t.value
+
+
+def measure_fp64_peak() -> float:
+    """FP64 FMA throughput of the current GPU in TFLOP/s."""
+    t = C.c_double()
+    _check(load().ib_measure_fp64_peak(C.byref(t)), "ib_measure_fp64_peak")
+    return t.value
 
 
 @dataclass
@@ -256,6 +283,25 @@ class Simulation:
         _check(self.lib.ib_get_counters(self.h, C.byref(k), C.byref(f)))
         return k.value, f.value
 
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(self.lib.ib_get_stream(self.h, C.byref(s)), "ib_get_stream")
+        return s.value or 0
+
+    def profile(self, enable: bool):
+        _check(self.lib.ib_profile(self.h, int(bool(enable))), "ib_profile")
+
+    def profile_read(self, kind: int):
+        n, t, b = C.c_int(), C.c_double(), C.c_double()
+        _check(self.lib.ib_profile_read(self.h, kind, C.byref(n), C.byref(t), C.byref(b)), "ib_profile_read")
+        return n.value, t.value, b.value
+
+    def work(self):
+        mv = C.c_longlong()
+        passes = (C.c_longlong * 4)()
+        _check(self.lib.ib_get_work(self.h, C.byref(mv), passes), "ib_get_work")
+        return mv.value, list(passes)
+
     def synchronize(self):
         _check(self.lib.ib_synchronize(self.h), "ib_synchronize")
 
@@ -366,3 +412,11 @@ class Simulation:
         _check(self.lib.ib_schur_solve(self.h, _ptr(np.ascontiguousarray(rhs, dtype=np.float64)), _ptr(f),
                                        C.byref(its)), "ib_schur_solve")
         return f, its.value
+
+
+if __name__ == "__main__":
+    import sys as _s
+    if len(_s.argv) > 1 and _s.argv[1] == "probe":
+        names = ["fp64_fma", "fp64_fma_half_lanes", "fp64_fma_1warp_per_sm", "fp32_fma", "int32_imad"]
+        for i, nme in enumerate(names):
+            print(f"{nme} {probe_throughput(i):.3f}")

@@ -136,6 +136,24 @@ int ib_struct_dx(IbCtx* ctx, const double* f, double* err);
 /* GMRES on the Schur operator (timestepper.F90:363-366): f updated in place */
 int ib_schur_solve(IbCtx* ctx, const double* rhs, double* f, int* iterations);
 
+/* ---- instrumentation (no counterpart in the reference) ---- */
+/* the cudaStream_t every kernel of this context runs on */
+int ib_get_stream(IbCtx* ctx, void** stream);
+/* enable (1) / disable (0) CUDA-event timing of each DST pass launch; enabling clears the totals */
+int ib_profile(IbCtx* ctx, int enable);
+/* work done since creation: Schur matvecs and DST passes by kind (0..3, see below) */
+int ib_get_work(IbCtx* ctx, long long* matvecs, long long* passes4);
+/* kernels launched by this library since it was loaded (all contexts) */
+long long ib_launch_count(void);
+/* measured FP64 FMA throughput of this GPU (TFLOP/s), from a register-resident FMA loop */
+int ib_measure_fp64_peak(double* tflops);
+/* which: 0 FP64 FMA, 1 FP64 FMA with half of each warp's lanes active (useful rate),
+ * 2 FP64 FMA with one warp per SM, 3 FP32 FMA, 4 INT32 IMAD; *value in T(FL)OP/s */
+int ib_probe_throughput(int which, double* value);
+/* kind 0: x pass, 1: y pass with diagonal, 2: y pass of the predictor, 3: plain y pass;
+ * count of timed launches, their summed device time (ms) and summed algorithmic DRAM bytes */
+int ib_profile_read(IbCtx* ctx, int kind, int* count, double* total_ms, double* bytes);
+
 #ifdef __cplusplus
 }
 #endif
