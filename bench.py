@@ -49,8 +49,9 @@ METRIC = "FSI steps/s @800x400x5 FP64"
 WORKLOAD = "plate800x400"
 # Schur matvecs per step of this workload (Krylov iterations + one initial-residual
 # product per GMRES cycle, summed over the FSI iterations), counted by the GPU
-# arm's ib_get_work over steps 4-8 on GB300; the CPU arm runs the same algorithm.
-MATVECS_PER_STEP = None
+# arm's ib_get_work (56.5 and 60 over the first steps after warm-up on GB300); the CPU
+# arm runs the same algorithm.
+MATVECS_PER_STEP = 58.0
 
 
 def _env_int(k, d):
@@ -286,27 +287,24 @@ def run_gpu(args, world, rank, local):
     e2e_s = _barrier_max(f0.elapsed_time(f1) / 1e3, world)
     e2e_value = world * args.steps / e2e_s
 
-    # ---- roofline of the dominant kernel: one more step with the DST passes event-timed
-    sim.profile(True)
-    sim.advance()
-    sim.synchronize()
-    kinds = {0: "k_dst_x", 1: "k_dst_y<DIAG>", 2: "k_dst_y<PRED>", 3: "k_dst_y<NONE>"}
-    prof = {kk: sim.profile_read(kk) for kk in kinds}
-    sim.profile(False)
-    dom = max(prof, key=lambda kk: prof[kk][1])
-    n_l, t_ms, bytes_ = prof[dom]
-    peak, peak_kind = _peaks()
-    achieved = (bytes_ / n_l) / ((t_ms / n_l) * 1e-3) / 1e9 if n_l else None
+    # ---- roofline of the dominant kernel (the DST-I x pass: largest share of the ncu launch
+    # list, profiles/launch_list_plate800x400.md), timed alone: 20 back-to-back full passes
+    # over the finest grid with CUDA events on the simulation's stream
     m, n = p.m, p.n
-    flops_pass = {0: 2.5 * (n - 1) * m * math.log2(2 * m), 1: 2 * 2.5 * (m - 1) * n * math.log2(2 * n)}
-    fp_flops = flops_pass[0] if dom == 0 else flops_pass[1]
+    ns = (m - 1) * (n - 1)
+    t_x = sim.time_pass(0, 20)
+    t_tri = sim.time_pass(1, 20)
+    bytes_x = 16.0 * ns                       # one field read, one written
+    achieved = bytes_x / (t_x * 1e-3) / 1e9
+    peak, peak_kind = _peaks()
+    flops_x = 2.5 * (n - 1) * m * math.log2(2 * m)
     fp64_peak = G.measure_fp64_peak()
-    fp_achieved = fp_flops / ((t_ms / n_l) * 1e-3) / 1e12 if n_l else None
+    fp_achieved = flops_x / (t_x * 1e-3) / 1e12
     traffic = None
     tpath = ROOT / "profiles" / "dst_traffic_800x400.txt"
     if tpath.exists():
         for line in tpath.read_text().splitlines():
-            if line.startswith(kinds[dom] + " dram_bytes_per_launch"):
+            if line.startswith("k_dst_x dram_bytes_per_launch"):
                 try:
                     traffic = float(line.split("=")[1])
                 except ValueError:
@@ -326,15 +324,15 @@ def run_gpu(args, world, rank, local):
         "work_per_step": {"schur_matvecs": mv_per_step, "ksp_iter": ksp_sum / args.steps,
                           "fsi_iter": fsi_sum / args.steps,
                           "dst_passes": [x / args.steps for x in passes_timed]},
-        "roofline": {"bound": "hbm", "kernel": kinds[dom], "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                     else "fallback 6.8 TB/s",
-                     "launches": n_l, "avg_launch_us": 1e3 * t_ms / n_l if n_l else None},
-        "fp64_roofline": {"kernel": kinds[dom], "achieved": fp_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                          "frac": (fp_achieved / fp64_peak) if fp_achieved else None,
-                          "flops_per_launch": fp_flops,
-                          "peak_source": "measured FP64 FMA loop on this GPU (ib_measure_fp64_peak)"},
+        "roofline": {"bound": "hbm", "kernel": "k_dst_x (DST-I along x, 399 rows of 799)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs, burst; kernel timed alone)"
+                     if peak_kind == "measured" else "of fallback 6.8 TB/s",
+                     "bytes_per_launch": bytes_x, "avg_launch_us": 1e3 * t_x},
+        "fp64_roofline": {"kernel": "k_dst_x", "achieved": fp_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                          "frac": fp_achieved / fp64_peak, "flops_per_launch": flops_x,
+                          "peak_source": "of measured FP64 FMA loop on this GPU (ib_measure_fp64_peak)"},
+        "tridiagonal_pass_us": 1e3 * t_tri,
     }
     result["gpu_launches"] = launches_timed
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -487,6 +487,12 @@ int ib_probe_throughput(int which, double* value) {
   return op_result(ib::probe_throughput(which, value), "probe failed");
 }
 
+int ib_time_pass(IbCtx* h, int kind, int reps, double* avg_ms) {
+  CTX_OR_FAIL(h);
+  if (!avg_ms || reps <= 0 || kind < 0 || kind > 1) return fail(IB_ERR_ARG, "bad argument");
+  return op_result(ib::op_time_pass(c, kind, reps, avg_ms), "time_pass failed");
+}
+
 int ib_profile(IbCtx* h, int enable) {
   CTX_OR_FAIL(h);
   if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "sync failed");

@@ -8,6 +8,7 @@
 #include "../../include/ib_gpu.h"
 #include "dst.cuh"
 #include "kernels.cuh"
+#include "tri.cuh"
 
 namespace ib {
 
@@ -34,18 +35,26 @@ struct Ctx {
   DevPool pool;
 
   DstPlan px, py;
-  DstLaunch lx, ly_none, ly_diag, ly_pred;
+  DstLaunch lx, ly_none;
+  DstLaunch lx_small;              // x passes over a few rows (latency-bound)
 
-  // spectral tables (myfft.F90:125-148), each (n-1)(m-1)
-  double* laminv = nullptr;        // 1/lam/normalize
-  double* lam1i_n = nullptr;       // lam1i(:,:,1)/normalize (ainv)
-  std::vector<double*> lam1, lam1i;
-  std::vector<double> vfac, con1, con2;
+  // per-mode tridiagonal operators replacing the y-direction spectral solves
+  TriOp tri_ctci, tri_ainv;
+  std::vector<TriOp> tri_pred;     // per level
+  TriLaunch tl;
+  std::vector<double> vfac, con1, con2, cvis;   // cvis = dt/(2 Delta_k^2 Re)
 
   // state per level
   std::vector<double*> omega, s, qx, qy, q0x, q0y, rhs_old;
   // Schur-operator scratch per level
   std::vector<double*> mv_w, mv_s, mv_qx, mv_qy;
+  // row treatments of the Schur operator's partial transforms (per vertex row)
+  unsigned char *rm_top = nullptr, *rm_coarse = nullptr, *rm_fine = nullptr, *rm_ring2 = nullptr;
+  double* wmat = nullptr;          // DST-I matrix of the x transform ((m-1) x (m-1))
+  int2* ring_pts = nullptr;        // (row, col) points get_bc reads
+  int n_ring_pts = 0;
+  int* edge_rows = nullptr;        // rows 0 and n-2 (apply_bc's bottom and top rows)
+  double* specY = nullptr;         // ainv's mode-space solution inside the Schur operator
   // work arrays
   double *spec1 = nullptr, *spec2 = nullptr, *rhs = nullptr, *rhsbc = nullptr;
   double *nlx = nullptr, *nly = nullptr, *hx = nullptr, *hy = nullptr, *vort = nullptr;
@@ -65,6 +74,14 @@ struct Ctx {
   TorsState ts{};
   double* err_fsi = nullptr;       // [0] max |dtheta|, [1..nt] per body
   GmresDev G{};
+  // the whole Krylov solve as one CUDA graph: while(restart cycles){ matvec; start;
+  // while(Arnoldi){ matvec; arnoldi } update } on the fixed buffers gm_b (rhs), gm_x (solution)
+  double *gm_b = nullptr, *gm_x = nullptr;
+  bool use_graph = true;
+  bool graph_failed = false;
+  cudaGraphExec_t solve_exec = nullptr;
+  cudaGraph_t solve_graph = nullptr;
+  long long kernels_per_matvec = 0;
   double* cholM = nullptr;         // nf x nf (num_stat)
   bool chol_ready = false;
 
@@ -112,6 +129,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
 int op_schur(Ctx* c, const double* x, double* y, bool with_b);
 int op_redistribute(Ctx* c, const double* f, double* frdst);
 int op_reg_prep(Ctx* c);
+int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms);
 int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason);
 int op_advance(Ctx* c);
 int check_err(Ctx* c);

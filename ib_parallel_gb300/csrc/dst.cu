@@ -55,6 +55,34 @@ void dst_plan_destroy(DstPlan* p) {
   p->tw = p->uw = nullptr; p->sn = nullptr;
 }
 
+struct DstDev {
+  int N, M, P, nrad;
+  int rad[kMaxRadices];
+  FastDiv fd_nb[kMaxRadices];   // butterflies per line of each stage (P/R)
+  FastDiv fd_ns[kMaxRadices];   // span of each stage (product of the earlier radices)
+  FastDiv fd_N, fd_P, fd_H;     // line length, complex length, half of it
+  const double2* tw;
+  const double2* uw;
+  const double* sn;
+};
+
+static DstDev to_dev(const DstPlan& p) {
+  DstDev d;
+  d.N = p.N; d.M = p.M; d.P = p.P; d.nrad = p.nrad;
+  int Ns = 1;
+  for (int i = 0; i < kMaxRadices; ++i) {
+    d.rad[i] = p.rad[i];
+    if (i < p.nrad) {
+      d.fd_nb[i] = FastDiv(p.P / p.rad[i]);
+      d.fd_ns[i] = FastDiv(Ns);
+      Ns *= p.rad[i];
+    }
+  }
+  d.fd_N = FastDiv(p.N); d.fd_P = FastDiv(p.P); d.fd_H = FastDiv(p.P / 2);
+  d.tw = p.tw; d.uw = p.uw; d.sn = p.sn;
+  return d;
+}
+
 // ------------------------------------------------------- device helpers
 __device__ __forceinline__ double2 cmul(double2 a, double2 w) {
   return make_double2(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
@@ -115,17 +143,18 @@ template <> struct Dft<5> {
 // One Stockham stage over B lines (line b at in + b*P).
 template <int R>
 __device__ __forceinline__ void stockham_stage(const double2* __restrict__ in, double2* __restrict__ out,
-                                               int P, int Ns, const double2* __restrict__ tw, int B,
-                                               int tid, int NT) {
-  const int nb = P / R;
+                                               int P, const FastDiv& fnb, const FastDiv& fns,
+                                               const double2* __restrict__ tw, int B, int tid, int NT) {
+  const int nb = fnb.d, Ns = fns.d;
   const int total = B * nb;
   const int twstep = P / (Ns * R);
   for (int it = tid; it < total; it += NT) {
-    int b = it / nb;
+    int b = fnb.div(it);
     int j = it - b * nb;
     const double2* src = in + b * P;
     double2* dst = out + b * P;
-    int k = j % Ns;
+    int jq = fns.div(j);
+    int k = j - jq * Ns;
     double2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
@@ -134,26 +163,10 @@ __device__ __forceinline__ void stockham_stage(const double2* __restrict__ in, d
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * twstep]));
     }
     Dft<R>::run(v);
-    int idxD = (j / Ns) * Ns * R + k;
+    int idxD = jq * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[idxD + r * Ns] = v[r];
   }
-}
-
-struct DstDev {
-  int N, M, P, nrad;
-  int rad[kMaxRadices];
-  const double2* tw;
-  const double2* uw;
-  const double* sn;
-};
-
-static DstDev to_dev(const DstPlan& p) {
-  DstDev d;
-  d.N = p.N; d.M = p.M; d.P = p.P; d.nrad = p.nrad;
-  for (int i = 0; i < kMaxRadices; ++i) d.rad[i] = p.rad[i];
-  d.tw = p.tw; d.uw = p.uw; d.sn = p.sn;
-  return d;
 }
 
 // Transform B lines in place: line b holds x_1..x_N at xb[b*ldx + 0..N-1] and
@@ -163,7 +176,7 @@ __device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2*
   const int P = pl.P, M = pl.M;
   // --- pre-processing: y (length M, real) written into zA viewed as doubles
   for (int it = tid; it < B * P; it += NT) {
-    int b = it / P;
+    int b = pl.fd_P.div(it);
     int t = it - b * P;
     const double* x = xb + b * ldx;
     double* y = reinterpret_cast<double*>(zA + b * P);
@@ -184,23 +197,21 @@ __device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2*
   // --- complex FFT of length P (Stockham, ping-pong zA <-> zB)
   double2* cur = zA;
   double2* nxt = zB;
-  int Ns = 1;
   for (int s = 0; s < pl.nrad; ++s) {
     int R = pl.rad[s];
     switch (R) {
-      case 2: stockham_stage<2>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
-      case 3: stockham_stage<3>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
-      case 4: stockham_stage<4>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
-      default: stockham_stage<5>(cur, nxt, P, Ns, pl.tw, B, tid, NT); break;
+      case 2: stockham_stage<2>(cur, nxt, P, pl.fd_nb[s], pl.fd_ns[s], pl.tw, B, tid, NT); break;
+      case 3: stockham_stage<3>(cur, nxt, P, pl.fd_nb[s], pl.fd_ns[s], pl.tw, B, tid, NT); break;
+      case 4: stockham_stage<4>(cur, nxt, P, pl.fd_nb[s], pl.fd_ns[s], pl.tw, B, tid, NT); break;
+      default: stockham_stage<5>(cur, nxt, P, pl.fd_nb[s], pl.fd_ns[s], pl.tw, B, tid, NT); break;
     }
-    Ns *= R;
     __syncthreads();
     double2* t = cur; cur = nxt; nxt = t;
   }
   // --- unpack the real FFT: even outputs directly, odd increments in place
   const int H = P / 2;
   for (int it = tid; it < B * H; it += NT) {
-    int b = it / H;
+    int b = pl.fd_H.div(it);
     int k = it - b * H;
     const double2* Z = cur + b * P;
     double* o = xb + b * ldx;
@@ -248,88 +259,204 @@ __device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2*
 
 // ------------------------------------------------------------- x pass
 template <int PRE>
+__device__ __forceinline__ double x_load(const DstXArgs& a, const GridDims& g, int row, int j, int nrows, int N,
+                                         int ld) {
+  size_t idx = (size_t)row * ld + j;
+  double v = 0.0;
+  if (PRE == PRE_COPY) {
+    v = a.in[idx];
+  } else if (PRE == PRE_COMBINE) {
+    v = fma(a.cb, a.in2[idx], a.ca * a.in[idx]) + a.in3[idx];
+  } else if (PRE == PRE_PRED) {
+    // con1 rhs + con2 rhs_old + rhsbc + (w - c L w)/normalize, L the 5-point
+    // Laplacian with zero boundary: alpha = (1-4c)/normalize, beta = c/normalize
+    double base = fma(a.cb, a.in2[idx], a.ca * a.in[idx]) + a.in3[idx];
+    const double* w = a.in4;
+    double nb = 0.0;
+    if (j > 0) nb += w[idx - 1];
+    if (j < N - 1) nb += w[idx + 1];
+    if (row > 0) nb += w[idx - ld];
+    if (row < nrows - 1) nb += w[idx + ld];
+    v = fma(a.beta, nb, fma(a.alpha, w[idx], base));
+  } else {
+    // apply_bc (operators_fluid.F90:539-549): left, right, bottom, top; a null input is zero
+    v = a.in ? a.in[idx] : 0.0;
+    int I = j + 2, J = row + 2;
+    if (I == 2) v = v + a.fac * a.ring[g.left + J - 1];
+    if (I == g.m) v = v + a.fac * a.ring[g.right + J - 1];
+    if (J == 2) v = v + a.fac * a.ring[g.bottom + I - 1];
+    if (J == g.n) v = v + a.fac * a.ring[g.top + I - 1];
+  }
+  return v;
+}
+
+template <int PRE>
 __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, DstXArgs a, GridDims g, int B) {
   extern __shared__ double2 smem2[];
+  __shared__ int s_mode[64];
+  __shared__ int s_any;
   const int ldx = pl.M;
   double* xb = reinterpret_cast<double*>(smem2);
   double2* zA = smem2 + (B * ldx) / 2;
   double2* zB = zA + B * pl.P;
   const int N = pl.N;
-  const int row0 = blockIdx.x * B;
-  for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
-    int b = it / N, j = it - b * N;
-    int row = row0 + b;
-    double v = 0.0;
-    if (row < nrows) {
-      size_t idx = (size_t)row * ld + j;
-      if (PRE == PRE_COPY) {
-        v = a.in[idx];
-      } else if (PRE == PRE_COMBINE) {
-        v = fma(a.cb, a.in2[idx], a.ca * a.in[idx]) + a.in3[idx];
-      } else {
-        // apply_bc (operators_fluid.F90:539-549): left, right, bottom, top
-        v = a.in[idx];
-        int I = j + 2, J = row + 2;
-        if (I == 2) v = v + a.fac * a.ring[g.left + J - 1];
-        if (I == g.m) v = v + a.fac * a.ring[g.right + J - 1];
-        if (J == 2) v = v + a.fac * a.ring[g.bottom + I - 1];
-        if (J == g.n) v = v + a.fac * a.ring[g.top + I - 1];
-      }
-    }
-    xb[b * ldx + j] = v;
+  const int line0 = blockIdx.x * B;
+  const int nl = a.nlines ? a.nlines : nrows;
+  __shared__ int s_row[64];
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  if (threadIdx.x < B) {
+    int line = line0 + threadIdx.x;
+    int row = a.nlines ? a.row0 + line * a.row_step : line;
+    s_row[threadIdx.x] = row;
+    int mode = ROW_FFT;
+    if (line >= nl || row >= nrows) mode = ROW_SKIP;
+    else if (a.rowrange) mode = (row >= a.rowrange[0] && row < a.rowrange[1]) ? ROW_FFT : a.rowrange[2];
+    else if (a.rowmode) mode = a.rowmode[row];
+    s_mode[threadIdx.x] = mode;
+    if (mode == ROW_FFT) atomicOr(&s_any, 1);
   }
   __syncthreads();
-  dst_lines(pl, B, xb, ldx, zA, zB);
+  const bool any_fft = s_any != 0;
+  if (any_fft) {
+    // 4 independent loads in flight per thread before the shared-memory stores
+    const int tot = B * N, nt = blockDim.x;
+    for (int it0 = threadIdx.x; it0 < tot; it0 += 4 * nt) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        int it = it0 + u * nt;
+        v[u] = 0.0;
+        if (it < tot) {
+          int b = pl.fd_N.div(it), j = it - b * N;
+          if (s_mode[b] == ROW_FFT) v[u] = x_load<PRE>(a, g, s_row[b], j, nrows, N, ld);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        int it = it0 + u * nt;
+        if (it < tot) {
+          int b = pl.fd_N.div(it), j = it - b * N;
+          xb[b * ldx + j] = v[u];
+        }
+      }
+    }
+    __syncthreads();
+    dst_lines(pl, B, xb, ldx, zA, zB);
+  }
   for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
-    int b = it / N, j = it - b * N;
-    int row = row0 + b;
-    if (row < nrows) a.out[(size_t)row * ld + j] = xb[b * ldx + j];
+    int b = pl.fd_N.div(it), j = it - b * N;
+    int row = s_row[b];
+    int mode = s_mode[b];
+    if (mode == ROW_SKIP) continue;
+    size_t o = (size_t)row * ld + j;
+    double v;
+    if (mode == ROW_FFT) {
+      v = xb[b * ldx + j];
+    } else if (mode == ROW_EDGES) {
+      double x1 = x_load<PRE>(a, g, row, 0, nrows, N, ld);
+      double xn = x_load<PRE>(a, g, row, N - 1, nrows, N, ld);
+      int k = j + 1;
+      double sk = __ldg(&pl.sn[k <= pl.P ? k : pl.M - k]);
+      v = 2.0 * sk * ((k & 1) ? x1 + xn : x1 - xn);
+    } else {
+      v = 0.0;
+    }
+    if (a.post_add) v = fma(a.post_scale, a.post_add[o], v);
+    a.out[o] = v;
   }
 }
 
+// Selected points of an inverse x transform, one warp per point.
+__global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, const int2* __restrict__ pts, int npts,
+                             const double* __restrict__ W, double* __restrict__ out) {
+  int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (gw >= npts) return;
+  int2 rc = pts[gw];
+  const double* sr = spec + (size_t)rc.x * ld;
+  const double* wc = W + (size_t)rc.y * N;
+  double acc = 0.0;
+  for (int k = lane; k < N; k += 32) acc = fma(sr[k], wc[k], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) out[(size_t)rc.x * ld + rc.y] = acc;
+}
+
+// Rows of the forward x transform of an apply_bc boundary field, one warp per output.
+__global__ void k_dst_ring_rows(int N, GridDims g, const double* __restrict__ ring, const int* __restrict__ rows,
+                                int nrows, const double* __restrict__ W, const double* __restrict__ post_add,
+                                double post_scale, double* __restrict__ out) {
+  int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (gw >= nrows * N) return;
+  int r = rows[gw / N], k = gw % N;
+  int J = r + 2;
+  const double* wk = W + (size_t)k * N;
+  double acc = 0.0;
+  for (int j = lane; j < N; j += 32) {
+    int I = j + 2;
+    double v = 0.0;
+    if (I == 2) v = v + ring[g.left + J - 1];
+    if (I == g.m) v = v + ring[g.right + J - 1];
+    if (J == 2) v = v + ring[g.bottom + I - 1];
+    if (J == g.n) v = v + ring[g.top + I - 1];
+    acc = fma(v, wk[j], acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    size_t o = (size_t)r * g.nsx + k;
+    out[o] = post_add ? fma(post_scale, post_add[o], acc) : acc;
+  }
+}
+
+int dst_matrix_table(const DstPlan& px, double* dev_out) {
+  const long double PI_L = 3.141592653589793238462643383279502884L;
+  const int N = px.N, M = px.M;
+  std::vector<double> w((size_t)N * N);
+  for (int j = 1; j <= N; ++j)
+    for (int k = 1; k <= N; ++k) {
+      long long num = (long long)j * k % (2LL * M);
+      w[(size_t)(j - 1) * N + (k - 1)] = (double)(2.0L * sinl(PI_L * (long double)num / (long double)M));
+    }
+  IB_CUDA_CHECK(cudaMemcpy(dev_out, w.data(), 8 * w.size(), cudaMemcpyHostToDevice));
+  return IB_OK;
+}
+
+int dst_x_points(const DstPlan& px, const double* spec, int ld, const int2* pts, int npts, const double* W,
+                 double* out, cudaStream_t st) {
+  if (npts <= 0) return IB_OK;
+  count_launch();
+  k_dst_points<<<cdiv(32LL * npts, 256), 256, 0, st>>>(px.N, spec, ld, pts, npts, W, out);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, const int* rows, int nrows,
+                    const double* W, const double* post_add, double post_scale, double* out, cudaStream_t st) {
+  if (nrows <= 0) return IB_OK;
+  count_launch();
+  k_dst_ring_rows<<<cdiv(32LL * nrows * px.N, 256), 256, 0, st>>>(px.N, g, ring, rows, nrows, W, post_add,
+                                                                   post_scale, out);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
 // ------------------------------------------------------------- y pass
-template <int MODE>
 __global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, DstYArgs a, int B) {
   extern __shared__ double2 smem2[];
   const int ldx = pl.M;
   const int N = pl.N;
   double* xa = reinterpret_cast<double*>(smem2);
-  double* xbb = xa + B * ldx;
-  double2* zA = reinterpret_cast<double2*>(MODE == YMODE_PRED ? xbb + B * ldx : xbb);
+  double2* zA = reinterpret_cast<double2*>(xa + B * ldx);
   double2* zB = zA + B * pl.P;
   const int col0 = blockIdx.x * B;
   for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
     int j = it / B, b = it - j * B;
     int col = col0 + b;
-    double v = 0.0, w = 0.0;
-    if (col < ncols) {
-      size_t idx = (size_t)j * ld + col;
-      v = a.a[idx];
-      if (MODE == YMODE_PRED) w = a.b[idx];
-    }
-    xa[b * ldx + j] = v;
-    if (MODE == YMODE_PRED) xbb[b * ldx + j] = w;
+    xa[b * ldx + j] = col < ncols ? a.a[(size_t)j * ld + col] : 0.0;
   }
   __syncthreads();
   dst_lines(pl, B, xa, ldx, zA, zB);
-  if (MODE == YMODE_PRED) dst_lines(pl, B, xbb, ldx, zA, zB);
-  if (MODE != YMODE_NONE) {
-    for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
-      int j = it / B, b = it - j * B;
-      int col = col0 + b;
-      if (col < ncols) {
-        size_t idx = (size_t)j * ld + col;
-        if (MODE == YMODE_DIAG) {
-          xa[b * ldx + j] = a.t1[idx] * xa[b * ldx + j];
-        } else {
-          // lam1i * (dst(rhs) + lam1 * dst(omega))   (operators_fluid.F90:657-661)
-          xa[b * ldx + j] = a.t1[idx] * fma(a.t2[idx], xbb[b * ldx + j], xa[b * ldx + j]);
-        }
-      }
-    }
-    __syncthreads();
-    dst_lines(pl, B, xa, ldx, zA, zB);
-  }
   for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
     int j = it / B, b = it - j * B;
     int col = col0 + b;
@@ -338,9 +465,7 @@ __global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, Dst
 }
 
 size_t dst_smem_x(const DstPlan& p, int B) { return (size_t)B * p.M * 8 * 3; }
-size_t dst_smem_y(const DstPlan& p, int B, DstYMode mode) {
-  return (size_t)B * p.M * 8 * (mode == YMODE_PRED ? 4 : 3);
-}
+size_t dst_smem_y(const DstPlan& p, int B, DstYMode) { return (size_t)B * p.M * 8 * 3; }
 
 template <typename K>
 static int launch_cfg(K kern, size_t smem) {
@@ -356,7 +481,7 @@ int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs&
                const DstLaunch& L, cudaStream_t st) {
   DstDev d = to_dev(px);
   size_t smem = dst_smem_x(px, L.B);
-  dim3 grid(cdiv(nrows, L.B));
+  dim3 grid(cdiv(a.nlines ? a.nlines : nrows, L.B));
   int rc = IB_OK;
   switch (pre) {
     case PRE_COPY:
@@ -371,6 +496,12 @@ int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs&
       count_launch();
       k_dst_x<PRE_COMBINE><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
       break;
+    case PRE_PRED:
+      rc = launch_cfg(k_dst_x<PRE_PRED>, smem);
+      if (rc) return rc;
+      count_launch();
+      k_dst_x<PRE_PRED><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      break;
     default:
       rc = launch_cfg(k_dst_x<PRE_APPLYBC>, smem);
       if (rc) return rc;
@@ -382,32 +513,15 @@ int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs&
   return IB_OK;
 }
 
-int dst_pass_y(const DstPlan& py, int ncols, int ld, DstYMode mode, const DstYArgs& a, const DstLaunch& L,
+int dst_pass_y(const DstPlan& py, int ncols, int ld, DstYMode, const DstYArgs& a, const DstLaunch& L,
                cudaStream_t st) {
   DstDev d = to_dev(py);
-  size_t smem = dst_smem_y(py, L.B, mode);
+  size_t smem = dst_smem_y(py, L.B, YMODE_NONE);
   dim3 grid(cdiv(ncols, L.B));
-  int rc = IB_OK;
-  switch (mode) {
-    case YMODE_NONE:
-      rc = launch_cfg(k_dst_y<YMODE_NONE>, smem);
-      if (rc) return rc;
-      count_launch();
-      k_dst_y<YMODE_NONE><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
-      break;
-    case YMODE_DIAG:
-      rc = launch_cfg(k_dst_y<YMODE_DIAG>, smem);
-      if (rc) return rc;
-      count_launch();
-      k_dst_y<YMODE_DIAG><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
-      break;
-    default:
-      rc = launch_cfg(k_dst_y<YMODE_PRED>, smem);
-      if (rc) return rc;
-      count_launch();
-      k_dst_y<YMODE_PRED><<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
-      break;
-  }
+  int rc = launch_cfg(k_dst_y, smem);
+  if (rc) return rc;
+  count_launch();
+  k_dst_y<<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -36,34 +36,59 @@ struct DstLaunch {
 int dst_plan_create(DstPlan* p, int N);   // N = M-1, M divisible by 4, M = 2^a 3^b 5^c
 void dst_plan_destroy(DstPlan* p);
 
-enum DstPre { PRE_COPY = 0, PRE_COMBINE = 1, PRE_APPLYBC = 2 };
-enum DstYMode { YMODE_NONE = 0, YMODE_DIAG = 1, YMODE_PRED = 2 };
+enum DstPre { PRE_COPY = 0, PRE_COMBINE = 1, PRE_APPLYBC = 2, PRE_PRED = 3 };
+enum DstYMode { YMODE_NONE = 0 };
 
 struct DstXArgs {
   const double* in = nullptr;    // nlines rows, row pitch ld
   const double* in2 = nullptr;   // PRE_COMBINE second operand
   const double* in3 = nullptr;   // PRE_COMBINE third operand
+  const double* in4 = nullptr;   // PRE_PRED vorticity
   double ca = 1.0, cb = 0.0;     // PRE_COMBINE: ca*in + cb*in2 + in3
+  double alpha = 0.0, beta = 0.0;  // PRE_PRED: + alpha*w + beta*(sum of the 4 neighbours of w)
   const double* ring = nullptr;  // PRE_APPLYBC boundary ring
   double fac = 1.0;              // PRE_APPLYBC factor
   double* out = nullptr;         // nlines rows, pitch ld
+  // optional output post-op: out = DST(row) + post_scale * post_add
+  const double* post_add = nullptr;
+  double post_scale = 0.0;
+  // optional per-row treatment (ROW_*); rows not listed are transformed
+  const unsigned char* rowmode = nullptr;
+  // optional device range [rr[0], rr[1]) of transformed rows; others get mode rr[2]
+  const int* rowrange = nullptr;
+  // optional strided row subset: line i is row row0 + i*row_step, i < nlines (0: all rows)
+  int nlines = 0, row0 = 0, row_step = 0;
 };
 
+// Per-row treatment in the x pass.  ROW_EDGES: the row (after the pre-op) is zero
+// except its first and last samples, whose transform is closed form:
+// Y_k = 2 sin(pi k/M) (x_1 + (-1)^(k+1) x_N).
+enum RowMode { ROW_ZERO = 0, ROW_FFT = 1, ROW_EDGES = 2, ROW_SKIP = 3 };
+
 struct DstYArgs {
-  double* a = nullptr;           // spectral buffer (in/out), rows of pitch ld
-  const double* b = nullptr;     // YMODE_PRED second input
-  const double* t1 = nullptr;    // DIAG table, or PRED lam1i
-  const double* t2 = nullptr;    // PRED lam1
+  double* a = nullptr;           // field (in/out), rows of pitch ld
 };
 
 // x direction: lines are the (n-1) rows of an (n-1)x(m-1) field, N = m-1.
 int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs& a,
                const GridDims& g, const DstLaunch& L, cudaStream_t st);
-// y direction: lines are the (m-1) columns, N = n-1, optional spectral combine.
+// y direction: lines are the (m-1) columns, N = n-1 (the plain 2-D DST only).
 int dst_pass_y(const DstPlan& py, int ncols, int ld, DstYMode mode, const DstYArgs& a,
                const DstLaunch& L, cudaStream_t st);
 
 size_t dst_smem_x(const DstPlan& p, int B);
+
+// The DST-I matrix of the x transform, W[j][k] = 2 sin(pi (j+1)(k+1)/M), N x N (symmetric).
+int dst_matrix_table(const DstPlan& px, double* dev_out);
+// Selected points of an inverse x transform: out[r*ld + c] = sum_k spec[r*ld + k] W[c][k]
+// for each (r, c) in pts (device int2 array), one warp per point.
+int dst_x_points(const DstPlan& px, const double* spec, int ld, const int2* pts, int npts, const double* W,
+                 double* out, cudaStream_t st);
+// Selected rows of a forward x transform of an apply_bc boundary field (a zero field with the
+// ring added as operators_fluid.F90:539-549 does): out[r*ld + k] = post_scale*post_add[r*ld+k]
+// + sum_j bc(r, j) W[j][k] for rows r in rows[0..nrows), one warp per output.
+int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, const int* rows, int nrows,
+                    const double* W, const double* post_add, double post_scale, double* out, cudaStream_t st);
 size_t dst_smem_y(const DstPlan& p, int B, DstYMode mode);
 
 }  // namespace ib

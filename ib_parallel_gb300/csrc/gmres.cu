@@ -28,13 +28,13 @@ __device__ double blk_sum(double v, double* red) {
 
 __global__ void k_gmres_init(GmresDev G) {
   if (threadIdx.x == 0) {
-    G.ist[0] = 0; G.ist[1] = 0; G.ist[2] = 0; G.ist[3] = 0;
+    G.ist[0] = 0; G.ist[1] = 0; G.ist[2] = 0; G.ist[3] = 0; G.ist[4] = 0;
   }
 }
 
 // Cycle start: r = b - A x (A x in G.Av), V0 = r/||r||, tolerance on the first cycle.
 __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const double* __restrict__ x, double rtol,
-                              double atol, int max_it) {
+                              double atol, int max_it, cudaGraphConditionalHandle h_inner, int use_cond) {
   __shared__ double red[33];
   const int nf = G.nf;
   double pr = 0.0, pb = 0.0;
@@ -73,31 +73,36 @@ __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const do
     else if (its >= max_it) reason = -3;
     G.ist[1] = reason;
     G.ist[3] = reason == 0 ? 1 : 0;
+    G.ist[4] += 1;  // restart cycles
+    if (use_cond) cudaGraphSetConditional(h_inner, reason == 0 ? 1u : 0u);
   }
 }
 
-// One Arnoldi step on w = A V[it] (in G.Av).
-__global__ void k_gmres_arnoldi(GmresDev G, int max_it) {
+// One Arnoldi step on w = A V[it] (in G.Av): classical Gram-Schmidt (all projections
+// against the unmodified w, one warp per projection), normalisation, Givens update.
+__global__ void k_gmres_arnoldi(GmresDev G, int max_it, cudaGraphConditionalHandle h_inner, int use_cond) {
   __shared__ double red[33];
   __shared__ double h[64];
-  if (G.ist[3] == 0) return;
+  if (G.ist[3] == 0) {
+    if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(h_inner, 0u);
+    return;
+  }
   const int nf = G.nf, R = G.restart;
   const int it = G.ist[2];
   double* w = G.V + (size_t)(it + 1) * nf;
-  for (int i = threadIdx.x; i < nf; i += blockDim.x) w[i] = G.Av[i];
-  __syncthreads();
-  // classical Gram-Schmidt: all projections against the unmodified w
-  for (int j = 0; j <= it; ++j) {
+  const double* Av = G.Av;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int j = warp; j <= it; j += nwarps) {
     const double* vj = G.V + (size_t)j * nf;
     double p = 0.0;
-    for (int i = threadIdx.x; i < nf; i += blockDim.x) p += w[i] * vj[i];
-    double s = blk_sum(p, red);
-    if (threadIdx.x == 0) h[j] = s;
+    for (int i = lane; i < nf; i += 32) p += Av[i] * vj[i];
+    for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+    if (lane == 0) h[j] = p;
   }
   __syncthreads();
   double pn = 0.0;
   for (int i = threadIdx.x; i < nf; i += blockDim.x) {
-    double v = w[i];
+    double v = Av[i];
     for (int j = 0; j <= it; ++j) v = v - h[j] * G.V[(size_t)j * nf + i];
     w[i] = v;
     pn += v * v;
@@ -149,12 +154,15 @@ __global__ void k_gmres_arnoldi(GmresDev G, int max_it) {
       else if (hapend) reason = -3;
     }
     G.ist[1] = reason;
-    G.ist[3] = (reason == 0 && itn < R && its < max_it) ? 1 : 0;
+    int active = (reason == 0 && itn < R && its < max_it) ? 1 : 0;
+    G.ist[3] = active;
+    if (use_cond) cudaGraphSetConditional(h_inner, (unsigned)active);
   }
 }
 
 // KSPGMRESBuildSoln: back substitution and x += V y.
-__global__ void k_gmres_update(GmresDev G, double* __restrict__ x) {
+__global__ void k_gmres_update(GmresDev G, double* __restrict__ x, int max_it, cudaGraphConditionalHandle h_outer,
+                               int use_cond) {
   __shared__ double y[64];
   const int nf = G.nf, R = G.restart;
   const int it = G.ist[2];
@@ -177,6 +185,15 @@ __global__ void k_gmres_update(GmresDev G, double* __restrict__ x) {
       x[i] = x[i] + u;
     }
   }
+  if (threadIdx.x == 0) {
+    G.ist[3] = 0;
+    if (use_cond) cudaGraphSetConditional(h_outer, (G.ist[1] == 0 && G.ist[0] < max_it) ? 1u : 0u);
+  }
+}
+
+__global__ void k_copy(int n, const double* __restrict__ a, double* __restrict__ b) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
 }
 
 int launch_gmres_init(const GmresDev& G, cudaStream_t st) {
@@ -186,21 +203,30 @@ int launch_gmres_init(const GmresDev& G, cudaStream_t st) {
   return IB_OK;
 }
 int launch_gmres_start(const GmresDev& G, const double* b, const double* x, double rtol, double atol, int max_it,
-                       cudaStream_t st) {
+                       cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) {
   count_launch();
-  k_gmres_start<<<1, kGmresThreads, 0, st>>>(G, b, x, rtol, atol, max_it);
+  k_gmres_start<<<1, kGmresThreads, 0, st>>>(G, b, x, rtol, atol, max_it, h, use_cond);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
-int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st) {
+int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st, cudaGraphConditionalHandle h,
+                         int use_cond) {
   count_launch();
-  k_gmres_arnoldi<<<1, kGmresThreads, 0, st>>>(G, max_it);
+  k_gmres_arnoldi<<<1, kGmresThreads, 0, st>>>(G, max_it, h, use_cond);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
-int launch_gmres_update(const GmresDev& G, double* x, cudaStream_t st) {
+int launch_gmres_update(const GmresDev& G, double* x, int max_it, cudaStream_t st, cudaGraphConditionalHandle h,
+                        int use_cond) {
   count_launch();
-  k_gmres_update<<<1, kGmresThreads, 0, st>>>(G, x);
+  k_gmres_update<<<1, kGmresThreads, 0, st>>>(G, x, max_it, h, use_cond);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+int launch_copy(int n, const double* a, double* b, cudaStream_t st) {
+  if (n <= 0) return IB_OK;
+  count_launch();
+  k_copy<<<cdiv(n, 256), 256, 0, st>>>(n, a, b);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

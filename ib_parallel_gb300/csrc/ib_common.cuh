@@ -60,9 +60,27 @@ __device__ __forceinline__ double ghost_vertex(const double* __restrict__ f,
 
 inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Division of a non-negative int by a runtime divisor d >= 1 with a multiply-high and a
+// shift (Granlund-Montgomery): q = (umulhi(n, mul) + n) >> shr, exact for n < 2^31.
+struct FastDiv {
+  unsigned mul = 0, shr = 0;
+  int d = 1;
+  __host__ __device__ FastDiv() {}
+  __host__ FastDiv(int dd) : d(dd) {
+    unsigned l = 0;
+    while ((1u << l) < (unsigned)dd) ++l;
+    unsigned long long m = (((1ull << 32) * ((1ull << l) - (unsigned long long)dd)) / (unsigned long long)dd) + 1ull;
+    mul = (unsigned)m;
+    shr = l;
+  }
+  __device__ __forceinline__ int div(int n) const { return (int)((__umulhi((unsigned)n, mul) + (unsigned)n) >> shr); }
+  __device__ __forceinline__ int mod(int n) const { return n - div(n) * d; }
+};
+
 // Number of kernels this library has launched (all contexts), for the benchmark's
 // launch count.  Defined in solver.cu.
 void count_launch();
+void count_launches(long long n);
 long long launch_count();
 
 }  // namespace ib

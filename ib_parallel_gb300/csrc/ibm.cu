@@ -81,8 +81,10 @@ __global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb,
     for (int p = 0; p < 7; ++p) wk[l * 7 + p] = d * d * dx[p] * dy[l];
 }
 
-// Bounding box of all stencils (one CTA).
-__global__ void k_reg_bbox(int nf, const int* __restrict__ ix, const int* __restrict__ iy, int* bbox) {
+// Bounding box of all stencils (one CTA).  bbox[0..3] = i0, j0, ni, nj of the face box;
+// bbox[4..6] and bbox[7..9] = [first, last+1) vertex row (0-based) that rot(E^T f) can touch
+// and that E(curl s) reads, followed by the treatment of the other rows (zero / skip).
+__global__ void k_reg_bbox(GridDims g, int nf, const int* __restrict__ ix, const int* __restrict__ iy, int* bbox) {
   __shared__ int s[4][32];
   int imin = 1 << 30, jmin = 1 << 30, imax = -(1 << 30), jmax = -(1 << 30);
   for (int k = threadIdx.x; k < nf; k += blockDim.x) {
@@ -109,6 +111,9 @@ __global__ void k_reg_bbox(int nf, const int* __restrict__ ix, const int* __rest
     bbox[1] = jmin - 3;
     bbox[2] = imax - imin + 7;
     bbox[3] = jmax - jmin + 7;
+    int rlo = max(0, jmin - 5), rhi = min(g.nsy - 1, jmax + 2) + 1;
+    bbox[4] = rlo; bbox[5] = rhi; bbox[6] = 0;   // ROW_ZERO
+    bbox[7] = rlo; bbox[8] = rhi; bbox[9] = 3;   // ROW_SKIP
   }
 }
 
@@ -171,7 +176,7 @@ int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* 
   count_launch();
   k_reg_weights<<<cdiv(nf, 128), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w, d_err);
   count_launch();
-  k_reg_bbox<<<1, 256, 0, st>>>(nf, r.ix, r.iy, r.bbox);
+  k_reg_bbox<<<1, 256, 0, st>>>(g, nf, r.ix, r.iy, r.bbox);
   count_launch();
   k_reg_lists<false><<<152 * 2, 128, 0, st>>>(nf, r.comp, r.ix, r.iy, r.bbox, r.cnt_x, r.cnt_y, nullptr,
                                               nullptr, r.max_faces);
@@ -224,12 +229,15 @@ int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, dou
   return IB_OK;
 }
 
-// E q: h0_out[k] = h0_in[k] + sum_slots w * q(face)  (sequential in slot order)
+// E q: h0_out[k] = h0_in[k] + sum_slots w * q(face).  One warp per unknown: the 49 slot
+// products are summed by a warp tree, then added to h0_in (fsinterface.F90:51-80 sums the
+// slots one by one; the difference is round-off).
 __global__ void k_regT(GridDims g, int nf, const double* __restrict__ qx, const double* __restrict__ qx0,
                        const double* __restrict__ qy, const double* __restrict__ qy0, const int* __restrict__ comp,
                        const int* __restrict__ ix, const int* __restrict__ iy, const double* __restrict__ w,
                        const double* __restrict__ h0_in, double* h0_out) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
   if (k >= nf) return;
   bool isx = comp[k] == 1;
   const double* q = isx ? qx : qy;
@@ -238,29 +246,60 @@ __global__ void k_regT(GridDims g, int nf, const double* __restrict__ qx, const 
   int ny = isx ? g.nuy : g.nvy;
   int cx = ix[k], cy = iy[k];
   const double* wk = w + (size_t)k * 49;
-  double vals[49];
-#pragma unroll
-  for (int l = 0; l < 7; ++l)
-#pragma unroll
-    for (int p = 0; p < 7; ++p) {
-      int fi = cx + p - 3, fj = cy + l - 3;
-      // stencil faces outside the grid (flagged as IB_ERR_DOMAIN) contribute nothing
-      bool in = fi >= 1 && fi <= ld && fj >= 1 && fj <= ny;
-      int idx = in ? (fj - 1) * ld + (fi - 1) : 0;
+  double acc = 0.0;
+  for (int sl = lane; sl < 49; sl += 32) {
+    int fi = cx + sl % 7 - 3, fj = cy + sl / 7 - 3;
+    // stencil faces outside the grid (flagged as IB_ERR_DOMAIN) contribute nothing
+    if (fi >= 1 && fi <= ld && fj >= 1 && fj <= ny) {
+      int idx = (fj - 1) * ld + (fi - 1);
       double v = q0 ? q[idx] + q0[idx] : q[idx];
-      vals[l * 7 + p] = in ? v : 0.0;
+      acc = fma(wk[sl], v, acc);
     }
-  double acc = h0_in ? h0_in[k] : 0.0;
-#pragma unroll
-  for (int s = 0; s < 49; ++s) acc = acc + wk[s] * vals[s];
-  h0_out[k] = acc;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) h0_out[k] = (h0_in ? h0_in[k] : 0.0) + acc;
 }
 
 int launch_regT(const GridDims& g, int nf, const double* qx, const double* qx0, const double* qy, const double* qy0,
                 const RegDev& r, const double* h0_in, double* h0_out, cudaStream_t st) {
   if (nf == 0) return IB_OK;
   count_launch();
-  k_regT<<<cdiv(nf, 64), 64, 0, st>>>(g, nf, qx, qx0, qy, qy0, r.comp, r.ix, r.iy, r.w, h0_in, h0_out);
+  k_regT<<<cdiv(32LL * nf, 128), 128, 0, st>>>(g, nf, qx, qx0, qy, qy0, r.comp, r.ix, r.iy, r.w, h0_in, h0_out);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+// E curl(s): h0_out[k] = h0_in[k] + sum_slots w * q(face), with q = curl(s) evaluated at the
+// stencil faces (operators_fluid.F90:423-471 fused into fsinterface.F90:51-80); s ghosts
+// come from the ring.
+__global__ void k_regT_s(GridDims g, int nf, const double* __restrict__ s, const double* __restrict__ ring,
+                         const int* __restrict__ comp, const int* __restrict__ ix, const int* __restrict__ iy,
+                         const double* __restrict__ w, const double* __restrict__ h0_in, double* h0_out) {
+  int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (k >= nf) return;
+  bool isx = comp[k] == 1;
+  int nxf = isx ? g.nux : g.nvx, nyf = isx ? g.nuy : g.nvy;
+  int cx = ix[k], cy = iy[k];
+  const double* wk = w + (size_t)k * 49;
+  double acc = 0.0;
+  for (int sl = lane; sl < 49; sl += 32) {
+    int fi = cx + sl % 7 - 3, fj = cy + sl / 7 - 3;
+    if (fi >= 1 && fi <= nxf && fj >= 1 && fj <= nyf) {
+      double q = isx ? ghost_vertex(s, ring, g, fi, fj + 1) - ghost_vertex(s, ring, g, fi, fj)
+                     : ghost_vertex(s, ring, g, fi, fj) - ghost_vertex(s, ring, g, fi + 1, fj);
+      acc = fma(wk[sl], q, acc);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) h0_out[k] = (h0_in ? h0_in[k] : 0.0) + acc;
+}
+
+int launch_regT_s(const GridDims& g, int nf, const double* s, const double* ring, const RegDev& r,
+                  const double* h0_in, double* h0_out, cudaStream_t st) {
+  if (nf == 0) return IB_OK;
+  count_launch();
+  k_regT_s<<<cdiv(32LL * nf, 128), 128, 0, st>>>(g, nf, s, ring, r.comp, r.ix, r.iy, r.w, h0_in, h0_out);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -25,7 +25,7 @@ struct RegDev {
   int* iy;
   double* w;        // nf*49, slot = (l+3)*7 + (p+3)
   // face-major contribution lists over the stencil bounding box, per component
-  int* bbox;        // [0..3] = i0, j0, ni, nj (same box for u- and v-faces)
+  int* bbox;        // [0..3] = i0, j0, ni, nj (same box for u- and v-faces); [4..9] row ranges
   int* cnt_x;       // bbox faces + 1 (exclusive offsets after the scan)
   int* cnt_y;
   int* lst_x;       // contributions: k*49 + slot, ascending k per face
@@ -42,6 +42,9 @@ int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, dou
 // h0 (+)= E q   (accumulate=1 keeps the incoming h0, fsinterface.F90:51-80)
 int launch_regT(const GridDims& g, int nf, const double* qx, const double* qx0, const double* qy,
                 const double* qy0, const RegDev& r, const double* h0_in, double* h0_out, cudaStream_t st);
+// h0_out = h0_in + E curl(s) with s ghosts from the ring (curl fused into regT)
+int launch_regT_s(const GridDims& g, int nf, const double* s, const double* ring, const RegDev& r,
+                  const double* h0_in, double* h0_out, cudaStream_t st);
 // finter = E^T f / E^T 1 on faces with weight > 1e-10 (operators_struct.F90:810-834)
 int launch_redistribute_field(const GridDims& g, int nf, const double* f, const RegDev& r, double* fx,
                               double* fy, cudaStream_t st);
@@ -75,15 +78,20 @@ struct GmresDev {
   double* sn;
   double* g;       // restart+1
   double* scal;    // [0]=ttol [1]=res [2]=bnorm [3]=rnorm
-  int* ist;        // [0]=its [1]=reason [2]=it (inner) [3]=active
+  int* ist;        // [0]=its [1]=reason [2]=it (inner) [3]=active [4]=restart cycles
   double* xin;     // matvec input
   double* Av;      // matvec output
 };
 int launch_gmres_init(const GmresDev& G, cudaStream_t st);
+// The optional graph conditional handle is set by the kernel when use_cond != 0: start
+// and arnoldi set the inner (Arnoldi) loop condition, update the outer (restart) one.
 int launch_gmres_start(const GmresDev& G, const double* b, const double* x, double rtol, double atol, int max_it,
-                       cudaStream_t st);
-int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st);
-int launch_gmres_update(const GmresDev& G, double* x, cudaStream_t st);
+                       cudaStream_t st, cudaGraphConditionalHandle h = 0, int use_cond = 0);
+int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st, cudaGraphConditionalHandle h = 0,
+                         int use_cond = 0);
+int launch_gmres_update(const GmresDev& G, double* x, int max_it, cudaStream_t st, cudaGraphConditionalHandle h = 0,
+                        int use_cond = 0);
+int launch_copy(int n, const double* a, double* b, cudaStream_t st);
 
 // dense symmetric positive definite solve (stationary-body path)
 int launch_cholesky(int n, double* A, int* d_err, cudaStream_t st);

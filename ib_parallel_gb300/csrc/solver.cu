@@ -19,6 +19,7 @@ static const double kPi = 4.0 * std::atan(1.0);  // parameters.F90:61
 
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 ProfScope::ProfScope(Ctx* cc, int kind, double bytes) : c(cc) {
@@ -36,32 +37,27 @@ ProfScope::~ProfScope() {
 // algorithmic DRAM bytes of one pass: each input field read once, the output written once
 static double pass_bytes(const Ctx* c, int nin, int nout) { return 8.0 * c->g.ns * (nin + nout); }
 
-// ------------------------------------------------------------- DST tuning
-static int time_pass(Ctx* c, int which, const DstLaunch& L, float* ms) {
+// ------------------------------------------------------------- tuning
+template <typename F>
+static int time_it(Ctx* c, F run, float* ms) {
   cudaEvent_t e0, e1;
   IB_CUDA_CHECK(cudaEventCreate(&e0));
   IB_CUDA_CHECK(cudaEventCreate(&e1));
-  auto run = [&]() -> int {
-    if (which == 0) {
-      DstXArgs a; a.in = c->spec2; a.out = c->spec1;
-      return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, a, c->g, L, c->st);
-    }
-    DstYArgs a; a.a = c->spec1; a.b = c->spec2; a.t1 = c->laminv; a.t2 = c->laminv;
-    DstYMode m = which == 1 ? YMODE_DIAG : (which == 2 ? YMODE_PRED : YMODE_NONE);
-    return dst_pass_y(c->py, c->g.nsx, c->g.nsx, m, a, L, c->st);
-  };
-  RC(run());
-  IB_CUDA_CHECK(cudaEventRecord(e0, c->st));
-  for (int r = 0; r < 3; ++r) RC(run());
-  IB_CUDA_CHECK(cudaEventRecord(e1, c->st));
-  IB_CUDA_CHECK(cudaEventSynchronize(e1));
-  IB_CUDA_CHECK(cudaEventElapsedTime(ms, e0, e1));
+  int rc = run();
+  if (rc == IB_OK) {
+    cudaEventRecord(e0, c->st);
+    for (int r = 0; r < 3 && rc == IB_OK; ++r) rc = run();
+    cudaEventRecord(e1, c->st);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  return IB_OK;
+  return rc;
 }
 
-static int tune_dst(Ctx* c) {
+// Launch shapes of the x pass, the y pass and the tridiagonal solve, chosen by timing.
+static int tune(Ctx* c) {
   int dev = 0, smem_max = 0;
   IB_CUDA_CHECK(cudaGetDevice(&dev));
   IB_CUDA_CHECK(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -69,26 +65,47 @@ static int tune_dst(Ctx* c) {
   IB_CUDA_CHECK(cudaMemsetAsync(c->spec2, 0, sizeof(double) * c->g.ns, c->st));
   const int Bs[] = {1, 2, 3, 4, 5, 6, 8, 10, 12, 16};
   const int NTs[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 512};
-  DstLaunch* outs[4] = {&c->lx, &c->ly_diag, &c->ly_pred, &c->ly_none};
-  for (int which = 0; which < 4; ++which) {
-    const DstPlan& pl = which == 0 ? c->px : c->py;
+  for (int which = 0; which < 3; ++which) {
+    const DstPlan& pl = which != 1 ? c->px : c->py;
+    DstLaunch* out = which == 0 ? &c->lx : (which == 1 ? &c->ly_none : &c->lx_small);
+    int nlines = which == 0 ? c->g.nsy : (which == 1 ? c->g.nsx : std::min(32, c->g.nsy));
     float best = 1e30f;
-    DstLaunch bestL = *outs[which];
+    DstLaunch bestL = *out;
     for (int B : Bs) {
-      size_t smem = which == 0 ? dst_smem_x(pl, B)
-                               : dst_smem_y(pl, B, which == 2 ? YMODE_PRED : YMODE_DIAG);
-      if ((long long)smem > smem_max) continue;
-      int nlines = which == 0 ? c->g.nsy : c->g.nsx;
-      if (B > nlines) continue;
+      size_t smem = which != 1 ? dst_smem_x(pl, B) : dst_smem_y(pl, B, YMODE_NONE);
+      if ((long long)smem > smem_max || B > nlines) continue;
       for (int NT : NTs) {
-        if (NT > 32 * B * 8) continue;  // more than 8 warps per line never helps
+        if (NT > 32 * B * 8) continue;
         DstLaunch L; L.B = B; L.NT = NT;
         float ms = 0;
-        if (time_pass(c, which, L, &ms) != IB_OK) { cudaGetLastError(); continue; }
+        auto run = [&]() -> int {
+          if (which != 1) {
+            DstXArgs a; a.in = c->spec2; a.out = c->spec1;
+            if (which == 2) { a.nlines = nlines; a.row0 = 0; a.row_step = 1; }
+            return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, a, c->g, L, c->st);
+          }
+          DstYArgs a; a.a = c->spec1;
+          return dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_NONE, a, L, c->st);
+        };
+        if (time_it(c, run, &ms) != IB_OK) { cudaGetLastError(); continue; }
         if (ms < best) { best = ms; bestL = L; }
       }
     }
-    *outs[which] = bestL;
+    *out = bestL;
+  }
+  {
+    float best = 1e30f;
+    TriLaunch bestT = c->tl;
+    for (int Mb : {1, 2, 4, 8, 16, 32}) {
+      if (Mb * c->tri_ctci.C > 1024 || (long long)tri_smem(c->tri_ctci, Mb) > smem_max) continue;
+      if ((Mb * c->tri_ctci.C) % 32 != 0 && Mb * c->tri_ctci.C > 32) continue;  // whole warps only
+      TriLaunch T; T.Mb = Mb;
+      float ms = 0;
+      auto run = [&]() -> int { return tri_solve(c->tri_ctci, c->spec1, c->spec1, c->g.nsx, T, c->st); };
+      if (time_it(c, run, &ms) != IB_OK) { cudaGetLastError(); continue; }
+      if (ms < best) { best = ms; bestT = T; }
+    }
+    c->tl = bestT;
   }
   return IB_OK;
 }
@@ -171,15 +188,20 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   size_t dbl = 0;
   dbl += (size_t)L * (3 * ns + 2 * nu + 2 * nv);         // state
   dbl += (size_t)L * (2 * ns + nu + nv);                 // Schur scratch
-  dbl += (size_t)(2 + 2 * L) * ns;                       // tables
-  dbl += 5 * ns + 2 * nu + 2 * nv;                       // work
+  int tri_s = 0, tri_C = 0;
+  tri_chunking(g.n, &tri_s, &tri_C);
+  size_t tri_n = tri_table_doubles(g.nsx, tri_s, tri_C);
+  dbl += (size_t)(2 + L) * tri_n;                        // tridiagonal tables
+  dbl += 6 * ns + 2 * nu + 2 * nv;                       // work (+ ainv mode-space copy)
+  dbl += (size_t)g.nsx * g.nsx + (size_t)g.nsy;          // DST matrix, row treatments
+  dbl += (size_t)g.m + g.n + 8;                          // get_bc points, edge rows
   dbl += (size_t)(L + 3) * nbc;                          // rings
   dbl += 7 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
   dbl += 6 * (size_t)nt + nt + 1;
-  dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 2 * (size_t)nf;
+  dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 4 * (size_t)nf + 2;
   if (p.num_stat) dbl += (size_t)nf * nf;
   dbl += 8 * stage_n;
-  size_t ints = 2 * (size_t)nf + 2 * (size_t)nf + 4 + 2 * (size_t)max_faces + 2 * 49 * (size_t)nf + 4 + 1;
+  size_t ints = 2 * (size_t)nf + 2 * (size_t)nf + 16 + 2 * (size_t)max_faces + 2 * 49 * (size_t)nf + 4 + 1;
   size_t bytes = dbl * 8 + ints * 4 + (size_t)nt * sizeof(TorsBody) + 256 * 400;
   if (cudaMalloc(&c->pool.base, bytes) != cudaSuccess) {
     *msg = "device allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM;
@@ -194,10 +216,14 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   lv(c->omega, ns); lv(c->s, ns); lv(c->rhs_old, ns);
   lv(c->qx, nu); lv(c->q0x, nu); lv(c->qy, nv); lv(c->q0y, nv);
   lv(c->mv_w, ns); lv(c->mv_s, ns); lv(c->mv_qx, nu); lv(c->mv_qy, nv);
-  c->laminv = P.take<double>(ns); c->lam1i_n = P.take<double>(ns);
-  lv(c->lam1, ns); lv(c->lam1i, ns);
+  double* tri_mem = P.take<double>((2 + L) * tri_n);
   c->spec1 = P.take<double>(ns); c->spec2 = P.take<double>(ns); c->rhs = P.take<double>(ns);
-  c->rhsbc = P.take<double>(ns); c->vort = P.take<double>(ns);
+  c->rhsbc = P.take<double>(ns); c->vort = P.take<double>(ns); c->specY = P.take<double>(ns);
+  c->wmat = P.take<double>((size_t)g.nsx * g.nsx);
+  c->ring_pts = P.take<int2>((size_t)g.m + g.n + 8);
+  c->edge_rows = P.take<int>(2);
+  c->rm_top = P.take<unsigned char>(g.nsy); c->rm_coarse = P.take<unsigned char>(g.nsy);
+  c->rm_fine = P.take<unsigned char>(g.nsy); c->rm_ring2 = P.take<unsigned char>(g.nsy);
   c->nlx = P.take<double>(nu); c->hx = P.take<double>(nu);
   c->nly = P.take<double>(nv); c->hy = P.take<double>(nv);
   lv(c->lastbc, nbc);
@@ -207,7 +233,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->tmpf2 = P.take<double>(nf); c->forces = P.take<double>(2 * nbody + 1);
   c->comp = P.take<int>(nf); c->bid = P.take<int>(nf);
   c->reg.comp = c->comp; c->reg.ix = P.take<int>(nf); c->reg.iy = P.take<int>(nf);
-  c->reg.w = P.take<double>(49 * (size_t)nf); c->reg.bbox = P.take<int>(4);
+  c->reg.w = P.take<double>(49 * (size_t)nf); c->reg.bbox = P.take<int>(16);
   c->reg.cnt_x = P.take<int>(max_faces); c->reg.cnt_y = P.take<int>(max_faces);
   c->reg.lst_x = P.take<int>(49 * (size_t)nf + 1); c->reg.lst_y = P.take<int>(49 * (size_t)nf + 1);
   c->reg.max_faces = max_faces; c->reg.max_list = 49 * nf;
@@ -219,14 +245,15 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->G.nf = nf; c->G.restart = R;
   c->G.V = P.take<double>((size_t)(R + 1) * nf); c->G.H = P.take<double>((size_t)(R + 1) * R);
   c->G.cs = P.take<double>(R + 1); c->G.sn = P.take<double>(R + 1); c->G.g = P.take<double>(R + 1);
-  c->G.scal = P.take<double>(4); c->G.ist = P.take<int>(4);
+  c->G.scal = P.take<double>(4); c->G.ist = P.take<int>(8);
+  c->gm_b = P.take<double>(nf + 1); c->gm_x = P.take<double>(nf + 1);
   c->G.xin = P.take<double>(nf); c->G.Av = P.take<double>(nf);
   if (p.num_stat) c->cholM = P.take<double>((size_t)nf * nf);
   c->d_err = P.take<int>(1);
   c->stage_n = stage_n;
   for (int i = 0; i < 8; ++i) c->stage[i] = P.take<double>(stage_n);
   if (!c->stage[7] || !c->d_err) { *msg = "internal pool overflow"; ctx_destroy(c); return IB_ERR_NOMEM; }
-  if (cudaMallocHost(&c->h_ist, 4 * sizeof(int)) != cudaSuccess ||
+  if (cudaMallocHost(&c->h_ist, 8 * sizeof(int)) != cudaSuccess ||
       cudaMallocHost(&c->h_scal, 4 * sizeof(double)) != cudaSuccess) {
     *msg = "pinned allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM;
   }
@@ -236,34 +263,65 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->prof_bytes.resize(Ctx::kProfMax);
   for (auto& e : c->prof_ev) IB_CUDA_CHECK(cudaEventCreate(&e));
 
-  // spectral tables (myfft.F90:125-148)
+  // spectral operators (myfft.F90:125-148) as per-mode tridiagonal systems
   {
-    std::vector<double> lam(ns), t1(ns), t2(ns);
-    for (int J = 2; J <= g.n; ++J)
-      for (int I = 2; I <= g.m; ++I) {
-        size_t q = (size_t)(J - 2) * g.nsx + (I - 2);
-        lam[q] = -2.0 * (std::cos(kPi * (double)(I - 1) / (double)g.m) + std::cos(kPi * (double)(J - 1) / (double)g.n) - 2.0);
-        t1[q] = 1.0 / lam[q] / c->normalize;
-      }
-    IB_CUDA_CHECK(cudaMemcpy(c->laminv, t1.data(), 8 * ns, cudaMemcpyHostToDevice));
     double del2 = c->delta * c->delta;
+    std::vector<double> lamx(g.nsx), shift(g.nsx);
+    for (int k = 1; k <= g.nsx; ++k) {
+      double sn = std::sin(kPi * (double)k / (2.0 * g.m));
+      lamx[k - 1] = 4.0 * sn * sn;  // 2 - 2 cos(pi k/m) without cancellation
+    }
     for (int k = 1; k <= L; ++k) {
       double del22 = del2 * std::pow(4.0, k - 1);
       c->vfac.push_back(0.5 * p.dt / p.Re / del22 / c->normalize);
       c->con1.push_back(1.5 * p.dt / del22 / c->normalize);
       c->con2.push_back(-0.5 * p.dt / del22 / c->normalize);
-      for (size_t q = 0; q < ns; ++q) {
-        t1[q] = (1.0 - 0.5 * p.dt * lam[q] / del22 / p.Re) / c->normalize;
-        t2[q] = 1.0 / (1.0 + 0.5 * p.dt * lam[q] / del22 / p.Re);
-      }
-      IB_CUDA_CHECK(cudaMemcpy(c->lam1[k - 1], t1.data(), 8 * ns, cudaMemcpyHostToDevice));
-      IB_CUDA_CHECK(cudaMemcpy(c->lam1i[k - 1], t2.data(), 8 * ns, cudaMemcpyHostToDevice));
-      if (k == 1) {
-        for (size_t q = 0; q < ns; ++q) t1[q] = t2[q] / c->normalize;
-        IB_CUDA_CHECK(cudaMemcpy(c->lam1i_n, t1.data(), 8 * ns, cudaMemcpyHostToDevice));
-      }
+      c->cvis.push_back(0.5 * p.dt / del22 / p.Re);
     }
+    int rc2 = tri_build(&c->tri_ctci, g.nsx, g.nsy, lamx.data(), 1.0 / (2.0 * g.m), tri_mem);
+    double c1 = c->cvis[0];
+    for (int k = 0; k < g.nsx; ++k) shift[k] = lamx[k] + 1.0 / c1;
+    if (rc2 == IB_OK) rc2 = tri_build(&c->tri_ainv, g.nsx, g.nsy, shift.data(), 1.0 / (2.0 * g.m * c1), tri_mem + tri_n);
+    c->tri_pred.resize(L);
+    for (int k = 0; k < L && rc2 == IB_OK; ++k) {
+      double ck = c->cvis[k];
+      for (int q = 0; q < g.nsx; ++q) shift[q] = lamx[q] + 1.0 / ck;
+      rc2 = tri_build(&c->tri_pred[k], g.nsx, g.nsy, shift.data(), 2.0 * g.n / ck, tri_mem + (2 + k) * tri_n);
+    }
+    if (rc2 != IB_OK) { *msg = "tridiagonal table upload failed"; ctx_destroy(c); return rc2; }
   }
+  // row treatments of the Schur operator's partial transforms (vertex row r = J-2):
+  // coarsify fills coarse rows J = n/4+2 .. 3n/4; apply_bc fills rows J = 2, n wholly and
+  // the first/last sample of every other row; get_bc reads rows J = n/4+1, 3n/4+1
+  {
+    std::vector<unsigned char> top(g.nsy), coarse(g.nsy), fine(g.nsy), ring2(g.nsy);
+    for (int r = 0; r < g.nsy; ++r) {
+      bool centre = r >= g.n / 4 && r <= 3 * g.n / 4 - 2;
+      bool edge = r == 0 || r == g.nsy - 1;
+      top[r] = centre ? ROW_FFT : ROW_ZERO;
+      coarse[r] = (centre || edge) ? ROW_FFT : ROW_EDGES;
+      fine[r] = edge ? ROW_SKIP : ROW_EDGES;   // the edge rows come from dst_x_ring_rows
+      ring2[r] = (r == g.n / 4 - 1 || r == 3 * g.n / 4 - 1) ? ROW_FFT : ROW_SKIP;
+    }
+    IB_CUDA_CHECK(cudaMemcpy(c->rm_top, top.data(), g.nsy, cudaMemcpyHostToDevice));
+    IB_CUDA_CHECK(cudaMemcpy(c->rm_coarse, coarse.data(), g.nsy, cudaMemcpyHostToDevice));
+    IB_CUDA_CHECK(cudaMemcpy(c->rm_fine, fine.data(), g.nsy, cudaMemcpyHostToDevice));
+    IB_CUDA_CHECK(cudaMemcpy(c->rm_ring2, ring2.data(), g.nsy, cudaMemcpyHostToDevice));
+    // points get_bc reads: rows J = n/4+1, 3n/4+1 at I = m/4+1..3m/4+1 and columns
+    // I = m/4+1, 3m/4+1 at J = n/4+1..3n/4+1 (vertex row r = J-2, column c = I-2)
+    std::vector<int2> pts;
+    for (int r : {g.n / 4 - 1, 3 * g.n / 4 - 1})
+      for (int cc = g.m / 4 - 1; cc <= 3 * g.m / 4 - 1; ++cc) pts.push_back(make_int2(r, cc));
+    for (int cc : {g.m / 4 - 1, 3 * g.m / 4 - 1})
+      for (int r = g.n / 4; r < 3 * g.n / 4 - 1; ++r) pts.push_back(make_int2(r, cc));
+    c->n_ring_pts = (int)pts.size();
+    IB_CUDA_CHECK(cudaMemcpy(c->ring_pts, pts.data(), sizeof(int2) * pts.size(), cudaMemcpyHostToDevice));
+    int er[2] = {0, g.nsy - 1};
+    IB_CUDA_CHECK(cudaMemcpy(c->edge_rows, er, sizeof(er), cudaMemcpyHostToDevice));
+    int rc3 = dst_matrix_table(c->px, c->wmat);
+    if (rc3 != IB_OK) { *msg = "DST matrix upload failed"; ctx_destroy(c); return rc3; }
+  }
+
   // frame fluxes q0 = q0p + q0r (variables.F90:299-360), constant in time
   {
     const double* uv = p.motion;
@@ -295,11 +353,11 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
 
   // default launch shapes, then tuned by timing
   c->lx.B = 2; c->lx.NT = 160;
+  c->lx_small.B = 1; c->lx_small.NT = 128;
   c->ly_none.B = 8; c->ly_none.NT = 160;
-  c->ly_diag.B = 8; c->ly_diag.NT = 160;
-  c->ly_pred.B = 4; c->ly_pred.NT = 160;
+  c->tl.Mb = 8;
   if (p.autotune) {
-    rc = tune_dst(c);
+    rc = tune(c);
     if (rc != IB_OK) { *msg = "DST tuning failed"; ctx_destroy(c); return rc; }
   }
   rc = op_reg_prep(c);
@@ -314,6 +372,8 @@ void ctx_destroy(Ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   dst_plan_destroy(&c->px);
   dst_plan_destroy(&c->py);
+  if (c->solve_exec) cudaGraphExecDestroy(c->solve_exec);
+  if (c->solve_graph) cudaGraphDestroy(c->solve_graph);
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -336,18 +396,17 @@ int check_err(Ctx* c) {
 }
 
 // ------------------------------------------------------------- operators
-static int ctci_like(Ctx* c, const double* in, double* out, const double* ring, const double* table) {
-  DstXArgs a;
-  a.in = in; a.out = c->spec1; a.ring = ring; a.fac = 1.0;
+// x transform -> per-mode tridiagonal solve along y -> x transform
+static int spectral_solve(Ctx* c, DstPre pre, const DstXArgs& a_in, const TriOp& op, double* out) {
+  DstXArgs a = a_in;
+  a.out = c->spec1;
   {
-    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, ring ? PRE_APPLYBC : PRE_COPY, a, c->g, c->lx, c->st));
+    ProfScope ps(c, 0, pass_bytes(c, pre == PRE_PRED ? 4 : 1, 1));
+    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, pre, a, c->g, c->lx, c->st));
   }
-  DstYArgs y;
-  y.a = c->spec1; y.t1 = table;
   {
-    ProfScope ps(c, 1, pass_bytes(c, 2, 1));
-    RC(dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_DIAG, y, c->ly_diag, c->st));
+    ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+    RC(tri_solve(op, c->spec1, c->spec1, c->g.nsx, c->tl, c->st));
   }
   DstXArgs b;
   b.in = c->spec1; b.out = out;
@@ -355,8 +414,19 @@ static int ctci_like(Ctx* c, const double* in, double* out, const double* ring, 
   return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, b, c->g, c->lx, c->st);
 }
 
-int op_ctci(Ctx* c, const double* in, double* out, const double* ring) { return ctci_like(c, in, out, ring, c->laminv); }
-int op_ainv(Ctx* c, const double* in, double* out) { return ctci_like(c, in, out, nullptr, c->lam1i_n); }
+// ctci (myfft.F90:177-188); ring != null applies apply_bc(fac 1) to a copy of the input
+int op_ctci(Ctx* c, const double* in, double* out, const double* ring) {
+  DstXArgs a;
+  a.in = in; a.ring = ring; a.fac = 1.0;
+  return spectral_solve(c, ring ? PRE_APPLYBC : PRE_COPY, a, c->tri_ctci, out);
+}
+
+// ainv (myfft.F90:161-173)
+int op_ainv(Ctx* c, const double* in, double* out) {
+  DstXArgs a;
+  a.in = in;
+  return spectral_solve(c, PRE_COPY, a, c->tri_ainv, out);
+}
 
 int op_dst(Ctx* c, const double* in, double* out) {
   DstXArgs a;
@@ -371,30 +441,17 @@ int op_dst(Ctx* c, const double* in, double* out) {
   return dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_NONE, y, c->ly_none, c->st);
 }
 
-// omega = dst(lam1i*(dst(con1 rhs + con2 rhs_old + rhsbc) + lam1*dst(omega)))  (operators_fluid.F90:649-663)
+// fluid_predictor (operators_fluid.F90:649-663):
+// omega = dst(lam1i*(dst(con1 rhs + con2 rhs_old + rhsbc) + lam1*dst(omega)))
+//       = S_x (2n/c)(1/c + lam_x + T_y)^-1 S_x[con1 rhs + con2 rhs_old + rhsbc + (omega - c L omega)/normalize]
 int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs_old, const double* rhsbc) {
   DstXArgs a;
-  a.in = rhs; a.in2 = rhs_old; a.in3 = rhsbc; a.ca = c->con1[k]; a.cb = c->con2[k]; a.out = c->spec1;
-  {
-    ProfScope ps(c, 0, pass_bytes(c, 3, 1));
-    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COMBINE, a, c->g, c->lx, c->st));
-  }
-  DstXArgs b;
-  b.in = om; b.out = c->spec2;
-  {
-    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-    RC(dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, b, c->g, c->lx, c->st));
-  }
-  DstYArgs y;
-  y.a = c->spec1; y.b = c->spec2; y.t1 = c->lam1i[k]; y.t2 = c->lam1[k];
-  {
-    ProfScope ps(c, 2, pass_bytes(c, 4, 1));
-    RC(dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_PRED, y, c->ly_pred, c->st));
-  }
-  DstXArgs d;
-  d.in = c->spec1; d.out = om;
-  ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-  return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, d, c->g, c->lx, c->st);
+  a.in = rhs; a.in2 = rhs_old; a.in3 = rhsbc; a.in4 = om;
+  a.ca = c->con1[k]; a.cb = c->con2[k];
+  double cv = c->cvis[k];
+  a.alpha = (1.0 - 4.0 * cv) / c->normalize;
+  a.beta = cv / c->normalize;
+  return spectral_solve(c, PRE_PRED, a, c->tri_pred[k], om);
 }
 
 // vort2flux (operators_fluid.F90:237-377).  all_curls=false computes the fluxes
@@ -414,17 +471,89 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
   return IB_OK;
 }
 
-// ab_times / a_times2 (timestepper.F90:774-782, operators_fluid.F90:14-120)
+// s on the next finer level's boundary only: the points get_bc reads, each an inverse x
+// transform evaluated as a dot product (spread over all SMs), then get_bc
+// (operators_fluid.F90:475-535) into the ring.
+static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring) {
+  const GridDims& g = c->g;
+  RC(dst_x_points(c->px, spec, g.nsx, c->ring_pts, c->n_ring_pts, c->wmat, s, c->st));
+  return launch_get_bc(g, s, 1.0, ring, c->st);
+}
+
+// ab_times / a_times2 (timestepper.F90:774-782, operators_fluid.F90:14-120):
+// y = E (vort2flux(ainv(rot(E^T x))))_1 + B x, evaluating only what E reads.
+//  * ainv: x transform of the rows rot(E^T x) can touch, tridiagonal solve (Y), full
+//    inverse transform (the vorticity every coarser level is coarsified from).
+//  * coarse levels: inputs are the coarsified centre rows plus the boundary values of
+//    apply_bc (closed-form transforms); outputs are needed on the finer boundary only.
+//  * finest level: its forward transform is 2m Y plus the boundary terms; its inverse is
+//    needed only on the rows E reads, and curl is fused into E.
 int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
   const GridDims& g = c->g;
+  const int L = c->L;
+  cudaStream_t st = c->st;
   c->n_matvec += 1;
-  RC(launch_reg(g, c->nf, x, c->reg, c->hx, c->hy, c->st));
-  RC(launch_rot(g, c->hx, c->hy, c->mv_w[0], c->st));
-  RC(op_ainv(c, c->mv_w[0], c->mv_w[0]));
-  for (int k = 1; k < c->L; ++k) IB_CUDA_CHECK(cudaMemsetAsync(c->mv_w[k], 0, 8 * (size_t)g.ns, c->st));
-  RC(op_vort2flux(c, c->mv_w.data(), c->mv_s.data(), c->mv_qx.data(), c->mv_qy.data(), false));
-  RC(launch_regT(g, c->nf, c->mv_qx[0], nullptr, c->mv_qy[0], nullptr, c->reg, nullptr, y, c->st));
-  if (with_b) RC(launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, x, y, c->st));
+  RC(launch_reg(g, c->nf, x, c->reg, c->hx, c->hy, st));
+  RC(launch_rot(g, c->hx, c->hy, c->vort, st));
+  {
+    DstXArgs a;
+    a.in = c->vort; a.out = c->specY; a.rowrange = c->reg.bbox + 4;
+    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
+  }
+  {
+    ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+    RC(tri_solve(c->tri_ainv, c->specY, c->specY, g.nsx, c->tl, st));
+  }
+  {
+    DstXArgs a;
+    a.in = c->specY; a.out = c->mv_w[0];
+    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
+  }
+  const double* ring0 = c->zero_ring;
+  if (L > 1) {
+    // outside their centres the coarse vorticities of the operator stay zero
+    for (int k = 1; k < L; ++k) RC(launch_coarsify(g, c->mv_w[k - 1], c->mv_w[k], st));
+    for (int k = L - 1; k >= 1; --k) {
+      DstXArgs a;
+      a.in = c->mv_w[k]; a.out = c->spec1;
+      a.ring = c->sbc; a.fac = 1.0;
+      a.rowmode = k == L - 1 ? c->rm_top : c->rm_coarse;
+      {
+        ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+        RC(dst_pass_x(c->px, g.nsy, g.nsx, k == L - 1 ? PRE_COPY : PRE_APPLYBC, a, g, c->lx, st));
+      }
+      {
+        ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+        RC(tri_solve(c->tri_ctci, c->spec1, c->spec1, g.nsx, c->tl, st));
+      }
+      RC(ring_from_modes(c, c->spec1, c->mv_s[k], c->sbc));
+    }
+    ring0 = c->sbc;
+  }
+  {
+    // S_x(vort1 + apply_bc(ring0)) = 2m Y + transform of the boundary terms: the two full
+    // boundary rows by dot products, the others in closed form (two nonzero samples)
+    RC(dst_x_ring_rows(c->px, g, ring0, c->edge_rows, 2, c->wmat, c->specY, 2.0 * g.m, c->spec1, st));
+    DstXArgs a;
+    a.in = nullptr; a.ring = ring0; a.fac = 1.0; a.out = c->spec1; a.rowmode = c->rm_fine;
+    a.post_add = c->specY; a.post_scale = 2.0 * g.m;
+    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_APPLYBC, a, g, c->lx, st));
+  }
+  {
+    ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+    RC(tri_solve(c->tri_ctci, c->spec1, c->spec1, g.nsx, c->tl, st));
+  }
+  {
+    DstXArgs a;
+    a.in = c->spec1; a.out = c->mv_s[0]; a.rowrange = c->reg.bbox + 7;
+    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
+  }
+  RC(launch_regT_s(g, c->nf, c->mv_s[0], ring0, c->reg, nullptr, y, st));
+  if (with_b) RC(launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, x, y, st));
   return IB_OK;
 }
 
@@ -433,20 +562,152 @@ int op_redistribute(Ctx* c, const double* f, double* frdst) {
   return launch_regT(c->g, c->nf, c->nlx, nullptr, c->nly, nullptr, c->reg, nullptr, frdst, c->st);
 }
 
+// Device time of `reps` back-to-back launches of one full pass over the finest grid
+// (kind 0: x pass, 1: tridiagonal solve), for the roofline of a kernel timed alone.
+int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms) {
+  cudaStream_t st = c->st;
+  auto run = [&]() -> int {
+    if (kind == 0) {
+      DstXArgs a; a.in = c->spec2; a.out = c->spec1;
+      return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, a, c->g, c->lx, st);
+    }
+    return tri_solve(c->tri_ctci, c->spec1, c->spec1, c->g.nsx, c->tl, st);
+  };
+  RC(run());
+  cudaEvent_t e0, e1;
+  IB_CUDA_CHECK(cudaEventCreate(&e0));
+  IB_CUDA_CHECK(cudaEventCreate(&e1));
+  IB_CUDA_CHECK(cudaEventRecord(e0, st));
+  for (int r = 0; r < reps; ++r) RC(run());
+  IB_CUDA_CHECK(cudaEventRecord(e1, st));
+  IB_CUDA_CHECK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *avg_ms = ms / reps;
+  return IB_OK;
+}
+
 int op_reg_prep(Ctx* c) {
   return launch_reg_build(c->g, c->nf, c->xb, c->yb, c->delta, c->p.offsetx, c->p.offsety, c->reg, c->d_err, c->st);
 }
 
 static int read_ist(Ctx* c) {
-  IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->G.ist, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->G.ist, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
   IB_CUDA_CHECK(cudaStreamSynchronize(c->st));
   return IB_OK;
+}
+
+// Adds a conditional (while) node after the current capture position of `st` and
+// returns its body graph.
+static int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body) {
+  cudaStreamCaptureStatus stat;
+  cudaGraph_t capg;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  IB_CUDA_CHECK(cudaStreamGetCaptureInfo(st, &stat, nullptr, &capg, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams pr = {};
+  pr.type = cudaGraphNodeTypeConditional;
+  pr.conditional.handle = h;
+  pr.conditional.type = cudaGraphCondTypeWhile;
+  pr.conditional.size = 1;
+  cudaGraphNode_t node;
+  IB_CUDA_CHECK(cudaGraphAddNode(&node, capg, deps, nullptr, ndeps, &pr));
+  IB_CUDA_CHECK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  *body = pr.conditional.phGraph_out[0];
+  return IB_OK;
+}
+
+static cudaGraph_t capture_graph(cudaStream_t st) {
+  cudaStreamCaptureStatus stat;
+  cudaGraph_t g = nullptr;
+  cudaStreamGetCaptureInfo(st, &stat, nullptr, &g, nullptr, nullptr, nullptr);
+  return g;
+}
+
+// Builds the graph of a whole GMRES solve (KSPSolve, timestepper.F90:363-366) on gm_b/gm_x.
+static int build_solve_graph(Ctx* c) {
+  const GmresDev& G = c->G;
+  const int max_it = c->p.gmres_max_it;
+  const double rtol = c->p.rtol, atol = c->p.atol;
+  cudaStream_t st = c->st, s1 = nullptr, s2 = nullptr;
+  IB_CUDA_CHECK(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+  IB_CUDA_CHECK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+  const bool prof = c->prof_on;
+  c->prof_on = false;
+  int rc = IB_OK;
+  cudaGraph_t graph = nullptr;
+  do {
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
+    rc = launch_gmres_init(G, st);
+    cudaGraphConditionalHandle h_out = 0, h_in = 0;
+    cudaGraph_t outer = nullptr, inner = nullptr;
+    if (rc == IB_OK && cudaGraphConditionalHandleCreate(&h_out, capture_graph(st), 1, cudaGraphCondAssignDefault) != cudaSuccess)
+      rc = IB_ERR_CUDA;
+    if (rc == IB_OK) rc = add_while(st, h_out, &outer);
+    // restart cycle: r = b - A x, V0, then the Arnoldi loop, then x += V y
+    if (rc == IB_OK && cudaStreamBeginCaptureToGraph(s1, outer, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+      rc = IB_ERR_CUDA;
+    if (rc == IB_OK && cudaGraphConditionalHandleCreate(&h_in, outer, 0, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+    if (rc == IB_OK) {
+      c->st = s1;
+      rc = launch_copy(c->nf, c->gm_x, G.xin, s1);
+      long long l0 = launch_count();
+      if (rc == IB_OK) rc = op_schur(c, G.xin, G.Av, true);
+      c->kernels_per_matvec = launch_count() - l0;
+      c->n_matvec -= 1;  // capture only
+      if (rc == IB_OK) rc = launch_gmres_start(G, c->gm_b, c->gm_x, rtol, atol, max_it, s1, h_in, 1);
+      if (rc == IB_OK) rc = add_while(s1, h_in, &inner);
+      if (rc == IB_OK && cudaStreamBeginCaptureToGraph(s2, inner, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        rc = IB_ERR_CUDA;
+      if (rc == IB_OK) {
+        c->st = s2;
+        rc = op_schur(c, G.xin, G.Av, true);
+        c->n_matvec -= 1;
+        if (rc == IB_OK) rc = launch_gmres_arnoldi(G, max_it, s2, h_in, 1);
+        cudaGraph_t tmp;
+        if (cudaStreamEndCapture(s2, &tmp) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+      }
+      c->st = s1;
+      if (rc == IB_OK) rc = launch_gmres_update(G, c->gm_x, max_it, s1, h_out, 1);
+      cudaGraph_t tmp;
+      if (cudaStreamEndCapture(s1, &tmp) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+    }
+    c->st = st;
+    if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+    if (rc == IB_OK && cudaGraphInstantiate(&c->solve_exec, graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+  } while (false);
+  c->st = st;
+  c->prof_on = prof;
+  cudaGetLastError();
+  if (rc == IB_OK) c->solve_graph = graph;
+  else if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(s1);
+  cudaStreamDestroy(s2);
+  return rc;
 }
 
 // KSPSolve with KSPGMRES (timestepper.F90:363-366); x is the initial guess.
 int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason) {
   const GmresDev& G = c->G;
   const int max_it = c->p.gmres_max_it;
+  if (c->use_graph && !c->prof_on && !c->graph_failed) {
+    if (!c->solve_exec && build_solve_graph(c) != IB_OK) c->graph_failed = true;
+    if (c->solve_exec) {
+      if (b != c->gm_b) IB_CUDA_CHECK(cudaMemcpyAsync(c->gm_b, b, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
+      if (x != c->gm_x) IB_CUDA_CHECK(cudaMemcpyAsync(c->gm_x, x, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
+      IB_CUDA_CHECK(cudaGraphLaunch(c->solve_exec, c->st));
+      if (x != c->gm_x) IB_CUDA_CHECK(cudaMemcpyAsync(x, c->gm_x, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
+      RC(read_ist(c));
+      long long it = c->h_ist[0], cycles = c->h_ist[4];
+      c->n_matvec += it + cycles;
+      count_launches((it + cycles) * c->kernels_per_matvec + it + 3 * cycles + 1);
+      *its = (int)it;
+      *reason = c->h_ist[1];
+      return IB_OK;
+    }
+  }
   RC(launch_gmres_init(G, c->st));
   for (;;) {
     IB_CUDA_CHECK(cudaMemcpyAsync(G.xin, x, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
@@ -460,7 +721,8 @@ int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason) {
       RC(read_ist(c));
       if (!c->h_ist[3]) break;
     }
-    RC(launch_gmres_update(G, x, c->st));
+    RC(launch_gmres_update(G, x, max_it, c->st));
+    RC(read_ist(c));
     if (c->h_ist[1] != 0 || c->h_ist[0] >= max_it) break;
   }
   *its = c->h_ist[0];

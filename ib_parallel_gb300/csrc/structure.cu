@@ -8,10 +8,10 @@
 namespace ib {
 
 // BR_build (operators_struct.F90:319-338): x-rows (j-1) ds sin(g0-th),
-// y-rows -(j-1) ds cos(g0-th).
-__device__ __forceinline__ double br_val(const TorsBody& b, double th, int j) {
-  if (j < b.npts) return (double)j * b.deltas * sin(b.gamma0 - th);
-  return -(double)(j - b.npts) * b.deltas * cos(b.gamma0 - th);
+// y-rows -(j-1) ds cos(g0-th).  sn, cs = sin, cos(g0-th), evaluated once per body.
+__device__ __forceinline__ double br_val(const TorsBody& b, double sn, double cs, int j) {
+  if (j < b.npts) return (double)j * b.deltas * sn;
+  return -(double)(j - b.npts) * b.deltas * cs;
 }
 
 __device__ double block_sum(double v) {
@@ -41,12 +41,13 @@ __global__ void k_tors_btimes(const TorsBody* __restrict__ tb, TorsState s, doub
                               const double* __restrict__ x, double* __restrict__ y) {
   TorsBody b = tb[blockIdx.x];
   double th = s.theta[blockIdx.x];
+  double sn = sin(b.gamma0 - th), cs = cos(b.gamma0 - th);
   double part = 0.0;
-  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, th, j) * x[b.off + j];
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn, cs, j) * x[b.off + j];
   double dot = block_sum(part);
   double scale = (delta * delta / b.deltas / dt) * (2.0 * b.deltas / dt);
   double c = dot / keff(b, dt) * scale;
-  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = y[b.off + j] + br_val(b, th, j) * c;
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = y[b.off + j] + br_val(b, sn, cs, j) * c;
 }
 
 // compute_rhs (operators_struct.F90:342-398): y = BR * delta*(r_theta - J r_phi - thetad)
@@ -61,7 +62,8 @@ __global__ void k_tors_rhs(const TorsBody* __restrict__ tb, TorsState s, double 
               (I * (4.0 / (dt * dt) * th0 + 4.0 / dt * thd0 + thdd0) + C * (thd0 + 2.0 / dt * th0) -
                (4.0 / (dt * dt) * I + 2.0 / dt * C + K) * th);
   double c = delta * (rth - jr - thd);
-  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = br_val(b, th, j) * c;
+  double sn = sin(b.gamma0 - th), cs = cos(b.gamma0 - th);
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = br_val(b, sn, cs, j) * c;
 }
 
 // compute_dx + update_xb (operators_struct.F90:402-505, 600-620); err = max |dtheta|
@@ -72,8 +74,9 @@ __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double d
   TorsBody b = tb[t];
   double th = s.theta[t], th0 = s.theta0[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
   double I = b.itheta, C = b.ctheta, K = b.ktheta;
+  double sn0 = sin(b.gamma0 - th), cs0 = cos(b.gamma0 - th);
   double part = 0.0;
-  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, th, j) * f[b.off + j];
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn0, cs0, j) * f[b.off + j];
   double brf = block_sum(part);
   double jr = 1.0 / (4.0 / (dt * dt) * I + 2.0 / dt * C + K) *
               (I * (4.0 / (dt * dt) * th0 + 4.0 / dt * thd0 + thdd0) + C * (thd0 + 2.0 / dt * th0) -
@@ -110,8 +113,9 @@ __global__ void k_tors_initial_acc(const TorsBody* __restrict__ tb, TorsState s,
   int t = blockIdx.x;
   TorsBody b = tb[t];
   double th = s.theta[t];
+  double sn = sin(b.gamma0 - th), cs = cos(b.gamma0 - th);
   double part = 0.0;
-  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, th, j) * f[b.off + j];
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn, cs, j) * f[b.off + j];
   double brf = block_sum(part);
   brf = brf * delta / b.deltas / dt;
   if (threadIdx.x == 0) {

@@ -1,0 +1,51 @@
+// Per-mode tridiagonal solves that replace the y-direction DST pairs of the
+// spectral solves in myfft.F90 (ctci, ainv) and operators_fluid.F90
+// (fluid_predictor).
+//
+// With S_y the DST-I along y (S_y S_y = 2n I) and T_y = tridiag(-1, 2, -1) the
+// 1-D Dirichlet Laplacian, S_y diag(f(lam_y)) S_y = 2n f(T_y).  So each 2-D
+// spectral solve
+//     S_x S_y [ g(lam_x + lam_y) (.) S_y S_x v ]
+// is an x transform, one tridiagonal solve per x mode k, and an x transform:
+//     ctci:  (1/2m) (lam_x(k) + T_y)^-1
+//     ainv:  (1/(2m c1)) (1/c1 + lam_x(k) + T_y)^-1
+//     predictor (level k): (2n/c) (1/c + lam_x(k) + T_y)^-1 applied to
+//            S_x[ con1 rhs + con2 rhs_old + rhsbc + (omega - c L omega)/normalize ]
+// where c = dt/(2 Delta_k^2 Re) and L the 5-point Laplacian with zero boundary.
+//
+// Every system is tridiag(-1, a_k, -1) of size n-1.  For parallelism it is cut
+// into C chunks of s = n/C - 1 rows separated by C-1 interface rows: each chunk is
+// solved with zero ends (Thomas with tabulated pivots), the interface values then
+// satisfy a constant-coefficient tridiagonal system of size C-1, and each chunk
+// adds the interface responses (tabulated).  5 FP64 operations per point.
+#pragma once
+#include "ib_common.cuh"
+
+namespace ib {
+
+struct TriOp {
+  int nx = 0, ny = 0;     // modes (m-1), rows (n-1)
+  int s = 0, C = 0;       // chunk rows, chunks: (s+1)*C = ny+1
+  double sigma = 1.0;     // right-hand-side scale
+  double* inv = nullptr;  // s x nx: 1/pivot
+  double* sinv = nullptr; // s x nx: sigma/pivot
+  double* gL = nullptr;   // s x nx: chunk response to a unit left end value
+  double* inv2 = nullptr; // (C-1) x nx: reduced-system 1/pivot
+  double* e2 = nullptr;   // (C-1) x nx: reduced-system B/pivot
+};
+
+struct TriLaunch {
+  int Mb = 8;             // modes per CTA
+};
+
+// Chunking for ny = n-1 rows (n divisible by 4): C*(s+1) = n.
+void tri_chunking(int n, int* s, int* C);
+// Tables for shifts a_k = 2 + shift_k (k = 0..nx-1), uploaded into caller-provided
+// device memory of tri_table_doubles() doubles.
+size_t tri_table_doubles(int nx, int s, int C);
+int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, double* dev_mem);
+// In place (F may equal U): U = sigma * A^-1 F for every mode column.
+int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaunch& L, cudaStream_t st);
+size_t tri_smem(const TriOp& op, int Mb);
+
+}  // namespace ib

@@ -38,7 +38,7 @@ EXPORTS = [
     "ib_vort2flux", "ib_reg_prep", "ib_reg", "ib_regT", "ib_redistribute", "ib_schur_apply",
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
-    "ib_launch_count", "ib_probe_throughput",
+    "ib_launch_count", "ib_probe_throughput", "ib_time_pass",
 ]
 
 
@@ -103,6 +103,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_measure_fp64_peak": ([D], C.c_int),
         "ib_launch_count": ([], C.c_longlong),
         "ib_probe_throughput": ([C.c_int, D], C.c_int),
+        "ib_time_pass": ([P, C.c_int, C.c_int, D], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -287,6 +288,12 @@ class Simulation:
         s = C.c_void_p()
         _check(self.lib.ib_get_stream(self.h, C.byref(s)), "ib_get_stream")
         return s.value or 0
+
+    def time_pass(self, kind: int, reps: int = 20) -> float:
+        """Average device ms of one full x pass (0) or tridiagonal solve (1) timed alone."""
+        ms = C.c_double()
+        _check(self.lib.ib_time_pass(self.h, kind, reps, C.byref(ms)), "ib_time_pass")
+        return ms.value
 
     def profile(self, enable: bool):
         _check(self.lib.ib_profile(self.h, int(bool(enable))), "ib_profile")

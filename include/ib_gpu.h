@@ -139,6 +139,9 @@ int ib_schur_solve(IbCtx* ctx, const double* rhs, double* f, int* iterations);
 /* ---- instrumentation (no counterpart in the reference) ---- */
 /* the cudaStream_t every kernel of this context runs on */
 int ib_get_stream(IbCtx* ctx, void** stream);
+/* average device time (ms) of `reps` back-to-back launches of one full pass over the finest
+ * grid: kind 0 the DST-I x pass, 1 the per-mode tridiagonal solve (scratch buffers only) */
+int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);
 /* enable (1) / disable (0) CUDA-event timing of each DST pass launch; enabling clears the totals */
 int ib_profile(IbCtx* ctx, int enable);
 /* work done since creation: Schur matvecs and DST passes by kind (0..3, see below) */
