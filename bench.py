@@ -333,6 +333,7 @@ def run_gpu(args, world, rank, local):
                           "frac": fp_achieved / fp64_peak, "flops_per_launch": flops_x,
                           "peak_source": "of measured FP64 FMA loop on this GPU (ib_measure_fp64_peak)"},
         "tridiagonal_pass_us": 1e3 * t_tri,
+        "schur_stages_us": sim.profile_schur(20),
     }
     result["gpu_launches"] = launches_timed
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -493,6 +493,12 @@ int ib_time_pass(IbCtx* h, int kind, int reps, double* avg_ms) {
   return op_result(ib::op_time_pass(c, kind, reps, avg_ms), "time_pass failed");
 }
 
+int ib_profile_schur(IbCtx* h, int reps, double* stage_ms) {
+  CTX_OR_FAIL(h);
+  if (!stage_ms || reps <= 0) return fail(IB_ERR_ARG, "bad argument");
+  return op_result(ib::op_profile_schur(c, reps, stage_ms), "profile_schur failed");
+}
+
 int ib_profile(IbCtx* h, int enable) {
   CTX_OR_FAIL(h);
   if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "sync failed");

@@ -100,6 +100,12 @@ struct Ctx {
   long long n_matvec = 0;
   long long n_pass[4] = {0, 0, 0, 0};
 
+  // optional stage timing of the Schur operator (ib_profile_schur): events at stage borders
+  static constexpr int kStages = 8;
+  bool stage_on = false;
+  cudaEvent_t stage_ev[kStages + 1] = {};
+  double stage_ms[kStages] = {0};
+
   // optional CUDA-event timing of DST passes (ib_profile)
   static constexpr int kProfMax = 8192;
   bool prof_on = false;
@@ -130,6 +136,7 @@ int op_schur(Ctx* c, const double* x, double* y, bool with_b);
 int op_redistribute(Ctx* c, const double* f, double* frdst);
 int op_reg_prep(Ctx* c);
 int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms);
+int op_profile_schur(Ctx* c, int reps, double* ms);
 int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason);
 int op_advance(Ctx* c);
 int check_err(Ctx* c);

@@ -379,6 +379,8 @@ void ctx_destroy(Ctx* c) {
   if (c->h_scal) cudaFreeHost(c->h_scal);
   for (auto& e : c->prof_ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : c->stage_ev)
+    if (e) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -493,8 +495,11 @@ int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
   const int L = c->L;
   cudaStream_t st = c->st;
   c->n_matvec += 1;
+  auto mark = [&](int i) { if (c->stage_on) cudaEventRecord(c->stage_ev[i], st); };
+  mark(0);
   RC(launch_reg(g, c->nf, x, c->reg, c->hx, c->hy, st));
   RC(launch_rot(g, c->hx, c->hy, c->vort, st));
+  mark(1);
   {
     DstXArgs a;
     a.in = c->vort; a.out = c->specY; a.rowrange = c->reg.bbox + 4;
@@ -511,10 +516,12 @@ int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
   }
+  mark(2);
   const double* ring0 = c->zero_ring;
   if (L > 1) {
     // outside their centres the coarse vorticities of the operator stay zero
     for (int k = 1; k < L; ++k) RC(launch_coarsify(g, c->mv_w[k - 1], c->mv_w[k], st));
+    mark(3);
     for (int k = L - 1; k >= 1; --k) {
       DstXArgs a;
       a.in = c->mv_w[k]; a.out = c->spec1;
@@ -531,7 +538,10 @@ int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
       RC(ring_from_modes(c, c->spec1, c->mv_s[k], c->sbc));
     }
     ring0 = c->sbc;
+  } else {
+    mark(3);
   }
+  mark(4);
   {
     // S_x(vort1 + apply_bc(ring0)) = 2m Y + transform of the boundary terms: the two full
     // boundary rows by dot products, the others in closed form (two nonzero samples)
@@ -542,18 +552,46 @@ int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_APPLYBC, a, g, c->lx, st));
   }
+  mark(5);
   {
     ProfScope ps(c, 1, pass_bytes(c, 1, 1));
     RC(tri_solve(c->tri_ctci, c->spec1, c->spec1, g.nsx, c->tl, st));
   }
+  mark(6);
   {
     DstXArgs a;
     a.in = c->spec1; a.out = c->mv_s[0]; a.rowrange = c->reg.bbox + 7;
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
   }
+  mark(7);
   RC(launch_regT_s(g, c->nf, c->mv_s[0], ring0, c->reg, nullptr, y, st));
   if (with_b) RC(launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, x, y, st));
+  mark(8);
+  return IB_OK;
+}
+
+// Device time of each stage of the Schur operator, summed over `reps` back-to-back
+// applications: 0 reg+rot, 1 ainv, 2 coarsify, 3 coarse levels, 4 finest forward,
+// 5 finest solve, 6 finest inverse rows, 7 E curl + B.
+int op_profile_schur(Ctx* c, int reps, double* ms) {
+  for (int i = 0; i <= Ctx::kStages; ++i)
+    if (!c->stage_ev[i]) IB_CUDA_CHECK(cudaEventCreate(&c->stage_ev[i]));
+  for (int i = 0; i < Ctx::kStages; ++i) ms[i] = 0.0;
+  RC(op_schur(c, c->G.xin, c->G.Av, true));
+  c->stage_on = true;
+  for (int r = 0; r < reps; ++r) {
+    int rc = op_schur(c, c->G.xin, c->G.Av, true);
+    if (rc != IB_OK) { c->stage_on = false; return rc; }
+    IB_CUDA_CHECK(cudaEventSynchronize(c->stage_ev[Ctx::kStages]));
+    for (int i = 0; i < Ctx::kStages; ++i) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, c->stage_ev[i], c->stage_ev[i + 1]);
+      ms[i] += t;
+    }
+  }
+  c->stage_on = false;
+  c->n_matvec -= reps + 1;
   return IB_OK;
 }
 

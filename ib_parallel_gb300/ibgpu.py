@@ -38,7 +38,7 @@ EXPORTS = [
     "ib_vort2flux", "ib_reg_prep", "ib_reg", "ib_regT", "ib_redistribute", "ib_schur_apply",
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
-    "ib_launch_count", "ib_probe_throughput", "ib_time_pass",
+    "ib_launch_count", "ib_probe_throughput", "ib_time_pass", "ib_profile_schur",
 ]
 
 
@@ -104,6 +104,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_launch_count": ([], C.c_longlong),
         "ib_probe_throughput": ([C.c_int, D], C.c_int),
         "ib_time_pass": ([P, C.c_int, C.c_int, D], C.c_int),
+        "ib_profile_schur": ([P, C.c_int, D], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -294,6 +295,15 @@ class Simulation:
         ms = C.c_double()
         _check(self.lib.ib_time_pass(self.h, kind, reps, C.byref(ms)), "ib_time_pass")
         return ms.value
+
+    SCHUR_STAGES = ["reg+rot", "ainv", "coarsify", "coarse levels", "finest forward", "finest solve",
+                    "finest inverse rows", "E curl + B"]
+
+    def profile_schur(self, reps: int = 20) -> dict:
+        """Average device us per Schur application of each of its stages."""
+        out = (C.c_double * 8)()
+        _check(self.lib.ib_profile_schur(self.h, reps, out), "ib_profile_schur")
+        return {n: 1e3 * out[i] / reps for i, n in enumerate(self.SCHUR_STAGES)}
 
     def profile(self, enable: bool):
         _check(self.lib.ib_profile(self.h, int(bool(enable))), "ib_profile")

@@ -142,6 +142,10 @@ int ib_get_stream(IbCtx* ctx, void** stream);
 /* average device time (ms) of `reps` back-to-back launches of one full pass over the finest
  * grid: kind 0 the DST-I x pass, 1 the per-mode tridiagonal solve (scratch buffers only) */
 int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);
+/* device time (ms, summed over reps back-to-back applications) of the 8 stages of the Schur
+ * operator: reg+rot, ainv, coarsify, coarse levels, finest forward, finest solve, finest
+ * inverse rows, E curl + B */
+int ib_profile_schur(IbCtx* ctx, int reps, double* stage_ms);
 /* enable (1) / disable (0) CUDA-event timing of each DST pass launch; enabling clears the totals */
 int ib_profile(IbCtx* ctx, int enable);
 /* work done since creation: Schur matvecs and DST passes by kind (0..3, see below) */
