@@ -13,6 +13,10 @@ static int fail(int rc, const char* what) {
   return rc;
 }
 
+namespace ib {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace ib
+
 struct IbCtx {
   Ctx* c;
 };

@@ -48,6 +48,36 @@ int dst_plan_create(DstPlan* p, int N) {
   return IB_OK;
 }
 
+size_t dst_plan_table_doubles(int N) {
+  int M = N + 1;
+  if (N < 3 || M % 4 != 0) return 0;
+  int rad[kMaxRadices], nrad = 0;
+  if (!factor_radices(M / 2, rad, &nrad)) return 0;
+  int P = M / 2;
+  return 2 * (size_t)P + 2 * (size_t)(P / 2) + (size_t)P + 1 + 4;
+}
+
+int dst_plan_init_external(DstPlan* p, int N, double* dev, cudaStream_t st) {
+  int M = N + 1;
+  if (dst_plan_table_doubles(N) == 0) return IB_ERR_ARG;
+  p->N = N; p->M = M; p->P = M / 2;
+  if (!factor_radices(p->P, p->rad, &p->nrad)) return IB_ERR_ARG;
+  std::vector<double2> tw(p->P), uw(p->P / 2);
+  std::vector<double> sn(p->P + 1);
+  for (int t = 0; t < p->P; ++t) tw[t] = twiddle(t, p->P);
+  for (int k = 0; k < p->P / 2; ++k) uw[k] = twiddle(k, M);
+  const long double PI_L = 3.141592653589793238462643383279502884L;
+  for (int j = 0; j <= p->P; ++j) sn[j] = (double)sinl(PI_L * (long double)j / (long double)M);
+  p->tw = reinterpret_cast<double2*>(dev);
+  p->uw = p->tw + p->P;
+  p->sn = reinterpret_cast<double*>(p->uw + p->P / 2);
+  IB_CUDA_CHECK(cudaMemcpyAsync(p->tw, tw.data(), sizeof(double2) * p->P, cudaMemcpyHostToDevice, st));
+  IB_CUDA_CHECK(cudaMemcpyAsync(p->uw, uw.data(), sizeof(double2) * (p->P / 2), cudaMemcpyHostToDevice, st));
+  IB_CUDA_CHECK(cudaMemcpyAsync(p->sn, sn.data(), sizeof(double) * (p->P + 1), cudaMemcpyHostToDevice, st));
+  IB_CUDA_CHECK(cudaStreamSynchronize(st));
+  return IB_OK;
+}
+
 void dst_plan_destroy(DstPlan* p) {
   if (p->tw) cudaFree(p->tw);
   if (p->uw) cudaFree(p->uw);

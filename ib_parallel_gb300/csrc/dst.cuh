@@ -35,6 +35,11 @@ struct DstLaunch {
 
 int dst_plan_create(DstPlan* p, int N);   // N = M-1, M divisible by 4, M = 2^a 3^b 5^c
 void dst_plan_destroy(DstPlan* p);
+// Doubles of device memory the tables of a plan of length N occupy (0 if N is unsupported).
+size_t dst_plan_table_doubles(int N);
+// Fills a plan's tables into caller-provided device memory (no allocation; the plan must not
+// be passed to dst_plan_destroy).  dev must hold dst_plan_table_doubles(N) doubles, 16-byte aligned.
+int dst_plan_init_external(DstPlan* p, int N, double* dev, cudaStream_t st);
 
 enum DstPre { PRE_COPY = 0, PRE_COMBINE = 1, PRE_APPLYBC = 2, PRE_PRED = 3 };
 enum DstYMode { YMODE_NONE = 0 };

@@ -38,7 +38,7 @@ EXPORTS = [
     "ib_vort2flux", "ib_reg_prep", "ib_reg", "ib_regT", "ib_redistribute", "ib_schur_apply",
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
-    "ib_launch_count", "ib_probe_throughput", "ib_time_pass", "ib_profile_schur",
+    "ib_launch_count", "ib_probe_throughput", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
 ]
 
 
@@ -105,6 +105,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_probe_throughput": ([C.c_int, D], C.c_int),
         "ib_time_pass": ([P, C.c_int, C.c_int, D], C.c_int),
         "ib_profile_schur": ([P, C.c_int, D], C.c_int),
+        "ib_ctci_static": ([C.c_int, C.c_int, P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -140,6 +141,15 @@ def probe_throughput(which: int) -> float:
     t = C.c_double()
     _check(load().ib_probe_throughput(which, C.byref(t)), "ib_probe_throughput")
     return t.value
+
+
+def ctci_static(m: int, n: int, vort_ptr: int, s_ptr: int, stream_ptr: int = 0) -> None:
+    """Context-free Poisson solve on device arrays (raw device addresses), allocating nothing.
+
+    Runs asynchronously on the given CUDA stream (0: the default stream); the grid must fit
+    the library's 16 MiB static scratch, and calls that overlap on the GPU race on it."""
+    _check(load().ib_ctci_static(m, n, C.c_void_p(vort_ptr), C.c_void_p(s_ptr), C.c_void_p(stream_ptr)),
+           "ib_ctci_static")
 
 
 def measure_fp64_peak() -> float:

@@ -107,6 +107,19 @@ int ib_apply_bc(IbCtx* ctx, double* vort, const double* ring, double fac);
 int ib_dst(IbCtx* ctx, const double* in, double* out);
 /* myfft.F90:177-188 ctci */
 int ib_ctci(IbCtx* ctx, const double* vort, double* s);
+/* The same Poisson solve for an m x n grid without a context and without allocating device
+ * memory.  It has no counterpart in the reference; it is for callers that may not allocate
+ * when they need the solve: a host that reserves its device memory once at start-up, a time
+ * loop that must not pay cudaFree's device-wide synchronisation, or code holding no IbCtx.
+ * vort and s are DEVICE arrays ((n-1) x (m-1), x fastest); the kernels run on `stream` (a
+ * cudaStream_t, NULL for the default stream) and the call returns without waiting for them.
+ * Scratch and tables live in one 16 MiB static device array that each GPU loading the library
+ * keeps until the process exits: grids needing more ((m-1)(n-1) plus the tables; 1600 x 800
+ * fits, 1920 x 960 does not) fail with IB_ERR_ARG.  The first call on a device, and the first
+ * after the grid size changes, does the set-up with synchronous copies: make it before any
+ * stream capture.  All calls on a device share the array: calls whose kernels overlap on the
+ * GPU race and give wrong results.  Errors are reported through ib_last_error(). */
+int ib_ctci_static(int m, int n, const double* vort, double* s, void* stream);
 /* myfft.F90:161-173 ainv (in place) */
 int ib_ainv(IbCtx* ctx, double* vort);
 /* operators_fluid.F90:649-663 fluid_predictor (omega in place) */
