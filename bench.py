@@ -49,9 +49,9 @@ METRIC = "FSI steps/s @800x400x5 FP64"
 WORKLOAD = "plate800x400"
 # Schur matvecs per step of this workload (Krylov iterations + one initial-residual
 # product per GMRES cycle, summed over the FSI iterations), counted by the GPU
-# arm's ib_get_work (56.5 and 60 over the first steps after warm-up on GB300); the CPU
-# arm runs the same algorithm.
-MATVECS_PER_STEP = 58.0
+# arm's ib_get_work (49.8 to 53 over the first steps after warm-up on GB300); the CPU
+# arm runs the same algorithm with the matrix-free operator.
+MATVECS_PER_STEP = 52.0
 
 
 def _env_int(k, d):
@@ -245,6 +245,8 @@ def run_gpu(args, world, rank, local):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
+        if args.profile_window:
+            torch.cuda.profiler.start()
         e0.record(stream)
         for _ in range(args.steps):
             sim.advance()
@@ -253,6 +255,8 @@ def run_gpu(args, world, rank, local):
             fsi_sum += f
         e1.record(stream)
         e1.synchronize()
+        if args.profile_window:
+            torch.cuda.profiler.stop()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     t_s = _barrier_max(ms / 1e3, world)
@@ -334,7 +338,10 @@ def run_gpu(args, world, rank, local):
                           "peak_source": "of measured FP64 FMA loop on this GPU (ib_measure_fp64_peak)"},
         "tridiagonal_pass_us": 1e3 * t_tri,
         "schur_stages_us": sim.profile_schur(20),
+        "influence": sim.influence_stats(),
     }
+    if not args.no_matrix_free:
+        result["matrix_free"] = _matrix_free_rate(p, bodies, args)
     result["gpu_launches"] = launches_timed
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
@@ -354,6 +361,32 @@ def run_gpu(args, world, rank, local):
     return 0
 
 
+def _matrix_free_rate(p, bodies, args):
+    """Steps/s of the same workload with the Schur operator applied matrix-free in every
+    Krylov iteration (schur_mode 1), timed the same way over the same number of steps."""
+    import dataclasses
+
+    import torch
+    from ib_parallel_gb300 import ibgpu as G
+    sim = G.Simulation(dataclasses.replace(p, schur_mode=1), bodies)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    for _ in range(args.warmup):
+        sim.advance()
+    sim.synchronize()
+    mv0, _ = sim.work()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        sim.advance()
+    e1.record(stream)
+    e1.synchronize()
+    mv1, _ = sim.work()
+    sim.close()
+    return {"value": args.steps / (e0.elapsed_time(e1) / 1e3), "unit": "steps/s",
+            "schur_matvecs_per_step": (mv1 - mv0) / args.steps}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,6 +394,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-matrix-free", action="store_true",
+                    help="skip timing the matrix-free Schur operator beside the default one")
+    ap.add_argument("--profile-window", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":

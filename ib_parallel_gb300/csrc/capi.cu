@@ -503,6 +503,34 @@ int ib_profile_schur(IbCtx* h, int reps, double* stage_ms) {
   return op_result(ib::op_profile_schur(c, reps, stage_ms), "profile_schur failed");
 }
 
+int ib_schur_matrix(IbCtx* h, double* S, int* status) {
+  CTX_OR_FAIL(h);
+  if (!S || !status) return fail(IB_ERR_ARG, "bad argument");
+  if (c->nf == 0) return fail(IB_ERR_STATE, "no body unknowns");
+  if (c->p.schur_mode != 0) return fail(IB_ERR_STATE, "influence matrix disabled (schur_mode 1)");
+  int rc = ib::inf_prepare(c);
+  if (rc != IB_OK) return op_result(rc, "influence matrix failed");
+  *status = c->inf.active ? 0 : (c->inf.flag_h ? c->inf.flag_h : 4);
+  if (c->inf.active &&
+      cudaMemcpyAsync(S, c->inf.S, sizeof(double) * (size_t)c->nf * c->nf, cudaMemcpyDefault, c->st) != cudaSuccess)
+    return fail(IB_ERR_CUDA, "copy failed");
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "sync failed");
+  return IB_OK;
+}
+
+int ib_get_influence_stats(IbCtx* h, long long* counts, double* build_ms) {
+  CTX_OR_FAIL(h);
+  if (!counts || !build_ms) return fail(IB_ERR_ARG, "bad argument");
+  const ib::Influence& I = c->inf;
+  counts[0] = I.builds;
+  counts[1] = I.columns;
+  counts[2] = I.assemblies;
+  counts[3] = I.fallbacks;
+  counts[4] = I.nR;
+  *build_ms = I.build_ms;
+  return IB_OK;
+}
+
 int ib_profile(IbCtx* h, int enable) {
   CTX_OR_FAIL(h);
   if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "sync failed");

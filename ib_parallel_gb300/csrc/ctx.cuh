@@ -12,6 +12,13 @@
 
 namespace ib {
 
+// Propagates a non-OK status to the caller.
+#define RC(x)                     \
+  do {                            \
+    int _rc = (x);                \
+    if (_rc != IB_OK) return _rc; \
+  } while (0)
+
 // Bump allocator over one device allocation made at ib_create.
 struct DevPool {
   char* base = nullptr;
@@ -24,6 +31,40 @@ struct DevPool {
     used += bytes;
     return p;
   }
+};
+
+// Influence matrix of the fluid part of the Schur operator for moving bodies.  The band R
+// is a set of 8 x 8 vertex tiles around the bodies' stencils; K[u][v] (column u contiguous,
+// nR x nR) is the finest-level streamfunction at band vertex v for a unit vorticity at band
+// vertex u, i.e. the map the matrix-free operator applies between rot and E curl.  Each
+// unknown k owns the 8 x 8 vertex patch P_k = rot(E^T e_k) (values and band indices); the
+// fluid Schur matrix is S_f = P^T K P (curl is the transpose of rot).
+struct Influence {
+  static constexpr int kTile = 8;
+  bool built = false;
+  bool active = false;        // S holds the operator at the current positions
+  bool patch_fresh = false;   // patches and flag match the current reg weights
+  int flag_h = 0;             // 1: a patch leaves the band; 2: a patch touches the boundary
+  int ntx = 0, nty = 0, ntile = 0, nR = 0;
+  std::vector<int2> tiles_h;
+  int* tile_of = nullptr;     // ntx*nty: tile index in the band or -1
+  int2* tiles = nullptr;      // band tiles (tile coordinates)
+  double* K = nullptr;
+  size_t capK = 0, capR = 0;
+  int* used = nullptr;        // nR: vertex touched by some patch
+  int* ulist = nullptr;       // compacted band indices of the touched vertices
+  int* upos = nullptr;        // nR: position in ulist or -1
+  int* nu = nullptr;          // number of touched vertices
+  double* T = nullptr;        // nf rows of nR: T[l][u] = (K P)[ulist[u]][l]
+  double* pval = nullptr;     // nf*64 patch values
+  int* pidx = nullptr;        // nf*64 patch band indices (-1: none)
+  double* S = nullptr;        // nf x nf row-major fluid Schur matrix
+  int* flag = nullptr;
+  int* h_flag = nullptr;      // pinned
+  int* rr_in = nullptr;       // row ranges of the precompute (3 ints each)
+  int* rr_out = nullptr;
+  long long builds = 0, columns = 0, assemblies = 0, fallbacks = 0;
+  double build_ms = 0.0;
 };
 
 struct Ctx {
@@ -79,9 +120,12 @@ struct Ctx {
   double *gm_b = nullptr, *gm_x = nullptr;
   bool use_graph = true;
   bool graph_failed = false;
-  cudaGraphExec_t solve_exec = nullptr;
+  cudaGraphExec_t solve_exec = nullptr;         // matrix-free operator
   cudaGraph_t solve_graph = nullptr;
-  long long kernels_per_matvec = 0;
+  cudaGraphExec_t solve_exec_dense = nullptr;   // assembled operator (Influence::S)
+  cudaGraph_t solve_graph_dense = nullptr;
+  long long kernels_per_matvec = 0, kernels_per_matvec_dense = 0;
+  Influence inf;
   double* cholM = nullptr;         // nf x nf (num_stat)
   bool chol_ready = false;
 
@@ -133,6 +177,15 @@ int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs
 int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy,
                  bool all_curls);
 int op_schur(Ctx* c, const double* x, double* y, bool with_b);
+int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out, double* s_out,
+                const double** ring0_out);
+// influence.cu
+int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
+void inf_free(Ctx* c);
+int inf_patch(Ctx* c);                 // patches + flag for the current weights (async)
+int inf_prepare(Ctx* c);               // build/rebuild the band if needed, assemble S
+int inf_dense_mv(Ctx* c, const double* x, double* y, bool with_b);
+int inf_build(Ctx* c);
 int op_redistribute(Ctx* c, const double* f, double* frdst);
 int op_reg_prep(Ctx* c);
 int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms);

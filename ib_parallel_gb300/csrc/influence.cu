@@ -1,0 +1,386 @@
+// Influence-matrix evaluation of the Schur operator a_times2 / ab_times
+// (operators_fluid.F90:14-120, timestepper.F90:774-782) for moving bodies.
+//
+// The operator is y = E curl G rot E^T x + B x, where G (vorticity on the finest level ->
+// finest-level streamfunction: ainv, then vort2flux with every coarser level) does not
+// depend on the body positions.  G is evaluated once on a band of vertices around the
+// bodies (one column per band vertex, each a matrix-free application of the fluid part),
+// and every FSI iteration assembles the dense nf x nf matrix
+//     S_f = P^T K P,   P = rot E^T (one 8 x 8 vertex patch per unknown; curl = rot^T)
+// in a few microseconds.  The Krylov iteration then multiplies by S_f instead of running
+// the nested-grid solve: the same linear operator, evaluated in another order.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+#include "ctx.cuh"
+
+namespace ib {
+
+namespace {
+constexpr int kT = Influence::kTile;   // tile edge (vertices)
+constexpr int kP = 64;                 // patch size (8 x 8 vertices)
+}  // namespace
+
+// Per unknown k (one CTA of 64 threads): the patch rot(E^T e_k) on the vertices
+// I in [cx-3, cx+4], J in [cy-3, cy+4], with each vertex's index in the band.
+// flag |= 1 when a patch vertex lies outside the band, |= 2 when it is not an interior
+// vertex (its streamfunction would come from the boundary ring).
+__global__ void k_inf_patch(GridDims g, int nf, const int* __restrict__ comp, const int* __restrict__ ix,
+                            const int* __restrict__ iy, const double* __restrict__ w,
+                            const int* __restrict__ tile_of, int ntx, double* __restrict__ pval,
+                            int* __restrict__ pidx, int* __restrict__ used, int* __restrict__ flag) {
+  const int k = blockIdx.x, q = threadIdx.x;
+  if (k >= nf || q >= kP) return;
+  const int di = q & 7, dj = q >> 3;
+  const int cx = ix[k], cy = iy[k];
+  const bool isx = comp[k] == 1;
+  const double* wk = w + (size_t)k * 49;
+  auto W = [&](int p, int l) -> double {
+    return (p >= -3 && p <= 3 && l >= -3 && l <= 3) ? wk[(l + 3) * 7 + (p + 3)] : 0.0;
+  };
+  const int p = di - 3, l = dj - 3;
+  // rot (operators_fluid.F90:203-233) of the spread unit force: a u-face (i,j) adds -1 to
+  // vertex (i,j) and +1 to (i,j+1); a v-face adds +1 to (i,j) and -1 to (i+1,j)
+  double v = isx ? W(p, l - 1) - W(p, l) : W(p, l) - W(p - 1, l);
+  const int a = cx - 3 + di - 2, b = cy - 3 + dj - 2;   // 0-based interior vertex
+  int idx = -1, fl = 0;
+  if (a < 0 || a >= g.nsx || b < 0 || b >= g.nsy) {
+    fl = 2;
+  } else if (!tile_of) {
+    fl = 1;
+  } else {
+    int t = tile_of[(b / kT) * ntx + a / kT];
+    if (t < 0) fl = 1;
+    else idx = t * kP + (b % kT) * kT + (a % kT);
+  }
+  if (idx < 0) v = 0.0;
+  pval[(size_t)k * kP + q] = v;
+  pidx[(size_t)k * kP + q] = idx;
+  if (idx >= 0) used[idx] = 1;
+  if (fl) atomicOr(flag, fl);
+}
+
+// Compaction of the touched band vertices (one CTA of 1024 threads).
+__global__ void k_inf_compact(int nR, const int* __restrict__ used, int* __restrict__ ulist,
+                              int* __restrict__ upos, int* __restrict__ nu) {
+  __shared__ int wsum[32];
+  __shared__ int base;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid == 0) base = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < nR; c0 += 1024) {
+    const int i = c0 + tid;
+    const int f = (i < nR && used[i]) ? 1 : 0;
+    int x = f;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int s = wsum[lane], inc = s;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+      }
+      wsum[lane] = inc - s;
+    }
+    __syncthreads();
+    const int pos = base + wsum[wid] + x - f;
+    if (i < nR) {
+      upos[i] = f ? pos : -1;
+      if (f) ulist[pos] = i;
+    }
+    __syncthreads();
+    if (tid == 1023) base = pos + f;
+    __syncthreads();
+  }
+  if (tid == 0) *nu = base;
+}
+
+// T[l][u] = sum_q P[q,l] K[ulist[u]][src_q]: the response at every touched vertex to the
+// patch of unknown l.  Grid (row blocks, nf); K columns are read coalesced along rows.
+__global__ void k_inf_kp(int nR, const double* __restrict__ K, const double* __restrict__ pval,
+                         const int* __restrict__ pidx, const int* __restrict__ ulist, const int* __restrict__ nu,
+                         double* __restrict__ T) {
+  __shared__ double sv[kP];
+  __shared__ int si[kP];
+  const int l = blockIdx.y;
+  if (threadIdx.x < kP) {
+    sv[threadIdx.x] = pval[(size_t)l * kP + threadIdx.x];
+    si[threadIdx.x] = pidx[(size_t)l * kP + threadIdx.x];
+  }
+  __syncthreads();
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= *nu) return;
+  const int r = ulist[u];
+  double acc = 0.0;
+#pragma unroll 8
+  for (int q = 0; q < kP; ++q) {
+    const int c = si[q];
+    if (c >= 0) acc = fma(sv[q], K[(size_t)c * nR + r], acc);
+  }
+  T[(size_t)l * nR + u] = acc;
+}
+
+// S[k][l] = sum_q P[q,k] T[l][upos(src_q)]  (E curl = P^T), one CTA per row k.
+__global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const int* __restrict__ pidx,
+                          const int* __restrict__ upos, const double* __restrict__ T, double* __restrict__ S) {
+  __shared__ double sv[kP];
+  __shared__ int su[kP];
+  const int k = blockIdx.x;
+  if (threadIdx.x < kP) {
+    const int c = pidx[(size_t)k * kP + threadIdx.x];
+    sv[threadIdx.x] = pval[(size_t)k * kP + threadIdx.x];
+    su[threadIdx.x] = c >= 0 ? upos[c] : -1;
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < nf; l += blockDim.x) {
+    const double* Tl = T + (size_t)l * nR;
+    double acc = 0.0;
+    for (int q = 0; q < kP; ++q) {
+      const int u = su[q];
+      if (u >= 0) acc = fma(sv[q], Tl[u], acc);
+    }
+    S[(size_t)k * nf + l] = acc;
+  }
+}
+
+// y = S x, one warp per row.
+__global__ void k_dense_mv(int n, const double* __restrict__ S, const double* __restrict__ x, double* __restrict__ y) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const double* Sr = S + (size_t)row * n;
+  double acc = 0.0;
+  for (int j = lane; j < n; j += 32) acc = fma(Sr[j], x[j], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[row] = acc;
+}
+
+// Column c of the precompute: unit vorticity at band vertex c (the previous one cleared),
+// and the row range of the forward transform (the one nonzero row).
+__global__ void k_inf_unit(int c, const int2* __restrict__ tiles, GridDims g, double* vort, int* prev, int* rr_in) {
+  if (threadIdx.x != 0) return;
+  const int p = *prev;
+  if (p >= 0) vort[p] = 0.0;
+  const int2 tc = tiles[c / kP];
+  const int q = c % kP;
+  const int a = tc.x * kT + (q % kT), b = tc.y * kT + q / kT;
+  if (a < g.nsx && b < g.nsy) {
+    const int o = b * g.nsx + a;
+    vort[o] = 1.0;
+    *prev = o;
+    rr_in[0] = b;
+    rr_in[1] = b + 1;
+  } else {
+    *prev = -1;
+    rr_in[0] = 0;
+    rr_in[1] = 1;
+  }
+  rr_in[2] = ROW_ZERO;
+}
+
+// K[c][v] = s(band vertex v) for every band vertex (0 for tile vertices outside the grid).
+__global__ void k_inf_gather(int c, int nR, const int2* __restrict__ tiles, GridDims g, const double* __restrict__ s,
+                             double* __restrict__ K) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nR) return;
+  const int2 tc = tiles[i / kP];
+  const int q = i % kP;
+  const int a = tc.x * kT + (q % kT), b = tc.y * kT + q / kT;
+  K[(size_t)c * nR + i] = (a < g.nsx && b < g.nsy) ? s[b * g.nsx + a] : 0.0;
+}
+
+int inf_alloc(Ctx* c) {
+  Influence& I = c->inf;
+  const int nf = std::max(c->nf, 1);
+  IB_CUDA_CHECK(cudaMalloc(&I.pval, sizeof(double) * (size_t)nf * kP));
+  IB_CUDA_CHECK(cudaMalloc(&I.pidx, sizeof(int) * (size_t)nf * kP));
+  IB_CUDA_CHECK(cudaMalloc(&I.S, sizeof(double) * (size_t)nf * nf));
+  IB_CUDA_CHECK(cudaMalloc(&I.flag, sizeof(int) * 16));
+  I.nu = I.flag + 4;
+  I.rr_in = I.flag + 8;
+  I.rr_out = I.flag + 12;
+  IB_CUDA_CHECK(cudaMemset(I.flag, 0, sizeof(int) * 16));
+  IB_CUDA_CHECK(cudaHostAlloc(&I.h_flag, sizeof(int) * 2, cudaHostAllocDefault));
+  I.ntx = cdiv(c->g.nsx, kT);
+  I.nty = cdiv(c->g.nsy, kT);
+  IB_CUDA_CHECK(cudaMalloc(&I.tile_of, sizeof(int) * (size_t)I.ntx * I.nty));
+  return IB_OK;
+}
+
+static void free_band(Influence& I) {
+  if (I.K) cudaFree(I.K);
+  if (I.used) cudaFree(I.used);
+  if (I.ulist) cudaFree(I.ulist);
+  if (I.upos) cudaFree(I.upos);
+  if (I.T) cudaFree(I.T);
+  if (I.tiles) cudaFree(I.tiles);
+  I.K = nullptr; I.used = I.ulist = I.upos = nullptr; I.T = nullptr; I.tiles = nullptr;
+  I.capK = I.capR = 0;
+}
+
+void inf_free(Ctx* c) {
+  Influence& I = c->inf;
+  free_band(I);
+  if (I.pval) cudaFree(I.pval);
+  if (I.pidx) cudaFree(I.pidx);
+  if (I.S) cudaFree(I.S);
+  if (I.flag) cudaFree(I.flag);
+  if (I.tile_of) cudaFree(I.tile_of);
+  if (I.h_flag) cudaFreeHost(I.h_flag);
+  I = Influence{};
+}
+
+int inf_patch(Ctx* c) {
+  Influence& I = c->inf;
+  if (c->nf == 0) return IB_OK;
+  IB_CUDA_CHECK(cudaMemsetAsync(I.flag, 0, sizeof(int), c->st));
+  if (I.built) IB_CUDA_CHECK(cudaMemsetAsync(I.used, 0, sizeof(int) * (size_t)I.nR, c->st));
+  count_launch();
+  k_inf_patch<<<c->nf, kP, 0, c->st>>>(c->g, c->nf, c->reg.comp, c->reg.ix, c->reg.iy, c->reg.w,
+                                       I.built ? I.tile_of : nullptr, I.ntx, I.pval, I.pidx, I.used, I.flag);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+static int read_flag(Ctx* c) {
+  Influence& I = c->inf;
+  IB_CUDA_CHECK(cudaMemcpyAsync(I.h_flag, I.flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  IB_CUDA_CHECK(cudaStreamSynchronize(c->st));
+  I.flag_h = I.h_flag[0];
+  I.patch_fresh = true;
+  return IB_OK;
+}
+
+// The band: every tile within `margin` vertices of some unknown's patch.  Then one
+// matrix-free application of the fluid part per band vertex fills K.
+int inf_build(Ctx* c) {
+  Influence& I = c->inf;
+  const GridDims& g = c->g;
+  const int nf = c->nf;
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<int> ix(nf), iy(nf);
+  IB_CUDA_CHECK(cudaStreamSynchronize(c->st));
+  IB_CUDA_CHECK(cudaMemcpy(ix.data(), c->reg.ix, sizeof(int) * nf, cudaMemcpyDeviceToHost));
+  IB_CUDA_CHECK(cudaMemcpy(iy.data(), c->reg.iy, sizeof(int) * nf, cudaMemcpyDeviceToHost));
+  const int M = c->p.influence_margin > 0 ? c->p.influence_margin : 8;
+  std::vector<int> tile_of((size_t)I.ntx * I.nty, -1);
+  std::vector<char> mark((size_t)I.ntx * I.nty, 0);
+  for (int k = 0; k < nf; ++k) {
+    int a0 = std::max(0, ix[k] - 5 - M), a1 = std::min(g.nsx - 1, ix[k] + 2 + M);
+    int b0 = std::max(0, iy[k] - 5 - M), b1 = std::min(g.nsy - 1, iy[k] + 2 + M);
+    if (a0 > a1 || b0 > b1) continue;
+    for (int tb = b0 / kT; tb <= b1 / kT; ++tb)
+      for (int ta = a0 / kT; ta <= a1 / kT; ++ta) mark[(size_t)tb * I.ntx + ta] = 1;
+  }
+  I.tiles_h.clear();
+  int bmin = g.nsy, bmax = -1;
+  for (int tb = 0; tb < I.nty; ++tb)
+    for (int ta = 0; ta < I.ntx; ++ta)
+      if (mark[(size_t)tb * I.ntx + ta]) {
+        tile_of[(size_t)tb * I.ntx + ta] = (int)I.tiles_h.size();
+        I.tiles_h.push_back(make_int2(ta, tb));
+        bmin = std::min(bmin, tb * kT);
+        bmax = std::max(bmax, std::min(g.nsy - 1, tb * kT + kT - 1));
+      }
+  I.ntile = (int)I.tiles_h.size();
+  I.nR = I.ntile * kP;
+  I.built = false;
+  I.active = false;
+  if (I.nR == 0) return IB_ERR_STATE;
+  const size_t nK = (size_t)I.nR * I.nR;
+  if (nK > I.capK || (size_t)I.nR > I.capR) {
+    free_band(I);
+    size_t freeb = 0, totalb = 0;
+    IB_CUDA_CHECK(cudaMemGetInfo(&freeb, &totalb));
+    const size_t need = 8 * nK + (size_t)I.nR * (12 + 8 * (size_t)std::max(nf, 1)) + 8 * (size_t)I.ntile;
+    if (need > freeb / 2) return IB_ERR_NOMEM;   // leave the rest of HBM to the caller
+    IB_CUDA_CHECK(cudaMalloc(&I.K, 8 * nK));
+    IB_CUDA_CHECK(cudaMalloc(&I.used, sizeof(int) * I.nR));
+    IB_CUDA_CHECK(cudaMalloc(&I.ulist, sizeof(int) * I.nR));
+    IB_CUDA_CHECK(cudaMalloc(&I.upos, sizeof(int) * I.nR));
+    IB_CUDA_CHECK(cudaMalloc(&I.T, sizeof(double) * (size_t)I.nR * std::max(nf, 1)));
+    I.capK = nK;
+    I.capR = I.nR;
+  }
+  if (I.tiles) cudaFree(I.tiles);
+  IB_CUDA_CHECK(cudaMalloc(&I.tiles, sizeof(int2) * I.ntile));
+  IB_CUDA_CHECK(cudaMemcpy(I.tiles, I.tiles_h.data(), sizeof(int2) * I.ntile, cudaMemcpyHostToDevice));
+  IB_CUDA_CHECK(cudaMemcpy(I.tile_of, tile_of.data(), sizeof(int) * tile_of.size(), cudaMemcpyHostToDevice));
+  const int rr_out_h[3] = {bmin, bmax + 1, ROW_SKIP};
+  IB_CUDA_CHECK(cudaMemcpy(I.rr_out, rr_out_h, sizeof(rr_out_h), cudaMemcpyHostToDevice));
+  // columns: unit vorticity at each band vertex through the fluid part of the operator
+  cudaStream_t st = c->st;
+  int* prev = I.flag + 2;
+  IB_CUDA_CHECK(cudaMemsetAsync(c->vort, 0, sizeof(double) * (size_t)g.ns, st));
+  const int minus1 = -1;
+  IB_CUDA_CHECK(cudaMemcpyAsync(prev, &minus1, sizeof(int), cudaMemcpyHostToDevice, st));
+  const bool prof = c->prof_on;
+  c->prof_on = false;
+  int rc = IB_OK;
+  for (int col = 0; col < I.nR && rc == IB_OK; ++col) {
+    count_launch();
+    k_inf_unit<<<1, 32, 0, st>>>(col, I.tiles, g, c->vort, prev, I.rr_in);
+    const double* ring0 = nullptr;
+    rc = schur_fluid(c, c->vort, I.rr_in, I.rr_out, c->mv_s[0], &ring0);
+    if (rc != IB_OK) break;
+    count_launch();
+    k_inf_gather<<<cdiv(I.nR, 256), 256, 0, st>>>(col, I.nR, I.tiles, g, c->mv_s[0], I.K);
+    if (cudaGetLastError() != cudaSuccess) rc = IB_ERR_CUDA;
+  }
+  c->prof_on = prof;
+  RC(rc);
+  IB_CUDA_CHECK(cudaMemsetAsync(c->vort, 0, sizeof(double) * (size_t)g.ns, st));
+  IB_CUDA_CHECK(cudaStreamSynchronize(st));
+  I.columns += I.nR;
+  I.builds += 1;
+  I.built = true;
+  I.patch_fresh = false;
+  I.build_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return IB_OK;
+}
+
+int inf_prepare(Ctx* c) {
+  Influence& I = c->inf;
+  I.active = false;
+  if (c->p.schur_mode != 0 || c->nf == 0) return IB_OK;
+  if (!I.patch_fresh) {
+    RC(inf_patch(c));
+    RC(read_flag(c));
+  }
+  if (I.flag_h & 2) { I.fallbacks += 1; return IB_OK; }
+  if (!I.built || (I.flag_h & 1)) {
+    int rc = inf_build(c);
+    if (rc == IB_ERR_NOMEM || rc == IB_ERR_STATE) { I.fallbacks += 1; return IB_OK; }
+    RC(rc);
+    RC(inf_patch(c));
+    RC(read_flag(c));
+    if (I.flag_h) { I.fallbacks += 1; return IB_OK; }
+  }
+  cudaStream_t st = c->st;
+  count_launch();
+  k_inf_compact<<<1, 1024, 0, st>>>(I.nR, I.used, I.ulist, I.upos, I.nu);
+  count_launch();
+  k_inf_kp<<<dim3(cdiv(I.nR, 128), c->nf), 128, 0, st>>>(I.nR, I.K, I.pval, I.pidx, I.ulist, I.nu, I.T);
+  count_launch();
+  k_inf_ptk<<<c->nf, 128, 0, st>>>(c->nf, I.nR, I.pval, I.pidx, I.upos, I.T, I.S);
+  IB_CUDA_CHECK(cudaGetLastError());
+  I.assemblies += 1;
+  I.active = true;
+  return IB_OK;
+}
+
+int inf_dense_mv(Ctx* c, const double* x, double* y, bool with_b) {
+  c->n_matvec += 1;
+  count_launch();
+  k_dense_mv<<<cdiv(32LL * c->nf, 256), 256, 0, c->st>>>(c->nf, c->inf.S, x, y);
+  IB_CUDA_CHECK(cudaGetLastError());
+  if (with_b) RC(launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, x, y, c->st));
+  return IB_OK;
+}
+
+}  // namespace ib

@@ -9,11 +9,6 @@
 
 namespace ib {
 
-#define RC(x)                   \
-  do {                          \
-    int _rc = (x);              \
-    if (_rc != IB_OK) return _rc; \
-  } while (0)
 
 static const double kPi = 4.0 * std::atan(1.0);  // parameters.F90:61
 
@@ -360,6 +355,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     rc = tune(c);
     if (rc != IB_OK) { *msg = "DST tuning failed"; ctx_destroy(c); return rc; }
   }
+  if (nf > 0 && inf_alloc(c) != IB_OK) { *msg = "device allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM; }
   rc = op_reg_prep(c);
   if (rc == IB_OK) rc = check_err(c);
   if (rc != IB_OK) { *msg = "body stencil outside the grid"; ctx_destroy(c); return rc; }
@@ -374,6 +370,9 @@ void ctx_destroy(Ctx* c) {
   dst_plan_destroy(&c->py);
   if (c->solve_exec) cudaGraphExecDestroy(c->solve_exec);
   if (c->solve_graph) cudaGraphDestroy(c->solve_graph);
+  if (c->solve_exec_dense) cudaGraphExecDestroy(c->solve_exec_dense);
+  if (c->solve_graph_dense) cudaGraphDestroy(c->solve_graph_dense);
+  inf_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -482,27 +481,24 @@ static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring) 
   return launch_get_bc(g, s, 1.0, ring, c->st);
 }
 
-// ab_times / a_times2 (timestepper.F90:774-782, operators_fluid.F90:14-120):
-// y = E (vort2flux(ainv(rot(E^T x))))_1 + B x, evaluating only what E reads.
-//  * ainv: x transform of the rows rot(E^T x) can touch, tridiagonal solve (Y), full
-//    inverse transform (the vorticity every coarser level is coarsified from).
+// The fluid part of the Schur operator between rot and E curl: the finest-level
+// streamfunction s_out = (vort2flux(ainv(vort)))_1 on the rows rr_out selects, and the ring
+// of level 1 in *ring0.  vort must be zero outside the rows rr_in selects.
+//  * ainv: x transform of the rows rr_in selects, tridiagonal solve (Y), full inverse
+//    transform (the vorticity every coarser level is coarsified from).
 //  * coarse levels: inputs are the coarsified centre rows plus the boundary values of
 //    apply_bc (closed-form transforms); outputs are needed on the finer boundary only.
 //  * finest level: its forward transform is 2m Y plus the boundary terms; its inverse is
-//    needed only on the rows E reads, and curl is fused into E.
-int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
+//    needed only on the rows rr_out selects.
+int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out, double* s_out,
+                const double** ring0_out) {
   const GridDims& g = c->g;
   const int L = c->L;
   cudaStream_t st = c->st;
-  c->n_matvec += 1;
   auto mark = [&](int i) { if (c->stage_on) cudaEventRecord(c->stage_ev[i], st); };
-  mark(0);
-  RC(launch_reg(g, c->nf, x, c->reg, c->hx, c->hy, st));
-  RC(launch_rot(g, c->hx, c->hy, c->vort, st));
-  mark(1);
   {
     DstXArgs a;
-    a.in = c->vort; a.out = c->specY; a.rowrange = c->reg.bbox + 4;
+    a.in = vort; a.out = c->specY; a.rowrange = rr_in;
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
   }
@@ -560,10 +556,28 @@ int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
   mark(6);
   {
     DstXArgs a;
-    a.in = c->spec1; a.out = c->mv_s[0]; a.rowrange = c->reg.bbox + 7;
+    a.in = c->spec1; a.out = s_out; a.rowrange = rr_out;
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
   }
+  *ring0_out = ring0;
+  return IB_OK;
+}
+
+// ab_times / a_times2 (timestepper.F90:774-782, operators_fluid.F90:14-120):
+// y = E (vort2flux(ainv(rot(E^T x))))_1 + B x, evaluating only what E reads: the rows
+// rot(E^T x) can touch go in, the rows E (curl s) reads come out, and curl is fused into E.
+int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
+  const GridDims& g = c->g;
+  cudaStream_t st = c->st;
+  c->n_matvec += 1;
+  auto mark = [&](int i) { if (c->stage_on) cudaEventRecord(c->stage_ev[i], st); };
+  mark(0);
+  RC(launch_reg(g, c->nf, x, c->reg, c->hx, c->hy, st));
+  RC(launch_rot(g, c->hx, c->hy, c->vort, st));
+  mark(1);
+  const double* ring0 = nullptr;
+  RC(schur_fluid(c, c->vort, c->reg.bbox + 4, c->reg.bbox + 7, c->mv_s[0], &ring0));
   mark(7);
   RC(launch_regT_s(g, c->nf, c->mv_s[0], ring0, c->reg, nullptr, y, st));
   if (with_b) RC(launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, x, y, st));
@@ -628,6 +642,8 @@ int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms) {
 }
 
 int op_reg_prep(Ctx* c) {
+  c->inf.patch_fresh = false;
+  c->inf.active = false;
   return launch_reg_build(c->g, c->nf, c->xb, c->yb, c->delta, c->p.offsetx, c->p.offsety, c->reg, c->d_err, c->st);
 }
 
@@ -664,8 +680,14 @@ static cudaGraph_t capture_graph(cudaStream_t st) {
   return g;
 }
 
+// The Schur operator the Krylov solver applies: the assembled matrix when the influence
+// matrix is active, else the matrix-free operator.
+static int schur_mv(Ctx* c, bool dense, const double* x, double* y) {
+  return dense ? inf_dense_mv(c, x, y, true) : op_schur(c, x, y, true);
+}
+
 // Builds the graph of a whole GMRES solve (KSPSolve, timestepper.F90:363-366) on gm_b/gm_x.
-static int build_solve_graph(Ctx* c) {
+static int build_solve_graph(Ctx* c, bool dense) {
   const GmresDev& G = c->G;
   const int max_it = c->p.gmres_max_it;
   const double rtol = c->p.rtol, atol = c->p.atol;
@@ -692,8 +714,8 @@ static int build_solve_graph(Ctx* c) {
       c->st = s1;
       rc = launch_copy(c->nf, c->gm_x, G.xin, s1);
       long long l0 = launch_count();
-      if (rc == IB_OK) rc = op_schur(c, G.xin, G.Av, true);
-      c->kernels_per_matvec = launch_count() - l0;
+      if (rc == IB_OK) rc = schur_mv(c, dense, G.xin, G.Av);
+      (dense ? c->kernels_per_matvec_dense : c->kernels_per_matvec) = launch_count() - l0;
       c->n_matvec -= 1;  // capture only
       if (rc == IB_OK) rc = launch_gmres_start(G, c->gm_b, c->gm_x, rtol, atol, max_it, s1, h_in, 1);
       if (rc == IB_OK) rc = add_while(s1, h_in, &inner);
@@ -701,7 +723,7 @@ static int build_solve_graph(Ctx* c) {
         rc = IB_ERR_CUDA;
       if (rc == IB_OK) {
         c->st = s2;
-        rc = op_schur(c, G.xin, G.Av, true);
+        rc = schur_mv(c, dense, G.xin, G.Av);
         c->n_matvec -= 1;
         if (rc == IB_OK) rc = launch_gmres_arnoldi(G, max_it, s2, h_in, 1);
         cudaGraph_t tmp;
@@ -714,12 +736,13 @@ static int build_solve_graph(Ctx* c) {
     }
     c->st = st;
     if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
-    if (rc == IB_OK && cudaGraphInstantiate(&c->solve_exec, graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+    if (rc == IB_OK && cudaGraphInstantiate(dense ? &c->solve_exec_dense : &c->solve_exec, graph, 0) != cudaSuccess)
+      rc = IB_ERR_CUDA;
   } while (false);
   c->st = st;
   c->prof_on = prof;
   cudaGetLastError();
-  if (rc == IB_OK) c->solve_graph = graph;
+  if (rc == IB_OK) (dense ? c->solve_graph_dense : c->solve_graph) = graph;
   else if (graph) cudaGraphDestroy(graph);
   cudaStreamDestroy(s1);
   cudaStreamDestroy(s2);
@@ -730,17 +753,20 @@ static int build_solve_graph(Ctx* c) {
 int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason) {
   const GmresDev& G = c->G;
   const int max_it = c->p.gmres_max_it;
+  const bool dense = c->inf.active;
   if (c->use_graph && !c->prof_on && !c->graph_failed) {
-    if (!c->solve_exec && build_solve_graph(c) != IB_OK) c->graph_failed = true;
-    if (c->solve_exec) {
+    cudaGraphExec_t& exec = dense ? c->solve_exec_dense : c->solve_exec;
+    if (!exec && build_solve_graph(c, dense) != IB_OK) c->graph_failed = true;
+    if (exec) {
       if (b != c->gm_b) IB_CUDA_CHECK(cudaMemcpyAsync(c->gm_b, b, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
       if (x != c->gm_x) IB_CUDA_CHECK(cudaMemcpyAsync(c->gm_x, x, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
-      IB_CUDA_CHECK(cudaGraphLaunch(c->solve_exec, c->st));
+      IB_CUDA_CHECK(cudaGraphLaunch(exec, c->st));
       if (x != c->gm_x) IB_CUDA_CHECK(cudaMemcpyAsync(x, c->gm_x, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
       RC(read_ist(c));
       long long it = c->h_ist[0], cycles = c->h_ist[4];
       c->n_matvec += it + cycles;
-      count_launches((it + cycles) * c->kernels_per_matvec + it + 3 * cycles + 1);
+      count_launches((it + cycles) * (dense ? c->kernels_per_matvec_dense : c->kernels_per_matvec) + it +
+                     3 * cycles + 1);
       *its = (int)it;
       *reason = c->h_ist[1];
       return IB_OK;
@@ -749,12 +775,12 @@ int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason) {
   RC(launch_gmres_init(G, c->st));
   for (;;) {
     IB_CUDA_CHECK(cudaMemcpyAsync(G.xin, x, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
-    RC(op_schur(c, G.xin, G.Av, true));
+    RC(schur_mv(c, dense, G.xin, G.Av));
     RC(launch_gmres_start(G, b, x, c->p.rtol, c->p.atol, max_it, c->st));
     RC(read_ist(c));
     if (c->h_ist[1] != 0) break;
     for (;;) {
-      RC(op_schur(c, G.xin, G.Av, true));
+      RC(schur_mv(c, dense, G.xin, G.Av));
       RC(launch_gmres_arnoldi(G, max_it, c->st));
       RC(read_ist(c));
       if (!c->h_ist[3]) break;
@@ -824,13 +850,25 @@ int op_advance(Ctx* c) {
         RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, st));
         RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, st));
         int its = 0, reason = 0;
+        RC(inf_prepare(c));
         RC(op_gmres(c, c->rhsf, c->f, &its, &reason));
         c->ksp_iter += its;
         RC(op_redistribute(c, c->f, c->f_rdst));
         RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, st));
-        if (c->nt > 0) RC(op_reg_prep(c));
+        const bool moved = c->nt > 0;
+        if (moved) RC(op_reg_prep(c));
+        // the next solve's patches, checked against the band with the same synchronisation
+        const bool patch = moved && p.schur_mode == 0 && c->inf.built;
+        if (patch) {
+          RC(inf_patch(c));
+          IB_CUDA_CHECK(cudaMemcpyAsync(c->inf.h_flag, c->inf.flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        }
         IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st));
         IB_CUDA_CHECK(cudaStreamSynchronize(st));
+        if (patch) {
+          c->inf.flag_h = c->inf.h_flag[0];
+          c->inf.patch_fresh = true;
+        }
         err = c->h_scal[0];
         if (!std::isfinite(err)) return IB_ERR_NONFINITE;
       }

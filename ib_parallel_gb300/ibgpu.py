@@ -39,6 +39,7 @@ EXPORTS = [
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
     "ib_launch_count", "ib_probe_throughput", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
+    "ib_schur_matrix", "ib_get_influence_stats",
 ]
 
 
@@ -53,7 +54,7 @@ class IbParams(C.Structure):
                 ("fsi_tol", C.c_double), ("atol", C.c_double), ("rtol", C.c_double),
                 ("num_stat", C.c_int), ("motion", C.c_double * 5),
                 ("gmres_restart", C.c_int), ("gmres_max_it", C.c_int), ("fsi_max_it", C.c_int),
-                ("autotune", C.c_int)]
+                ("autotune", C.c_int), ("schur_mode", C.c_int), ("influence_margin", C.c_int)]
 
 
 class IbBody(C.Structure):
@@ -106,6 +107,8 @@ def load(path: Optional[os.PathLike] = None):
         "ib_time_pass": ([P, C.c_int, C.c_int, D], C.c_int),
         "ib_profile_schur": ([P, C.c_int, D], C.c_int),
         "ib_ctci_static": ([C.c_int, C.c_int, P, P, P], C.c_int),
+        "ib_schur_matrix": ([P, P, C.POINTER(C.c_int)], C.c_int),
+        "ib_get_influence_stats": ([P, C.POINTER(C.c_longlong), D], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -196,6 +199,8 @@ class Params:
     gmres_max_it: int = 10000
     fsi_max_it: int = 1000
     autotune: bool = True
+    schur_mode: int = 0          # 0 influence matrix (matrix-free fallback), 1 matrix-free
+    influence_margin: int = 0    # band slack in vertices (0: 8)
 
     def to_c(self) -> IbParams:
         p = IbParams()
@@ -205,6 +210,8 @@ class Params:
             setattr(p, k, float(getattr(self, k)))
         p.num_stat = int(bool(self.num_stat))
         p.autotune = int(bool(self.autotune))
+        p.schur_mode = int(self.schur_mode)
+        p.influence_margin = int(self.influence_margin)
         for i in range(5):
             p.motion[i] = float(self.motion[i])
         return p
@@ -314,6 +321,21 @@ class Simulation:
         out = (C.c_double * 8)()
         _check(self.lib.ib_profile_schur(self.h, reps, out), "ib_profile_schur")
         return {n: 1e3 * out[i] / reps for i, n in enumerate(self.SCHUR_STAGES)}
+
+    def schur_matrix(self):
+        """Assembled fluid Schur matrix (nf x nf) from the influence matrix, or None when the
+        solver falls back to the matrix-free operator at the current positions."""
+        S = np.zeros((self.nf, self.nf))
+        st = C.c_int(0)
+        _check(self.lib.ib_schur_matrix(self.h, _ptr(S), C.byref(st)), "ib_schur_matrix")
+        return S if st.value == 0 else None
+
+    def influence_stats(self) -> dict:
+        counts = (C.c_longlong * 5)()
+        ms = C.c_double()
+        _check(self.lib.ib_get_influence_stats(self.h, counts, C.byref(ms)), "ib_get_influence_stats")
+        return {"builds": counts[0], "columns": counts[1], "assemblies": counts[2], "fallbacks": counts[3],
+                "band_vertices": counts[4], "build_ms": ms.value}
 
     def profile(self, enable: bool):
         _check(self.lib.ib_profile(self.h, int(bool(enable))), "ib_profile")

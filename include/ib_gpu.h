@@ -47,6 +47,14 @@ typedef struct IbParams {
   int gmres_max_it;   /* PETSc default 10000 */
   int fsi_max_it;     /* timestepper.F90:318 iterates while fsi_count <= 1000 */
   int autotune;       /* pick DST launch shapes by timing at ib_create */
+  /* How GMRES applies the Schur operator of moving (torsional) bodies.  0: through an
+   * influence matrix -- the fluid's vorticity-to-streamfunction map restricted to a band of
+   * vertices around the bodies, computed once and rebuilt when a body leaves the band -- from
+   * which each FSI iteration assembles the dense nf x nf operator (same operator as the
+   * matrix-free one up to round-off); solves whose stencils touch the domain boundary fall back
+   * to the matrix-free operator.  1: always matrix-free (a_times2 per Krylov iteration). */
+  int schur_mode;
+  int influence_margin; /* vertices of slack around the stencils in the band (0: 8) */
 } IbParams;
 
 /* One input/body.NNN.inp (grid.F90:252-288).  fam: 1 rigid, 2 torsional.
@@ -159,6 +167,16 @@ int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);
  * operator: reg+rot, ainv, coarsify, coarse levels, finest forward, finest solve, finest
  * inverse rows, E curl + B */
 int ib_profile_schur(IbCtx* ctx, int reps, double* stage_ms);
+/* Fluid part of the Schur matrix (a_times2 without B, operators_fluid.F90:14-120: the matrix
+ * timestepper.F90:560-598 builds column by column for stationary bodies) at the current body
+ * positions, assembled from the influence matrix (schur_mode 0; built on first use):
+ * S[k*nf + l].  *status is 0 when S was assembled; nonzero when the stencils touch the domain
+ * boundary or the band does not fit in memory (the solver then uses the matrix-free operator
+ * and S is not written). */
+int ib_schur_matrix(IbCtx* ctx, double* S, int* status);
+/* influence-matrix work since creation: counts = {band builds, columns computed, assemblies,
+ * matrix-free fallbacks, band vertices}, build_ms = host wall time of the builds */
+int ib_get_influence_stats(IbCtx* ctx, long long* counts, double* build_ms);
 /* enable (1) / disable (0) CUDA-event timing of each DST pass launch; enabling clears the totals */
 int ib_profile(IbCtx* ctx, int enable);
 /* work done since creation: Schur matvecs and DST passes by kind (0..3, see below) */
