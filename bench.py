@@ -339,6 +339,7 @@ def run_gpu(args, world, rank, local):
         "tridiagonal_pass_us": 1e3 * t_tri,
         "schur_stages_us": sim.profile_schur(20),
         "influence": sim.influence_stats(),
+        "step_phases_us": _step_phases(sim, 5),
     }
     if not args.no_matrix_free:
         result["matrix_free"] = _matrix_free_rate(p, bodies, args)
@@ -359,6 +360,16 @@ def run_gpu(args, world, rank, local):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def _step_phases(sim, steps):
+    """Device time per step of each phase of ib_advance (CUDA events), over a few more steps."""
+    sim.step_profile(1)
+    for _ in range(steps):
+        sim.advance()
+    out = sim.step_profile(0)
+    out["steps"] = steps
+    return out
 
 
 def _matrix_free_rate(p, bodies, args):

@@ -503,11 +503,17 @@ int ib_profile_schur(IbCtx* h, int reps, double* stage_ms) {
   return op_result(ib::op_profile_schur(c, reps, stage_ms), "profile_schur failed");
 }
 
+int ib_step_profile(IbCtx* h, int mode, double* phase_ms, long long* nsteps) {
+  CTX_OR_FAIL(h);
+  if (mode < 0 || mode > 2) return fail(IB_ERR_ARG, "bad mode");
+  return op_result(ib::op_step_profile(c, mode, phase_ms, nsteps), "step_profile failed");
+}
+
 int ib_schur_matrix(IbCtx* h, double* S, int* status) {
   CTX_OR_FAIL(h);
   if (!S || !status) return fail(IB_ERR_ARG, "bad argument");
   if (c->nf == 0) return fail(IB_ERR_STATE, "no body unknowns");
-  if (c->p.schur_mode != 0) return fail(IB_ERR_STATE, "influence matrix disabled (schur_mode 1)");
+  if (c->p.schur_mode == 1) return fail(IB_ERR_STATE, "influence matrix disabled (schur_mode 1)");
   int rc = ib::inf_prepare(c);
   if (rc != IB_OK) return op_result(rc, "influence matrix failed");
   *status = c->inf.active ? 0 : (c->inf.flag_h ? c->inf.flag_h : 4);

@@ -58,7 +58,11 @@ struct Influence {
   double* T = nullptr;        // nf rows of nR: T[l][u] = (K P)[ulist[u]][l]
   double* pval = nullptr;     // nf*64 patch values
   int* pidx = nullptr;        // nf*64 patch band indices (-1: none)
-  double* S = nullptr;        // nf x nf row-major fluid Schur matrix
+  double* S = nullptr;        // nf x nf row-major fluid Schur matrix (P^T K P)
+  double* St = nullptr;       // nf x nf column-major operator the solver applies: S + B
+  double* brv = nullptr;      // nf: BR entry of each torsional unknown
+  double* bco = nullptr;      // nf: b_times2 coefficient of the unknown's body
+  int* bod = nullptr;         // nf: torsional body of the unknown, -1 for rigid ones
   int* flag = nullptr;
   int* h_flag = nullptr;      // pinned
   int* rr_in = nullptr;       // row ranges of the precompute (3 ints each)
@@ -119,6 +123,7 @@ struct Ctx {
   // while(Arnoldi){ matvec; arnoldi } update } on the fixed buffers gm_b (rhs), gm_x (solution)
   double *gm_b = nullptr, *gm_x = nullptr;
   bool use_graph = true;
+  bool use_fused = true;           // one-kernel GMRES on the assembled operator
   bool graph_failed = false;
   cudaGraphExec_t solve_exec = nullptr;         // matrix-free operator
   cudaGraph_t solve_graph = nullptr;
@@ -149,6 +154,15 @@ struct Ctx {
   bool stage_on = false;
   cudaEvent_t stage_ev[kStages + 1] = {};
   double stage_ms[kStages] = {0};
+
+  // optional phase timing of the time step (ib_step_profile): 0 predictor, 1 vort2flux,
+  // 2 FSI right-hand side, 3 Schur assembly, 4 GMRES, 5 FSI update (redistribute, structure,
+  // weights, synchronisation), 6 correction
+  static constexpr int kStepPhases = 7;
+  bool step_prof = false;
+  cudaEvent_t step_ev[10] = {};
+  double step_ms[kStepPhases] = {0};
+  long long step_n = 0;
 
   // optional CUDA-event timing of DST passes (ib_profile)
   static constexpr int kProfMax = 8192;
@@ -184,7 +198,7 @@ int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
 int inf_patch(Ctx* c);                 // patches + flag for the current weights (async)
 int inf_prepare(Ctx* c);               // build/rebuild the band if needed, assemble S
-int inf_dense_mv(Ctx* c, const double* x, double* y, bool with_b);
+int inf_dense_mv(Ctx* c, const double* x, double* y);   // (S + B) x
 int inf_build(Ctx* c);
 int op_redistribute(Ctx* c, const double* f, double* frdst);
 int op_reg_prep(Ctx* c);
@@ -192,6 +206,7 @@ int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms);
 int op_profile_schur(Ctx* c, int reps, double* ms);
 int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason);
 int op_advance(Ctx* c);
+int op_step_profile(Ctx* c, int mode, double* ms, long long* nsteps);
 int check_err(Ctx* c);
 
 }  // namespace ib

@@ -317,4 +317,214 @@ int launch_unit(int n, int i, double* e, cudaStream_t st) {
   return IB_OK;
 }
 
+// ---------------------------------------------------------------- fused dense solve
+namespace {
+struct FusedSmem {
+  int nf, R;
+  size_t base_doubles() const {
+    return (size_t)(R + 1) * nf + 3 * (size_t)nf + (size_t)(R + 1) * R + 5 * (size_t)(R + 1) + 33;
+  }
+  size_t with_a() const { return base_doubles() + (size_t)nf * nf; }
+};
+}  // namespace
+
+// One CTA of 32*ceil(nf/32) threads (one vector element per thread), so every scalar FP64
+// recurrence and reduction runs on the fewest warps: an FP64 warp instruction occupies its
+// SMSP's FP64 pipe for the same time whatever the number of active lanes.  Thread i
+// handles element i in every vector loop, as the 512-thread kernels do, and the block sums
+// reduce the same per-warp partials in the same order (the extra warps of those kernels add
+// zeros), so both solvers produce identical iterates.
+__global__ void k_gmres_fused(GmresDev G, const double* __restrict__ Atg, int a_in_smem, const double* __restrict__ b,
+                              double* __restrict__ x, double rtol, double atol, int max_it) {
+  extern __shared__ double sm[];
+  __shared__ int s_reason;
+  __shared__ double s_res;
+  const int nf = G.nf, R = G.restart;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  double* V = sm;                           // (R+1) x nf
+  double* Av = V + (size_t)(R + 1) * nf;    // nf
+  double* xs = Av + nf;                     // nf
+  double* bs = xs + nf;                     // nf
+  double* H = bs + nf;                      // (R+1) x R, column it at H + it*(R+1)
+  double* cs = H + (size_t)(R + 1) * R;     // R+1
+  double* sn = cs + (R + 1);
+  double* g = sn + (R + 1);
+  double* h = g + (R + 1);
+  double* yv = h + (R + 1);
+  double* red = yv + (R + 1);               // 33
+  double* As = red + 33;
+  const double* At = a_in_smem ? As : Atg;
+  if (a_in_smem)
+    for (int i = tid; i < nf * nf; i += blockDim.x) As[i] = Atg[i];
+  for (int i = tid; i < nf; i += blockDim.x) {
+    xs[i] = x[i];
+    bs[i] = b[i];
+  }
+  __syncthreads();
+
+  // out = A in, A column-major, one thread per row (k_dense_mv)
+  auto matvec = [&](const double* in, double* out) {
+    for (int r = tid; r < nf; r += blockDim.x) {
+      double acc = 0.0;
+      for (int j = 0; j < nf; ++j) acc = fma(At[(size_t)j * nf + r], in[j], acc);
+      out[r] = acc;
+    }
+    __syncthreads();
+  };
+
+  int its = 0, cycles = 0, reason = 0, it = 0;
+  double ttol = 0.0;
+  for (;;) {
+    // cycle start (k_gmres_start): r = b - A x, V0 = r/||r||
+    matvec(xs, Av);
+    double pr = 0.0, pb = 0.0;
+    for (int i = tid; i < nf; i += blockDim.x) {
+      double r = bs[i] - Av[i];
+      V[i] = r;
+      pr += r * r;
+      pb += bs[i] * bs[i];
+    }
+    const double rnorm = sqrt(blk_sum(pr, red));
+    const double bnorm = sqrt(blk_sum(pb, red));
+    if (its == 0) {
+      double rnorm0 = bnorm != 0.0 ? bnorm : rnorm;
+      ttol = fmax(rtol * rnorm0, atol);
+    }
+    const double inv0 = rnorm != 0.0 ? 1.0 / rnorm : 0.0;
+    for (int i = tid; i < nf; i += blockDim.x) V[i] = rnorm != 0.0 ? V[i] * inv0 : V[i];
+    cycles += 1;
+    it = 0;
+    reason = 0;
+    if (rnorm == 0.0) reason = 2;
+    else if (rnorm <= ttol) reason = 3;
+    else if (its >= max_it) reason = -3;
+    if (tid == 0) {
+      g[0] = rnorm;
+      s_res = rnorm;
+    }
+    __syncthreads();
+    if (reason != 0) break;
+    // Arnoldi steps (k_gmres_arnoldi)
+    for (;;) {
+      matvec(V + (size_t)it * nf, Av);
+      for (int j = warp; j <= it; j += nwarps) {
+        const double* vj = V + (size_t)j * nf;
+        double p = 0.0;
+        for (int i = lane; i < nf; i += 32) p += Av[i] * vj[i];
+        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+        if (lane == 0) h[j] = p;
+      }
+      __syncthreads();
+      double* w = V + (size_t)(it + 1) * nf;
+      double pn = 0.0;
+      for (int i = tid; i < nf; i += blockDim.x) {
+        double v = Av[i];
+        for (int j = 0; j <= it; ++j) v = v - h[j] * V[(size_t)j * nf + i];
+        w[i] = v;
+        pn += v * v;
+      }
+      const double tt = sqrt(blk_sum(pn, red));
+      const double inv = tt != 0.0 ? 1.0 / tt : 0.0;
+      for (int i = tid; i < nf; i += blockDim.x) w[i] = tt != 0.0 ? w[i] * inv : w[i];
+      if (tid == 0) {
+        double* col = H + (size_t)it * (R + 1);
+        for (int j = 0; j <= it; ++j) col[j] = h[j];
+        col[it + 1] = tt;
+        double hapbnd = fabs(tt / g[it]);
+        if (hapbnd > 1.0e-30) hapbnd = 1.0e-30;
+        bool hapend = tt < hapbnd;
+        for (int j = 0; j < it; ++j) {
+          double t0 = col[j];
+          col[j] = cs[j] * t0 + sn[j] * col[j + 1];
+          col[j + 1] = cs[j] * col[j + 1] - sn[j] * t0;
+        }
+        double res;
+        int rsn = 0;
+        if (!hapend) {
+          double nrm = sqrt(col[it] * col[it] + col[it + 1] * col[it + 1]);
+          if (nrm == 0.0) {
+            rsn = -9;
+            res = s_res;
+          } else {
+            cs[it] = col[it] / nrm;
+            sn[it] = col[it + 1] / nrm;
+            g[it + 1] = -(sn[it] * g[it]);
+            g[it] = cs[it] * g[it];
+            col[it] = cs[it] * col[it] + sn[it] * col[it + 1];
+            res = fabs(g[it + 1]);
+          }
+        } else {
+          res = 0.0;
+        }
+        if (rsn == 0) {
+          if (res <= ttol) rsn = 2;
+          else if (hapend) rsn = -3;
+        }
+        s_res = res;
+        s_reason = rsn;
+      }
+      __syncthreads();
+      reason = s_reason;
+      it += 1;
+      its += 1;
+      if (reason != 0 || it >= R || its >= max_it) break;
+    }
+    // KSPGMRESBuildSoln (k_gmres_update): back substitution and x += V y
+    if (tid == 0 && it > 0) {
+      int k = it - 1;
+      auto HH = [&](int r, int c) { return H[(size_t)c * (R + 1) + r]; };
+      yv[k] = g[k] / HH(k, k);
+      for (int i = k - 1; i >= 0; --i) {
+        double tt = g[i];
+        for (int j = i + 1; j <= k; ++j) tt = tt - HH(i, j) * yv[j];
+        yv[i] = tt / HH(i, i);
+      }
+    }
+    __syncthreads();
+    if (it > 0) {
+      for (int i = tid; i < nf; i += blockDim.x) {
+        double u = 0.0;
+        for (int j = 0; j < it; ++j) u = u + yv[j] * V[(size_t)j * nf + i];
+        xs[i] = xs[i] + u;
+      }
+    }
+    __syncthreads();
+    if (reason != 0 || its >= max_it) break;
+  }
+  for (int i = tid; i < nf; i += blockDim.x) x[i] = xs[i];
+  if (tid == 0) {
+    G.ist[0] = its;
+    G.ist[1] = reason;
+    G.ist[2] = it;
+    G.ist[3] = 0;
+    G.ist[4] = cycles;
+    G.scal[0] = ttol;
+    G.scal[1] = s_res;
+  }
+}
+
+int launch_gmres_fused(const GmresDev& G, const double* At, const double* b, double* x, double rtol, double atol,
+                       int max_it, cudaStream_t st) {
+  // one element per thread and the same element-to-warp map as the 512-thread kernels
+  if (G.nf <= 0 || G.nf > kGmresThreads) return IB_ERR_ARG;
+  const int threads = 32 * ((G.nf + 31) / 32);
+  FusedSmem fs{G.nf, G.restart};
+  int dev = 0, optin = 0;
+  IB_CUDA_CHECK(cudaGetDevice(&dev));
+  IB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t limit = (size_t)optin - 1024;   // static shared memory of the kernel and the reductions
+  int a_in = 1;
+  size_t bytes = 8 * fs.with_a();
+  if (bytes > limit) {
+    a_in = 0;
+    bytes = 8 * fs.base_doubles();
+    if (bytes > limit) return IB_ERR_ARG;
+  }
+  IB_CUDA_CHECK(cudaFuncSetAttribute(k_gmres_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  count_launch();
+  k_gmres_fused<<<1, threads, bytes, st>>>(G, At, a_in, b, x, rtol, atol, max_it);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
 }  // namespace ib

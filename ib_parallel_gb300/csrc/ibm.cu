@@ -48,37 +48,48 @@ __device__ double deltafnc_dev(double x1, double x2, double dr) {
   return v / dr;
 }
 
-// Per unknown: stencil origin and the 49 weights (l outer, p inner).
+// Per unknown (one warp): stencil origin and the 49 weights (l outer, p inner).  Lanes 0-6
+// evaluate the x factors, lanes 7-13 the y factors (one delta function each, so the
+// FP64-latency-bound evaluations run side by side), then every lane writes weights.
 __global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb, const double* __restrict__ yb,
                               double d, double ox, double oy, const int* __restrict__ comp, int* ix, int* iy,
                               double* w, int* err) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (k >= nf) return;
-  double xk = xb[k], yk = yb[k];
-  int cx = (int)((xk + ox) / d) + 1;   // Fortran INT truncates toward zero
-  int cy = (int)((yk + oy) / d) + 1;
-  ix[k] = cx;
-  iy[k] = cy;
+  const double xk = xb[k], yk = yb[k];
+  const int cx = (int)((xk + ox) / d) + 1;   // Fortran INT truncates toward zero
+  const int cy = (int)((yk + oy) / d) + 1;
   const double d2 = 0.5 * d;
-  bool isx = comp[k] == 1;
-  // faces touched: u-face i in [1,m+1], j in [1,n]; v-face i in [1,m], j in [1,n+1]
-  int imax = isx ? g.m + 1 : g.m, jmax = isx ? g.n : g.n + 1;
-  if (cx - 3 < 1 || cx + 3 > imax || cy - 3 < 1 || cy + 3 > jmax) atomicExch(err, IB_ERR_DOMAIN);
-  double dx[7], dy[7];
-#pragma unroll
-  for (int q = 0; q < 7; ++q) {
-    int off = q - 3;
-    double x = d * (double)(cx - 1 + off) - ox;
-    double y = d * (double)(cy - 1 + off) - oy;
-    if (isx) y = y + d2; else x = x + d2;
-    dx[q] = deltafnc_dev(x, xk, d);
-    dy[q] = deltafnc_dev(y, yk, d);
+  const bool isx = comp[k] == 1;
+  if (lane == 0) {
+    ix[k] = cx;
+    iy[k] = cy;
+    // faces touched: u-face i in [1,m+1], j in [1,n]; v-face i in [1,m], j in [1,n+1]
+    int imax = isx ? g.m + 1 : g.m, jmax = isx ? g.n : g.n + 1;
+    if (cx - 3 < 1 || cx + 3 > imax || cy - 3 < 1 || cy + 3 > jmax) atomicExch(err, IB_ERR_DOMAIN);
+  }
+  double f = 0.0;
+  if (lane < 14) {
+    const int q = lane % 7, off = q - 3;
+    if (lane < 7) {
+      double x = d * (double)(cx - 1 + off) - ox;
+      if (!isx) x = x + d2;
+      f = deltafnc_dev(x, xk, d);
+    } else {
+      double y = d * (double)(cy - 1 + off) - oy;
+      if (isx) y = y + d2;
+      f = deltafnc_dev(y, yk, d);
+    }
   }
   double* wk = w + (size_t)k * 49;
-#pragma unroll
-  for (int l = 0; l < 7; ++l)
-#pragma unroll
-    for (int p = 0; p < 7; ++p) wk[l * 7 + p] = d * d * dx[p] * dy[l];
+  for (int base = 0; base < 49; base += 32) {   // same trip count on every lane (shuffles)
+    const int sl = base + lane;
+    const int l = sl < 49 ? sl / 7 : 0, p = sl < 49 ? sl % 7 : 0;
+    const double dxp = __shfl_sync(0xffffffffu, f, p);
+    const double dyl = __shfl_sync(0xffffffffu, f, 7 + l);
+    if (sl < 49) wk[sl] = d * d * dxp * dyl;
+  }
 }
 
 // Bounding box of all stencils (one CTA).  bbox[0..3] = i0, j0, ni, nj of the face box;
@@ -145,26 +156,37 @@ __global__ void k_reg_lists(int nf, const int* __restrict__ comp, const int* __r
   }
 }
 
-// Exclusive scan of both count arrays (one CTA, 1024 threads).
+// Exclusive scan of both count arrays (one CTA, 1024 threads): each thread sums a run of
+// consecutive faces, the runs are scanned with warp shuffles, then written back.
 __global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y, int max_faces) {
-  __shared__ int part[1024];
-  int nface = bbox[2] * bbox[3];
+  __shared__ int wsum[32];
+  const int nface = bbox[2] * bbox[3];
   if (nface + 1 > max_faces) return;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   for (int c = 0; c < 2; ++c) {
     int* cnt = c == 0 ? cnt_x : cnt_y;
-    int per = (nface + blockDim.x - 1) / blockDim.x;
-    int s0 = threadIdx.x * per, s1 = min(s0 + per, nface);
+    const int per = (nface + blockDim.x - 1) / blockDim.x;
+    const int s0 = min(tid * per, nface), s1 = min(s0 + per, nface);
     int sum = 0;
     for (int i = s0; i < s1; ++i) sum += cnt[i];
-    part[threadIdx.x] = sum;
+    int inc = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[wid] = inc;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int run = 0;
-      for (int q = 0; q < (int)blockDim.x; ++q) { int v = part[q]; part[q] = run; run += v; }
-      cnt[nface] = run;
+    if (wid == 0) {
+      int v = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0, winc = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, winc, o);
+        if (lane >= o) winc += y;
+      }
+      wsum[lane] = winc - v;
+      if (lane == 31) cnt[nface] = winc;
     }
     __syncthreads();
-    int run = part[threadIdx.x];
+    int run = wsum[wid] + inc - sum;
     for (int i = s0; i < s1; ++i) { int v = cnt[i]; cnt[i] = run; run += v; }
     __syncthreads();
   }
@@ -174,7 +196,8 @@ int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* 
                      double offy, RegDev& r, int* d_err, cudaStream_t st) {
   if (nf == 0) return IB_OK;
   count_launch();
-  k_reg_weights<<<cdiv(nf, 128), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w, d_err);
+  k_reg_weights<<<cdiv(32LL * nf, 128), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w,
+                                                       d_err);
   count_launch();
   k_reg_bbox<<<1, 256, 0, st>>>(g, nf, r.ix, r.iy, r.bbox);
   count_launch();

@@ -125,9 +125,29 @@ __global__ void k_inf_kp(int nR, const double* __restrict__ K, const double* __r
   T[(size_t)l * nR + u] = acc;
 }
 
-// S[k][l] = sum_q P[q,k] T[l][upos(src_q)]  (E curl = P^T), one CTA per row k.
+// BR rows and b_times2 coefficients of the torsional unknowns (one warp per body), so that
+// the rank-one B of b_times2 (operators_struct.F90:14-127) can be added to the matrix:
+// B[k][l] = BR_k BR_l (delta^2/ds/dt)(2 ds/dt) / K_eff for k, l on the same body.
+__global__ void k_inf_bvec(const TorsBody* __restrict__ tb, TorsState ts, double dt, double delta,
+                           double* __restrict__ brv, double* __restrict__ bco, int* __restrict__ bod) {
+  const int t = blockIdx.x;
+  const TorsBody b = tb[t];
+  const double th = ts.theta[t];
+  const double sv = sin(b.gamma0 - th), cv = cos(b.gamma0 - th);
+  const double co = btimes_scale(b, dt, delta) / keff(b, dt);
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) {
+    brv[b.off + j] = br_val(b, sv, cv, j);
+    bco[b.off + j] = co;
+    bod[b.off + j] = t;
+  }
+}
+
+// S[k][l] = sum_q P[q,k] T[l][upos(src_q)]  (E curl = P^T), one CTA per row k; also the
+// solver's column-major operator St[l][k] = S[k][l] + B[k][l].
 __global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const int* __restrict__ pidx,
-                          const int* __restrict__ upos, const double* __restrict__ T, double* __restrict__ S) {
+                          const int* __restrict__ upos, const double* __restrict__ T,
+                          const double* __restrict__ brv, const double* __restrict__ bco,
+                          const int* __restrict__ bod, double* __restrict__ S, double* __restrict__ St) {
   __shared__ double sv[kP];
   __shared__ int su[kP];
   const int k = blockIdx.x;
@@ -137,6 +157,7 @@ __global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const
     su[threadIdx.x] = c >= 0 ? upos[c] : -1;
   }
   __syncthreads();
+  const int bk = bod[k];
   for (int l = threadIdx.x; l < nf; l += blockDim.x) {
     const double* Tl = T + (size_t)l * nR;
     double acc = 0.0;
@@ -145,19 +166,18 @@ __global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const
       if (u >= 0) acc = fma(sv[q], Tl[u], acc);
     }
     S[(size_t)k * nf + l] = acc;
+    const double bkl = (bk >= 0 && bod[l] == bk) ? brv[k] * brv[l] * bco[k] : 0.0;
+    St[(size_t)l * nf + k] = acc + bkl;
   }
 }
 
-// y = S x, one warp per row.
-__global__ void k_dense_mv(int n, const double* __restrict__ S, const double* __restrict__ x, double* __restrict__ y) {
-  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const double* Sr = S + (size_t)row * n;
+// y = A x with A column-major (At[j][r] = A[r][j]): one thread per row, summing in j order.
+__global__ void k_dense_mv(int n, const double* __restrict__ At, const double* __restrict__ x, double* __restrict__ y) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
   double acc = 0.0;
-  for (int j = lane; j < n; j += 32) acc = fma(Sr[j], x[j], acc);
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) y[row] = acc;
+  for (int j = 0; j < n; ++j) acc = fma(At[(size_t)j * n + r], x[j], acc);
+  y[r] = acc;
 }
 
 // Column c of the precompute: unit vorticity at band vertex c (the previous one cleared),
@@ -200,6 +220,10 @@ int inf_alloc(Ctx* c) {
   IB_CUDA_CHECK(cudaMalloc(&I.pval, sizeof(double) * (size_t)nf * kP));
   IB_CUDA_CHECK(cudaMalloc(&I.pidx, sizeof(int) * (size_t)nf * kP));
   IB_CUDA_CHECK(cudaMalloc(&I.S, sizeof(double) * (size_t)nf * nf));
+  IB_CUDA_CHECK(cudaMalloc(&I.St, sizeof(double) * (size_t)nf * nf));
+  IB_CUDA_CHECK(cudaMalloc(&I.brv, sizeof(double) * (size_t)nf));
+  IB_CUDA_CHECK(cudaMalloc(&I.bco, sizeof(double) * (size_t)nf));
+  IB_CUDA_CHECK(cudaMalloc(&I.bod, sizeof(int) * (size_t)nf));
   IB_CUDA_CHECK(cudaMalloc(&I.flag, sizeof(int) * 16));
   I.nu = I.flag + 4;
   I.rr_in = I.flag + 8;
@@ -229,6 +253,10 @@ void inf_free(Ctx* c) {
   if (I.pval) cudaFree(I.pval);
   if (I.pidx) cudaFree(I.pidx);
   if (I.S) cudaFree(I.S);
+  if (I.St) cudaFree(I.St);
+  if (I.brv) cudaFree(I.brv);
+  if (I.bco) cudaFree(I.bco);
+  if (I.bod) cudaFree(I.bod);
   if (I.flag) cudaFree(I.flag);
   if (I.tile_of) cudaFree(I.tile_of);
   if (I.h_flag) cudaFreeHost(I.h_flag);
@@ -347,7 +375,7 @@ int inf_build(Ctx* c) {
 int inf_prepare(Ctx* c) {
   Influence& I = c->inf;
   I.active = false;
-  if (c->p.schur_mode != 0 || c->nf == 0) return IB_OK;
+  if (c->p.schur_mode == 1 || c->nf == 0) return IB_OK;
   if (!I.patch_fresh) {
     RC(inf_patch(c));
     RC(read_flag(c));
@@ -366,20 +394,25 @@ int inf_prepare(Ctx* c) {
   k_inf_compact<<<1, 1024, 0, st>>>(I.nR, I.used, I.ulist, I.upos, I.nu);
   count_launch();
   k_inf_kp<<<dim3(cdiv(I.nR, 128), c->nf), 128, 0, st>>>(I.nR, I.K, I.pval, I.pidx, I.ulist, I.nu, I.T);
+  IB_CUDA_CHECK(cudaMemsetAsync(I.bod, 0xff, sizeof(int) * (size_t)c->nf, st));   // -1: no B term
+  if (c->nt > 0) {
+    count_launch();
+    k_inf_bvec<<<c->nt, 32, 0, st>>>(c->tb, c->ts, c->p.dt, c->delta, I.brv, I.bco, I.bod);
+  }
   count_launch();
-  k_inf_ptk<<<c->nf, 128, 0, st>>>(c->nf, I.nR, I.pval, I.pidx, I.upos, I.T, I.S);
+  k_inf_ptk<<<c->nf, 128, 0, st>>>(c->nf, I.nR, I.pval, I.pidx, I.upos, I.T, I.brv, I.bco, I.bod, I.S, I.St);
   IB_CUDA_CHECK(cudaGetLastError());
   I.assemblies += 1;
   I.active = true;
   return IB_OK;
 }
 
-int inf_dense_mv(Ctx* c, const double* x, double* y, bool with_b) {
+// y = (S + B) x from the assembled column-major operator (B is part of it).
+int inf_dense_mv(Ctx* c, const double* x, double* y) {
   c->n_matvec += 1;
   count_launch();
-  k_dense_mv<<<cdiv(32LL * c->nf, 256), 256, 0, c->st>>>(c->nf, c->inf.S, x, y);
+  k_dense_mv<<<cdiv(c->nf, 128), 128, 0, c->st>>>(c->nf, c->inf.St, x, y);
   IB_CUDA_CHECK(cudaGetLastError());
-  if (with_b) RC(launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, x, y, c->st));
   return IB_OK;
 }
 

@@ -59,6 +59,20 @@ struct TorsBody {
 struct TorsState {  // device arrays of length nt
   double *theta, *thetad, *thetadd, *theta0, *thetad0, *thetadd0;
 };
+// BR_build (operators_struct.F90:319-338): x-rows (j-1) ds sin(g0-th),
+// y-rows -(j-1) ds cos(g0-th).  sn, cs = sin, cos(g0-th), evaluated once per body.
+__device__ __forceinline__ double br_val(const TorsBody& b, double sn, double cs, int j) {
+  if (j < b.npts) return (double)j * b.deltas * sn;
+  return -(double)(j - b.npts) * b.deltas * cs;
+}
+// effective stiffness of the Newmark update (operators_struct.F90:402-505)
+__device__ __forceinline__ double keff(const TorsBody& b, double dt) {
+  return 4.0 / (dt * dt) * b.itheta + 2.0 / dt * b.ctheta + b.ktheta;
+}
+// b_times2 scale (delta^2/ds/dt)(2 ds/dt), operators_struct.F90:14-127
+__device__ __forceinline__ double btimes_scale(const TorsBody& b, double dt, double delta) {
+  return (delta * delta / b.deltas / dt) * (2.0 * b.deltas / dt);
+}
 int launch_tors_btimes(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, const double* x,
                        double* y, cudaStream_t st);
 int launch_tors_rhs(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, double* y,
@@ -92,6 +106,12 @@ int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st, cudaGra
 int launch_gmres_update(const GmresDev& G, double* x, int max_it, cudaStream_t st, cudaGraphConditionalHandle h = 0,
                         int use_cond = 0);
 int launch_copy(int n, const double* a, double* b, cudaStream_t st);
+// The whole solve in one CTA for a dense operator A, column-major (At[j*nf + r] = A[r][j]):
+// the operations of the start / arnoldi / update kernels in the same order, with A applied
+// one row per thread.  Writes G.ist like them.  Returns IB_ERR_ARG (nothing launched) when
+// nf exceeds 512 or the Krylov basis does not fit in shared memory.
+int launch_gmres_fused(const GmresDev& G, const double* At, const double* b, double* x, double rtol, double atol,
+                       int max_it, cudaStream_t st);
 
 // dense symmetric positive definite solve (stationary-body path)
 int launch_cholesky(int n, double* A, int* d_err, cudaStream_t st);

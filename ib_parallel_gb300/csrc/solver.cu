@@ -351,6 +351,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->lx_small.B = 1; c->lx_small.NT = 128;
   c->ly_none.B = 8; c->ly_none.NT = 160;
   c->tl.Mb = 8;
+  c->use_fused = p.schur_mode != 2;
   if (p.autotune) {
     rc = tune(c);
     if (rc != IB_OK) { *msg = "DST tuning failed"; ctx_destroy(c); return rc; }
@@ -683,7 +684,7 @@ static cudaGraph_t capture_graph(cudaStream_t st) {
 // The Schur operator the Krylov solver applies: the assembled matrix when the influence
 // matrix is active, else the matrix-free operator.
 static int schur_mv(Ctx* c, bool dense, const double* x, double* y) {
-  return dense ? inf_dense_mv(c, x, y, true) : op_schur(c, x, y, true);
+  return dense ? inf_dense_mv(c, x, y) : op_schur(c, x, y, true);
 }
 
 // Builds the graph of a whole GMRES solve (KSPSolve, timestepper.F90:363-366) on gm_b/gm_x.
@@ -754,6 +755,18 @@ int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason) {
   const GmresDev& G = c->G;
   const int max_it = c->p.gmres_max_it;
   const bool dense = c->inf.active;
+  if (dense && c->use_fused) {
+    // the whole solve in one kernel on the assembled matrix
+    int rc = launch_gmres_fused(G, c->inf.St, b, x, c->p.rtol, c->p.atol, max_it, c->st);
+    if (rc == IB_OK) {
+      RC(read_ist(c));
+      c->n_matvec += c->h_ist[0] + c->h_ist[4];
+      *its = c->h_ist[0];
+      *reason = c->h_ist[1];
+      return IB_OK;
+    }
+    if (rc != IB_ERR_ARG) return rc;
+  }
   if (c->use_graph && !c->prof_on && !c->graph_failed) {
     cudaGraphExec_t& exec = dense ? c->solve_exec_dense : c->solve_exec;
     if (!exec && build_solve_graph(c, dense) != IB_OK) c->graph_failed = true;
@@ -809,6 +822,34 @@ static int preprocess_chol(Ctx* c) {
   return IB_OK;
 }
 
+// mode 1: start (totals cleared), 0: stop, 2: read only.  ms[7] totals, *nsteps steps timed.
+int op_step_profile(Ctx* c, int mode, double* ms, long long* nsteps) {
+  if (mode == 1) {
+    for (auto& e : c->step_ev)
+      if (!e) IB_CUDA_CHECK(cudaEventCreate(&e));
+    for (double& v : c->step_ms) v = 0.0;
+    c->step_n = 0;
+    c->step_prof = true;
+  } else if (mode == 0) {
+    c->step_prof = false;
+  }
+  if (ms)
+    for (int i = 0; i < Ctx::kStepPhases; ++i) ms[i] = c->step_ms[i];
+  if (nsteps) *nsteps = c->step_n;
+  return IB_OK;
+}
+
+static void step_mark(Ctx* c, int i) {
+  if (c->step_prof) cudaEventRecord(c->step_ev[i], c->st);
+}
+
+// adds the time between events a and b (both complete) to phase ph
+static void step_acc(Ctx* c, int ph, int a, int b) {
+  if (!c->step_prof) return;
+  float t = 0.f;
+  if (cudaEventElapsedTime(&t, c->step_ev[a], c->step_ev[b]) == cudaSuccess) c->step_ms[ph] += t;
+}
+
 // timestepper.F90:18-556
 int op_advance(Ctx* c) {
   const GridDims& g = c->g;
@@ -818,6 +859,7 @@ int op_advance(Ctx* c) {
   c->itime += 1;
   const int it = c->itime;
   if (it == 1 && p.num_stat && c->nf > 0) RC(preprocess_chol(c));
+  step_mark(c, 0);
   // boundary values of the previous step (timestepper.F90:103-117)
   for (int k = 0; k < L - 1; ++k) RC(launch_get_bc(g, c->omega[k + 1], 0.25, c->lastbc[k], st));
   IB_CUDA_CHECK(cudaMemsetAsync(c->lastbc[L - 1], 0, 8 * (size_t)g.nbc, st));
@@ -835,7 +877,9 @@ int op_advance(Ctx* c) {
     RC(op_predictor(c, k, c->omega[k], c->rhs, c->rhs_old[k], c->rhsbc));
     IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs, 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, st));
   }
+  step_mark(c, 1);
   RC(op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true));
+  step_mark(c, 2);
   // forces (timestepper.F90:249-486)
   if (c->nf > 0) {
     if (!p.num_stat) {
@@ -846,25 +890,34 @@ int op_advance(Ctx* c) {
       c->ksp_iter = 0;
       while (err >= p.fsi_tol && fsi_count <= p.fsi_max_it) {
         fsi_count += 1;
+        step_mark(c, 3);
         IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, st));
         RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, st));
         RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, st));
         int its = 0, reason = 0;
+        step_mark(c, 4);
         RC(inf_prepare(c));
+        step_mark(c, 5);
         RC(op_gmres(c, c->rhsf, c->f, &its, &reason));
+        step_mark(c, 6);
         c->ksp_iter += its;
         RC(op_redistribute(c, c->f, c->f_rdst));
         RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, st));
         const bool moved = c->nt > 0;
         if (moved) RC(op_reg_prep(c));
         // the next solve's patches, checked against the band with the same synchronisation
-        const bool patch = moved && p.schur_mode == 0 && c->inf.built;
+        const bool patch = moved && p.schur_mode != 1 && c->inf.built;
         if (patch) {
           RC(inf_patch(c));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->inf.h_flag, c->inf.flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         }
         IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st));
+        step_mark(c, 7);
         IB_CUDA_CHECK(cudaStreamSynchronize(st));
+        step_acc(c, 2, 3, 4);
+        step_acc(c, 3, 4, 5);
+        step_acc(c, 4, 5, 6);
+        step_acc(c, 5, 6, 7);
         if (patch) {
           c->inf.flag_h = c->inf.h_flag[0];
           c->inf.patch_fresh = true;
@@ -880,12 +933,21 @@ int op_advance(Ctx* c) {
     }
   }
   // correction on the finest grid (timestepper.F90:488-553)
+  step_mark(c, 8);
   RC(launch_reg(g, c->nf, c->f, c->reg, c->hx, c->hy, st));
   RC(launch_rot(g, c->hx, c->hy, c->vort, st));
   RC(op_ainv(c, c->vort, c->vort));
   RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], st));
   RC(op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true));
-  return check_err(c);
+  step_mark(c, 9);
+  int rc = check_err(c);
+  if (c->step_prof) {
+    step_acc(c, 0, 0, 1);
+    step_acc(c, 1, 1, 2);
+    step_acc(c, 6, 8, 9);
+    c->step_n += 1;
+  }
+  return rc;
 }
 
 }  // namespace ib

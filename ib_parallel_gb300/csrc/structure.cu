@@ -1,18 +1,15 @@
 // Torsional-body (family 2) structure operators of operators_struct.F90: a rigid
 // plate hinged at its first point on a torsional spring/damper, integrated with
 // the trapezoidal Newmark scheme.  Each body is handled by one CTA; the only
-// reduction is the BR . x dot product.  Gravity and pseudo-forces are zero in the
+// reduction is the BR . x dot product.  The scalar recurrences (sin, cos, divisions)
+// are FP64-latency-bound and every thread evaluates them, so rhs, dx and initial_acc
+// run one warp per body; b_times keeps 256 threads, whose reduction order the fused
+// Krylov kernel reproduces.  Gravity and pseudo-forces are zero in the
 // reference user hooks (user.F90:178-206) and are omitted.
 #include "kernels.cuh"
 
 namespace ib {
 
-// BR_build (operators_struct.F90:319-338): x-rows (j-1) ds sin(g0-th),
-// y-rows -(j-1) ds cos(g0-th).  sn, cs = sin, cos(g0-th), evaluated once per body.
-__device__ __forceinline__ double br_val(const TorsBody& b, double sn, double cs, int j) {
-  if (j < b.npts) return (double)j * b.deltas * sn;
-  return -(double)(j - b.npts) * b.deltas * cs;
-}
 
 __device__ double block_sum(double v) {
   __shared__ double red[32];
@@ -32,9 +29,6 @@ __device__ double block_sum(double v) {
   return s;
 }
 
-__device__ __forceinline__ double keff(const TorsBody& b, double dt) {
-  return 4.0 / (dt * dt) * b.itheta + 2.0 / dt * b.ctheta + b.ktheta;
-}
 
 // b_times2 (operators_struct.F90:14-127): y += BR (BR . x)/K_eff * (delta^2/ds/dt)(2 ds/dt)
 __global__ void k_tors_btimes(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
@@ -45,8 +39,7 @@ __global__ void k_tors_btimes(const TorsBody* __restrict__ tb, TorsState s, doub
   double part = 0.0;
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn, cs, j) * x[b.off + j];
   double dot = block_sum(part);
-  double scale = (delta * delta / b.deltas / dt) * (2.0 * b.deltas / dt);
-  double c = dot / keff(b, dt) * scale;
+  double c = dot / keff(b, dt) * btimes_scale(b, dt, delta);
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = y[b.off + j] + br_val(b, sn, cs, j) * c;
 }
 
@@ -144,7 +137,7 @@ int launch_tors_rhs(int nt, const TorsBody* tb, const TorsState& s, double dt, d
                     cudaStream_t st) {
   if (nt == 0) return IB_OK;
   count_launch();
-  k_tors_rhs<<<nt, 256, 0, st>>>(tb, s, dt, delta, y);
+  k_tors_rhs<<<nt, 32, 0, st>>>(tb, s, dt, delta, y);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
@@ -156,7 +149,7 @@ int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, do
   }
   // err[1..nt] holds per-body |dtheta|, err[0] their maximum
   count_launch();
-  k_tors_dx<<<nt, 256, 0, st>>>(tb, s, dt, delta, f, xb, yb, err + 1);
+  k_tors_dx<<<nt, 32, 0, st>>>(tb, s, dt, delta, f, xb, yb, err + 1);
   count_launch();
   k_max_reduce<<<1, 32, 0, st>>>(nt, err + 1, err);
   IB_CUDA_CHECK(cudaGetLastError());
@@ -166,7 +159,7 @@ int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, doub
                             const double* f, cudaStream_t st) {
   if (nt == 0) return IB_OK;
   count_launch();
-  k_tors_initial_acc<<<nt, 256, 0, st>>>(tb, s, dt, delta, f);
+  k_tors_initial_acc<<<nt, 32, 0, st>>>(tb, s, dt, delta, f);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -39,7 +39,7 @@ EXPORTS = [
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
     "ib_launch_count", "ib_probe_throughput", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
-    "ib_schur_matrix", "ib_get_influence_stats",
+    "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile",
 ]
 
 
@@ -108,6 +108,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_profile_schur": ([P, C.c_int, D], C.c_int),
         "ib_ctci_static": ([C.c_int, C.c_int, P, P, P], C.c_int),
         "ib_schur_matrix": ([P, P, C.POINTER(C.c_int)], C.c_int),
+        "ib_step_profile": ([P, C.c_int, D, C.POINTER(C.c_longlong)], C.c_int),
         "ib_get_influence_stats": ([P, C.POINTER(C.c_longlong), D], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -199,7 +200,7 @@ class Params:
     gmres_max_it: int = 10000
     fsi_max_it: int = 1000
     autotune: bool = True
-    schur_mode: int = 0          # 0 influence matrix (matrix-free fallback), 1 matrix-free
+    schur_mode: int = 0          # 0 influence matrix + one-kernel GMRES, 1 matrix-free, 2 influence + graph GMRES
     influence_margin: int = 0    # band slack in vertices (0: 8)
 
     def to_c(self) -> IbParams:
@@ -329,6 +330,15 @@ class Simulation:
         st = C.c_int(0)
         _check(self.lib.ib_schur_matrix(self.h, _ptr(S), C.byref(st)), "ib_schur_matrix")
         return S if st.value == 0 else None
+
+    STEP_PHASES = ["predictor", "vort2flux", "fsi rhs", "schur assembly", "gmres", "fsi update", "correction"]
+
+    def step_profile(self, mode: int) -> dict:
+        """mode 1 start, 0 stop, 2 read: average device us per step of each phase of ib_advance."""
+        ms = (C.c_double * 7)()
+        n = C.c_longlong(0)
+        _check(self.lib.ib_step_profile(self.h, mode, ms, C.byref(n)), "ib_step_profile")
+        return {k: (1e3 * ms[i] / n.value if n.value else 0.0) for i, k in enumerate(self.STEP_PHASES)}
 
     def influence_stats(self) -> dict:
         counts = (C.c_longlong * 5)()

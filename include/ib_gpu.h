@@ -52,7 +52,9 @@ typedef struct IbParams {
    * vertices around the bodies, computed once and rebuilt when a body leaves the band -- from
    * which each FSI iteration assembles the dense nf x nf operator (same operator as the
    * matrix-free one up to round-off); solves whose stencils touch the domain boundary fall back
-   * to the matrix-free operator.  1: always matrix-free (a_times2 per Krylov iteration). */
+   * to the matrix-free operator; GMRES on the assembled matrix runs as one kernel.
+   * 1: always matrix-free (a_times2 per Krylov iteration).  2: as 0, with GMRES as one
+   * kernel per Krylov step (the graph the matrix-free operator uses), for comparisons. */
   int schur_mode;
   int influence_margin; /* vertices of slack around the stencils in the band (0: 8) */
 } IbParams;
@@ -167,6 +169,11 @@ int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);
  * operator: reg+rot, ainv, coarsify, coarse levels, finest forward, finest solve, finest
  * inverse rows, E curl + B */
 int ib_profile_schur(IbCtx* ctx, int reps, double* stage_ms);
+/* device time of the phases of ib_advance, summed over the steps since it was started:
+ * mode 1 starts (clears), 0 stops, 2 only reads.  phase_ms[7] (may be NULL): predictor,
+ * vort2flux, FSI right-hand side, Schur assembly, GMRES, FSI update (redistribute, structure,
+ * weights, host synchronisation), correction; *nsteps (may be NULL): steps timed */
+int ib_step_profile(IbCtx* ctx, int mode, double* phase_ms, long long* nsteps);
 /* Fluid part of the Schur matrix (a_times2 without B, operators_fluid.F90:14-120: the matrix
  * timestepper.F90:560-598 builds column by column for stationary bodies) at the current body
  * positions, assembled from the influence matrix (schur_mode 0; built on first use):

@@ -58,6 +58,22 @@ def test_steps_match_matrix_free():
     gm.close()
 
 
+def test_fused_solver_matches_graph_solver():
+    # the one-kernel GMRES performs the graph solver's operations in the same order
+    body = small_plate()
+    gf = G.Simulation(G.Params(**PLATE), [body])
+    gg = G.Simulation(G.Params(**dict(PLATE, schur_mode=2)), [body])
+    for _ in range(3):
+        gf.advance()
+        gg.advance()
+        assert gf.counters() == gg.counters()
+        assert np.array_equal(gf.get_vector("f"), gg.get_vector("f"))
+        assert np.array_equal(gf.body_state()[0], gg.body_state()[0])
+    assert np.array_equal(gf.get_field("omega", 0), gg.get_field("omega", 0))
+    gf.close()
+    gg.close()
+
+
 def test_band_rebuild_after_move():
     o, g = pair(dict(PLATE, influence_margin=2), [small_plate()])
     assert g.schur_matrix() is not None
