@@ -1,29 +1,92 @@
 // Device GMRES with the semantics of PETSc 3.11 KSPGMRES as the reference
 // configures it (variables.F90:565-574): restart 30, classical Gram-Schmidt
-// without refinement (borthog2.c), Givens-rotation least squares, nonzero
-// initial guess, unpreconditioned residual norm, convergence when the rotated
-// residual estimate <= max(rtol*||b||, atol) (KSPConvergedDefault).  Each kernel
-// is one CTA; the operator (the Schur matvec) runs between them and reads
-// G.xin, writes G.Av.
+// without refinement (borthog2.c), Givens-rotation least squares, nonzero initial
+// guess, unpreconditioned residual norm, convergence when the rotated residual
+// estimate <= max(rtol*||b||, atol) (KSPConvergedDefault).
+//
+// Two drivers share one arithmetic.  The graph solver runs one CTA per kernel with the
+// operator (the Schur matvec) between them, reading G.xin and writing G.Av.  The cluster
+// solver (k_gmres_cluster) runs a whole solve on an assembled dense operator across a
+// cluster of kSlices CTAs, each owning one slice of the unknowns.  Every inner product and
+// norm is summed the way the cluster must sum it: a sequential partial per slice, then the
+// kSlices partials in slice order; and the dense product splits each row into kSlices
+// column segments reduced by a fixed shuffle tree.  So both drivers produce identical
+// iterates.
+#include <cooperative_groups.h>
+
 #include "kernels.cuh"
 
 namespace ib {
 
+namespace cg = cooperative_groups;
+
 constexpr int kGmresThreads = 512;
 
-__device__ double blk_sum(double v, double* red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[w] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
-    red[32] = s;
+// [lo, hi) of slice c of n unknowns
+__device__ __forceinline__ int slice_size(int n) { return (n + kSlices - 1) / kSlices; }
+__device__ __forceinline__ void slice_range(int n, int c, int* lo, int* hi) {
+  int ns = slice_size(n);
+  *lo = min(n, c * ns);
+  *hi = min(n, *lo + ns);
+}
+
+// Givens update of Arnoldi step `it` (KSPGMRESUpdateHessenberg): the new Hessenberg column is
+// h[0..it], tt; the previous rotations are applied with the rotated value carried in a
+// register (one dependent FMA per rotation), then the new rotation, the rotated residual g
+// and the convergence reason.  Writes H column `it` (ld = restart+1).
+__device__ void givens_step(double* __restrict__ col, const double* __restrict__ h, double tt, int it,
+                            double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g, double prev_res,
+                            double ttol, double* res_out, int* reason_out) {
+  double hapbnd = fabs(tt / g[it]);
+  if (hapbnd > 1.0e-30) hapbnd = 1.0e-30;
+  const bool hapend = tt < hapbnd;
+  double c = h[0];
+  for (int j = 0; j < it; ++j) {
+    const double nxt = h[j + 1];
+    const double cj = cs[j], sj = sn[j];
+    col[j] = fma(sj, nxt, cj * c);
+    c = fma(-sj, c, cj * nxt);
   }
-  __syncthreads();
-  return red[32];
+  col[it + 1] = tt;
+  double res;
+  int reason = 0;
+  if (!hapend) {
+    const double nrm = sqrt(fma(c, c, tt * tt));
+    if (nrm == 0.0) {
+      reason = -9;  // KSP_DIVERGED_NULL
+      res = prev_res;
+      col[it] = c;
+    } else {
+      const double ci = c / nrm, si = tt / nrm;
+      cs[it] = ci;
+      sn[it] = si;
+      g[it + 1] = -(si * g[it]);
+      g[it] = ci * g[it];
+      col[it] = fma(si, tt, ci * c);
+      res = fabs(g[it + 1]);
+    }
+  } else {
+    col[it] = c;
+    res = 0.0;
+  }
+  if (reason == 0) {
+    if (res <= ttol) reason = 2;
+    else if (hapend) reason = -3;
+  }
+  *res_out = res;
+  *reason_out = reason;
+}
+
+// KSPGMRESBuildSoln back substitution: y[0..k] from H (ld = R+1) and g.
+__device__ void back_substitute(const double* __restrict__ H, int R, const double* __restrict__ g, int k,
+                                double* __restrict__ y) {
+  auto HH = [&](int r, int c) { return H[(size_t)c * (R + 1) + r]; };
+  y[k] = g[k] / HH(k, k);
+  for (int i = k - 1; i >= 0; --i) {
+    double tt = g[i];
+    for (int j = i + 1; j <= k; ++j) tt = fma(-HH(i, j), y[j], tt);
+    y[i] = tt / HH(i, i);
+  }
 }
 
 __global__ void k_gmres_init(GmresDev G) {
@@ -35,18 +98,32 @@ __global__ void k_gmres_init(GmresDev G) {
 // Cycle start: r = b - A x (A x in G.Av), V0 = r/||r||, tolerance on the first cycle.
 __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const double* __restrict__ x, double rtol,
                               double atol, int max_it, cudaGraphConditionalHandle h_inner, int use_cond) {
-  __shared__ double red[33];
-  const int nf = G.nf;
-  double pr = 0.0, pb = 0.0;
-  for (int i = threadIdx.x; i < nf; i += blockDim.x) {
-    double r = b[i] - G.Av[i];
-    G.V[i] = r;
-    pr += r * r;
-    pb += b[i] * b[i];
+  __shared__ double part[2 * kSlices];
+  __shared__ double s_norm[2];
+  const int nf = G.nf, tid = threadIdx.x;
+  for (int i = tid; i < nf; i += blockDim.x) G.V[i] = b[i] - G.Av[i];
+  __syncthreads();
+  if (tid < 2 * kSlices) {
+    int lo, hi;
+    slice_range(nf, tid % kSlices, &lo, &hi);
+    const double* v = tid < kSlices ? G.V : b;
+    double a = 0.0;
+    for (int i = lo; i < hi; ++i) a = fma(v[i], v[i], a);
+    part[tid] = a;
   }
-  double rnorm = sqrt(blk_sum(pr, red));
-  double bnorm = sqrt(blk_sum(pb, red));
-  int its = G.ist[0];
+  __syncthreads();
+  if (tid == 0) {
+    double r2 = part[0], b2 = part[kSlices];
+    for (int c = 1; c < kSlices; ++c) {
+      r2 += part[c];
+      b2 += part[kSlices + c];
+    }
+    s_norm[0] = sqrt(r2);
+    s_norm[1] = sqrt(b2);
+  }
+  __syncthreads();
+  const double rnorm = s_norm[0], bnorm = s_norm[1];
+  const int its = G.ist[0];
   double ttol;
   if (its == 0) {
     double rnorm0 = bnorm != 0.0 ? bnorm : rnorm;
@@ -54,13 +131,13 @@ __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const do
   } else {
     ttol = G.scal[0];
   }
-  double inv = rnorm != 0.0 ? 1.0 / rnorm : 0.0;
-  for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+  const double inv = rnorm != 0.0 ? 1.0 / rnorm : 0.0;
+  for (int i = tid; i < nf; i += blockDim.x) {
     double v = rnorm != 0.0 ? G.V[i] * inv : G.V[i];
     G.V[i] = v;
     G.xin[i] = v;
   }
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     G.scal[0] = ttol;
     G.scal[1] = rnorm;
     G.scal[2] = bnorm;
@@ -79,82 +156,75 @@ __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const do
 }
 
 // One Arnoldi step on w = A V[it] (in G.Av): classical Gram-Schmidt (all projections
-// against the unmodified w, one warp per projection), normalisation, Givens update.
+// against the unmodified w), normalisation, Givens update.
 __global__ void k_gmres_arnoldi(GmresDev G, int max_it, cudaGraphConditionalHandle h_inner, int use_cond) {
-  __shared__ double red[33];
+  __shared__ double part[64 * kSlices];
   __shared__ double h[64];
+  __shared__ double s_tt;
   if (G.ist[3] == 0) {
     if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(h_inner, 0u);
     return;
   }
-  const int nf = G.nf, R = G.restart;
+  const int nf = G.nf, R = G.restart, tid = threadIdx.x;
   const int it = G.ist[2];
   double* w = G.V + (size_t)(it + 1) * nf;
   const double* Av = G.Av;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int j = warp; j <= it; j += nwarps) {
+  // projections: a partial per (j, slice), then the slices in order
+  for (int q = tid; q < (it + 1) * kSlices; q += blockDim.x) {
+    const int j = q / kSlices, c = q % kSlices;
+    int lo, hi;
+    slice_range(nf, c, &lo, &hi);
     const double* vj = G.V + (size_t)j * nf;
-    double p = 0.0;
-    for (int i = lane; i < nf; i += 32) p += Av[i] * vj[i];
-    for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-    if (lane == 0) h[j] = p;
+    double a = 0.0;
+    for (int i = lo; i < hi; ++i) a = fma(Av[i], vj[i], a);
+    part[q] = a;
   }
   __syncthreads();
-  double pn = 0.0;
-  for (int i = threadIdx.x; i < nf; i += blockDim.x) {
-    double v = Av[i];
-    for (int j = 0; j <= it; ++j) v = v - h[j] * G.V[(size_t)j * nf + i];
-    w[i] = v;
-    pn += v * v;
+  if (tid <= it) {
+    double s = part[tid * kSlices];
+    for (int c = 1; c < kSlices; ++c) s += part[tid * kSlices + c];
+    h[tid] = s;
   }
-  double tt = sqrt(blk_sum(pn, red));
-  double inv = tt != 0.0 ? 1.0 / tt : 0.0;
-  for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+  __syncthreads();
+  for (int i = tid; i < nf; i += blockDim.x) {
+    double v = Av[i];
+    for (int j = 0; j <= it; ++j) v = fma(-h[j], G.V[(size_t)j * nf + i], v);
+    w[i] = v;
+  }
+  __syncthreads();
+  if (tid < kSlices) {
+    int lo, hi;
+    slice_range(nf, tid, &lo, &hi);
+    double a = 0.0;
+    for (int i = lo; i < hi; ++i) a = fma(w[i], w[i], a);
+    part[tid] = a;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double s = part[0];
+    for (int c = 1; c < kSlices; ++c) s += part[c];
+    s_tt = sqrt(s);
+  }
+  __syncthreads();
+  const double tt = s_tt;
+  const double inv = tt != 0.0 ? 1.0 / tt : 0.0;
+  for (int i = tid; i < nf; i += blockDim.x) {
     double v = tt != 0.0 ? w[i] * inv : w[i];
     w[i] = v;
     G.xin[i] = v;
   }
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     double* col = G.H + (size_t)it * (R + 1);
-    for (int j = 0; j <= it; ++j) col[j] = h[j];
-    col[it + 1] = tt;
-    double hapbnd = fabs(tt / G.g[it]);
-    if (hapbnd > 1.0e-30) hapbnd = 1.0e-30;
-    bool hapend = tt < hapbnd;
-    for (int j = 0; j < it; ++j) {
-      double t0 = col[j];
-      col[j] = G.cs[j] * t0 + G.sn[j] * col[j + 1];
-      col[j + 1] = G.cs[j] * col[j + 1] - G.sn[j] * t0;
-    }
     double res;
-    int reason = 0;
-    if (!hapend) {
-      double nrm = sqrt(col[it] * col[it] + col[it + 1] * col[it + 1]);
-      if (nrm == 0.0) {
-        reason = -9;  // KSP_DIVERGED_NULL
-        res = G.scal[1];
-      } else {
-        G.cs[it] = col[it] / nrm;
-        G.sn[it] = col[it + 1] / nrm;
-        G.g[it + 1] = -(G.sn[it] * G.g[it]);
-        G.g[it] = G.cs[it] * G.g[it];
-        col[it] = G.cs[it] * col[it] + G.sn[it] * col[it + 1];
-        res = fabs(G.g[it + 1]);
-      }
-    } else {
-      res = 0.0;
-    }
-    int itn = it + 1;
-    int its = G.ist[0] + 1;
+    int reason;
+    givens_step(col, h, tt, it, G.cs, G.sn, G.g, G.scal[1], G.scal[0], &res, &reason);
+    const int itn = it + 1;
+    const int its = G.ist[0] + 1;
     G.ist[2] = itn;
     G.ist[0] = its;
     G.scal[1] = res;
-    if (reason == 0) {
-      if (res <= G.scal[0]) reason = 2;
-      else if (hapend) reason = -3;
-    }
     G.ist[1] = reason;
-    int active = (reason == 0 && itn < R && its < max_it) ? 1 : 0;
+    const int active = (reason == 0 && itn < R && its < max_it) ? 1 : 0;
     G.ist[3] = active;
     if (use_cond) cudaGraphSetConditional(h_inner, (unsigned)active);
   }
@@ -166,22 +236,12 @@ __global__ void k_gmres_update(GmresDev G, double* __restrict__ x, int max_it, c
   __shared__ double y[64];
   const int nf = G.nf, R = G.restart;
   const int it = G.ist[2];
-  if (threadIdx.x == 0 && it > 0) {
-    int k = it - 1;
-    const double* H = G.H;
-    auto HH = [&](int r, int c) { return H[(size_t)c * (R + 1) + r]; };
-    y[k] = G.g[k] / HH(k, k);
-    for (int i = k - 1; i >= 0; --i) {
-      double tt = G.g[i];
-      for (int j = i + 1; j <= k; ++j) tt = tt - HH(i, j) * y[j];
-      y[i] = tt / HH(i, i);
-    }
-  }
+  if (threadIdx.x == 0 && it > 0) back_substitute(G.H, R, G.g, it - 1, y);
   __syncthreads();
   if (it > 0) {
     for (int i = threadIdx.x; i < nf; i += blockDim.x) {
       double u = 0.0;
-      for (int j = 0; j < it; ++j) u = u + y[j] * G.V[(size_t)j * nf + i];
+      for (int j = 0; j < it; ++j) u = fma(y[j], G.V[(size_t)j * nf + i], u);
       x[i] = x[i] + u;
     }
   }
@@ -317,212 +377,279 @@ int launch_unit(int n, int i, double* e, cudaStream_t st) {
   return IB_OK;
 }
 
-// ---------------------------------------------------------------- fused dense solve
+// ---------------------------------------------------------------- cluster dense solve
 namespace {
-struct FusedSmem {
-  int nf, R;
-  size_t base_doubles() const {
-    return (size_t)(R + 1) * nf + 3 * (size_t)nf + (size_t)(R + 1) * R + 5 * (size_t)(R + 1) + 33;
+// Shared-memory layout of one CTA of the cluster solver (doubles).
+struct ClusterSmem {
+  int nf, R, ns;
+  size_t base() const {
+    return (size_t)(R + 1) * ns + nf + 3 * (size_t)ns + 2 * (size_t)(R + 1) + (size_t)(R + 1) * R +
+           4 * (size_t)(R + 1) + 8;
   }
-  size_t with_a() const { return base_doubles() + (size_t)nf * nf; }
+  size_t with_a() const { return base() + (size_t)ns * nf; }
 };
 }  // namespace
 
-// One CTA of 32*ceil(nf/32) threads (one vector element per thread), so every scalar FP64
-// recurrence and reduction runs on the fewest warps: an FP64 warp instruction occupies its
-// SMSP's FP64 pipe for the same time whatever the number of active lanes.  Thread i
-// handles element i in every vector loop, as the 512-thread kernels do, and the block sums
-// reduce the same per-warp partials in the same order (the extra warps of those kernels add
-// zeros), so both solvers produce identical iterates.
-__global__ void k_gmres_fused(GmresDev G, const double* __restrict__ Atg, int a_in_smem, const double* __restrict__ b,
-                              double* __restrict__ x, double rtol, double atol, int max_it) {
-  extern __shared__ double sm[];
-  __shared__ int s_reason;
-  __shared__ double s_res;
+// One restarted GMRES solve on the assembled operator A (column-major, At[j*nf + r] = A[r][j])
+// across a cluster of kSlices CTAs.  CTA c owns the rows and vector elements of slice c: its
+// rows of A, its slice of every Krylov vector, of x and of b.  Per Arnoldi step:
+//   A: the product of its rows with the full current vector (kSlices threads per row), and
+//      its partial projections; meanwhile the last warp applies the Givens update of the
+//      previous step;                                                        cluster barrier
+//      the previous step's convergence decision is read from CTA 0 (every CTA branches
+//      alike), then the projections are summed over the slices in order;
+//   B: w = A v - sum h_j v_j on the slice and its partial norm;              cluster barrier
+//   C: the norm, the normalised slice;                                       cluster barrier
+//   D: every CTA gathers the full new vector through distributed shared memory.
+// No thread waits on a flag: the only waits are the cluster and CTA barriers, which every
+// thread of every CTA reaches the same number of times.
+__global__ void __cluster_dims__(kSlices, 1, 1)
+    k_gmres_cluster(GmresDev G, const double* __restrict__ At, int a_in_smem, const double* __restrict__ b,
+                    double* __restrict__ x, double rtol, double atol, int max_it) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
   const int nf = G.nf, R = G.restart;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  double* V = sm;                           // (R+1) x nf
-  double* Av = V + (size_t)(R + 1) * nf;    // nf
-  double* xs = Av + nf;                     // nf
-  double* bs = xs + nf;                     // nf
-  double* H = bs + nf;                      // (R+1) x R, column it at H + it*(R+1)
-  double* cs = H + (size_t)(R + 1) * R;     // R+1
+  const int ns = slice_size(nf);
+  int r0, r1;
+  slice_range(nf, rank, &r0, &r1);
+  const int nl = r1 - r0;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nwork = (int)blockDim.x - 32;     // the last warp applies the Givens updates
+  const bool gwarp = tid >= nwork;
+  extern __shared__ double sm[];
+  double* Vs = sm;                                  // (R+1) x ns
+  double* vfull = Vs + (size_t)(R + 1) * ns;        // nf
+  double* avs = vfull + nf;                         // ns
+  double* xsl = avs + ns;                           // ns
+  double* bsl = xsl + ns;                           // ns
+  double* hp = bsl + ns;                            // R+1 partial projections (read remotely)
+  double* h = hp + (R + 1);                         // R+1
+  double* H = h + (R + 1);                          // (R+1) x R
+  double* cs = H + (size_t)(R + 1) * R;
   double* sn = cs + (R + 1);
   double* g = sn + (R + 1);
-  double* h = g + (R + 1);
-  double* yv = h + (R + 1);
-  double* red = yv + (R + 1);               // 33
-  double* As = red + 33;
-  const double* At = a_in_smem ? As : Atg;
+  double* yv = g + (R + 1);
+  double* scal = yv + (R + 1);                      // [0],[1] partials (read remotely), [2] tt, [3] res,
+                                                    // [4] 1/tt, [5] rnorm, [6] bnorm, [7] ttol
+  double* As = scal + 8;                            // nl x nf row-major when a_in_smem
+  __shared__ int s_reason;                          // read remotely from CTA 0
+  auto remote = [&](double* p, int c) -> const double* { return cl.map_shared_rank(p, c); };
+  auto bar_work = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(nwork)); };
+
   if (a_in_smem)
-    for (int i = tid; i < nf * nf; i += blockDim.x) As[i] = Atg[i];
-  for (int i = tid; i < nf; i += blockDim.x) {
-    xs[i] = x[i];
-    bs[i] = b[i];
+    for (int q = tid; q < nl * nf; q += blockDim.x) {
+      const int rl = q / nf, j = q - rl * nf;
+      As[q] = At[(size_t)j * nf + r0 + rl];
+    }
+  for (int i = tid; i < nl; i += blockDim.x) {
+    xsl[i] = x[r0 + i];
+    bsl[i] = b[r0 + i];
   }
   __syncthreads();
 
-  // out = A in, A column-major, one thread per row (k_dense_mv)
-  auto matvec = [&](const double* in, double* out) {
-    for (int r = tid; r < nf; r += blockDim.x) {
-      double acc = 0.0;
-      for (int j = 0; j < nf; ++j) acc = fma(At[(size_t)j * nf + r], in[j], acc);
-      out[r] = acc;
+  // avs = rows of A times vfull: kSlices column segments per row, reduced by a fixed tree
+  const int cw = slice_size(nf);
+  auto matvec = [&]() {
+    for (int base = 0; base < ns * kSlices; base += nwork) {
+      const int q = base + tid, rl = q / kSlices, seg = q % kSlices;
+      double p = 0.0;
+      if (rl < nl) {
+        const int j0 = min(nf, seg * cw), j1 = min(nf, j0 + cw);
+        if (a_in_smem) {
+          const double* Ar = As + (size_t)rl * nf;
+          for (int j = j0; j < j1; ++j) p = fma(Ar[j], vfull[j], p);
+        } else {
+          for (int j = j0; j < j1; ++j) p = fma(At[(size_t)j * nf + r0 + rl], vfull[j], p);
+        }
+      }
+      p += __shfl_xor_sync(0xffffffffu, p, 4);
+      p += __shfl_xor_sync(0xffffffffu, p, 2);
+      p += __shfl_xor_sync(0xffffffffu, p, 1);
+      if (rl < nl && seg == 0) avs[rl] = p;
     }
-    __syncthreads();
+  };
+  auto gather = [&](double* src, int stride_slot) {   // vfull[i] = slot of the owner's slice
+    for (int i = tid; i < nf; i += blockDim.x) {
+      const int c = i / ns;
+      vfull[i] = remote(src + (size_t)stride_slot * ns, c)[i - c * ns];
+    }
   };
 
-  int its = 0, cycles = 0, reason = 0, it = 0;
+  int its = 0, cycles = 0, reason = 0, k = 0;
   double ttol = 0.0;
   for (;;) {
-    // cycle start (k_gmres_start): r = b - A x, V0 = r/||r||
-    matvec(xs, Av);
-    double pr = 0.0, pb = 0.0;
+    // ---- cycle start (k_gmres_start): r = b - A x, V0 = r/||r||
+    cl.sync();                                    // every x slice is final
     for (int i = tid; i < nf; i += blockDim.x) {
-      double r = bs[i] - Av[i];
-      V[i] = r;
-      pr += r * r;
-      pb += bs[i] * bs[i];
+      const int c = i / ns;
+      vfull[i] = remote(xsl, c)[i - c * ns];
     }
-    const double rnorm = sqrt(blk_sum(pr, red));
-    const double bnorm = sqrt(blk_sum(pb, red));
-    if (its == 0) {
-      double rnorm0 = bnorm != 0.0 ? bnorm : rnorm;
-      ttol = fmax(rtol * rnorm0, atol);
-    }
-    const double inv0 = rnorm != 0.0 ? 1.0 / rnorm : 0.0;
-    for (int i = tid; i < nf; i += blockDim.x) V[i] = rnorm != 0.0 ? V[i] * inv0 : V[i];
-    cycles += 1;
-    it = 0;
-    reason = 0;
-    if (rnorm == 0.0) reason = 2;
-    else if (rnorm <= ttol) reason = 3;
-    else if (its >= max_it) reason = -3;
+    __syncthreads();
+    if (!gwarp) matvec();
+    __syncthreads();
+    for (int i = tid; i < nl; i += blockDim.x) Vs[i] = bsl[i] - avs[i];
+    __syncthreads();
     if (tid == 0) {
+      double a = 0.0, bb = 0.0;
+      for (int i = 0; i < nl; ++i) a = fma(Vs[i], Vs[i], a);
+      for (int i = 0; i < nl; ++i) bb = fma(bsl[i], bsl[i], bb);
+      scal[0] = a;
+      scal[1] = bb;
+    }
+    cl.sync();
+    if (tid == 0) {
+      double r2 = remote(scal, 0)[0], b2 = remote(scal, 0)[1];
+      for (int c = 1; c < kSlices; ++c) {
+        r2 += remote(scal, c)[0];
+        b2 += remote(scal, c)[1];
+      }
+      const double rnorm = sqrt(r2), bnorm = sqrt(b2);
+      if (its == 0) {
+        double rnorm0 = bnorm != 0.0 ? bnorm : rnorm;
+        scal[7] = fmax(rtol * rnorm0, atol);
+      }
+      scal[5] = rnorm;
+      scal[6] = bnorm;
+      scal[3] = rnorm;
       g[0] = rnorm;
-      s_res = rnorm;
+      int rs = 0;
+      if (rnorm == 0.0) rs = 2;
+      else if (rnorm <= scal[7]) rs = 3;
+      else if (its >= max_it) rs = -3;
+      s_reason = rs;
     }
     __syncthreads();
+    {
+      const double rnorm = scal[5];
+      const double inv = rnorm != 0.0 ? 1.0 / rnorm : 0.0;
+      for (int i = tid; i < nl; i += blockDim.x) Vs[i] = rnorm != 0.0 ? Vs[i] * inv : Vs[i];
+    }
+    cycles += 1;
+    cl.sync();                                    // V0 slices and CTA 0's decision are visible
+    reason = *cl.map_shared_rank(&s_reason, 0);
+    ttol = scal[7];
     if (reason != 0) break;
-    // Arnoldi steps (k_gmres_arnoldi)
-    for (;;) {
-      matvec(V + (size_t)it * nf, Av);
-      for (int j = warp; j <= it; j += nwarps) {
-        const double* vj = V + (size_t)j * nf;
-        double p = 0.0;
-        for (int i = lane; i < nf; i += 32) p += Av[i] * vj[i];
-        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-        if (lane == 0) h[j] = p;
-      }
-      __syncthreads();
-      double* w = V + (size_t)(it + 1) * nf;
-      double pn = 0.0;
-      for (int i = tid; i < nf; i += blockDim.x) {
-        double v = Av[i];
-        for (int j = 0; j <= it; ++j) v = v - h[j] * V[(size_t)j * nf + i];
-        w[i] = v;
-        pn += v * v;
-      }
-      const double tt = sqrt(blk_sum(pn, red));
-      const double inv = tt != 0.0 ? 1.0 / tt : 0.0;
-      for (int i = tid; i < nf; i += blockDim.x) w[i] = tt != 0.0 ? w[i] * inv : w[i];
-      if (tid == 0) {
-        double* col = H + (size_t)it * (R + 1);
-        for (int j = 0; j <= it; ++j) col[j] = h[j];
-        col[it + 1] = tt;
-        double hapbnd = fabs(tt / g[it]);
-        if (hapbnd > 1.0e-30) hapbnd = 1.0e-30;
-        bool hapend = tt < hapbnd;
-        for (int j = 0; j < it; ++j) {
-          double t0 = col[j];
-          col[j] = cs[j] * t0 + sn[j] * col[j + 1];
-          col[j + 1] = cs[j] * col[j + 1] - sn[j] * t0;
-        }
-        double res;
-        int rsn = 0;
-        if (!hapend) {
-          double nrm = sqrt(col[it] * col[it] + col[it + 1] * col[it + 1]);
-          if (nrm == 0.0) {
-            rsn = -9;
-            res = s_res;
-          } else {
-            cs[it] = col[it] / nrm;
-            sn[it] = col[it + 1] / nrm;
-            g[it + 1] = -(sn[it] * g[it]);
-            g[it] = cs[it] * g[it];
-            col[it] = cs[it] * col[it] + sn[it] * col[it + 1];
-            res = fabs(g[it + 1]);
-          }
-        } else {
-          res = 0.0;
-        }
-        if (rsn == 0) {
-          if (res <= ttol) rsn = 2;
-          else if (hapend) rsn = -3;
-        }
-        s_res = res;
-        s_reason = rsn;
-      }
-      __syncthreads();
-      reason = s_reason;
-      it += 1;
-      its += 1;
-      if (reason != 0 || it >= R || its >= max_it) break;
-    }
-    // KSPGMRESBuildSoln (k_gmres_update): back substitution and x += V y
-    if (tid == 0 && it > 0) {
-      int k = it - 1;
-      auto HH = [&](int r, int c) { return H[(size_t)c * (R + 1) + r]; };
-      yv[k] = g[k] / HH(k, k);
-      for (int i = k - 1; i >= 0; --i) {
-        double tt = g[i];
-        for (int j = i + 1; j <= k; ++j) tt = tt - HH(i, j) * yv[j];
-        yv[i] = tt / HH(i, i);
-      }
-    }
+    gather(Vs, 0);
     __syncthreads();
-    if (it > 0) {
-      for (int i = tid; i < nf; i += blockDim.x) {
-        double u = 0.0;
-        for (int j = 0; j < it; ++j) u = u + yv[j] * V[(size_t)j * nf + i];
-        xs[i] = xs[i] + u;
+    // ---- Arnoldi steps (k_gmres_arnoldi), the Givens update of step k-1 during step k
+    k = 0;
+    for (;;) {
+      if (!gwarp) {
+        matvec();
+        bar_work();
+        if (tid <= k) {
+          double a = 0.0;
+          const double* vj = Vs + (size_t)tid * ns;
+          for (int i = 0; i < nl; ++i) a = fma(avs[i], vj[i], a);
+          hp[tid] = a;
+        }
+      } else if (k > 0 && lane == 0) {
+        double res;
+        int rs;
+        givens_step(H + (size_t)(k - 1) * (R + 1), h, scal[2], k - 1, cs, sn, g, scal[3], ttol, &res, &rs);
+        scal[3] = res;
+        s_reason = rs;
       }
+      cl.sync();                                  // partial projections; Givens of step k-1
+      if (k > 0) {
+        reason = *cl.map_shared_rank(&s_reason, 0);
+        if (reason != 0 || k >= R || its >= max_it) break;
+      }
+      if (tid <= k) {
+        double s = remote(hp, 0)[tid];
+        for (int c = 1; c < kSlices; ++c) s += remote(hp, c)[tid];
+        h[tid] = s;
+      }
+      __syncthreads();
+      double* w = Vs + (size_t)(k + 1) * ns;
+      for (int i = tid; i < nl; i += blockDim.x) {
+        double v = avs[i];
+        for (int j = 0; j <= k; ++j) v = fma(-h[j], Vs[(size_t)j * ns + i], v);
+        w[i] = v;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double a = 0.0;
+        for (int i = 0; i < nl; ++i) a = fma(w[i], w[i], a);
+        scal[0] = a;
+      }
+      cl.sync();                                  // partial norms
+      if (tid == 0) {
+        double s = remote(scal, 0)[0];
+        for (int c = 1; c < kSlices; ++c) s += remote(scal, c)[0];
+        const double tt = sqrt(s);
+        scal[2] = tt;
+        scal[4] = tt != 0.0 ? 1.0 / tt : 0.0;
+      }
+      __syncthreads();
+      {
+        const double tt = scal[2], inv = scal[4];
+        for (int i = tid; i < nl; i += blockDim.x) w[i] = tt != 0.0 ? w[i] * inv : w[i];
+      }
+      cl.sync();                                  // the new vector's slices
+      gather(Vs, k + 1);
+      __syncthreads();
+      its += 1;
+      k += 1;
     }
+    // ---- KSPGMRESBuildSoln (k_gmres_update): back substitution and x += V y on the slice
+    if (tid == 0 && k > 0) back_substitute(H, R, g, k - 1, yv);
+    __syncthreads();
+    if (k > 0)
+      for (int i = tid; i < nl; i += blockDim.x) {
+        double u = 0.0;
+        for (int j = 0; j < k; ++j) u = fma(yv[j], Vs[(size_t)j * ns + i], u);
+        xsl[i] = xsl[i] + u;
+      }
     __syncthreads();
     if (reason != 0 || its >= max_it) break;
   }
-  for (int i = tid; i < nf; i += blockDim.x) x[i] = xs[i];
-  if (tid == 0) {
+  for (int i = tid; i < nl; i += blockDim.x) x[r0 + i] = xsl[i];
+  if (rank == 0 && tid == 0) {
     G.ist[0] = its;
     G.ist[1] = reason;
-    G.ist[2] = it;
+    G.ist[2] = k;
     G.ist[3] = 0;
     G.ist[4] = cycles;
     G.scal[0] = ttol;
-    G.scal[1] = s_res;
+    G.scal[1] = scal[3];
   }
+  cl.sync();                                      // no CTA exits while others read its memory
 }
 
 int launch_gmres_fused(const GmresDev& G, const double* At, const double* b, double* x, double rtol, double atol,
                        int max_it, cudaStream_t st) {
-  // one element per thread and the same element-to-warp map as the 512-thread kernels
-  if (G.nf <= 0 || G.nf > kGmresThreads) return IB_ERR_ARG;
-  const int threads = 32 * ((G.nf + 31) / 32);
-  FusedSmem fs{G.nf, G.restart};
+  if (G.nf <= 0 || G.restart > 63) return IB_ERR_ARG;
+  ClusterSmem cs{G.nf, G.restart, (G.nf + kSlices - 1) / kSlices};
+  // at least R+1 work threads: one per projection of the longest Arnoldi step
+  const int work = max(64, 32 * ((cs.ns * kSlices + 31) / 32));
+  const int threads = work + 32;
+  if (threads > 1024) return IB_ERR_ARG;
   int dev = 0, optin = 0;
   IB_CUDA_CHECK(cudaGetDevice(&dev));
   IB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const size_t limit = (size_t)optin - 1024;   // static shared memory of the kernel and the reductions
+  const size_t limit = (size_t)optin - 1024;
   int a_in = 1;
-  size_t bytes = 8 * fs.with_a();
+  size_t bytes = 8 * cs.with_a();
   if (bytes > limit) {
     a_in = 0;
-    bytes = 8 * fs.base_doubles();
+    bytes = 8 * cs.base();
     if (bytes > limit) return IB_ERR_ARG;
   }
-  IB_CUDA_CHECK(cudaFuncSetAttribute(k_gmres_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  IB_CUDA_CHECK(cudaFuncSetAttribute(k_gmres_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  // the cluster must fit on the device as launched
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kSlices);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = bytes;
+  cfg.stream = st;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, k_gmres_cluster, &cfg) != cudaSuccess || nclusters < 1) {
+    cudaGetLastError();
+    return IB_ERR_ARG;
+  }
   count_launch();
-  k_gmres_fused<<<1, threads, bytes, st>>>(G, At, a_in, b, x, rtol, atol, max_it);
+  k_gmres_cluster<<<kSlices, threads, bytes, st>>>(G, At, a_in, b, x, rtol, atol, max_it);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -171,13 +171,22 @@ __global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const
   }
 }
 
-// y = A x with A column-major (At[j][r] = A[r][j]): one thread per row, summing in j order.
+// y = A x with A column-major (At[j][r] = A[r][j]): kSlices threads per row, each summing one
+// column segment in order, combined by a fixed shuffle tree -- the product the cluster
+// GMRES solver forms, so that both solvers see identical operator outputs.
 __global__ void k_dense_mv(int n, const double* __restrict__ At, const double* __restrict__ x, double* __restrict__ y) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  double acc = 0.0;
-  for (int j = 0; j < n; ++j) acc = fma(At[(size_t)j * n + r], x[j], acc);
-  y[r] = acc;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = q / kSlices, seg = q % kSlices;
+  const int cw = (n + kSlices - 1) / kSlices;
+  double p = 0.0;
+  if (r < n) {
+    const int j0 = min(n, seg * cw), j1 = min(n, j0 + cw);
+    for (int j = j0; j < j1; ++j) p = fma(At[(size_t)j * n + r], x[j], p);
+  }
+  p += __shfl_xor_sync(0xffffffffu, p, 4);
+  p += __shfl_xor_sync(0xffffffffu, p, 2);
+  p += __shfl_xor_sync(0xffffffffu, p, 1);
+  if (r < n && seg == 0) y[r] = p;
 }
 
 // Column c of the precompute: unit vorticity at band vertex c (the previous one cleared),
@@ -411,7 +420,7 @@ int inf_prepare(Ctx* c) {
 int inf_dense_mv(Ctx* c, const double* x, double* y) {
   c->n_matvec += 1;
   count_launch();
-  k_dense_mv<<<cdiv(c->nf, 128), 128, 0, c->st>>>(c->nf, c->inf.St, x, y);
+  k_dense_mv<<<cdiv((long long)kSlices * c->nf, 128), 128, 0, c->st>>>(c->nf, c->inf.St, x, y);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -83,7 +83,10 @@ int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, doub
                             const double* f, cudaStream_t st);
 int launch_tors_save(int nt, const TorsState& s, cudaStream_t st);
 
-// gmres.cu -- PETSc KSPGMRES as configured in variables.F90:565-574
+// gmres.cu -- PETSc KSPGMRES as configured in variables.F90:565-574.  Reductions over the
+// unknowns are summed per slice (kSlices contiguous slices of ceil(nf/kSlices)), then over
+// the slices in order; dense products split each row into kSlices column segments.
+constexpr int kSlices = 8;
 struct GmresDev {
   int nf, restart;
   double* V;       // (restart+1) * nf
@@ -106,10 +109,10 @@ int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st, cudaGra
 int launch_gmres_update(const GmresDev& G, double* x, int max_it, cudaStream_t st, cudaGraphConditionalHandle h = 0,
                         int use_cond = 0);
 int launch_copy(int n, const double* a, double* b, cudaStream_t st);
-// The whole solve in one CTA for a dense operator A, column-major (At[j*nf + r] = A[r][j]):
-// the operations of the start / arnoldi / update kernels in the same order, with A applied
-// one row per thread.  Writes G.ist like them.  Returns IB_ERR_ARG (nothing launched) when
-// nf exceeds 512 or the Krylov basis does not fit in shared memory.
+// The whole solve on a dense operator A, column-major (At[j*nf + r] = A[r][j]), as one
+// cluster of kSlices CTAs: the operations of the start / arnoldi / update kernels in the same
+// order, with A applied by the same segmented row products as k_dense_mv.  Writes G.ist like
+// them.  Returns IB_ERR_ARG (nothing launched) when the problem does not fit the cluster.
 int launch_gmres_fused(const GmresDev& G, const double* At, const double* b, double* x, double rtol, double atol,
                        int max_it, cudaStream_t st);
 
