@@ -71,6 +71,13 @@ struct Influence {
   double build_ms = 0.0;
 };
 
+// A fixed phase of the time step replayed as one CUDA graph.
+struct PhaseGraph {
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;   // kernels in the graph
+  bool failed = false;
+};
+
 struct Ctx {
   IbParams p{};
   GridDims g{};
@@ -93,6 +100,8 @@ struct Ctx {
   std::vector<double*> omega, s, qx, qy, q0x, q0y, rhs_old;
   // Schur-operator scratch per level
   std::vector<double*> mv_w, mv_s, mv_qx, mv_qy;
+  // vort2flux: per-level mode-space fields and the ring each level receives
+  std::vector<double*> hat, ringv;
   // row treatments of the Schur operator's partial transforms (per vertex row)
   unsigned char *rm_top = nullptr, *rm_coarse = nullptr, *rm_fine = nullptr, *rm_ring2 = nullptr;
   double* wmat = nullptr;          // DST-I matrix of the x transform ((m-1) x (m-1))
@@ -131,6 +140,9 @@ struct Ctx {
   cudaGraph_t solve_graph_dense = nullptr;
   long long kernels_per_matvec = 0, kernels_per_matvec_dense = 0;
   Influence inf;
+  // predictor, first vort2flux and correction as graphs (from the second step on)
+  bool use_step_graphs = true;
+  PhaseGraph graph_pred, graph_v2f, graph_corr;
   double* cholM = nullptr;         // nf x nf (num_stat)
   bool chol_ready = false;
 

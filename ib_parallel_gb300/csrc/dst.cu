@@ -1,6 +1,7 @@
 // Batched DST-I kernels (see dst.cuh for the algorithm).
 #include "dst.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -289,18 +290,18 @@ __device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2*
 
 // ------------------------------------------------------------- x pass
 template <int PRE>
-__device__ __forceinline__ double x_load(const DstXArgs& a, const GridDims& g, int row, int j, int nrows, int N,
-                                         int ld) {
+__device__ __forceinline__ double x_load(const DstXArgs& a, const double* __restrict__ in, const GridDims& g, int row,
+                                         int j, int nrows, int N, int ld) {
   size_t idx = (size_t)row * ld + j;
   double v = 0.0;
   if (PRE == PRE_COPY) {
-    v = a.in[idx];
+    v = in[idx];
   } else if (PRE == PRE_COMBINE) {
-    v = fma(a.cb, a.in2[idx], a.ca * a.in[idx]) + a.in3[idx];
+    v = fma(a.cb, a.in2[idx], a.ca * in[idx]) + a.in3[idx];
   } else if (PRE == PRE_PRED) {
     // con1 rhs + con2 rhs_old + rhsbc + (w - c L w)/normalize, L the 5-point
     // Laplacian with zero boundary: alpha = (1-4c)/normalize, beta = c/normalize
-    double base = fma(a.cb, a.in2[idx], a.ca * a.in[idx]) + a.in3[idx];
+    double base = fma(a.cb, a.in2[idx], a.ca * in[idx]) + a.in3[idx];
     const double* w = a.in4;
     double nb = 0.0;
     if (j > 0) nb += w[idx - 1];
@@ -310,7 +311,7 @@ __device__ __forceinline__ double x_load(const DstXArgs& a, const GridDims& g, i
     v = fma(a.beta, nb, fma(a.alpha, w[idx], base));
   } else {
     // apply_bc (operators_fluid.F90:539-549): left, right, bottom, top; a null input is zero
-    v = a.in ? a.in[idx] : 0.0;
+    v = in ? in[idx] : 0.0;
     int I = j + 2, J = row + 2;
     if (I == 2) v = v + a.fac * a.ring[g.left + J - 1];
     if (I == g.m) v = v + a.fac * a.ring[g.right + J - 1];
@@ -321,7 +322,10 @@ __device__ __forceinline__ double x_load(const DstXArgs& a, const GridDims& g, i
 }
 
 template <int PRE>
-__global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, DstXArgs a, GridDims g, int B) {
+__global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, const __grid_constant__ DstXArgs a,
+                                               GridDims g, int B) {
+  const double* ain = a.nlev ? a.lin[blockIdx.y] : a.in;
+  double* aout = a.nlev ? a.lout[blockIdx.y] : a.out;
   extern __shared__ double2 smem2[];
   __shared__ int s_mode[64];
   __shared__ int s_any;
@@ -359,7 +363,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, Dst
         v[u] = 0.0;
         if (it < tot) {
           int b = pl.fd_N.div(it), j = it - b * N;
-          if (s_mode[b] == ROW_FFT) v[u] = x_load<PRE>(a, g, s_row[b], j, nrows, N, ld);
+          if (s_mode[b] == ROW_FFT) v[u] = x_load<PRE>(a, ain, g, s_row[b], j, nrows, N, ld);
         }
       }
 #pragma unroll
@@ -384,8 +388,8 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, Dst
     if (mode == ROW_FFT) {
       v = xb[b * ldx + j];
     } else if (mode == ROW_EDGES) {
-      double x1 = x_load<PRE>(a, g, row, 0, nrows, N, ld);
-      double xn = x_load<PRE>(a, g, row, N - 1, nrows, N, ld);
+      double x1 = x_load<PRE>(a, ain, g, row, 0, nrows, N, ld);
+      double xn = x_load<PRE>(a, ain, g, row, N - 1, nrows, N, ld);
       int k = j + 1;
       double sk = __ldg(&pl.sn[k <= pl.P ? k : pl.M - k]);
       v = 2.0 * sk * ((k & 1) ? x1 + xn : x1 - xn);
@@ -393,7 +397,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, Dst
       v = 0.0;
     }
     if (a.post_add) v = fma(a.post_scale, a.post_add[o], v);
-    a.out[o] = v;
+    aout[o] = v;
   }
 }
 
@@ -437,6 +441,83 @@ __global__ void k_dst_ring_rows(int N, GridDims g, const double* __restrict__ ri
     size_t o = (size_t)r * g.nsx + k;
     out[o] = post_add ? fma(post_scale, post_add[o], acc) : acc;
   }
+}
+
+// out = post_scale*post_add + S_x(apply_bc(ring)) on every row (operators_fluid.F90:539-549 with
+// factor 1 on a zero field).  The first nEdge CTAs take the two edge rows 0 and n-2, whose
+// boundary field is a full row: both rows are built once per CTA in shared memory and one warp
+// per mode k reads row k of the (symmetric) DST matrix once for both dot products.  The other
+// CTAs take the interior rows, whose boundary field is zero except x_1 = ring(left) and
+// x_N = ring(right): Y_k = 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N).  In place allowed.
+__global__ void __launch_bounds__(256) k_dst_bc_modes(DstDev pl, GridDims g, const double* __restrict__ ring,
+                                                      const double* __restrict__ W,
+                                                      const double* __restrict__ post_add, double post_scale,
+                                                      double* __restrict__ out, int nEdge, int nColBlk) {
+  const int N = pl.N;
+  if ((int)blockIdx.x >= nEdge) {
+    const int b = blockIdx.x - nEdge;
+    const int r = b / nColBlk + 1;
+    const int k = (b - (r - 1) * nColBlk) * blockDim.x + threadIdx.x;
+    if (k >= N || r >= g.nsy - 1) return;
+    const int J = r + 2;
+    const double x1 = 0.0 + ring[g.left + J - 1];
+    const double xn = 0.0 + ring[g.right + J - 1];
+    const int kk = k + 1;
+    const double sk = __ldg(&pl.sn[kk <= pl.P ? kk : pl.M - kk]);
+    double v = 2.0 * sk * ((kk & 1) ? x1 + xn : x1 - xn);
+    const size_t o = (size_t)r * g.nsx + k;
+    if (post_add) v = fma(post_scale, post_add[o], v);
+    out[o] = v;
+    return;
+  }
+  extern __shared__ double bc[];   // 2 x N: rows 0 and n-2 of the boundary field
+  for (int q = threadIdx.x; q < 2 * N; q += blockDim.x) {
+    const int e = q / N, j = q - e * N;
+    const int I = j + 2, J = e == 0 ? 2 : g.n;
+    double v = 0.0;
+    if (I == 2) v = v + ring[g.left + J - 1];
+    if (I == g.m) v = v + ring[g.right + J - 1];
+    if (J == 2) v = v + ring[g.bottom + I - 1];
+    if (J == g.n) v = v + ring[g.top + I - 1];
+    bc[q] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (k >= N) return;
+  const double* wk = W + (size_t)k * N;
+  double a0 = 0.0, a1 = 0.0;
+#pragma unroll 5
+  for (int j = lane; j < N; j += 32) {
+    const double w = wk[j];
+    a0 = fma(bc[j], w, a0);
+    a1 = fma(bc[N + j], w, a1);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+  }
+  if (lane == 0) {
+    const size_t o0 = (size_t)k, o1 = (size_t)(g.nsy - 1) * g.nsx + k;
+    out[o0] = post_add ? fma(post_scale, post_add[o0], a0) : a0;
+    out[o1] = post_add ? fma(post_scale, post_add[o1], a1) : a1;
+  }
+}
+
+int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W,
+                   const double* post_add, double post_scale, double* out, cudaStream_t st) {
+  const int N = px.N;
+  const size_t smem = 2 * sizeof(double) * (size_t)N;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_dst_bc_modes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return IB_ERR_CUDA;
+  const int nEdge = cdiv(N, 8), nColBlk = cdiv(N, 256);
+  const int nblk = nEdge + nColBlk * std::max(0, g.nsy - 2);
+  DstDev d = to_dev(px);
+  count_launch();
+  k_dst_bc_modes<<<nblk, 256, smem, st>>>(d, g, ring, W, post_add, post_scale, out, nEdge, nColBlk);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
 }
 
 int dst_matrix_table(const DstPlan& px, double* dev_out) {
@@ -509,9 +590,10 @@ static int launch_cfg(K kern, size_t smem) {
 
 int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs& a, const GridDims& g,
                const DstLaunch& L, cudaStream_t st) {
+  if (a.nlev < 0 || a.nlev > kMaxBatch || (a.nlev && pre != PRE_COPY)) return IB_ERR_ARG;
   DstDev d = to_dev(px);
   size_t smem = dst_smem_x(px, L.B);
-  dim3 grid(cdiv(a.nlines ? a.nlines : nrows, L.B));
+  dim3 grid(cdiv(a.nlines ? a.nlines : nrows, L.B), a.nlev ? a.nlev : 1);
   int rc = IB_OK;
   switch (pre) {
     case PRE_COPY:

@@ -17,6 +17,7 @@
 namespace ib {
 
 constexpr int kMaxRadices = 16;
+constexpr int kMaxBatch = 16;   // levels one batched x pass can carry
 
 struct DstPlan {
   int N = 0, M = 0, P = 0;
@@ -63,6 +64,11 @@ struct DstXArgs {
   const int* rowrange = nullptr;
   // optional strided row subset: line i is row row0 + i*row_step, i < nlines (0: all rows)
   int nlines = 0, row0 = 0, row_step = 0;
+  // optional batch over grid levels (PRE_COPY only): level l (blockIdx.y) reads lin[l] and
+  // writes lout[l], each a full field of pitch ld; in/out are then unused
+  int nlev = 0;
+  const double* lin[kMaxBatch] = {};
+  double* lout[kMaxBatch] = {};
 };
 
 // Per-row treatment in the x pass.  ROW_EDGES: the row (after the pre-op) is zero
@@ -94,6 +100,11 @@ int dst_x_points(const DstPlan& px, const double* spec, int ld, const int2* pts,
 // + sum_j bc(r, j) W[j][k] for rows r in rows[0..nrows), one warp per output.
 int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, const int* rows, int nrows,
                     const double* W, const double* post_add, double post_scale, double* out, cudaStream_t st);
+// out = post_scale*post_add + S_x(apply_bc(ring)) on every row (factor 1, zero field): the two
+// edge rows by dot products with W, the interior rows in closed form
+// 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N).  In place allowed (out == post_add).
+int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W,
+                   const double* post_add, double post_scale, double* out, cudaStream_t st);
 size_t dst_smem_y(const DstPlan& p, int B, DstYMode mode);
 
 }  // namespace ib

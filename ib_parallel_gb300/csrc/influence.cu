@@ -132,8 +132,7 @@ __global__ void k_inf_bvec(const TorsBody* __restrict__ tb, TorsState ts, double
                            double* __restrict__ brv, double* __restrict__ bco, int* __restrict__ bod) {
   const int t = blockIdx.x;
   const TorsBody b = tb[t];
-  const double th = ts.theta[t];
-  const double sv = sin(b.gamma0 - th), cv = cos(b.gamma0 - th);
+  const double sv = ts.sinv[t], cv = ts.cosv[t];
   const double co = btimes_scale(b, dt, delta) / keff(b, dt);
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) {
     brv[b.off + j] = br_val(b, sv, cv, j);

@@ -58,6 +58,7 @@ struct TorsBody {
 };
 struct TorsState {  // device arrays of length nt
   double *theta, *thetad, *thetadd, *theta0, *thetad0, *thetadd0;
+  double *sinv, *cosv;  // sin, cos (gamma0 - theta) at the current theta, kept with theta
 };
 // BR_build (operators_struct.F90:319-338): x-rows (j-1) ds sin(g0-th),
 // y-rows -(j-1) ds cos(g0-th).  sn, cs = sin, cos(g0-th), evaluated once per body.
@@ -82,6 +83,8 @@ int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, do
 int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta,
                             const double* f, cudaStream_t st);
 int launch_tors_save(int nt, const TorsState& s, cudaStream_t st);
+// recomputes sinv, cosv from theta (after theta is set other than by k_tors_dx)
+int launch_tors_trig(int nt, const TorsBody* tb, const TorsState& s, cudaStream_t st);
 
 // gmres.cu -- PETSc KSPGMRES as configured in variables.F90:565-574.  Reductions over the
 // unknowns are summed per slice (kSlices contiguous slices of ceil(nf/kSlices)), then over

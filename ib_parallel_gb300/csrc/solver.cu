@@ -191,8 +191,9 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)g.nsx * g.nsx + (size_t)g.nsy;          // DST matrix, row treatments
   dbl += (size_t)g.m + g.n + 8;                          // get_bc points, edge rows
   dbl += (size_t)(L + 3) * nbc;                          // rings
+  dbl += (size_t)L * ns + (size_t)L * nbc + 2 * L;       // per-level spectra and rings (vort2flux)
   dbl += 7 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
-  dbl += 6 * (size_t)nt + nt + 1;
+  dbl += 8 * (size_t)nt + nt + 3;
   dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 4 * (size_t)nf + 2;
   if (p.num_stat) dbl += (size_t)nf * nf;
   dbl += 8 * stage_n;
@@ -223,6 +224,8 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->nly = P.take<double>(nv); c->hy = P.take<double>(nv);
   lv(c->lastbc, nbc);
   c->omegabc = P.take<double>(nbc); c->sbc = P.take<double>(nbc); c->zero_ring = P.take<double>(nbc);
+  c->hat.resize(L); c->ringv.resize(L);
+  for (int k = 0; k < L; ++k) { c->hat[k] = P.take<double>(ns); c->ringv[k] = P.take<double>(nbc); }
   c->f = P.take<double>(nf); c->f_rdst = P.take<double>(nf); c->xb = P.take<double>(nf);
   c->yb = P.take<double>(nf); c->rhsf = P.take<double>(nf); c->tmpf = P.take<double>(nf);
   c->tmpf2 = P.take<double>(nf); c->forces = P.take<double>(2 * nbody + 1);
@@ -236,6 +239,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->ts.theta = P.take<double>(nt + 1); c->ts.thetad = P.take<double>(nt + 1);
   c->ts.thetadd = P.take<double>(nt + 1); c->ts.theta0 = P.take<double>(nt + 1);
   c->ts.thetad0 = P.take<double>(nt + 1); c->ts.thetadd0 = P.take<double>(nt + 1);
+  c->ts.sinv = P.take<double>(nt + 1); c->ts.cosv = P.take<double>(nt + 1);
   c->err_fsi = P.take<double>(nt + 1);
   c->G.nf = nf; c->G.restart = R;
   c->G.V = P.take<double>((size_t)(R + 1) * nf); c->G.H = P.take<double>((size_t)(R + 1) * R);
@@ -344,6 +348,8 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     IB_CUDA_CHECK(cudaMemcpy(c->bid, c->bid_h.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
   }
   if (nt > 0) IB_CUDA_CHECK(cudaMemcpy(c->tb, c->tb_h.data(), sizeof(TorsBody) * nt, cudaMemcpyHostToDevice));
+  rc = launch_tors_trig(nt, c->tb, c->ts, c->st);
+  if (rc != IB_OK) { *msg = "device initialisation failed"; ctx_destroy(c); return rc; }
   for (int i = 0; i < nbody; ++i) c->bodies_h.push_back(bodies[i]);
 
   // default launch shapes, then tuned by timing
@@ -372,6 +378,8 @@ void ctx_destroy(Ctx* c) {
   if (c->solve_exec) cudaGraphExecDestroy(c->solve_exec);
   if (c->solve_graph) cudaGraphDestroy(c->solve_graph);
   if (c->solve_exec_dense) cudaGraphExecDestroy(c->solve_exec_dense);
+  for (PhaseGraph* ph : {&c->graph_pred, &c->graph_v2f, &c->graph_corr})
+    if (ph->exec) cudaGraphExecDestroy(ph->exec);
   if (c->solve_graph_dense) cudaGraphDestroy(c->solve_graph_dense);
   inf_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
@@ -456,20 +464,52 @@ int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs
   return spectral_solve(c, PRE_PRED, a, c->tri_pred[k], om);
 }
 
+static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring);
+
 // vort2flux (operators_fluid.F90:237-377).  all_curls=false computes the fluxes
-// of the finest level only (the Schur operator reads nothing else).
+// of the finest level only.
+//
+// Only the boundary values a level receives from the next coarser one depend on the
+// coarse-to-fine recursion, and they enter through apply_bc on the boundary rows and
+// columns.  So the x transforms of every level's vorticity run as one batched pass; then,
+// coarse to fine in mode space, each level adds the transform of its boundary terms
+// (closed form on interior rows, dot products on the two edge rows), solves its per-mode
+// tridiagonal systems and evaluates the next finer level's ring from its modes at the few
+// points get_bc reads; one batched inverse pass and the curls finish.
 int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy, bool all_curls) {
   const int L = c->L;
   const GridDims& g = c->g;
-  for (int k = 1; k < L; ++k) RC(launch_coarsify(g, w[k - 1], w[k], c->st));
-  RC(op_ctci(c, w[L - 1], s[L - 1], nullptr));
-  if (all_curls || L == 1) RC(launch_curl(g, s[L - 1], c->zero_ring, qx[L - 1], qy[L - 1], c->st));
-  if (L > 1) RC(launch_get_bc(g, s[L - 1], 1.0, c->sbc, c->st));
-  for (int k = L - 2; k >= 0; --k) {
-    RC(op_ctci(c, w[k], s[k], c->sbc));
-    if (all_curls || k == 0) RC(launch_curl(g, s[k], c->sbc, qx[k], qy[k], c->st));
-    if (k > 0) RC(launch_get_bc(g, s[k], 1.0, c->sbc, c->st));
+  cudaStream_t st = c->st;
+  if (L > kMaxBatch) return IB_ERR_ARG;
+  for (int k = 1; k < L; ++k) RC(launch_coarsify(g, w[k - 1], w[k], st));
+  {
+    DstXArgs a;
+    a.nlev = L;
+    for (int k = 0; k < L; ++k) { a.lin[k] = w[k]; a.lout[k] = c->hat[k]; }
+    ProfScope ps(c, 0, pass_bytes(c, L, L));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
   }
+  for (int k = L - 1; k >= 0; --k) {
+    double* F = c->hat[k];
+    if (k < L - 1) {
+      // boundary terms from the ring of level k (get_bc of level k+1), apply_bc with fac 1
+      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, F, 1.0, F, st));
+    }
+    {
+      ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+      RC(tri_solve(c->tri_ctci, F, F, g.nsx, c->tl, st));
+    }
+    if (k > 0) RC(ring_from_modes(c, F, s[k], c->ringv[k - 1]));
+  }
+  {
+    DstXArgs a;
+    a.nlev = L;
+    for (int k = 0; k < L; ++k) { a.lin[k] = c->hat[k]; a.lout[k] = s[k]; }
+    ProfScope ps(c, 0, pass_bytes(c, L, L));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
+  }
+  for (int k = L - 1; k >= 0; --k)
+    if (all_curls || k == 0) RC(launch_curl(g, s[k], k == L - 1 ? c->zero_ring : c->ringv[k], qx[k], qy[k], st));
   return IB_OK;
 }
 
@@ -542,12 +582,8 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
   {
     // S_x(vort1 + apply_bc(ring0)) = 2m Y + transform of the boundary terms: the two full
     // boundary rows by dot products, the others in closed form (two nonzero samples)
-    RC(dst_x_ring_rows(c->px, g, ring0, c->edge_rows, 2, c->wmat, c->specY, 2.0 * g.m, c->spec1, st));
-    DstXArgs a;
-    a.in = nullptr; a.ring = ring0; a.fac = 1.0; a.out = c->spec1; a.rowmode = c->rm_fine;
-    a.post_add = c->specY; a.post_scale = 2.0 * g.m;
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_APPLYBC, a, g, c->lx, st));
+    RC(dst_x_bc_modes(c->px, g, ring0, c->wmat, c->specY, 2.0 * g.m, c->spec1, st));
   }
   mark(5);
   {
@@ -850,6 +886,38 @@ static void step_acc(Ctx* c, int ph, int a, int b) {
   if (cudaEventElapsedTime(&t, c->step_ev[a], c->step_ev[b]) == cudaSuccess) c->step_ms[ph] += t;
 }
 
+// Runs one fixed phase of the step (the same kernels on the same buffers every step) through a
+// CUDA graph captured on first use, which removes the gaps between its dependent launches.
+// If capture fails the phase runs directly from then on.
+template <typename F>
+static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
+  if (!c->use_step_graphs || c->prof_on || c->stage_on || ph.failed) return fn();
+  if (!ph.exec) {
+    const long long l0 = launch_count();
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      cudaGetLastError();
+      ph.failed = true;
+      return fn();
+    }
+    const int rc = fn();
+    const cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+    ph.launches = launch_count() - l0;
+    count_launches(-ph.launches);   // captured, not run
+    if (rc != IB_OK || e != cudaSuccess || cudaGraphInstantiate(&ph.exec, graph, 0) != cudaSuccess) {
+      cudaGetLastError();
+      if (graph) cudaGraphDestroy(graph);
+      ph.exec = nullptr;
+      ph.failed = true;
+      return fn();
+    }
+    cudaGraphDestroy(graph);
+  }
+  IB_CUDA_CHECK(cudaGraphLaunch(ph.exec, c->st));
+  count_launches(ph.launches);
+  return IB_OK;
+}
+
 // timestepper.F90:18-556
 int op_advance(Ctx* c) {
   const GridDims& g = c->g;
@@ -860,25 +928,34 @@ int op_advance(Ctx* c) {
   const int it = c->itime;
   if (it == 1 && p.num_stat && c->nf > 0) RC(preprocess_chol(c));
   step_mark(c, 0);
-  // boundary values of the previous step (timestepper.F90:103-117)
-  for (int k = 0; k < L - 1; ++k) RC(launch_get_bc(g, c->omega[k + 1], 0.25, c->lastbc[k], st));
-  IB_CUDA_CHECK(cudaMemsetAsync(c->lastbc[L - 1], 0, 8 * (size_t)g.nbc, st));
-  // predictor, coarse to fine (timestepper.F90:121-236)
-  for (int k = L - 1; k >= 0; --k) {
-    const double* obc = c->zero_ring;
-    if (k < L - 1) {
-      RC(launch_get_bc(g, c->omega[k + 1], 0.25, c->omegabc, st));
-      obc = c->omegabc;
+  // boundary values of the previous step (timestepper.F90:103-117) and the predictor, coarse
+  // to fine (timestepper.F90:121-236)
+  auto predictor = [&]() -> int {
+    for (int k = 0; k < L - 1; ++k) RC(launch_get_bc(g, c->omega[k + 1], 0.25, c->lastbc[k], c->st));
+    IB_CUDA_CHECK(cudaMemsetAsync(c->lastbc[L - 1], 0, 8 * (size_t)g.nbc, c->st));
+    for (int k = L - 1; k >= 0; --k) {
+      const double* obc = c->zero_ring;
+      if (k < L - 1) {
+        RC(launch_get_bc(g, c->omega[k + 1], 0.25, c->omegabc, c->st));
+        obc = c->omegabc;
+      }
+      RC(launch_nonlinear(g, c->omega[k], c->lastbc[k], c->qx[k], c->q0x[k], c->qy[k], c->q0y[k], c->nlx, c->nly,
+                          c->st));
+      RC(launch_rhsbc(g, c->rhsbc, c->lastbc[k], obc, c->vfac[k], c->st));
+      RC(launch_rot(g, c->nlx, c->nly, c->rhs, c->st));
+      if (it == 1)
+        IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs, 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, c->st));
+      RC(op_predictor(c, k, c->omega[k], c->rhs, c->rhs_old[k], c->rhsbc));
+      IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs, 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, c->st));
     }
-    RC(launch_nonlinear(g, c->omega[k], c->lastbc[k], c->qx[k], c->q0x[k], c->qy[k], c->q0y[k], c->nlx, c->nly, st));
-    RC(launch_rhsbc(g, c->rhsbc, c->lastbc[k], obc, c->vfac[k], st));
-    RC(launch_rot(g, c->nlx, c->nly, c->rhs, st));
-    if (it == 1) IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs, 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, st));
-    RC(op_predictor(c, k, c->omega[k], c->rhs, c->rhs_old[k], c->rhsbc));
-    IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs, 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, st));
-  }
+    return IB_OK;
+  };
+  if (it == 1) RC(predictor());   // the first step also seeds rhs_old
+  else RC(run_phase(c, c->graph_pred, predictor));
   step_mark(c, 1);
-  RC(op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true));
+  RC(run_phase(c, c->graph_v2f, [&]() {
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true);
+  }));
   step_mark(c, 2);
   // forces (timestepper.F90:249-486)
   if (c->nf > 0) {
@@ -934,11 +1011,13 @@ int op_advance(Ctx* c) {
   }
   // correction on the finest grid (timestepper.F90:488-553)
   step_mark(c, 8);
-  RC(launch_reg(g, c->nf, c->f, c->reg, c->hx, c->hy, st));
-  RC(launch_rot(g, c->hx, c->hy, c->vort, st));
-  RC(op_ainv(c, c->vort, c->vort));
-  RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], st));
-  RC(op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true));
+  RC(run_phase(c, c->graph_corr, [&]() -> int {
+    RC(launch_reg(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
+    RC(launch_rot(g, c->hx, c->hy, c->vort, c->st));
+    RC(op_ainv(c, c->vort, c->vort));
+    RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], c->st));
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true);
+  }));
   step_mark(c, 9);
   int rc = check_err(c);
   if (c->step_prof) {

@@ -34,8 +34,7 @@ __device__ double block_sum(double v) {
 __global__ void k_tors_btimes(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
                               const double* __restrict__ x, double* __restrict__ y) {
   TorsBody b = tb[blockIdx.x];
-  double th = s.theta[blockIdx.x];
-  double sn = sin(b.gamma0 - th), cs = cos(b.gamma0 - th);
+  double sn = s.sinv[blockIdx.x], cs = s.cosv[blockIdx.x];
   double part = 0.0;
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn, cs, j) * x[b.off + j];
   double dot = block_sum(part);
@@ -55,7 +54,7 @@ __global__ void k_tors_rhs(const TorsBody* __restrict__ tb, TorsState s, double 
               (I * (4.0 / (dt * dt) * th0 + 4.0 / dt * thd0 + thdd0) + C * (thd0 + 2.0 / dt * th0) -
                (4.0 / (dt * dt) * I + 2.0 / dt * C + K) * th);
   double c = delta * (rth - jr - thd);
-  double sn = sin(b.gamma0 - th), cs = cos(b.gamma0 - th);
+  double sn = s.sinv[t], cs = s.cosv[t];
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = br_val(b, sn, cs, j) * c;
 }
 
@@ -67,7 +66,7 @@ __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double d
   TorsBody b = tb[t];
   double th = s.theta[t], th0 = s.theta0[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
   double I = b.itheta, C = b.ctheta, K = b.ktheta;
-  double sn0 = sin(b.gamma0 - th), cs0 = cos(b.gamma0 - th);
+  double sn0 = s.sinv[t], cs0 = s.cosv[t];
   double part = 0.0;
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn0, cs0, j) * f[b.off + j];
   double brf = block_sum(part);
@@ -85,6 +84,11 @@ __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double d
   }
   double g = b.gamma0 - thn;
   double cg = cos(g), sg = sin(g);
+  __syncthreads();   // every thread has read the old sinv, cosv
+  if (threadIdx.x == 0) {
+    s.sinv[t] = sg;
+    s.cosv[t] = cg;
+  }
   for (int j = threadIdx.x; j < b.npts; j += blockDim.x) {
     double px = b.xbf0 + (double)j * b.deltas * cg;
     double py = b.ybf0 + (double)j * b.deltas * sg;
@@ -106,7 +110,7 @@ __global__ void k_tors_initial_acc(const TorsBody* __restrict__ tb, TorsState s,
   int t = blockIdx.x;
   TorsBody b = tb[t];
   double th = s.theta[t];
-  double sn = sin(b.gamma0 - th), cs = cos(b.gamma0 - th);
+  double sn = s.sinv[t], cs = s.cosv[t];
   double part = 0.0;
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn, cs, j) * f[b.off + j];
   double brf = block_sum(part);
@@ -115,6 +119,14 @@ __global__ void k_tors_initial_acc(const TorsBody* __restrict__ tb, TorsState s,
     double ftint = b.ktheta * th;
     s.thetadd[t] = 1.0 / b.itheta * (-b.ctheta * s.thetad[t] - ftint + brf * b.deltas);
   }
+}
+
+__global__ void k_tors_trig(int nt, const TorsBody* __restrict__ tb, TorsState s) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  double g = tb[t].gamma0 - s.theta[t];
+  s.sinv[t] = sin(g);
+  s.cosv[t] = cos(g);
 }
 
 __global__ void k_tors_save(int nt, TorsState s) {
@@ -163,6 +175,14 @@ int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, doub
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
+int launch_tors_trig(int nt, const TorsBody* tb, const TorsState& s, cudaStream_t st) {
+  if (nt == 0) return IB_OK;
+  count_launch();
+  k_tors_trig<<<cdiv(nt, 64), 64, 0, st>>>(nt, tb, s);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
 int launch_tors_save(int nt, const TorsState& s, cudaStream_t st) {
   if (nt == 0) return IB_OK;
   count_launch();
