@@ -75,8 +75,13 @@ struct Influence {
 struct PhaseGraph {
   cudaGraphExec_t exec = nullptr;
   long long launches = 0;   // kernels in the graph
+  long long passes[4] = {0, 0, 0, 0};   // DST passes by kind in the graph
   bool failed = false;
 };
+inline void drop_phase(PhaseGraph* ph) {
+  if (ph->exec) cudaGraphExecDestroy(ph->exec);
+  *ph = PhaseGraph{};
+}
 
 struct Ctx {
   IbParams p{};
@@ -143,6 +148,9 @@ struct Ctx {
   // predictor, first vort2flux and correction as graphs (from the second step on)
   bool use_step_graphs = true;
   PhaseGraph graph_pred, graph_v2f, graph_corr;
+  // FSI iteration: right-hand side, Schur assembly, update (redistribute, structure, weights)
+  PhaseGraph graph_fsi_rhs, graph_fsi_asm, graph_fsi_upd;
+  FusedPlan fused_plan;
   double* cholM = nullptr;         // nf x nf (num_stat)
   bool chol_ready = false;
 
@@ -210,6 +218,7 @@ int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
 int inf_patch(Ctx* c);                 // patches + flag for the current weights (async)
 int inf_prepare(Ctx* c);               // build/rebuild the band if needed, assemble S
+int inf_assemble(Ctx* c);              // the assembly kernels only
 int inf_dense_mv(Ctx* c, const double* x, double* y);   // (S + B) x
 int inf_build(Ctx* c);
 int op_redistribute(Ctx* c, const double* f, double* frdst);

@@ -617,39 +617,47 @@ __global__ void __cluster_dims__(kSlices, 1, 1)
   cl.sync();                                      // no CTA exits while others read its memory
 }
 
-int launch_gmres_fused(const GmresDev& G, const double* At, const double* b, double* x, double rtol, double atol,
-                       int max_it, cudaStream_t st) {
-  if (G.nf <= 0 || G.restart > 63) return IB_ERR_ARG;
-  ClusterSmem cs{G.nf, G.restart, (G.nf + kSlices - 1) / kSlices};
-  // at least R+1 work threads: one per projection of the longest Arnoldi step
-  const int work = max(64, 32 * ((cs.ns * kSlices + 31) / 32));
-  const int threads = work + 32;
-  if (threads > 1024) return IB_ERR_ARG;
-  int dev = 0, optin = 0;
-  IB_CUDA_CHECK(cudaGetDevice(&dev));
-  IB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const size_t limit = (size_t)optin - 1024;
-  int a_in = 1;
-  size_t bytes = 8 * cs.with_a();
-  if (bytes > limit) {
-    a_in = 0;
-    bytes = 8 * cs.base();
-    if (bytes > limit) return IB_ERR_ARG;
+int launch_gmres_fused(const GmresDev& G, FusedPlan* plan, const double* At, const double* b, double* x, double rtol,
+                       double atol, int max_it, cudaStream_t st) {
+  if (plan->state < 0) {
+    plan->state = 0;
+    if (G.nf <= 0 || G.restart > 63) return IB_ERR_ARG;
+    ClusterSmem cs{G.nf, G.restart, (G.nf + kSlices - 1) / kSlices};
+    // at least R+1 work threads: one per projection of the longest Arnoldi step
+    const int work = max(64, 32 * ((cs.ns * kSlices + 31) / 32));
+    const int threads = work + 32;
+    if (threads > 1024) return IB_ERR_ARG;
+    int dev = 0, optin = 0;
+    IB_CUDA_CHECK(cudaGetDevice(&dev));
+    IB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t limit = (size_t)optin - 1024;
+    int a_in = 1;
+    size_t bytes = 8 * cs.with_a();
+    if (bytes > limit) {
+      a_in = 0;
+      bytes = 8 * cs.base();
+      if (bytes > limit) return IB_ERR_ARG;
+    }
+    IB_CUDA_CHECK(cudaFuncSetAttribute(k_gmres_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    // the cluster must fit on the device as launched
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kSlices);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.stream = st;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_gmres_cluster, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      return IB_ERR_ARG;
+    }
+    plan->threads = threads;
+    plan->a_in = a_in;
+    plan->bytes = bytes;
+    plan->state = 1;
   }
-  IB_CUDA_CHECK(cudaFuncSetAttribute(k_gmres_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  // the cluster must fit on the device as launched
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kSlices);
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = bytes;
-  cfg.stream = st;
-  int nclusters = 0;
-  if (cudaOccupancyMaxActiveClusters(&nclusters, k_gmres_cluster, &cfg) != cudaSuccess || nclusters < 1) {
-    cudaGetLastError();
-    return IB_ERR_ARG;
-  }
+  if (plan->state != 1) return IB_ERR_ARG;
   count_launch();
-  k_gmres_cluster<<<kSlices, threads, bytes, st>>>(G, At, a_in, b, x, rtol, atol, max_it);
+  k_gmres_cluster<<<kSlices, plan->threads, plan->bytes, st>>>(G, At, plan->a_in, b, x, rtol, atol, max_it);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

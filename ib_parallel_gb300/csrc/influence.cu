@@ -326,6 +326,9 @@ int inf_build(Ctx* c) {
   I.ntile = (int)I.tiles_h.size();
   I.nR = I.ntile * kP;
   I.built = false;
+  // the captured FSI phases bake in the band's buffers and size
+  drop_phase(&c->graph_fsi_asm);
+  drop_phase(&c->graph_fsi_upd);
   I.active = false;
   if (I.nR == 0) return IB_ERR_STATE;
   const size_t nK = (size_t)I.nR * I.nR;
@@ -397,6 +400,15 @@ int inf_prepare(Ctx* c) {
     RC(read_flag(c));
     if (I.flag_h) { I.fallbacks += 1; return IB_OK; }
   }
+  RC(inf_assemble(c));
+  I.assemblies += 1;
+  I.active = true;
+  return IB_OK;
+}
+
+// The assembly kernels alone (no host decisions): S, St from K and the current patches.
+int inf_assemble(Ctx* c) {
+  Influence& I = c->inf;
   cudaStream_t st = c->st;
   count_launch();
   k_inf_compact<<<1, 1024, 0, st>>>(I.nR, I.used, I.ulist, I.upos, I.nu);
@@ -410,8 +422,6 @@ int inf_prepare(Ctx* c) {
   count_launch();
   k_inf_ptk<<<c->nf, 128, 0, st>>>(c->nf, I.nR, I.pval, I.pidx, I.upos, I.T, I.brv, I.bco, I.bod, I.S, I.St);
   IB_CUDA_CHECK(cudaGetLastError());
-  I.assemblies += 1;
-  I.active = true;
   return IB_OK;
 }
 

@@ -112,12 +112,18 @@ int launch_gmres_arnoldi(const GmresDev& G, int max_it, cudaStream_t st, cudaGra
 int launch_gmres_update(const GmresDev& G, double* x, int max_it, cudaStream_t st, cudaGraphConditionalHandle h = 0,
                         int use_cond = 0);
 int launch_copy(int n, const double* a, double* b, cudaStream_t st);
+// Launch shape of the cluster solver, worked out on first use (state -1) and kept.
+struct FusedPlan {
+  int state = -1;   // 1 launchable, 0 not (the problem does not fit the cluster)
+  int threads = 0, a_in = 0;
+  size_t bytes = 0;
+};
 // The whole solve on a dense operator A, column-major (At[j*nf + r] = A[r][j]), as one
 // cluster of kSlices CTAs: the operations of the start / arnoldi / update kernels in the same
 // order, with A applied by the same segmented row products as k_dense_mv.  Writes G.ist like
 // them.  Returns IB_ERR_ARG (nothing launched) when the problem does not fit the cluster.
-int launch_gmres_fused(const GmresDev& G, const double* At, const double* b, double* x, double rtol, double atol,
-                       int max_it, cudaStream_t st);
+int launch_gmres_fused(const GmresDev& G, FusedPlan* plan, const double* At, const double* b, double* x, double rtol,
+                       double atol, int max_it, cudaStream_t st);
 
 // dense symmetric positive definite solve (stationary-body path)
 int launch_cholesky(int n, double* A, int* d_err, cudaStream_t st);

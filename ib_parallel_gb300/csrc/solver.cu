@@ -378,8 +378,9 @@ void ctx_destroy(Ctx* c) {
   if (c->solve_exec) cudaGraphExecDestroy(c->solve_exec);
   if (c->solve_graph) cudaGraphDestroy(c->solve_graph);
   if (c->solve_exec_dense) cudaGraphExecDestroy(c->solve_exec_dense);
-  for (PhaseGraph* ph : {&c->graph_pred, &c->graph_v2f, &c->graph_corr})
-    if (ph->exec) cudaGraphExecDestroy(ph->exec);
+  for (PhaseGraph* ph : {&c->graph_pred, &c->graph_v2f, &c->graph_corr, &c->graph_fsi_rhs, &c->graph_fsi_asm,
+                         &c->graph_fsi_upd})
+    drop_phase(ph);
   if (c->solve_graph_dense) cudaGraphDestroy(c->solve_graph_dense);
   inf_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
@@ -793,7 +794,7 @@ int op_gmres(Ctx* c, const double* b, double* x, int* its, int* reason) {
   const bool dense = c->inf.active;
   if (dense && c->use_fused) {
     // the whole solve in one kernel on the assembled matrix
-    int rc = launch_gmres_fused(G, c->inf.St, b, x, c->p.rtol, c->p.atol, max_it, c->st);
+    int rc = launch_gmres_fused(G, &c->fused_plan, c->inf.St, b, x, c->p.rtol, c->p.atol, max_it, c->st);
     if (rc == IB_OK) {
       RC(read_ist(c));
       c->n_matvec += c->h_ist[0] + c->h_ist[4];
@@ -894,6 +895,8 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
   if (!c->use_step_graphs || c->prof_on || c->stage_on || ph.failed) return fn();
   if (!ph.exec) {
     const long long l0 = launch_count();
+    long long p0[4];
+    for (int i = 0; i < 4; ++i) p0[i] = c->n_pass[i];
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
       cudaGetLastError();
@@ -904,6 +907,10 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
     const cudaError_t e = cudaStreamEndCapture(c->st, &graph);
     ph.launches = launch_count() - l0;
     count_launches(-ph.launches);   // captured, not run
+    for (int i = 0; i < 4; ++i) {
+      ph.passes[i] = c->n_pass[i] - p0[i];
+      c->n_pass[i] = p0[i];
+    }
     if (rc != IB_OK || e != cudaSuccess || cudaGraphInstantiate(&ph.exec, graph, 0) != cudaSuccess) {
       cudaGetLastError();
       if (graph) cudaGraphDestroy(graph);
@@ -915,6 +922,7 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
   }
   IB_CUDA_CHECK(cudaGraphLaunch(ph.exec, c->st));
   count_launches(ph.launches);
+  for (int i = 0; i < 4; ++i) c->n_pass[i] += ph.passes[i];
   return IB_OK;
 }
 
@@ -965,39 +973,77 @@ int op_advance(Ctx* c) {
       double err = 10.0;
       int fsi_count = 0;
       c->ksp_iter = 0;
+      const bool moved = c->nt > 0;
       while (err >= p.fsi_tol && fsi_count <= p.fsi_max_it) {
         fsi_count += 1;
         step_mark(c, 3);
-        IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, st));
-        RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, st));
-        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, st));
-        int its = 0, reason = 0;
+        RC(run_phase(c, c->graph_fsi_rhs, [&]() -> int {
+          IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, c->st));
+          RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, c->st));
+          return launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, c->st);
+        }));
         step_mark(c, 4);
-        RC(inf_prepare(c));
-        step_mark(c, 5);
-        RC(op_gmres(c, c->rhsf, c->f, &its, &reason));
-        step_mark(c, 6);
-        c->ksp_iter += its;
-        RC(op_redistribute(c, c->f, c->f_rdst));
-        RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, st));
-        const bool moved = c->nt > 0;
-        if (moved) RC(op_reg_prep(c));
-        // the next solve's patches, checked against the band with the same synchronisation
-        const bool patch = moved && p.schur_mode != 1 && c->inf.built;
-        if (patch) {
-          RC(inf_patch(c));
-          IB_CUDA_CHECK(cudaMemcpyAsync(c->inf.h_flag, c->inf.flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        // Schur operator at the current positions: the band is valid and every patch lies in
+        // it (checked at the end of the previous iteration) -> the captured assembly; else
+        // the host path (build / rebuild / matrix-free fallback)
+        Influence& I = c->inf;
+        if (p.schur_mode != 1 && I.built && I.patch_fresh && I.flag_h == 0) {
+          RC(run_phase(c, c->graph_fsi_asm, [&]() { return inf_assemble(c); }));
+          I.assemblies += 1;
+          I.active = true;
+        } else {
+          RC(inf_prepare(c));
         }
-        IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st));
+        step_mark(c, 5);
+        // the cluster solver's counters come back with this iteration's synchronisation
+        bool async = false;
+        if (I.active && c->use_fused) {
+          int rc = launch_gmres_fused(c->G, &c->fused_plan, I.St, c->rhsf, c->f, p.rtol, p.atol, p.gmres_max_it,
+                                      c->st);
+          if (rc == IB_OK) {
+            IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->G.ist, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+            async = true;
+          } else if (rc != IB_ERR_ARG) {
+            return rc;
+          }
+        }
+        if (!async) {
+          int its = 0, reason = 0;
+          RC(op_gmres(c, c->rhsf, c->f, &its, &reason));
+          c->ksp_iter += its;
+        }
+        step_mark(c, 6);
+        // redistribute, structure update, weights at the new positions and the next solve's
+        // patches (checked against the band with the same synchronisation)
+        const bool patch = moved && p.schur_mode != 1 && I.built;
+        RC(run_phase(c, c->graph_fsi_upd, [&]() -> int {
+          RC(op_redistribute(c, c->f, c->f_rdst));
+          RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, c->st));
+          if (moved) RC(op_reg_prep(c));
+          if (patch) {
+            RC(inf_patch(c));
+            IB_CUDA_CHECK(cudaMemcpyAsync(I.h_flag, I.flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+          }
+          IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+          return IB_OK;
+        }));
+        if (moved) {   // what op_reg_prep records on the host (not replayed by the graph)
+          I.patch_fresh = false;
+          I.active = false;
+        }
         step_mark(c, 7);
         IB_CUDA_CHECK(cudaStreamSynchronize(st));
         step_acc(c, 2, 3, 4);
         step_acc(c, 3, 4, 5);
         step_acc(c, 4, 5, 6);
         step_acc(c, 5, 6, 7);
+        if (async) {
+          c->ksp_iter += c->h_ist[0];
+          c->n_matvec += c->h_ist[0] + c->h_ist[4];
+        }
         if (patch) {
-          c->inf.flag_h = c->inf.h_flag[0];
-          c->inf.patch_fresh = true;
+          I.flag_h = I.h_flag[0];
+          I.patch_fresh = true;
         }
         err = c->h_scal[0];
         if (!std::isfinite(err)) return IB_ERR_NONFINITE;
