@@ -93,7 +93,6 @@ static int tune(Ctx* c) {
     TriLaunch bestT = c->tl;
     for (int Mb : {1, 2, 4, 8, 16, 32}) {
       if (Mb * c->tri_ctci.C > 1024 || (long long)tri_smem(c->tri_ctci, Mb) > smem_max) continue;
-      if ((Mb * c->tri_ctci.C) % 32 != 0 && Mb * c->tri_ctci.C > 32) continue;  // whole warps only
       TriLaunch T; T.Mb = Mb;
       float ms = 0;
       auto run = [&]() -> int { return tri_solve(c->tri_ctci, c->spec1, c->spec1, c->g.nsx, T, c->st); };
@@ -1060,7 +1059,19 @@ int op_advance(Ctx* c) {
   RC(run_phase(c, c->graph_corr, [&]() -> int {
     RC(launch_reg(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
     RC(launch_rot(g, c->hx, c->hy, c->vort, c->st));
-    RC(op_ainv(c, c->vort, c->vort));
+    // ainv of rot(E^T f): the input is zero outside the rows the body's stencils touch, so
+    // the forward transform runs on those rows only (the others' modes are zero)
+    if (c->nf > 0) {
+      DstXArgs a;
+      a.in = c->vort; a.out = c->spec1; a.rowrange = c->reg.bbox + 4;
+      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, c->st));
+      RC(tri_solve(c->tri_ainv, c->spec1, c->spec1, g.nsx, c->tl, c->st));
+      DstXArgs b;
+      b.in = c->spec1; b.out = c->vort;
+      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx, c->st));
+    } else {
+      RC(op_ainv(c, c->vort, c->vort));
+    }
     RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], c->st));
     return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true);
   }));
