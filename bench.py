@@ -73,9 +73,13 @@ def _peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region.
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Sampling starts before the region (the first sample is awaited) at 50 ms intervals; each
+    sample carries nvidia-smi's timestamp, and the summary keeps the samples that fall inside
+    the region marked by begin()/end()."""
+
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -83,15 +87,26 @@ class Clocks:
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         self.p = None
         self.gpu = gpu_index
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        deadline = time.time() + 5.0
+        while self.p and time.time() < deadline and not self._rows():
+            time.sleep(0.02)
         return self
+
+    def begin(self):
+        self.t0 = time.time()
+
+    def end(self):
+        self.t1 = time.time()
+        time.sleep(0.1)   # let a sample taken at the end of the region reach the file
 
     def __exit__(self, *a):
         if self.p:
@@ -101,24 +116,45 @@ class Clocks:
             except Exception:
                 self.p.kill()
 
-    def summary(self):
+    def _rows(self):
         self.f.flush()
         rows = []
         try:
             for line in Path(self.f.name).read_text().splitlines():
                 parts = [x.strip() for x in line.split(",")]
-                if len(parts) >= 9:
+                if len(parts) >= 10:
                     rows.append(parts)
         except OSError:
             pass
+        return rows
+
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        try:
+            return datetime.datetime.strptime(text, "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
+    def summary(self):
+        rows = self._rows()
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        inside = rows
+        where = "all samples"
+        if self.t0 is not None and self.t1 is not None:
+            sel = [r for r in rows if (self._stamp(r[0]) or 0.0) >= self.t0 - 0.06 and
+                   (self._stamp(r[0]) or 0.0) <= self.t1 + 0.06]
+            if sel:
+                inside, where = sel, "samples inside the timed region"
+            else:
+                where = "no sample fell inside the timed region; all samples of the run"
+        sm = [float(r[2]) for r in inside if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in inside if r[3].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in inside for i in range(4) if r[6 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(inside), "source": where}
 
 
 def _dist():
@@ -247,6 +283,7 @@ def run_gpu(args, world, rank, local):
     with Clocks(local) as clk:
         if args.profile_window:
             torch.cuda.profiler.start()
+        clk.begin()
         e0.record(stream)
         for _ in range(args.steps):
             sim.advance()
@@ -255,6 +292,7 @@ def run_gpu(args, world, rank, local):
             fsi_sum += f
         e1.record(stream)
         e1.synchronize()
+        clk.end()
         if args.profile_window:
             torch.cuda.profiler.stop()
     torch.cuda.synchronize()
