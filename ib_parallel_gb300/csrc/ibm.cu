@@ -53,7 +53,7 @@ __device__ double deltafnc_dev(double x1, double x2, double dr) {
 // FP64-latency-bound evaluations run side by side), then every lane writes weights.
 __global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb, const double* __restrict__ yb,
                               double d, double ox, double oy, const int* __restrict__ comp, int* ix, int* iy,
-                              double* w, int* err) {
+                              double* w, int* stale, int* err) {
   const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (k >= nf) return;
@@ -63,6 +63,8 @@ __global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb,
   const double d2 = 0.5 * d;
   const bool isx = comp[k] == 1;
   if (lane == 0) {
+    // the contribution lists depend on the stencil origins only: rebuild them when one moved
+    if (ix[k] != cx || iy[k] != cy) atomicOr(stale, 1);
     ix[k] = cx;
     iy[k] = cy;
     // faces touched: u-face i in [1,m+1], j in [1,n]; v-face i in [1,m], j in [1,n+1]
@@ -95,8 +97,10 @@ __global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb,
 // Bounding box of all stencils (one CTA).  bbox[0..3] = i0, j0, ni, nj of the face box;
 // bbox[4..6] and bbox[7..9] = [first, last+1) vertex row (0-based) that rot(E^T f) can touch
 // and that E(curl s) reads, followed by the treatment of the other rows (zero / skip).
-__global__ void k_reg_bbox(GridDims g, int nf, const int* __restrict__ ix, const int* __restrict__ iy, int* bbox) {
+__global__ void k_reg_bbox(GridDims g, int nf, const int* __restrict__ ix, const int* __restrict__ iy, int* bbox,
+                           const int* __restrict__ stale) {
   __shared__ int s[4][32];
+  if (!*stale) return;
   int imin = 1 << 30, jmin = 1 << 30, imax = -(1 << 30), jmax = -(1 << 30);
   for (int k = threadIdx.x; k < nf; k += blockDim.x) {
     imin = min(imin, ix[k]); imax = max(imax, ix[k]);
@@ -132,7 +136,8 @@ __global__ void k_reg_bbox(GridDims g, int nf, const int* __restrict__ ix, const
 template <bool FILL>
 __global__ void k_reg_lists(int nf, const int* __restrict__ comp, const int* __restrict__ ix,
                             const int* __restrict__ iy, const int* __restrict__ bbox, int* cnt_x, int* cnt_y,
-                            int* lst_x, int* lst_y, int max_faces) {
+                            int* lst_x, int* lst_y, int max_faces, const int* __restrict__ stale) {
+  if (!*stale) return;
   int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
   int nface = ni * nj;
   if (nface + 1 > max_faces) return;
@@ -158,8 +163,10 @@ __global__ void k_reg_lists(int nf, const int* __restrict__ comp, const int* __r
 
 // Exclusive scan of both count arrays (one CTA, 1024 threads): each thread sums a run of
 // consecutive faces, the runs are scanned with warp shuffles, then written back.
-__global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y, int max_faces) {
+__global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y, int max_faces,
+                           const int* __restrict__ stale) {
   __shared__ int wsum[32];
+  if (!*stale) return;
   const int nface = bbox[2] * bbox[3];
   if (nface + 1 > max_faces) return;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -195,19 +202,21 @@ __global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y,
 int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
                      double offy, RegDev& r, int* d_err, cudaStream_t st) {
   if (nf == 0) return IB_OK;
+  // bbox, lists and scan skip their work (return at once) unless a stencil origin moved
+  IB_CUDA_CHECK(cudaMemsetAsync(r.stale, 0, sizeof(int), st));
   count_launch();
   k_reg_weights<<<cdiv(32LL * nf, 128), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w,
-                                                       d_err);
+                                                       r.stale, d_err);
   count_launch();
-  k_reg_bbox<<<1, 256, 0, st>>>(g, nf, r.ix, r.iy, r.bbox);
+  k_reg_bbox<<<1, 256, 0, st>>>(g, nf, r.ix, r.iy, r.bbox, r.stale);
   count_launch();
   k_reg_lists<false><<<152 * 2, 128, 0, st>>>(nf, r.comp, r.ix, r.iy, r.bbox, r.cnt_x, r.cnt_y, nullptr,
-                                              nullptr, r.max_faces);
+                                              nullptr, r.max_faces, r.stale);
   count_launch();
-  k_reg_scan<<<1, 1024, 0, st>>>(r.bbox, r.cnt_x, r.cnt_y, r.max_faces);
+  k_reg_scan<<<1, 1024, 0, st>>>(r.bbox, r.cnt_x, r.cnt_y, r.max_faces, r.stale);
   count_launch();
   k_reg_lists<true><<<152 * 2, 128, 0, st>>>(nf, r.comp, r.ix, r.iy, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y,
-                                             r.max_faces);
+                                             r.max_faces, r.stale);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -32,6 +32,7 @@ struct RegDev {
   int* lst_y;
   int max_faces;    // capacity of cnt_* (faces)
   int max_list;     // capacity of lst_*
+  int* stale;       // set by the weights kernel when a stencil origin moved: lists to rebuild
 };
 
 int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,

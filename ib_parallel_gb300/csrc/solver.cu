@@ -196,7 +196,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 4 * (size_t)nf + 2;
   if (p.num_stat) dbl += (size_t)nf * nf;
   dbl += 8 * stage_n;
-  size_t ints = 2 * (size_t)nf + 2 * (size_t)nf + 16 + 2 * (size_t)max_faces + 2 * 49 * (size_t)nf + 4 + 1;
+  size_t ints = 2 * (size_t)nf + 2 * (size_t)nf + 16 + 2 * (size_t)max_faces + 2 * 49 * (size_t)nf + 4 + 2;
   size_t bytes = dbl * 8 + ints * 4 + (size_t)nt * sizeof(TorsBody) + 256 * 400;
   if (cudaMalloc(&c->pool.base, bytes) != cudaSuccess) {
     *msg = "device allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM;
@@ -233,6 +233,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->reg.w = P.take<double>(49 * (size_t)nf); c->reg.bbox = P.take<int>(16);
   c->reg.cnt_x = P.take<int>(max_faces); c->reg.cnt_y = P.take<int>(max_faces);
   c->reg.lst_x = P.take<int>(49 * (size_t)nf + 1); c->reg.lst_y = P.take<int>(49 * (size_t)nf + 1);
+  c->reg.stale = P.take<int>(1);
   c->reg.max_faces = max_faces; c->reg.max_list = 49 * nf;
   c->tb = P.take<TorsBody>(nt + 1);
   c->ts.theta = P.take<double>(nt + 1); c->ts.thetad = P.take<double>(nt + 1);
