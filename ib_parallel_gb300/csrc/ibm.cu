@@ -48,33 +48,40 @@ __device__ double deltafnc_dev(double x1, double x2, double dr) {
   return v / dr;
 }
 
-// Per unknown (one warp): stencil origin and the 49 weights (l outer, p inner).  Lanes 0-6
-// evaluate the x factors, lanes 7-13 the y factors (one delta function each, so the
-// FP64-latency-bound evaluations run side by side), then every lane writes weights.
-__global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb, const double* __restrict__ yb,
-                              double d, double ox, double oy, const int* __restrict__ comp, int* ix, int* iy,
-                              double* w, int* stale, int* err) {
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (k >= nf) return;
-  const double xk = xb[k], yk = yb[k];
-  const int cx = (int)((xk + ox) / d) + 1;   // Fortran INT truncates toward zero
-  const int cy = (int)((yk + oy) / d) + 1;
+// Stencil origins and the 49 weights (l outer, p inner) of 8 unknowns per CTA (4 warps).
+// With phi the fractional position of a point in its cell, the 7 stencil offsets q sit at
+// distances |q - 3 - phi| (in cells), so offsets {3,4}, {2,5} and {1,6} fall in the first,
+// second and third piece of the delta function and offset 0 at its edge.  Warp w evaluates
+// one offset pair for the x and y factors of all 8 unknowns, so its lanes take one branch of
+// the FP64-latency-bound evaluation instead of all three; the factors then meet in shared
+// memory for the products.
+__global__ void __launch_bounds__(128) k_reg_weights(GridDims g, int nf, const double* __restrict__ xb,
+                                                     const double* __restrict__ yb, double d, double ox,
+                                                     double oy, const int* __restrict__ comp, int* ix, int* iy,
+                                                     double* w, int* stale, int* err) {
+  __shared__ double fac[16][7];    // [2*unknown + axis][offset], axis 0: x factor, 1: y factor
+  const int k0 = blockIdx.x * 8;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double d2 = 0.5 * d;
-  const bool isx = comp[k] == 1;
-  if (lane == 0) {
-    // the contribution lists depend on the stencil origins only: rebuild them when one moved
-    if (ix[k] != cx || iy[k] != cy) atomicOr(stale, 1);
-    ix[k] = cx;
-    iy[k] = cy;
-    // faces touched: u-face i in [1,m+1], j in [1,n]; v-face i in [1,m], j in [1,n+1]
-    int imax = isx ? g.m + 1 : g.m, jmax = isx ? g.n : g.n + 1;
-    if (cx - 3 < 1 || cx + 3 > imax || cy - 3 < 1 || cy + 3 > jmax) atomicExch(err, IB_ERR_DOMAIN);
+  // this lane's (pair, offset)
+  int pi, q;
+  if (warp < 3) {
+    pi = lane >> 1;
+    const int lo = 3 - warp, hi = 4 + warp;   // {3,4}, {2,5}, {1,6}
+    q = (lane & 1) ? hi : lo;
+  } else {
+    pi = lane;
+    q = 0;
   }
-  double f = 0.0;
-  if (lane < 14) {
-    const int q = lane % 7, off = q - 3;
-    if (lane < 7) {
+  const int k = k0 + (pi >> 1), axis = pi & 1;
+  if (pi < 16 && k < nf) {
+    const double xk = xb[k], yk = yb[k];
+    const int cx = (int)((xk + ox) / d) + 1;   // Fortran INT truncates toward zero
+    const int cy = (int)((yk + oy) / d) + 1;
+    const bool isx = comp[k] == 1;
+    const int off = q - 3;
+    double f;
+    if (axis == 0) {
       double x = d * (double)(cx - 1 + off) - ox;
       if (!isx) x = x + d2;
       f = deltafnc_dev(x, xk, d);
@@ -83,14 +90,23 @@ __global__ void k_reg_weights(GridDims g, int nf, const double* __restrict__ xb,
       if (isx) y = y + d2;
       f = deltafnc_dev(y, yk, d);
     }
+    fac[pi][q] = f;
+    if (warp == 3 && axis == 0) {
+      // the contribution lists depend on the stencil origins only: rebuild them when one moved
+      if (ix[k] != cx || iy[k] != cy) atomicOr(stale, 1);
+      ix[k] = cx;
+      iy[k] = cy;
+      // faces touched: u-face i in [1,m+1], j in [1,n]; v-face i in [1,m], j in [1,n+1]
+      int imax = isx ? g.m + 1 : g.m, jmax = isx ? g.n : g.n + 1;
+      if (cx - 3 < 1 || cx + 3 > imax || cy - 3 < 1 || cy + 3 > jmax) atomicExch(err, IB_ERR_DOMAIN);
+    }
   }
-  double* wk = w + (size_t)k * 49;
-  for (int base = 0; base < 49; base += 32) {   // same trip count on every lane (shuffles)
-    const int sl = base + lane;
-    const int l = sl < 49 ? sl / 7 : 0, p = sl < 49 ? sl % 7 : 0;
-    const double dxp = __shfl_sync(0xffffffffu, f, p);
-    const double dyl = __shfl_sync(0xffffffffu, f, 7 + l);
-    if (sl < 49) wk[sl] = d * d * dxp * dyl;
+  __syncthreads();
+  for (int t = threadIdx.x; t < 8 * 49; t += blockDim.x) {
+    const int u = t / 49, sl = t - u * 49;
+    if (k0 + u >= nf) break;
+    const int l = sl / 7, p = sl - l * 7;
+    w[(size_t)(k0 + u) * 49 + sl] = d * d * fac[2 * u][p] * fac[2 * u + 1][l];
   }
 }
 
@@ -205,8 +221,8 @@ int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* 
   // bbox, lists and scan skip their work (return at once) unless a stencil origin moved
   IB_CUDA_CHECK(cudaMemsetAsync(r.stale, 0, sizeof(int), st));
   count_launch();
-  k_reg_weights<<<cdiv(32LL * nf, 128), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w,
-                                                       r.stale, d_err);
+  k_reg_weights<<<cdiv(nf, 8), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w, r.stale,
+                                              d_err);
   count_launch();
   k_reg_bbox<<<1, 256, 0, st>>>(g, nf, r.ix, r.iy, r.bbox, r.stale);
   count_launch();
