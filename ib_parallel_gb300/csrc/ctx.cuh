@@ -89,6 +89,11 @@ struct Ctx {
   int L = 0;
   double delta = 0, normalize = 0;
   cudaStream_t st = nullptr;
+  // second stream of the predictor: the levels' nonlinear terms run on it while the
+  // coarse-to-fine chain of solves runs on st (one fork event, one event per level)
+  cudaStream_t st_aux = nullptr;
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> ev_lv;
   DevPool pool;
 
   DstPlan px, py;
@@ -103,6 +108,7 @@ struct Ctx {
 
   // state per level
   std::vector<double*> omega, s, qx, qy, q0x, q0y, rhs_old;
+  std::vector<double*> rhs_lv;     // this step's nonlinear right-hand side per level
   // Schur-operator scratch per level
   std::vector<double*> mv_w, mv_s, mv_qx, mv_qy;
   // vort2flux: per-level mode-space fields and the ring each level receives

@@ -264,28 +264,45 @@ __device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2*
     }
   }
   __syncthreads();
-  // --- inclusive prefix sum over positions 0,2,...,2(P-1): odd outputs
+  // --- inclusive prefix sum over positions 0,2,...,2(P-1): odd outputs.  Each line is scanned
+  // by a group of wpl warps (all warps of the CTA share the lines): short sequential runs per
+  // thread, a warp shuffle scan, then the group's warp totals in shared memory.
+  __shared__ double s_wt[32];
   const int lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
-  const int c = (P + 31) >> 5;
-  for (int b = warp; b < B; b += nwarps) {
-    double* o = xb + b * ldx;
-    int s0 = lane * c;
-    int s1 = min(s0 + c, P);
+  const int wpl = nwarps >= B ? nwarps / B : 1;           // warps per line
+  const int groups = nwarps >= B ? B : nwarps;            // lines in flight at once
+  const int c = (P + 32 * wpl - 1) / (32 * wpl);
+  for (int b0 = 0; b0 < B; b0 += groups) {
+    const int grp = warp / wpl, gw = warp - grp * wpl;
+    const int b = b0 + grp;
+    const bool act = grp < groups && b < B;
+    double* o = xb + (act ? b : 0) * ldx;
+    const int gt = gw * 32 + lane;
+    const int s0 = min(gt * c, P), s1 = min(s0 + c, P);
     double acc = 0.0;
-    for (int i = s0; i < s1; ++i) acc += o[2 * i];
+    if (act)
+      for (int i = s0; i < s1; ++i) acc += o[2 * i];
+    double incl = acc;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      double v = __shfl_up_sync(0xffffffffu, acc, off);
-      if (lane >= off) acc += v;
+      double v = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += v;
     }
-    double run = __shfl_up_sync(0xffffffffu, acc, 1);
-    if (lane == 0) run = 0.0;
-    for (int i = s0; i < s1; ++i) {
-      run += o[2 * i];
-      o[2 * i] = run;
+    if (lane == 31 && grp < groups) s_wt[grp * wpl + gw] = incl;
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = 0.0;
+    __syncthreads();
+    if (act) {
+      double run = 0.0;
+      for (int j = 0; j < gw; ++j) run += s_wt[grp * wpl + j];
+      run += excl;
+      for (int i = s0; i < s1; ++i) {
+        run += o[2 * i];
+        o[2 * i] = run;
+      }
     }
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 // ------------------------------------------------------------- x pass
@@ -301,7 +318,31 @@ __device__ __forceinline__ double x_load(const DstXArgs& a, const double* __rest
   } else if (PRE == PRE_PRED) {
     // con1 rhs + con2 rhs_old + rhsbc + (w - c L w)/normalize, L the 5-point
     // Laplacian with zero boundary: alpha = (1-4c)/normalize, beta = c/normalize
-    double base = fma(a.cb, a.in2[idx], a.ca * in[idx]) + a.in3[idx];
+    const double ro = a.in2[idx], r = in[idx];
+    double base = fma(a.cb, ro, a.ca * r);
+    if (a.save) a.save[idx] = r;
+    if (a.in3) {
+      base = base + a.in3[idx];
+    } else {
+      const int I = j + 2, J = row + 2;
+      if (I == 2 || I == g.m || J == 2 || J == g.n) {
+        // rhsbc = 0; apply_bc(rhsbc, lastbc, f); apply_bc(rhsbc, 0.25 get_bc(coarse), f)
+        double x = 0.0;
+        const double* ra = a.ring;
+        if (I == 2) x = x + a.fac * ra[g.left + J - 1];
+        if (I == g.m) x = x + a.fac * ra[g.right + J - 1];
+        if (J == 2) x = x + a.fac * ra[g.bottom + I - 1];
+        if (J == g.n) x = x + a.fac * ra[g.top + I - 1];
+        if (a.coarse) {
+          const double* cs = a.coarse;
+          if (I == 2) x = x + a.fac * (ring_value(cs, g, g.left + J - 1) * 0.25);
+          if (I == g.m) x = x + a.fac * (ring_value(cs, g, g.right + J - 1) * 0.25);
+          if (J == 2) x = x + a.fac * (ring_value(cs, g, g.bottom + I - 1) * 0.25);
+          if (J == g.n) x = x + a.fac * (ring_value(cs, g, g.top + I - 1) * 0.25);
+        }
+        base = base + x;
+      }
+    }
     const double* w = a.in4;
     double nb = 0.0;
     if (j > 0) nb += w[idx - 1];

@@ -52,8 +52,12 @@ struct DstXArgs {
   const double* in4 = nullptr;   // PRE_PRED vorticity
   double ca = 1.0, cb = 0.0;     // PRE_COMBINE: ca*in + cb*in2 + in3
   double alpha = 0.0, beta = 0.0;  // PRE_PRED: + alpha*w + beta*(sum of the 4 neighbours of w)
-  const double* ring = nullptr;  // PRE_APPLYBC boundary ring
-  double fac = 1.0;              // PRE_APPLYBC factor
+  const double* ring = nullptr;  // PRE_APPLYBC boundary ring; PRE_PRED without in3: first rhsbc ring
+  double fac = 1.0;              // PRE_APPLYBC factor; PRE_PRED without in3: rhsbc factor
+  // PRE_PRED without in3: rhsbc (timestepper.F90:184-189) is formed on the fly from `ring` and
+  // the boundary ring 0.25*get_bc(coarse) of the next coarser level's field (none if null)
+  const double* coarse = nullptr;
+  double* save = nullptr;        // PRE_PRED: receives a copy of `in` (may alias in2)
   double* out = nullptr;         // nlines rows, pitch ld
   // optional output post-op: out = DST(row) + post_scale * post_add
   const double* post_add = nullptr;

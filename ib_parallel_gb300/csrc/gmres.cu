@@ -7,11 +7,10 @@
 // Two drivers share one arithmetic.  The graph solver runs one CTA per kernel with the
 // operator (the Schur matvec) between them, reading G.xin and writing G.Av.  The cluster
 // solver (k_gmres_cluster) runs a whole solve on an assembled dense operator across a
-// cluster of kSlices CTAs, each owning one slice of the unknowns.  Every inner product and
-// norm is summed the way the cluster must sum it: a sequential partial per slice, then the
-// kSlices partials in slice order; and the dense product splits each row into kSlices
-// column segments reduced by a fixed shuffle tree.  So both drivers produce identical
-// iterates.
+// cluster of kSlices CTAs, each owning one slice of the unknowns.  Every inner product,
+// norm and Gram-Schmidt update is summed in the fixed order kernels.cuh states, which the
+// graph kernels evaluate with one thread per sum and the cluster with lanes and shuffle
+// trees; so both drivers produce identical iterates.
 #include <cooperative_groups.h>
 
 #include "kernels.cuh"
@@ -30,16 +29,81 @@ __device__ __forceinline__ void slice_range(int n, int c, int* lo, int* hi) {
   *hi = min(n, *lo + ns);
 }
 
+static_assert(kSlices == 8, "the pairwise trees below are written for 8 slices");
+
+// The fixed summation orders, one thread per sum (the cluster solver's lane forms match).
+__device__ __forceinline__ double slice_dot_seq(const double* __restrict__ a, const double* __restrict__ b, int lo,
+                                                int hi) {
+  const int n = hi - lo, LP = slice_blocks_p2(n);
+  // the pairwise tree over the LP block sums, streamed: merge equal-sized subtrees
+  double st[32];
+  int sz[32], top = 0;
+  for (int k = 0; k < LP; ++k) {
+    double p[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int i = lo + 4 * k + t;
+      p[t] = i < hi ? a[i] * b[i] : 0.0;
+    }
+    double v = (p[0] + p[1]) + (p[2] + p[3]);
+    int w = 1;
+    while (top > 0 && sz[top - 1] == w) {
+      v = st[top - 1] + v;
+      w *= 2;
+      --top;
+    }
+    st[top] = v;
+    sz[top] = w;
+    ++top;
+  }
+  return st[0];
+}
+__device__ __forceinline__ double tree8_seq(const double* p) {
+  return ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
+}
+// Row i of w = Av - sum_{j<=it} h_j V_j (V with row pitch ld).
+__device__ __forceinline__ double cgs_row_seq(double av, const double* __restrict__ h, const double* __restrict__ V,
+                                              size_t ld, int i, int it) {
+  double p[8];
+#pragma unroll
+  for (int g = 0; g < 8; ++g) {
+    double t = g == 0 ? av : 0.0;
+    for (int j = g; j <= it; j += 8) t = fma(-h[j], V[(size_t)j * ld + i], t);
+    p[g] = t;
+  }
+  return tree8_seq(p);
+}
+
+// Happy breakdown (KSPGMRESUpdateHessenberg): tt < min(|tt/g|, haptol = 1e-30).  The bound
+// never exceeds haptol, so the quotient is formed only when tt itself is below it.
+__device__ __forceinline__ bool happy_breakdown(double tt, double g) {
+  if (!(tt < 1.0e-30)) return false;
+  double hapbnd = fabs(tt / g);
+  if (hapbnd > 1.0e-30) hapbnd = 1.0e-30;
+  return tt < hapbnd;
+}
+
+// Norm of a new Krylov vector from its squared norm s: tt and the scale 1/tt applied to it
+// (rsqrt and a product: a square root and a division cost about 600 cycles each here).
+__device__ __forceinline__ void norm_and_scale(double s, double* tt, double* inv) {
+  if (s > 0.0) {
+    const double r = rsqrt(s);
+    *inv = r;
+    *tt = s * r;
+  } else {
+    *tt = sqrt(s);
+    *inv = 0.0;
+  }
+}
+
 // Givens update of Arnoldi step `it` (KSPGMRESUpdateHessenberg): the new Hessenberg column is
 // h[0..it], tt; the previous rotations are applied with the rotated value carried in a
-// register (one dependent FMA per rotation), then the new rotation, the rotated residual g
-// and the convergence reason.  Writes H column `it` (ld = restart+1).
+// register (one dependent FMA per rotation), then the new rotation (from rsqrt of c^2+tt^2),
+// the rotated residual g and the convergence reason.  Writes H column `it` (ld = restart+1).
 __device__ void givens_step(double* __restrict__ col, const double* __restrict__ h, double tt, int it,
                             double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g, double prev_res,
                             double ttol, double* res_out, int* reason_out) {
-  double hapbnd = fabs(tt / g[it]);
-  if (hapbnd > 1.0e-30) hapbnd = 1.0e-30;
-  const bool hapend = tt < hapbnd;
+  const bool hapend = happy_breakdown(tt, g[it]);
   double c = h[0];
   for (int j = 0; j < it; ++j) {
     const double nxt = h[j + 1];
@@ -51,13 +115,14 @@ __device__ void givens_step(double* __restrict__ col, const double* __restrict__
   double res;
   int reason = 0;
   if (!hapend) {
-    const double nrm = sqrt(fma(c, c, tt * tt));
-    if (nrm == 0.0) {
+    const double r2 = fma(c, c, tt * tt);
+    if (r2 == 0.0) {
       reason = -9;  // KSP_DIVERGED_NULL
       res = prev_res;
       col[it] = c;
     } else {
-      const double ci = c / nrm, si = tt / nrm;
+      const double rn = rsqrt(r2);
+      const double ci = c * rn, si = tt * rn;
       cs[it] = ci;
       sn[it] = si;
       g[it + 1] = -(si * g[it]);
@@ -77,15 +142,24 @@ __device__ void givens_step(double* __restrict__ col, const double* __restrict__
   *reason_out = reason;
 }
 
-// KSPGMRESBuildSoln back substitution: y[0..k] from H (ld = R+1) and g.
+// KSPGMRESBuildSoln back substitution y[0..k] = R^-1 g (R the rotated Hessenberg, ld = R+1), on
+// one whole warp: the pivot reciprocals at once, then a column sweep (y_j = r_j / R_jj as
+// r_j * (1/R_jj); every r_l, l < j, loses R_lj y_j on its own lane).  rc: k+1 doubles.
 __device__ void back_substitute(const double* __restrict__ H, int R, const double* __restrict__ g, int k,
-                                double* __restrict__ y) {
+                                double* __restrict__ y, double* __restrict__ rc) {
+  const int lane = threadIdx.x & 31;
   auto HH = [&](int r, int c) { return H[(size_t)c * (R + 1) + r]; };
-  y[k] = g[k] / HH(k, k);
-  for (int i = k - 1; i >= 0; --i) {
-    double tt = g[i];
-    for (int j = i + 1; j <= k; ++j) tt = fma(-HH(i, j), y[j], tt);
-    y[i] = tt / HH(i, i);
+  for (int l = lane; l <= k; l += 32) {
+    y[l] = g[l];
+    rc[l] = __drcp_rn(HH(l, l));
+  }
+  __syncwarp();
+  for (int j = k; j >= 0; --j) {
+    const double yj = y[j] * rc[j];
+    __syncwarp();
+    for (int l = lane; l < j; l += 32) y[l] = fma(-HH(l, j), yj, y[l]);
+    if (lane == 0) y[j] = yj;
+    __syncwarp();
   }
 }
 
@@ -107,19 +181,12 @@ __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const do
     int lo, hi;
     slice_range(nf, tid % kSlices, &lo, &hi);
     const double* v = tid < kSlices ? G.V : b;
-    double a = 0.0;
-    for (int i = lo; i < hi; ++i) a = fma(v[i], v[i], a);
-    part[tid] = a;
+    part[tid] = slice_dot_seq(v, v, lo, hi);
   }
   __syncthreads();
   if (tid == 0) {
-    double r2 = part[0], b2 = part[kSlices];
-    for (int c = 1; c < kSlices; ++c) {
-      r2 += part[c];
-      b2 += part[kSlices + c];
-    }
-    s_norm[0] = sqrt(r2);
-    s_norm[1] = sqrt(b2);
+    s_norm[0] = sqrt(tree8_seq(part));
+    s_norm[1] = sqrt(tree8_seq(part + kSlices));
   }
   __syncthreads();
   const double rnorm = s_norm[0], bnorm = s_norm[1];
@@ -160,7 +227,7 @@ __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const do
 __global__ void k_gmres_arnoldi(GmresDev G, int max_it, cudaGraphConditionalHandle h_inner, int use_cond) {
   __shared__ double part[64 * kSlices];
   __shared__ double h[64];
-  __shared__ double s_tt;
+  __shared__ double s_tt[2];
   if (G.ist[3] == 0) {
     if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(h_inner, 0u);
     return;
@@ -174,40 +241,23 @@ __global__ void k_gmres_arnoldi(GmresDev G, int max_it, cudaGraphConditionalHand
     const int j = q / kSlices, c = q % kSlices;
     int lo, hi;
     slice_range(nf, c, &lo, &hi);
-    const double* vj = G.V + (size_t)j * nf;
-    double a = 0.0;
-    for (int i = lo; i < hi; ++i) a = fma(Av[i], vj[i], a);
-    part[q] = a;
+    part[q] = slice_dot_seq(Av, G.V + (size_t)j * nf, lo, hi);
   }
   __syncthreads();
-  if (tid <= it) {
-    double s = part[tid * kSlices];
-    for (int c = 1; c < kSlices; ++c) s += part[tid * kSlices + c];
-    h[tid] = s;
-  }
+  if (tid <= it) h[tid] = tree8_seq(part + tid * kSlices);
   __syncthreads();
-  for (int i = tid; i < nf; i += blockDim.x) {
-    double v = Av[i];
-    for (int j = 0; j <= it; ++j) v = fma(-h[j], G.V[(size_t)j * nf + i], v);
-    w[i] = v;
-  }
+  for (int i = tid; i < nf; i += blockDim.x) w[i] = cgs_row_seq(Av[i], h, G.V, nf, i, it);
   __syncthreads();
   if (tid < kSlices) {
     int lo, hi;
     slice_range(nf, tid, &lo, &hi);
-    double a = 0.0;
-    for (int i = lo; i < hi; ++i) a = fma(w[i], w[i], a);
-    part[tid] = a;
+    part[tid] = slice_dot_seq(w, w, lo, hi);
   }
   __syncthreads();
-  if (tid == 0) {
-    double s = part[0];
-    for (int c = 1; c < kSlices; ++c) s += part[c];
-    s_tt = sqrt(s);
-  }
+  if (tid == 0) norm_and_scale(tree8_seq(part), &s_tt[0], &s_tt[1]);
   __syncthreads();
-  const double tt = s_tt;
-  const double inv = tt != 0.0 ? 1.0 / tt : 0.0;
+  const double tt = s_tt[0];
+  const double inv = s_tt[1];
   for (int i = tid; i < nf; i += blockDim.x) {
     double v = tt != 0.0 ? w[i] * inv : w[i];
     w[i] = v;
@@ -233,10 +283,10 @@ __global__ void k_gmres_arnoldi(GmresDev G, int max_it, cudaGraphConditionalHand
 // KSPGMRESBuildSoln: back substitution and x += V y.
 __global__ void k_gmres_update(GmresDev G, double* __restrict__ x, int max_it, cudaGraphConditionalHandle h_outer,
                                int use_cond) {
-  __shared__ double y[64];
+  __shared__ double y[64], rc[64];
   const int nf = G.nf, R = G.restart;
   const int it = G.ist[2];
-  if (threadIdx.x == 0 && it > 0) back_substitute(G.H, R, G.g, it - 1, y);
+  if (threadIdx.x < 32 && it > 0) back_substitute(G.H, R, G.g, it - 1, y, rc);
   __syncthreads();
   if (it > 0) {
     for (int i = threadIdx.x; i < nf; i += blockDim.x) {
@@ -383,29 +433,95 @@ namespace {
 struct ClusterSmem {
   int nf, R, ns;
   size_t base() const {
-    return (size_t)(R + 1) * ns + nf + 3 * (size_t)ns + 2 * (size_t)(R + 1) + (size_t)(R + 1) * R +
-           4 * (size_t)(R + 1) + 8;
+    return (size_t)(R + 1) * ns + nf + 4 * (size_t)ns + 2 * (size_t)(R + 1) + (size_t)(R + 1) * R +
+           4 * (size_t)(R + 1) + 8 + 2 * (size_t)R + 32;
   }
   size_t with_a() const { return base() + (size_t)ns * nf; }
 };
 }  // namespace
 
+// Warps 0-2 run the dense product and the projections; warp 3 the Givens update meanwhile;
+// all four the rest.  Each warp sits on its own SM sub-partition, and an FP64 instruction
+// holds its sub-partition's FP64 pipe for the same time whatever its active lanes, so every
+// sum below is spread over lanes (shuffle trees) rather than run down one thread.
+constexpr int kClusterThreads = 128;
+constexpr int kProdThreads = 96;
+
+// givens_step's arithmetic on one whole warp: the products off the rotated value's chain and
+// the column entries on all lanes, the chain on lane 0.  buf: 2*it doubles of shared memory.
+__device__ void givens_step_warp(double* __restrict__ col, const double* __restrict__ h, double tt, int it,
+                                 double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g,
+                                 double prev_res, double ttol, double* __restrict__ buf, double* res_out,
+                                 int* reason_out) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  double* pj = buf;        // cs[j] * h[j+1]
+  double* cj = buf + it;   // the rotated value before rotation j
+  for (int j = lane; j < it; j += 32) pj[j] = cs[j] * h[j + 1];
+  __syncwarp();
+  double c = h[0];
+  if (lane == 0)
+    for (int j = 0; j < it; ++j) {
+      cj[j] = c;
+      c = fma(-sn[j], c, pj[j]);
+    }
+  __syncwarp();
+  c = __shfl_sync(full, c, 0);
+  for (int j = lane; j < it; j += 32) col[j] = fma(sn[j], h[j + 1], cs[j] * cj[j]);
+  const double gi = g[it];
+  const bool hapend = happy_breakdown(tt, gi);
+  const double r2 = fma(c, c, tt * tt);
+  const double rn = r2 != 0.0 ? rsqrt(r2) : 0.0;
+  const double ci = c * rn, si = tt * rn;
+  if (lane == 0) {
+    col[it + 1] = tt;
+    double res;
+    int reason = 0;
+    if (!hapend) {
+      if (r2 == 0.0) {
+        reason = -9;  // KSP_DIVERGED_NULL
+        res = prev_res;
+        col[it] = c;
+      } else {
+        cs[it] = ci;
+        sn[it] = si;
+        g[it + 1] = -(si * gi);
+        g[it] = ci * gi;
+        col[it] = fma(si, tt, ci * c);
+        res = fabs(g[it + 1]);
+      }
+    } else {
+      col[it] = c;
+      res = 0.0;
+    }
+    if (reason == 0) {
+      if (res <= ttol) reason = 2;
+      else if (hapend) reason = -3;
+    }
+    *res_out = res;
+    *reason_out = reason;
+  }
+  __syncwarp();
+}
+
 // One restarted GMRES solve on the assembled operator A (column-major, At[j*nf + r] = A[r][j])
 // across a cluster of kSlices CTAs.  CTA c owns the rows and vector elements of slice c: its
 // rows of A, its slice of every Krylov vector, of x and of b.  Per Arnoldi step:
-//   A: the product of its rows with the full current vector (kSlices threads per row), and
-//      its partial projections; meanwhile the last warp applies the Givens update of the
-//      previous step;                                                        cluster barrier
+//   A: warps 0-2 form the product of its rows with the full current vector (rows in groups of
+//      S lanes) and its partial projections; meanwhile warp 3 applies the Givens update of
+//      the previous step;                                                    cluster barrier
 //      the previous step's convergence decision is read from CTA 0 (every CTA branches
-//      alike), then the projections are summed over the slices in order;
-//   B: w = A v - sum h_j v_j on the slice and its partial norm;              cluster barrier
+//      alike), then the projections are summed over the slices (8 lanes per projection);
+//   B: w = A v - sum h_j v_j on the slice (8 lanes per row) and its partial norm;
+//                                                                            cluster barrier
 //   C: the norm, the normalised slice;                                       cluster barrier
 //   D: every CTA gathers the full new vector through distributed shared memory.
 // No thread waits on a flag: the only waits are the cluster and CTA barriers, which every
 // thread of every CTA reaches the same number of times.
-__global__ void __cluster_dims__(kSlices, 1, 1)
+__global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThreads)
     k_gmres_cluster(GmresDev G, const double* __restrict__ At, int a_in_smem, const double* __restrict__ b,
                     double* __restrict__ x, double rtol, double atol, int max_it) {
+  const unsigned full = 0xffffffffu;
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   const int nf = G.nf, R = G.restart;
@@ -413,9 +529,7 @@ __global__ void __cluster_dims__(kSlices, 1, 1)
   int r0, r1;
   slice_range(nf, rank, &r0, &r1);
   const int nl = r1 - r0;
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int nwork = (int)blockDim.x - 32;     // the last warp applies the Givens updates
-  const bool gwarp = tid >= nwork;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   extern __shared__ double sm[];
   double* Vs = sm;                                  // (R+1) x ns
   double* vfull = Vs + (size_t)(R + 1) * ns;        // nf
@@ -431,10 +545,36 @@ __global__ void __cluster_dims__(kSlices, 1, 1)
   double* yv = g + (R + 1);
   double* scal = yv + (R + 1);                      // [0],[1] partials (read remotely), [2] tt, [3] res,
                                                     // [4] 1/tt, [5] rnorm, [6] bnorm, [7] ttol
-  double* As = scal + 8;                            // nl x nf row-major when a_in_smem
+  double* gbuf = scal + 8;                          // 2R: Givens scratch
+  double* wbuf = gbuf + 2 * (size_t)R;              // ns: the new vector before scaling (read remotely)
+  double* nblk = wbuf + ns;                         // 32: block partials of its norm
+  double* As = nblk + 32;                           // nl x nf row-major when a_in_smem
   __shared__ int s_reason;                          // read remotely from CTA 0
   auto remote = [&](double* p, int c) -> const double* { return cl.map_shared_rank(p, c); };
-  auto bar_work = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(nwork)); };
+  auto bar_prod = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(kProdThreads)); };
+  // slice partial of a.b in the fixed order: lane blk of an aligned group of LP lanes forms
+  // block blk ((p0+p1)+(p2+p3) over rows 4blk..4blk+3), the group's xor tree the rest (valid
+  // on every lane of the group); every lane of the warp calls it
+  const int LP = slice_blocks_p2(nl);
+  auto slice_dot_lanes = [&](const double* a, const double* bb, int blk, bool on) -> double {
+    double p[4] = {0.0, 0.0, 0.0, 0.0};
+    if (on)
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int i = 4 * blk + t;
+        if (i < nl) p[t] = a[i] * bb[i];
+      }
+    double v = (p[0] + p[1]) + (p[2] + p[3]);
+    for (int off = 1; off < LP; off <<= 1) v += __shfl_xor_sync(full, v, off);
+    return v;
+  };
+  // pairwise tree over an aligned group of 8 lanes (valid on all 8)
+  auto tree8 = [&](double p) -> double {
+    p += __shfl_xor_sync(full, p, 1);
+    p += __shfl_xor_sync(full, p, 2);
+    p += __shfl_xor_sync(full, p, 4);
+    return p;
+  };
 
   if (a_in_smem)
     for (int q = tid; q < nl * nf; q += blockDim.x) {
@@ -447,25 +587,26 @@ __global__ void __cluster_dims__(kSlices, 1, 1)
   }
   __syncthreads();
 
-  // avs = rows of A times vfull: kSlices column segments per row, reduced by a fixed tree
-  const int cw = slice_size(nf);
+  // avs = rows of A times vfull (warps 0-2): rows in groups of S lanes, one column segment
+  // per lane, joined by seg_tree (k_dense_mv's layout and order)
+  const int S = mv_segments(nf), gpw = 32 / S, cw = (nf + S - 1) / S;
+  const int grp = lane / S, seg = lane - grp * S;
   auto matvec = [&]() {
-    for (int base = 0; base < ns * kSlices; base += nwork) {
-      const int q = base + tid, rl = q / kSlices, seg = q % kSlices;
+    for (int rb = 0; rb < nl; rb += 3 * gpw) {
+      const int rl = rb + warp * gpw + grp;
+      const bool live = grp < gpw && rl < nl;
       double p = 0.0;
-      if (rl < nl) {
+      if (live) {
         const int j0 = min(nf, seg * cw), j1 = min(nf, j0 + cw);
         if (a_in_smem) {
           const double* Ar = As + (size_t)rl * nf;
-          for (int j = j0; j < j1; ++j) p = fma(Ar[j], vfull[j], p);
+              p = seg_dot(j0, j1, [&](int j, double acc) { return fma(Ar[j], vfull[j], acc); });
         } else {
-          for (int j = j0; j < j1; ++j) p = fma(At[(size_t)j * nf + r0 + rl], vfull[j], p);
+          p = seg_dot(j0, j1, [&](int j, double acc) { return fma(At[(size_t)j * nf + r0 + rl], vfull[j], acc); });
         }
       }
-      p += __shfl_xor_sync(0xffffffffu, p, 4);
-      p += __shfl_xor_sync(0xffffffffu, p, 2);
-      p += __shfl_xor_sync(0xffffffffu, p, 1);
-      if (rl < nl && seg == 0) avs[rl] = p;
+      p = seg_tree(p, seg, S);
+      if (live && seg == 0) avs[rl] = p;
     }
   };
   auto gather = [&](double* src, int stride_slot) {   // vfull[i] = slot of the owner's slice
@@ -480,43 +621,38 @@ __global__ void __cluster_dims__(kSlices, 1, 1)
   for (;;) {
     // ---- cycle start (k_gmres_start): r = b - A x, V0 = r/||r||
     cl.sync();                                    // every x slice is final
-    for (int i = tid; i < nf; i += blockDim.x) {
-      const int c = i / ns;
-      vfull[i] = remote(xsl, c)[i - c * ns];
-    }
+    gather(xsl, 0);
     __syncthreads();
-    if (!gwarp) matvec();
+    if (warp < 3) matvec();
     __syncthreads();
     for (int i = tid; i < nl; i += blockDim.x) Vs[i] = bsl[i] - avs[i];
     __syncthreads();
-    if (tid == 0) {
-      double a = 0.0, bb = 0.0;
-      for (int i = 0; i < nl; ++i) a = fma(Vs[i], Vs[i], a);
-      for (int i = 0; i < nl; ++i) bb = fma(bsl[i], bsl[i], bb);
-      scal[0] = a;
-      scal[1] = bb;
+    if (warp == 0) {   // lanes 0-15: ||r||^2 partial, lanes 16-31: ||b||^2 partial
+      const double* v = lane < 16 ? Vs : bsl;
+      const double t = slice_dot_lanes(v, v, lane & 15, (lane & 15) < LP);
+      if (lane == 0) scal[0] = t;
+      if (lane == 16) scal[1] = t;
     }
     cl.sync();
-    if (tid == 0) {
-      double r2 = remote(scal, 0)[0], b2 = remote(scal, 0)[1];
-      for (int c = 1; c < kSlices; ++c) {
-        r2 += remote(scal, c)[0];
-        b2 += remote(scal, c)[1];
+    if (warp == 0) {   // lanes 0-7: the slices' r partials, lanes 8-15: their b partials
+      const double p = tree8(lane < 16 ? remote(scal, lane & 7)[lane >> 3] : 0.0);
+      const double nrm = sqrt(p);
+      const double rnorm = __shfl_sync(full, nrm, 0), bnorm = __shfl_sync(full, nrm, 8);
+      if (lane == 0) {
+        if (its == 0) {
+          double rnorm0 = bnorm != 0.0 ? bnorm : rnorm;
+          scal[7] = fmax(rtol * rnorm0, atol);
+        }
+        scal[5] = rnorm;
+        scal[6] = bnorm;
+        scal[3] = rnorm;
+        g[0] = rnorm;
+        int rs = 0;
+        if (rnorm == 0.0) rs = 2;
+        else if (rnorm <= scal[7]) rs = 3;
+        else if (its >= max_it) rs = -3;
+        s_reason = rs;
       }
-      const double rnorm = sqrt(r2), bnorm = sqrt(b2);
-      if (its == 0) {
-        double rnorm0 = bnorm != 0.0 ? bnorm : rnorm;
-        scal[7] = fmax(rtol * rnorm0, atol);
-      }
-      scal[5] = rnorm;
-      scal[6] = bnorm;
-      scal[3] = rnorm;
-      g[0] = rnorm;
-      int rs = 0;
-      if (rnorm == 0.0) rs = 2;
-      else if (rnorm <= scal[7]) rs = 3;
-      else if (its >= max_it) rs = -3;
-      s_reason = rs;
     }
     __syncthreads();
     {
@@ -534,66 +670,98 @@ __global__ void __cluster_dims__(kSlices, 1, 1)
     // ---- Arnoldi steps (k_gmres_arnoldi), the Givens update of step k-1 during step k
     k = 0;
     for (;;) {
-      if (!gwarp) {
+      if (warp < 3) {
         matvec();
-        bar_work();
-        if (tid <= k) {
-          double a = 0.0;
-          const double* vj = Vs + (size_t)tid * ns;
-          for (int i = 0; i < nl; ++i) a = fma(avs[i], vj[i], a);
-          hp[tid] = a;
+        bar_prod();
+        for (int q0 = 0; q0 < LP * (k + 1); q0 += kProdThreads) {   // LP lanes per projection
+          const int q = q0 + tid, j = q / LP, blk = q - j * LP;
+          const bool on = j <= k;
+          const double t = slice_dot_lanes(avs, Vs + (size_t)(on ? j : 0) * ns, blk, on);
+          if (on && blk == 0) hp[j] = t;
         }
-      } else if (k > 0 && lane == 0) {
-        double res;
-        int rs;
-        givens_step(H + (size_t)(k - 1) * (R + 1), h, scal[2], k - 1, cs, sn, g, scal[3], ttol, &res, &rs);
-        scal[3] = res;
-        s_reason = rs;
+      } else if (k > 0) {
+        double res = 0.0;
+        int rs = 0;
+        givens_step_warp(H + (size_t)(k - 1) * (R + 1), h, scal[2], k - 1, cs, sn, g, scal[3], ttol, gbuf, &res,
+                         &rs);
+        if (lane == 0) {
+          scal[3] = res;
+          s_reason = rs;
+        }
       }
       cl.sync();                                  // partial projections; Givens of step k-1
-      if (k > 0) {
-        reason = *cl.map_shared_rank(&s_reason, 0);
-        if (reason != 0 || k >= R || its >= max_it) break;
-      }
-      if (tid <= k) {
-        double s = remote(hp, 0)[tid];
-        for (int c = 1; c < kSlices; ++c) s += remote(hp, c)[tid];
-        h[tid] = s;
+      {
+        // the first pass's slice partials are loaded together with CTA 0's decision
+        const int j = tid >> 3;
+        double p = j <= k ? remote(hp, tid & 7)[j] : 0.0;
+        if (k > 0) {
+          reason = *cl.map_shared_rank(&s_reason, 0);
+          if (reason != 0 || k >= R || its >= max_it) break;
+        }
+        p = tree8(p);
+        if (j <= k && (tid & 7) == 0) h[j] = p;
+        for (int q0 = kClusterThreads; q0 < 8 * (k + 1); q0 += kClusterThreads) {   // 8 lanes (slices) per j
+          const int q = q0 + tid, jj = q >> 3;
+          const double pp = tree8(jj <= k ? remote(hp, q & 7)[jj] : 0.0);
+          if (jj <= k && (q & 7) == 0) h[jj] = pp;
+        }
       }
       __syncthreads();
-      double* w = Vs + (size_t)(k + 1) * ns;
-      for (int i = tid; i < nl; i += blockDim.x) {
-        double v = avs[i];
-        for (int j = 0; j <= k; ++j) v = fma(-h[j], Vs[(size_t)j * ns + i], v);
-        w[i] = v;
+      // w = avs - sum_j h_j V_j on the slice (8 lanes, one chain each, per row) into wbuf; the
+      // lanes 0, 8, 16, 24 of a warp hold 4 consecutive rows: one block of the norm partial
+      const int npass = (8 * nl + kClusterThreads - 1) / kClusterThreads;
+      for (int q0 = 0; q0 < 8 * nl; q0 += kClusterThreads) {
+        const int q = q0 + tid, i = q >> 3, gq = q & 7;
+        double p = 0.0;
+        if (i < nl) {
+          p = gq == 0 ? avs[i] : 0.0;
+          for (int j = gq; j <= k; j += 8) p = fma(-h[j], Vs[(size_t)j * ns + i], p);
+        }
+        p = tree8(p);
+        if (i < nl && gq == 0) wbuf[i] = p;
+        double sq = i < nl ? p * p : 0.0;
+        sq += __shfl_xor_sync(full, sq, 8);
+        sq += __shfl_xor_sync(full, sq, 16);
+        if (lane == 0) nblk[q >> 5] = sq;
       }
       __syncthreads();
-      if (tid == 0) {
-        double a = 0.0;
-        for (int i = 0; i < nl; ++i) a = fma(w[i], w[i], a);
-        scal[0] = a;
+      if (warp == 0) {
+        double v = lane < LP && lane < 4 * npass ? nblk[lane] : 0.0;
+        for (int off = 1; off < LP; off <<= 1) v += __shfl_xor_sync(full, v, off);
+        if (lane == 0) scal[0] = v;
       }
-      cl.sync();                                  // partial norms
-      if (tid == 0) {
-        double s = remote(scal, 0)[0];
-        for (int c = 1; c < kSlices; ++c) s += remote(scal, c)[0];
-        const double tt = sqrt(s);
-        scal[2] = tt;
-        scal[4] = tt != 0.0 ? 1.0 / tt : 0.0;
+      cl.sync();                                  // partial norms and the unscaled slices
+      // the new vector: every CTA gathers the unscaled slices while warp 0 forms the norm,
+      // then scales its gathered copy and its own slice alike (the products of a normalise-
+      // then-gather, with one cluster barrier fewer)
+      {
+        const double pn = (warp == 0 && lane < 8) ? remote(scal, lane)[0] : 0.0;
+        for (int i = tid; i < nf; i += blockDim.x) {
+          const int c = i / ns;
+          vfull[i] = remote(wbuf, c)[i - c * ns];
+        }
+        if (warp == 0) {
+          double tt, inv;
+          norm_and_scale(tree8(pn), &tt, &inv);
+          if (lane == 0) {
+            scal[2] = tt;
+            scal[4] = inv;
+          }
+        }
       }
       __syncthreads();
       {
         const double tt = scal[2], inv = scal[4];
-        for (int i = tid; i < nl; i += blockDim.x) w[i] = tt != 0.0 ? w[i] * inv : w[i];
+        double* w = Vs + (size_t)(k + 1) * ns;
+        for (int i = tid; i < nl; i += blockDim.x) w[i] = tt != 0.0 ? wbuf[i] * inv : wbuf[i];
+        for (int i = tid; i < nf; i += blockDim.x) vfull[i] = tt != 0.0 ? vfull[i] * inv : vfull[i];
       }
-      cl.sync();                                  // the new vector's slices
-      gather(Vs, k + 1);
       __syncthreads();
       its += 1;
       k += 1;
     }
     // ---- KSPGMRESBuildSoln (k_gmres_update): back substitution and x += V y on the slice
-    if (tid == 0 && k > 0) back_substitute(H, R, g, k - 1, yv);
+    if (warp == 0 && k > 0) back_substitute(H, R, g, k - 1, yv, gbuf);
     __syncthreads();
     if (k > 0)
       for (int i = tid; i < nl; i += blockDim.x) {
@@ -623,10 +791,8 @@ int launch_gmres_fused(const GmresDev& G, FusedPlan* plan, const double* At, con
     plan->state = 0;
     if (G.nf <= 0 || G.restart > 63) return IB_ERR_ARG;
     ClusterSmem cs{G.nf, G.restart, (G.nf + kSlices - 1) / kSlices};
-    // at least R+1 work threads: one per projection of the longest Arnoldi step
-    const int work = max(64, 32 * ((cs.ns * kSlices + 31) / 32));
-    const int threads = work + 32;
-    if (threads > 1024) return IB_ERR_ARG;
+    if (slice_blocks_p2(cs.ns) > 16) return IB_ERR_ARG;   // a slice's norm blocks on 16 lanes
+    const int threads = kClusterThreads;
     int dev = 0, optin = 0;
     IB_CUDA_CHECK(cudaGetDevice(&dev));
     IB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));

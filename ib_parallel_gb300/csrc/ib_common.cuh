@@ -58,6 +58,25 @@ __device__ __forceinline__ double ghost_vertex(const double* __restrict__ f,
   return f[(J - 2) * g.nsx + (I - 2)];
 }
 
+// get_bc (operators_fluid.F90:475-535 with grid.F90:1091-1140) at ring index t: the value of
+// the next coarser level's field s on this level's boundary; coincident points copied,
+// midpoints averaged.
+__device__ __forceinline__ double ring_value(const double* __restrict__ s, const GridDims& g, int t) {
+  auto S = [&](int I, int J) { return s[(J - 2) * g.nsx + (I - 2)]; };
+  if (t >= g.bottom) {  // bottom / top edges: p = 0..m
+    bool top = t >= g.top;
+    int p = t - (top ? g.top : g.bottom);
+    int J = top ? 3 * g.n / 4 + 1 : g.n / 4 + 1;
+    int I = g.m / 4 + 1 + p / 2;
+    return (p & 1) ? 0.5 * (S(I, J) + S(I + 1, J)) : S(I, J);
+  }
+  bool right = t >= g.right;   // left / right edges: p = 0..n
+  int p = t - (right ? g.right : g.left);
+  int I = right ? 3 * g.m / 4 + 1 : g.m / 4 + 1;
+  int J = g.n / 4 + 1 + p / 2;
+  return (p & 1) ? 0.5 * (S(I, J) + S(I, J + 1)) : S(I, J);
+}
+
 inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 // Division of a non-negative int by a runtime divisor d >= 1 with a multiply-high and a

@@ -174,18 +174,18 @@ __global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const
 // column segment in order, combined by a fixed shuffle tree -- the product the cluster
 // GMRES solver forms, so that both solvers see identical operator outputs.
 __global__ void k_dense_mv(int n, const double* __restrict__ At, const double* __restrict__ x, double* __restrict__ y) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int r = q / kSlices, seg = q % kSlices;
-  const int cw = (n + kSlices - 1) / kSlices;
+  // rows in groups of S lanes, 32/S groups per warp (the cluster solver's layout)
+  const int S = mv_segments(n), gpw = 32 / S, cw = (n + S - 1) / S;
+  const int lane = threadIdx.x & 31, grp = lane / S, seg = lane - grp * S;
+  const int r = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * gpw + grp;
+  const bool live = grp < gpw && r < n;
   double p = 0.0;
-  if (r < n) {
+  if (live) {
     const int j0 = min(n, seg * cw), j1 = min(n, j0 + cw);
-    for (int j = j0; j < j1; ++j) p = fma(At[(size_t)j * n + r], x[j], p);
+    p = seg_dot(j0, j1, [&](int j, double acc) { return fma(At[(size_t)j * n + r], x[j], acc); });
   }
-  p += __shfl_xor_sync(0xffffffffu, p, 4);
-  p += __shfl_xor_sync(0xffffffffu, p, 2);
-  p += __shfl_xor_sync(0xffffffffu, p, 1);
-  if (r < n && seg == 0) y[r] = p;
+  p = seg_tree(p, seg, S);
+  if (live && seg == 0) y[r] = p;
 }
 
 // Column c of the precompute: unit vorticity at band vertex c (the previous one cleared),
@@ -429,7 +429,8 @@ int inf_assemble(Ctx* c) {
 int inf_dense_mv(Ctx* c, const double* x, double* y) {
   c->n_matvec += 1;
   count_launch();
-  k_dense_mv<<<cdiv((long long)kSlices * c->nf, 128), 128, 0, c->st>>>(c->nf, c->inf.St, x, y);
+  const int gpw = 32 / mv_segments(c->nf);
+  k_dense_mv<<<cdiv(32LL * cdiv(c->nf, gpw), 128), 128, 0, c->st>>>(c->nf, c->inf.St, x, y);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -11,6 +11,13 @@ int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vo
 int launch_curl(const GridDims& g, const double* s, const double* sbc, double* qx, double* qy, cudaStream_t st);
 int launch_coarsify(const GridDims& g, const double* fine, double* coarse, cudaStream_t st);
 int launch_get_bc(const GridDims& g, const double* s, double fac, double* ring, cudaStream_t st);
+// Rings of every level in one launch: dst[l] = fac * get_bc(src[l]), zero where src[l] is null.
+constexpr int kMaxLevels = 16;
+struct RingBatch {
+  const double* src[kMaxLevels] = {};
+  double* dst[kMaxLevels] = {};
+};
+int launch_get_bc_levels(const GridDims& g, const RingBatch& rb, int nlev, double fac, cudaStream_t st);
 int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st);
 int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st);
 int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st);
@@ -87,10 +94,62 @@ int launch_tors_save(int nt, const TorsState& s, cudaStream_t st);
 // recomputes sinv, cosv from theta (after theta is set other than by k_tors_dx)
 int launch_tors_trig(int nt, const TorsBody* tb, const TorsState& s, cudaStream_t st);
 
-// gmres.cu -- PETSc KSPGMRES as configured in variables.F90:565-574.  Reductions over the
-// unknowns are summed per slice (kSlices contiguous slices of ceil(nf/kSlices)), then over
-// the slices in order; dense products split each row into kSlices column segments.
+// gmres.cu -- PETSc KSPGMRES as configured in variables.F90:565-574.  Every driver sums in
+// one fixed order, so all produce the same iterates:
+//   * a slice partial (kSlices contiguous slices of ceil(nf/kSlices) unknowns) takes the
+//     rounded products in blocks of 4 consecutive rows, each block (p0+p1)+(p2+p3), and
+//     the blocks by a pairwise tree over slice_blocks_p2(n) entries (missing rows and
+//     blocks are 0);
+//   * the kSlices slice partials are combined by the pairwise tree
+//     ((p0+p1)+(p2+p3))+((p4+p5)+(p6+p7));
+//   * w = Av - sum_j h_j v_j runs eight chains (j = g, g+8, ...; chain 0 starts at Av) joined
+//     by the same pairwise tree;
+//   * a dense row product splits the row into mv_segments(nf) column segments of
+//     ceil(nf/S) columns, each summed as two chains (even and odd offsets) and e + o, the
+//     segments joined by a pairwise tree (seg_tree).
 constexpr int kSlices = 8;
+
+// Blocks of 4 rows in a slice of n rows, rounded up to a power of two (at least 1).
+__host__ __device__ inline int slice_blocks_p2(int n) {
+  int p = 1;
+  while (4 * p < n) p <<= 1;
+  return p;
+}
+
+// Column segments per row of the dense product: the most (at most kSlices) for which the
+// rows of one slice, in groups of S lanes that stay within a warp, fit in three warps.
+__host__ __device__ inline int mv_segments(int nf) {
+  const int nl = (nf + kSlices - 1) / kSlices;
+  for (int S = kSlices; S > 1; --S)
+    if (3 * (32 / S) >= nl) return S;
+  return 1;
+}
+
+// One row segment of the dense product: two chains over even and odd offsets, e + o.
+template <typename F>
+__device__ __forceinline__ double seg_dot(int j0, int j1, F&& term_fma) {
+  double e = 0.0, o = 0.0;
+  int j = j0;
+#pragma unroll 4
+  for (; j + 1 < j1; j += 2) {
+    e = term_fma(j, e);
+    o = term_fma(j + 1, o);
+  }
+  if (j < j1) e = term_fma(j, e);
+  return e + o;
+}
+
+// Pairwise tree over the S lanes of a row group (lane = group base + seg): at stride off,
+// seg adds seg+off when seg is a multiple of 2*off.  The sum is valid at seg 0.  Every lane
+// of the warp must call it.
+__device__ __forceinline__ double seg_tree(double p, int seg, int S) {
+  const int lane = threadIdx.x & 31;
+  for (int off = 1; off < S; off <<= 1) {
+    const double q = __shfl_sync(0xffffffffu, p, min(lane + off, 31));
+    if ((seg & (2 * off - 1)) == 0 && seg + off < S) p += q;
+  }
+  return p;
+}
 struct GmresDev {
   int nf, restart;
   double* V;       // (restart+1) * nf

@@ -138,6 +138,13 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete c; *msg = "stream creation failed"; return IB_ERR_CUDA;
   }
+  {
+    bool ok = cudaStreamCreateWithFlags(&c->st_aux, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+    c->ev_lv.assign(L, nullptr);
+    for (int k = 0; k < L && ok; ++k) ok = cudaEventCreateWithFlags(&c->ev_lv[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) { *msg = "stream or event creation failed"; ctx_destroy(c); return IB_ERR_CUDA; }
+  }
   int rc = dst_plan_create(&c->px, g.nsx);
   if (rc == IB_OK) rc = dst_plan_create(&c->py, g.nsy);
   if (rc != IB_OK) { *msg = "unsupported DST size (m, n must be 2^a 3^b 5^c)"; ctx_destroy(c); return rc; }
@@ -181,6 +188,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   stage_n = std::max(stage_n, nbc);
   size_t dbl = 0;
   dbl += (size_t)L * (3 * ns + 2 * nu + 2 * nv);         // state
+  dbl += (size_t)L * ns;                                 // per-level predictor right-hand sides
   dbl += (size_t)L * (2 * ns + nu + nv);                 // Schur scratch
   int tri_s = 0, tri_C = 0;
   tri_chunking(g.n, &tri_s, &tri_C);
@@ -208,7 +216,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     v.resize(L);
     for (int k = 0; k < L; ++k) v[k] = P.take<double>(n);
   };
-  lv(c->omega, ns); lv(c->s, ns); lv(c->rhs_old, ns);
+  lv(c->omega, ns); lv(c->s, ns); lv(c->rhs_old, ns); lv(c->rhs_lv, ns);
   lv(c->qx, nu); lv(c->q0x, nu); lv(c->qy, nv); lv(c->q0y, nv);
   lv(c->mv_w, ns); lv(c->mv_s, ns); lv(c->mv_qx, nu); lv(c->mv_qy, nv);
   double* tri_mem = P.take<double>((2 + L) * tri_n);
@@ -390,6 +398,11 @@ void ctx_destroy(Ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->stage_ev)
     if (e) cudaEventDestroy(e);
+  if (c->st_aux) cudaStreamSynchronize(c->st_aux);
+  for (auto& e : c->ev_lv)
+    if (e) cudaEventDestroy(e);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->st_aux) cudaStreamDestroy(c->st_aux);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -463,6 +476,20 @@ int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs
   a.alpha = (1.0 - 4.0 * cv) / c->normalize;
   a.beta = cv / c->normalize;
   return spectral_solve(c, PRE_PRED, a, c->tri_pred[k], om);
+}
+
+// The time step's form of the predictor at level k: rhsbc (timestepper.F90:184-189) is formed
+// inside the x pass from lastbc and the coarser level's updated vorticity (null on the
+// coarsest level), and the pass also copies rhs into rhs_old (timestepper.F90:228).
+static int op_predictor_step(Ctx* c, int k, const double* rhs, double* rhs_old, const double* coarse) {
+  DstXArgs a;
+  a.in = rhs; a.in2 = rhs_old; a.save = rhs_old; a.in4 = c->omega[k];
+  a.ring = c->lastbc[k]; a.fac = c->vfac[k]; a.coarse = coarse;
+  a.ca = c->con1[k]; a.cb = c->con2[k];
+  double cv = c->cvis[k];
+  a.alpha = (1.0 - 4.0 * cv) / c->normalize;
+  a.beta = cv / c->normalize;
+  return spectral_solve(c, PRE_PRED, a, c->tri_pred[k], c->omega[k]);
 }
 
 static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring);
@@ -939,22 +966,31 @@ int op_advance(Ctx* c) {
   // boundary values of the previous step (timestepper.F90:103-117) and the predictor, coarse
   // to fine (timestepper.F90:121-236)
   auto predictor = [&]() -> int {
-    for (int k = 0; k < L - 1; ++k) RC(launch_get_bc(g, c->omega[k + 1], 0.25, c->lastbc[k], c->st));
-    IB_CUDA_CHECK(cudaMemsetAsync(c->lastbc[L - 1], 0, 8 * (size_t)g.nbc, c->st));
+    // lastbc from the vorticity before the update, every level in one launch (zero on the
+    // coarsest level)
+    RingBatch rb;
+    for (int k = 0; k < L; ++k) {
+      rb.src[k] = k < L - 1 ? c->omega[k + 1] : nullptr;
+      rb.dst[k] = c->lastbc[k];
+    }
+    RC(launch_get_bc_levels(g, rb, L, 0.25, st));
+    // fork: the nonlinear right-hand sides of all levels (old vorticity and fluxes only) on
+    // the second stream, coarsest first, each level's solve waiting for its own
+    IB_CUDA_CHECK(cudaEventRecord(c->ev_fork, st));
+    IB_CUDA_CHECK(cudaStreamWaitEvent(c->st_aux, c->ev_fork, 0));
     for (int k = L - 1; k >= 0; --k) {
-      const double* obc = c->zero_ring;
-      if (k < L - 1) {
-        RC(launch_get_bc(g, c->omega[k + 1], 0.25, c->omegabc, c->st));
-        obc = c->omegabc;
-      }
       RC(launch_nonlinear(g, c->omega[k], c->lastbc[k], c->qx[k], c->q0x[k], c->qy[k], c->q0y[k], c->nlx, c->nly,
-                          c->st));
-      RC(launch_rhsbc(g, c->rhsbc, c->lastbc[k], obc, c->vfac[k], c->st));
-      RC(launch_rot(g, c->nlx, c->nly, c->rhs, c->st));
+                          c->st_aux));
+      RC(launch_rot(g, c->nlx, c->nly, c->rhs_lv[k], c->st_aux));
       if (it == 1)
-        IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs, 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, c->st));
-      RC(op_predictor(c, k, c->omega[k], c->rhs, c->rhs_old[k], c->rhsbc));
-      IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs, 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, c->st));
+        IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs_lv[k], 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice,
+                                      c->st_aux));
+      IB_CUDA_CHECK(cudaEventRecord(c->ev_lv[k], c->st_aux));
+    }
+    // the coarse-to-fine chain; waiting for level 0's event joins the second stream
+    for (int k = L - 1; k >= 0; --k) {
+      IB_CUDA_CHECK(cudaStreamWaitEvent(st, c->ev_lv[k], 0));
+      RC(op_predictor_step(c, k, c->rhs_lv[k], c->rhs_old[k], k < L - 1 ? c->omega[k + 1] : nullptr));
     }
     return IB_OK;
   };

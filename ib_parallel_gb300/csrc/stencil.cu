@@ -92,22 +92,17 @@ __global__ void k_coarsify(GridDims g, const double* __restrict__ fine, double* 
 __global__ void k_get_bc(GridDims g, const double* __restrict__ s, double fac, double* __restrict__ ring) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.nbc) return;
-  auto S = [&](int I, int J) { return s[(J - 2) * g.nsx + (I - 2)]; };
-  double v;
-  if (t >= g.bottom) {  // bottom / top edges: p = 0..m
-    bool top = t >= g.top;
-    int p = t - (top ? g.top : g.bottom);
-    int J = top ? 3 * g.n / 4 + 1 : g.n / 4 + 1;
-    int I = g.m / 4 + 1 + p / 2;
-    v = (p & 1) ? 0.5 * (S(I, J) + S(I + 1, J)) : S(I, J);
-  } else {              // left / right edges: p = 0..n
-    bool right = t >= g.right;
-    int p = t - (right ? g.right : g.left);
-    int I = right ? 3 * g.m / 4 + 1 : g.m / 4 + 1;
-    int J = g.n / 4 + 1 + p / 2;
-    v = (p & 1) ? 0.5 * (S(I, J) + S(I, J + 1)) : S(I, J);
-  }
-  ring[t] = v * fac;
+  ring[t] = ring_value(s, g, t) * fac;
+}
+
+// The same for every level at once (blockIdx.y = level): ring l from field src[l], or zero
+// where src[l] is null.
+__global__ void k_get_bc_levels(GridDims g, RingBatch rb, double fac) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int l = blockIdx.y;
+  if (t >= g.nbc) return;
+  const double* s = rb.src[l];
+  rb.dst[l][t] = s ? ring_value(s, g, t) * fac : 0.0;
 }
 
 // ------------------------------------------------------------- apply_bc
@@ -189,6 +184,12 @@ int launch_coarsify(const GridDims& g, const double* fine, double* coarse, cudaS
 int launch_get_bc(const GridDims& g, const double* s, double fac, double* ring, cudaStream_t st) {
   count_launch();
   k_get_bc<<<blocks(g.nbc), 256, 0, st>>>(g, s, fac, ring);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_get_bc_levels(const GridDims& g, const RingBatch& rb, int nlev, double fac, cudaStream_t st) {
+  if (nlev < 1 || nlev > kMaxLevels) return IB_ERR_ARG;
+  count_launch();
+  k_get_bc_levels<<<dim3(blocks(g.nbc), nlev), 256, 0, st>>>(g, rb, fac);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st) {

@@ -20,15 +20,23 @@ void tri_chunking(int n, int* s, int* C) {
   *C = n / bestd;
 }
 
-size_t tri_table_doubles(int nx, int s, int C) { return (size_t)nx * (3 * (size_t)s + 2 * (size_t)(C - 1) + 2); }
+size_t tri_table_doubles(int nx, int s, int C) {
+  const size_t m = C > 1 ? (size_t)(C - 1) : 1;
+  return (size_t)nx * (3 * (size_t)s + m * m);
+}
 
 int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, double* dev) {
   int s = 0, C = 0;
   tri_chunking(ny + 1, &s, &C);
   op->nx = nx; op->ny = ny; op->s = s; op->C = C; op->sigma = sigma;
-  const size_t S = (size_t)s * nx, R = (size_t)(C > 1 ? C - 1 : 1) * nx;
-  std::vector<double> inv(S), sinv(S), gL(S), inv2(R, 0.0), e2(R, 0.0);
-  std::vector<long double> beta(s), d(s), g(s);
+  const int m = C > 1 ? C - 1 : 1;
+  const size_t S = (size_t)s * nx, R = (size_t)m * m * nx;
+  std::vector<double> tab(3 * S + R, 0.0);
+  double* inv = tab.data();
+  double* sinv = inv + S;
+  double* gL = inv + 2 * S;
+  double* rinv = inv + 3 * S;
+  std::vector<long double> beta(s), d(s), g(s), bp(m), z(m), x(m);
   for (int k = 0; k < nx; ++k) {
     long double a = 2.0L + (long double)shift[k];
     beta[0] = a;
@@ -43,82 +51,81 @@ int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, doub
     g[s - 1] = d[s - 1];
     for (int j = s - 2; j >= 0; --j) g[j] = d[j] + g[j + 1] / beta[j];
     for (int j = 0; j < s; ++j) gL[(size_t)j * nx + k] = (double)g[j];
-    // interface system tridiag(-B, A, -B), size C-1
+    if (C < 2) continue;
+    // interface system tridiag(-B, A, -B) of size m = C-1, tabulated as its dense inverse
+    // (one Thomas solve per unit vector, in extended precision)
     long double A = a - 2.0L * g[0], B = g[s - 1];
-    long double bp = A;
-    for (int c = 0; c < C - 1; ++c) {
-      if (c > 0) bp = A - B * B / bp;
-      inv2[(size_t)c * nx + k] = (double)(1.0L / bp);
-      e2[(size_t)c * nx + k] = (double)(B / bp);
+    bp[0] = A;
+    for (int c = 1; c < m; ++c) bp[c] = A - B * B / bp[c - 1];
+    for (int j = 0; j < m; ++j) {
+      for (int c = 0; c < m; ++c) z[c] = ((c == j ? 1.0L : 0.0L) + (c > 0 ? B * z[c - 1] : 0.0L)) / bp[c];
+      x[m - 1] = z[m - 1];
+      for (int c = m - 2; c >= 0; --c) x[c] = z[c] + (B / bp[c]) * x[c + 1];
+      for (int c = 0; c < m; ++c) rinv[((size_t)c * m + j) * nx + k] = (double)x[c];
     }
   }
   op->inv = dev;
   op->sinv = dev + S;
   op->gL = dev + 2 * S;
-  op->inv2 = dev + 3 * S;
-  op->e2 = dev + 3 * S + R;
-  IB_CUDA_CHECK(cudaMemcpy(op->inv, inv.data(), 8 * S, cudaMemcpyHostToDevice));
-  IB_CUDA_CHECK(cudaMemcpy(op->sinv, sinv.data(), 8 * S, cudaMemcpyHostToDevice));
-  IB_CUDA_CHECK(cudaMemcpy(op->gL, gL.data(), 8 * S, cudaMemcpyHostToDevice));
-  IB_CUDA_CHECK(cudaMemcpy(op->inv2, inv2.data(), 8 * R, cudaMemcpyHostToDevice));
-  IB_CUDA_CHECK(cudaMemcpy(op->e2, e2.data(), 8 * R, cudaMemcpyHostToDevice));
+  op->rinv = dev + 3 * S;
+  IB_CUDA_CHECK(cudaMemcpy(dev, tab.data(), 8 * tab.size(), cudaMemcpyHostToDevice));
   return IB_OK;
 }
 
-// One CTA: Mb consecutive modes x C chunks (thread t: mode t % Mb, chunk t / Mb).  The
-// CTA's ny x Mb tile and its factor tables are staged in shared memory, so the
-// sequential recurrences run on shared-memory latency.
-__global__ void k_tri(TriOp op, const double* F, double* U, int ld, int Mb) {
+// One CTA: Mb consecutive modes x C chunks (thread t: mode t % Mb, chunk t / Mb, so a warp
+// holds 32/Mb chunks of Mb modes).  The CTA's ny x Mb tile and its factor tables are staged
+// in shared memory, so the sequential recurrences run on shared-memory latency.  The
+// interface values come from the tabulated inverse of the interface system: every chunk
+// thread forms one of them with C-1 independent products, instead of one thread per mode
+// running a 2(C-1)-step recurrence while the rest of its warp idles (an FP64 warp
+// instruction costs the same issue time whatever its active lanes).
+__global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb) {
   extern __shared__ double sm[];
   const int C = op.C, s = op.s, d = s + 1, nx = op.nx, ny = op.ny;
+  const int m = C > 1 ? C - 1 : 1;
+  const int trows = 3 * s + (C > 1 ? m * m : 0);   // table rows staged: inv, sinv, gL, rinv
   double* tile = sm;                       // ny x Mb
   double* t_inv = tile + (size_t)ny * Mb;  // s x Mb
   double* t_sinv = t_inv + s * Mb;
   double* t_gL = t_sinv + s * Mb;
-  double* t_inv2 = t_gL + s * Mb;          // (C-1) x Mb
-  double* t_e2 = t_inv2 + (C - 1) * Mb;
-  double* pfirst = t_e2 + (C - 1) * Mb;    // C x Mb
+  double* t_r = t_gL + s * Mb;             // m*m x Mb
+  double* pfirst = t_inv + (size_t)trows * Mb;  // C x Mb
   double* plast = pfirst + C * Mb;
-  double* yv = plast + C * Mb;             // (C+1) x Mb
+  double* hv = plast + C * Mb;             // (C+1) x Mb: interface right-hand sides
+  double* yv = hv + (C + 1) * Mb;          // (C+1) x Mb: interface values
   const int k0 = blockIdx.x * Mb;
   const int nthr = blockDim.x;
-  // stage the tile and the tables (coalesced along modes): thread t owns mode column t % Mb
-  // and rows t / Mb + i * (nthr / Mb); no division inside the loops
+  // stage the tile (rows of F) and the tables (rows of op.inv.., contiguous with stride nx),
+  // coalesced along modes, 8 loads in flight per thread: thread t owns mode column t % Mb
+  // and rows t / Mb + i * (nthr / Mb)
   const int rstep = nthr / Mb;
   const int kl0 = threadIdx.x % Mb, r00 = threadIdx.x / Mb;
   const bool kin = k0 + kl0 < nx && r00 < rstep;
   {
     const double* src = F + k0 + kl0;
-    for (int r = r00; r < ny; r += 4 * rstep) {
-      double v[4];
+    const double* tsrc = op.inv + min(k0 + kl0, nx - 1);
+    const int tot = ny + trows;
+    for (int r = r00; r < tot; r += 8 * rstep) {
+      double v[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 8; ++u) {
         int rr = r + u * rstep;
-        v[u] = (kin && rr < ny) ? src[(size_t)rr * ld] : 0.0;
+        v[u] = 0.0;
+        if (rr < ny) { if (kin) v[u] = src[(size_t)rr * ld]; }
+        else if (rr < tot) v[u] = __ldg(tsrc + (size_t)(rr - ny) * nx);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 8; ++u) {
         int rr = r + u * rstep;
-        if (rr < ny && r00 < rstep) tile[rr * Mb + kl0] = v[u];
+        if (rr < tot && r00 < rstep) tile[rr * Mb + kl0] = v[u];
       }
     }
-  }
-  for (int q = threadIdx.x; q < s * Mb; q += nthr) {
-    int j = q / Mb, kl = q - j * Mb, k = min(k0 + kl, nx - 1);
-    t_inv[q] = op.inv[(size_t)j * nx + k];
-    t_sinv[q] = op.sinv[(size_t)j * nx + k];
-    t_gL[q] = op.gL[(size_t)j * nx + k];
-  }
-  for (int q = threadIdx.x; q < (C - 1) * Mb; q += nthr) {
-    int j = q / Mb, kl = q - j * Mb, k = min(k0 + kl, nx - 1);
-    t_inv2[q] = op.inv2[(size_t)j * nx + k];
-    t_e2[q] = op.e2[(size_t)j * nx + k];
   }
   __syncthreads();
   const int t = threadIdx.x;
   const int kl = t % Mb, c = t / Mb;
   const bool active = c < C;
-  // phase 1: chunk solves with zero ends; interface rows keep sigma*f until phase 3
+  // phase 1: chunk solves with zero ends; interface rows keep f until phase 2
   if (active) {
     double* col = tile + c * d * Mb + kl;
     const double* ti = t_inv + kl;
@@ -137,22 +144,27 @@ __global__ void k_tri(TriOp op, const double* F, double* U, int ld, int Mb) {
     pfirst[c * Mb + kl] = u;
   }
   __syncthreads();
-  // phase 2: interface values, one thread per mode
-  if (c == 0) {
-    double dp = 0.0;
-    for (int ci = 1; ci < C; ++ci) {
-      int q = (ci - 1) * Mb + kl;
-      double h = fma(op.sigma, tile[(ci * d - 1) * Mb + kl], plast[(ci - 1) * Mb + kl] + pfirst[ci * Mb + kl]);
-      dp = fma(t_e2[q], dp, t_inv2[q] * h);
-      yv[ci * Mb + kl] = dp;
+  // phase 2a: right-hand side of interface c (between chunks c-1 and c)
+  if (active && c >= 1)
+    hv[c * Mb + kl] = fma(op.sigma, tile[(c * d - 1) * Mb + kl], plast[(c - 1) * Mb + kl] + pfirst[c * Mb + kl]);
+  __syncthreads();
+  // phase 2b: interface value c = row c-1 of the interface inverse times the right-hand sides
+  if (active) {
+    if (c >= 1) {
+      const double* rr = t_r + (size_t)(c - 1) * m * Mb + kl;
+      const double* hh = hv + Mb + kl;
+      double y0 = 0.0, y1 = 0.0;
+      int j = 0;
+      for (; j + 1 < m; j += 2) {
+        y0 = fma(rr[j * Mb], hh[j * Mb], y0);
+        y1 = fma(rr[(j + 1) * Mb], hh[(j + 1) * Mb], y1);
+      }
+      if (j < m) y0 = fma(rr[j * Mb], hh[j * Mb], y0);
+      yv[c * Mb + kl] = y0 + y1;
+    } else {
+      yv[kl] = 0.0;
+      yv[C * Mb + kl] = 0.0;
     }
-    double y = 0.0;
-    for (int ci = C - 1; ci >= 1; --ci) {
-      y = fma(t_e2[(ci - 1) * Mb + kl], y, yv[ci * Mb + kl]);
-      yv[ci * Mb + kl] = y;
-    }
-    yv[kl] = 0.0;
-    yv[C * Mb + kl] = 0.0;
   }
   __syncthreads();
   // phase 3: add the interface responses; interface rows take the interface values
@@ -176,7 +188,8 @@ __global__ void k_tri(TriOp op, const double* F, double* U, int ld, int Mb) {
 }
 
 size_t tri_smem(const TriOp& op, int Mb) {
-  return sizeof(double) * (size_t)Mb * ((size_t)op.ny + 3 * op.s + 2 * (op.C - 1) + 2 * op.C + op.C + 1);
+  const size_t m = op.C > 1 ? (size_t)(op.C - 1) : 0;
+  return sizeof(double) * (size_t)Mb * ((size_t)op.ny + 3 * (size_t)op.s + m * m + 2 * (size_t)op.C + 2 * ((size_t)op.C + 1));
 }
 
 int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaunch& L, cudaStream_t st) {

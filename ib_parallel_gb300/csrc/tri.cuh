@@ -16,8 +16,9 @@
 // Every system is tridiag(-1, a_k, -1) of size n-1.  For parallelism it is cut
 // into C chunks of s = n/C - 1 rows separated by C-1 interface rows: each chunk is
 // solved with zero ends (Thomas with tabulated pivots), the interface values then
-// satisfy a constant-coefficient tridiagonal system of size C-1, and each chunk
-// adds the interface responses (tabulated).  5 FP64 operations per point.
+// satisfy a constant-coefficient tridiagonal system of size C-1 (solved with its
+// tabulated inverse), and each chunk adds the interface responses (tabulated).
+// 5 FP64 operations per point.
 #pragma once
 #include "ib_common.cuh"
 
@@ -30,8 +31,7 @@ struct TriOp {
   double* inv = nullptr;  // s x nx: 1/pivot
   double* sinv = nullptr; // s x nx: sigma/pivot
   double* gL = nullptr;   // s x nx: chunk response to a unit left end value
-  double* inv2 = nullptr; // (C-1) x nx: reduced-system 1/pivot
-  double* e2 = nullptr;   // (C-1) x nx: reduced-system B/pivot
+  double* rinv = nullptr; // (C-1)^2 x nx: inverse of the interface system, row-major per mode
 };
 
 struct TriLaunch {
