@@ -124,8 +124,8 @@ int ib_ctci(IbCtx* ctx, const double* vort, double* s);
  * vort and s are DEVICE arrays ((n-1) x (m-1), x fastest); the kernels run on `stream` (a
  * cudaStream_t, NULL for the default stream) and the call returns without waiting for them.
  * Scratch and tables live in one 16 MiB static device array that each GPU loading the library
- * keeps until the process exits: grids needing more ((m-1)(n-1) plus the tables; 1600 x 800
- * fits, 1920 x 960 does not) fail with IB_ERR_ARG.  The first call on a device, and the first
+ * keeps until the process exits: grids needing more ((m-1)(n-1) plus the tables; 1200 x 600
+ * fits, 1280 x 640 does not) fail with IB_ERR_ARG.  The first call on a device, and the first
  * after the grid size changes, does the set-up with synchronous copies: make it before any
  * stream capture.  All calls on a device share the array: calls whose kernels overlap on the
  * GPU race and give wrong results.  Errors are reported through ib_last_error(). */

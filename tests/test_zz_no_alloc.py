@@ -65,8 +65,9 @@ def test_ctci_static_rejects_oversized_grid():
     # checked before any CUDA call, so the dummy (never dereferenced) pointers are safe
     lib = G.load()
     dummy = C.c_void_p(0x1000)
-    rc = lib.ib_ctci_static(1920, 960, dummy, dummy, None)
-    assert rc == IB_ERR_ARG
-    assert "16 MiB" in lib.ib_last_error().decode()
+    for m, n in [(1920, 960), (1280, 640)]:
+        rc = lib.ib_ctci_static(m, n, dummy, dummy, None)
+        assert rc == IB_ERR_ARG
+        assert "16 MiB" in lib.ib_last_error().decode()
     rc = lib.ib_ctci_static(64, 30, dummy, dummy, None)
     assert rc == IB_ERR_ARG
