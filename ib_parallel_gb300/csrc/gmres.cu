@@ -447,28 +447,28 @@ struct ClusterSmem {
 constexpr int kClusterThreads = 128;
 constexpr int kProdThreads = 96;
 
-// givens_step's arithmetic on one whole warp: the products off the rotated value's chain and
-// the column entries on all lanes, the chain on lane 0.  buf: 2*it doubles of shared memory.
+// givens_step's arithmetic on one whole warp (it < 32): lane j holds rotation j and the
+// product cs[j]*h[j+1] in registers, the chain of rotated values runs on every lane in step
+// (each step's operands by shuffle, so nothing waits on shared memory), lane j keeps the value
+// before rotation j and forms column entry j.
 __device__ void givens_step_warp(double* __restrict__ col, const double* __restrict__ h, double tt, int it,
                                  double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g,
-                                 double prev_res, double ttol, double* __restrict__ buf, double* res_out,
-                                 int* reason_out) {
+                                 double prev_res, double ttol, double* res_out, int* reason_out) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  double* pj = buf;        // cs[j] * h[j+1]
-  double* cj = buf + it;   // the rotated value before rotation j
-  for (int j = lane; j < it; j += 32) pj[j] = cs[j] * h[j + 1];
-  __syncwarp();
-  double c = h[0];
-  if (lane == 0)
-    for (int j = 0; j < it; ++j) {
-      cj[j] = c;
-      c = fma(-sn[j], c, pj[j]);
-    }
-  __syncwarp();
-  c = __shfl_sync(full, c, 0);
-  for (int j = lane; j < it; j += 32) col[j] = fma(sn[j], h[j + 1], cs[j] * cj[j]);
-  const double gi = g[it];
+  const bool mine = lane < it;
+  const double csj = mine ? cs[lane] : 0.0, snj = mine ? sn[lane] : 0.0;
+  const double hj1 = mine ? h[lane + 1] : 0.0;
+  const double pj = csj * hj1;
+  const double gi = g[it];   // read by every lane before lane 0 rewrites it
+  double c = h[0], cmine = 0.0;
+#pragma unroll 8
+  for (int j = 0; j < it; ++j) {
+    const double sj = __shfl_sync(full, snj, j), pp = __shfl_sync(full, pj, j);
+    if (lane == j) cmine = c;
+    c = fma(-sj, c, pp);
+  }
+  if (mine) col[lane] = fma(snj, hj1, csj * cmine);
   const bool hapend = happy_breakdown(tt, gi);
   const double r2 = fma(c, c, tt * tt);
   const double rn = r2 != 0.0 ? rsqrt(r2) : 0.0;
@@ -512,10 +512,10 @@ __device__ void givens_step_warp(double* __restrict__ col, const double* __restr
 //      the previous step;                                                    cluster barrier
 //      the previous step's convergence decision is read from CTA 0 (every CTA branches
 //      alike), then the projections are summed over the slices (8 lanes per projection);
-//   B: w = A v - sum h_j v_j on the slice (8 lanes per row) and its partial norm;
-//                                                                            cluster barrier
-//   C: the norm, the normalised slice;                                       cluster barrier
-//   D: every CTA gathers the full new vector through distributed shared memory.
+//   B: w = A v - sum h_j v_j on the slice (8 lanes per row) and its partial norm, the
+//      unscaled slice kept for the others to read;                           cluster barrier
+//   C: every CTA gathers the unscaled slices while forming the norm, then scales its gathered
+//      copy and its own slice by 1/norm.
 // No thread waits on a flag: the only waits are the cluster and CTA barriers, which every
 // thread of every CTA reaches the same number of times.
 __global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThreads)
@@ -682,8 +682,7 @@ __global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThread
       } else if (k > 0) {
         double res = 0.0;
         int rs = 0;
-        givens_step_warp(H + (size_t)(k - 1) * (R + 1), h, scal[2], k - 1, cs, sn, g, scal[3], ttol, gbuf, &res,
-                         &rs);
+        givens_step_warp(H + (size_t)(k - 1) * (R + 1), h, scal[2], k - 1, cs, sn, g, scal[3], ttol, &res, &rs);
         if (lane == 0) {
           scal[3] = res;
           s_reason = rs;
@@ -741,9 +740,10 @@ __global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThread
           vfull[i] = remote(wbuf, c)[i - c * ns];
         }
         if (warp == 0) {
-          double tt, inv;
-          norm_and_scale(tree8(pn), &tt, &inv);
+          const double sq = tree8(pn);
           if (lane == 0) {
+            double tt, inv;
+            norm_and_scale(sq, &tt, &inv);
             scal[2] = tt;
             scal[4] = inv;
           }
@@ -789,7 +789,7 @@ int launch_gmres_fused(const GmresDev& G, FusedPlan* plan, const double* At, con
                        double atol, int max_it, cudaStream_t st) {
   if (plan->state < 0) {
     plan->state = 0;
-    if (G.nf <= 0 || G.restart > 63) return IB_ERR_ARG;
+    if (G.nf <= 0 || G.restart > 32) return IB_ERR_ARG;   // the Givens warp holds a rotation per lane
     ClusterSmem cs{G.nf, G.restart, (G.nf + kSlices - 1) / kSlices};
     if (slice_blocks_p2(cs.ns) > 16) return IB_ERR_ARG;   // a slice's norm blocks on 16 lanes
     const int threads = kClusterThreads;
