@@ -99,6 +99,7 @@ struct Ctx {
   DstPlan px, py;
   DstLaunch lx, ly_none;
   DstLaunch lx_small;              // x passes over a few rows (latency-bound)
+  DstLaunch lx_batch;              // x passes over every level at once
 
   // per-mode tridiagonal operators replacing the y-direction spectral solves
   TriOp tri_ctci, tri_ainv;

@@ -202,7 +202,7 @@ __device__ __forceinline__ void stockham_stage(const double2* __restrict__ in, d
 
 // Transform B lines in place: line b holds x_1..x_N at xb[b*ldx + 0..N-1] and
 // receives Y_1..Y_N there.  zA, zB: B*P complex workspace each.
-__device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2* zA, double2* zB) {
+__device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2* zA, double2* zB, int narrow_scan) {
   const int tid = threadIdx.x, NT = blockDim.x;
   const int P = pl.P, M = pl.M;
   // --- pre-processing: y (length M, real) written into zA viewed as doubles
@@ -264,11 +264,36 @@ __device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2*
     }
   }
   __syncthreads();
-  // --- inclusive prefix sum over positions 0,2,...,2(P-1): odd outputs.  Each line is scanned
-  // by a group of wpl warps (all warps of the CTA share the lines): short sequential runs per
-  // thread, a warp shuffle scan, then the group's warp totals in shared memory.
-  __shared__ double s_wt[32];
+  // --- inclusive prefix sum over positions 0,2,...,2(P-1): odd outputs
   const int lane = tid & 31, warp = tid >> 5, nwarps = NT >> 5;
+  if (narrow_scan) {
+    // one warp per line: sequential runs of ceil(P/32) per lane and a warp shuffle scan, the
+    // fewest FP64 instructions (for launches whose other CTAs keep the SM busy meanwhile)
+    const int c = (P + 31) >> 5;
+    for (int b = warp; b < B; b += nwarps) {
+      double* o = xb + b * ldx;
+      const int s0 = min(lane * c, P), s1 = min(s0 + c, P);
+      double acc = 0.0;
+      for (int i = s0; i < s1; ++i) acc += o[2 * i];
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        double v = __shfl_up_sync(0xffffffffu, acc, off);
+        if (lane >= off) acc += v;
+      }
+      double run = __shfl_up_sync(0xffffffffu, acc, 1);
+      if (lane == 0) run = 0.0;
+      for (int i = s0; i < s1; ++i) {
+        run += o[2 * i];
+        o[2 * i] = run;
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  // every warp of the CTA takes part: a group of wpl warps per line, short sequential runs per
+  // thread, a warp shuffle scan, then the group's warp totals in shared memory (the shortest
+  // dependent chain, for latency-bound launches)
+  __shared__ double s_wt[32];
   const int wpl = nwarps >= B ? nwarps / B : 1;           // warps per line
   const int groups = nwarps >= B ? B : nwarps;            // lines in flight at once
   const int c = (P + 32 * wpl - 1) / (32 * wpl);
@@ -364,7 +389,7 @@ __device__ __forceinline__ double x_load(const DstXArgs& a, const double* __rest
 
 template <int PRE>
 __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, const __grid_constant__ DstXArgs a,
-                                               GridDims g, int B) {
+                                               GridDims g, int B, int narrow_scan) {
   const double* ain = a.nlev ? a.lin[blockIdx.y] : a.in;
   double* aout = a.nlev ? a.lout[blockIdx.y] : a.out;
   extern __shared__ double2 smem2[];
@@ -417,7 +442,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
       }
     }
     __syncthreads();
-    dst_lines(pl, B, xb, ldx, zA, zB);
+    dst_lines(pl, B, xb, ldx, zA, zB, narrow_scan);
   }
   for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
     int b = pl.fd_N.div(it), j = it - b * N;
@@ -594,7 +619,7 @@ int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, co
 }
 
 // ------------------------------------------------------------- y pass
-__global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, DstYArgs a, int B) {
+__global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, DstYArgs a, int B, int narrow_scan) {
   extern __shared__ double2 smem2[];
   const int ldx = pl.M;
   const int N = pl.N;
@@ -608,7 +633,7 @@ __global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, Dst
     xa[b * ldx + j] = col < ncols ? a.a[(size_t)j * ld + col] : 0.0;
   }
   __syncthreads();
-  dst_lines(pl, B, xa, ldx, zA, zB);
+  dst_lines(pl, B, xa, ldx, zA, zB, narrow_scan);
   for (int it = threadIdx.x; it < B * N; it += blockDim.x) {
     int j = it / B, b = it - j * B;
     int col = col0 + b;
@@ -622,6 +647,10 @@ size_t dst_smem_y(const DstPlan& p, int B, DstYMode) { return (size_t)B * p.M * 
 template <typename K>
 static int launch_cfg(K kern, size_t smem) {
   static_assert(sizeof(K) > 0, "");
+  // the largest shared-memory carveout: the transforms' occupancy is bound by shared memory
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
+      cudaSuccess)
+    return IB_ERR_CUDA;
   if (smem > 48 * 1024) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return IB_ERR_CUDA;
@@ -641,25 +670,25 @@ int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs&
       rc = launch_cfg(k_dst_x<PRE_COPY>, smem);
       if (rc) return rc;
       count_launch();
-      k_dst_x<PRE_COPY><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      k_dst_x<PRE_COPY><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B, L.narrow_scan);
       break;
     case PRE_COMBINE:
       rc = launch_cfg(k_dst_x<PRE_COMBINE>, smem);
       if (rc) return rc;
       count_launch();
-      k_dst_x<PRE_COMBINE><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      k_dst_x<PRE_COMBINE><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B, L.narrow_scan);
       break;
     case PRE_PRED:
       rc = launch_cfg(k_dst_x<PRE_PRED>, smem);
       if (rc) return rc;
       count_launch();
-      k_dst_x<PRE_PRED><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      k_dst_x<PRE_PRED><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B, L.narrow_scan);
       break;
     default:
       rc = launch_cfg(k_dst_x<PRE_APPLYBC>, smem);
       if (rc) return rc;
       count_launch();
-      k_dst_x<PRE_APPLYBC><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B);
+      k_dst_x<PRE_APPLYBC><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B, L.narrow_scan);
       break;
   }
   IB_CUDA_CHECK(cudaGetLastError());
@@ -674,7 +703,7 @@ int dst_pass_y(const DstPlan& py, int ncols, int ld, DstYMode, const DstYArgs& a
   int rc = launch_cfg(k_dst_y, smem);
   if (rc) return rc;
   count_launch();
-  k_dst_y<<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B);
+  k_dst_y<<<grid, L.NT, smem, st>>>(d, ncols, ld, a, L.B, L.narrow_scan);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

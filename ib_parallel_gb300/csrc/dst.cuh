@@ -32,6 +32,7 @@ struct DstPlan {
 struct DstLaunch {
   int B = 1;       // lines per CTA
   int NT = 128;    // threads per CTA
+  int narrow_scan = 0;   // 1: one warp scans each line (fewer FP64 instructions); 0: all warps
 };
 
 int dst_plan_create(DstPlan* p, int N);   // N = M-1, M divisible by 4, M = 2^a 3^b 5^c

@@ -60,10 +60,12 @@ static int tune(Ctx* c) {
   IB_CUDA_CHECK(cudaMemsetAsync(c->spec2, 0, sizeof(double) * c->g.ns, c->st));
   const int Bs[] = {1, 2, 3, 4, 5, 6, 8, 10, 12, 16};
   const int NTs[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 512};
-  for (int which = 0; which < 3; ++which) {
+  // 0: one level's x pass, 1: y pass, 2: x pass over a few rows, 3: x pass over every level
+  for (int which = 0; which < 4; ++which) {
+    if (which == 3 && c->L < 2) { c->lx_batch = c->lx; continue; }
     const DstPlan& pl = which != 1 ? c->px : c->py;
-    DstLaunch* out = which == 0 ? &c->lx : (which == 1 ? &c->ly_none : &c->lx_small);
-    int nlines = which == 0 ? c->g.nsy : (which == 1 ? c->g.nsx : std::min(32, c->g.nsy));
+    DstLaunch* out = which == 0 ? &c->lx : (which == 1 ? &c->ly_none : (which == 2 ? &c->lx_small : &c->lx_batch));
+    int nlines = which == 1 ? c->g.nsx : (which == 2 ? std::min(32, c->g.nsy) : c->g.nsy);
     float best = 1e30f;
     DstLaunch bestL = *out;
     for (int B : Bs) {
@@ -71,19 +73,25 @@ static int tune(Ctx* c) {
       if ((long long)smem > smem_max || B > nlines) continue;
       for (int NT : NTs) {
         if (NT > 32 * B * 8) continue;
-        DstLaunch L; L.B = B; L.NT = NT;
-        float ms = 0;
-        auto run = [&]() -> int {
-          if (which != 1) {
+        for (int narrow = 0; narrow < 2; ++narrow) {
+          DstLaunch L; L.B = B; L.NT = NT; L.narrow_scan = narrow;
+          float ms = 0;
+          auto run = [&]() -> int {
+            if (which == 1) {
+              DstYArgs a; a.a = c->spec1;
+              return dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_NONE, a, L, c->st);
+            }
             DstXArgs a; a.in = c->spec2; a.out = c->spec1;
             if (which == 2) { a.nlines = nlines; a.row0 = 0; a.row_step = 1; }
+            if (which == 3) {   // every level: the per-level fields as inputs, the spectra as outputs
+              a.nlev = c->L;
+              for (int k = 0; k < c->L; ++k) { a.lin[k] = c->s[k]; a.lout[k] = c->hat[k]; }
+            }
             return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, a, c->g, L, c->st);
-          }
-          DstYArgs a; a.a = c->spec1;
-          return dst_pass_y(c->py, c->g.nsx, c->g.nsx, YMODE_NONE, a, L, c->st);
-        };
-        if (time_it(c, run, &ms) != IB_OK) { cudaGetLastError(); continue; }
-        if (ms < best) { best = ms; bestL = L; }
+          };
+          if (time_it(c, run, &ms) != IB_OK) { cudaGetLastError(); continue; }
+          if (ms < best) { best = ms; bestL = L; }
+        }
       }
     }
     *out = bestL;
@@ -363,6 +371,8 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   // default launch shapes, then tuned by timing
   c->lx.B = 2; c->lx.NT = 160;
   c->lx_small.B = 1; c->lx_small.NT = 128;
+  c->lx_batch = c->lx;
+  c->lx_batch.narrow_scan = 1;   // untuned: the throughput-bound batched passes scan with one warp
   c->ly_none.B = 8; c->ly_none.NT = 160;
   c->tl.Mb = 8;
   c->use_fused = p.schur_mode != 2;
@@ -515,7 +525,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     a.nlev = L;
     for (int k = 0; k < L; ++k) { a.lin[k] = w[k]; a.lout[k] = c->hat[k]; }
     ProfScope ps(c, 0, pass_bytes(c, L, L));
-    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
   for (int k = L - 1; k >= 0; --k) {
     double* F = c->hat[k];
@@ -534,7 +544,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     a.nlev = L;
     for (int k = 0; k < L; ++k) { a.lin[k] = c->hat[k]; a.lout[k] = s[k]; }
     ProfScope ps(c, 0, pass_bytes(c, L, L));
-    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
   for (int k = L - 1; k >= 0; --k)
     if (all_curls || k == 0) RC(launch_curl(g, s[k], k == L - 1 ? c->zero_ring : c->ringv[k], qx[k], qy[k], st));
