@@ -199,7 +199,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)L * ns;                                 // per-level predictor right-hand sides
   dbl += (size_t)L * (2 * ns + nu + nv);                 // Schur scratch
   int tri_s = 0, tri_C = 0;
-  tri_chunking(g.n, &tri_s, &tri_C);
+  tri_chunking(g.n, g.nsx, &tri_s, &tri_C);
   size_t tri_n = tri_table_doubles(g.nsx, tri_s, tri_C);
   dbl += (size_t)(2 + L) * tri_n;                        // tridiagonal tables
   dbl += 6 * ns + 2 * nu + 2 * nv;                       // work (+ ainv mode-space copy)

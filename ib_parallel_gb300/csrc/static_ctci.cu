@@ -56,7 +56,7 @@ static size_t needed(int m, int n) {
   size_t plan = dst_plan_table_doubles(m - 1);
   if (plan == 0) return 0;
   int s = 0, C = 0;
-  tri_chunking(n, &s, &C);
+  tri_chunking(n, m - 1, &s, &C);
   return align4((size_t)(m - 1) * (n - 1)) + align4(plan) + align4(tri_table_doubles(m - 1, s, C));
 }
 

@@ -1,4 +1,5 @@
 // Chunked per-mode tridiagonal solver (see tri.cuh).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -6,15 +7,28 @@
 
 namespace ib {
 
-void tri_chunking(int n, int* s, int* C) {
-  // chunk period d = s+1 divides n; pick the divisor closest to sqrt(n), at most 32 chunks
-  int best = n, bestd = 1;
+void tri_chunking(int n, int nx, int* s, int* C) {
+  // The chunk period d = s+1 divides n, at most 32 chunks.  Every FP64 warp instruction holds
+  // its SM sub-partition's FP64 pipe for the same time whatever its active lanes, so the cost
+  // of one solve is the FP64 instructions of one chunk thread (about 5 per chunk row and one
+  // per interface) times the warps a sub-partition runs, minimised over the launch shapes
+  // (Mb modes x C chunks per CTA, Mb a power of two) the tuner can pick.
+  constexpr int kSMs = 152;   // GB300: 4 sub-partitions each
+  long long best = -1;
+  int bestd = n;
   for (int d = 2; d <= n; ++d) {
     if (n % d) continue;
-    int c = n / d;
+    const int c = n / d;
     if (c > 32) continue;
-    int score = std::abs(d * d - n);
-    if (score < best) { best = score; bestd = d; }
+    const long long per = 5LL * (d - 1) + c;
+    for (int Mb = 1; Mb <= 32; Mb *= 2) {
+      if (Mb * c > 1024) break;
+      const long long wpc = (Mb * c + 31) / 32;                 // warps per CTA
+      const long long ncta = (nx + Mb - 1) / Mb;
+      const long long mult = ((ncta + kSMs - 1) / kSMs * wpc + 3) / 4;   // warps per sub-partition
+      const long long cost = per * mult;
+      if (best < 0 || cost < best || (cost == best && d > bestd)) { best = cost; bestd = d; }
+    }
   }
   *s = bestd - 1;
   *C = n / bestd;
@@ -27,7 +41,7 @@ size_t tri_table_doubles(int nx, int s, int C) {
 
 int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, double* dev) {
   int s = 0, C = 0;
-  tri_chunking(ny + 1, &s, &C);
+  tri_chunking(ny + 1, nx, &s, &C);
   op->nx = nx; op->ny = ny; op->s = s; op->C = C; op->sigma = sigma;
   const int m = C > 1 ? C - 1 : 1;
   const size_t S = (size_t)s * nx, R = (size_t)m * m * nx;
@@ -187,6 +201,117 @@ __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld,
   }
 }
 
+// The same solve with each thread's chunk in registers (S = op.s known at compile time): the
+// chunk rows and the interface row above are loaded straight from F (all loads in flight at
+// once), the thread's row of the interface inverse is prefetched into registers, only the
+// pivot and response tables (shared by a mode's chunks) are staged in shared memory, and the
+// result is stored straight to U.  Same arithmetic as k_tri.  In place allowed: a thread
+// writes only the rows it read, after the CTA's barriers.
+constexpr int kTriMaxM = 31;   // interfaces (C-1) the register prefetch holds
+template <int S>
+__global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb) {
+  extern __shared__ double sm[];
+  const int C = op.C, d = S + 1, nx = op.nx;
+  const int m = C > 1 ? C - 1 : 1;
+  double* t_inv = sm;                      // S x Mb
+  double* t_sinv = t_inv + S * Mb;
+  double* t_gL = t_sinv + S * Mb;
+  double* pfirst = t_gL + S * Mb;          // C x Mb
+  double* plast = pfirst + C * Mb;
+  double* hv = plast + C * Mb;             // (C+1) x Mb
+  double* yv = hv + (C + 1) * Mb;          // (C+1) x Mb
+  const int k0 = blockIdx.x * Mb, nthr = blockDim.x;
+  const int t = threadIdx.x, kl = t % Mb, c = t / Mb;
+  const int k = min(k0 + kl, nx - 1);
+  const bool chunk = c < C, store = chunk && k0 + kl < nx;
+  const int r0 = c * d;
+  double f[S];
+#pragma unroll
+  for (int j = 0; j < S; ++j) f[j] = chunk ? F[(size_t)(r0 + j) * ld + k] : 0.0;
+  const double fi = (chunk && c >= 1) ? F[(size_t)(r0 - 1) * ld + k] : 0.0;
+  double rr[kTriMaxM];
+#pragma unroll
+  for (int j = 0; j < kTriMaxM; ++j)
+    rr[j] = (chunk && c >= 1 && j < m) ? __ldg(op.rinv + ((size_t)(c - 1) * m + j) * nx + k) : 0.0;
+  for (int q = t; q < 3 * S * Mb; q += nthr) {
+    const int row = q / Mb, kk = q - row * Mb;
+    t_inv[q] = __ldg(op.inv + (size_t)row * nx + min(k0 + kk, nx - 1));
+  }
+  __syncthreads();
+  // phase 1: chunk solve with zero ends
+  if (chunk) {
+    double dp = 0.0;
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      dp = fma(t_sinv[j * Mb + kl], f[j], t_inv[j * Mb + kl] * dp);
+      f[j] = dp;
+    }
+    plast[c * Mb + kl] = dp;
+    double u = dp;
+#pragma unroll
+    for (int j = S - 2; j >= 0; --j) {
+      u = fma(t_inv[j * Mb + kl], u, f[j]);
+      f[j] = u;
+    }
+    pfirst[c * Mb + kl] = u;
+  }
+  __syncthreads();
+  // phase 2a: right-hand side of interface c
+  if (chunk && c >= 1) hv[c * Mb + kl] = fma(op.sigma, fi, plast[(c - 1) * Mb + kl] + pfirst[c * Mb + kl]);
+  __syncthreads();
+  // phase 2b: interface value c
+  if (chunk) {
+    if (c >= 1) {
+      const double* hh = hv + Mb + kl;
+      double y0 = 0.0, y1 = 0.0;
+#pragma unroll
+      for (int j = 0; j + 1 < kTriMaxM; j += 2) {
+        if (j + 1 < m) {
+          y0 = fma(rr[j], hh[j * Mb], y0);
+          y1 = fma(rr[j + 1], hh[(j + 1) * Mb], y1);
+        } else if (j < m) {
+          y0 = fma(rr[j], hh[j * Mb], y0);
+        }
+      }
+      if ((kTriMaxM & 1) && m == kTriMaxM) y0 = fma(rr[kTriMaxM - 1], hh[(kTriMaxM - 1) * Mb], y0);
+      yv[c * Mb + kl] = y0 + y1;
+    } else {
+      yv[kl] = 0.0;
+      yv[C * Mb + kl] = 0.0;
+    }
+  }
+  __syncthreads();
+  // phase 3: interface responses, straight to U
+  if (store) {
+    const double yl = yv[c * Mb + kl], yr = yv[(c + 1) * Mb + kl];
+    double* dst = U + k;
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      double u = f[j];
+      u = fma(yl, t_gL[j * Mb + kl], u);
+      u = fma(yr, t_gL[(S - 1 - j) * Mb + kl], u);
+      dst[(size_t)(r0 + j) * ld] = u;
+    }
+    if (c >= 1) dst[(size_t)(r0 - 1) * ld] = yl;
+  }
+}
+
+static size_t tri_reg_smem(const TriOp& op, int Mb) {
+  return sizeof(double) * (size_t)Mb * (3 * (size_t)op.s + 2 * (size_t)op.C + 2 * ((size_t)op.C + 1));
+}
+
+template <int S>
+static int launch_tri_reg(const TriOp& op, const double* F, double* U, int ld, int Mb, int threads, cudaStream_t st) {
+  const size_t smem = tri_reg_smem(op, Mb);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_tri_reg<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return IB_ERR_CUDA;
+  count_launch();
+  k_tri_reg<S><<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
 size_t tri_smem(const TriOp& op, int Mb) {
   const size_t m = op.C > 1 ? (size_t)(op.C - 1) : 0;
   return sizeof(double) * (size_t)Mb * ((size_t)op.ny + 3 * (size_t)op.s + m * m + 2 * (size_t)op.C + 2 * ((size_t)op.C + 1));
@@ -197,6 +322,20 @@ int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaun
   int threads = Mb * op.C;
   threads = ((threads + 31) / 32) * 32;
   if (threads > 1024) { Mb = 1024 / op.C; threads = ((Mb * op.C + 31) / 32) * 32; }
+  if (op.C - 1 <= kTriMaxM && op.C <= 256) {
+    // at most 256 threads (the register-resident chunk needs the registers)
+    const int Mr = std::max(1, std::min(Mb, 256 / op.C));
+    const int tr = ((Mr * op.C + 31) / 32) * 32;
+    switch (op.s) {
+#define IB_TRI_REG(SS) \
+      case SS: return launch_tri_reg<SS>(op, F, U, ld, Mr, tr, st);
+      IB_TRI_REG(1) IB_TRI_REG(2) IB_TRI_REG(3) IB_TRI_REG(4) IB_TRI_REG(5) IB_TRI_REG(6) IB_TRI_REG(7)
+      IB_TRI_REG(8) IB_TRI_REG(9) IB_TRI_REG(11) IB_TRI_REG(12) IB_TRI_REG(14) IB_TRI_REG(15) IB_TRI_REG(19)
+      IB_TRI_REG(23) IB_TRI_REG(24) IB_TRI_REG(29) IB_TRI_REG(31) IB_TRI_REG(39)
+#undef IB_TRI_REG
+      default: break;
+    }
+  }
   size_t smem = tri_smem(op, Mb);
   if (smem > 48 * 1024) {
     if (cudaFuncSetAttribute(k_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -38,8 +38,8 @@ struct TriLaunch {
   int Mb = 8;             // modes per CTA
 };
 
-// Chunking for ny = n-1 rows (n divisible by 4): C*(s+1) = n.
-void tri_chunking(int n, int* s, int* C);
+// Chunking for ny = n-1 rows (n divisible by 4) and nx modes: C*(s+1) = n.
+void tri_chunking(int n, int nx, int* s, int* C);
 // Tables for shifts a_k = 2 + shift_k (k = 0..nx-1), uploaded into caller-provided
 // device memory of tri_table_doubles() doubles.
 size_t tri_table_doubles(int nx, int s, int C);

@@ -21,7 +21,8 @@ def _rand(rng, shape):
     return rng.standard_normal(shape)
 
 
-@pytest.mark.parametrize("mn", [(64, 32), (60, 40), (96, 48), (120, 36), (40, 200)])
+# the sizes cover the tridiagonal solve's chunk lengths 1, 2, 3, 7 and (800 x 400) 24
+@pytest.mark.parametrize("mn", [(64, 32), (60, 40), (96, 48), (120, 36), (40, 200), (800, 400)])
 def test_dst_sizes(mn):
     m, n = mn
     kw = dict(SMALL, m=m, n=n, mgridlev=2)
@@ -29,7 +30,9 @@ def test_dst_sizes(mn):
     rng = np.random.default_rng(m * 1000 + n)
     x = _rand(rng, (n - 1, m - 1))
     assert rel(g.dst(x), o.dst(x)) < TOL_OP
-    assert rel(g.ctci(x), o.ctci(x)) < TOL_OP
+    # ctci's lowest modes have condition ~ (2n/pi)^2, and the oracle applies the y direction by
+    # a DST pair where the device solves per-mode tridiagonal systems: round-off grows with n^2
+    assert rel(g.ctci(x), o.ctci(x)) < TOL_OP * max(1.0, (n / 100.0) ** 2)
     assert rel(g.ainv(x), o.ainv(x)) < TOL_OP
     g.close()
 
