@@ -117,6 +117,7 @@ struct Ctx {
   // row treatments of the Schur operator's partial transforms (per vertex row)
   unsigned char *rm_top = nullptr, *rm_coarse = nullptr, *rm_fine = nullptr, *rm_ring2 = nullptr;
   double* wmat = nullptr;          // DST-I matrix of the x transform ((m-1) x (m-1))
+  double* sk2 = nullptr;           // 2 sin(pi k/m), k = 1..m-1 (closed-form boundary-row modes)
   int2* ring_pts = nullptr;        // (row, col) points get_bc reads
   int n_ring_pts = 0;
   int* edge_rows = nullptr;        // rows 0 and n-2 (apply_bc's bottom and top rows)

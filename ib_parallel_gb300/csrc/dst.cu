@@ -476,8 +476,19 @@ __global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, con
   int2 rc = pts[gw];
   const double* sr = spec + (size_t)rc.x * ld;
   const double* wc = W + (size_t)rc.y * N;
-  double acc = 0.0;
-  for (int k = lane; k < N; k += 32) acc = fma(sr[k], wc[k], acc);
+  // four accumulators (k = lane + 32(4t + a)) keep four loads per operand in flight
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int k = lane;
+  for (; k + 96 < N; k += 128) {
+    a0 = fma(sr[k], wc[k], a0);
+    a1 = fma(sr[k + 32], wc[k + 32], a1);
+    a2 = fma(sr[k + 64], wc[k + 64], a2);
+    a3 = fma(sr[k + 96], wc[k + 96], a3);
+  }
+  if (k < N) a0 = fma(sr[k], wc[k], a0);
+  if (k + 32 < N) a1 = fma(sr[k + 32], wc[k + 32], a1);
+  if (k + 64 < N) a2 = fma(sr[k + 64], wc[k + 64], a2);
+  double acc = (a0 + a1) + (a2 + a3);
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) out[(size_t)rc.x * ld + rc.y] = acc;
 }
@@ -513,27 +524,36 @@ __global__ void k_dst_ring_rows(int N, GridDims g, const double* __restrict__ ri
 // factor 1 on a zero field).  The first nEdge CTAs take the two edge rows 0 and n-2, whose
 // boundary field is a full row: both rows are built once per CTA in shared memory and one warp
 // per mode k reads row k of the (symmetric) DST matrix once for both dot products.  The other
-// CTAs take the interior rows, whose boundary field is zero except x_1 = ring(left) and
-// x_N = ring(right): Y_k = 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N).  In place allowed.
+// CTAs take kRowsPerCta interior rows each, whose boundary field is zero except
+// x_1 = ring(left) and x_N = ring(right): Y_k = 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N), one FMA per
+// output from the row's two sums and the tabulated 2 sin(pi k/M).  In place allowed.
+constexpr int kRowsPerCta = 8;
 __global__ void __launch_bounds__(256) k_dst_bc_modes(DstDev pl, GridDims g, const double* __restrict__ ring,
-                                                      const double* __restrict__ W,
+                                                      const double* __restrict__ W, const double* __restrict__ sk2,
                                                       const double* __restrict__ post_add, double post_scale,
-                                                      double* __restrict__ out, int nEdge, int nColBlk) {
+                                                      double* __restrict__ out, int nEdge) {
   const int N = pl.N;
   if ((int)blockIdx.x >= nEdge) {
-    const int b = blockIdx.x - nEdge;
-    const int r = b / nColBlk + 1;
-    const int k = (b - (r - 1) * nColBlk) * blockDim.x + threadIdx.x;
-    if (k >= N || r >= g.nsy - 1) return;
-    const int J = r + 2;
-    const double x1 = 0.0 + ring[g.left + J - 1];
-    const double xn = 0.0 + ring[g.right + J - 1];
-    const int kk = k + 1;
-    const double sk = __ldg(&pl.sn[kk <= pl.P ? kk : pl.M - kk]);
-    double v = 2.0 * sk * ((kk & 1) ? x1 + xn : x1 - xn);
-    const size_t o = (size_t)r * g.nsx + k;
-    if (post_add) v = fma(post_scale, post_add[o], v);
-    out[o] = v;
+    __shared__ double s_sum[kRowsPerCta][2];   // x_1 + x_N, x_1 - x_N per row
+    const int r0 = 1 + ((int)blockIdx.x - nEdge) * kRowsPerCta;
+    const int nr = min(kRowsPerCta, g.nsy - 1 - r0);
+    if ((int)threadIdx.x < nr) {
+      const int J = r0 + (int)threadIdx.x + 2;
+      const double x1 = 0.0 + ring[g.left + J - 1];
+      const double xn = 0.0 + ring[g.right + J - 1];
+      s_sum[threadIdx.x][0] = x1 + xn;
+      s_sum[threadIdx.x][1] = x1 - xn;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+      const double a = __ldg(&sk2[k]);
+      const int par = (k & 1);   // mode kk = k+1 odd <=> k even
+      for (int i = 0; i < nr; ++i) {
+        const size_t o = (size_t)(r0 + i) * g.nsx + k;
+        const double sv = s_sum[i][par];
+        out[o] = post_add ? fma(a, sv, post_scale * post_add[o]) : a * sv;
+      }
+    }
     return;
   }
   extern __shared__ double bc[];   // 2 x N: rows 0 and n-2 of the boundary field
@@ -570,19 +590,31 @@ __global__ void __launch_bounds__(256) k_dst_bc_modes(DstDev pl, GridDims g, con
   }
 }
 
-int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W,
+int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W, const double* sk2,
                    const double* post_add, double post_scale, double* out, cudaStream_t st) {
   const int N = px.N;
   const size_t smem = 2 * sizeof(double) * (size_t)N;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_dst_bc_modes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return IB_ERR_CUDA;
-  const int nEdge = cdiv(N, 8), nColBlk = cdiv(N, 256);
-  const int nblk = nEdge + nColBlk * std::max(0, g.nsy - 2);
+  const int nEdge = cdiv(N, 8);
+  const int nblk = nEdge + cdiv(std::max(0, g.nsy - 2), kRowsPerCta);
   DstDev d = to_dev(px);
   count_launch();
-  k_dst_bc_modes<<<nblk, 256, smem, st>>>(d, g, ring, W, post_add, post_scale, out, nEdge, nColBlk);
+  k_dst_bc_modes<<<nblk, 256, smem, st>>>(d, g, ring, W, sk2, post_add, post_scale, out, nEdge);
   IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int dst_sin2_table(const DstPlan& px, double* dev_out) {
+  const long double PI_L = 3.141592653589793238462643383279502884L;
+  std::vector<double> v(px.N);
+  for (int k = 1; k <= px.N; ++k) {
+    const int kk = k <= px.P ? k : px.M - k;   // the plan's sin table entry the transform uses
+    const double sk = (double)sinl(PI_L * (long double)kk / (long double)px.M);
+    v[k - 1] = 2.0 * sk;
+  }
+  IB_CUDA_CHECK(cudaMemcpy(dev_out, v.data(), 8 * v.size(), cudaMemcpyHostToDevice));
   return IB_OK;
 }
 

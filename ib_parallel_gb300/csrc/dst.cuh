@@ -107,9 +107,12 @@ int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, co
                     const double* W, const double* post_add, double post_scale, double* out, cudaStream_t st);
 // out = post_scale*post_add + S_x(apply_bc(ring)) on every row (factor 1, zero field): the two
 // edge rows by dot products with W, the interior rows in closed form
-// 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N).  In place allowed (out == post_add).
-int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W,
+// 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) from sk2[k-1] = 2 sin(pi k/M) (dst_sin2_table).  In place
+// allowed (out == post_add).
+int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W, const double* sk2,
                    const double* post_add, double post_scale, double* out, cudaStream_t st);
+// sk2[k-1] = 2 sin(pi k/M), k = 1..N, into N doubles of device memory.
+int dst_sin2_table(const DstPlan& px, double* dev_out);
 size_t dst_smem_y(const DstPlan& p, int B, DstYMode mode);
 
 }  // namespace ib

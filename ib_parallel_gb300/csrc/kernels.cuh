@@ -18,6 +18,14 @@ struct RingBatch {
   double* dst[kMaxLevels] = {};
 };
 int launch_get_bc_levels(const GridDims& g, const RingBatch& rb, int nlev, double fac, cudaStream_t st);
+// curl of every level in one launch: level l from s[l] with ghosts from the ring sbc[l]
+struct CurlBatch {
+  const double* s[kMaxLevels] = {};
+  const double* sbc[kMaxLevels] = {};
+  double* qx[kMaxLevels] = {};
+  double* qy[kMaxLevels] = {};
+};
+int launch_curl_levels(const GridDims& g, const CurlBatch& cb, int nlev, cudaStream_t st);
 int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st);
 int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st);
 int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st);

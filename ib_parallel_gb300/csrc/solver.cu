@@ -35,16 +35,21 @@ static double pass_bytes(const Ctx* c, int nin, int nout) { return 8.0 * c->g.ns
 // ------------------------------------------------------------- tuning
 template <typename F>
 static int time_it(Ctx* c, F run, float* ms) {
+  // the least of three trials of three runs each, after a warm-up run: one slow trial (a clock
+  // ramp, another context's work) must not decide a launch shape the whole run keeps
   cudaEvent_t e0, e1;
   IB_CUDA_CHECK(cudaEventCreate(&e0));
   IB_CUDA_CHECK(cudaEventCreate(&e1));
   int rc = run();
-  if (rc == IB_OK) {
+  *ms = 1e30f;
+  for (int trial = 0; trial < 3 && rc == IB_OK; ++trial) {
     cudaEventRecord(e0, c->st);
     for (int r = 0; r < 3 && rc == IB_OK; ++r) rc = run();
     cudaEventRecord(e1, c->st);
     cudaEventSynchronize(e1);
-    cudaEventElapsedTime(ms, e0, e1);
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = std::min(*ms, t);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -204,6 +209,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)(2 + L) * tri_n;                        // tridiagonal tables
   dbl += 6 * ns + 2 * nu + 2 * nv;                       // work (+ ainv mode-space copy)
   dbl += (size_t)g.nsx * g.nsx + (size_t)g.nsy;          // DST matrix, row treatments
+  dbl += (size_t)g.nsx;                                  // 2 sin(pi k/m) table
   dbl += (size_t)g.m + g.n + 8;                          // get_bc points, edge rows
   dbl += (size_t)(L + 3) * nbc;                          // rings
   dbl += (size_t)L * ns + (size_t)L * nbc + 2 * L;       // per-level spectra and rings (vort2flux)
@@ -231,6 +237,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->spec1 = P.take<double>(ns); c->spec2 = P.take<double>(ns); c->rhs = P.take<double>(ns);
   c->rhsbc = P.take<double>(ns); c->vort = P.take<double>(ns); c->specY = P.take<double>(ns);
   c->wmat = P.take<double>((size_t)g.nsx * g.nsx);
+  c->sk2 = P.take<double>(g.nsx);
   c->ring_pts = P.take<int2>((size_t)g.m + g.n + 8);
   c->edge_rows = P.take<int>(2);
   c->rm_top = P.take<unsigned char>(g.nsy); c->rm_coarse = P.take<unsigned char>(g.nsy);
@@ -334,6 +341,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     int er[2] = {0, g.nsy - 1};
     IB_CUDA_CHECK(cudaMemcpy(c->edge_rows, er, sizeof(er), cudaMemcpyHostToDevice));
     int rc3 = dst_matrix_table(c->px, c->wmat);
+    if (rc3 == IB_OK) rc3 = dst_sin2_table(c->px, c->sk2);
     if (rc3 != IB_OK) { *msg = "DST matrix upload failed"; ctx_destroy(c); return rc3; }
   }
 
@@ -531,7 +539,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     double* F = c->hat[k];
     if (k < L - 1) {
       // boundary terms from the ring of level k (get_bc of level k+1), apply_bc with fac 1
-      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, F, 1.0, F, st));
+      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, F, 1.0, F, st));
     }
     {
       ProfScope ps(c, 1, pass_bytes(c, 1, 1));
@@ -546,9 +554,15 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     ProfScope ps(c, 0, pass_bytes(c, L, L));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
-  for (int k = L - 1; k >= 0; --k)
-    if (all_curls || k == 0) RC(launch_curl(g, s[k], k == L - 1 ? c->zero_ring : c->ringv[k], qx[k], qy[k], st));
-  return IB_OK;
+  if (!all_curls) return launch_curl(g, s[0], L == 1 ? c->zero_ring : c->ringv[0], qx[0], qy[0], st);
+  CurlBatch cb;
+  for (int k = 0; k < L; ++k) {
+    cb.s[k] = s[k];
+    cb.sbc[k] = k == L - 1 ? c->zero_ring : c->ringv[k];
+    cb.qx[k] = qx[k];
+    cb.qy[k] = qy[k];
+  }
+  return launch_curl_levels(g, cb, L, st);
 }
 
 // s on the next finer level's boundary only: the points get_bc reads, each an inverse x
@@ -621,7 +635,7 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
     // S_x(vort1 + apply_bc(ring0)) = 2m Y + transform of the boundary terms: the two full
     // boundary rows by dot products, the others in closed form (two nonzero samples)
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-    RC(dst_x_bc_modes(c->px, g, ring0, c->wmat, c->specY, 2.0 * g.m, c->spec1, st));
+    RC(dst_x_bc_modes(c->px, g, ring0, c->wmat, c->sk2, c->specY, 2.0 * g.m, c->spec1, st));
   }
   mark(5);
   {

@@ -69,6 +69,22 @@ __global__ void k_curl(GridDims g, const double* __restrict__ s, const double* _
   }
 }
 
+// The same for every level at once (blockIdx.y = level).
+__global__ void k_curl_levels(GridDims g, CurlBatch cb) {
+  const int l = blockIdx.y;
+  const double* __restrict__ s = cb.s[l];
+  const double* __restrict__ sbc = cb.sbc[l];
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < g.nu) {
+    int i = t % g.nux + 1, j = t / g.nux + 1;
+    cb.qx[l][t] = ghost_vertex(s, sbc, g, i, j + 1) - ghost_vertex(s, sbc, g, i, j);
+  } else if (t < g.nu + g.nv) {
+    int u = t - g.nu;
+    int i = u % g.nvx + 1, j = u / g.nvx + 1;
+    cb.qy[l][u] = ghost_vertex(s, sbc, g, i, j) - ghost_vertex(s, sbc, g, i + 1, j);
+  }
+}
+
 // ------------------------------------------------------------- coarsify
 // operators_fluid.F90:381-419 with grid.F90:1061-1087: the full-weighting sum
 // at odd fine points I=3..m-1, J=3..n-1 overwrites coarse point
@@ -173,6 +189,12 @@ int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vo
 int launch_curl(const GridDims& g, const double* s, const double* sbc, double* qx, double* qy, cudaStream_t st) {
   count_launch();
   k_curl<<<blocks(g.nu + g.nv), 256, 0, st>>>(g, s, sbc, qx, qy);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_curl_levels(const GridDims& g, const CurlBatch& cb, int nlev, cudaStream_t st) {
+  if (nlev < 1 || nlev > kMaxLevels) return IB_ERR_ARG;
+  count_launch();
+  k_curl_levels<<<dim3(blocks(g.nu + g.nv), nlev), 256, 0, st>>>(g, cb);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_coarsify(const GridDims& g, const double* fine, double* coarse, cudaStream_t st) {
