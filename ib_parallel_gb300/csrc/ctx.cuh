@@ -89,11 +89,6 @@ struct Ctx {
   int L = 0;
   double delta = 0, normalize = 0;
   cudaStream_t st = nullptr;
-  // second stream of the predictor: the levels' nonlinear terms run on it while the
-  // coarse-to-fine chain of solves runs on st (one fork event, one event per level)
-  cudaStream_t st_aux = nullptr;
-  cudaEvent_t ev_fork = nullptr;
-  std::vector<cudaEvent_t> ev_lv;
   DevPool pool;
 
   DstPlan px, py;

@@ -331,8 +331,26 @@ __device__ void dst_lines(const DstDev& pl, int B, double* xb, int ldx, double2*
 }
 
 // ------------------------------------------------------------- x pass
+// The pre-op operands of one CTA's level (the top-level fields, or level blockIdx.y of a batch).
+struct XPre {
+  const double *in2, *in3, *in4, *ring;
+  double* save;
+  double ca, cb, alpha, beta, fac;
+};
+__device__ __forceinline__ XPre x_pre(const DstXArgs& a, int l, bool batch) {
+  XPre p;
+  if (batch) {
+    p.in2 = a.lin2[l]; p.in3 = nullptr; p.in4 = a.lin4[l]; p.ring = a.lring[l]; p.save = a.lsave[l];
+    p.ca = a.lca[l]; p.cb = a.lcb[l]; p.alpha = a.lalpha[l]; p.beta = a.lbeta[l]; p.fac = a.lfac[l];
+  } else {
+    p.in2 = a.in2; p.in3 = a.in3; p.in4 = a.in4; p.ring = a.ring; p.save = a.save;
+    p.ca = a.ca; p.cb = a.cb; p.alpha = a.alpha; p.beta = a.beta; p.fac = a.fac;
+  }
+  return p;
+}
+
 template <int PRE>
-__device__ __forceinline__ double x_load(const DstXArgs& a, const double* __restrict__ in, const GridDims& g, int row,
+__device__ __forceinline__ double x_load(const XPre& a, const double* __restrict__ in, const GridDims& g, int row,
                                          int j, int nrows, int N, int ld) {
   size_t idx = (size_t)row * ld + j;
   double v = 0.0;
@@ -351,20 +369,13 @@ __device__ __forceinline__ double x_load(const DstXArgs& a, const double* __rest
     } else {
       const int I = j + 2, J = row + 2;
       if (I == 2 || I == g.m || J == 2 || J == g.n) {
-        // rhsbc = 0; apply_bc(rhsbc, lastbc, f); apply_bc(rhsbc, 0.25 get_bc(coarse), f)
+        // rhsbc = 0; apply_bc(rhsbc, lastbc, f)
         double x = 0.0;
         const double* ra = a.ring;
         if (I == 2) x = x + a.fac * ra[g.left + J - 1];
         if (I == g.m) x = x + a.fac * ra[g.right + J - 1];
         if (J == 2) x = x + a.fac * ra[g.bottom + I - 1];
         if (J == g.n) x = x + a.fac * ra[g.top + I - 1];
-        if (a.coarse) {
-          const double* cs = a.coarse;
-          if (I == 2) x = x + a.fac * (ring_value(cs, g, g.left + J - 1) * 0.25);
-          if (I == g.m) x = x + a.fac * (ring_value(cs, g, g.right + J - 1) * 0.25);
-          if (J == 2) x = x + a.fac * (ring_value(cs, g, g.bottom + I - 1) * 0.25);
-          if (J == g.n) x = x + a.fac * (ring_value(cs, g, g.top + I - 1) * 0.25);
-        }
         base = base + x;
       }
     }
@@ -392,6 +403,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
                                                GridDims g, int B, int narrow_scan) {
   const double* ain = a.nlev ? a.lin[blockIdx.y] : a.in;
   double* aout = a.nlev ? a.lout[blockIdx.y] : a.out;
+  const XPre pre = x_pre(a, blockIdx.y, PRE == PRE_PRED && a.nlev > 0);
   extern __shared__ double2 smem2[];
   __shared__ int s_mode[64];
   __shared__ int s_any;
@@ -429,7 +441,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
         v[u] = 0.0;
         if (it < tot) {
           int b = pl.fd_N.div(it), j = it - b * N;
-          if (s_mode[b] == ROW_FFT) v[u] = x_load<PRE>(a, ain, g, s_row[b], j, nrows, N, ld);
+          if (s_mode[b] == ROW_FFT) v[u] = x_load<PRE>(pre, ain, g, s_row[b], j, nrows, N, ld);
         }
       }
 #pragma unroll
@@ -454,8 +466,8 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
     if (mode == ROW_FFT) {
       v = xb[b * ldx + j];
     } else if (mode == ROW_EDGES) {
-      double x1 = x_load<PRE>(a, ain, g, row, 0, nrows, N, ld);
-      double xn = x_load<PRE>(a, ain, g, row, N - 1, nrows, N, ld);
+      double x1 = x_load<PRE>(pre, ain, g, row, 0, nrows, N, ld);
+      double xn = x_load<PRE>(pre, ain, g, row, N - 1, nrows, N, ld);
       int k = j + 1;
       double sk = __ldg(&pl.sn[k <= pl.P ? k : pl.M - k]);
       v = 2.0 * sk * ((k & 1) ? x1 + xn : x1 - xn);
@@ -692,7 +704,7 @@ static int launch_cfg(K kern, size_t smem) {
 
 int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs& a, const GridDims& g,
                const DstLaunch& L, cudaStream_t st) {
-  if (a.nlev < 0 || a.nlev > kMaxBatch || (a.nlev && pre != PRE_COPY)) return IB_ERR_ARG;
+  if (a.nlev < 0 || a.nlev > kMaxBatch || (a.nlev && pre != PRE_COPY && pre != PRE_PRED)) return IB_ERR_ARG;
   DstDev d = to_dev(px);
   size_t smem = dst_smem_x(px, L.B);
   dim3 grid(cdiv(a.nlines ? a.nlines : nrows, L.B), a.nlev ? a.nlev : 1);

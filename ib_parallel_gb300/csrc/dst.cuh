@@ -55,9 +55,7 @@ struct DstXArgs {
   double alpha = 0.0, beta = 0.0;  // PRE_PRED: + alpha*w + beta*(sum of the 4 neighbours of w)
   const double* ring = nullptr;  // PRE_APPLYBC boundary ring; PRE_PRED without in3: first rhsbc ring
   double fac = 1.0;              // PRE_APPLYBC factor; PRE_PRED without in3: rhsbc factor
-  // PRE_PRED without in3: rhsbc (timestepper.F90:184-189) is formed on the fly from `ring` and
-  // the boundary ring 0.25*get_bc(coarse) of the next coarser level's field (none if null)
-  const double* coarse = nullptr;
+  // PRE_PRED without in3: rhsbc (timestepper.F90:184-189) is formed on the fly from `ring`
   double* save = nullptr;        // PRE_PRED: receives a copy of `in` (may alias in2)
   double* out = nullptr;         // nlines rows, pitch ld
   // optional output post-op: out = DST(row) + post_scale * post_add
@@ -69,11 +67,18 @@ struct DstXArgs {
   const int* rowrange = nullptr;
   // optional strided row subset: line i is row row0 + i*row_step, i < nlines (0: all rows)
   int nlines = 0, row0 = 0, row_step = 0;
-  // optional batch over grid levels (PRE_COPY only): level l (blockIdx.y) reads lin[l] and
-  // writes lout[l], each a full field of pitch ld; in/out are then unused
+  // optional batch over grid levels (PRE_COPY, PRE_PRED): level l (blockIdx.y) reads lin[l] and
+  // writes lout[l], each a full field of pitch ld; in/out are then unused.  PRE_PRED takes every
+  // other operand and coefficient of level l from the l-arrays below.
   int nlev = 0;
   const double* lin[kMaxBatch] = {};
   double* lout[kMaxBatch] = {};
+  const double* lin2[kMaxBatch] = {};
+  const double* lin4[kMaxBatch] = {};
+  const double* lring[kMaxBatch] = {};
+  double* lsave[kMaxBatch] = {};
+  double lca[kMaxBatch] = {}, lcb[kMaxBatch] = {}, lalpha[kMaxBatch] = {}, lbeta[kMaxBatch] = {};
+  double lfac[kMaxBatch] = {};
 };
 
 // Per-row treatment in the x pass.  ROW_EDGES: the row (after the pre-op) is zero

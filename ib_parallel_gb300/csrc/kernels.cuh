@@ -26,6 +26,20 @@ struct CurlBatch {
   double* qy[kMaxLevels] = {};
 };
 int launch_curl_levels(const GridDims& g, const CurlBatch& cb, int nlev, cudaStream_t st);
+// nonlinear terms then rot of every level (two launches): level l's nonlinear terms of om[l]
+// (ghosts from the ring bc[l], fluxes q + q0) into the scratch nlx[l], nly[l], their rot into out[l]
+struct NlBatch {
+  const double* om[kMaxLevels] = {};
+  const double* bc[kMaxLevels] = {};
+  const double* qx[kMaxLevels] = {};
+  const double* q0x[kMaxLevels] = {};
+  const double* qy[kMaxLevels] = {};
+  const double* q0y[kMaxLevels] = {};
+  double* nlx[kMaxLevels] = {};
+  double* nly[kMaxLevels] = {};
+  double* out[kMaxLevels] = {};
+};
+int launch_nonlinear_rot_levels(const GridDims& g, const NlBatch& b, int nlev, cudaStream_t st);
 int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st);
 int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st);
 int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st);

@@ -151,13 +151,6 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete c; *msg = "stream creation failed"; return IB_ERR_CUDA;
   }
-  {
-    bool ok = cudaStreamCreateWithFlags(&c->st_aux, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) == cudaSuccess;
-    c->ev_lv.assign(L, nullptr);
-    for (int k = 0; k < L && ok; ++k) ok = cudaEventCreateWithFlags(&c->ev_lv[k], cudaEventDisableTiming) == cudaSuccess;
-    if (!ok) { *msg = "stream or event creation failed"; ctx_destroy(c); return IB_ERR_CUDA; }
-  }
   int rc = dst_plan_create(&c->px, g.nsx);
   if (rc == IB_OK) rc = dst_plan_create(&c->py, g.nsy);
   if (rc != IB_OK) { *msg = "unsupported DST size (m, n must be 2^a 3^b 5^c)"; ctx_destroy(c); return rc; }
@@ -416,11 +409,6 @@ void ctx_destroy(Ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->stage_ev)
     if (e) cudaEventDestroy(e);
-  if (c->st_aux) cudaStreamSynchronize(c->st_aux);
-  for (auto& e : c->ev_lv)
-    if (e) cudaEventDestroy(e);
-  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->st_aux) cudaStreamDestroy(c->st_aux);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -496,21 +484,7 @@ int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs
   return spectral_solve(c, PRE_PRED, a, c->tri_pred[k], om);
 }
 
-// The time step's form of the predictor at level k: rhsbc (timestepper.F90:184-189) is formed
-// inside the x pass from lastbc and the coarser level's updated vorticity (null on the
-// coarsest level), and the pass also copies rhs into rhs_old (timestepper.F90:228).
-static int op_predictor_step(Ctx* c, int k, const double* rhs, double* rhs_old, const double* coarse) {
-  DstXArgs a;
-  a.in = rhs; a.in2 = rhs_old; a.save = rhs_old; a.in4 = c->omega[k];
-  a.ring = c->lastbc[k]; a.fac = c->vfac[k]; a.coarse = coarse;
-  a.ca = c->con1[k]; a.cb = c->con2[k];
-  double cv = c->cvis[k];
-  a.alpha = (1.0 - 4.0 * cv) / c->normalize;
-  a.beta = cv / c->normalize;
-  return spectral_solve(c, PRE_PRED, a, c->tri_pred[k], c->omega[k]);
-}
-
-static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring);
+static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring, double fac = 1.0);
 
 // vort2flux (operators_fluid.F90:237-377).  all_curls=false computes the fluxes
 // of the finest level only.
@@ -568,10 +542,10 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
 // s on the next finer level's boundary only: the points get_bc reads, each an inverse x
 // transform evaluated as a dot product (spread over all SMs), then get_bc
 // (operators_fluid.F90:475-535) into the ring.
-static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring) {
+static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring, double fac) {
   const GridDims& g = c->g;
   RC(dst_x_points(c->px, spec, g.nsx, c->ring_pts, c->n_ring_pts, c->wmat, s, c->st));
-  return launch_get_bc(g, s, 1.0, ring, c->st);
+  return launch_get_bc(g, s, fac, ring, c->st);
 }
 
 // The fluid part of the Schur operator between rot and E curl: the finest-level
@@ -977,6 +951,71 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
   return IB_OK;
 }
 
+// The predictor of every level (timestepper.F90:103-236), coarse to fine.  Level k's solve
+// depends on the coarser levels only through rhsbc's second ring, 0.25 get_bc(omega_{k+1})
+// of the updated coarser vorticity, which enters on the boundary rows and columns.  So the
+// nonlinear terms and the forward transforms (with the combine, the stencil, lastbc's part of
+// rhsbc, and the copy of rhs into rhs_old) run as batched launches over all levels; then,
+// coarse to fine in mode space, each level adds the transform of its second ring (closed form
+// on interior rows, dot products on the two edge rows), solves its per-mode tridiagonal
+// systems and evaluates the next finer level's ring from its modes at the points get_bc
+// reads; one batched inverse pass writes every level's vorticity.
+static int op_predict_levels(Ctx* c, bool seed_rhs_old) {
+  const GridDims& g = c->g;
+  const int L = c->L;
+  cudaStream_t st = c->st;
+  if (L > kMaxBatch) return IB_ERR_ARG;
+  // lastbc from the vorticity before the update (zero on the coarsest level)
+  RingBatch rb;
+  for (int k = 0; k < L; ++k) {
+    rb.src[k] = k < L - 1 ? c->omega[k + 1] : nullptr;
+    rb.dst[k] = c->lastbc[k];
+  }
+  RC(launch_get_bc_levels(g, rb, L, 0.25, st));
+  // nonlinear terms (operators_fluid.F90:553-587) and their rot, into rhs_lv
+  NlBatch nb;
+  for (int k = 0; k < L; ++k) {
+    nb.om[k] = c->omega[k]; nb.bc[k] = c->lastbc[k];
+    nb.qx[k] = c->qx[k]; nb.q0x[k] = c->q0x[k]; nb.qy[k] = c->qy[k]; nb.q0y[k] = c->q0y[k];
+    nb.nlx[k] = c->mv_qx[k]; nb.nly[k] = c->mv_qy[k];
+    nb.out[k] = c->rhs_lv[k];
+  }
+  RC(launch_nonlinear_rot_levels(g, nb, L, st));
+  if (seed_rhs_old)   // the first step: rhs_old = rhs
+    for (int k = 0; k < L; ++k)
+      IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs_lv[k], 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, st));
+  {
+    DstXArgs a;
+    a.nlev = L;
+    for (int k = 0; k < L; ++k) {
+      const double cv = c->cvis[k];
+      a.lin[k] = c->rhs_lv[k]; a.lin2[k] = c->rhs_old[k]; a.lsave[k] = c->rhs_old[k]; a.lin4[k] = c->omega[k];
+      a.lring[k] = c->lastbc[k]; a.lfac[k] = c->vfac[k];
+      a.lca[k] = c->con1[k]; a.lcb[k] = c->con2[k];
+      a.lalpha[k] = (1.0 - 4.0 * cv) / c->normalize;
+      a.lbeta[k] = cv / c->normalize;
+      a.lout[k] = c->hat[k];
+    }
+    ProfScope ps(c, 0, pass_bytes(c, 4 * L, L));
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_PRED, a, g, c->lx_batch, st));
+  }
+  for (int k = L - 1; k >= 0; --k) {
+    double* F = c->hat[k];
+    // the second ring: ringv[k] = vfac[k] * 0.25 get_bc(omega_{k+1}), left by level k+1
+    if (k < L - 1) RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, F, 1.0, F, st));
+    {
+      ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+      RC(tri_solve(c->tri_pred[k], F, F, g.nsx, c->tl, st));
+    }
+    if (k > 0) RC(ring_from_modes(c, F, c->spec2, c->ringv[k - 1], 0.25 * c->vfac[k - 1]));
+  }
+  DstXArgs b;
+  b.nlev = L;
+  for (int k = 0; k < L; ++k) { b.lin[k] = c->hat[k]; b.lout[k] = c->omega[k]; }
+  ProfScope ps(c, 0, pass_bytes(c, L, L));
+  return dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx_batch, st);
+}
+
 // timestepper.F90:18-556
 int op_advance(Ctx* c) {
   const GridDims& g = c->g;
@@ -989,35 +1028,7 @@ int op_advance(Ctx* c) {
   step_mark(c, 0);
   // boundary values of the previous step (timestepper.F90:103-117) and the predictor, coarse
   // to fine (timestepper.F90:121-236)
-  auto predictor = [&]() -> int {
-    // lastbc from the vorticity before the update, every level in one launch (zero on the
-    // coarsest level)
-    RingBatch rb;
-    for (int k = 0; k < L; ++k) {
-      rb.src[k] = k < L - 1 ? c->omega[k + 1] : nullptr;
-      rb.dst[k] = c->lastbc[k];
-    }
-    RC(launch_get_bc_levels(g, rb, L, 0.25, st));
-    // fork: the nonlinear right-hand sides of all levels (old vorticity and fluxes only) on
-    // the second stream, coarsest first, each level's solve waiting for its own
-    IB_CUDA_CHECK(cudaEventRecord(c->ev_fork, st));
-    IB_CUDA_CHECK(cudaStreamWaitEvent(c->st_aux, c->ev_fork, 0));
-    for (int k = L - 1; k >= 0; --k) {
-      RC(launch_nonlinear(g, c->omega[k], c->lastbc[k], c->qx[k], c->q0x[k], c->qy[k], c->q0y[k], c->nlx, c->nly,
-                          c->st_aux));
-      RC(launch_rot(g, c->nlx, c->nly, c->rhs_lv[k], c->st_aux));
-      if (it == 1)
-        IB_CUDA_CHECK(cudaMemcpyAsync(c->rhs_old[k], c->rhs_lv[k], 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice,
-                                      c->st_aux));
-      IB_CUDA_CHECK(cudaEventRecord(c->ev_lv[k], c->st_aux));
-    }
-    // the coarse-to-fine chain; waiting for level 0's event joins the second stream
-    for (int k = L - 1; k >= 0; --k) {
-      IB_CUDA_CHECK(cudaStreamWaitEvent(st, c->ev_lv[k], 0));
-      RC(op_predictor_step(c, k, c->rhs_lv[k], c->rhs_old[k], k < L - 1 ? c->omega[k + 1] : nullptr));
-    }
-    return IB_OK;
-  };
+  auto predictor = [&]() -> int { return op_predict_levels(c, it == 1); };
   if (it == 1) RC(predictor());   // the first step also seeds rhs_old
   else RC(run_phase(c, c->graph_pred, predictor));
   step_mark(c, 1);

@@ -7,11 +7,11 @@ namespace ib {
 // operators_fluid.F90:553-587.  omega ghosts come from the ring (bc); fluxes
 // outside the physical face grids are zero.  qx, qy are the total fluxes q+q0,
 // passed as q and q0 and summed on the fly.
-__global__ void k_nonlinear(GridDims g, const double* __restrict__ om, const double* __restrict__ bc,
-                            const double* __restrict__ qx, const double* __restrict__ q0x,
-                            const double* __restrict__ qy, const double* __restrict__ q0y,
-                            double* __restrict__ nlx, double* __restrict__ nly) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void nonlinear_at(const GridDims& g, int t, const double* __restrict__ om,
+                                             const double* __restrict__ bc, const double* __restrict__ qx,
+                                             const double* __restrict__ q0x, const double* __restrict__ qy,
+                                             const double* __restrict__ q0y, double* __restrict__ nlx,
+                                             double* __restrict__ nly) {
   auto QX = [&](int i, int j) -> double {  // i=1..m+1, j=0..n+1
     if (j < 1 || j > g.n) return 0.0;
     int idx = (j - 1) * g.nux + (i - 1);
@@ -40,11 +40,24 @@ __global__ void k_nonlinear(GridDims g, const double* __restrict__ om, const dou
   }
 }
 
+__global__ void k_nonlinear(GridDims g, const double* __restrict__ om, const double* __restrict__ bc,
+                            const double* __restrict__ qx, const double* __restrict__ q0x,
+                            const double* __restrict__ qy, const double* __restrict__ q0y,
+                            double* __restrict__ nlx, double* __restrict__ nly) {
+  nonlinear_at(g, blockIdx.x * blockDim.x + threadIdx.x, om, bc, qx, q0x, qy, q0y, nlx, nly);
+}
+
+// Every level at once (blockIdx.y = level).
+__global__ void k_nonlinear_levels(GridDims g, NlBatch b) {
+  const int l = blockIdx.y;
+  nonlinear_at(g, blockIdx.x * blockDim.x + threadIdx.x, b.om[l], b.bc[l], b.qx[l], b.q0x[l], b.qy[l], b.q0y[l],
+               b.nlx[l], b.nly[l]);
+}
+
 // ------------------------------------------------------------------ rot
 // rot_int + rot_bc (operators_fluid.F90:203-233): the transpose of curl.
-__global__ void k_rot(GridDims g, const double* __restrict__ hx, const double* __restrict__ hy,
-                      double* __restrict__ vort) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void rot_at(const GridDims& g, int t, const double* __restrict__ hx,
+                                       const double* __restrict__ hy, double* __restrict__ vort) {
   if (t >= g.ns) return;
   int I = t % g.nsx + 2, J = t / g.nsx + 2;
   double a = hy[(J - 1) * g.nvx + (I - 1)];
@@ -52,6 +65,15 @@ __global__ void k_rot(GridDims g, const double* __restrict__ hx, const double* _
   double c = hx[(J - 1) * g.nux + (I - 1)];
   double d = hx[(J - 2) * g.nux + (I - 1)];
   vort[t] = a - b - c + d;
+}
+__global__ void k_rot(GridDims g, const double* __restrict__ hx, const double* __restrict__ hy,
+                      double* __restrict__ vort) {
+  rot_at(g, blockIdx.x * blockDim.x + threadIdx.x, hx, hy, vort);
+}
+// Every level at once (blockIdx.y = level): level l from b.nlx[l], b.nly[l] into b.out[l].
+__global__ void k_rot_levels(GridDims g, NlBatch b) {
+  const int l = blockIdx.y;
+  rot_at(g, blockIdx.x * blockDim.x + threadIdx.x, b.nlx[l], b.nly[l], b.out[l]);
 }
 
 // ----------------------------------------------------------------- curl
@@ -179,6 +201,15 @@ int launch_nonlinear(const GridDims& g, const double* om, const double* bc, cons
                      const double* qy, const double* q0y, double* nlx, double* nly, cudaStream_t st) {
   count_launch();
   k_nonlinear<<<blocks(g.nu + g.nv), 256, 0, st>>>(g, om, bc, qx, q0x, qy, q0y, nlx, nly);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_nonlinear_rot_levels(const GridDims& g, const NlBatch& b, int nlev, cudaStream_t st) {
+  if (nlev < 1 || nlev > kMaxLevels) return IB_ERR_ARG;
+  count_launch();
+  k_nonlinear_levels<<<dim3(blocks(g.nu + g.nv), nlev), 256, 0, st>>>(g, b);
+  IB_CUDA_CHECK(cudaGetLastError());
+  count_launch();
+  k_rot_levels<<<dim3(blocks(g.ns), nlev), 256, 0, st>>>(g, b);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vort, cudaStream_t st) {
