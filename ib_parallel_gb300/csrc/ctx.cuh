@@ -153,6 +153,11 @@ struct Ctx {
   PhaseGraph graph_pred, graph_v2f, graph_corr;
   // FSI iteration: right-hand side, Schur assembly, update (redistribute, structure, weights)
   PhaseGraph graph_fsi_rhs, graph_fsi_asm, graph_fsi_upd;
+  // the FSI iterations of a step on the device (a while node around one iteration's common
+  // path; counters [0] iterations [1] Krylov iterations [2] operator products [3] band flag)
+  PhaseGraph graph_fsi_loop;
+  long long fsi_body_launches = 0;
+  int* fsi_cnt = nullptr;
   FusedPlan fused_plan;
   double* cholM = nullptr;         // nf x nf (num_stat)
   bool chol_ready = false;

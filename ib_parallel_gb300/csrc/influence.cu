@@ -329,6 +329,7 @@ int inf_build(Ctx* c) {
   // the captured FSI phases bake in the band's buffers and size
   drop_phase(&c->graph_fsi_asm);
   drop_phase(&c->graph_fsi_upd);
+  drop_phase(&c->graph_fsi_loop);
   I.active = false;
   if (I.nR == 0) return IB_ERR_STATE;
   const size_t nK = (size_t)I.nR * I.nR;

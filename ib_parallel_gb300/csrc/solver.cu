@@ -211,7 +211,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 4 * (size_t)nf + 2;
   if (p.num_stat) dbl += (size_t)nf * nf;
   dbl += 8 * stage_n;
-  size_t ints = 2 * (size_t)nf + 2 * (size_t)nf + 16 + 2 * (size_t)max_faces + 2 * 49 * (size_t)nf + 4 + 2;
+  size_t ints = 2 * (size_t)nf + 2 * (size_t)nf + 16 + 2 * (size_t)max_faces + 2 * 49 * (size_t)nf + 4 + 2 + 8;
   size_t bytes = dbl * 8 + ints * 4 + (size_t)nt * sizeof(TorsBody) + 256 * 400;
   if (cudaMalloc(&c->pool.base, bytes) != cudaSuccess) {
     *msg = "device allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM;
@@ -257,6 +257,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->ts.thetad0 = P.take<double>(nt + 1); c->ts.thetadd0 = P.take<double>(nt + 1);
   c->ts.sinv = P.take<double>(nt + 1); c->ts.cosv = P.take<double>(nt + 1);
   c->err_fsi = P.take<double>(nt + 1);
+  c->fsi_cnt = P.take<int>(8);
   c->G.nf = nf; c->G.restart = R;
   c->G.V = P.take<double>((size_t)(R + 1) * nf); c->G.H = P.take<double>((size_t)(R + 1) * R);
   c->G.cs = P.take<double>(R + 1); c->G.sn = P.take<double>(R + 1); c->G.g = P.take<double>(R + 1);
@@ -398,7 +399,7 @@ void ctx_destroy(Ctx* c) {
   if (c->solve_graph) cudaGraphDestroy(c->solve_graph);
   if (c->solve_exec_dense) cudaGraphExecDestroy(c->solve_exec_dense);
   for (PhaseGraph* ph : {&c->graph_pred, &c->graph_v2f, &c->graph_corr, &c->graph_fsi_rhs, &c->graph_fsi_asm,
-                         &c->graph_fsi_upd})
+                         &c->graph_fsi_upd, &c->graph_fsi_loop})
     drop_phase(ph);
   if (c->solve_graph_dense) cudaGraphDestroy(c->solve_graph_dense);
   inf_free(c);
@@ -951,6 +952,95 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
   return IB_OK;
 }
 
+// ------------------------------------------------------------- FSI iterations on the device
+__global__ void k_fsi_loop_init(int* cnt) {
+  if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
+}
+
+// End of one device FSI iteration: the counters (the cluster solver's G.ist: [0] Krylov
+// iterations, [4] restart cycles) and the loop condition of timestepper.F90:249 (fsi error
+// at or above the tolerance, iteration count within the limit), which also stops when the
+// next operator's patches leave the influence band (the host rebuilds it) or the error is
+// not finite (the host reports it).
+__global__ void k_fsi_loop_cond(int* cnt, const int* __restrict__ ist, const double* __restrict__ err,
+                                const int* __restrict__ band_flag, double tol, int max_it,
+                                cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0) return;
+  const double e = err[0];
+  const int n = cnt[0] + 1;
+  cnt[0] = n;
+  cnt[1] += ist[0];
+  cnt[2] += ist[0] + ist[4];
+  cnt[3] = *band_flag;
+  const bool go = isfinite(e) && e >= tol && n <= max_it && *band_flag == 0;
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// Captures the graph of a step's FSI iterations: the counters reset, then a while node whose
+// body is one iteration on the assembled operator (right-hand side, assembly, the cluster
+// Krylov solve, redistribution, structure update, weights and patches at the new positions)
+// and the condition.  The body's launches are counted once (fsi_body_launches).
+static int build_fsi_loop(Ctx* c) {
+  const GridDims& g = c->g;
+  const IbParams& p = c->p;
+  Influence& I = c->inf;
+  cudaStream_t st = c->st, s1 = nullptr;
+  IB_CUDA_CHECK(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+  int rc = IB_OK;
+  cudaGraph_t graph = nullptr;
+  const long long l0 = launch_count();
+  do {
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
+    count_launch();
+    k_fsi_loop_init<<<1, 32, 0, st>>>(c->fsi_cnt);
+    cudaGraphConditionalHandle h = 0;
+    cudaGraph_t body = nullptr;
+    if (cudaGraphConditionalHandleCreate(&h, capture_graph(st), 1, cudaGraphCondAssignDefault) != cudaSuccess)
+      rc = IB_ERR_CUDA;
+    if (rc == IB_OK) rc = add_while(st, h, &body);
+    if (rc == IB_OK && cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
+                           cudaSuccess)
+      rc = IB_ERR_CUDA;
+    if (rc == IB_OK) {
+      c->st = s1;
+      const long long b0 = launch_count();
+      auto iteration = [&]() -> int {
+        IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s1));
+        RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s1));
+        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s1));
+        RC(inf_assemble(c));
+        RC(launch_gmres_fused(c->G, &c->fused_plan, I.St, c->rhsf, c->f, p.rtol, p.atol, p.gmres_max_it, s1));
+        RC(op_redistribute(c, c->f, c->f_rdst));
+        RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, s1));
+        RC(op_reg_prep(c));
+        RC(inf_patch(c));
+        count_launch();
+        k_fsi_loop_cond<<<1, 32, 0, s1>>>(c->fsi_cnt, c->G.ist, c->err_fsi, I.flag, p.fsi_tol, p.fsi_max_it, h);
+        IB_CUDA_CHECK(cudaGetLastError());
+        return IB_OK;
+      };
+      rc = iteration();
+      c->fsi_body_launches = launch_count() - b0;
+      cudaGraph_t tmp;
+      if (cudaStreamEndCapture(s1, &tmp) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+      c->st = st;
+    }
+    if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+    if (rc == IB_OK && cudaGraphInstantiate(&c->graph_fsi_loop.exec, graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+  } while (false);
+  c->st = st;
+  count_launches(-(launch_count() - l0));   // captured, not run
+  cudaGetLastError();
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(s1);
+  if (rc != IB_OK) {
+    if (c->graph_fsi_loop.exec) cudaGraphExecDestroy(c->graph_fsi_loop.exec);
+    c->graph_fsi_loop.exec = nullptr;
+    c->graph_fsi_loop.failed = true;
+  }
+  return rc;
+}
+
 // The predictor of every level (timestepper.F90:103-236), coarse to fine.  Level k's solve
 // depends on the coarser levels only through rhsbc's second ring, 0.25 get_bc(omega_{k+1})
 // of the updated coarser vorticity, which enters on the boundary rows and columns.  So the
@@ -1045,6 +1135,31 @@ int op_advance(Ctx* c) {
       int fsi_count = 0;
       c->ksp_iter = 0;
       const bool moved = c->nt > 0;
+      // the iterations on the device while the operator stays assembled on a valid band (the
+      // host loop below takes over when a patch leaves it, and runs every step that needs the
+      // band built, the matrix-free operator or per-phase timing)
+      {
+        Influence& I = c->inf;
+        const bool device_loop = moved && p.schur_mode != 1 && c->use_step_graphs && c->use_fused && !c->prof_on &&
+                                 !c->stage_on && !c->graph_fsi_loop.failed && c->fused_plan.state == 1 && I.built &&
+                                 I.patch_fresh && I.flag_h == 0;
+        if (device_loop && (c->graph_fsi_loop.exec || build_fsi_loop(c) == IB_OK)) {
+          IB_CUDA_CHECK(cudaGraphLaunch(c->graph_fsi_loop.exec, st));
+          IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+          IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st));
+          IB_CUDA_CHECK(cudaStreamSynchronize(st));
+          fsi_count = c->h_ist[0];
+          c->ksp_iter += c->h_ist[1];
+          c->n_matvec += c->h_ist[2];
+          count_launches(1 + c->fsi_body_launches * (long long)fsi_count);
+          I.assemblies += fsi_count;
+          I.flag_h = c->h_ist[3];
+          I.patch_fresh = true;
+          I.active = false;
+          err = c->h_scal[0];
+          if (!std::isfinite(err)) return IB_ERR_NONFINITE;
+        }
+      }
       while (err >= p.fsi_tol && fsi_count <= p.fsi_max_it) {
         fsi_count += 1;
         step_mark(c, 3);
