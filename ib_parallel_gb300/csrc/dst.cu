@@ -505,6 +505,80 @@ __global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, con
   if (lane == 0) out[(size_t)rc.x * ld + rc.y] = acc;
 }
 
+// fac * get_bc (operators_fluid.F90:475-535) of the inverse x transform of a coarser level's
+// modes, without the transform: each CTA takes kRingSeg consecutive entries of one ring side,
+// evaluates the kRingSeg/2 + 1 coarse vertices they read (one warp each, the dot product of
+// k_dst_points), then forms the entries (coincident points copied, midpoints averaged).
+constexpr int kRingSeg = 32;
+constexpr int kRingWarps = kRingSeg / 2 + 1;
+__global__ void __launch_bounds__(32 * kRingWarps) k_ring_modes(int N, GridDims g, const double* __restrict__ spec,
+                                                                 int ld, const double* __restrict__ W, double fac,
+                                                                 double* __restrict__ ring) {
+  __shared__ double sp[kRingWarps];
+  const int nlr = (g.n + 1 + kRingSeg - 1) / kRingSeg, nbt = (g.m + 1 + kRingSeg - 1) / kRingSeg;
+  int b = blockIdx.x, side, c;
+  if (b < 2 * nlr) {
+    side = b / nlr;
+    c = b - side * nlr;
+  } else {
+    b -= 2 * nlr;
+    side = 2 + b / nbt;
+    c = b - (side - 2) * nbt;
+  }
+  const bool lr = side < 2;
+  const int len = lr ? g.n + 1 : g.m + 1;   // entries on this side
+  const int qmax = (len - 1) / 2;           // its last coarse vertex
+  const int q0 = c * (kRingSeg / 2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = q0 + warp;
+  double acc = 0.0;
+  if (q <= qmax) {
+    int I, J;
+    if (lr) {
+      I = side == 0 ? g.m / 4 + 1 : 3 * g.m / 4 + 1;
+      J = g.n / 4 + 1 + q;
+    } else {
+      J = side == 2 ? g.n / 4 + 1 : 3 * g.n / 4 + 1;
+      I = g.m / 4 + 1 + q;
+    }
+    const double* sr = spec + (size_t)(J - 2) * ld;
+    const double* wc = W + (size_t)(I - 2) * N;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int k = lane;
+    for (; k + 96 < N; k += 128) {
+      a0 = fma(sr[k], wc[k], a0);
+      a1 = fma(sr[k + 32], wc[k + 32], a1);
+      a2 = fma(sr[k + 64], wc[k + 64], a2);
+      a3 = fma(sr[k + 96], wc[k + 96], a3);
+    }
+    if (k < N) a0 = fma(sr[k], wc[k], a0);
+    if (k + 32 < N) a1 = fma(sr[k + 32], wc[k + 32], a1);
+    if (k + 64 < N) a2 = fma(sr[k + 64], wc[k + 64], a2);
+    acc = (a0 + a1) + (a2 + a3);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) sp[warp] = acc;
+  __syncthreads();
+  if ((int)threadIdx.x < kRingSeg) {
+    const int p = c * kRingSeg + (int)threadIdx.x;
+    if (p < len) {
+      const int qq = p / 2 - q0;
+      const double v = (p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq];
+      const int t = (side == 0 ? g.left : side == 1 ? g.right : side == 2 ? g.bottom : g.top) + p;
+      ring[t] = v * fac;
+    }
+  }
+}
+
+int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W, double fac,
+                        double* ring, cudaStream_t st) {
+  const int nlr = cdiv(g.n + 1, kRingSeg), nbt = cdiv(g.m + 1, kRingSeg);
+  count_launch();
+  k_ring_modes<<<2 * (nlr + nbt), 32 * kRingWarps, 0, st>>>(px.N, g, spec, ld, W, fac, ring);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
 // Rows of the forward x transform of an apply_bc boundary field, one warp per output.
 __global__ void k_dst_ring_rows(int N, GridDims g, const double* __restrict__ ring, const int* __restrict__ rows,
                                 int nrows, const double* __restrict__ W, const double* __restrict__ post_add,
@@ -557,13 +631,19 @@ __global__ void __launch_bounds__(256) k_dst_bc_modes(DstDev pl, GridDims g, con
       s_sum[threadIdx.x][1] = x1 - xn;
     }
     __syncthreads();
+    // out may alias post_add: every load of a thread's outputs is issued before its stores
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
       const double a = __ldg(&sk2[k]);
       const int par = (k & 1);   // mode kk = k+1 odd <=> k even
-      for (int i = 0; i < nr; ++i) {
-        const size_t o = (size_t)(r0 + i) * g.nsx + k;
+      double pa[kRowsPerCta];
+#pragma unroll
+      for (int i = 0; i < kRowsPerCta; ++i)
+        pa[i] = (post_add && i < nr) ? post_add[(size_t)(r0 + i) * g.nsx + k] : 0.0;
+#pragma unroll
+      for (int i = 0; i < kRowsPerCta; ++i) {
+        if (i >= nr) break;
         const double sv = s_sum[i][par];
-        out[o] = post_add ? fma(a, sv, post_scale * post_add[o]) : a * sv;
+        out[(size_t)(r0 + i) * g.nsx + k] = post_add ? fma(a, sv, post_scale * pa[i]) : a * sv;
       }
     }
     return;

@@ -116,6 +116,10 @@ int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, co
 // allowed (out == post_add).
 int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W, const double* sk2,
                    const double* post_add, double post_scale, double* out, cudaStream_t st);
+// ring = fac * get_bc of the inverse x transform of a coarser level's modes (spec, pitch ld),
+// evaluated at the points get_bc reads only (dot products with W).
+int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W, double fac,
+                        double* ring, cudaStream_t st);
 // sk2[k-1] = 2 sin(pi k/M), k = 1..N, into N doubles of device memory.
 int dst_sin2_table(const DstPlan& px, double* dev_out);
 size_t dst_smem_y(const DstPlan& p, int B, DstYMode mode);
