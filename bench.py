@@ -377,6 +377,7 @@ def run_gpu(args, world, rank, local):
         "tridiagonal_pass_us": 1e3 * t_tri,
         "schur_stages_us": sim.profile_schur(20),
         "influence": sim.influence_stats(),
+        "launch_shapes": sim.launch_shapes(),
         "step_phases_us": _step_phases(sim, 5),
     }
     if not args.no_matrix_free:

@@ -509,6 +509,19 @@ int ib_step_profile(IbCtx* h, int mode, double* phase_ms, long long* nsteps) {
   return op_result(ib::op_step_profile(c, mode, phase_ms, nsteps), "step_profile failed");
 }
 
+int ib_get_launch_shapes(IbCtx* h, int* shapes) {
+  CTX_OR_FAIL(h);
+  if (!shapes) return fail(IB_ERR_ARG, "bad argument");
+  int i = 0;
+  for (const ib::DstLaunch* L : {&c->lx, &c->lx_small, &c->lx_batch, &c->ly_none}) {
+    shapes[i++] = L->B;
+    shapes[i++] = L->NT;
+    shapes[i++] = L->narrow_scan;
+  }
+  shapes[i] = c->tl.Mb;
+  return IB_OK;
+}
+
 int ib_schur_matrix(IbCtx* h, double* S, int* status) {
   CTX_OR_FAIL(h);
   if (!S || !status) return fail(IB_ERR_ARG, "bad argument");

@@ -487,8 +487,9 @@ int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs
 
 static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring, double fac = 1.0);
 
-// vort2flux (operators_fluid.F90:237-377).  all_curls=false computes the fluxes
-// of the finest level only.
+// vort2flux (operators_fluid.F90:237-377).  all_levels=false writes the streamfunction and the
+// fluxes of the finest level only (the coarser levels' vorticity is still coarsified and their
+// modes still give the finest level its boundary values).
 //
 // Only the boundary values a level receives from the next coarser one depend on the
 // coarse-to-fine recursion, and they enter through apply_bc on the boundary rows and
@@ -497,7 +498,7 @@ static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring, 
 // (closed form on interior rows, dot products on the two edge rows), solves its per-mode
 // tridiagonal systems and evaluates the next finer level's ring from its modes at the few
 // points get_bc reads; one batched inverse pass and the curls finish.
-int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy, bool all_curls) {
+int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy, bool all_levels) {
   const int L = c->L;
   const GridDims& g = c->g;
   cudaStream_t st = c->st;
@@ -522,6 +523,15 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     }
     if (k > 0) RC(ring_from_modes(c, F, s[k], c->ringv[k - 1]));
   }
+  if (!all_levels) {
+    DstXArgs a;
+    a.in = c->hat[0]; a.out = s[0];
+    {
+      ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
+    }
+    return launch_curl(g, s[0], L == 1 ? c->zero_ring : c->ringv[0], qx[0], qy[0], st);
+  }
   {
     DstXArgs a;
     a.nlev = L;
@@ -529,7 +539,6 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     ProfScope ps(c, 0, pass_bytes(c, L, L));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
-  if (!all_curls) return launch_curl(g, s[0], L == 1 ? c->zero_ring : c->ringv[0], qx[0], qy[0], st);
   CurlBatch cb;
   for (int k = 0; k < L; ++k) {
     cb.s[k] = s[k];
@@ -1121,8 +1130,11 @@ int op_advance(Ctx* c) {
   if (it == 1) RC(predictor());   // the first step also seeds rhs_old
   else RC(run_phase(c, c->graph_pred, predictor));
   step_mark(c, 1);
+  // the FSI iterations read the finest level's fluxes only (timestepper.F90:240-245), and the
+  // correction's vort2flux rewrites every level's streamfunction and fluxes before they are
+  // read again: here the coarser levels are coarsified and solved in mode space only
   RC(run_phase(c, c->graph_v2f, [&]() {
-    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true);
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), false);
   }));
   step_mark(c, 2);
   // forces (timestepper.F90:249-486)

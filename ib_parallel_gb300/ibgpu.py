@@ -39,7 +39,7 @@ EXPORTS = [
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
     "ib_launch_count", "ib_probe_throughput", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
-    "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile",
+    "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile", "ib_get_launch_shapes",
 ]
 
 
@@ -110,6 +110,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_schur_matrix": ([P, P, C.POINTER(C.c_int)], C.c_int),
         "ib_step_profile": ([P, C.c_int, D, C.POINTER(C.c_longlong)], C.c_int),
         "ib_get_influence_stats": ([P, C.POINTER(C.c_longlong), D], C.c_int),
+        "ib_get_launch_shapes": ([P, I], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -339,6 +340,16 @@ class Simulation:
         n = C.c_longlong(0)
         _check(self.lib.ib_step_profile(self.h, mode, ms, C.byref(n)), "ib_step_profile")
         return {k: (1e3 * ms[i] / n.value if n.value else 0.0) for i, k in enumerate(self.STEP_PHASES)}
+
+    def launch_shapes(self) -> dict:
+        """The launch shapes the context runs with (tuned at creation when autotune is set)."""
+        v = (C.c_int * 13)()
+        _check(self.lib.ib_get_launch_shapes(self.h, v), "ib_get_launch_shapes")
+        names = ["x_one_level", "x_few_rows", "x_all_levels", "y"]
+        out = {n: {"lines_per_cta": v[3 * i], "threads": v[3 * i + 1], "one_warp_scan": v[3 * i + 2]}
+               for i, n in enumerate(names)}
+        out["tridiagonal_modes_per_cta"] = v[12]
+        return out
 
     def influence_stats(self) -> dict:
         counts = (C.c_longlong * 5)()

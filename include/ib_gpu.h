@@ -174,6 +174,10 @@ int ib_profile_schur(IbCtx* ctx, int reps, double* stage_ms);
  * vort2flux, FSI right-hand side, Schur assembly, GMRES, FSI update (redistribute, structure,
  * weights, host synchronisation), correction; *nsteps (may be NULL): steps timed */
 int ib_step_profile(IbCtx* ctx, int mode, double* phase_ms, long long* nsteps);
+/* The launch shapes the context runs with (chosen by timing at ib_create when autotune is set):
+ * shapes[0..12] = x pass of one level (lines per CTA, threads, one-warp scan), x pass over a few
+ * rows (3), x pass over every level (3), y pass (3), modes per CTA of the tridiagonal solve */
+int ib_get_launch_shapes(IbCtx* ctx, int* shapes);
 /* Fluid part of the Schur matrix (a_times2 without B, operators_fluid.F90:14-120: the matrix
  * timestepper.F90:560-598 builds column by column for stationary bodies) at the current body
  * positions, assembled from the influence matrix (schur_mode 0; built on first use):
