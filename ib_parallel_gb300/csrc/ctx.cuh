@@ -217,7 +217,7 @@ int op_ainv(Ctx* c, const double* in, double* out);
 int op_dst(Ctx* c, const double* in, double* out);
 int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs_old, const double* rhsbc);
 int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy,
-                 bool all_levels);
+                 bool all_levels, bool hat0_given = false);
 int op_schur(Ctx* c, const double* x, double* y, bool with_b);
 int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out, double* s_out,
                 const double** ring0_out);

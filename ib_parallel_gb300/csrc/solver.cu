@@ -498,24 +498,29 @@ static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring, 
 // (closed form on interior rows, dot products on the two edge rows), solves its per-mode
 // tridiagonal systems and evaluates the next finer level's ring from its modes at the few
 // points get_bc reads; one batched inverse pass and the curls finish.
-int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy, bool all_levels) {
+int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy, bool all_levels,
+                 bool hat0_given) {
   const int L = c->L;
   const GridDims& g = c->g;
   cudaStream_t st = c->st;
   if (L > kMaxBatch) return IB_ERR_ARG;
+  // hat0_given: hat[0] holds modes Y with w[0] = S_x Y (the predictor's), so S_x w[0] = 2m Y and
+  // the finest level skips its forward transform (its boundary terms scale Y by 2m)
+  const bool skip0 = hat0_given && L >= 2;
   for (int k = 1; k < L; ++k) RC(launch_coarsify(g, w[k - 1], w[k], st));
   {
     DstXArgs a;
-    a.nlev = L;
-    for (int k = 0; k < L; ++k) { a.lin[k] = w[k]; a.lout[k] = c->hat[k]; }
-    ProfScope ps(c, 0, pass_bytes(c, L, L));
+    const int k0 = skip0 ? 1 : 0;
+    a.nlev = L - k0;
+    for (int k = k0; k < L; ++k) { a.lin[k - k0] = w[k]; a.lout[k - k0] = c->hat[k]; }
+    ProfScope ps(c, 0, pass_bytes(c, L - k0, L - k0));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
   for (int k = L - 1; k >= 0; --k) {
     double* F = c->hat[k];
     if (k < L - 1) {
       // boundary terms from the ring of level k (get_bc of level k+1), apply_bc with fac 1
-      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, F, 1.0, F, st));
+      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, F, k == 0 && skip0 ? 2.0 * g.m : 1.0, F, st));
     }
     {
       ProfScope ps(c, 1, pass_bytes(c, 1, 1));
@@ -1134,7 +1139,7 @@ int op_advance(Ctx* c) {
   // correction's vort2flux rewrites every level's streamfunction and fluxes before they are
   // read again: here the coarser levels are coarsified and solved in mode space only
   RC(run_phase(c, c->graph_v2f, [&]() {
-    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), false);
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), false, true);
   }));
   step_mark(c, 2);
   // forces (timestepper.F90:249-486)
@@ -1152,8 +1157,8 @@ int op_advance(Ctx* c) {
       {
         Influence& I = c->inf;
         const bool device_loop = moved && p.schur_mode != 1 && c->use_step_graphs && c->use_fused && !c->prof_on &&
-                                 !c->stage_on && !c->graph_fsi_loop.failed && c->fused_plan.state == 1 && I.built &&
-                                 I.patch_fresh && I.flag_h == 0;
+                                 !c->stage_on && !c->step_prof && !c->graph_fsi_loop.failed &&
+                                 c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
         if (device_loop && (c->graph_fsi_loop.exec || build_fsi_loop(c) == IB_OK)) {
           IB_CUDA_CHECK(cudaGraphLaunch(c->graph_fsi_loop.exec, st));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
