@@ -280,6 +280,8 @@ def run_gpu(args, world, rank, local):
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    if args.host_fsi_loop:
+        sim.step_profile(1)
     with Clocks(local) as clk:
         if args.profile_window:
             torch.cuda.profiler.start()
@@ -295,6 +297,8 @@ def run_gpu(args, world, rank, local):
         clk.end()
         if args.profile_window:
             torch.cuda.profiler.stop()
+    if args.host_fsi_loop:
+        sim.step_profile(0)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     t_s = _barrier_max(ms / 1e3, world)
@@ -448,6 +452,10 @@ def main():
                     help="skip timing the matrix-free Schur operator beside the default one")
     ap.add_argument("--profile-window", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+    ap.add_argument("--host-fsi-loop", action="store_true",
+                    help="run the timed steps with per-phase timing on, so that the FSI iterations run from the "
+                         "host and each of their kernels is a separate launch (a profiler lists kernels inside "
+                         "the device loop's graph node only as the graph)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":

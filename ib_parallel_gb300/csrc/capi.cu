@@ -487,7 +487,7 @@ int ib_measure_fp64_peak(double* tflops) {
 }
 
 int ib_probe_throughput(int which, double* value) {
-  if (!value || which < 0 || which > 4) return fail(IB_ERR_ARG, "bad probe");
+  if (!value || which < 0 || which > 13) return fail(IB_ERR_ARG, "bad probe");
   return op_result(ib::probe_throughput(which, value), "probe failed");
 }
 

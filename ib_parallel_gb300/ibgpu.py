@@ -489,4 +489,8 @@ if __name__ == "__main__":
     if len(_s.argv) > 1 and _s.argv[1] == "probe":
         names = ["fp64_fma", "fp64_fma_half_lanes", "fp64_fma_1warp_per_sm", "fp32_fma", "int32_imad"]
         for i, nme in enumerate(names):
-            print(f"{nme} {probe_throughput(i):.3f}")
+            print(f"{nme} {probe_throughput(i):.3f} T(FL)OP/s")
+        lat = ["fp64_fma", "sqrt", "division", "rsqrt", "reciprocal_rn", "cluster_barrier_8cta",
+               "dsmem_load_chain", "shuffle_plus_dadd", "cta_barrier_128thr"]
+        for i, nme in enumerate(lat):
+            print(f"latency_{nme} {probe_throughput(5 + i):.1f} cycles")

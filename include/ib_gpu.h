@@ -197,7 +197,10 @@ long long ib_launch_count(void);
 /* measured FP64 FMA throughput of this GPU (TFLOP/s), from a register-resident FMA loop */
 int ib_measure_fp64_peak(double* tflops);
 /* which: 0 FP64 FMA, 1 FP64 FMA with half of each warp's lanes active (useful rate),
- * 2 FP64 FMA with one warp per SM, 3 FP32 FMA, 4 INT32 IMAD; *value in T(FL)OP/s */
+ * 2 FP64 FMA with one warp per SM, 3 FP32 FMA, 4 INT32 IMAD; *value in T(FL)OP/s.
+ * which 5..13: latencies of dependent operations in cycles - FP64 FMA, sqrt, division, rsqrt,
+ * correctly rounded reciprocal, cluster barrier (8 CTAs), load from another CTA's shared
+ * memory, warp shuffle + FP64 add, CTA barrier */
 int ib_probe_throughput(int which, double* value);
 /* kind 0: x pass, 1: y pass with diagonal, 2: y pass of the predictor, 3: plain y pass;
  * count of timed launches, their summed device time (ms) and summed algorithmic DRAM bytes */
