@@ -17,6 +17,23 @@ static double2 twiddle(long long num, long long den) {
   return make_double2((double)cosl(a), (double)(-sinl(a)));
 }
 
+static bool factor_radices(int P, int* rad, int* nrad);
+
+// The Stockham stages' twiddles, stage by stage: the stage of span Ns (the product of the earlier
+// radices) and radix R uses w^(r k P/(Ns R)), r = 1..R-1, k = 0..Ns-1, stored at
+// Ns - 1 + (r-1) Ns + k, so that a warp's lanes (consecutive k) read consecutive entries.  The
+// stages' blocks [Ns - 1, R Ns - 1) tile [0, P - 1).
+static void stage_twiddles(int P, const int* rad, int nrad, std::vector<double2>& tw) {
+  tw.assign(P, make_double2(1.0, 0.0));
+  int Ns = 1;
+  for (int s = 0; s < nrad; ++s) {
+    const int R = rad[s], step = P / (Ns * R);
+    for (int r = 1; r < R; ++r)
+      for (int k = 0; k < Ns; ++k) tw[Ns - 1 + (r - 1) * Ns + k] = twiddle((long long)r * k * step, P);
+    Ns *= R;
+  }
+}
+
 static bool factor_radices(int P, int* rad, int* nrad) {
   // radix-5 and radix-3 stages first (no twiddles in the first stage), then 4, then 2.
   int n = 0, q = P;
@@ -34,9 +51,9 @@ int dst_plan_create(DstPlan* p, int N) {
   if (N < 3 || M % 4 != 0) return IB_ERR_ARG;
   p->N = N; p->M = M; p->P = M / 2;
   if (!factor_radices(p->P, p->rad, &p->nrad)) return IB_ERR_ARG;
-  std::vector<double2> tw(p->P), uw(p->P / 2);
+  std::vector<double2> tw, uw(p->P / 2);
   std::vector<double> sn(p->P + 1);
-  for (int t = 0; t < p->P; ++t) tw[t] = twiddle(t, p->P);
+  stage_twiddles(p->P, p->rad, p->nrad, tw);
   for (int k = 0; k < p->P / 2; ++k) uw[k] = twiddle(k, M);
   const long double PI_L = 3.141592653589793238462643383279502884L;
   for (int j = 0; j <= p->P; ++j) sn[j] = (double)sinl(PI_L * (long double)j / (long double)M);
@@ -63,9 +80,9 @@ int dst_plan_init_external(DstPlan* p, int N, double* dev, cudaStream_t st) {
   if (dst_plan_table_doubles(N) == 0) return IB_ERR_ARG;
   p->N = N; p->M = M; p->P = M / 2;
   if (!factor_radices(p->P, p->rad, &p->nrad)) return IB_ERR_ARG;
-  std::vector<double2> tw(p->P), uw(p->P / 2);
+  std::vector<double2> tw, uw(p->P / 2);
   std::vector<double> sn(p->P + 1);
-  for (int t = 0; t < p->P; ++t) tw[t] = twiddle(t, p->P);
+  stage_twiddles(p->P, p->rad, p->nrad, tw);
   for (int k = 0; k < p->P / 2; ++k) uw[k] = twiddle(k, M);
   const long double PI_L = 3.141592653589793238462643383279502884L;
   for (int j = 0; j <= p->P; ++j) sn[j] = (double)sinl(PI_L * (long double)j / (long double)M);
@@ -178,7 +195,7 @@ __device__ __forceinline__ void stockham_stage(const double2* __restrict__ in, d
                                                const double2* __restrict__ tw, int B, int tid, int NT) {
   const int nb = fnb.d, Ns = fns.d;
   const int total = B * nb;
-  const int twstep = P / (Ns * R);
+  const double2* __restrict__ tws = tw + Ns - 1;   // this stage's twiddles (stage_twiddles)
   for (int it = tid; it < total; it += NT) {
     int b = fnb.div(it);
     int j = it - b * nb;
@@ -191,7 +208,7 @@ __device__ __forceinline__ void stockham_stage(const double2* __restrict__ in, d
     for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
     if (Ns > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * twstep]));
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tws[(r - 1) * Ns + k]));
     }
     Dft<R>::run(v);
     int idxD = jq * Ns * R + k;

@@ -23,7 +23,7 @@ struct DstPlan {
   int N = 0, M = 0, P = 0;
   int nrad = 0;
   int rad[kMaxRadices] = {0};
-  double2* tw = nullptr;   // P entries: exp(-2 pi i t / P)
+  double2* tw = nullptr;   // P entries: the Stockham stages' twiddles, stage by stage (dst.cu)
   double2* uw = nullptr;   // P/2 entries: exp(-2 pi i k / M)
   double* sn = nullptr;    // P+1 entries: sin(j pi / M)
 };
