@@ -504,9 +504,11 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
   const GridDims& g = c->g;
   cudaStream_t st = c->st;
   if (L > kMaxBatch) return IB_ERR_ARG;
-  // hat0_given: hat[0] holds modes Y with w[0] = S_x Y (the predictor's), so S_x w[0] = 2m Y and
-  // the finest level skips its forward transform (its boundary terms scale Y by 2m)
+  // hat0_given: hat[0] holds modes Y with w[0] = S_x Y, so S_x w[0] = 2m Y and the finest level
+  // skips its forward transform (its boundary terms scale Y by 2m).  With all_levels false the
+  // finest level is then solved in spec2, leaving Y in hat[0] for the correction.
   const bool skip0 = hat0_given && L >= 2;
+  double* F0 = skip0 && !all_levels ? c->spec2 : c->hat[0];
   for (int k = 1; k < L; ++k) RC(launch_coarsify(g, w[k - 1], w[k], st));
   {
     DstXArgs a;
@@ -517,10 +519,11 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
   for (int k = L - 1; k >= 0; --k) {
-    double* F = c->hat[k];
+    double* F = k == 0 ? F0 : c->hat[k];
     if (k < L - 1) {
       // boundary terms from the ring of level k (get_bc of level k+1), apply_bc with fac 1
-      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, F, k == 0 && skip0 ? 2.0 * g.m : 1.0, F, st));
+      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, c->hat[k], k == 0 && skip0 ? 2.0 * g.m : 1.0, F,
+                        st));
     }
     {
       ProfScope ps(c, 1, pass_bytes(c, 1, 1));
@@ -530,7 +533,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
   }
   if (!all_levels) {
     DstXArgs a;
-    a.in = c->hat[0]; a.out = s[0];
+    a.in = F0; a.out = s[0];
     {
       ProfScope ps(c, 0, pass_bytes(c, 1, 1));
       RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
@@ -1276,7 +1279,10 @@ int op_advance(Ctx* c) {
       RC(op_ainv(c, c->vort, c->vort));
     }
     RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], c->st));
-    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true);
+    // omega_1 was S_x Y (the predictor's modes, still in hat[0]) and vort is S_x Y' (ainv's
+    // modes, in spec1): the corrected omega_1 has modes Y - Y'
+    if (L >= 2) RC(launch_sub(g.ns, c->hat[0], c->spec1, c->hat[0], c->st));
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2);
   }));
   step_mark(c, 9);
   int rc = check_err(c);
