@@ -415,7 +415,8 @@ int inf_assemble(Ctx* c) {
   k_inf_compact<<<1, 1024, 0, st>>>(I.nR, I.used, I.ulist, I.upos, I.nu);
   count_launch();
   k_inf_kp<<<dim3(cdiv(I.nR, 128), c->nf), 128, 0, st>>>(I.nR, I.K, I.pval, I.pidx, I.ulist, I.nu, I.T);
-  IB_CUDA_CHECK(cudaMemsetAsync(I.bod, 0xff, sizeof(int) * (size_t)c->nf, st));   // -1: no B term
+  // -1: no B term (unknowns of rigid bodies; k_inf_bvec sets every torsional body's own)
+  if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(I.bod, 0xff, sizeof(int) * (size_t)c->nf, st));
   if (c->nt > 0) {
     count_launch();
     k_inf_bvec<<<c->nt, 32, 0, st>>>(c->tb, c->ts, c->p.dt, c->delta, I.brv, I.bco, I.bod);

@@ -1021,7 +1021,7 @@ static int build_fsi_loop(Ctx* c) {
       c->st = s1;
       const long long b0 = launch_count();
       auto iteration = [&]() -> int {
-        IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s1));
+        if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s1));
         RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s1));
         RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s1));
         RC(inf_assemble(c));
@@ -1183,7 +1183,8 @@ int op_advance(Ctx* c) {
         fsi_count += 1;
         step_mark(c, 3);
         RC(run_phase(c, c->graph_fsi_rhs, [&]() -> int {
-          IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, c->st));
+          // k_tors_rhs writes every unknown of a torsional body: rigid bodies' start at zero
+          if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, c->st));
           RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, c->st));
           return launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, c->st);
         }));

@@ -61,7 +61,7 @@ __global__ void k_tors_rhs(const TorsBody* __restrict__ tb, TorsState s, double 
 // compute_dx + update_xb (operators_struct.F90:402-505, 600-620); err = max |dtheta|
 __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
                           const double* __restrict__ f, double* __restrict__ xb, double* __restrict__ yb,
-                          double* __restrict__ err_per_body) {
+                          double* __restrict__ err_per_body, double* __restrict__ err_max) {
   int t = blockIdx.x;
   TorsBody b = tb[t];
   double th = s.theta[t], th0 = s.theta0[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
@@ -81,6 +81,7 @@ __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double d
     s.thetad[t] = -thd0 + 2.0 / dt * (thn - th0);
     s.thetadd[t] = -thdd0 - 4.0 / dt * thd0 + 4.0 / (dt * dt) * (thn - th0);
     err_per_body[t] = fabs(dth);
+    if (err_max) *err_max = fabs(dth);   // one body: its error is the maximum
   }
   double g = b.gamma0 - thn;
   double cg = cos(g), sg = sin(g);
@@ -161,9 +162,11 @@ int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, do
   }
   // err[1..nt] holds per-body |dtheta|, err[0] their maximum
   count_launch();
-  k_tors_dx<<<nt, 32, 0, st>>>(tb, s, dt, delta, f, xb, yb, err + 1);
-  count_launch();
-  k_max_reduce<<<1, 32, 0, st>>>(nt, err + 1, err);
+  k_tors_dx<<<nt, 32, 0, st>>>(tb, s, dt, delta, f, xb, yb, err + 1, nt == 1 ? err : nullptr);
+  if (nt > 1) {
+    count_launch();
+    k_max_reduce<<<1, 32, 0, st>>>(nt, err + 1, err);
+  }
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
