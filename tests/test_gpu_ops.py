@@ -21,8 +21,9 @@ def _rand(rng, shape):
     return rng.standard_normal(shape)
 
 
-# the sizes cover the tridiagonal solve's chunk lengths 1, 2, 3, 7 and (800 x 400) 24
-@pytest.mark.parametrize("mn", [(64, 32), (60, 40), (96, 48), (120, 36), (40, 200), (800, 400)])
+# the sizes cover the tridiagonal solve's chunk lengths 1, 2, 3, 7, (800 x 400) 24 in registers,
+# and (40 x 540) 17, which runs the shared-memory kernel
+@pytest.mark.parametrize("mn", [(64, 32), (60, 40), (96, 48), (120, 36), (40, 200), (800, 400), (40, 540)])
 def test_dst_sizes(mn):
     m, n = mn
     kw = dict(SMALL, m=m, n=n, mgridlev=2)
