@@ -418,6 +418,7 @@ __device__ __forceinline__ double x_load(const XPre& a, const double* __restrict
 template <int PRE>
 __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, const __grid_constant__ DstXArgs a,
                                                GridDims g, int B, int narrow_scan) {
+  IB_GRID_DEP_WAIT();
   const double* ain = a.nlev ? a.lin[blockIdx.y] : a.in;
   double* aout = a.nlev ? a.lout[blockIdx.y] : a.out;
   const XPre pre = x_pre(a, blockIdx.y, PRE == PRE_PRED && a.nlev > 0);
@@ -499,6 +500,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
 // Selected points of an inverse x transform, one warp per point.
 __global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, const int2* __restrict__ pts, int npts,
                              const double* __restrict__ W, double* __restrict__ out) {
+  IB_GRID_DEP_WAIT();
   int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (gw >= npts) return;
@@ -531,6 +533,7 @@ constexpr int kRingWarps = kRingSeg / 2 + 1;
 __global__ void __launch_bounds__(32 * kRingWarps) k_ring_modes(int N, GridDims g, const double* __restrict__ spec,
                                                                  int ld, const double* __restrict__ W, double fac,
                                                                  double* __restrict__ ring) {
+  IB_GRID_DEP_WAIT();
   __shared__ double sp[kRingWarps];
   const int nlr = (g.n + 1 + kRingSeg - 1) / kRingSeg, nbt = (g.m + 1 + kRingSeg - 1) / kRingSeg;
   int b = blockIdx.x, side, c;
@@ -600,6 +603,7 @@ int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec
 __global__ void k_dst_ring_rows(int N, GridDims g, const double* __restrict__ ring, const int* __restrict__ rows,
                                 int nrows, const double* __restrict__ W, const double* __restrict__ post_add,
                                 double post_scale, double* __restrict__ out) {
+  IB_GRID_DEP_WAIT();
   int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (gw >= nrows * N) return;
@@ -635,6 +639,7 @@ __global__ void __launch_bounds__(256) k_dst_bc_modes(DstDev pl, GridDims g, con
                                                       const double* __restrict__ W, const double* __restrict__ sk2,
                                                       const double* __restrict__ post_add, double post_scale,
                                                       double* __restrict__ out, int nEdge) {
+  IB_GRID_DEP_WAIT();
   const int N = pl.N;
   if ((int)blockIdx.x >= nEdge) {
     __shared__ double s_sum[kRowsPerCta][2];   // x_1 + x_N, x_1 - x_N per row
@@ -761,6 +766,7 @@ int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, co
 
 // ------------------------------------------------------------- y pass
 __global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, DstYArgs a, int B, int narrow_scan) {
+  IB_GRID_DEP_WAIT();
   extern __shared__ double2 smem2[];
   const int ldx = pl.M;
   const int N = pl.N;

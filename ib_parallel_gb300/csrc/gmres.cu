@@ -164,6 +164,7 @@ __device__ void back_substitute(const double* __restrict__ H, int R, const doubl
 }
 
 __global__ void k_gmres_init(GmresDev G) {
+  IB_GRID_DEP_WAIT();
   if (threadIdx.x == 0) {
     G.ist[0] = 0; G.ist[1] = 0; G.ist[2] = 0; G.ist[3] = 0; G.ist[4] = 0;
   }
@@ -172,6 +173,7 @@ __global__ void k_gmres_init(GmresDev G) {
 // Cycle start: r = b - A x (A x in G.Av), V0 = r/||r||, tolerance on the first cycle.
 __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const double* __restrict__ x, double rtol,
                               double atol, int max_it, cudaGraphConditionalHandle h_inner, int use_cond) {
+  IB_GRID_DEP_WAIT();
   __shared__ double part[2 * kSlices];
   __shared__ double s_norm[2];
   const int nf = G.nf, tid = threadIdx.x;
@@ -225,6 +227,7 @@ __global__ void k_gmres_start(GmresDev G, const double* __restrict__ b, const do
 // One Arnoldi step on w = A V[it] (in G.Av): classical Gram-Schmidt (all projections
 // against the unmodified w), normalisation, Givens update.
 __global__ void k_gmres_arnoldi(GmresDev G, int max_it, cudaGraphConditionalHandle h_inner, int use_cond) {
+  IB_GRID_DEP_WAIT();
   __shared__ double part[64 * kSlices];
   __shared__ double h[64];
   __shared__ double s_tt[2];
@@ -283,6 +286,7 @@ __global__ void k_gmres_arnoldi(GmresDev G, int max_it, cudaGraphConditionalHand
 // KSPGMRESBuildSoln: back substitution and x += V y.
 __global__ void k_gmres_update(GmresDev G, double* __restrict__ x, int max_it, cudaGraphConditionalHandle h_outer,
                                int use_cond) {
+  IB_GRID_DEP_WAIT();
   __shared__ double y[64], rc[64];
   const int nf = G.nf, R = G.restart;
   const int it = G.ist[2];
@@ -302,6 +306,7 @@ __global__ void k_gmres_update(GmresDev G, double* __restrict__ x, int max_it, c
 }
 
 __global__ void k_copy(int n, const double* __restrict__ a, double* __restrict__ b) {
+  IB_GRID_DEP_WAIT();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = a[i];
 }
@@ -347,6 +352,7 @@ int launch_copy(int n, const double* a, double* b, cudaStream_t st) {
 // lower factor L in place of the lower triangle (L[i*n+j], j<=i).  One CTA,
 // right-looking, column by column.
 __global__ void k_cholesky(int n, double* A, int* err) {
+  IB_GRID_DEP_WAIT();
   __shared__ double piv;
   for (int k = 0; k < n; ++k) {
     if (threadIdx.x == 0) {
@@ -371,6 +377,7 @@ __global__ void k_cholesky(int n, double* A, int* err) {
 }
 
 __global__ void k_chol_solve(int n, const double* __restrict__ L, const double* __restrict__ b, double* x) {
+  IB_GRID_DEP_WAIT();
   extern __shared__ double y[];
   for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = b[i];
   __syncthreads();
@@ -390,10 +397,12 @@ __global__ void k_chol_solve(int n, const double* __restrict__ L, const double* 
 }
 
 __global__ void k_copy_col(int n, const double* __restrict__ src, double* M, int col) {
+  IB_GRID_DEP_WAIT();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) M[(size_t)i * n + col] = src[i];
 }
 __global__ void k_unit(int n, int i, double* e) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) e[t] = (t == i) ? 1.0 : 0.0;
 }
@@ -521,6 +530,7 @@ __device__ void givens_step_warp(double* __restrict__ col, const double* __restr
 __global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThreads)
     k_gmres_cluster(GmresDev G, const double* __restrict__ At, int a_in_smem, const double* __restrict__ b,
                     double* __restrict__ x, double rtol, double atol, int max_it) {
+  IB_GRID_DEP_WAIT();
   const unsigned full = 0xffffffffu;
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();

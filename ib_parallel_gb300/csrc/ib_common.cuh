@@ -96,6 +96,12 @@ struct FastDiv {
   __device__ __forceinline__ int mod(int n) const { return n - div(n) * d; }
 };
 
+// Programmatic dependent launch: in the captured step graphs the edges between kernels are
+// programmatic (make_edges_programmatic), so a kernel's CTAs may be scheduled while its
+// predecessor finishes.  Every kernel of this library therefore waits here, first thing, for
+// its predecessor's completion and memory; launched without such an edge it returns at once.
+#define IB_GRID_DEP_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+
 // Number of kernels this library has launched (all contexts), for the benchmark's
 // launch count.  Defined in solver.cu.
 void count_launch();

@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(128) k_reg_weights(GridDims g, int nf, const d
                                                      const double* __restrict__ yb, double d, double ox,
                                                      double oy, const int* __restrict__ comp, int* ix, int* iy,
                                                      double* w, int* stale, int* err) {
+  IB_GRID_DEP_WAIT();
   __shared__ double fac[16][7];    // [2*unknown + axis][offset], axis 0: x factor, 1: y factor
   const int k0 = blockIdx.x * 8;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -115,6 +116,7 @@ __global__ void __launch_bounds__(128) k_reg_weights(GridDims g, int nf, const d
 // and that E(curl s) reads, followed by the treatment of the other rows (zero / skip).
 __global__ void k_reg_bbox(GridDims g, int nf, const int* __restrict__ ix, const int* __restrict__ iy, int* bbox,
                            const int* __restrict__ stale) {
+  IB_GRID_DEP_WAIT();
   __shared__ int s[4][32];
   if (!*stale) return;
   int imin = 1 << 30, jmin = 1 << 30, imax = -(1 << 30), jmax = -(1 << 30);
@@ -153,6 +155,7 @@ template <bool FILL>
 __global__ void k_reg_lists(int nf, const int* __restrict__ comp, const int* __restrict__ ix,
                             const int* __restrict__ iy, const int* __restrict__ bbox, int* cnt_x, int* cnt_y,
                             int* lst_x, int* lst_y, int max_faces, const int* __restrict__ stale) {
+  IB_GRID_DEP_WAIT();
   if (!*stale) return;
   int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
   int nface = ni * nj;
@@ -181,6 +184,7 @@ __global__ void k_reg_lists(int nf, const int* __restrict__ comp, const int* __r
 // consecutive faces, the runs are scanned with warp shuffles, then written back.
 __global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y, int max_faces,
                            const int* __restrict__ stale) {
+  IB_GRID_DEP_WAIT();
   __shared__ int wsum[32];
   if (!*stale) return;
   const int nface = bbox[2] * bbox[3];
@@ -242,6 +246,7 @@ __global__ void k_reg(GridDims g, const double* __restrict__ h0, const double* _
                       const int* __restrict__ bbox, const int* __restrict__ cnt_x, const int* __restrict__ cnt_y,
                       const int* __restrict__ lst_x, const int* __restrict__ lst_y, double* hx, double* hy,
                       int max_faces) {
+  IB_GRID_DEP_WAIT();
   int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
   int nface = ni * nj;
   if (nface + 1 > max_faces) return;
@@ -284,6 +289,7 @@ __global__ void k_regT(GridDims g, int nf, const double* __restrict__ qx, const 
                        const double* __restrict__ qy, const double* __restrict__ qy0, const int* __restrict__ comp,
                        const int* __restrict__ ix, const int* __restrict__ iy, const double* __restrict__ w,
                        const double* __restrict__ h0_in, double* h0_out) {
+  IB_GRID_DEP_WAIT();
   int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (k >= nf) return;
@@ -323,6 +329,7 @@ int launch_regT(const GridDims& g, int nf, const double* qx, const double* qx0, 
 __global__ void k_regT_s(GridDims g, int nf, const double* __restrict__ s, const double* __restrict__ ring,
                          const int* __restrict__ comp, const int* __restrict__ ix, const int* __restrict__ iy,
                          const double* __restrict__ w, const double* __restrict__ h0_in, double* h0_out) {
+  IB_GRID_DEP_WAIT();
   int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (k >= nf) return;
@@ -357,6 +364,7 @@ __global__ void k_redist_field(GridDims g, const double* __restrict__ f, const d
                                const int* __restrict__ bbox, const int* __restrict__ cnt_x,
                                const int* __restrict__ cnt_y, const int* __restrict__ lst_x,
                                const int* __restrict__ lst_y, double* fx, double* fy, int max_faces) {
+  IB_GRID_DEP_WAIT();
   int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
   int nface = ni * nj;
   if (nface + 1 > max_faces) return;
@@ -396,6 +404,7 @@ int launch_redistribute_field(const GridDims& g, int nf, const double* f, const 
 // write_force2: out[b] = 2 delta sum_x f/dt, out[nbody+b] = 2 delta sum_y f/dt
 __global__ void k_force_coeffs(int nf, int nbody, const int* __restrict__ comp, const int* __restrict__ bid,
                                const double* __restrict__ f, double dt, double delta, double* out) {
+  IB_GRID_DEP_WAIT();
   // one thread per body, sequential in unknown order
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbody) return;

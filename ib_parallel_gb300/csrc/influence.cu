@@ -30,6 +30,7 @@ __global__ void k_inf_patch(GridDims g, int nf, const int* __restrict__ comp, co
                             const int* __restrict__ iy, const double* __restrict__ w,
                             const int* __restrict__ tile_of, int ntx, double* __restrict__ pval,
                             int* __restrict__ pidx, int* __restrict__ used, int* __restrict__ flag) {
+  IB_GRID_DEP_WAIT();
   const int k = blockIdx.x, q = threadIdx.x;
   if (k >= nf || q >= kP) return;
   const int di = q & 7, dj = q >> 3;
@@ -64,6 +65,7 @@ __global__ void k_inf_patch(GridDims g, int nf, const int* __restrict__ comp, co
 // Compaction of the touched band vertices (one CTA of 1024 threads).
 __global__ void k_inf_compact(int nR, const int* __restrict__ used, int* __restrict__ ulist,
                               int* __restrict__ upos, int* __restrict__ nu) {
+  IB_GRID_DEP_WAIT();
   __shared__ int wsum[32];
   __shared__ int base;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -105,6 +107,7 @@ __global__ void k_inf_compact(int nR, const int* __restrict__ used, int* __restr
 __global__ void k_inf_kp(int nR, const double* __restrict__ K, const double* __restrict__ pval,
                          const int* __restrict__ pidx, const int* __restrict__ ulist, const int* __restrict__ nu,
                          double* __restrict__ T) {
+  IB_GRID_DEP_WAIT();
   __shared__ double sv[kP];
   __shared__ int si[kP];
   const int l = blockIdx.y;
@@ -130,6 +133,7 @@ __global__ void k_inf_kp(int nR, const double* __restrict__ K, const double* __r
 // B[k][l] = BR_k BR_l (delta^2/ds/dt)(2 ds/dt) / K_eff for k, l on the same body.
 __global__ void k_inf_bvec(const TorsBody* __restrict__ tb, TorsState ts, double dt, double delta,
                            double* __restrict__ brv, double* __restrict__ bco, int* __restrict__ bod) {
+  IB_GRID_DEP_WAIT();
   const int t = blockIdx.x;
   const TorsBody b = tb[t];
   const double sv = ts.sinv[t], cv = ts.cosv[t];
@@ -147,6 +151,7 @@ __global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const
                           const int* __restrict__ upos, const double* __restrict__ T,
                           const double* __restrict__ brv, const double* __restrict__ bco,
                           const int* __restrict__ bod, double* __restrict__ S, double* __restrict__ St) {
+  IB_GRID_DEP_WAIT();
   __shared__ double sv[kP];
   __shared__ int su[kP];
   const int k = blockIdx.x;
@@ -174,6 +179,7 @@ __global__ void k_inf_ptk(int nf, int nR, const double* __restrict__ pval, const
 // column segment in order, combined by a fixed shuffle tree -- the product the cluster
 // GMRES solver forms, so that both solvers see identical operator outputs.
 __global__ void k_dense_mv(int n, const double* __restrict__ At, const double* __restrict__ x, double* __restrict__ y) {
+  IB_GRID_DEP_WAIT();
   // rows in groups of S lanes, 32/S groups per warp (the cluster solver's layout)
   const int S = mv_segments(n), gpw = 32 / S, cw = (n + S - 1) / S;
   const int lane = threadIdx.x & 31, grp = lane / S, seg = lane - grp * S;
@@ -191,6 +197,7 @@ __global__ void k_dense_mv(int n, const double* __restrict__ At, const double* _
 // Column c of the precompute: unit vorticity at band vertex c (the previous one cleared),
 // and the row range of the forward transform (the one nonzero row).
 __global__ void k_inf_unit(int c, const int2* __restrict__ tiles, GridDims g, double* vort, int* prev, int* rr_in) {
+  IB_GRID_DEP_WAIT();
   if (threadIdx.x != 0) return;
   const int p = *prev;
   if (p >= 0) vort[p] = 0.0;
@@ -214,6 +221,7 @@ __global__ void k_inf_unit(int c, const int2* __restrict__ tiles, GridDims g, do
 // K[c][v] = s(band vertex v) for every band vertex (0 for tile vertices outside the grid).
 __global__ void k_inf_gather(int c, int nR, const int2* __restrict__ tiles, GridDims g, const double* __restrict__ s,
                              double* __restrict__ K) {
+  IB_GRID_DEP_WAIT();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nR) return;
   const int2 tc = tiles[i / kP];

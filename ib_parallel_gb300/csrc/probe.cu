@@ -10,6 +10,7 @@ namespace ib {
 
 template <int ACTIVE>
 __global__ void k_dfma_probe(double* out, int iters, double a, double b) {
+  IB_GRID_DEP_WAIT();
   if ((int)(threadIdx.x & 31) >= ACTIVE) return;
   double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
   for (int i = 0; i < iters; ++i) {
@@ -20,6 +21,7 @@ __global__ void k_dfma_probe(double* out, int iters, double a, double b) {
 }
 
 __global__ void k_ffma_probe(float* out, int iters, float a, float b) {
+  IB_GRID_DEP_WAIT();
   float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
   for (int i = 0; i < iters; ++i) {
     x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
@@ -29,6 +31,7 @@ __global__ void k_ffma_probe(float* out, int iters, float a, float b) {
 }
 
 __global__ void k_imad_probe(unsigned* out, int iters, unsigned a, unsigned b) {
+  IB_GRID_DEP_WAIT();
   unsigned x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
   for (int i = 0; i < iters; ++i) {
     x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
@@ -89,6 +92,7 @@ int probe_fp64(double* tflops) { return probe_throughput(0, tflops); }
 // [7] warp shuffle + FP64 add, [8] CTA barrier.
 namespace cgp = cooperative_groups;
 __global__ void __cluster_dims__(8, 1, 1) k_latency_probe(long long* out, double a, double b, int n) {
+  IB_GRID_DEP_WAIT();
   cgp::cluster_group cl = cgp::this_cluster();
   __shared__ double buf[64];
   const int tid = threadIdx.x;

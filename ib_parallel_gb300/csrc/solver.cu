@@ -929,6 +929,37 @@ static void step_acc(Ctx* c, int ph, int a, int b) {
   if (cudaEventElapsedTime(&t, c->step_ev[a], c->step_ev[b]) == cudaSuccess) c->step_ms[ph] += t;
 }
 
+// Turns every ordinary kernel-to-kernel edge of a captured graph into a programmatic one: the
+// dependent kernel may be scheduled while its predecessor finishes (every kernel here starts
+// with IB_GRID_DEP_WAIT).  Edges to or from other nodes keep full serialisation.  An edge the
+// driver refuses to convert is put back as it was.
+static void make_edges_programmatic(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return;
+  }
+  std::vector<cudaGraphNode_t> from(n), to(n);
+  std::vector<cudaGraphEdgeData> ed(n);
+  if (cudaGraphGetEdges(g, from.data(), to.data(), ed.data(), &n) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType ta, tb;
+    if (cudaGraphNodeGetType(from[i], &ta) != cudaSuccess || cudaGraphNodeGetType(to[i], &tb) != cudaSuccess) continue;
+    if (ta != cudaGraphNodeTypeKernel || tb != cudaGraphNodeTypeKernel) continue;
+    if (ed[i].type != cudaGraphDependencyTypeDefault || ed[i].from_port != cudaGraphKernelNodePortDefault) continue;
+    cudaGraphEdgeData e = {};
+    e.from_port = cudaGraphKernelNodePortProgrammatic;
+    e.type = cudaGraphDependencyTypeProgrammatic;
+    if (cudaGraphRemoveDependencies(g, &from[i], &to[i], &ed[i], 1) != cudaSuccess) continue;
+    if (cudaGraphAddDependencies(g, &from[i], &to[i], &e, 1) != cudaSuccess)
+      cudaGraphAddDependencies(g, &from[i], &to[i], &ed[i], 1);
+  }
+  cudaGetLastError();
+}
+
 // Runs one fixed phase of the step (the same kernels on the same buffers every step) through a
 // CUDA graph captured on first use, which removes the gaps between its dependent launches.
 // If capture fails the phase runs directly from then on.
@@ -953,6 +984,7 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
       ph.passes[i] = c->n_pass[i] - p0[i];
       c->n_pass[i] = p0[i];
     }
+    if (rc == IB_OK && e == cudaSuccess) make_edges_programmatic(graph);
     if (rc != IB_OK || e != cudaSuccess || cudaGraphInstantiate(&ph.exec, graph, 0) != cudaSuccess) {
       cudaGetLastError();
       if (graph) cudaGraphDestroy(graph);
@@ -970,6 +1002,7 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
 
 // ------------------------------------------------------------- FSI iterations on the device
 __global__ void k_fsi_loop_init(int* cnt) {
+  IB_GRID_DEP_WAIT();
   if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
 }
 
@@ -981,6 +1014,7 @@ __global__ void k_fsi_loop_init(int* cnt) {
 __global__ void k_fsi_loop_cond(int* cnt, const int* __restrict__ ist, const double* __restrict__ err,
                                 const int* __restrict__ band_flag, double tol, int max_it,
                                 cudaGraphConditionalHandle h) {
+  IB_GRID_DEP_WAIT();
   if (threadIdx.x != 0) return;
   const double e = err[0];
   const int n = cnt[0] + 1;
@@ -1042,6 +1076,10 @@ static int build_fsi_loop(Ctx* c) {
       c->st = st;
     }
     if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+    if (rc == IB_OK) {
+      make_edges_programmatic(body);
+      make_edges_programmatic(graph);
+    }
     if (rc == IB_OK && cudaGraphInstantiate(&c->graph_fsi_loop.exec, graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
   } while (false);
   c->st = st;

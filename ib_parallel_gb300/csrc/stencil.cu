@@ -44,11 +44,13 @@ __global__ void k_nonlinear(GridDims g, const double* __restrict__ om, const dou
                             const double* __restrict__ qx, const double* __restrict__ q0x,
                             const double* __restrict__ qy, const double* __restrict__ q0y,
                             double* __restrict__ nlx, double* __restrict__ nly) {
+  IB_GRID_DEP_WAIT();
   nonlinear_at(g, blockIdx.x * blockDim.x + threadIdx.x, om, bc, qx, q0x, qy, q0y, nlx, nly);
 }
 
 // Every level at once (blockIdx.y = level).
 __global__ void k_nonlinear_levels(GridDims g, NlBatch b) {
+  IB_GRID_DEP_WAIT();
   const int l = blockIdx.y;
   nonlinear_at(g, blockIdx.x * blockDim.x + threadIdx.x, b.om[l], b.bc[l], b.qx[l], b.q0x[l], b.qy[l], b.q0y[l],
                b.nlx[l], b.nly[l]);
@@ -68,10 +70,12 @@ __device__ __forceinline__ void rot_at(const GridDims& g, int t, const double* _
 }
 __global__ void k_rot(GridDims g, const double* __restrict__ hx, const double* __restrict__ hy,
                       double* __restrict__ vort) {
+  IB_GRID_DEP_WAIT();
   rot_at(g, blockIdx.x * blockDim.x + threadIdx.x, hx, hy, vort);
 }
 // Every level at once (blockIdx.y = level): level l from b.nlx[l], b.nly[l] into b.out[l].
 __global__ void k_rot_levels(GridDims g, NlBatch b) {
+  IB_GRID_DEP_WAIT();
   const int l = blockIdx.y;
   rot_at(g, blockIdx.x * blockDim.x + threadIdx.x, b.nlx[l], b.nly[l], b.out[l]);
 }
@@ -80,6 +84,7 @@ __global__ void k_rot_levels(GridDims g, NlBatch b) {
 // curl_int + curl_bc (operators_fluid.F90:423-471), s ghosts from the ring.
 __global__ void k_curl(GridDims g, const double* __restrict__ s, const double* __restrict__ sbc,
                        double* __restrict__ qx, double* __restrict__ qy) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < g.nu) {
     int i = t % g.nux + 1, j = t / g.nux + 1;
@@ -93,6 +98,7 @@ __global__ void k_curl(GridDims g, const double* __restrict__ s, const double* _
 
 // The same for every level at once (blockIdx.y = level).
 __global__ void k_curl_levels(GridDims g, CurlBatch cb) {
+  IB_GRID_DEP_WAIT();
   const int l = blockIdx.y;
   const double* __restrict__ s = cb.s[l];
   const double* __restrict__ sbc = cb.sbc[l];
@@ -112,6 +118,7 @@ __global__ void k_curl_levels(GridDims g, CurlBatch cb) {
 // at odd fine points I=3..m-1, J=3..n-1 overwrites coarse point
 // ((I-1)/2+m/4+1, (J-1)/2+n/4+1).
 __global__ void k_coarsify(GridDims g, const double* __restrict__ fine, double* __restrict__ coarse) {
+  IB_GRID_DEP_WAIT();
   int cx = g.m / 2 - 1, cy = g.n / 2 - 1;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cx * cy) return;
@@ -128,6 +135,7 @@ __global__ void k_coarsify(GridDims g, const double* __restrict__ fine, double* 
 // operators_fluid.F90:475-535 with grid.F90:1091-1140: coarse values on the
 // fine boundary; coincident points copied, midpoints averaged; times fac.
 __global__ void k_get_bc(GridDims g, const double* __restrict__ s, double fac, double* __restrict__ ring) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.nbc) return;
   ring[t] = ring_value(s, g, t) * fac;
@@ -136,6 +144,7 @@ __global__ void k_get_bc(GridDims g, const double* __restrict__ s, double fac, d
 // The same for every level at once (blockIdx.y = level): ring l from field src[l], or zero
 // where src[l] is null.
 __global__ void k_get_bc_levels(GridDims g, RingBatch rb, double fac) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int l = blockIdx.y;
   if (t >= g.nbc) return;
@@ -146,6 +155,7 @@ __global__ void k_get_bc_levels(GridDims g, RingBatch rb, double fac) {
 // ------------------------------------------------------------- apply_bc
 // operators_fluid.F90:539-549 in place: left, right, bottom, top.
 __global__ void k_apply_bc(GridDims g, double* __restrict__ v, const double* __restrict__ ring, double fac) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.ns) return;
   int I = t % g.nsx + 2, J = t / g.nsx + 2;
@@ -161,6 +171,7 @@ __global__ void k_apply_bc(GridDims g, double* __restrict__ v, const double* __r
 // rhsbc = 0; apply_bc(rhsbc, a, f); apply_bc(rhsbc, b, f)   (timestepper.F90:184-189)
 __global__ void k_rhsbc(GridDims g, double* __restrict__ v, const double* __restrict__ ra,
                         const double* __restrict__ rb, double fac) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.ns) return;
   int I = t % g.nsx + 2, J = t / g.nsx + 2;
@@ -182,14 +193,17 @@ __global__ void k_rhsbc(GridDims g, double* __restrict__ v, const double* __rest
 // -------------------------------------------------------- vector helpers
 __global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
                         double* __restrict__ z) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) z[t] = a * x[t] + b * y[t];
 }
 __global__ void k_sub(int n, const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ z) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) z[t] = x[t] - y[t];
 }
 __global__ void k_fill(int n, double v, double* __restrict__ z) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) z[t] = v;
 }

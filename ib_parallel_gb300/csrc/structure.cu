@@ -33,6 +33,7 @@ __device__ double block_sum(double v) {
 // b_times2 (operators_struct.F90:14-127): y += BR (BR . x)/K_eff * (delta^2/ds/dt)(2 ds/dt)
 __global__ void k_tors_btimes(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
                               const double* __restrict__ x, double* __restrict__ y) {
+  IB_GRID_DEP_WAIT();
   TorsBody b = tb[blockIdx.x];
   double sn = s.sinv[blockIdx.x], cs = s.cosv[blockIdx.x];
   double part = 0.0;
@@ -45,6 +46,7 @@ __global__ void k_tors_btimes(const TorsBody* __restrict__ tb, TorsState s, doub
 // compute_rhs (operators_struct.F90:342-398): y = BR * delta*(r_theta - J r_phi - thetad)
 __global__ void k_tors_rhs(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
                            double* __restrict__ y) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x;
   TorsBody b = tb[t];
   double th = s.theta[t], th0 = s.theta0[t], thd = s.thetad[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
@@ -62,6 +64,7 @@ __global__ void k_tors_rhs(const TorsBody* __restrict__ tb, TorsState s, double 
 __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
                           const double* __restrict__ f, double* __restrict__ xb, double* __restrict__ yb,
                           double* __restrict__ err_per_body, double* __restrict__ err_max) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x;
   TorsBody b = tb[t];
   double th = s.theta[t], th0 = s.theta0[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
@@ -99,6 +102,7 @@ __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double d
 }
 
 __global__ void k_max_reduce(int n, const double* __restrict__ v, double* out) {
+  IB_GRID_DEP_WAIT();
   double m = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, v[i]);
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -108,6 +112,7 @@ __global__ void k_max_reduce(int n, const double* __restrict__ v, double* out) {
 // initial_acc (operators_struct.F90:233-294)
 __global__ void k_tors_initial_acc(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
                                    const double* __restrict__ f) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x;
   TorsBody b = tb[t];
   double th = s.theta[t];
@@ -123,6 +128,7 @@ __global__ void k_tors_initial_acc(const TorsBody* __restrict__ tb, TorsState s,
 }
 
 __global__ void k_tors_trig(int nt, const TorsBody* __restrict__ tb, TorsState s) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
   double g = tb[t].gamma0 - s.theta[t];
@@ -131,6 +137,7 @@ __global__ void k_tors_trig(int nt, const TorsBody* __restrict__ tb, TorsState s
 }
 
 __global__ void k_tors_save(int nt, TorsState s) {
+  IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
   s.theta0[t] = s.theta[t];

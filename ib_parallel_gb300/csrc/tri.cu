@@ -94,6 +94,7 @@ int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, doub
 // running a 2(C-1)-step recurrence while the rest of its warp idles (an FP64 warp
 // instruction costs the same issue time whatever its active lanes).
 __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb) {
+  IB_GRID_DEP_WAIT();
   extern __shared__ double sm[];
   const int C = op.C, s = op.s, d = s + 1, nx = op.nx, ny = op.ny;
   const int m = C > 1 ? C - 1 : 1;
@@ -210,6 +211,7 @@ __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld,
 constexpr int kTriMaxM = 31;   // interfaces (C-1) the register prefetch holds
 template <int S>
 __global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb) {
+  IB_GRID_DEP_WAIT();
   extern __shared__ double sm[];
   const int C = op.C, d = S + 1, nx = op.nx;
   const int m = C > 1 ? C - 1 : 1;
