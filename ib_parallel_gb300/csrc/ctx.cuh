@@ -109,6 +109,9 @@ struct Ctx {
   std::vector<double*> mv_w, mv_s, mv_qx, mv_qy;
   // vort2flux: per-level mode-space fields and the ring each level receives
   std::vector<double*> hat, ringv;
+  // per level: the boundary terms its solve adds (TriBc: ring end sums, edge-row transforms)
+  std::vector<double*> sdv, edgev;
+  double* emat = nullptr;          // edge matrix (dst_edge_matrix), (m-1) x (m-1)
   // row treatments of the Schur operator's partial transforms (per vertex row)
   unsigned char *rm_top = nullptr, *rm_coarse = nullptr, *rm_fine = nullptr, *rm_ring2 = nullptr;
   double* wmat = nullptr;          // DST-I matrix of the x transform ((m-1) x (m-1))

@@ -497,17 +497,10 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
   }
 }
 
-// Selected points of an inverse x transform, one warp per point.
-__global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, const int2* __restrict__ pts, int npts,
-                             const double* __restrict__ W, double* __restrict__ out) {
-  IB_GRID_DEP_WAIT();
-  int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (gw >= npts) return;
-  int2 rc = pts[gw];
-  const double* sr = spec + (size_t)rc.x * ld;
-  const double* wc = W + (size_t)rc.y * N;
-  // four accumulators (k = lane + 32(4t + a)) keep four loads per operand in flight
+// sum_k sr[k] wc[k] over k < N on one warp (the lane's partial sums, not yet reduced): four
+// accumulators (k = lane + 32(4t + a)) keep four loads per operand in flight.
+__device__ __forceinline__ double warp_dot_part(const double* __restrict__ sr, const double* __restrict__ wc, int N,
+                                                int lane) {
   double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
   int k = lane;
   for (; k + 96 < N; k += 128) {
@@ -519,8 +512,23 @@ __global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, con
   if (k < N) a0 = fma(sr[k], wc[k], a0);
   if (k + 32 < N) a1 = fma(sr[k + 32], wc[k + 32], a1);
   if (k + 64 < N) a2 = fma(sr[k + 64], wc[k + 64], a2);
-  double acc = (a0 + a1) + (a2 + a3);
+  return (a0 + a1) + (a2 + a3);
+}
+
+__device__ __forceinline__ double warp_sum(double acc) {
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
+// Selected points of an inverse x transform, one warp per point.
+__global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, const int2* __restrict__ pts, int npts,
+                             const double* __restrict__ W, double* __restrict__ out) {
+  IB_GRID_DEP_WAIT();
+  int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (gw >= npts) return;
+  int2 rc = pts[gw];
+  const double acc = warp_sum(warp_dot_part(spec + (size_t)rc.x * ld, W + (size_t)rc.y * N, N, lane));
   if (lane == 0) out[(size_t)rc.x * ld + rc.y] = acc;
 }
 
@@ -561,22 +569,9 @@ __global__ void __launch_bounds__(32 * kRingWarps) k_ring_modes(int N, GridDims 
       J = side == 2 ? g.n / 4 + 1 : 3 * g.n / 4 + 1;
       I = g.m / 4 + 1 + q;
     }
-    const double* sr = spec + (size_t)(J - 2) * ld;
-    const double* wc = W + (size_t)(I - 2) * N;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    int k = lane;
-    for (; k + 96 < N; k += 128) {
-      a0 = fma(sr[k], wc[k], a0);
-      a1 = fma(sr[k + 32], wc[k + 32], a1);
-      a2 = fma(sr[k + 64], wc[k + 64], a2);
-      a3 = fma(sr[k + 96], wc[k + 96], a3);
-    }
-    if (k < N) a0 = fma(sr[k], wc[k], a0);
-    if (k + 32 < N) a1 = fma(sr[k + 32], wc[k + 32], a1);
-    if (k + 64 < N) a2 = fma(sr[k + 64], wc[k + 64], a2);
-    acc = (a0 + a1) + (a2 + a3);
+    acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  acc = warp_sum(acc);
   if (lane == 0) sp[warp] = acc;
   __syncthreads();
   if ((int)threadIdx.x < kRingSeg) {
@@ -596,6 +591,152 @@ int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec
   count_launch();
   k_ring_modes<<<2 * (nlr + nbt), 32 * kRingWarps, 0, st>>>(px.N, g, spec, ld, W, fac, ring);
   IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+// The same ring, and with it what the finer level's solve adds to its right-hand side modes
+// (the boundary terms of apply_bc, operators_fluid.F90:539-549, transformed along x):
+//  - sd[r] = x_1 + x_N and sd[nsy + r] = x_1 - x_N of its row r, the ring's left and right
+//    entries r+1 (closed form 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) of every row's two end values);
+//  - edge[k] and edge[N + k]: the x transform of the ring's bottom and top entries 1..m-1,
+//    which is fac E s_J, E the edge matrix and s_J the coarse modes of the row get_bc reads.
+// CTAs [0, nlr): 16 entries of both the left and the right side (9 coarse vertices each);
+// [nlr, nlr + 2 nbt): 32 entries of the bottom or top side, as k_ring_modes; then one warp per
+// mode k for the two edge dot products.
+constexpr int kReWarps = 18;
+constexpr int kReLrSeg = 16;
+__global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, const double* __restrict__ spec,
+                                                             int ld, const double* __restrict__ W,
+                                                             const double* __restrict__ E, double fac,
+                                                             double* __restrict__ ring, double* __restrict__ sd,
+                                                             double* __restrict__ edge, int nlr, int nbt) {
+  IB_GRID_DEP_WAIT();
+  __shared__ double sp[kReWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int b = blockIdx.x;
+  if (b < nlr) {
+    constexpr int nq = kReLrSeg / 2 + 1;   // coarse vertices per side
+    const int len = g.n + 1, qmax = (len - 1) / 2;
+    const int q0 = b * (kReLrSeg / 2);
+    const int side = warp < nq ? 0 : 1;
+    const int q = q0 + warp - side * nq;
+    double acc = 0.0;
+    if (warp < 2 * nq && q <= qmax) {
+      const int I = side == 0 ? g.m / 4 + 1 : 3 * g.m / 4 + 1;
+      const int J = g.n / 4 + 1 + q;
+      acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) sp[warp] = acc;
+    __syncthreads();
+    if ((int)threadIdx.x < kReLrSeg) {
+      const int p = b * kReLrSeg + (int)threadIdx.x;
+      if (p < len) {
+        const int qq = p / 2 - q0;
+        const double vl = (p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq];
+        const double vr = (p & 1) ? 0.5 * (sp[nq + qq] + sp[nq + qq + 1]) : sp[nq + qq];
+        const double xl = vl * fac, xr = vr * fac;
+        ring[g.left + p] = xl;
+        ring[g.right + p] = xr;
+        const int r = p - 1;
+        if (r >= 0 && r < g.nsy) {
+          sd[r] = xl + xr;
+          sd[g.nsy + r] = xl - xr;
+        }
+      }
+    }
+    return;
+  }
+  b -= nlr;
+  if (b < 2 * nbt) {
+    constexpr int nq = kRingSeg / 2 + 1;
+    const int side = b / nbt, c = b - side * nbt;
+    const int len = g.m + 1, qmax = (len - 1) / 2;
+    const int q0 = c * (kRingSeg / 2);
+    const int q = q0 + warp;
+    double acc = 0.0;
+    if (warp < nq && q <= qmax) {
+      const int J = side == 0 ? g.n / 4 + 1 : 3 * g.n / 4 + 1;
+      const int I = g.m / 4 + 1 + q;
+      acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) sp[warp] = acc;
+    __syncthreads();
+    if ((int)threadIdx.x < kRingSeg) {
+      const int p = c * kRingSeg + (int)threadIdx.x;
+      if (p < len) {
+        const int qq = p / 2 - q0;
+        const double v = (p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq];
+        ring[(side == 0 ? g.bottom : g.top) + p] = v * fac;
+      }
+    }
+    return;
+  }
+  b -= 2 * nbt;
+  const int k = b * kReWarps + warp;
+  if (k >= N) return;
+  const double* ek = E + (size_t)k * N;
+  const double* s0 = spec + (size_t)(g.n / 4 - 1) * ld;       // J = n/4 + 1
+  const double* s1 = spec + (size_t)(3 * g.n / 4 - 1) * ld;   // J = 3n/4 + 1
+  double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+  int j = lane;
+  for (; j + 32 < N; j += 64) {
+    const double e0 = ek[j], e1 = ek[j + 32];
+    a0 = fma(e0, s0[j], a0);
+    b0 = fma(e0, s1[j], b0);
+    a1 = fma(e1, s0[j + 32], a1);
+    b1 = fma(e1, s1[j + 32], b1);
+  }
+  if (j < N) {
+    a0 = fma(ek[j], s0[j], a0);
+    b0 = fma(ek[j], s1[j], b0);
+  }
+  a0 = warp_sum(a0 + a1);
+  b0 = warp_sum(b0 + b1);
+  if (lane == 0) {
+    edge[k] = fac * a0;
+    edge[N + k] = fac * b0;
+  }
+}
+
+int dst_ring_edge_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W,
+                             const double* E, double fac, double* ring, double* sd, double* edge, cudaStream_t st) {
+  const int nlr = cdiv(g.n + 1, kReLrSeg), nbt = cdiv(g.m + 1, kRingSeg);
+  count_launch();
+  k_ring_edge<<<nlr + 2 * nbt + cdiv(px.N, kReWarps), 32 * kReWarps, 0, st>>>(px.N, g, spec, ld, W, E, fac, ring, sd,
+                                                                              edge, nlr, nbt);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+// E[k][k'] = sum_j W[k][j] P(j, k'), P(j, .) the row of W at the coarse vertex get_bc puts on
+// entry p = j+1 of a side (I = m/4 + 1 + p/2 for even p, the mean of two for odd p).  One
+// thread per entry; compensated dot product (Ogita, Rump and Oishi's Dot2: error-free product
+// by fma and Knuth's two-sum), so E is close to the exact product of the tabulated W.
+__global__ void k_edge_matrix(int N, int mq, const double* __restrict__ W, double* __restrict__ E) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)N * N) return;
+  const int k = (int)(idx / N), kp = (int)(idx - (long long)k * N);
+  const double* wk = W + (size_t)k * N;
+  double sum = 0.0, comp = 0.0;
+  for (int j = 0; j < N; ++j) {
+    const int p = j + 1, r0 = mq - 1 + p / 2;
+    const double pw = (p & 1) ? 0.5 * (W[(size_t)r0 * N + kp] + W[(size_t)(r0 + 1) * N + kp]) : W[(size_t)r0 * N + kp];
+    const double a = wk[j];
+    const double h = a * pw, l = fma(a, pw, -h);
+    const double t = sum + h, z = t - sum;
+    comp += ((sum - (t - z)) + (h - z)) + l;
+    sum = t;
+  }
+  E[idx] = sum + comp;
+}
+
+int dst_edge_matrix(const DstPlan& px, const GridDims& g, const double* W, double* E) {
+  const long long n = (long long)px.N * px.N;
+  k_edge_matrix<<<(unsigned)cdiv(n, 256), 256>>>(px.N, g.m / 4, W, E);
+  IB_CUDA_CHECK(cudaGetLastError());
+  IB_CUDA_CHECK(cudaDeviceSynchronize());
   return IB_OK;
 }
 

@@ -120,6 +120,16 @@ int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, con
 // evaluated at the points get_bc reads only (dot products with W).
 int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W, double fac,
                         double* ring, cudaStream_t st);
+// The same ring, plus the boundary terms the finer level's solve adds to its right-hand side
+// modes (tri_solve's TriBc): sd (2 x nsy) the sums and differences of the ring's left and right
+// entries 1..n-1, edge (2 x N) the x transforms of its bottom and top entries 1..m-1, from the
+// edge matrix E (dst_edge_matrix) and the coarse modes of the two rows get_bc reads.
+int dst_ring_edge_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W,
+                             const double* E, double fac, double* ring, double* sd, double* edge, cudaStream_t st);
+// E = W P (N x N, device): P maps the coarse modes of one row to the get_bc values on entries
+// 1..m-1 of a finer level's bottom or top side, so W P maps them to that side's x transform.
+// Computed on the device at set-up (synchronous).
+int dst_edge_matrix(const DstPlan& px, const GridDims& g, const double* W, double* E);
 // sk2[k-1] = 2 sin(pi k/M), k = 1..N, into N doubles of device memory.
 int dst_sin2_table(const DstPlan& px, double* dev_out);
 size_t dst_smem_y(const DstPlan& p, int B, DstYMode mode);

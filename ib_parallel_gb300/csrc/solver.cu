@@ -206,6 +206,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)g.m + g.n + 8;                          // get_bc points, edge rows
   dbl += (size_t)(L + 3) * nbc;                          // rings
   dbl += (size_t)L * ns + (size_t)L * nbc + 2 * L;       // per-level spectra and rings (vort2flux)
+  dbl += (size_t)g.nsx * g.nsx + (size_t)L * (2 * (size_t)g.nsy + 2 * (size_t)g.nsx);   // edge matrix, terms
   dbl += 7 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
   dbl += 8 * (size_t)nt + nt + 3;
   dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 4 * (size_t)nf + 2;
@@ -241,6 +242,9 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->omegabc = P.take<double>(nbc); c->sbc = P.take<double>(nbc); c->zero_ring = P.take<double>(nbc);
   c->hat.resize(L); c->ringv.resize(L);
   for (int k = 0; k < L; ++k) { c->hat[k] = P.take<double>(ns); c->ringv[k] = P.take<double>(nbc); }
+  c->emat = P.take<double>((size_t)g.nsx * g.nsx);
+  c->sdv.resize(L); c->edgev.resize(L);
+  for (int k = 0; k < L; ++k) { c->sdv[k] = P.take<double>(2 * (size_t)g.nsy); c->edgev[k] = P.take<double>(2 * (size_t)g.nsx); }
   c->f = P.take<double>(nf); c->f_rdst = P.take<double>(nf); c->xb = P.take<double>(nf);
   c->yb = P.take<double>(nf); c->rhsf = P.take<double>(nf); c->tmpf = P.take<double>(nf);
   c->tmpf2 = P.take<double>(nf); c->forces = P.take<double>(2 * nbody + 1);
@@ -336,6 +340,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     IB_CUDA_CHECK(cudaMemcpy(c->edge_rows, er, sizeof(er), cudaMemcpyHostToDevice));
     int rc3 = dst_matrix_table(c->px, c->wmat);
     if (rc3 == IB_OK) rc3 = dst_sin2_table(c->px, c->sk2);
+    if (rc3 == IB_OK && L > 1) rc3 = dst_edge_matrix(c->px, g, c->wmat, c->emat);
     if (rc3 != IB_OK) { *msg = "DST matrix upload failed"; ctx_destroy(c); return rc3; }
   }
 
@@ -487,6 +492,23 @@ int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs
 
 static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring, double fac = 1.0);
 
+// The boundary terms level k's solve adds: from its ring, left by level k+1.
+static TriBc level_bc(Ctx* c, int k, double post_scale) {
+  TriBc bc;
+  bc.sk2 = c->sk2;
+  bc.sd = c->sdv[k];
+  bc.edge = c->edgev[k];
+  bc.post_scale = post_scale;
+  return bc;
+}
+
+// Level k's ring (fac * get_bc of the coarser level's streamfunction or vorticity, from its
+// modes spec) and the boundary terms of its solve.
+static int ring_edge_from_modes(Ctx* c, const double* spec, int k, double fac) {
+  return dst_ring_edge_from_modes(c->px, c->g, spec, c->g.nsx, c->wmat, c->emat, fac, c->ringv[k], c->sdv[k],
+                                  c->edgev[k], c->st);
+}
+
 // vort2flux (operators_fluid.F90:237-377).  all_levels=false writes the streamfunction and the
 // fluxes of the finest level only (the coarser levels' vorticity is still coarsified and their
 // modes still give the finest level its boundary values).
@@ -520,16 +542,15 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
   }
   for (int k = L - 1; k >= 0; --k) {
     double* F = k == 0 ? F0 : c->hat[k];
-    if (k < L - 1) {
-      // boundary terms from the ring of level k (get_bc of level k+1), apply_bc with fac 1
-      RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, c->hat[k], k == 0 && skip0 ? 2.0 * g.m : 1.0, F,
-                        st));
-    }
+    // boundary terms of the ring of level k (get_bc of level k+1), apply_bc with fac 1, added
+    // by the solve as it loads its right-hand side
+    TriBc bc;
+    if (k < L - 1) bc = level_bc(c, k, k == 0 && skip0 ? 2.0 * g.m : 1.0);
     {
       ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-      RC(tri_solve(c->tri_ctci, F, F, g.nsx, c->tl, st));
+      RC(tri_solve(c->tri_ctci, c->hat[k], F, g.nsx, c->tl, st, bc));
     }
-    if (k > 0) RC(ring_from_modes(c, F, s[k], c->ringv[k - 1]));
+    if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 1.0));
   }
   if (!all_levels) {
     DstXArgs a;
@@ -1145,13 +1166,15 @@ static int op_predict_levels(Ctx* c, bool seed_rhs_old) {
   }
   for (int k = L - 1; k >= 0; --k) {
     double* F = c->hat[k];
-    // the second ring: ringv[k] = vfac[k] * 0.25 get_bc(omega_{k+1}), left by level k+1
-    if (k < L - 1) RC(dst_x_bc_modes(c->px, g, c->ringv[k], c->wmat, c->sk2, F, 1.0, F, st));
+    // the second ring: ringv[k] = vfac[k] * 0.25 get_bc(omega_{k+1}), left by level k+1 with
+    // its boundary terms, added by the solve
+    TriBc bc;
+    if (k < L - 1) bc = level_bc(c, k, 1.0);
     {
       ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-      RC(tri_solve(c->tri_pred[k], F, F, g.nsx, c->tl, st));
+      RC(tri_solve(c->tri_pred[k], F, F, g.nsx, c->tl, st, bc));
     }
-    if (k > 0) RC(ring_from_modes(c, F, c->spec2, c->ringv[k - 1], 0.25 * c->vfac[k - 1]));
+    if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 0.25 * c->vfac[k - 1]));
   }
   DstXArgs b;
   b.nlev = L;

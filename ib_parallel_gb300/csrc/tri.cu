@@ -86,6 +86,17 @@ int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, doub
   return IB_OK;
 }
 
+// Row r of mode k's right-hand side with the boundary terms (TriBc).
+__device__ __forceinline__ double tri_rhs(const TriBc& b, int ny, int nx, int r, int k, double f) {
+  double v = b.post_scale == 1.0 ? f : b.post_scale * f;
+  if (b.sd) {
+    v = fma(__ldg(b.sk2 + k), b.sd[(k & 1) * ny + r], v);
+    if (r == 0) v += b.edge[k];
+    if (r == ny - 1) v += b.edge[nx + k];
+  }
+  return v;
+}
+
 // One CTA: Mb consecutive modes x C chunks (thread t: mode t % Mb, chunk t / Mb, so a warp
 // holds 32/Mb chunks of Mb modes).  The CTA's ny x Mb tile and its factor tables are staged
 // in shared memory, so the sequential recurrences run on shared-memory latency.  The
@@ -93,7 +104,7 @@ int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, doub
 // thread forms one of them with C-1 independent products, instead of one thread per mode
 // running a 2(C-1)-step recurrence while the rest of its warp idles (an FP64 warp
 // instruction costs the same issue time whatever its active lanes).
-__global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb) {
+__global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb, TriBc bc) {
   IB_GRID_DEP_WAIT();
   extern __shared__ double sm[];
   const int C = op.C, s = op.s, d = s + 1, nx = op.nx, ny = op.ny;
@@ -126,7 +137,7 @@ __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld,
       for (int u = 0; u < 8; ++u) {
         int rr = r + u * rstep;
         v[u] = 0.0;
-        if (rr < ny) { if (kin) v[u] = src[(size_t)rr * ld]; }
+        if (rr < ny) { if (kin) v[u] = tri_rhs(bc, ny, nx, rr, k0 + kl0, src[(size_t)rr * ld]); }
         else if (rr < tot) v[u] = __ldg(tsrc + (size_t)(rr - ny) * nx);
       }
 #pragma unroll
@@ -210,7 +221,8 @@ __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld,
 // writes only the rows it read, after the CTA's barriers.
 constexpr int kTriMaxM = 31;   // interfaces (C-1) the register prefetch holds
 template <int S>
-__global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb) {
+__global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb,
+                                                 TriBc bc) {
   IB_GRID_DEP_WAIT();
   extern __shared__ double sm[];
   const int C = op.C, d = S + 1, nx = op.nx;
@@ -230,7 +242,25 @@ __global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restr
   double f[S];
 #pragma unroll
   for (int j = 0; j < S; ++j) f[j] = chunk ? F[(size_t)(r0 + j) * ld + k] : 0.0;
-  const double fi = (chunk && c >= 1) ? F[(size_t)(r0 - 1) * ld + k] : 0.0;
+  double fi = (chunk && c >= 1) ? F[(size_t)(r0 - 1) * ld + k] : 0.0;
+  if (chunk && (bc.sd || bc.post_scale != 1.0)) {
+    // boundary terms (tri_rhs) on the chunk rows and the interface row above; row 0 is chunk
+    // 0's first row and row ny-1 chunk C-1's last
+    const double ps = bc.post_scale;
+    if (bc.sd) {
+      const double a = __ldg(bc.sk2 + k);
+      const double* sdk = bc.sd + (k & 1) * op.ny;
+#pragma unroll
+      for (int j = 0; j < S; ++j) f[j] = fma(a, sdk[r0 + j], ps == 1.0 ? f[j] : ps * f[j]);
+      if (c >= 1) fi = fma(a, sdk[r0 - 1], ps == 1.0 ? fi : ps * fi);
+      if (c == 0) f[0] += bc.edge[k];
+      if (c == C - 1) f[S - 1] += bc.edge[nx + k];
+    } else {
+#pragma unroll
+      for (int j = 0; j < S; ++j) f[j] *= ps;
+      fi *= ps;
+    }
+  }
   double rr[kTriMaxM];
 #pragma unroll
   for (int j = 0; j < kTriMaxM; ++j)
@@ -303,13 +333,14 @@ static size_t tri_reg_smem(const TriOp& op, int Mb) {
 }
 
 template <int S>
-static int launch_tri_reg(const TriOp& op, const double* F, double* U, int ld, int Mb, int threads, cudaStream_t st) {
+static int launch_tri_reg(const TriOp& op, const double* F, double* U, int ld, int Mb, int threads, const TriBc& bc,
+                          cudaStream_t st) {
   const size_t smem = tri_reg_smem(op, Mb);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_tri_reg<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return IB_ERR_CUDA;
   count_launch();
-  k_tri_reg<S><<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb);
+  k_tri_reg<S><<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb, bc);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
@@ -319,7 +350,8 @@ size_t tri_smem(const TriOp& op, int Mb) {
   return sizeof(double) * (size_t)Mb * ((size_t)op.ny + 3 * (size_t)op.s + m * m + 2 * (size_t)op.C + 2 * ((size_t)op.C + 1));
 }
 
-int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaunch& L, cudaStream_t st) {
+int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaunch& L, cudaStream_t st,
+              const TriBc& bc) {
   int Mb = L.Mb;
   int threads = Mb * op.C;
   threads = ((threads + 31) / 32) * 32;
@@ -330,7 +362,7 @@ int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaun
     const int tr = ((Mr * op.C + 31) / 32) * 32;
     switch (op.s) {
 #define IB_TRI_REG(SS) \
-      case SS: return launch_tri_reg<SS>(op, F, U, ld, Mr, tr, st);
+      case SS: return launch_tri_reg<SS>(op, F, U, ld, Mr, tr, bc, st);
       IB_TRI_REG(1) IB_TRI_REG(2) IB_TRI_REG(3) IB_TRI_REG(4) IB_TRI_REG(5) IB_TRI_REG(6) IB_TRI_REG(7)
       IB_TRI_REG(8) IB_TRI_REG(9) IB_TRI_REG(11) IB_TRI_REG(12) IB_TRI_REG(14) IB_TRI_REG(15) IB_TRI_REG(19)
       IB_TRI_REG(23) IB_TRI_REG(24) IB_TRI_REG(29) IB_TRI_REG(31) IB_TRI_REG(39)
@@ -344,7 +376,7 @@ int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaun
       return IB_ERR_CUDA;
   }
   count_launch();
-  k_tri<<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb);
+  k_tri<<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb, bc);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -44,8 +44,20 @@ void tri_chunking(int n, int nx, int* s, int* C);
 // device memory of tri_table_doubles() doubles.
 size_t tri_table_doubles(int nx, int s, int C);
 int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, double* dev_mem);
-// In place (F may equal U): U = sigma * A^-1 F for every mode column.
-int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaunch& L, cudaStream_t st);
+// Boundary terms a solve adds to its right-hand side as it loads it (a finer level of the
+// coarse-to-fine recursions, dst_ring_edge_from_modes): row r of mode k is
+//     post_scale F[r][k] + sk2[k] sd[(k & 1) ny + r]  (+ edge[k] on row 0, + edge[nx + k] on row ny-1).
+// sd == nullptr: post_scale F only.
+struct TriBc {
+  const double* sk2 = nullptr;
+  const double* sd = nullptr;
+  const double* edge = nullptr;
+  double post_scale = 1.0;
+};
+
+// In place (F may equal U): U = sigma * A^-1 (F with the boundary terms bc) for every mode column.
+int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaunch& L, cudaStream_t st,
+              const TriBc& bc = TriBc());
 size_t tri_smem(const TriOp& op, int Mb);
 
 }  // namespace ib
