@@ -160,6 +160,7 @@ struct Ctx {
   // path; counters [0] iterations [1] Krylov iterations [2] operator products [3] band flag)
   PhaseGraph graph_fsi_loop;
   long long fsi_body_launches = 0;
+  long long fsi_post_launches = 0;
   int* fsi_cnt = nullptr;
   FusedPlan fused_plan;
   double* cholM = nullptr;         // nf x nf (num_stat)

@@ -219,14 +219,20 @@ __global__ void k_reg_scan(const int* __restrict__ bbox, int* cnt_x, int* cnt_y,
   }
 }
 
-int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
-                     double offy, RegDev& r, int* d_err, cudaStream_t st) {
+int launch_reg_weights(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
+                       double offy, RegDev& r, int* d_err, cudaStream_t st) {
   if (nf == 0) return IB_OK;
-  // bbox, lists and scan skip their work (return at once) unless a stencil origin moved
+  // launch_reg_lists skips its work (each kernel returns at once) unless a stencil origin moved
   IB_CUDA_CHECK(cudaMemsetAsync(r.stale, 0, sizeof(int), st));
   count_launch();
   k_reg_weights<<<cdiv(nf, 8), 128, 0, st>>>(g, nf, xb, yb, delta, offx, offy, r.comp, r.ix, r.iy, r.w, r.stale,
                                               d_err);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int launch_reg_lists(int nf, RegDev& r, const GridDims& g, cudaStream_t st) {
+  if (nf == 0) return IB_OK;
   count_launch();
   k_reg_bbox<<<1, 256, 0, st>>>(g, nf, r.ix, r.iy, r.bbox, r.stale);
   count_launch();
@@ -239,6 +245,12 @@ int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* 
                                              r.max_faces, r.stale);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
+}
+
+int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
+                     double offy, RegDev& r, int* d_err, cudaStream_t st) {
+  const int rc = launch_reg_weights(g, nf, xb, yb, delta, offx, offy, r, d_err, st);
+  return rc != IB_OK ? rc : launch_reg_lists(nf, r, g, st);
 }
 
 // E^T h0: every face of the box gets the ordered sum of weight*h0 over its list.

@@ -66,6 +66,11 @@ struct RegDev {
 
 int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
                      double offy, RegDev& r, int* d_err, cudaStream_t st);
+// The same in two parts: the origins and weights (and whether an origin moved), then the
+// bounding box and the contribution lists, which only E^T (reg, redistribution) reads.
+int launch_reg_weights(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
+                       double offy, RegDev& r, int* d_err, cudaStream_t st);
+int launch_reg_lists(int nf, RegDev& r, const GridDims& g, cudaStream_t st);
 // hx, hy must be zero outside the stencil box; this writes every face in the box.
 int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, double* hx, double* hy,
                cudaStream_t st);

@@ -1048,19 +1048,33 @@ __global__ void k_fsi_loop_cond(int* cnt, const int* __restrict__ ist, const dou
 }
 
 // Captures the graph of a step's FSI iterations: the counters reset, then a while node whose
-// body is one iteration on the assembled operator (right-hand side, assembly, the cluster
-// Krylov solve, redistribution, structure update, weights and patches at the new positions)
-// and the condition.  The body's launches are counted once (fsi_body_launches).
+// body is one iteration on the assembled operator, and after it the contribution lists of the
+// final positions.  The body runs its independent parts side by side:
+//     s1: assembly ----------------------> Krylov solve -> structure update --> weights,
+//     s2: right-hand side ----------------^            \-> redistribution --^   patches,
+//     s3: contribution lists of the current weights ------^                      condition
+// The lists (read only by E^T, i.e. the redistribution, and after the loop by the
+// correction) are rebuilt at the start of the iteration after the weights they belong to,
+// so they leave the chain from one solve to the next.  The body's launches are counted once
+// (fsi_body_launches), the lists after the loop in fsi_post_launches.
 static int build_fsi_loop(Ctx* c) {
   const GridDims& g = c->g;
   const IbParams& p = c->p;
   Influence& I = c->inf;
-  cudaStream_t st = c->st, s1 = nullptr;
-  IB_CUDA_CHECK(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+  cudaStream_t st = c->st, s1 = nullptr, s2 = nullptr, s3 = nullptr;
+  cudaEvent_t ev[5] = {};
   int rc = IB_OK;
+  if (cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking) != cudaSuccess)
+    rc = IB_ERR_CUDA;
+  for (int i = 0; i < 5 && rc == IB_OK; ++i)
+    if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess) rc = IB_ERR_CUDA;
+  cudaEvent_t ev_fork = ev[0], ev_rhs = ev[1], ev_lists = ev[2], ev_f = ev[3], ev_rd = ev[4];
   cudaGraph_t graph = nullptr;
   const long long l0 = launch_count();
   do {
+    if (rc != IB_OK) break;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
     count_launch();
     k_fsi_loop_init<<<1, 32, 0, st>>>(c->fsi_cnt);
@@ -1076,14 +1090,37 @@ static int build_fsi_loop(Ctx* c) {
       c->st = s1;
       const long long b0 = launch_count();
       auto iteration = [&]() -> int {
-        if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s1));
-        RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s1));
-        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s1));
+        IB_CUDA_CHECK(cudaEventRecord(ev_fork, s1));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_fork, 0));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s3, ev_fork, 0));
+        // s2: right-hand side
+        if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s2));
+        RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s2));
+        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s2));
+        IB_CUDA_CHECK(cudaEventRecord(ev_rhs, s2));
+        // s3: contribution lists of the current weights
+        RC(launch_reg_lists(c->nf, c->reg, g, s3));
+        IB_CUDA_CHECK(cudaEventRecord(ev_lists, s3));
+        // s1: assembly and solve
         RC(inf_assemble(c));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));
         RC(launch_gmres_fused(c->G, &c->fused_plan, I.St, c->rhsf, c->f, p.rtol, p.atol, p.gmres_max_it, s1));
-        RC(op_redistribute(c, c->f, c->f_rdst));
+        // s2: redistribution with the current weights, beside the structure update on s1
+        IB_CUDA_CHECK(cudaEventRecord(ev_f, s1));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_f, 0));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_lists, 0));
+        c->st = s2;
+        const int rrd = op_redistribute(c, c->f, c->f_rdst);
+        c->st = s1;
+        RC(rrd);
+        IB_CUDA_CHECK(cudaEventRecord(ev_rd, s2));
         RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, s1));
-        RC(op_reg_prep(c));
+        // weights and patches at the new positions (the weights overwrite what the
+        // redistribution reads)
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rd, 0));
+        I.patch_fresh = false;
+        I.active = false;
+        RC(launch_reg_weights(g, c->nf, c->xb, c->yb, c->delta, p.offsetx, p.offsety, c->reg, c->d_err, s1));
         RC(inf_patch(c));
         count_launch();
         k_fsi_loop_cond<<<1, 32, 0, s1>>>(c->fsi_cnt, c->G.ist, c->err_fsi, I.flag, p.fsi_tol, p.fsi_max_it, h);
@@ -1096,6 +1133,11 @@ static int build_fsi_loop(Ctx* c) {
       if (cudaStreamEndCapture(s1, &tmp) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
       c->st = st;
     }
+    if (rc == IB_OK) {
+      const long long a0 = launch_count();
+      rc = launch_reg_lists(c->nf, c->reg, g, st);
+      c->fsi_post_launches = launch_count() - a0;
+    }
     if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
     if (rc == IB_OK) {
       make_edges_programmatic(body);
@@ -1107,7 +1149,11 @@ static int build_fsi_loop(Ctx* c) {
   count_launches(-(launch_count() - l0));   // captured, not run
   cudaGetLastError();
   if (graph) cudaGraphDestroy(graph);
-  cudaStreamDestroy(s1);
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
+  if (s3) cudaStreamDestroy(s3);
+  if (s2) cudaStreamDestroy(s2);
+  if (s1) cudaStreamDestroy(s1);
   if (rc != IB_OK) {
     if (c->graph_fsi_loop.exec) cudaGraphExecDestroy(c->graph_fsi_loop.exec);
     c->graph_fsi_loop.exec = nullptr;
@@ -1231,7 +1277,7 @@ int op_advance(Ctx* c) {
           fsi_count = c->h_ist[0];
           c->ksp_iter += c->h_ist[1];
           c->n_matvec += c->h_ist[2];
-          count_launches(1 + c->fsi_body_launches * (long long)fsi_count);
+          count_launches(1 + c->fsi_body_launches * (long long)fsi_count + c->fsi_post_launches);
           I.assemblies += fsi_count;
           I.flag_h = c->h_ist[3];
           I.patch_fresh = true;
