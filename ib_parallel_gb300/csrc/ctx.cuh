@@ -160,6 +160,11 @@ struct Ctx {
   // path; counters [0] iterations [1] Krylov iterations [2] operator products [3] band flag)
   PhaseGraph graph_fsi_loop;
   long long fsi_body_launches = 0;
+  // origins and weights of the current positions, copied at the start of a device FSI
+  // iteration for its redistribution (the weights are rebuilt meanwhile)
+  int* reg_ix_s = nullptr;
+  int* reg_iy_s = nullptr;
+  double* reg_w_s = nullptr;
   long long fsi_post_launches = 0;
   int* fsi_cnt = nullptr;
   FusedPlan fused_plan;
@@ -228,9 +233,16 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
 // influence.cu
 int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
-int inf_patch(Ctx* c);                 // patches + flag for the current weights (async)
+// patches + flag for the current weights (async); cleared: the band flag and the touched-vertex
+// flags are already zero (the device FSI loop clears them as it reads them)
+int inf_patch(Ctx* c, bool cleared = false);
 int inf_prepare(Ctx* c);               // build/rebuild the band if needed, assemble S
 int inf_assemble(Ctx* c);              // the assembly kernels only
+// the same in parts: K P on the touched vertices (clear_used: clear the touched-vertex flags
+// as they are read), the B rows, P^T (K P) + B
+int inf_assemble_kp(Ctx* c, cudaStream_t st, bool clear_used);
+int inf_assemble_b(Ctx* c, cudaStream_t st);
+int inf_assemble_ptk(Ctx* c, cudaStream_t st);
 int inf_dense_mv(Ctx* c, const double* x, double* y);   // (S + B) x
 int inf_build(Ctx* c);
 int op_redistribute(Ctx* c, const double* f, double* frdst);

@@ -253,6 +253,26 @@ int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* 
   return rc != IB_OK ? rc : launch_reg_lists(nf, r, g, st);
 }
 
+__global__ void k_reg_snapshot(int nf, const int* __restrict__ ix, const int* __restrict__ iy,
+                               const double* __restrict__ w, int* ix_s, int* iy_s, double* w_s) {
+  IB_GRID_DEP_WAIT();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 49 * nf; i += gridDim.x * blockDim.x) {
+    w_s[i] = w[i];
+    if (i < nf) {
+      ix_s[i] = ix[i];
+      iy_s[i] = iy[i];
+    }
+  }
+}
+
+int launch_reg_snapshot(int nf, const RegDev& r, int* ix_s, int* iy_s, double* w_s, cudaStream_t st) {
+  if (nf == 0) return IB_OK;
+  count_launch();
+  k_reg_snapshot<<<cdiv(49LL * nf, 256), 256, 0, st>>>(nf, r.ix, r.iy, r.w, ix_s, iy_s, w_s);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
 // E^T h0: every face of the box gets the ordered sum of weight*h0 over its list.
 __global__ void k_reg(GridDims g, const double* __restrict__ h0, const double* __restrict__ w,
                       const int* __restrict__ bbox, const int* __restrict__ cnt_x, const int* __restrict__ cnt_y,
@@ -401,10 +421,11 @@ __global__ void k_redist_field(GridDims g, const double* __restrict__ f, const d
   }
 }
 
+// Writes the faces of the box that have contributions and leaves the others as they were:
+// every face a stencil reads has one (the stencil's own unknown), so E of the result
+// (launch_regT with the same weights) reads written faces only.
 int launch_redistribute_field(const GridDims& g, int nf, const double* f, const RegDev& r, double* fx,
                               double* fy, cudaStream_t st) {
-  IB_CUDA_CHECK(cudaMemsetAsync(fx, 0, sizeof(double) * g.nu, st));
-  IB_CUDA_CHECK(cudaMemsetAsync(fy, 0, sizeof(double) * g.nv, st));
   if (nf == 0) return IB_OK;
   count_launch();
   k_redist_field<<<152 * 2, 128, 0, st>>>(g, f, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, fx, fy,

@@ -62,9 +62,11 @@ __global__ void k_inf_patch(GridDims g, int nf, const int* __restrict__ comp, co
   if (fl) atomicOr(flag, fl);
 }
 
-// Compaction of the touched band vertices (one CTA of 1024 threads).
-__global__ void k_inf_compact(int nR, const int* __restrict__ used, int* __restrict__ ulist,
-                              int* __restrict__ upos, int* __restrict__ nu) {
+// Compaction of the touched band vertices (one CTA of 1024 threads).  clear: also clears the
+// flags it read, so the next k_inf_patch starts from zero (patches recomputed every iteration;
+// a stationary body's patches are computed once and their flags kept).
+__global__ void k_inf_compact(int nR, int* __restrict__ used, int* __restrict__ ulist,
+                              int* __restrict__ upos, int* __restrict__ nu, int clear) {
   IB_GRID_DEP_WAIT();
   __shared__ int wsum[32];
   __shared__ int base;
@@ -74,6 +76,7 @@ __global__ void k_inf_compact(int nR, const int* __restrict__ used, int* __restr
   for (int c0 = 0; c0 < nR; c0 += 1024) {
     const int i = c0 + tid;
     const int f = (i < nR && used[i]) ? 1 : 0;
+    if (f && clear) used[i] = 0;
     int x = f;
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -279,11 +282,13 @@ void inf_free(Ctx* c) {
   I = Influence{};
 }
 
-int inf_patch(Ctx* c) {
+int inf_patch(Ctx* c, bool cleared) {
   Influence& I = c->inf;
   if (c->nf == 0) return IB_OK;
-  IB_CUDA_CHECK(cudaMemsetAsync(I.flag, 0, sizeof(int), c->st));
-  if (I.built) IB_CUDA_CHECK(cudaMemsetAsync(I.used, 0, sizeof(int) * (size_t)I.nR, c->st));
+  if (!cleared) {
+    IB_CUDA_CHECK(cudaMemsetAsync(I.flag, 0, sizeof(int), c->st));
+    if (I.built) IB_CUDA_CHECK(cudaMemsetAsync(I.used, 0, sizeof(int) * (size_t)I.nR, c->st));
+  }
   count_launch();
   k_inf_patch<<<c->nf, kP, 0, c->st>>>(c->g, c->nf, c->reg.comp, c->reg.ix, c->reg.iy, c->reg.w,
                                        I.built ? I.tile_of : nullptr, I.ntx, I.pval, I.pidx, I.used, I.flag);
@@ -416,23 +421,40 @@ int inf_prepare(Ctx* c) {
 }
 
 // The assembly kernels alone (no host decisions): S, St from K and the current patches.
-int inf_assemble(Ctx* c) {
+int inf_assemble_kp(Ctx* c, cudaStream_t st, bool clear_used) {
   Influence& I = c->inf;
-  cudaStream_t st = c->st;
   count_launch();
-  k_inf_compact<<<1, 1024, 0, st>>>(I.nR, I.used, I.ulist, I.upos, I.nu);
+  k_inf_compact<<<1, 1024, 0, st>>>(I.nR, I.used, I.ulist, I.upos, I.nu, clear_used ? 1 : 0);
   count_launch();
   k_inf_kp<<<dim3(cdiv(I.nR, 128), c->nf), 128, 0, st>>>(I.nR, I.K, I.pval, I.pidx, I.ulist, I.nu, I.T);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int inf_assemble_b(Ctx* c, cudaStream_t st) {
+  Influence& I = c->inf;
   // -1: no B term (unknowns of rigid bodies; k_inf_bvec sets every torsional body's own)
   if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(I.bod, 0xff, sizeof(int) * (size_t)c->nf, st));
   if (c->nt > 0) {
     count_launch();
     k_inf_bvec<<<c->nt, 32, 0, st>>>(c->tb, c->ts, c->p.dt, c->delta, I.brv, I.bco, I.bod);
   }
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int inf_assemble_ptk(Ctx* c, cudaStream_t st) {
+  Influence& I = c->inf;
   count_launch();
   k_inf_ptk<<<c->nf, 128, 0, st>>>(c->nf, I.nR, I.pval, I.pidx, I.upos, I.T, I.brv, I.bco, I.bod, I.S, I.St);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
+}
+
+int inf_assemble(Ctx* c) {
+  RC(inf_assemble_kp(c, c->st, false));
+  RC(inf_assemble_b(c, c->st));
+  return inf_assemble_ptk(c, c->st);
 }
 
 // y = (S + B) x from the assembled column-major operator (B is part of it).

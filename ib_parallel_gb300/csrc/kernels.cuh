@@ -71,6 +71,8 @@ int launch_reg_build(const GridDims& g, int nf, const double* xb, const double* 
 int launch_reg_weights(const GridDims& g, int nf, const double* xb, const double* yb, double delta, double offx,
                        double offy, RegDev& r, int* d_err, cudaStream_t st);
 int launch_reg_lists(int nf, RegDev& r, const GridDims& g, cudaStream_t st);
+// Copies of the origins and weights (ix_s, iy_s: nf ints; w_s: 49 nf doubles).
+int launch_reg_snapshot(int nf, const RegDev& r, int* ix_s, int* iy_s, double* w_s, cudaStream_t st);
 // hx, hy must be zero outside the stencil box; this writes every face in the box.
 int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, double* hx, double* hy,
                cudaStream_t st);

@@ -208,6 +208,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)L * ns + (size_t)L * nbc + 2 * L;       // per-level spectra and rings (vort2flux)
   dbl += (size_t)g.nsx * g.nsx + (size_t)L * (2 * (size_t)g.nsy + 2 * (size_t)g.nsx);   // edge matrix, terms
   dbl += 7 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
+  dbl += 49 * (size_t)nf + (size_t)nf + 1;               // weights snapshot (+ its origins, as doubles)
   dbl += 8 * (size_t)nt + nt + 3;
   dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 4 * (size_t)nf + 2;
   if (p.num_stat) dbl += (size_t)nf * nf;
@@ -254,6 +255,9 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->reg.cnt_x = P.take<int>(max_faces); c->reg.cnt_y = P.take<int>(max_faces);
   c->reg.lst_x = P.take<int>(49 * (size_t)nf + 1); c->reg.lst_y = P.take<int>(49 * (size_t)nf + 1);
   c->reg.stale = P.take<int>(1);
+  c->reg_w_s = P.take<double>(49 * (size_t)nf + 1);
+  c->reg_ix_s = P.take<int>(nf + 1);
+  c->reg_iy_s = P.take<int>(nf + 1);
   c->reg.max_faces = max_faces; c->reg.max_list = 49 * nf;
   c->tb = P.take<TorsBody>(nt + 1);
   c->ts.theta = P.take<double>(nt + 1); c->ts.thetad = P.take<double>(nt + 1);
@@ -710,10 +714,12 @@ int op_profile_schur(Ctx* c, int reps, double* ms) {
   return IB_OK;
 }
 
-int op_redistribute(Ctx* c, const double* f, double* frdst) {
-  RC(launch_redistribute_field(c->g, c->nf, f, c->reg, c->nlx, c->nly, c->st));
-  return launch_regT(c->g, c->nf, c->nlx, nullptr, c->nly, nullptr, c->reg, nullptr, frdst, c->st);
+static int redistribute_with(Ctx* c, const RegDev& r, const double* f, double* frdst) {
+  RC(launch_redistribute_field(c->g, c->nf, f, r, c->nlx, c->nly, c->st));
+  return launch_regT(c->g, c->nf, c->nlx, nullptr, c->nly, nullptr, r, nullptr, frdst, c->st);
 }
+
+int op_redistribute(Ctx* c, const double* f, double* frdst) { return redistribute_with(c, c->reg, f, frdst); }
 
 // Device time of `reps` back-to-back launches of one full pass over the finest grid
 // (kind 0: x pass, 1: tridiagonal solve), for the roofline of a kernel timed alone.
@@ -1022,9 +1028,10 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
 }
 
 // ------------------------------------------------------------- FSI iterations on the device
-__global__ void k_fsi_loop_init(int* cnt) {
+__global__ void k_fsi_loop_init(int* cnt, int* band_flag) {
   IB_GRID_DEP_WAIT();
   if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) *band_flag = 0;
 }
 
 // End of one device FSI iteration: the counters (the cluster solver's G.ist: [0] Krylov
@@ -1033,29 +1040,32 @@ __global__ void k_fsi_loop_init(int* cnt) {
 // next operator's patches leave the influence band (the host rebuilds it) or the error is
 // not finite (the host reports it).
 __global__ void k_fsi_loop_cond(int* cnt, const int* __restrict__ ist, const double* __restrict__ err,
-                                const int* __restrict__ band_flag, double tol, int max_it,
-                                cudaGraphConditionalHandle h) {
+                                int* band_flag, double tol, int max_it, cudaGraphConditionalHandle h) {
   IB_GRID_DEP_WAIT();
   if (threadIdx.x != 0) return;
   const double e = err[0];
   const int n = cnt[0] + 1;
+  const int bf = *band_flag;
+  *band_flag = 0;   // the next iteration's patches start from zero
   cnt[0] = n;
   cnt[1] += ist[0];
   cnt[2] += ist[0] + ist[4];
-  cnt[3] = *band_flag;
-  const bool go = isfinite(e) && e >= tol && n <= max_it && *band_flag == 0;
+  cnt[3] = bf;
+  const bool go = isfinite(e) && e >= tol && n <= max_it && bf == 0;
   cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
 // Captures the graph of a step's FSI iterations: the counters reset, then a while node whose
 // body is one iteration on the assembled operator, and after it the contribution lists of the
 // final positions.  The body runs its independent parts side by side:
-//     s1: assembly ----------------------> Krylov solve -> structure update --> weights,
-//     s2: right-hand side ----------------^            \-> redistribution --^   patches,
-//     s3: contribution lists of the current weights ------^                      condition
+//     s1: K P ---------> P^T K P + B -> Krylov solve -> structure update -> weights, patches -> condition
+//     s2: B rows, right-hand side --^                \-> redistribution ------------------^
+//     s3: copy of the current weights, their contribution lists ----^
 // The lists (read only by E^T, i.e. the redistribution, and after the loop by the
 // correction) are rebuilt at the start of the iteration after the weights they belong to,
-// so they leave the chain from one solve to the next.  The body's launches are counted once
+// and the redistribution reads the copy, so neither is on the chain from one solve to the
+// next.  The band flag and the touched-vertex flags are cleared by the kernels that read
+// them (the condition, the compaction), so the patches need no memsets.  The body's launches are counted once
 // (fsi_body_launches), the lists after the loop in fsi_post_launches.
 static int build_fsi_loop(Ctx* c) {
   const GridDims& g = c->g;
@@ -1077,7 +1087,7 @@ static int build_fsi_loop(Ctx* c) {
     if (rc != IB_OK) break;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
     count_launch();
-    k_fsi_loop_init<<<1, 32, 0, st>>>(c->fsi_cnt);
+    k_fsi_loop_init<<<1, 32, 0, st>>>(c->fsi_cnt, I.flag);
     cudaGraphConditionalHandle h = 0;
     cudaGraph_t body = nullptr;
     if (cudaGraphConditionalHandleCreate(&h, capture_graph(st), 1, cudaGraphCondAssignDefault) != cudaSuccess)
@@ -1093,35 +1103,42 @@ static int build_fsi_loop(Ctx* c) {
         IB_CUDA_CHECK(cudaEventRecord(ev_fork, s1));
         IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_fork, 0));
         IB_CUDA_CHECK(cudaStreamWaitEvent(s3, ev_fork, 0));
-        // s2: right-hand side
+        // s2: the B rows and the right-hand side
+        RC(inf_assemble_b(c, s2));
         if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s2));
         RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s2));
         RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s2));
         IB_CUDA_CHECK(cudaEventRecord(ev_rhs, s2));
-        // s3: contribution lists of the current weights
+        // s3: a copy of the current origins and weights and their contribution lists
+        RC(launch_reg_snapshot(c->nf, c->reg, c->reg_ix_s, c->reg_iy_s, c->reg_w_s, s3));
         RC(launch_reg_lists(c->nf, c->reg, g, s3));
         IB_CUDA_CHECK(cudaEventRecord(ev_lists, s3));
         // s1: assembly and solve
-        RC(inf_assemble(c));
+        RC(inf_assemble_kp(c, s1, true));
         IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));
+        RC(inf_assemble_ptk(c, s1));
         RC(launch_gmres_fused(c->G, &c->fused_plan, I.St, c->rhsf, c->f, p.rtol, p.atol, p.gmres_max_it, s1));
-        // s2: redistribution with the current weights, beside the structure update on s1
+        // s2: redistribution with the copy, beside the structure update and the weights and
+        // patches at the new positions on s1
         IB_CUDA_CHECK(cudaEventRecord(ev_f, s1));
         IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_f, 0));
         IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_lists, 0));
+        RegDev snap = c->reg;
+        snap.ix = c->reg_ix_s;
+        snap.iy = c->reg_iy_s;
+        snap.w = c->reg_w_s;
         c->st = s2;
-        const int rrd = op_redistribute(c, c->f, c->f_rdst);
+        const int rrd = redistribute_with(c, snap, c->f, c->f_rdst);
         c->st = s1;
         RC(rrd);
         IB_CUDA_CHECK(cudaEventRecord(ev_rd, s2));
         RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, s1));
-        // weights and patches at the new positions (the weights overwrite what the
-        // redistribution reads)
-        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rd, 0));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_lists, 0));   // the copy and the lists are taken
         I.patch_fresh = false;
         I.active = false;
         RC(launch_reg_weights(g, c->nf, c->xb, c->yb, c->delta, p.offsetx, p.offsety, c->reg, c->d_err, s1));
-        RC(inf_patch(c));
+        RC(inf_patch(c, true));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rd, 0));
         count_launch();
         k_fsi_loop_cond<<<1, 32, 0, s1>>>(c->fsi_cnt, c->G.ist, c->err_fsi, I.flag, p.fsi_tol, p.fsi_max_it, h);
         IB_CUDA_CHECK(cudaGetLastError());
