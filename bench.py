@@ -383,6 +383,7 @@ def run_gpu(args, world, rank, local):
         "influence": sim.influence_stats(),
         "launch_shapes": sim.launch_shapes(),
         "step_phases_us": _step_phases(sim, 5),
+        "step_phases_device_loop_us": _step_phases(sim, 5, device_loop=True),
     }
     if not args.no_matrix_free:
         result["matrix_free"] = _matrix_free_rate(p, bodies, args)
@@ -405,12 +406,15 @@ def run_gpu(args, world, rank, local):
     return 0
 
 
-def _step_phases(sim, steps):
-    """Device time per step of each phase of ib_advance (CUDA events), over a few more steps."""
-    sim.step_profile(1)
+def _step_phases(sim, steps, device_loop=False):
+    """Device time per step of each phase of ib_advance (CUDA events), over a few more steps:
+    the FSI iterations phase by phase from the host, or (device_loop) the device FSI loop as
+    one phase."""
+    sim.step_profile(3 if device_loop else 1)
     for _ in range(steps):
         sim.advance()
     out = sim.step_profile(0)
+    out = {k: v for k, v in out.items() if v > 0.0}
     out["steps"] = steps
     return out
 

@@ -505,7 +505,7 @@ int ib_profile_schur(IbCtx* h, int reps, double* stage_ms) {
 
 int ib_step_profile(IbCtx* h, int mode, double* phase_ms, long long* nsteps) {
   CTX_OR_FAIL(h);
-  if (mode < 0 || mode > 2) return fail(IB_ERR_ARG, "bad mode");
+  if (mode < 0 || mode > 3) return fail(IB_ERR_ARG, "bad mode");
   return op_result(ib::op_step_profile(c, mode, phase_ms, nsteps), "step_profile failed");
 }
 

@@ -165,6 +165,9 @@ struct Ctx {
   int* reg_ix_s = nullptr;
   int* reg_iy_s = nullptr;
   double* reg_w_s = nullptr;
+  // the device FSI loop's fused update: theta, sin, cos before they are committed, its ticket
+  double* tors_next = nullptr;     // 3 x (nt + 1)
+  unsigned* fsi_done = nullptr;
   long long fsi_post_launches = 0;
   int* fsi_cnt = nullptr;
   FusedPlan fused_plan;
@@ -194,9 +197,11 @@ struct Ctx {
 
   // optional phase timing of the time step (ib_step_profile): 0 predictor, 1 vort2flux,
   // 2 FSI right-hand side, 3 Schur assembly, 4 GMRES, 5 FSI update (redistribute, structure,
-  // weights, synchronisation), 6 correction
-  static constexpr int kStepPhases = 7;
+  // weights, synchronisation), 6 correction, 7 the device FSI loop (its graph and the
+  // synchronisation that reads its counters; step_prof_dev: the device loop stays on)
+  static constexpr int kStepPhases = 8;
   bool step_prof = false;
+  bool step_prof_dev = false;
   cudaEvent_t step_ev[10] = {};
   double step_ms[kStepPhases] = {0};
   long long step_n = 0;

@@ -7,108 +7,25 @@
 // reg is a face-major gather: for every face of the stencil bounding box the
 // contributing unknowns are listed in ascending order, so each face sums its
 // contributions in the same order as the reference's sequential scatter-add.
-#include "kernels.cuh"
+#include "fsi_dev.cuh"
 
 namespace ib {
 
-// Smoothed 6-point delta function.  Literals without a d exponent in the Fortran
-// source are default REAL, i.e. single precision: they appear as float literals.
-__device__ double deltafnc_dev(double x1, double x2, double dr) {
-  double r = fabs(x1 - x2);
-  double r1 = r / dr;
-  double r2 = r1 * r1;
-  double r3 = r2 * r1;
-  double r4 = r3 * r1;
-  const double s3 = sqrt(3.0);
-  double v;
-  if (r1 <= 1.0) {
-    double a5 = asin((1.0 / 2.0) * s3 * (2.0 * r1 - 1.0));
-    double a8 = sqrt(1.0 - 12.0 * r2 + 12.0 * r1);
-    v = 0.4166666667e-1 * r4 + ((double)(-.1388888889f) + 0.3472222222e-1 * a8) * r3 +
-        (-0.7121664902e-1 - 0.5208333333e-1 * a8 + (double)(0.2405626122f) * a5) * r2 +
-        (-(double)(.2405626122f) * a5 - (double)(.3792313933f) + (double)(.1012731481f) * a8) * r1 +
-        0.8018753741e-1 * a5 - 0.4195601852e-1 * a8 + (double)(.6485698427f);
-  } else if (r1 <= 2.0) {
-    double a6 = asin((1.0 / 2.0) * s3 * (-3.0 + 2.0 * r1));
-    double a9 = sqrt(-23.0 + 36.0 * r1 - 12.0 * r2);
-    v = -0.6250000000e-1 * r4 + ((double)(.4861111111f) - 0.1736111111e-1 * a9) * r3 +
-        ((double)(-1.143175026f) + 0.7812500000e-1 * a9 - (double)(.1202813061f) * a6) * r2 +
-        ((double)(.8751991178f) + (double)(.3608439183f) * a6 - (double)(.1548032407f) * a9) * r1 -
-        (double)(.2806563809f) * a6 + 0.822848104e-2 + (double)(.1150173611f) * a9;
-  } else if (r1 <= 3.0) {
-    double a1 = asin((1.0 / 2.0 * (2.0 * r1 - 5.0)) * s3);
-    double a7 = sqrt(-71.0 - 12.0 * r2 + 60.0 * r1);
-    v = 0.2083333333e-1 * r4 + (0.3472222222e-2 * a7 - (double)(.2638888889f)) * r3 +
-        ((double)(1.214391675f) - 0.2604166667e-1 * a7 + 0.2405626122e-1 * a1) * r2 +
-        (-(double)(.1202813061f) * a1 - (double)(2.449273192f) + 0.7262731481e-1 * a7) * r1 +
-        (double)(.1523563211f) * a1 + (double)(1.843201677f) - 0.7306134259e-1 * a7;
-  } else {
-    v = 0.0;
-  }
-  return v / dr;
-}
-
-// Stencil origins and the 49 weights (l outer, p inner) of 8 unknowns per CTA (4 warps).
-// With phi the fractional position of a point in its cell, the 7 stencil offsets q sit at
-// distances |q - 3 - phi| (in cells), so offsets {3,4}, {2,5} and {1,6} fall in the first,
-// second and third piece of the delta function and offset 0 at its edge.  Warp w evaluates
-// one offset pair for the x and y factors of all 8 unknowns, so its lanes take one branch of
-// the FP64-latency-bound evaluation instead of all three; the factors then meet in shared
-// memory for the products.
+// Stencil origins and weights of 8 unknowns per CTA (reg_weights_cta).
 __global__ void __launch_bounds__(128) k_reg_weights(GridDims g, int nf, const double* __restrict__ xb,
                                                      const double* __restrict__ yb, double d, double ox,
                                                      double oy, const int* __restrict__ comp, int* ix, int* iy,
                                                      double* w, int* stale, int* err) {
   IB_GRID_DEP_WAIT();
   __shared__ double fac[16][7];    // [2*unknown + axis][offset], axis 0: x factor, 1: y factor
+  __shared__ double pos[8][2];
   const int k0 = blockIdx.x * 8;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const double d2 = 0.5 * d;
-  // this lane's (pair, offset)
-  int pi, q;
-  if (warp < 3) {
-    pi = lane >> 1;
-    const int lo = 3 - warp, hi = 4 + warp;   // {3,4}, {2,5}, {1,6}
-    q = (lane & 1) ? hi : lo;
-  } else {
-    pi = lane;
-    q = 0;
-  }
-  const int k = k0 + (pi >> 1), axis = pi & 1;
-  if (pi < 16 && k < nf) {
-    const double xk = xb[k], yk = yb[k];
-    const int cx = (int)((xk + ox) / d) + 1;   // Fortran INT truncates toward zero
-    const int cy = (int)((yk + oy) / d) + 1;
-    const bool isx = comp[k] == 1;
-    const int off = q - 3;
-    double f;
-    if (axis == 0) {
-      double x = d * (double)(cx - 1 + off) - ox;
-      if (!isx) x = x + d2;
-      f = deltafnc_dev(x, xk, d);
-    } else {
-      double y = d * (double)(cy - 1 + off) - oy;
-      if (isx) y = y + d2;
-      f = deltafnc_dev(y, yk, d);
-    }
-    fac[pi][q] = f;
-    if (warp == 3 && axis == 0) {
-      // the contribution lists depend on the stencil origins only: rebuild them when one moved
-      if (ix[k] != cx || iy[k] != cy) atomicOr(stale, 1);
-      ix[k] = cx;
-      iy[k] = cy;
-      // faces touched: u-face i in [1,m+1], j in [1,n]; v-face i in [1,m], j in [1,n+1]
-      int imax = isx ? g.m + 1 : g.m, jmax = isx ? g.n : g.n + 1;
-      if (cx - 3 < 1 || cx + 3 > imax || cy - 3 < 1 || cy + 3 > jmax) atomicExch(err, IB_ERR_DOMAIN);
-    }
+  if ((int)threadIdx.x < 8 && k0 + (int)threadIdx.x < nf) {
+    pos[threadIdx.x][0] = xb[k0 + threadIdx.x];
+    pos[threadIdx.x][1] = yb[k0 + threadIdx.x];
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < 8 * 49; t += blockDim.x) {
-    const int u = t / 49, sl = t - u * 49;
-    if (k0 + u >= nf) break;
-    const int l = sl / 7, p = sl - l * 7;
-    w[(size_t)(k0 + u) * 49 + sl] = d * d * fac[2 * u][p] * fac[2 * u + 1][l];
-  }
+  reg_weights_cta(g, nf, k0, pos, d, ox, oy, comp, ix, iy, w, stale, err, fac, nullptr, nullptr);
 }
 
 // Bounding box of all stencils (one CTA).  bbox[0..3] = i0, j0, ni, nj of the face box;
@@ -428,8 +345,9 @@ int launch_redistribute_field(const GridDims& g, int nf, const double* f, const 
                               double* fy, cudaStream_t st) {
   if (nf == 0) return IB_OK;
   count_launch();
-  k_redist_field<<<152 * 2, 128, 0, st>>>(g, f, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, fx, fy,
-                                          r.max_faces);
+  // about one box face per thread (a stencil covers 49 faces; the loop strides over the rest)
+  const int nblk = std::max(8, std::min(152 * 2, cdiv(49LL * nf, 128)));
+  k_redist_field<<<nblk, 128, 0, st>>>(g, f, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, fx, fy, r.max_faces);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

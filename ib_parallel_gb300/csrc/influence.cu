@@ -14,6 +14,7 @@
 #include <cmath>
 
 #include "ctx.cuh"
+#include "fsi_dev.cuh"
 
 namespace ib {
 
@@ -22,10 +23,7 @@ constexpr int kT = Influence::kTile;   // tile edge (vertices)
 constexpr int kP = 64;                 // patch size (8 x 8 vertices)
 }  // namespace
 
-// Per unknown k (one CTA of 64 threads): the patch rot(E^T e_k) on the vertices
-// I in [cx-3, cx+4], J in [cy-3, cy+4], with each vertex's index in the band.
-// flag |= 1 when a patch vertex lies outside the band, |= 2 when it is not an interior
-// vertex (its streamfunction would come from the boundary ring).
+// Per unknown k (one CTA of 64 threads): its patch (patch_entry).
 __global__ void k_inf_patch(GridDims g, int nf, const int* __restrict__ comp, const int* __restrict__ ix,
                             const int* __restrict__ iy, const double* __restrict__ w,
                             const int* __restrict__ tile_of, int ntx, double* __restrict__ pval,
@@ -33,33 +31,7 @@ __global__ void k_inf_patch(GridDims g, int nf, const int* __restrict__ comp, co
   IB_GRID_DEP_WAIT();
   const int k = blockIdx.x, q = threadIdx.x;
   if (k >= nf || q >= kP) return;
-  const int di = q & 7, dj = q >> 3;
-  const int cx = ix[k], cy = iy[k];
-  const bool isx = comp[k] == 1;
-  const double* wk = w + (size_t)k * 49;
-  auto W = [&](int p, int l) -> double {
-    return (p >= -3 && p <= 3 && l >= -3 && l <= 3) ? wk[(l + 3) * 7 + (p + 3)] : 0.0;
-  };
-  const int p = di - 3, l = dj - 3;
-  // rot (operators_fluid.F90:203-233) of the spread unit force: a u-face (i,j) adds -1 to
-  // vertex (i,j) and +1 to (i,j+1); a v-face adds +1 to (i,j) and -1 to (i+1,j)
-  double v = isx ? W(p, l - 1) - W(p, l) : W(p, l) - W(p - 1, l);
-  const int a = cx - 3 + di - 2, b = cy - 3 + dj - 2;   // 0-based interior vertex
-  int idx = -1, fl = 0;
-  if (a < 0 || a >= g.nsx || b < 0 || b >= g.nsy) {
-    fl = 2;
-  } else if (!tile_of) {
-    fl = 1;
-  } else {
-    int t = tile_of[(b / kT) * ntx + a / kT];
-    if (t < 0) fl = 1;
-    else idx = t * kP + (b % kT) * kT + (a % kT);
-  }
-  if (idx < 0) v = 0.0;
-  pval[(size_t)k * kP + q] = v;
-  pidx[(size_t)k * kP + q] = idx;
-  if (idx >= 0) used[idx] = 1;
-  if (fl) atomicOr(flag, fl);
+  patch_entry(g, k, q, comp[k] == 1, ix[k], iy[k], w + (size_t)k * 49, tile_of, ntx, kT, pval, pidx, used, flag);
 }
 
 // Compaction of the touched band vertices (one CTA of 1024 threads).  clear: also clears the

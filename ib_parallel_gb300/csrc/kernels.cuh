@@ -92,6 +92,9 @@ int launch_force_coeffs(int nf, int nbody, const int* comp, const int* bid, cons
 struct TorsBody {
   int off, npts;
   double gamma0, itheta, ktheta, ctheta, deltas, xbf0, ybf0;
+  // step constants of compute_dx (launch_tors_consts): 4/dt^2, 4/dt, 2/dt, the effective
+  // stiffness 4/dt^2 I + 2/dt C + K and its reciprocal, deltas / (4/dt^2 I + K), delta/deltas/dt
+  double a44, a4, a2, keff, keff_inv, bq, bs;
 };
 struct TorsState {  // device arrays of length nt
   double *theta, *thetad, *thetadd, *theta0, *thetad0, *thetadd0;
@@ -117,6 +120,41 @@ int launch_tors_rhs(int nt, const TorsBody* tb, const TorsState& s, double dt, d
                     cudaStream_t st);
 int launch_tors_dx(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta, const double* f,
                    double* xb, double* yb, double* err, cudaStream_t st);
+// The end of one device FSI iteration in one kernel (fsi_update.cu): structure update,
+// weights and influence patches at the new positions, and the loop condition.
+struct FsiUpdateArgs {
+  // structure: torsional bodies, the solved forces, positions, err[0] max and err[1..nt]
+  const TorsBody* tb;
+  TorsState ts;
+  int nt;
+  double dt, delta;
+  const double* f;
+  double *xb, *yb, *err;
+  double *th_next, *sin_next, *cos_next;   // nt each: written before they are committed
+  // weights (RegDev's origins and weights, the stale flag, the domain error)
+  GridDims g;
+  int nf;
+  double ox, oy;
+  const int* comp;
+  int *ix, *iy;
+  double* w;
+  int *stale, *d_err;
+  // patches: the band's tile map (tile x tile vertices), patch values and indices, flags
+  const int* tile_of;
+  int ntx, tile;
+  double* pval;
+  int *pidx, *used, *flag;
+  // condition: counters (as k_fsi_loop_cond), the Krylov counters, the ticket
+  int* cnt;
+  const int* ist;
+  double tol;
+  int max_it;
+  cudaGraphConditionalHandle h;
+  unsigned* done;
+};
+int launch_fsi_update(const FsiUpdateArgs& a, cudaStream_t st);
+// The step constants of every torsional body record (set-up, after the records are uploaded).
+int launch_tors_consts(int nt, TorsBody* tb, double dt, double delta, cudaStream_t st);
 int launch_tors_initial_acc(int nt, const TorsBody* tb, const TorsState& s, double dt, double delta,
                             const double* f, cudaStream_t st);
 int launch_tors_save(int nt, const TorsState& s, cudaStream_t st);

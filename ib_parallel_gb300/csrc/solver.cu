@@ -209,6 +209,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)g.nsx * g.nsx + (size_t)L * (2 * (size_t)g.nsy + 2 * (size_t)g.nsx);   // edge matrix, terms
   dbl += 7 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
   dbl += 49 * (size_t)nf + (size_t)nf + 1;               // weights snapshot (+ its origins, as doubles)
+  dbl += 3 * ((size_t)nt + 1) + 1;                       // fused FSI update: theta, sin, cos; ticket
   dbl += 8 * (size_t)nt + nt + 3;
   dbl += (size_t)(R + 1) * nf + (size_t)(R + 1) * R + 3 * (R + 1) + 4 + 4 * (size_t)nf + 2;
   if (p.num_stat) dbl += (size_t)nf * nf;
@@ -258,6 +259,8 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->reg_w_s = P.take<double>(49 * (size_t)nf + 1);
   c->reg_ix_s = P.take<int>(nf + 1);
   c->reg_iy_s = P.take<int>(nf + 1);
+  c->tors_next = P.take<double>(3 * ((size_t)nt + 1));
+  c->fsi_done = P.take<unsigned>(2);
   c->reg.max_faces = max_faces; c->reg.max_list = 49 * nf;
   c->tb = P.take<TorsBody>(nt + 1);
   c->ts.theta = P.take<double>(nt + 1); c->ts.thetad = P.take<double>(nt + 1);
@@ -375,7 +378,8 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     IB_CUDA_CHECK(cudaMemcpy(c->bid, c->bid_h.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
   }
   if (nt > 0) IB_CUDA_CHECK(cudaMemcpy(c->tb, c->tb_h.data(), sizeof(TorsBody) * nt, cudaMemcpyHostToDevice));
-  rc = launch_tors_trig(nt, c->tb, c->ts, c->st);
+  rc = launch_tors_consts(nt, c->tb, p.dt, c->delta, c->st);
+  if (rc == IB_OK) rc = launch_tors_trig(nt, c->tb, c->ts, c->st);
   if (rc != IB_OK) { *msg = "device initialisation failed"; ctx_destroy(c); return rc; }
   for (int i = 0; i < nbody; ++i) c->bodies_h.push_back(bodies[i]);
 
@@ -928,14 +932,17 @@ static int preprocess_chol(Ctx* c) {
   return IB_OK;
 }
 
-// mode 1: start (totals cleared), 0: stop, 2: read only.  ms[7] totals, *nsteps steps timed.
+// mode 1: start (totals cleared) with the FSI iterations run from the host, phase by phase;
+// 3: start with the device FSI loop kept (timed as one phase); 0: stop; 2: read only.
+// ms[8] totals, *nsteps steps timed.
 int op_step_profile(Ctx* c, int mode, double* ms, long long* nsteps) {
-  if (mode == 1) {
+  if (mode == 1 || mode == 3) {
     for (auto& e : c->step_ev)
       if (!e) IB_CUDA_CHECK(cudaEventCreate(&e));
     for (double& v : c->step_ms) v = 0.0;
     c->step_n = 0;
     c->step_prof = true;
+    c->step_prof_dev = mode == 3;
   } else if (mode == 0) {
     c->step_prof = false;
   }
@@ -1028,10 +1035,13 @@ static int run_phase(Ctx* c, PhaseGraph& ph, F&& fn) {
 }
 
 // ------------------------------------------------------------- FSI iterations on the device
-__global__ void k_fsi_loop_init(int* cnt, int* band_flag) {
+__global__ void k_fsi_loop_init(int* cnt, int* band_flag, unsigned* done) {
   IB_GRID_DEP_WAIT();
   if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
-  if (threadIdx.x == 0) *band_flag = 0;
+  if (threadIdx.x == 0) {
+    *band_flag = 0;
+    *done = 0u;
+  }
 }
 
 // End of one device FSI iteration: the counters (the cluster solver's G.ist: [0] Krylov
@@ -1058,14 +1068,15 @@ __global__ void k_fsi_loop_cond(int* cnt, const int* __restrict__ ist, const dou
 // Captures the graph of a step's FSI iterations: the counters reset, then a while node whose
 // body is one iteration on the assembled operator, and after it the contribution lists of the
 // final positions.  The body runs its independent parts side by side:
-//     s1: K P ---------> P^T K P + B -> Krylov solve -> structure update -> weights, patches -> condition
-//     s2: B rows, right-hand side --^                \-> redistribution ------------------^
-//     s3: copy of the current weights, their contribution lists ----^
+//     s1: K P ---------> P^T K P + B -> Krylov solve -> structure update, weights, patches, condition
+//     s2: B rows, right-hand side --^                \-> redistribution ----------------------------->|
+//     s3: copy of the current weights, their contribution lists -----------^
 // The lists (read only by E^T, i.e. the redistribution, and after the loop by the
 // correction) are rebuilt at the start of the iteration after the weights they belong to,
 // and the redistribution reads the copy, so neither is on the chain from one solve to the
 // next.  The band flag and the touched-vertex flags are cleared by the kernels that read
-// them (the condition, the compaction), so the patches need no memsets.  The body's launches are counted once
+// them (the condition, the compaction), so the patches need no memsets; the end of the
+// iteration is one kernel (k_fsi_update).  The body's launches are counted once
 // (fsi_body_launches), the lists after the loop in fsi_post_launches.
 static int build_fsi_loop(Ctx* c) {
   const GridDims& g = c->g;
@@ -1087,7 +1098,7 @@ static int build_fsi_loop(Ctx* c) {
     if (rc != IB_OK) break;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
     count_launch();
-    k_fsi_loop_init<<<1, 32, 0, st>>>(c->fsi_cnt, I.flag);
+    k_fsi_loop_init<<<1, 32, 0, st>>>(c->fsi_cnt, I.flag, c->fsi_done);
     cudaGraphConditionalHandle h = 0;
     cudaGraph_t body = nullptr;
     if (cudaGraphConditionalHandleCreate(&h, capture_graph(st), 1, cudaGraphCondAssignDefault) != cudaSuccess)
@@ -1112,6 +1123,7 @@ static int build_fsi_loop(Ctx* c) {
         // s3: a copy of the current origins and weights and their contribution lists
         RC(launch_reg_snapshot(c->nf, c->reg, c->reg_ix_s, c->reg_iy_s, c->reg_w_s, s3));
         RC(launch_reg_lists(c->nf, c->reg, g, s3));
+        IB_CUDA_CHECK(cudaMemsetAsync(c->reg.stale, 0, sizeof(int), s3));   // for the weights below
         IB_CUDA_CHECK(cudaEventRecord(ev_lists, s3));
         // s1: assembly and solve
         RC(inf_assemble_kp(c, s1, true));
@@ -1132,16 +1144,23 @@ static int build_fsi_loop(Ctx* c) {
         c->st = s1;
         RC(rrd);
         IB_CUDA_CHECK(cudaEventRecord(ev_rd, s2));
-        RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, s1));
-        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_lists, 0));   // the copy and the lists are taken
+        // structure update, weights and patches at the new positions, the condition (after the
+        // copy and the lists of the current weights are taken)
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_lists, 0));
         I.patch_fresh = false;
         I.active = false;
-        RC(launch_reg_weights(g, c->nf, c->xb, c->yb, c->delta, p.offsetx, p.offsety, c->reg, c->d_err, s1));
-        RC(inf_patch(c, true));
-        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rd, 0));
-        count_launch();
-        k_fsi_loop_cond<<<1, 32, 0, s1>>>(c->fsi_cnt, c->G.ist, c->err_fsi, I.flag, p.fsi_tol, p.fsi_max_it, h);
-        IB_CUDA_CHECK(cudaGetLastError());
+        FsiUpdateArgs u;
+        u.tb = c->tb; u.ts = c->ts; u.nt = c->nt; u.dt = p.dt; u.delta = c->delta; u.f = c->f;
+        u.xb = c->xb; u.yb = c->yb; u.err = c->err_fsi;
+        u.th_next = c->tors_next; u.sin_next = c->tors_next + (c->nt + 1); u.cos_next = c->tors_next + 2 * (c->nt + 1);
+        u.g = g; u.nf = c->nf; u.ox = p.offsetx; u.oy = p.offsety; u.comp = c->reg.comp;
+        u.ix = c->reg.ix; u.iy = c->reg.iy; u.w = c->reg.w; u.stale = c->reg.stale; u.d_err = c->d_err;
+        u.tile_of = I.tile_of; u.ntx = I.ntx; u.tile = Influence::kTile;
+        u.pval = I.pval; u.pidx = I.pidx; u.used = I.used; u.flag = I.flag;
+        u.cnt = c->fsi_cnt; u.ist = c->G.ist; u.tol = p.fsi_tol; u.max_it = p.fsi_max_it; u.h = h;
+        u.done = c->fsi_done;
+        RC(launch_fsi_update(u, s1));
+        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rd, 0));   // the body ends with the redistribution
         return IB_OK;
       };
       rc = iteration();
@@ -1284,13 +1303,19 @@ int op_advance(Ctx* c) {
       {
         Influence& I = c->inf;
         const bool device_loop = moved && p.schur_mode != 1 && c->use_step_graphs && c->use_fused && !c->prof_on &&
-                                 !c->stage_on && !c->step_prof && !c->graph_fsi_loop.failed &&
+                                 !c->stage_on && (!c->step_prof || c->step_prof_dev) &&
+                                 !c->graph_fsi_loop.failed &&
                                  c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
         if (device_loop && (c->graph_fsi_loop.exec || build_fsi_loop(c) == IB_OK)) {
           IB_CUDA_CHECK(cudaGraphLaunch(c->graph_fsi_loop.exec, st));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st));
           IB_CUDA_CHECK(cudaStreamSynchronize(st));
+          if (c->step_prof) {
+            step_mark(c, 3);
+            cudaEventSynchronize(c->step_ev[3]);
+            step_acc(c, 7, 2, 3);
+          }
           fsi_count = c->h_ist[0];
           c->ksp_iter += c->h_ist[1];
           c->n_matvec += c->h_ist[2];

@@ -6,7 +6,7 @@
 // run one warp per body; b_times keeps 256 threads, whose reduction order the fused
 // Krylov kernel reproduces.  Gravity and pseudo-forces are zero in the
 // reference user hooks (user.F90:178-206) and are omitted.
-#include "kernels.cuh"
+#include "fsi_dev.cuh"
 
 namespace ib {
 
@@ -60,45 +60,52 @@ __global__ void k_tors_rhs(const TorsBody* __restrict__ tb, TorsState s, double 
   for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) y[b.off + j] = br_val(b, sn, cs, j) * c;
 }
 
-// compute_dx + update_xb (operators_struct.F90:402-505, 600-620); err = max |dtheta|
+// compute_dx + update_xb (operators_struct.F90:402-505, 600-620); err = max |dtheta|.  One
+// warp per body (tors_dx_warp).
 __global__ void k_tors_dx(const TorsBody* __restrict__ tb, TorsState s, double dt, double delta,
                           const double* __restrict__ f, double* __restrict__ xb, double* __restrict__ yb,
                           double* __restrict__ err_per_body, double* __restrict__ err_max) {
   IB_GRID_DEP_WAIT();
-  int t = blockIdx.x;
-  TorsBody b = tb[t];
-  double th = s.theta[t], th0 = s.theta0[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
-  double I = b.itheta, C = b.ctheta, K = b.ktheta;
-  double sn0 = s.sinv[t], cs0 = s.cosv[t];
-  double part = 0.0;
-  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) part += br_val(b, sn0, cs0, j) * f[b.off + j];
-  double brf = block_sum(part);
-  double jr = 1.0 / (4.0 / (dt * dt) * I + 2.0 / dt * C + K) *
-              (I * (4.0 / (dt * dt) * th0 + 4.0 / dt * thd0 + thdd0) + C * (thd0 + 2.0 / dt * th0) -
-               (4.0 / (dt * dt) * I + 2.0 / dt * C + K) * th);
-  brf = b.deltas / (4.0 / (dt * dt) * I + K) * brf * (delta / b.deltas / dt);
-  double dth = jr + brf;
-  double thn = th + dth;
+  const int t = blockIdx.x;
+  const TorsBody b = tb[t];
+  const TorsDx u = tors_dx_warp(b, s, t, f);
+  const double cg = cos(u.g), sg = sin(u.g);
+  const double th0 = s.theta0[t], thd0 = s.thetad0[t], thdd0 = s.thetadd0[t];
+  __syncwarp();   // every lane has read the old theta, sinv, cosv
   if (threadIdx.x == 0) {
-    s.theta[t] = thn;
-    s.thetad[t] = -thd0 + 2.0 / dt * (thn - th0);
-    s.thetadd[t] = -thdd0 - 4.0 / dt * thd0 + 4.0 / (dt * dt) * (thn - th0);
-    err_per_body[t] = fabs(dth);
-    if (err_max) *err_max = fabs(dth);   // one body: its error is the maximum
-  }
-  double g = b.gamma0 - thn;
-  double cg = cos(g), sg = sin(g);
-  __syncthreads();   // every thread has read the old sinv, cosv
-  if (threadIdx.x == 0) {
+    s.theta[t] = u.thn;
+    tors_rates(b, u.thn, th0, thd0, thdd0, &s.thetad[t], &s.thetadd[t]);
+    err_per_body[t] = fabs(u.dth);
+    if (err_max) *err_max = fabs(u.dth);   // one body: its error is the maximum
     s.sinv[t] = sg;
     s.cosv[t] = cg;
   }
-  for (int j = threadIdx.x; j < b.npts; j += blockDim.x) {
-    double px = b.xbf0 + (double)j * b.deltas * cg;
-    double py = b.ybf0 + (double)j * b.deltas * sg;
-    xb[b.off + j] = px; xb[b.off + b.npts + j] = px;
-    yb[b.off + j] = py; yb[b.off + b.npts + j] = py;
+  for (int j = threadIdx.x; j < 2 * b.npts; j += blockDim.x) {
+    const double2 pp = tors_point(b, j, sg, cg);
+    xb[b.off + j] = pp.x;
+    yb[b.off + j] = pp.y;
   }
+}
+
+__global__ void k_tors_consts(int nt, TorsBody* tb, double dt, double delta) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  TorsBody& b = tb[t];
+  const double I = b.itheta, C = b.ctheta, K = b.ktheta;
+  b.a44 = 4.0 / (dt * dt);
+  b.a4 = 4.0 / dt;
+  b.a2 = 2.0 / dt;
+  b.keff = b.a44 * I + b.a2 * C + K;
+  b.keff_inv = 1.0 / b.keff;
+  b.bq = b.deltas / (b.a44 * I + K);
+  b.bs = delta / b.deltas / dt;
+}
+
+int launch_tors_consts(int nt, TorsBody* tb, double dt, double delta, cudaStream_t st) {
+  if (nt == 0) return IB_OK;
+  k_tors_consts<<<cdiv(nt, 128), 128, 0, st>>>(nt, tb, dt, delta);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
 }
 
 __global__ void k_max_reduce(int n, const double* __restrict__ v, double* out) {

@@ -332,11 +332,13 @@ class Simulation:
         _check(self.lib.ib_schur_matrix(self.h, _ptr(S), C.byref(st)), "ib_schur_matrix")
         return S if st.value == 0 else None
 
-    STEP_PHASES = ["predictor", "vort2flux", "fsi rhs", "schur assembly", "gmres", "fsi update", "correction"]
+    STEP_PHASES = ["predictor", "vort2flux", "fsi rhs", "schur assembly", "gmres", "fsi update", "correction",
+                   "fsi device loop"]
 
     def step_profile(self, mode: int) -> dict:
-        """mode 1 start, 0 stop, 2 read: average device us per step of each phase of ib_advance."""
-        ms = (C.c_double * 7)()
+        """mode 1 start (FSI iterations from the host, phase by phase), 3 start (device FSI loop
+        kept, timed as one phase), 0 stop, 2 read: average device us per step of each phase."""
+        ms = (C.c_double * 8)()
         n = C.c_longlong(0)
         _check(self.lib.ib_step_profile(self.h, mode, ms, C.byref(n)), "ib_step_profile")
         return {k: (1e3 * ms[i] / n.value if n.value else 0.0) for i, k in enumerate(self.STEP_PHASES)}

@@ -170,9 +170,11 @@ int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);
  * inverse rows, E curl + B */
 int ib_profile_schur(IbCtx* ctx, int reps, double* stage_ms);
 /* device time of the phases of ib_advance, summed over the steps since it was started:
- * mode 1 starts (clears), 0 stops, 2 only reads.  phase_ms[7] (may be NULL): predictor,
- * vort2flux, FSI right-hand side, Schur assembly, GMRES, FSI update (redistribute, structure,
- * weights, host synchronisation), correction; *nsteps (may be NULL): steps timed */
+ * mode 1 starts (clears) with the FSI iterations run from the host phase by phase, mode 3
+ * starts with the device FSI loop kept, 0 stops, 2 only reads.  phase_ms[8] (may be NULL):
+ * predictor, vort2flux, FSI right-hand side, Schur assembly, GMRES, FSI update (redistribute,
+ * structure, weights, host synchronisation), correction, device FSI loop (mode 3: its graph and
+ * the synchronisation that reads its counters); *nsteps (may be NULL): steps timed */
 int ib_step_profile(IbCtx* ctx, int mode, double* phase_ms, long long* nsteps);
 /* The launch shapes the context runs with (chosen by timing at ib_create when autotune is set):
  * shapes[0..12] = x pass of one level (lines per CTA, threads, one-warp scan), x pass over a few
