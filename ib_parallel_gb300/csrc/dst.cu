@@ -600,11 +600,15 @@ int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec
 //    entries r+1 (closed form 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) of every row's two end values);
 //  - edge[k] and edge[N + k]: the x transform of the ring's bottom and top entries 1..m-1,
 //    which is fac E s_J, E the edge matrix and s_J the coarse modes of the row get_bc reads.
-// CTAs [0, nlr): 16 entries of both the left and the right side (9 coarse vertices each);
-// [nlr, nlr + 2 nbt): 32 entries of the bottom or top side, as k_ring_modes; then one warp per
-// mode k for the two edge dot products.
-constexpr int kReWarps = 18;
-constexpr int kReLrSeg = 16;
+// Every warp forms FP64 dot products of length N, so the work is spread over many CTAs of
+// kReWarps warps (an FP64 warp instruction holds its SM sub-partition's pipe for the same time
+// whatever its lanes, so a CTA's warps share four pipes): CTAs [0, nlr) take kReLrSeg entries of
+// both the left and the right side (kReLrSeg/2 + 1 coarse vertices each); [nlr, nlr + 2 nbt)
+// kReTbSeg entries of the bottom or top side; then one warp per mode k for the two edge dot
+// products.
+constexpr int kReWarps = 8;
+constexpr int kReLrSeg = kReWarps - 2;          // 2 (kReLrSeg/2 + 1) = kReWarps
+constexpr int kReTbSeg = 2 * (kReWarps - 1);    // kReTbSeg/2 + 1 = kReWarps
 __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, const double* __restrict__ spec,
                                                              int ld, const double* __restrict__ W,
                                                              const double* __restrict__ E, double fac,
@@ -621,7 +625,7 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
     const int side = warp < nq ? 0 : 1;
     const int q = q0 + warp - side * nq;
     double acc = 0.0;
-    if (warp < 2 * nq && q <= qmax) {
+    if (q <= qmax) {
       const int I = side == 0 ? g.m / 4 + 1 : 3 * g.m / 4 + 1;
       const int J = g.n / 4 + 1 + q;
       acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
@@ -649,13 +653,12 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
   }
   b -= nlr;
   if (b < 2 * nbt) {
-    constexpr int nq = kRingSeg / 2 + 1;
     const int side = b / nbt, c = b - side * nbt;
     const int len = g.m + 1, qmax = (len - 1) / 2;
-    const int q0 = c * (kRingSeg / 2);
+    const int q0 = c * (kReTbSeg / 2);
     const int q = q0 + warp;
     double acc = 0.0;
-    if (warp < nq && q <= qmax) {
+    if (q <= qmax) {
       const int J = side == 0 ? g.n / 4 + 1 : 3 * g.n / 4 + 1;
       const int I = g.m / 4 + 1 + q;
       acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
@@ -663,8 +666,8 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
     acc = warp_sum(acc);
     if (lane == 0) sp[warp] = acc;
     __syncthreads();
-    if ((int)threadIdx.x < kRingSeg) {
-      const int p = c * kRingSeg + (int)threadIdx.x;
+    if ((int)threadIdx.x < kReTbSeg) {
+      const int p = c * kReTbSeg + (int)threadIdx.x;
       if (p < len) {
         const int qq = p / 2 - q0;
         const double v = (p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq];
@@ -702,7 +705,7 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
 
 int dst_ring_edge_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W,
                              const double* E, double fac, double* ring, double* sd, double* edge, cudaStream_t st) {
-  const int nlr = cdiv(g.n + 1, kReLrSeg), nbt = cdiv(g.m + 1, kRingSeg);
+  const int nlr = cdiv(g.n + 1, kReLrSeg), nbt = cdiv(g.m + 1, kReTbSeg);
   count_launch();
   k_ring_edge<<<nlr + 2 * nbt + cdiv(px.N, kReWarps), 32 * kReWarps, 0, st>>>(px.N, g, spec, ld, W, E, fac, ring, sd,
                                                                               edge, nlr, nbt);

@@ -158,7 +158,7 @@ __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld,
     const double* ts = t_sinv + kl;
     double dp = 0.0;
     for (int j = 0; j < s; ++j) {
-      dp = fma(ts[j * Mb], col[j * Mb], ti[j * Mb] * dp);
+      dp = fma(ti[j * Mb], dp, ts[j * Mb] * col[j * Mb]);
       col[j * Mb] = dp;
     }
     plast[c * Mb + kl] = dp;
@@ -270,12 +270,13 @@ __global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restr
     t_inv[q] = __ldg(op.inv + (size_t)row * nx + min(k0 + kk, nx - 1));
   }
   __syncthreads();
-  // phase 1: chunk solve with zero ends
+  // phase 1: chunk solve with zero ends (the products sigma/pivot * f are off the forward
+  // recurrence, which takes one FMA per row)
   if (chunk) {
     double dp = 0.0;
 #pragma unroll
     for (int j = 0; j < S; ++j) {
-      dp = fma(t_sinv[j * Mb + kl], f[j], t_inv[j * Mb + kl] * dp);
+      dp = fma(t_inv[j * Mb + kl], dp, t_sinv[j * Mb + kl] * f[j]);
       f[j] = dp;
     }
     plast[c * Mb + kl] = dp;
