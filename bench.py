@@ -267,6 +267,8 @@ def run_gpu(args, world, rank, local):
     from ib_parallel_gb300 import geometry as GEO
     from ib_parallel_gb300 import ibgpu as G
     p, bodies = GEO.config_plate_800x400()
+    if args.no_autotune:
+        p.autotune = 0
     sim = G.Simulation(p, bodies)
     stream = torch.cuda.ExternalStream(sim.stream())
     L = p.mgridlev
@@ -456,6 +458,9 @@ def main():
                     help="skip timing the matrix-free Schur operator beside the default one")
     ap.add_argument("--profile-window", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="run with the default launch shapes instead of tuning them by timing at creation (for "
+                         "profiler captures, whose replays would mislead the tuner)")
     ap.add_argument("--host-fsi-loop", action="store_true",
                     help="run the timed steps with per-phase timing on, so that the FSI iterations run from the "
                          "host and each of their kernels is a separate launch (a profiler lists kernels inside "

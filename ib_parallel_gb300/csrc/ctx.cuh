@@ -109,6 +109,9 @@ struct Ctx {
   std::vector<double*> mv_w, mv_s, mv_qx, mv_qy;
   // vort2flux: per-level mode-space fields and the ring each level receives
   std::vector<double*> hat, ringv;
+  // vort2flux's modes of the coarser levels (k >= 1; hat[k] keeps the predictor's meanwhile)
+  std::vector<double*> v2f_modes;
+  unsigned char* rm_v2f = nullptr; // the rows coarsify writes: transformed; the others: ROW_SCALE
   // per level: the boundary terms its solve adds (TriBc: ring end sums, edge-row transforms)
   std::vector<double*> sdv, edgev;
   double* emat = nullptr;          // edge matrix (dst_edge_matrix), (m-1) x (m-1)
@@ -230,8 +233,10 @@ int op_ctci(Ctx* c, const double* in, double* out, const double* ring);  // ring
 int op_ainv(Ctx* c, const double* in, double* out);
 int op_dst(Ctx* c, const double* in, double* out);
 int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs_old, const double* rhsbc);
+// coarse_modes_given: the coarser levels' vorticity outside the rows coarsify writes is the
+// inverse x transform of the predictor's modes still in hat[k] (within a time step only)
 int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy,
-                 bool all_levels, bool hat0_given = false);
+                 bool all_levels, bool hat0_given = false, bool coarse_modes_given = false);
 int op_schur(Ctx* c, const double* x, double* y, bool with_b);
 int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out, double* s_out,
                 const double** ring0_out);

@@ -489,6 +489,8 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
       int k = j + 1;
       double sk = __ldg(&pl.sn[k <= pl.P ? k : pl.M - k]);
       v = 2.0 * sk * ((k & 1) ? x1 + xn : x1 - xn);
+    } else if (mode == ROW_SCALE) {
+      v = a.row_scale * (a.nlev ? a.lin2[blockIdx.y] : a.in2)[o];
     } else {
       v = 0.0;
     }

@@ -63,6 +63,7 @@ struct DstXArgs {
   double post_scale = 0.0;
   // optional per-row treatment (ROW_*); rows not listed are transformed
   const unsigned char* rowmode = nullptr;
+  double row_scale = 0.0;        // ROW_SCALE rows: row_scale * in2 (lin2[level])
   // optional device range [rr[0], rr[1]) of transformed rows; others get mode rr[2]
   const int* rowrange = nullptr;
   // optional strided row subset: line i is row row0 + i*row_step, i < nlines (0: all rows)
@@ -83,8 +84,10 @@ struct DstXArgs {
 
 // Per-row treatment in the x pass.  ROW_EDGES: the row (after the pre-op) is zero
 // except its first and last samples, whose transform is closed form:
-// Y_k = 2 sin(pi k/M) (x_1 + (-1)^(k+1) x_N).
-enum RowMode { ROW_ZERO = 0, ROW_FFT = 1, ROW_EDGES = 2, ROW_SKIP = 3 };
+// Y_k = 2 sin(pi k/M) (x_1 + (-1)^(k+1) x_N).  ROW_SCALE: the row's transform is known,
+// row_scale times the same row of in2 (lin2 of the level in a batch): a row equal to the
+// inverse transform S Y of modes Y has the transform S S Y = 2m Y.
+enum RowMode { ROW_ZERO = 0, ROW_FFT = 1, ROW_EDGES = 2, ROW_SKIP = 3, ROW_SCALE = 4 };
 
 struct DstYArgs {
   double* a = nullptr;           // field (in/out), rows of pitch ld

@@ -207,6 +207,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)(L + 3) * nbc;                          // rings
   dbl += (size_t)L * ns + (size_t)L * nbc + 2 * L;       // per-level spectra and rings (vort2flux)
   dbl += (size_t)g.nsx * g.nsx + (size_t)L * (2 * (size_t)g.nsy + 2 * (size_t)g.nsx);   // edge matrix, terms
+  dbl += (size_t)(L - 1) * ns + (size_t)g.nsy;           // vort2flux's coarse-level modes, row modes
   dbl += 7 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
   dbl += 49 * (size_t)nf + (size_t)nf + 1;               // weights snapshot (+ its origins, as doubles)
   dbl += 3 * ((size_t)nt + 1) + 1;                       // fused FSI update: theta, sin, cos; ticket
@@ -245,6 +246,9 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->hat.resize(L); c->ringv.resize(L);
   for (int k = 0; k < L; ++k) { c->hat[k] = P.take<double>(ns); c->ringv[k] = P.take<double>(nbc); }
   c->emat = P.take<double>((size_t)g.nsx * g.nsx);
+  c->v2f_modes.assign(L, nullptr);
+  for (int k = 1; k < L; ++k) c->v2f_modes[k] = P.take<double>(ns);
+  c->rm_v2f = P.take<unsigned char>(g.nsy);
   c->sdv.resize(L); c->edgev.resize(L);
   for (int k = 0; k < L; ++k) { c->sdv[k] = P.take<double>(2 * (size_t)g.nsy); c->edgev[k] = P.take<double>(2 * (size_t)g.nsx); }
   c->f = P.take<double>(nf); c->f_rdst = P.take<double>(nf); c->xb = P.take<double>(nf);
@@ -321,10 +325,11 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   // coarsify fills coarse rows J = n/4+2 .. 3n/4; apply_bc fills rows J = 2, n wholly and
   // the first/last sample of every other row; get_bc reads rows J = n/4+1, 3n/4+1
   {
-    std::vector<unsigned char> top(g.nsy), coarse(g.nsy), fine(g.nsy), ring2(g.nsy);
+    std::vector<unsigned char> top(g.nsy), coarse(g.nsy), fine(g.nsy), ring2(g.nsy), v2f(g.nsy);
     for (int r = 0; r < g.nsy; ++r) {
       bool centre = r >= g.n / 4 && r <= 3 * g.n / 4 - 2;
       bool edge = r == 0 || r == g.nsy - 1;
+      v2f[r] = centre ? ROW_FFT : ROW_SCALE;
       top[r] = centre ? ROW_FFT : ROW_ZERO;
       coarse[r] = (centre || edge) ? ROW_FFT : ROW_EDGES;
       fine[r] = edge ? ROW_SKIP : ROW_EDGES;   // the edge rows come from dst_x_ring_rows
@@ -334,6 +339,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     IB_CUDA_CHECK(cudaMemcpy(c->rm_coarse, coarse.data(), g.nsy, cudaMemcpyHostToDevice));
     IB_CUDA_CHECK(cudaMemcpy(c->rm_fine, fine.data(), g.nsy, cudaMemcpyHostToDevice));
     IB_CUDA_CHECK(cudaMemcpy(c->rm_ring2, ring2.data(), g.nsy, cudaMemcpyHostToDevice));
+    IB_CUDA_CHECK(cudaMemcpy(c->rm_v2f, v2f.data(), g.nsy, cudaMemcpyHostToDevice));
     // points get_bc reads: rows J = n/4+1, 3n/4+1 at I = m/4+1..3m/4+1 and columns
     // I = m/4+1, 3m/4+1 at J = n/4+1..3n/4+1 (vertex row r = J-2, column c = I-2)
     std::vector<int2> pts;
@@ -529,7 +535,7 @@ static int ring_edge_from_modes(Ctx* c, const double* spec, int k, double fac) {
 // tridiagonal systems and evaluates the next finer level's ring from its modes at the few
 // points get_bc reads; one batched inverse pass and the curls finish.
 int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy, bool all_levels,
-                 bool hat0_given) {
+                 bool hat0_given, bool coarse_modes_given) {
   const int L = c->L;
   const GridDims& g = c->g;
   cudaStream_t st = c->st;
@@ -539,24 +545,37 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
   // finest level is then solved in spec2, leaving Y in hat[0] for the correction.
   const bool skip0 = hat0_given && L >= 2;
   double* F0 = skip0 && !all_levels ? c->spec2 : c->hat[0];
+  // The coarser levels are transformed and solved in v2f_modes[k].  coarse_modes_given: their
+  // vorticity is S_x Y_k, Y_k the predictor's modes still in hat[k], except on the rows
+  // coarsify writes, so only those rows are transformed and the others take 2m Y_k.
+  const bool cm = coarse_modes_given && skip0;
+  auto modes = [&](int k) -> double* { return k == 0 ? c->hat[0] : c->v2f_modes[k]; };
   for (int k = 1; k < L; ++k) RC(launch_coarsify(g, w[k - 1], w[k], st));
   {
     DstXArgs a;
     const int k0 = skip0 ? 1 : 0;
     a.nlev = L - k0;
-    for (int k = k0; k < L; ++k) { a.lin[k - k0] = w[k]; a.lout[k - k0] = c->hat[k]; }
+    for (int k = k0; k < L; ++k) {
+      a.lin[k - k0] = w[k];
+      a.lout[k - k0] = modes(k);
+      if (cm) a.lin2[k - k0] = c->hat[k];
+    }
+    if (cm) {
+      a.rowmode = c->rm_v2f;
+      a.row_scale = 2.0 * g.m;
+    }
     ProfScope ps(c, 0, pass_bytes(c, L - k0, L - k0));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
   for (int k = L - 1; k >= 0; --k) {
-    double* F = k == 0 ? F0 : c->hat[k];
+    double* F = k == 0 ? F0 : modes(k);
     // boundary terms of the ring of level k (get_bc of level k+1), apply_bc with fac 1, added
     // by the solve as it loads its right-hand side
     TriBc bc;
     if (k < L - 1) bc = level_bc(c, k, k == 0 && skip0 ? 2.0 * g.m : 1.0);
     {
       ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-      RC(tri_solve(c->tri_ctci, c->hat[k], F, g.nsx, c->tl, st, bc));
+      RC(tri_solve(c->tri_ctci, modes(k), F, g.nsx, c->tl, st, bc));
     }
     if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 1.0));
   }
@@ -572,7 +591,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
   {
     DstXArgs a;
     a.nlev = L;
-    for (int k = 0; k < L; ++k) { a.lin[k] = c->hat[k]; a.lout[k] = s[k]; }
+    for (int k = 0; k < L; ++k) { a.lin[k] = modes(k); a.lout[k] = s[k]; }
     ProfScope ps(c, 0, pass_bytes(c, L, L));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
@@ -1285,7 +1304,7 @@ int op_advance(Ctx* c) {
   // correction's vort2flux rewrites every level's streamfunction and fluxes before they are
   // read again: here the coarser levels are coarsified and solved in mode space only
   RC(run_phase(c, c->graph_v2f, [&]() {
-    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), false, true);
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), false, true, true);
   }));
   step_mark(c, 2);
   // forces (timestepper.F90:249-486)
@@ -1432,7 +1451,7 @@ int op_advance(Ctx* c) {
     // omega_1 was S_x Y (the predictor's modes, still in hat[0]) and vort is S_x Y' (ainv's
     // modes, in spec1): the corrected omega_1 has modes Y - Y'
     if (L >= 2) RC(launch_sub(g.ns, c->hat[0], c->spec1, c->hat[0], c->st));
-    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2);
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true);
   }));
   step_mark(c, 9);
   int rc = check_err(c);
