@@ -112,6 +112,7 @@ struct Ctx {
   // vort2flux's modes of the coarser levels (k >= 1; hat[k] keeps the predictor's meanwhile)
   std::vector<double*> v2f_modes;
   unsigned char* rm_v2f = nullptr; // the rows coarsify writes: transformed; the others: ROW_SCALE
+  unsigned char* rm_pinv = nullptr;   // the rows coarsify writes: skipped; the others: transformed
   // per level: the boundary terms its solve adds (TriBc: ring end sums, edge-row transforms)
   std::vector<double*> sdv, edgev;
   double* emat = nullptr;          // edge matrix (dst_edge_matrix), (m-1) x (m-1)

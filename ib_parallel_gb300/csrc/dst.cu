@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
     int mode = ROW_FFT;
     if (line >= nl || row >= nrows) mode = ROW_SKIP;
     else if (a.rowrange) mode = (row >= a.rowrange[0] && row < a.rowrange[1]) ? ROW_FFT : a.rowrange[2];
-    else if (a.rowmode) mode = a.rowmode[row];
+    else if (a.rowmode && (int)blockIdx.y >= a.rowmode_level0) mode = a.rowmode[row];
     s_mode[threadIdx.x] = mode;
     if (mode == ROW_FFT) atomicOr(&s_any, 1);
   }

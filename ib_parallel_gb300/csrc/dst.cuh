@@ -63,6 +63,7 @@ struct DstXArgs {
   double post_scale = 0.0;
   // optional per-row treatment (ROW_*); rows not listed are transformed
   const unsigned char* rowmode = nullptr;
+  int rowmode_level0 = 0;        // in a batch, levels below this transform every row
   double row_scale = 0.0;        // ROW_SCALE rows: row_scale * in2 (lin2[level])
   // optional device range [rr[0], rr[1]) of transformed rows; others get mode rr[2]
   const int* rowrange = nullptr;
