@@ -601,7 +601,35 @@ __global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThread
   // per lane, joined by seg_tree (k_dense_mv's layout and order)
   const int S = mv_segments(nf), gpw = 32 / S, cw = (nf + S - 1) / S;
   const int grp = lane / S, seg = lane - grp * S;
+  // When the slice's rows take one pass of the three warps and a segment fits, each lane keeps
+  // its segment of its row in registers for the whole solve (the same two chains, same order)
+  constexpr int kRegSeg = 20;
+  const bool a_in_regs = nl <= 3 * gpw && cw <= kRegSeg;
+  const int rl_r = warp * gpw + grp;
+  const bool live_r = warp < 3 && grp < gpw && rl_r < nl;
+  const int j0_r = min(nf, seg * cw), len_r = live_r ? min(nf, j0_r + cw) - j0_r : 0;
+  double areg[kRegSeg];
   auto matvec = [&]() {
+    if (a_in_regs) {
+      double p = 0.0;
+      if (live_r) {
+        double e = 0.0, o = 0.0;
+        const double* v = vfull + j0_r;
+#pragma unroll
+        for (int t = 0; t < kRegSeg; t += 2) {
+          if (t + 1 < len_r) {
+            e = fma(areg[t], v[t], e);
+            o = fma(areg[t + 1], v[t + 1], o);
+          } else if (t < len_r) {
+            e = fma(areg[t], v[t], e);
+          }
+        }
+        p = e + o;
+      }
+      p = seg_tree(p, seg, S);
+      if (live_r && seg == 0) avs[rl_r] = p;
+      return;
+    }
     for (int rb = 0; rb < nl; rb += 3 * gpw) {
       const int rl = rb + warp * gpw + grp;
       const bool live = grp < gpw && rl < nl;
@@ -626,6 +654,14 @@ __global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThread
     }
   };
 
+  if (a_in_regs) {
+#pragma unroll
+    for (int t = 0; t < kRegSeg; ++t) {
+      const int j = j0_r + t;
+      areg[t] = 0.0;
+      if (t < len_r) areg[t] = a_in_smem ? As[(size_t)rl_r * nf + j] : At[(size_t)j * nf + r0 + rl_r];
+    }
+  }
   int its = 0, cycles = 0, reason = 0, k = 0;
   double ttol = 0.0;
   for (;;) {
