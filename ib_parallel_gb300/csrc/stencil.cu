@@ -48,14 +48,6 @@ __global__ void k_nonlinear(GridDims g, const double* __restrict__ om, const dou
   nonlinear_at(g, blockIdx.x * blockDim.x + threadIdx.x, om, bc, qx, q0x, qy, q0y, nlx, nly);
 }
 
-// Every level at once (blockIdx.y = level).
-__global__ void k_nonlinear_levels(GridDims g, NlBatch b) {
-  IB_GRID_DEP_WAIT();
-  const int l = blockIdx.y;
-  nonlinear_at(g, blockIdx.x * blockDim.x + threadIdx.x, b.om[l], b.bc[l], b.qx[l], b.q0x[l], b.qy[l], b.q0y[l],
-               b.nlx[l], b.nly[l]);
-}
-
 // ------------------------------------------------------------------ rot
 // rot_int + rot_bc (operators_fluid.F90:203-233): the transpose of curl.
 __device__ __forceinline__ void rot_at(const GridDims& g, int t, const double* __restrict__ hx,
@@ -73,11 +65,85 @@ __global__ void k_rot(GridDims g, const double* __restrict__ hx, const double* _
   IB_GRID_DEP_WAIT();
   rot_at(g, blockIdx.x * blockDim.x + threadIdx.x, hx, hy, vort);
 }
-// Every level at once (blockIdx.y = level): level l from b.nlx[l], b.nly[l] into b.out[l].
-__global__ void k_rot_levels(GridDims g, NlBatch b) {
+// nonlinear then rot of every level at once (blockIdx.y = level), on tiles of kNlTx x kNlTy
+// vertices: the tile's total face fluxes (q + q0), their averages at the vertices and the
+// ghosted vorticity are formed once in shared memory and serve every term that reads them,
+// so the FP64 work per vertex falls from 25 to 15 operations; the face fields of the nonlinear
+// terms stay in shared memory.  Same averages and products as nonlinear_at and rot_at.
+constexpr int kNlTx = 32, kNlTy = 8;
+__global__ void __launch_bounds__(kNlTx * kNlTy) k_nonlinear_rot_levels(GridDims g, NlBatch b, int tiles_x) {
   IB_GRID_DEP_WAIT();
+  __shared__ double sQy[kNlTy + 2][kNlTx + 1];   // QY(i, j), i = I0-1+c, j = J0-1+r
+  __shared__ double sQx[kNlTy + 1][kNlTx + 2];   // QX(i, j), i = I0-1+c, j = J0-1+r
+  __shared__ double sW[kNlTy + 2][kNlTx + 2];    // omega with ghosts, i = I0-1+c, j = J0-1+r
+  __shared__ double sV[kNlTy + 2][kNlTx];        // v averaged at vertex (i, j), i = I0+c, j = J0-1+r
+  __shared__ double sU[kNlTy][kNlTx + 2];        // u averaged at vertex (i, j), i = I0-1+c, j = J0+r
+  __shared__ double sNx[kNlTy + 1][kNlTx];       // nlx at u-face (i, j), i = I0+c, j = J0-1+r
+  __shared__ double sNy[kNlTy][kNlTx + 1];       // nly at v-face (i, j), i = I0-1+c, j = J0+r
   const int l = blockIdx.y;
-  rot_at(g, blockIdx.x * blockDim.x + threadIdx.x, b.nlx[l], b.nly[l], b.out[l]);
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int I0 = 2 + tx * kNlTx, J0 = 2 + ty * kNlTy;
+  const double* __restrict__ om = b.om[l];
+  const double* __restrict__ bc = b.bc[l];
+  const double* __restrict__ qx = b.qx[l];
+  const double* __restrict__ q0x = b.q0x[l];
+  const double* __restrict__ qy = b.qy[l];
+  const double* __restrict__ q0y = b.q0y[l];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // fluxes outside the physical face grids are zero; entries beyond the vertex grid serve only
+  // vertices outside the interior, which write nothing
+  for (int q = tid; q < (kNlTy + 2) * (kNlTx + 1); q += nt) {
+    const int r = q / (kNlTx + 1), c = q - r * (kNlTx + 1);
+    const int i = I0 - 1 + c, j = J0 - 1 + r;
+    double v = 0.0;
+    if (i >= 1 && i <= g.m && j >= 1 && j <= g.n + 1) {
+      const int idx = (j - 1) * g.nvx + (i - 1);
+      v = qy[idx] + (q0y ? q0y[idx] : 0.0);
+    }
+    sQy[r][c] = v;
+  }
+  for (int q = tid; q < (kNlTy + 1) * (kNlTx + 2); q += nt) {
+    const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+    const int i = I0 - 1 + c, j = J0 - 1 + r;
+    double v = 0.0;
+    if (i >= 1 && i <= g.m + 1 && j >= 1 && j <= g.n) {
+      const int idx = (j - 1) * g.nux + (i - 1);
+      v = qx[idx] + (q0x ? q0x[idx] : 0.0);
+    }
+    sQx[r][c] = v;
+  }
+  for (int q = tid; q < (kNlTy + 2) * (kNlTx + 2); q += nt) {
+    const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+    const int i = I0 - 1 + c, j = J0 - 1 + r;
+    sW[r][c] = (i >= 1 && i <= g.m + 1 && j >= 1 && j <= g.n + 1) ? ghost_vertex(om, bc, g, i, j) : 0.0;
+  }
+  __syncthreads();
+  for (int q = tid; q < (kNlTy + 2) * kNlTx; q += nt) {
+    const int r = q / kNlTx, c = q - r * kNlTx;
+    sV[r][c] = 0.5 * (sQy[r][c + 1] + sQy[r][c]);   // 0.5 (QY(i, j) + QY(i-1, j))
+  }
+  for (int q = tid; q < kNlTy * (kNlTx + 2); q += nt) {
+    const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+    sU[r][c] = 0.5 * (sQx[r + 1][c] + sQx[r][c]);   // 0.5 (QX(i, j) + QX(i, j-1))
+  }
+  __syncthreads();
+  for (int q = tid; q < (kNlTy + 1) * kNlTx; q += nt) {
+    const int r = q / kNlTx, c = q - r * kNlTx;
+    const double v1 = sV[r + 1][c], v0 = sV[r][c], w1 = sW[r + 1][c + 1], w0 = sW[r][c + 1];
+    sNx[r][c] = 0.5 * (v1 * w1 + v0 * w0);
+  }
+  for (int q = tid; q < kNlTy * (kNlTx + 1); q += nt) {
+    const int r = q / (kNlTx + 1), c = q - r * (kNlTx + 1);
+    const double u1 = sU[r][c + 1], u0 = sU[r][c], w1 = sW[r + 1][c + 1], w0 = sW[r + 1][c];
+    sNy[r][c] = -0.5 * (u1 * w1 + u0 * w0);
+  }
+  __syncthreads();
+  const int cx = tid % kNlTx, cy = tid / kNlTx;
+  const int I = I0 + cx, J = J0 + cy;
+  if (cy < kNlTy && I <= g.m && J <= g.n) {
+    const double a = sNy[cy][cx + 1], bb = sNy[cy][cx], c = sNx[cy + 1][cx], d = sNx[cy][cx];
+    b.out[l][(size_t)(J - 2) * g.nsx + (I - 2)] = a - bb - c + d;
+  }
 }
 
 // ----------------------------------------------------------------- curl
@@ -219,11 +285,9 @@ int launch_nonlinear(const GridDims& g, const double* om, const double* bc, cons
 }
 int launch_nonlinear_rot_levels(const GridDims& g, const NlBatch& b, int nlev, cudaStream_t st) {
   if (nlev < 1 || nlev > kMaxLevels) return IB_ERR_ARG;
+  const int tiles_x = cdiv(g.nsx, kNlTx), tiles_y = cdiv(g.nsy, kNlTy);
   count_launch();
-  k_nonlinear_levels<<<dim3(blocks(g.nu + g.nv), nlev), 256, 0, st>>>(g, b);
-  IB_CUDA_CHECK(cudaGetLastError());
-  count_launch();
-  k_rot_levels<<<dim3(blocks(g.ns), nlev), 256, 0, st>>>(g, b);
+  k_nonlinear_rot_levels<<<dim3(tiles_x * tiles_y, nlev), kNlTx * kNlTy, 0, st>>>(g, b, tiles_x);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vort, cudaStream_t st) {
