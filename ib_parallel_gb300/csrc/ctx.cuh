@@ -236,8 +236,10 @@ int op_dst(Ctx* c, const double* in, double* out);
 int op_predictor(Ctx* c, int k, double* om, const double* rhs, const double* rhs_old, const double* rhsbc);
 // coarse_modes_given: the coarser levels' vorticity outside the rows coarsify writes is the
 // inverse x transform of the predictor's modes still in hat[k] (within a time step only)
+// hat0_add (with hat0_given): the finest level's modes are hat[0] + hat0_add
 int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy,
-                 bool all_levels, bool hat0_given = false, bool coarse_modes_given = false);
+                 bool all_levels, bool hat0_given = false, bool coarse_modes_given = false,
+                 const double* hat0_add = nullptr);
 int op_schur(Ctx* c, const double* x, double* y, bool with_b);
 int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out, double* s_out,
                 const double** ring0_out);

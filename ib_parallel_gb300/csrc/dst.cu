@@ -353,15 +353,18 @@ struct XPre {
   const double *in2, *in3, *in4, *ring;
   double* save;
   double ca, cb, alpha, beta, fac;
+  const int* box;
 };
 __device__ __forceinline__ XPre x_pre(const DstXArgs& a, int l, bool batch) {
   XPre p;
   if (batch) {
     p.in2 = a.lin2[l]; p.in3 = nullptr; p.in4 = a.lin4[l]; p.ring = a.lring[l]; p.save = a.lsave[l];
     p.ca = a.lca[l]; p.cb = a.lcb[l]; p.alpha = a.lalpha[l]; p.beta = a.lbeta[l]; p.fac = a.lfac[l];
+    p.box = nullptr;
   } else {
     p.in2 = a.in2; p.in3 = a.in3; p.in4 = a.in4; p.ring = a.ring; p.save = a.save;
     p.ca = a.ca; p.cb = a.cb; p.alpha = a.alpha; p.beta = a.beta; p.fac = a.fac;
+    p.box = a.box;
   }
   return p;
 }
@@ -375,6 +378,17 @@ __device__ __forceinline__ double x_load(const XPre& a, const double* __restrict
     v = in[idx];
   } else if (PRE == PRE_COMBINE) {
     v = fma(a.cb, a.in2[idx], a.ca * in[idx]) + a.in3[idx];
+  } else if (PRE == PRE_ROT) {
+    const int I = j + 2, J = row + 2;
+    const int i0 = a.box[0], j0 = a.box[1], i1 = i0 + a.box[2], j1 = j0 + a.box[3];
+    auto inbox = [&](int i, int jj) { return i >= i0 && i < i1 && jj >= j0 && jj < j1; };
+    const double* hx = in;
+    const double* hy = a.in2;
+    const double va = inbox(I, J) ? hy[(size_t)(J - 1) * g.nvx + (I - 1)] : 0.0;
+    const double vb = inbox(I - 1, J) ? hy[(size_t)(J - 1) * g.nvx + (I - 2)] : 0.0;
+    const double vc = inbox(I, J) ? hx[(size_t)(J - 1) * g.nux + (I - 1)] : 0.0;
+    const double vd = inbox(I, J - 1) ? hx[(size_t)(J - 2) * g.nux + (I - 1)] : 0.0;
+    v = va - vb - vc + vd;
   } else if (PRE == PRE_PRED) {
     // con1 rhs + con2 rhs_old + rhsbc + (w - c L w)/normalize, L the 5-point
     // Laplacian with zero boundary: alpha = (1-4c)/normalize, beta = c/normalize
@@ -976,6 +990,13 @@ int dst_pass_x(const DstPlan& px, int nrows, int ld, DstPre pre, const DstXArgs&
       if (rc) return rc;
       count_launch();
       k_dst_x<PRE_PRED><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B, L.narrow_scan);
+      break;
+    case PRE_ROT:
+      if (!a.box || !a.in2) return IB_ERR_ARG;
+      rc = launch_cfg(k_dst_x<PRE_ROT>, smem);
+      if (rc) return rc;
+      count_launch();
+      k_dst_x<PRE_ROT><<<grid, L.NT, smem, st>>>(d, nrows, ld, a, g, L.B, L.narrow_scan);
       break;
     default:
       rc = launch_cfg(k_dst_x<PRE_APPLYBC>, smem);

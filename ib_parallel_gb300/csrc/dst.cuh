@@ -43,7 +43,7 @@ size_t dst_plan_table_doubles(int N);
 // be passed to dst_plan_destroy).  dev must hold dst_plan_table_doubles(N) doubles, 16-byte aligned.
 int dst_plan_init_external(DstPlan* p, int N, double* dev, cudaStream_t st);
 
-enum DstPre { PRE_COPY = 0, PRE_COMBINE = 1, PRE_APPLYBC = 2, PRE_PRED = 3 };
+enum DstPre { PRE_COPY = 0, PRE_COMBINE = 1, PRE_APPLYBC = 2, PRE_PRED = 3, PRE_ROT = 4 };
 enum DstYMode { YMODE_NONE = 0 };
 
 struct DstXArgs {
@@ -57,6 +57,9 @@ struct DstXArgs {
   double fac = 1.0;              // PRE_APPLYBC factor; PRE_PRED without in3: rhsbc factor
   // PRE_PRED without in3: rhsbc (timestepper.F90:184-189) is formed on the fly from `ring`
   double* save = nullptr;        // PRE_PRED: receives a copy of `in` (may alias in2)
+  // PRE_ROT: rot (operators_fluid.F90:203-233) of the face fields in (u-faces) and in2
+  // (v-faces), read only inside the face box box[0..3] = i0, j0, ni, nj (zero outside)
+  const int* box = nullptr;
   double* out = nullptr;         // nlines rows, pitch ld
   // optional output post-op: out = DST(row) + post_scale * post_add
   const double* post_add = nullptr;

@@ -191,10 +191,11 @@ int launch_reg_snapshot(int nf, const RegDev& r, int* ix_s, int* iy_s, double* w
 }
 
 // E^T h0: every face of the box gets the ordered sum of weight*h0 over its list.
+// zero_empty: faces of the box with no contribution are written as zero (else left as they are).
 __global__ void k_reg(GridDims g, const double* __restrict__ h0, const double* __restrict__ w,
                       const int* __restrict__ bbox, const int* __restrict__ cnt_x, const int* __restrict__ cnt_y,
                       const int* __restrict__ lst_x, const int* __restrict__ lst_y, double* hx, double* hy,
-                      int max_faces) {
+                      int max_faces, int zero_empty) {
   IB_GRID_DEP_WAIT();
   int i0 = bbox[0], j0 = bbox[1], ni = bbox[2], nj = bbox[3];
   int nface = ni * nj;
@@ -206,10 +207,10 @@ __global__ void k_reg(GridDims g, const double* __restrict__ h0, const double* _
     const int* cnt = cx ? cnt_x : cnt_y;
     const int* lst = cx ? lst_x : lst_y;
     int a = cnt[fidx], b = cnt[fidx + 1];
-    if (a == b) continue;
     // faces outside the grid (a body too close to the edge, flagged as IB_ERR_DOMAIN
     // when the weights were built) are skipped rather than written
     if (fi < 1 || fj < 1 || fi > (cx ? g.nux : g.nvx) || fj > (cx ? g.nuy : g.nvy)) continue;
+    if (a == b && !zero_empty) continue;
     double acc = 0.0;
     for (int q = a; q < b; ++q) {
       int e = lst[q];
@@ -226,7 +227,16 @@ int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, dou
   IB_CUDA_CHECK(cudaMemsetAsync(hy, 0, sizeof(double) * g.nv, st));
   if (nf == 0) return IB_OK;
   count_launch();
-  k_reg<<<152 * 2, 128, 0, st>>>(g, h0, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, hx, hy, r.max_faces);
+  k_reg<<<152 * 2, 128, 0, st>>>(g, h0, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, hx, hy, r.max_faces, 0);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int launch_reg_box(const GridDims& g, int nf, const double* h0, const RegDev& r, double* hx, double* hy,
+                   cudaStream_t st) {
+  if (nf == 0) return IB_OK;
+  count_launch();
+  k_reg<<<152 * 2, 128, 0, st>>>(g, h0, r.w, r.bbox, r.cnt_x, r.cnt_y, r.lst_x, r.lst_y, hx, hy, r.max_faces, 1);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -76,6 +76,10 @@ int launch_reg_snapshot(int nf, const RegDev& r, int* ix_s, int* iy_s, double* w
 // hx, hy must be zero outside the stencil box; this writes every face in the box.
 int launch_reg(const GridDims& g, int nf, const double* h0, const RegDev& r, double* hx, double* hy,
                cudaStream_t st);
+// The same without clearing the fields: every face of the box is written (zero where no
+// unknown contributes), the faces outside it are left as they are (read through the box only).
+int launch_reg_box(const GridDims& g, int nf, const double* h0, const RegDev& r, double* hx, double* hy,
+                   cudaStream_t st);
 // h0 (+)= E q   (accumulate=1 keeps the incoming h0, fsinterface.F90:51-80)
 int launch_regT(const GridDims& g, int nf, const double* qx, const double* qx0, const double* qy,
                 const double* qy0, const RegDev& r, const double* h0_in, double* h0_out, cudaStream_t st);

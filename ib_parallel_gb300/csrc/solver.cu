@@ -538,7 +538,7 @@ static int ring_edge_from_modes(Ctx* c, const double* spec, int k, double fac) {
 // tridiagonal systems and evaluates the next finer level's ring from its modes at the few
 // points get_bc reads; one batched inverse pass and the curls finish.
 int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, double* const* qy, bool all_levels,
-                 bool hat0_given, bool coarse_modes_given) {
+                 bool hat0_given, bool coarse_modes_given, const double* hat0_add) {
   const int L = c->L;
   const GridDims& g = c->g;
   cudaStream_t st = c->st;
@@ -576,6 +576,7 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     // by the solve as it loads its right-hand side
     TriBc bc;
     if (k < L - 1) bc = level_bc(c, k, k == 0 && skip0 ? 2.0 * g.m : 1.0);
+    if (k == 0 && skip0) bc.add2 = hat0_add;
     {
       ProfScope ps(c, 1, pass_bytes(c, 1, 1));
       RC(tri_solve(c->tri_ctci, modes(k), F, g.nsx, c->tl, st, bc));
@@ -1439,24 +1440,32 @@ int op_advance(Ctx* c) {
   // correction on the finest grid (timestepper.F90:488-553)
   step_mark(c, 8);
   RC(run_phase(c, c->graph_corr, [&]() -> int {
+    if (c->nf > 0) {
+      // ainv of rot(E^T f): rot is formed as the x pass loads its rows (the face fields are
+      // read inside the stencil box only, which E^T writes wholly), and the input is zero
+      // outside the rows the stencils touch, so the forward transform runs on those rows
+      // only (the others' modes are zero).  The solve negates its right-hand side on load, so
+      // spec1 = -Y' (ainv's modes) exactly, and the inverse pass adds S_x(-Y') to omega_1 as
+      // it stores: omega_1 - vort in one pass.
+      RC(launch_reg_box(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
+      DstXArgs a;
+      a.in = c->hx; a.in2 = c->hy; a.box = c->reg.bbox; a.out = c->spec1; a.rowrange = c->reg.bbox + 4;
+      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_ROT, a, g, c->lx_small, c->st));
+      TriBc neg;
+      neg.post_scale = -1.0;
+      RC(tri_solve(c->tri_ainv, c->spec1, c->spec1, g.nsx, c->tl, c->st, neg));
+      DstXArgs b;
+      b.in = c->spec1; b.out = c->omega[0]; b.post_add = c->omega[0]; b.post_scale = 1.0;
+      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx, c->st));
+      // omega_1 was S_x Y (the predictor's modes, still in hat[0]): the corrected omega_1 has
+      // modes Y - Y' = hat[0] + spec1, which the finest level's solve forms as it loads them
+      return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true,
+                          L >= 2 ? c->spec1 : nullptr);
+    }
     RC(launch_reg(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
     RC(launch_rot(g, c->hx, c->hy, c->vort, c->st));
-    // ainv of rot(E^T f): the input is zero outside the rows the body's stencils touch, so
-    // the forward transform runs on those rows only (the others' modes are zero)
-    if (c->nf > 0) {
-      DstXArgs a;
-      a.in = c->vort; a.out = c->spec1; a.rowrange = c->reg.bbox + 4;
-      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, c->st));
-      RC(tri_solve(c->tri_ainv, c->spec1, c->spec1, g.nsx, c->tl, c->st));
-      DstXArgs b;
-      b.in = c->spec1; b.out = c->vort;
-      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx, c->st));
-    } else {
-      RC(op_ainv(c, c->vort, c->vort));
-    }
+    RC(op_ainv(c, c->vort, c->vort));
     RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], c->st));
-    // omega_1 was S_x Y (the predictor's modes, still in hat[0]) and vort is S_x Y' (ainv's
-    // modes, in spec1): the corrected omega_1 has modes Y - Y'
     if (L >= 2) RC(launch_sub(g.ns, c->hat[0], c->spec1, c->hat[0], c->st));
     return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true);
   }));

@@ -137,7 +137,13 @@ __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld,
       for (int u = 0; u < 8; ++u) {
         int rr = r + u * rstep;
         v[u] = 0.0;
-        if (rr < ny) { if (kin) v[u] = tri_rhs(bc, ny, nx, rr, k0 + kl0, src[(size_t)rr * ld]); }
+        if (rr < ny) {
+          if (kin) {
+            double f = src[(size_t)rr * ld];
+            if (bc.add2) f = f + bc.add2[(size_t)rr * ld + k0 + kl0];
+            v[u] = tri_rhs(bc, ny, nx, rr, k0 + kl0, f);
+          }
+        }
         else if (rr < tot) v[u] = __ldg(tsrc + (size_t)(rr - ny) * nx);
       }
 #pragma unroll
@@ -243,6 +249,11 @@ __global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restr
 #pragma unroll
   for (int j = 0; j < S; ++j) f[j] = chunk ? F[(size_t)(r0 + j) * ld + k] : 0.0;
   double fi = (chunk && c >= 1) ? F[(size_t)(r0 - 1) * ld + k] : 0.0;
+  if (chunk && bc.add2) {
+#pragma unroll
+    for (int j = 0; j < S; ++j) f[j] = f[j] + bc.add2[(size_t)(r0 + j) * ld + k];
+    if (c >= 1) fi = fi + bc.add2[(size_t)(r0 - 1) * ld + k];
+  }
   if (chunk && (bc.sd || bc.post_scale != 1.0)) {
     // boundary terms (tri_rhs) on the chunk rows and the interface row above; row 0 is chunk
     // 0's first row and row ny-1 chunk C-1's last

@@ -46,12 +46,14 @@ size_t tri_table_doubles(int nx, int s, int C);
 int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, double* dev_mem);
 // Boundary terms a solve adds to its right-hand side as it loads it (a finer level of the
 // coarse-to-fine recursions, dst_ring_edge_from_modes): row r of mode k is
-//     post_scale F[r][k] + sk2[k] sd[(k & 1) ny + r]  (+ edge[k] on row 0, + edge[nx + k] on row ny-1).
-// sd == nullptr: post_scale F only.
+//     post_scale (F[r][k] + add2[r][k]) + sk2[k] sd[(k & 1) ny + r]
+//     (+ edge[k] on row 0, + edge[nx + k] on row ny-1).
+// sd == nullptr: post_scale (F + add2) only; add2 == nullptr: F alone (add2 has F's pitch).
 struct TriBc {
   const double* sk2 = nullptr;
   const double* sd = nullptr;
   const double* edge = nullptr;
+  const double* add2 = nullptr;
   double post_scale = 1.0;
 };
 
