@@ -113,6 +113,14 @@ struct Ctx {
   std::vector<double*> v2f_modes;
   unsigned char* rm_v2f = nullptr; // the rows coarsify writes: transformed; the others: ROW_SCALE
   unsigned char* rm_pinv = nullptr;   // the rows coarsify writes: skipped; the others: transformed
+  // The step's first vort2flux transforms the finest level back only on the rows E(curl s)
+  // reads (plus kFsiRowMargin) when the FSI iterations may run on the device; v2f_rows[0..1]
+  // receives the rows, q0_partial says s and q of the finest level hold only those.
+  static constexpr int kFsiRowMargin = 8;
+  bool v2f_partial = false;
+  bool q0_partial = false;
+  int* v2f_rows = nullptr;
+  double* v2f_f0 = nullptr;        // the finest level's solved modes of that call
   // per level: the boundary terms its solve adds (TriBc: ring end sums, edge-row transforms)
   std::vector<double*> sdv, edgev;
   double* emat = nullptr;          // edge matrix (dst_edge_matrix), (m-1) x (m-1)

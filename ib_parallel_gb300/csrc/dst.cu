@@ -455,7 +455,14 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
     s_row[threadIdx.x] = row;
     int mode = ROW_FFT;
     if (line >= nl || row >= nrows) mode = ROW_SKIP;
-    else if (a.rowrange) mode = (row >= a.rowrange[0] && row < a.rowrange[1]) ? ROW_FFT : a.rowrange[2];
+    else if (a.rowrange) {
+      const int lo = max(0, a.rowrange[0] - a.row_margin), hi = min(nrows, a.rowrange[1] + a.row_margin);
+      mode = (row >= lo && row < hi) ? ROW_FFT : a.rowrange[2];
+      if (a.rows_used && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+        a.rows_used[0] = lo;
+        a.rows_used[1] = hi;
+      }
+    }
     else if (a.rowmode && (int)blockIdx.y >= a.rowmode_level0) mode = a.rowmode[row];
     s_mode[threadIdx.x] = mode;
     if (mode == ROW_FFT) atomicOr(&s_any, 1);

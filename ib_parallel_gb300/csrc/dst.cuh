@@ -70,6 +70,8 @@ struct DstXArgs {
   double row_scale = 0.0;        // ROW_SCALE rows: row_scale * in2 (lin2[level])
   // optional device range [rr[0], rr[1]) of transformed rows; others get mode rr[2]
   const int* rowrange = nullptr;
+  int row_margin = 0;            // rowrange widened by this many rows on each side (clamped)
+  int* rows_used = nullptr;      // receives the (widened) range of transformed rows
   // optional strided row subset: line i is row row0 + i*row_step, i < nlines (0: all rows)
   int nlines = 0, row0 = 0, row_step = 0;
   // optional batch over grid levels (PRE_COPY, PRE_PRED): level l (blockIdx.y) reads lin[l] and

@@ -82,6 +82,12 @@ __global__ void __launch_bounds__(128) k_fsi_update(FsiUpdateArgs a) {
   __syncthreads();
   reg_weights_cta(a.g, a.nf, k0, pos, a.delta, a.ox, a.oy, a.comp, a.ix, a.iy, a.w, a.stale, a.d_err, fac, wsm,
                   org);
+  if (a.rows && tid < 8 && k0 + tid < kend) {
+    // E(curl s) at this stencil reads the streamfunction on vertex rows cy-5 .. cy+2
+    const int cy = org[tid][1];
+    const int r0 = max(0, cy - 5), r1 = min(a.g.nsy - 1, cy + 2);
+    if (r0 < a.rows[0] || r1 >= a.rows[1]) atomicOr(a.flag, 4);
+  }
   for (int t = tid; t < 8 * 64; t += blockDim.x) {
     const int u = t >> 6, q = t & 63;
     if (k0 + u >= kend) break;

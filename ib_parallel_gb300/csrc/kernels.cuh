@@ -148,6 +148,9 @@ struct FsiUpdateArgs {
   int ntx, tile;
   double* pval;
   int *pidx, *used, *flag;
+  // rows [rows[0], rows[1]) of the finest streamfunction and fluxes that are valid (null: all);
+  // an unknown whose stencil needs others sets bit 4 of the band flag, which ends the loop
+  const int* rows;
   // condition: counters (as k_fsi_loop_cond), the Krylov counters, the ticket
   int* cnt;
   const int* ist;

@@ -258,6 +258,8 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   for (int k = 1; k < L; ++k) c->v2f_modes[k] = P.take<double>(ns);
   c->rm_v2f = P.take<unsigned char>(g.nsy);
   c->rm_pinv = P.take<unsigned char>(g.nsy);
+  c->v2f_rows = P.take<int>(4);
+  c->v2f_partial = nf > 0 && nt > 0 && !p.num_stat;
   c->sdv.resize(L); c->edgev.resize(L);
   for (int k = 0; k < L; ++k) { c->sdv[k] = P.take<double>(2 * (size_t)g.nsy); c->edgev[k] = P.take<double>(2 * (size_t)g.nsx); }
   c->f = P.take<double>(nf); c->f_rdst = P.take<double>(nf); c->xb = P.take<double>(nf);
@@ -594,6 +596,12 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
   if (!all_levels) {
     DstXArgs a;
     a.in = F0; a.out = s[0];
+    c->v2f_f0 = F0;
+    if (c->v2f_partial) {   // the rows E(curl s) reads, widened; the others are left as they are
+      a.rowrange = c->reg.bbox + 7;
+      a.row_margin = Ctx::kFsiRowMargin;
+      a.rows_used = c->v2f_rows;
+    }
     {
       ProfScope ps(c, 0, pass_bytes(c, 1, 1));
       RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
@@ -1188,6 +1196,7 @@ static int build_fsi_loop(Ctx* c) {
         u.ix = c->reg.ix; u.iy = c->reg.iy; u.w = c->reg.w; u.stale = c->reg.stale; u.d_err = c->d_err;
         u.tile_of = I.tile_of; u.ntx = I.ntx; u.tile = Influence::kTile;
         u.pval = I.pval; u.pidx = I.pidx; u.used = I.used; u.flag = I.flag;
+        u.rows = c->v2f_partial ? c->v2f_rows : nullptr;
         u.cnt = c->fsi_cnt; u.ist = c->G.ist; u.tol = p.fsi_tol; u.max_it = p.fsi_max_it; u.h = h;
         u.done = c->fsi_done;
         RC(launch_fsi_update(u, s1));
@@ -1322,6 +1331,7 @@ int op_advance(Ctx* c) {
   RC(run_phase(c, c->graph_v2f, [&]() {
     return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), false, true, true);
   }));
+  c->q0_partial = c->v2f_partial;
   step_mark(c, 2);
   // forces (timestepper.F90:249-486)
   if (c->nf > 0) {
@@ -1356,7 +1366,7 @@ int op_advance(Ctx* c) {
           c->n_matvec += c->h_ist[2];
           count_launches(1 + c->fsi_body_launches * (long long)fsi_count + c->fsi_post_launches);
           I.assemblies += fsi_count;
-          I.flag_h = c->h_ist[3];
+          I.flag_h = c->h_ist[3] & 3;   // bit 4: a stencil left the rows of s computed (below)
           I.patch_fresh = true;
           I.active = false;
           err = c->h_scal[0];
@@ -1364,6 +1374,14 @@ int op_advance(Ctx* c) {
         }
       }
       while (err >= p.fsi_tol && fsi_count <= p.fsi_max_it) {
+        if (c->q0_partial) {
+          // the host iterations read the finest fluxes at any stencil: complete s and q
+          DstXArgs a;
+          a.in = c->v2f_f0; a.out = c->s[0];
+          RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
+          RC(launch_curl(g, c->s[0], L == 1 ? c->zero_ring : c->ringv[0], c->qx[0], c->qy[0], st));
+          c->q0_partial = false;
+        }
         fsi_count += 1;
         step_mark(c, 3);
         RC(run_phase(c, c->graph_fsi_rhs, [&]() -> int {
