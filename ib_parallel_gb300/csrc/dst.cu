@@ -353,18 +353,24 @@ struct XPre {
   const double *in2, *in3, *in4, *ring;
   double* save;
   double ca, cb, alpha, beta, fac;
-  const int* box;
+  int bi0, bj0, bi1, bj1;   // PRE_ROT: the face box [bi0, bi1) x [bj0, bj1), read once per CTA
 };
 __device__ __forceinline__ XPre x_pre(const DstXArgs& a, int l, bool batch) {
   XPre p;
   if (batch) {
     p.in2 = a.lin2[l]; p.in3 = nullptr; p.in4 = a.lin4[l]; p.ring = a.lring[l]; p.save = a.lsave[l];
     p.ca = a.lca[l]; p.cb = a.lcb[l]; p.alpha = a.lalpha[l]; p.beta = a.lbeta[l]; p.fac = a.lfac[l];
-    p.box = nullptr;
+    p.bi0 = p.bj0 = p.bi1 = p.bj1 = 0;
   } else {
     p.in2 = a.in2; p.in3 = a.in3; p.in4 = a.in4; p.ring = a.ring; p.save = a.save;
     p.ca = a.ca; p.cb = a.cb; p.alpha = a.alpha; p.beta = a.beta; p.fac = a.fac;
-    p.box = a.box;
+    p.bi0 = p.bj0 = p.bi1 = p.bj1 = 0;
+    if (a.box) {
+      p.bi0 = a.box[0];
+      p.bj0 = a.box[1];
+      p.bi1 = p.bi0 + a.box[2];
+      p.bj1 = p.bj0 + a.box[3];
+    }
   }
   return p;
 }
@@ -380,8 +386,7 @@ __device__ __forceinline__ double x_load(const XPre& a, const double* __restrict
     v = fma(a.cb, a.in2[idx], a.ca * in[idx]) + a.in3[idx];
   } else if (PRE == PRE_ROT) {
     const int I = j + 2, J = row + 2;
-    const int i0 = a.box[0], j0 = a.box[1], i1 = i0 + a.box[2], j1 = j0 + a.box[3];
-    auto inbox = [&](int i, int jj) { return i >= i0 && i < i1 && jj >= j0 && jj < j1; };
+    auto inbox = [&](int i, int jj) { return i >= a.bi0 && i < a.bi1 && jj >= a.bj0 && jj < a.bj1; };
     const double* hx = in;
     const double* hy = a.in2;
     const double va = inbox(I, J) ? hy[(size_t)(J - 1) * g.nvx + (I - 1)] : 0.0;
