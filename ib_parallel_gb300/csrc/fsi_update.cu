@@ -1,6 +1,6 @@
 // The end of one device FSI iteration in one kernel: structure update, weights and influence
-// patches at the new positions, and the loop condition (k_tors_dx, k_reg_weights,
-// k_inf_patch and k_fsi_loop_cond of the per-stage path, on the same device bodies).
+// patches at the new positions (k_tors_dx, k_reg_weights and k_inf_patch of the host loop, on
+// the same device bodies), and the loop condition.
 #include "fsi_dev.cuh"
 
 namespace ib {

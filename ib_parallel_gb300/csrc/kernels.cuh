@@ -151,7 +151,8 @@ struct FsiUpdateArgs {
   // rows [rows[0], rows[1]) of the finest streamfunction and fluxes that are valid (null: all);
   // an unknown whose stencil needs others sets bit 4 of the band flag, which ends the loop
   const int* rows;
-  // condition: counters (as k_fsi_loop_cond), the Krylov counters, the ticket
+  // condition: counters ([0] iterations, [1] Krylov iterations, [2] operator applications,
+  // [3] band flag), the cluster solver's counters, the ticket
   int* cnt;
   const int* ist;
   double tol;

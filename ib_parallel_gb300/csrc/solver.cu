@@ -1083,27 +1083,6 @@ __global__ void k_fsi_loop_init(int* cnt, int* band_flag, unsigned* done) {
   }
 }
 
-// End of one device FSI iteration: the counters (the cluster solver's G.ist: [0] Krylov
-// iterations, [4] restart cycles) and the loop condition of timestepper.F90:249 (fsi error
-// at or above the tolerance, iteration count within the limit), which also stops when the
-// next operator's patches leave the influence band (the host rebuilds it) or the error is
-// not finite (the host reports it).
-__global__ void k_fsi_loop_cond(int* cnt, const int* __restrict__ ist, const double* __restrict__ err,
-                                int* band_flag, double tol, int max_it, cudaGraphConditionalHandle h) {
-  IB_GRID_DEP_WAIT();
-  if (threadIdx.x != 0) return;
-  const double e = err[0];
-  const int n = cnt[0] + 1;
-  const int bf = *band_flag;
-  *band_flag = 0;   // the next iteration's patches start from zero
-  cnt[0] = n;
-  cnt[1] += ist[0];
-  cnt[2] += ist[0] + ist[4];
-  cnt[3] = bf;
-  const bool go = isfinite(e) && e >= tol && n <= max_it && bf == 0;
-  cudaGraphSetConditional(h, go ? 1u : 0u);
-}
-
 // Captures the graph of a step's FSI iterations: the counters reset, then a while node whose
 // body is one iteration on the assembled operator, and after it the contribution lists of the
 // final positions.  The body runs its independent parts side by side:
