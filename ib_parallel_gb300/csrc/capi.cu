@@ -121,6 +121,16 @@ int ib_advance(IbCtx* h, int* itime) {
   CTX_OR_FAIL(h);
   int rc = ib::op_advance(c);
   if (itime) *itime = c->itime;
+  if (rc == IB_ERR_GMRES) {
+    std::string m = "advance: the step is complete, but a Krylov solve stopped without converging (KSP reason " +
+                    std::to_string(c->gmres_reason) + ")";
+    return fail(rc, m.c_str());
+  }
+  if (rc == IB_ERR_FSI) {
+    std::string m = "advance: the step is complete, but the FSI iterations stopped at fsi_max_it with error " +
+                    std::to_string(c->fsi_err_capped);
+    return fail(rc, m.c_str());
+  }
   return op_result(rc, "advance failed");
 }
 
@@ -484,11 +494,6 @@ int ib_measure_fp64_peak(double* tflops) {
   if (!tflops) return fail(IB_ERR_ARG, "null output");
   int rc = ib::probe_fp64(tflops);
   return op_result(rc, "fp64 probe failed");
-}
-
-int ib_probe_throughput(int which, double* value) {
-  if (!value || which < 0 || which > 13) return fail(IB_ERR_ARG, "bad probe");
-  return op_result(ib::probe_throughput(which, value), "probe failed");
 }
 
 int ib_time_pass(IbCtx* h, int kind, int reps, double* avg_ms) {

@@ -196,6 +196,10 @@ struct Ctx {
   size_t stage_n = 0;
 
   int itime = 0, ksp_iter = 0, fsi_iter = 0;
+  // outcome of the last step's solves: the most negative KSP reason of its Krylov solves (0
+  // if none failed), and the FSI error when the loop stopped at fsi_max_it (else 0)
+  int gmres_reason = 0;
+  double fsi_err_capped = 0.0;
 
   // work counters (host side): Schur matvecs and DST passes by kind
   long long n_matvec = 0;

@@ -14,7 +14,8 @@ namespace ib {
 //  3. their patches;
 //  4. the CTA that finishes last (a ticket taken after a fence: no CTA waits for another)
 //     commits theta, sin and cos, forms the maximum error and the loop condition of
-//     timestepper.F90:249, clears the band flag for the next patches and resets the ticket.
+//     timestepper.F90:249, keeps the most negative reason of the iterations' Krylov solves,
+//     clears the band flag for the next patches and resets the ticket.
 __global__ void __launch_bounds__(128) k_fsi_update(FsiUpdateArgs a) {
   IB_GRID_DEP_WAIT();
   __shared__ double fac[16][7];
@@ -119,6 +120,7 @@ __global__ void __launch_bounds__(128) k_fsi_update(FsiUpdateArgs a) {
   a.cnt[1] += a.ist[0];
   a.cnt[2] += a.ist[0] + a.ist[4];
   a.cnt[3] = bf;
+  a.cnt[4] = min(a.cnt[4], a.ist[1]);   // a failed Krylov solve (negative KSP reason) sticks
   const bool go = isfinite(e) && e >= a.tol && n <= a.max_it && bf == 0;
   cudaGraphSetConditional(a.h, go ? 1u : 0u);
   *a.done = 0u;

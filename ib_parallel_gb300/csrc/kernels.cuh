@@ -266,8 +266,7 @@ int launch_chol_solve(int n, const double* Lf, const double* b, double* x, cudaS
 int launch_copy_col(int n, const double* src, double* M, int col, cudaStream_t st);
 int launch_unit(int n, int i, double* e, cudaStream_t st);
 
-// probe.cu -- FP64 FMA throughput of the device (the FP64 roof of the DST kernels)
+// fp64_peak.cu -- FP64 FMA throughput of the device (the FP64 roof of the DST kernels)
 int probe_fp64(double* tflops);
-int probe_throughput(int which, double* value);
 
 }  // namespace ib

@@ -1294,6 +1294,8 @@ int op_advance(Ctx* c) {
   const int L = c->L;
   const IbParams& p = c->p;
   cudaStream_t st = c->st;
+  c->gmres_reason = 0;
+  c->fsi_err_capped = 0.0;
   c->itime += 1;
   const int it = c->itime;
   if (it == 1 && p.num_stat && c->nf > 0) RC(preprocess_chol(c));
@@ -1320,6 +1322,7 @@ int op_advance(Ctx* c) {
       double err = 10.0;
       int fsi_count = 0;
       c->ksp_iter = 0;
+      c->gmres_reason = 0;
       const bool moved = c->nt > 0;
       // the iterations on the device while the operator stays assembled on a valid band (the
       // host loop below takes over when a patch leaves it, and runs every step that needs the
@@ -1332,7 +1335,7 @@ int op_advance(Ctx* c) {
                                  c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
         if (device_loop && (c->graph_fsi_loop.exec || build_fsi_loop(c) == IB_OK)) {
           IB_CUDA_CHECK(cudaGraphLaunch(c->graph_fsi_loop.exec, st));
-          IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+          IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st));
           IB_CUDA_CHECK(cudaStreamSynchronize(st));
           if (c->step_prof) {
@@ -1346,6 +1349,7 @@ int op_advance(Ctx* c) {
           count_launches(1 + c->fsi_body_launches * (long long)fsi_count + c->fsi_post_launches);
           I.assemblies += fsi_count;
           I.flag_h = c->h_ist[3] & 3;   // bit 4: a stencil left the rows of s computed (below)
+          c->gmres_reason = std::min(c->gmres_reason, c->h_ist[4]);
           I.patch_fresh = true;
           I.active = false;
           err = c->h_scal[0];
@@ -1398,6 +1402,7 @@ int op_advance(Ctx* c) {
           int its = 0, reason = 0;
           RC(op_gmres(c, c->rhsf, c->f, &its, &reason));
           c->ksp_iter += its;
+          c->gmres_reason = std::min(c->gmres_reason, reason);
         }
         step_mark(c, 6);
         // redistribute, structure update, weights at the new positions and the next solve's
@@ -1427,6 +1432,7 @@ int op_advance(Ctx* c) {
         if (async) {
           c->ksp_iter += c->h_ist[0];
           c->n_matvec += c->h_ist[0] + c->h_ist[4];
+          c->gmres_reason = std::min(c->gmres_reason, c->h_ist[1]);
         }
         if (patch) {
           I.flag_h = I.h_flag[0];
@@ -1436,6 +1442,9 @@ int op_advance(Ctx* c) {
         if (!std::isfinite(err)) return IB_ERR_NONFINITE;
       }
       c->fsi_iter = fsi_count;
+      // the loop of timestepper.F90:318 ends at fsi_max_it + 1 iterations without reaching
+      // fsi_tol; the reference carries on silently, this step reports it (after finishing)
+      c->fsi_err_capped = err >= p.fsi_tol ? err : 0.0;
     } else {
       RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, nullptr, c->rhsf, st));
       RC(launch_chol_solve(c->nf, c->cholM, c->rhsf, c->f, st));
@@ -1476,6 +1485,10 @@ int op_advance(Ctx* c) {
   }));
   step_mark(c, 9);
   int rc = check_err(c);
+  // the step is complete either way; a Krylov solve that stopped without converging, or an
+  // FSI loop that stopped at its cap, is reported once the state is consistent
+  if (rc == IB_OK && c->gmres_reason < 0) rc = IB_ERR_GMRES;
+  else if (rc == IB_OK && c->fsi_err_capped > 0.0) rc = IB_ERR_FSI;
   if (c->step_prof) {
     step_acc(c, 0, 0, 1);
     step_acc(c, 1, 1, 2);

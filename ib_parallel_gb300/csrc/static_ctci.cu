@@ -10,8 +10,9 @@
 // library holds until the process exits, and the caller passes the input and output.
 //
 // Set-up: the first call on a device, and the first call after the grid size changes,
-// looks up the array's device address and fills the tables with synchronous host-to-device
-// copies; make that call before any stream capture.  Later calls with the same grid only
+// looks up the array's device address, fills the tables with host-to-device copies and waits
+// for the device to finish them (cudaDeviceSynchronize); make that call before any stream
+// capture.  Later calls with the same grid only
 // launch three kernels on the caller's stream and return without waiting for them.
 //
 // Every call on a device shares the one array, which keeps what the last call left there.
@@ -75,6 +76,11 @@ int static_ctci(int m, int n, const double* vort, double* s, cudaStream_t st) {
                    "fit in 2^21 doubles)");
     return IB_ERR_ARG;
   }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    set_last_error("ib_ctci_static: no current CUDA device");
+    return IB_ERR_CUDA;
+  }
   for (const void* ptr : {static_cast<const void*>(vort), static_cast<const void*>(s)}) {
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess ||
@@ -83,11 +89,11 @@ int static_ctci(int m, int n, const double* vort, double* s, cudaStream_t st) {
       set_last_error("ib_ctci_static: vort and s must be device (or managed) memory");
       return IB_ERR_ARG;
     }
-  }
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-    set_last_error("ib_ctci_static: no current CUDA device");
-    return IB_ERR_CUDA;
+    // the kernels run on the current device: memory of another GPU would be a peer access
+    if (at.type == cudaMemoryTypeDevice && at.device != dev) {
+      set_last_error("ib_ctci_static: vort and s must be memory of the current device");
+      return IB_ERR_ARG;
+    }
   }
   GridDims g;
   g.init(m, n);
@@ -106,7 +112,10 @@ int static_ctci(int m, int n, const double* vort, double* s, cudaStream_t st) {
     }
     if (S->m != m || S->n != n) {
       // tables after the scratch field: DST plan of the x transform, then the tridiagonal
-      // factors of (lam_x(k) + T_y)^-1 / (2m) (the same operator the context path uses)
+      // factors of (lam_x(k) + T_y)^-1 / (2m) (the same operator the context path uses).
+      // The recorded grid is cleared first: if an upload below fails, no later call may take
+      // the half-rewritten tables for the old grid's.
+      S->m = 0; S->n = 0;
       double* plan_mem = S->base + align4((size_t)g.ns);
       int rc = dst_plan_init_external(&S->px, g.nsx, plan_mem, st);
       if (rc != IB_OK) { set_last_error("ib_ctci_static: table upload failed"); return rc; }
@@ -119,6 +128,13 @@ int static_ctci(int m, int n, const double* vort, double* s, cudaStream_t st) {
       }
       rc = tri_build(&S->tri, g.nsx, g.nsy, lamx.data(), 1.0 / (2.0 * m), tri_mem);
       if (rc != IB_OK) { set_last_error("ib_ctci_static: table upload failed"); return rc; }
+      // tri_build copies from pageable host memory, and such a copy may return before its DMA
+      // has reached the device; the solve kernels run on the caller's stream, which nothing
+      // orders after that copy.  Wait for it here (set-up runs outside any stream capture).
+      if (cudaDeviceSynchronize() != cudaSuccess) {
+        set_last_error("ib_ctci_static: table upload failed");
+        return IB_ERR_CUDA;
+      }
       S->m = m; S->n = n;
     }
   }

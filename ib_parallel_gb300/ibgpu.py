@@ -38,7 +38,7 @@ EXPORTS = [
     "ib_vort2flux", "ib_reg_prep", "ib_reg", "ib_regT", "ib_redistribute", "ib_schur_apply",
     "ib_schur_apply_fluid", "ib_struct_btimes", "ib_struct_rhs", "ib_struct_dx", "ib_schur_solve",
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
-    "ib_launch_count", "ib_probe_throughput", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
+    "ib_launch_count", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
     "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile", "ib_get_launch_shapes",
 ]
 
@@ -103,7 +103,6 @@ def load(path: Optional[os.PathLike] = None):
         "ib_get_work": ([P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
         "ib_measure_fp64_peak": ([D], C.c_int),
         "ib_launch_count": ([], C.c_longlong),
-        "ib_probe_throughput": ([C.c_int, D], C.c_int),
         "ib_time_pass": ([P, C.c_int, C.c_int, D], C.c_int),
         "ib_profile_schur": ([P, C.c_int, D], C.c_int),
         "ib_ctci_static": ([C.c_int, C.c_int, P, P, P], C.c_int),
@@ -139,13 +138,6 @@ def _ptr(a):
 def launch_count() -> int:
     """Kernels launched by libibgpu.so since it was loaded."""
     return int(load().ib_launch_count())
-
-
-def probe_throughput(which: int) -> float:
-    """0 FP64 FMA, 1 FP64 FMA half lanes, 2 FP64 FMA one warp/SM, 3 FP32 FMA, 4 INT32 IMAD (T/s)."""
-    t = C.c_double()
-    _check(load().ib_probe_throughput(which, C.byref(t)), "ib_probe_throughput")
-    return t.value
 
 
 def ctci_static(m: int, n: int, vort_ptr: int, s_ptr: int, stream_ptr: int = 0) -> None:
@@ -478,6 +470,14 @@ class Simulation:
         _check(self.lib.ib_struct_rhs(self.h, _ptr(out)), "ib_struct_rhs")
         return out
 
+    def struct_dx(self, f) -> float:
+        """compute_dx (operators_struct.F90:402-505): hinge angles and positions from force f;
+        returns the FSI error max |dtheta|."""
+        err = C.c_double()
+        _check(self.lib.ib_struct_dx(self.h, _ptr(np.ascontiguousarray(f, dtype=np.float64)), C.byref(err)),
+               "ib_struct_dx")
+        return err.value
+
     def schur_solve(self, rhs, f0):
         f = np.array(f0, dtype=np.float64, copy=True)
         its = C.c_int()
@@ -485,14 +485,3 @@ class Simulation:
                                        C.byref(its)), "ib_schur_solve")
         return f, its.value
 
-
-if __name__ == "__main__":
-    import sys as _s
-    if len(_s.argv) > 1 and _s.argv[1] == "probe":
-        names = ["fp64_fma", "fp64_fma_half_lanes", "fp64_fma_1warp_per_sm", "fp32_fma", "int32_imad"]
-        for i, nme in enumerate(names):
-            print(f"{nme} {probe_throughput(i):.3f} T(FL)OP/s")
-        lat = ["fp64_fma", "sqrt", "division", "rsqrt", "reciprocal_rn", "cluster_barrier_8cta",
-               "dsmem_load_chain", "shuffle_plus_dadd", "cta_barrier_128thr"]
-        for i, nme in enumerate(lat):
-            print(f"latency_{nme} {probe_throughput(5 + i):.1f} cycles")

@@ -83,7 +83,13 @@ int ib_create(const IbParams* p, const IbBody* bodies, int nbody, IbCtx** out);
 int ib_destroy(IbCtx* ctx);
 int ib_synchronize(IbCtx* ctx);
 
-/* timestepper.F90:18-556 advance(itime): increments *itime and advances one step. */
+/* timestepper.F90:18-556 advance(itime): increments *itime and advances one step.
+ * The reference never checks its solvers (KSP reasons are not read, timestepper.F90:363-366;
+ * the FSI loop of timestepper.F90:318 ends silently after 1000 iterations).  Here the step is
+ * always completed, and then IB_ERR_GMRES is returned if one of its Krylov solves stopped
+ * without converging (iteration cap gmres_max_it or breakdown: a negative KSP reason), or
+ * IB_ERR_FSI if the FSI iterations stopped at fsi_max_it + 1 without reaching fsi_tol;
+ * ib_last_error() gives the reason or the final FSI error. */
 int ib_advance(IbCtx* ctx, int* itime);
 
 /* state access (the arrays of variables.F90:10-33) */
@@ -121,14 +127,15 @@ int ib_ctci(IbCtx* ctx, const double* vort, double* s);
  * memory.  It has no counterpart in the reference; it is for callers that may not allocate
  * when they need the solve: a host that reserves its device memory once at start-up, a time
  * loop that must not pay cudaFree's device-wide synchronisation, or code holding no IbCtx.
- * vort and s are DEVICE arrays ((n-1) x (m-1), x fastest); the kernels run on `stream` (a
- * cudaStream_t, NULL for the default stream) and the call returns without waiting for them.
- * Scratch and tables live in one 16 MiB static device array that each GPU loading the library
- * keeps until the process exits: grids needing more ((m-1)(n-1) plus the tables; 1200 x 600
- * fits, 1280 x 640 does not) fail with IB_ERR_ARG.  The first call on a device, and the first
- * after the grid size changes, does the set-up with synchronous copies: make it before any
- * stream capture.  All calls on a device share the array: calls whose kernels overlap on the
- * GPU race and give wrong results.  Errors are reported through ib_last_error(). */
+ * vort and s are DEVICE arrays of the current device ((n-1) x (m-1), x fastest); the kernels
+ * run on `stream` (a cudaStream_t, NULL for the default stream) and the call returns without
+ * waiting for them.  Scratch and tables live in one 16 MiB static device array that each GPU
+ * loading the library keeps until the process exits: grids needing more ((m-1)(n-1) plus the
+ * tables; 1200 x 600 fits, 1280 x 640 does not) fail with IB_ERR_ARG.  The first call on a
+ * device, and the first after the grid size changes, does the set-up: it copies the tables and
+ * waits for the whole device (cudaDeviceSynchronize), so make it before any stream capture.
+ * All calls on a device share the array: calls whose kernels overlap on the GPU race and give
+ * wrong results.  Errors are reported through ib_last_error(). */
 int ib_ctci_static(int m, int n, const double* vort, double* s, void* stream);
 /* myfft.F90:161-173 ainv (in place) */
 int ib_ainv(IbCtx* ctx, double* vort);
@@ -198,12 +205,6 @@ int ib_get_work(IbCtx* ctx, long long* matvecs, long long* passes4);
 long long ib_launch_count(void);
 /* measured FP64 FMA throughput of this GPU (TFLOP/s), from a register-resident FMA loop */
 int ib_measure_fp64_peak(double* tflops);
-/* which: 0 FP64 FMA, 1 FP64 FMA with half of each warp's lanes active (useful rate),
- * 2 FP64 FMA with one warp per SM, 3 FP32 FMA, 4 INT32 IMAD; *value in T(FL)OP/s.
- * which 5..13: latencies of dependent operations in cycles - FP64 FMA, sqrt, division, rsqrt,
- * correctly rounded reciprocal, cluster barrier (8 CTAs), load from another CTA's shared
- * memory, warp shuffle + FP64 add, CTA barrier */
-int ib_probe_throughput(int which, double* value);
 /* kind 0: x pass, 1: y pass with diagonal, 2: y pass of the predictor, 3: plain y pass;
  * count of timed launches, their summed device time (ms) and summed algorithmic DRAM bytes */
 int ib_profile_read(IbCtx* ctx, int kind, int* count, double* total_ms, double* bytes);

@@ -1,0 +1,150 @@
+"""Step-level parity at the benchmark sizes (timestepper.F90:18-556, 318-454).
+
+Two workloads, as configured for the benchmark and for the rigid cylinder:
+  * plate800x400: hinged plate of 51 points, 800x400 cells x 5 levels, Re=500, dt=1e-3;
+  * cylinder400x200: 157-point rigid cylinder, 400x200 x 3 levels, Re=100, dt=0.004.
+
+Checked at these sizes because several paths exist only there: the first vort2flux's row
+ranges with their margin, the coarse levels' scaled rows, the predictor's skipped centre
+rows, the 16 x 24 register tridiagonal chunking, the 70-tile influence band and the device
+FSI loop's band-flag exits.
+
+The reference's GMRES (PETSc GMRES(30), classical Gram-Schmidt) stops at a round-off-
+dependent iteration, so the Krylov paths are checked two ways:
+  * tight: both solvers run to rtol 1e-14 (the remedy for parity through an iterative solve);
+    the plate's Schur operator at 2-grid-spacing points is well conditioned, and the oracle's
+    own GMRES agrees with a direct solve to ~1e-13 there;
+  * conditional: one FSI iteration a step (fsi_tol above any error) and the oracle handed the
+    GPU's solution for its solve; every other quantity of the step must match.
+The rigid cylinder runs the stationary-body direct solve (num_stat, no stopping point) and,
+with GMRES, the conditional check: its Schur operator (points one grid spacing apart) has
+condition ~6e4, where GMRES(30)+CGS does not reach 1e-10 in thousands of iterations (the
+oracle's solve stalls the same way), so IB_ERR_GMRES is expected there.
+Tolerances: 1e-11 relative after one step, 1e-10 after three, 1e-9 after ten.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+import scipy.fft as sfft
+
+import ib_oracle as O
+from helpers import rel
+from ib_parallel_gb300 import geometry as GEO
+from ib_parallel_gb300 import ibgpu as G
+
+pytestmark = pytest.mark.gpu
+WORKERS = os.cpu_count() or 1
+IB_ERR_GMRES = 4
+
+
+def _pair(p, bodies, **over):
+    kw = {k: getattr(p, k) for k in ("m", "n", "mgridlev", "dt", "Re", "len", "offsetx", "offsety", "fsi_tol",
+                                      "atol", "rtol", "num_stat", "motion", "gmres_restart", "gmres_max_it")}
+    kw.update(over)
+    ob = [O.Body(x=b.x.copy(), y=b.y.copy(), fam=b.fam, gamma0_deg=b.gamma0_deg, itheta=b.itheta,
+                 ktheta=b.ktheta, ctheta=b.ctheta) for b in bodies]
+    o = O.IBOracle(O.Params(**kw), ob)
+    g = G.Simulation(G.Params(**kw, autotune=False), bodies)
+    return o, g
+
+
+def _compare(o, g, tol):
+    worst = {}
+    for k in range(o.L):
+        for name, ref in (("omega", o.omega[k]), ("s", o.s[k]), ("qx", o.qx[k]), ("qy", o.qy[k])):
+            e = rel(g.get_field(name, k), ref)
+            worst[f"{name}{k}"] = e
+    if o.nf:
+        worst["f"] = rel(g.get_vector("f"), o.f)
+        worst["f_rdst"] = rel(g.get_vector("f_rdst"), o.f_rdst)
+        cx, cy = g.forces()
+        ox, oy = o.force_coeffs(o.f)
+        worst["cd_cl"] = rel(np.r_[cx, cy], np.r_[ox, oy])
+        if o.tors:
+            worst["theta"] = rel(g.body_state()[0], o.theta)
+            worst["xb"] = rel(g.get_vector("xb"), o.xb)
+    bad = {k: v for k, v in worst.items() if not v < tol}
+    assert not bad, (tol, bad)
+    return max(worst.values())
+
+
+def _advance_rc(g):
+    it = C.c_int()
+    return g.lib.ib_advance(g.h, C.byref(it))
+
+
+def test_plate800x400_tight_free_running():
+    p, bodies = GEO.config_plate_800x400()
+    o, g = _pair(p, bodies, rtol=1e-14, atol=1e-16, fsi_tol=1e-12)
+    with sfft.set_workers(WORKERS):
+        for step in range(3):
+            o.advance()
+            g.advance()
+            assert g.counters()[1] == o.fsi_iter
+            _compare(o, g, 1e-11 if step == 0 else 1e-10)
+    assert g.influence_stats()["builds"] >= 1 and g.influence_stats()["fallbacks"] == 0
+    g.close()
+
+
+def test_plate800x400_conditional_on_solve():
+    # the benchmark's tolerances; one FSI iteration a step, so the oracle can take each solve
+    p, bodies = GEO.config_plate_800x400()
+    o, g = _pair(p, bodies, fsi_tol=1e3)
+    with sfft.set_workers(WORKERS):
+        for step in range(3):
+            g.advance()
+            fg = g.get_vector("f")
+            its_g, fsi = g.counters()
+            assert fsi == 1
+            o.gmres = lambda b, x0, op, fg=fg, its=its_g: (fg.copy(), its, 2)
+            o.advance()
+            _compare(o, g, 1e-11 if step == 0 else 1e-10)
+    g.close()
+
+
+def test_plate800x400_benchmark_settings():
+    # the benchmark's own settings, free running: its GMRES stops at rtol 1e-10 on each side
+    # after a round-off-dependent number of iterations, so fields agree to the solver's
+    # tolerance (and the FSI iteration counts exactly)
+    p, bodies = GEO.config_plate_800x400()
+    o, g = _pair(p, bodies)
+    with sfft.set_workers(WORKERS):
+        for step in range(2):
+            o.advance()
+            g.advance()
+            assert g.counters()[1] == o.fsi_iter
+            k_g = g.counters()[0]
+            assert 0.7 <= k_g / o.ksp_iter <= 1.3
+    _compare(o, g, 1e-7)
+    g.close()
+
+
+@pytest.mark.parametrize("steps", [1, 10])
+def test_cylinder400x200_direct(steps):
+    p, bodies = GEO.config_cylinder_400x200()
+    o, g = _pair(p, bodies, num_stat=True)
+    with sfft.set_workers(WORKERS):
+        for step in range(steps):
+            o.advance()
+            g.advance()
+    _compare(o, g, 1e-11 if steps == 1 else 1e-9)
+    g.close()
+
+
+def test_cylinder400x200_gmres_conditional():
+    # GMRES as configured (rtol 1e-10); the solve stalls at this conditioning on both sides, so
+    # the step reports IB_ERR_GMRES, and the rest of the step is checked on the GPU's solution
+    p, bodies = GEO.config_cylinder_400x200()
+    o, g = _pair(p, bodies, gmres_max_it=600)
+    with sfft.set_workers(WORKERS):
+        for step in range(3):
+            rc = _advance_rc(g)
+            assert rc in (G.IB_OK, IB_ERR_GMRES), g.lib.ib_last_error()
+            fg = g.get_vector("f")
+            its_g, _ = g.counters()
+            o.gmres = lambda b, x0, op, fg=fg, its=its_g: (fg.copy(), its, 2)
+            o.advance()
+            _compare(o, g, 1e-11 if step == 0 else 1e-10)
+    g.close()

@@ -117,3 +117,27 @@ def test_plate_struct_ops():
     assert rel(g.struct_btimes(x), o.b_times(x)) < 1e-13
     assert rel(g.schur_apply(x), o.a_times(x)) < 1e-12
     g.close()
+
+
+def test_plate_struct_rhs_dx():
+    # compute_dx (operators_struct.F90:402-505, update_xb :600-620) and compute_rhs (:342-398)
+    # on the same state: a random force moves the hinge angle, the positions follow, and the
+    # structural right-hand side at the new angle (theta0 = 0, as at the start of a step) is
+    # compared; a second force then moves it again from there
+    o, g = pair(PLATE, [small_plate()])
+    rng = np.random.default_rng(8)
+    assert np.abs(g.struct_rhs()).max() == 0.0 and np.abs(o.compute_rhs()).max() == 0.0
+    for _ in range(2):
+        f = 1e-2 * _rand(rng, o.nf)
+        err_o = o.compute_dx(f)
+        err_g = g.struct_dx(f)
+        assert abs(err_g - err_o) <= 1e-13 * abs(err_o)
+        th, thd, thdd = g.body_state()
+        assert rel(th, o.theta) < 1e-13
+        assert rel(thd, o.thetad) < 1e-13
+        assert rel(thdd, o.thetadd) < 1e-13
+        assert rel(g.get_vector("xb"), o.xb) < 1e-14
+        assert rel(g.get_vector("yb"), o.yb) < 1e-14
+        assert rel(g.struct_rhs(), o.compute_rhs()) < 1e-13
+    g.close()
+

@@ -12,6 +12,10 @@ checked three ways:
     round-off sensitivity (1e-6) and Krylov iteration counts within a factor 2
     (restarted GMRES with CGS reaches its tolerance after a round-off-dependent
     number of cycles).
+At these small sizes the body points lie about one grid spacing apart and the Schur
+operator's condition number is ~1e3-1e4, so even GMRES run to rtol 1e-14 leaves the force
+1e-11 to 1e-10 away from a direct solve: the tight free-running check is made at the
+benchmark size instead (tests/test_gpu_fullsize.py), where the operator is well conditioned.
 """
 import numpy as np
 import pytest
@@ -83,3 +87,24 @@ def test_plate_fsi_steps():
     xb = g.get_vector("xb")
     assert rel(xb, o.xb) < 1e-9
     g.close()
+
+
+def test_plate_conditional_on_solve():
+    # one FSI iteration a step (fsi_tol above any error), the oracle handed the GPU's solve:
+    # structure right-hand side, regT, redistribution, compute_dx, the new weights and the
+    # correction with the moved stencils must all match
+    o, g = pair(dict(PLATE, fsi_tol=1e3), [small_plate()])
+    for step in range(10):
+        g.advance()
+        fg = g.get_vector("f")
+        its_g, fsi = g.counters()
+        assert fsi == 1
+        o.gmres = lambda b, x0, op, fg=fg, its=its_g: (fg.copy(), its, 2)
+        o.advance()
+        tol = 1e-11 if step == 0 else 1e-10
+        _compare(o, g, tol)
+        th, _, _ = g.body_state()
+        assert rel(th, o.theta) < tol
+        assert rel(g.get_vector("xb"), o.xb) < tol
+    g.close()
+
