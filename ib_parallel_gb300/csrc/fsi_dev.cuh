@@ -75,9 +75,13 @@ __device__ __forceinline__ void tors_rates(const TorsBody& b, double thn, double
   *thdd = -thdd0 - b.a4 * thd0 + b.a44 * (thn - th0);
 }
 // Position of unknown idx (0..2 npts-1) of a torsional body at sin, cos (gamma0 - theta).
+// Each product and the sum are rounded separately, as update_xb writes them
+// (operators_struct.F90:600-620): the positions decide which side of a stencil edge a grid
+// point falls on.
 __device__ __forceinline__ double2 tors_point(const TorsBody& b, int idx, double sg, double cg) {
   const int j = idx < b.npts ? idx : idx - b.npts;
-  return make_double2(b.xbf0 + (double)j * b.deltas * cg, b.ybf0 + (double)j * b.deltas * sg);
+  const double r = __dmul_rn((double)j, b.deltas);
+  return make_double2(__dadd_rn(b.xbf0, __dmul_rn(r, cg)), __dadd_rn(b.ybf0, __dmul_rn(r, sg)));
 }
 
 // Stencil origins and the 49 weights (l outer, p inner) of the 8 unknowns k0..k0+7 on one CTA
@@ -112,13 +116,18 @@ __device__ __forceinline__ void reg_weights_cta(const GridDims& g, int nf, int k
     const bool isx = comp[k] == 1;
     const int off = q - 3;
     double fv;
+    // The grid coordinate is rounded after the product and again after the sum, as the
+    // reference's expression delta*(indexx-1+p)-offsetx is (grid.F90:459-528): the delta
+    // function is discontinuous at 3 cells (its single-precision constants leave about 1e-8
+    // there), so a point on a grid line (e.g. x = 0 with offsetx = 1, delta = 0.02) must see
+    // the same side of that edge, which a fused multiply-add could change by one rounding.
     if (axis == 0) {
-      double x = d * (double)(cx - 1 + off) - ox;
-      if (!isx) x = x + d2;
+      double x = __dsub_rn(__dmul_rn(d, (double)(cx - 1 + off)), ox);
+      if (!isx) x = __dadd_rn(x, d2);
       fv = deltafnc_dev(x, xk, d);
     } else {
-      double y = d * (double)(cy - 1 + off) - oy;
-      if (isx) y = y + d2;
+      double y = __dsub_rn(__dmul_rn(d, (double)(cy - 1 + off)), oy);
+      if (isx) y = __dadd_rn(y, d2);
       fv = deltafnc_dev(y, yk, d);
     }
     fac[pi][q] = fv;

@@ -120,3 +120,21 @@ def test_device_fsi_loop_matches_host_loop():
     assert gd.influence_stats()["assemblies"] == gh.influence_stats()["assemblies"]
     gd.close()
     gh.close()
+
+
+def test_schur_with_points_on_grid_lines():
+    # 400x200 on [-1,7]x[-2,2] (delta = 0.02): the plate's hinge at the origin lies on a grid
+    # line in x and in y, so its outermost stencil points sit exactly 3 cells away, where the
+    # reference's delta function has a ~1e-8 step; the operator must still match the oracle's
+    from ib_parallel_gb300 import geometry as GEO
+    kw = dict(m=400, n=200, mgridlev=1, dt=1e-3, Re=500.0, len=8.0, offsetx=1.0, offsety=2.0, autotune=False)
+    o, g = pair(kw, [GEO.torsional_plate(51, 1.0, -10.0)])
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal(o.nf)
+    assert rel(g.schur_apply(x, with_b=False), o.a_times(x, with_b=False)) < 1e-12
+    assert rel(g.schur_apply(x), o.a_times(x)) < 1e-12
+    S = g.schur_matrix()
+    assert S is not None
+    So = np.stack([o.a_times(e, with_b=False) for e in np.eye(o.nf)], axis=1)
+    assert rel(S, So) < TOL_MAT
+    g.close()
