@@ -301,7 +301,9 @@ __global__ void k_gmres_update(GmresDev G, double* __restrict__ x, int max_it, c
   }
   if (threadIdx.x == 0) {
     G.ist[3] = 0;
-    if (use_cond) cudaGraphSetConditional(h_outer, (G.ist[1] == 0 && G.ist[0] < max_it) ? 1u : 0u);
+    // the iteration cap reached inside a cycle ends the solve as KSP_DIVERGED_ITS
+    if (G.ist[1] == 0 && G.ist[0] >= max_it) G.ist[1] = -3;
+    if (use_cond) cudaGraphSetConditional(h_outer, G.ist[1] == 0 ? 1u : 0u);
   }
 }
 
@@ -821,7 +823,7 @@ __global__ void __cluster_dims__(kSlices, 1, 1) __launch_bounds__(kClusterThread
   for (int i = tid; i < nl; i += blockDim.x) x[r0 + i] = xsl[i];
   if (rank == 0 && tid == 0) {
     G.ist[0] = its;
-    G.ist[1] = reason;
+    G.ist[1] = reason == 0 && its >= max_it ? -3 : reason;   // KSP_DIVERGED_ITS
     G.ist[2] = k;
     G.ist[3] = 0;
     G.ist[4] = cycles;
