@@ -6,27 +6,31 @@ twice the grid spacing apart; 10 degrees incidence plus a seeded 0.01 tip
 perturbation), Re=500, fine grid 800x400 on [-1,7]x[-2,2], 5 levels, dt=1e-3,
 GMRES and FSI tolerances 1e-10.  The plate is the torsional-spring body
 (family 2) the reference implements; inputs are synthetic (no dataset is
-involved).
+involved).  A second workload, ``cylinder400x200`` (157-point rigid cylinder,
+400x200 x 3 levels, Re=100, dt=0.004, the stationary-body direct solve), is
+reported in the same line under ``workloads``.
 
 ``python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]``
 
 GPU arm: W untimed steps from the impulsive start, then K steps timed with CUDA
-events on the simulation's stream (the state, about 100 MB per level set, is
-larger than L2 only in aggregate; every step re-reads all levels).  ``e2e``
-times K more steps through the C ABI with host buffers: each step uploads the
-frame fluxes q0 of all levels from pinned memory (the per-step motion input of
-motion_potential/motion_rotation, variables.F90:299-360) and reads the force
-coefficients and hinge angle back.  With N>1 every rank advances its own
-replica of the simulation (the step does not shard; no collective in the data
-path) and ``value`` is the sum over ranks.
+events on the simulation's stream (state, tables and the influence band, about
+0.5 GB, are larger than L2).  ``e2e`` times K more steps through the C ABI with
+host buffers: each step uploads the frame fluxes q0 of all levels from pinned
+memory (the per-step motion input of motion_potential/motion_rotation,
+variables.F90:299-360) and reads the force coefficients and hinge angle back.
+``long_run`` times a fresh simulation over many steps from the impulsive start
+with every influence-band build inside the timed region.  With N>1 every rank
+advances its own replica of the simulation (the step does not shard; no
+collective in the data path) and ``value`` is the sum over ranks.
 
-Reference arm: the reference (Fortran + PETSc + FFTW + MPI) cannot be built in
-this image or on the GPU machine, so the CPU restatement in ``oracle/`` (numpy +
-scipy.fft, all host cores) is timed on the same workload.  One oracle step takes
-tens of seconds, so each "step" is a bounded sample: the non-Krylov part of a
-step (predictor on all levels, two vort2flux, correction) measured once per
-step plus a few Schur matvecs, scaled to the Krylov matvecs per step this
-workload needs.
+CPU arms (``--impl reference`` and ``cpu_baseline``): the reference (Fortran +
+PETSc + FFTW + MPI) cannot be built in this image or on the GPU machine, so the CPU
+restatement in ``oracle/`` (numpy + scipy.fft on all host threads) advances the
+same workload through whole time steps from the same impulsive start, with its
+own GMRES and FSI loop.  It is a numpy port, a weaker baseline than the
+compiled reference would be; it runs the reference's matrix-free Schur
+operator, so ``matrix_free`` (the GPU on that same algorithm) is printed beside
+it as the algorithm-matched comparison.
 """
 from __future__ import annotations
 
@@ -47,11 +51,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "FSI steps/s @800x400x5 FP64"
 WORKLOAD = "plate800x400"
-# Schur matvecs per step of this workload (Krylov iterations + one initial-residual
-# product per GMRES cycle, summed over the FSI iterations), counted by the GPU
-# arm's ib_get_work (49.8 to 53 over the first steps after warm-up on GB300); the CPU
-# arm runs the same algorithm with the matrix-free operator.
-MATVECS_PER_STEP = 52.0
+C1_WORKLOAD = "cylinder400x200"
 
 
 def _env_int(k, d):
@@ -185,45 +185,36 @@ def _barrier(world: int):
         dist.barrier()
 
 
-def _oracle_sample(p, bodies, n_mv: int, workers: int):
-    """Time the oracle's non-Krylov part of one step and n_mv Schur matvecs."""
+def _oracle(p, bodies):
     sys.path.insert(0, str(ROOT / "oracle"))
-    import scipy.fft as sfft
     import ib_oracle as O
     po = O.Params(**{k: getattr(p, k) for k in O.Params.__dataclass_fields__ if hasattr(p, k)})
-    ob = [O.Body(x=b.x, y=b.y, fam=b.fam, gamma0_deg=b.gamma0_deg, itheta=b.itheta, ktheta=b.ktheta,
-                 ctheta=b.ctheta) for b in bodies]
-    o = O.IBOracle(po, ob)
-    rng = np.random.default_rng(0)
-    for k in range(o.L):  # a developed-looking state so nothing is trivially zero
-        o.omega[k] = 1e-3 * rng.standard_normal(o.omega[k].shape)
+    ob = [O.Body(x=b.x.copy(), y=b.y.copy(), fam=b.fam, gamma0_deg=b.gamma0_deg, itheta=b.itheta,
+                 ktheta=b.ktheta, ctheta=b.ctheta) for b in bodies]
+    return O.IBOracle(po, ob)
+
+
+def _oracle_steps(p, bodies, workers, untimed=0, timed=None, budget_s=None, min_steps=2):
+    """Whole time steps of the oracle (IBOracle.advance: predictor, vort2flux, its own GMRES
+    and FSI loop, correction) from the impulsive start: `untimed` steps first, then either
+    `timed` steps or as many as fit in budget_s (at least min_steps).  Returns the wall time
+    of each timed step and the oracle."""
+    import scipy.fft as sfft
+    o = _oracle(p, bodies)
+    times = []
     with sfft.set_workers(workers):
-        t0 = time.perf_counter()
-        L = o.L
-        lastbc = [o.get_bc(o.omega[k + 1], 0.25) for k in range(L - 1)] + [np.zeros(o.nbc)]
-        for k in range(L - 1, -1, -1):
-            obc = o.get_bc(o.omega[k + 1], 0.25) if k < L - 1 else np.zeros(o.nbc)
-            nlx, nly = o.nonlinear(o.omega[k], o.qx[k] + o.q0x[k], o.qy[k] + o.q0y[k], lastbc[k])
-            rb = np.zeros_like(o.omega[k])
-            o.apply_bc(rb, lastbc[k], o.vfac[k]); o.apply_bc(rb, obc, o.vfac[k])
-            rhs = o.rot(nlx, nly)
-            o.omega[k] = o.fluid_predictor(o.omega[k], rhs, o.rhs_old[k], rb, k)
-            o.rhs_old[k] = rhs
-        o.s, o.qx, o.qy = o.vort2flux(o.omega)
-        rhsf = o.regT(o.qx[0] + o.q0x[0], o.qy[0] + o.q0y[0], o.compute_rhs())
-        o.f_rdst = o.redistribute(rhsf)
-        hx, hy = o.reg(rhsf)
-        o.omega[0] = o.omega[0] - o.ainv(o.rot(hx, hy))
-        o.s, o.qx, o.qy = o.vort2flux(o.omega)
-        t_fixed = time.perf_counter() - t0
-        x = rng.standard_normal(o.nf)
-        o.a_times(x)
-        t0 = time.perf_counter()
-        for _ in range(n_mv):
-            x = o.a_times(x)
-            x = x / np.linalg.norm(x)
-        t_mv = (time.perf_counter() - t0) / n_mv
-    return t_fixed, t_mv
+        for _ in range(untimed):
+            o.advance()
+        t_all = time.perf_counter()
+        while True:
+            t0 = time.perf_counter()
+            o.advance()
+            times.append(time.perf_counter() - t0)
+            if timed is not None and len(times) >= timed:
+                break
+            if budget_s is not None and len(times) >= min_steps and time.perf_counter() - t_all >= budget_s:
+                break
+    return times, o
 
 
 def run_reference(args, world, rank):
@@ -232,28 +223,144 @@ def run_reference(args, world, rank):
     from ib_parallel_gb300 import geometry as GEO
     p, bodies = GEO.config_plate_800x400()
     cores = os.cpu_count() or 1
-    mv = MATVECS_PER_STEP
-    if mv is None:
-        print(json.dumps({"impl": "reference", "unavailable": "matvecs per step not yet measured on GB300"}))
-        return 0
-    per_step = []
-    for i in range(args.warmup + args.steps):
-        t_fixed, t_mv = _oracle_sample(p, bodies, n_mv=2, workers=cores)
-        if i >= args.warmup:
-            per_step.append(t_fixed + mv * t_mv)
-    T = float(np.mean(per_step))
-    value = 1.0 / T
-    sample = (f"oracle port (numpy+scipy.fft, {cores} threads): per step the non-Krylov part of a step once "
-              f"plus 2 Schur matvecs, scaled to {mv} matvecs/step")
+    times, o = _oracle_steps(p, bodies, cores, untimed=args.warmup, timed=args.steps)
+    T = float(np.sum(times))
+    value = len(times) / T
+    sample = (f"oracle port (numpy + scipy.fft, {cores} threads; the Fortran reference cannot be built here): "
+              f"{len(times)} whole time steps ({args.warmup + 1}..{args.warmup + len(times)} from the impulsive "
+              f"start, each with its own GMRES and FSI loop; last step {o.ksp_iter} Krylov iterations, "
+              f"{o.fsi_iter} FSI iterations), {T:.1f} s")
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * T, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": "800x400", "levels": 5, "body_points": 51},
+            "warmup": args.warmup, "ms_per_step": 1e3 * T / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded hinged plate)",
+            "config": {"workload": WORKLOAD, "grid": "800x400", "levels": 5, "body_points": 51, "Re": 500,
+                       "dt": 1e-3, "gmres_rtol": 1e-10, "fsi_tol": 1e-10, "parallelism": "replicas1"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def _algorithmic_bytes(m, n, L, nf):
+    """Compulsory DRAM bytes of the reference's step (each array argument of the routines it
+    calls read once, each output written once; FP64): the predictor on every level, two
+    vort2flux, the correction, and per Krylov iteration one matrix-free Schur product."""
+    ns, nu, nv = (m - 1) * (n - 1), (m + 1) * n, m * (n + 1)
+    pred = 8.0 * (4 * ns + nu + nv)
+    v2f = 8.0 * ((2 * ns + nu + nv) + (L - 1) * (3.25 * ns + nu + nv))
+    corr = 8.0 * (3 * ns + nu + nv) + v2f
+    fixed = L * pred + v2f + corr
+    matvec = 8.0 * 3 * ns + v2f + 49.0 * nf * 56.0
+    return fixed, matvec
+
+
+def _timed_steps(sim, stream, steps):
+    """K steps of sim timed with CUDA events on its stream; returns (seconds, ksp, fsi sums)."""
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ksp_sum = fsi_sum = 0
+    e0.record(stream)
+    for _ in range(steps):
+        sim.advance()
+        k, f = sim.counters()
+        ksp_sum += k
+        fsi_sum += f
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3, ksp_sum, fsi_sum
+
+
+def _e2e_steps(sim, stream, steps):
+    """K steps through the C ABI with host buffers: each step uploads the frame fluxes q0 of
+    all levels from pinned memory and reads the force coefficients (and hinge angles) back."""
+    import torch
+    from ib_parallel_gb300 import ibgpu as G
+    L = sim.params.mgridlev
+    q0x = [torch.from_numpy(sim.get_field("q0x", k)).pin_memory() for k in range(L)]
+    q0y = [torch.from_numpy(sim.get_field("q0y", k)).pin_memory() for k in range(L)]
+    cx = torch.zeros(max(1, sim.nbody), dtype=torch.float64).pin_memory()
+    cy = torch.zeros_like(cx)
+    th = torch.zeros(max(1, sim.ntors), dtype=torch.float64).pin_memory()
+    h2d = sum(t.numel() * 8 for t in q0x + q0y)
+    d2h = (2 * sim.nbody + sim.ntors) * 8
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(steps):
+        for k in range(L):
+            sim.set_field("q0x", k, q0x[k])
+            sim.set_field("q0y", k, q0y[k])
+        sim.advance()
+        G._check(sim.lib.ib_get_forces(sim.h, G.C.c_void_p(cx.data_ptr()), G.C.c_void_p(cy.data_ptr())))
+        if sim.ntors:
+            G._check(sim.lib.ib_get_body_state(sim.h, G.C.c_void_p(th.data_ptr()), None, None))
+    f1.record(stream)
+    f1.synchronize()
+    return f0.elapsed_time(f1) / 1e3, h2d, d2h
+
+
+def _long_run(p, bodies, steps):
+    """A fresh simulation timed from its first step over `steps` steps, with every influence-
+    band build and rebuild inside the timed region (wall clock around synchronised steps)."""
+    import torch
+    from ib_parallel_gb300 import ibgpu as G
+    sim = G.Simulation(p, bodies)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.advance()
+    sim.synchronize()
+    T = time.perf_counter() - t0
+    st = sim.influence_stats()
+    th = sim.body_state()[0]
+    sim.close()
+    return {"value": steps / T, "unit": "steps/s", "steps": steps, "seconds": T,
+            "band_builds": st["builds"], "band_build_ms": st["build_ms"], "fallbacks": st["fallbacks"],
+            "final_theta": [float(x) for x in th],
+            "note": "from the impulsive start, host wall clock, every band build inside the region"}
+
+
+def _c1_workload(args):
+    """The rigid cylinder (400x200 x 3 levels, 157 points, Re=100, dt=0.004) through the
+    stationary-body direct solve: device-timed and end-to-end steps/s, and the oracle timed on
+    whole steps after its own preprocessing."""
+    import torch
+    from ib_parallel_gb300 import geometry as GEO
+    from ib_parallel_gb300 import ibgpu as G
+    p, bodies = GEO.config_cylinder_400x200()
+    p.num_stat = True
+    sim = G.Simulation(p, bodies)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    for _ in range(max(3, args.warmup)):
+        sim.advance()
+    sim.synchronize()
+    steps = max(args.steps, 20)
+    t, _, _ = _timed_steps(sim, stream, steps)
+    te, h2d, d2h = _e2e_steps(sim, stream, steps)
+    cx, cy = sim.forces()
+    sim.close()
+    out = {"workload": C1_WORKLOAD, "metric": "steps/s @400x200x3 FP64 (direct solve)", "value": steps / t,
+           "unit": "steps/s", "steps": steps, "ms_per_step": 1e3 * t / steps,
+           "e2e": {"value": steps / te, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "config": {"grid": "400x200", "levels": 3, "body_points": 157, "Re": 100, "dt": 0.004,
+                      "solve": "num_stat (Cholesky of the assembled Schur matrix at step 1)"},
+           "cd_cl_last": [float(cx[0]), float(cy[0])],
+           "gmres_note": "with GMRES(30) at rtol 1e-10 the Schur solve of this body (points one grid spacing "
+                         "apart, condition ~6e4) does not converge in thousands of iterations, in the oracle "
+                         "as on the GPU (ib_advance returns IB_ERR_GMRES); the direct solve is the usable path"}
+    if not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        times, o = _oracle_steps(p, bodies, cores, untimed=1, budget_s=8.0, min_steps=5)
+        cpu = len(times) / float(np.sum(times))
+        out["cpu_baseline"] = {"value": cpu, "unit": "steps/s", "cores": cores, "kind": "port",
+                               "sample": f"oracle port, {len(times)} whole steps (2..{len(times) + 1}) after its "
+                                         f"step-1 preprocessing, {cores} threads"}
+        out["gpu_over_cpu"] = out["value"] / cpu
+        out["e2e_over_cpu"] = out["e2e"]["value"] / cpu
+    return out
 
 
 def run_gpu(args, world, rank, local):
@@ -271,39 +378,27 @@ def run_gpu(args, world, rank, local):
         p.autotune = 0
     sim = G.Simulation(p, bodies)
     stream = torch.cuda.ExternalStream(sim.stream())
-    L = p.mgridlev
     for _ in range(args.warmup):
         sim.advance()
     sim.synchronize()
     mv0, passes0 = sim.work()
     launches0 = G.launch_count()
-    ksp_sum, fsi_sum = 0, 0
     _barrier(world)
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     if args.host_fsi_loop:
         sim.step_profile(1)
     with Clocks(local) as clk:
         if args.profile_window:
             torch.cuda.profiler.start()
         clk.begin()
-        e0.record(stream)
-        for _ in range(args.steps):
-            sim.advance()
-            k, f = sim.counters()
-            ksp_sum += k
-            fsi_sum += f
-        e1.record(stream)
-        e1.synchronize()
+        t_local, ksp_sum, fsi_sum = _timed_steps(sim, stream, args.steps)
         clk.end()
         if args.profile_window:
             torch.cuda.profiler.stop()
     if args.host_fsi_loop:
         sim.step_profile(0)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    t_s = _barrier_max(ms / 1e3, world)
+    t_s = _barrier_max(t_local, world)
     mv1, passes1 = sim.work()
     launches_timed = G.launch_count() - launches0
     mv_per_step = (mv1 - mv0) / args.steps
@@ -311,34 +406,15 @@ def run_gpu(args, world, rank, local):
     value = world * args.steps / t_s
 
     # ---- end to end through the C ABI with host buffers
-    q0x = [torch.from_numpy(sim.get_field("q0x", k)).pin_memory() for k in range(L)]
-    q0y = [torch.from_numpy(sim.get_field("q0y", k)).pin_memory() for k in range(L)]
-    cx = torch.zeros(max(1, sim.nbody), dtype=torch.float64).pin_memory()
-    cy = torch.zeros_like(cx)
-    th = torch.zeros(max(1, sim.ntors), dtype=torch.float64).pin_memory()
-    h2d = sum(t.numel() * 8 for t in q0x + q0y)
-    d2h = (2 * sim.nbody + sim.ntors) * 8
     _barrier(world)
-    torch.cuda.synchronize()
-    f0 = torch.cuda.Event(enable_timing=True)
-    f1 = torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    for _ in range(args.steps):
-        for k in range(L):
-            sim.set_field("q0x", k, q0x[k])
-            sim.set_field("q0y", k, q0y[k])
-        sim.advance()
-        G._check(sim.lib.ib_get_forces(sim.h, G.C.c_void_p(cx.data_ptr()), G.C.c_void_p(cy.data_ptr())))
-        G._check(sim.lib.ib_get_body_state(sim.h, G.C.c_void_p(th.data_ptr()), None, None))
-    f1.record(stream)
-    f1.synchronize()
-    e2e_s = _barrier_max(f0.elapsed_time(f1) / 1e3, world)
+    e2e_local, h2d, d2h = _e2e_steps(sim, stream, args.steps)
+    e2e_s = _barrier_max(e2e_local, world)
     e2e_value = world * args.steps / e2e_s
 
-    # ---- roofline of the dominant kernel (the DST-I x pass: largest share of the ncu launch
-    # list, profiles/launch_list_plate800x400.md), timed alone: 20 back-to-back full passes
-    # over the finest grid with CUDA events on the simulation's stream
-    m, n = p.m, p.n
+    # ---- roofline of the dominant kernel (the DST-I x pass, the largest share of the step's
+    # launch list), timed alone: 20 back-to-back full passes over the finest grid with CUDA
+    # events on the simulation's stream
+    m, n, L = p.m, p.n, p.mgridlev
     ns = (m - 1) * (n - 1)
     t_x = sim.time_pass(0, 20)
     t_tri = sim.time_pass(1, 20)
@@ -357,7 +433,12 @@ def run_gpu(args, world, rank, local):
                     traffic = float(line.split("=")[1])
                 except ValueError:
                     traffic = None
-    k_final, f_final = sim.counters()
+    # the step against HBM on the reference's accounting: the compulsory bytes of the
+    # routines it calls, with one matrix-free Schur product per Krylov iteration
+    fixed_b, matvec_b = _algorithmic_bytes(m, n, L, sim.nf)
+    ksp_per_step = ksp_sum / args.steps
+    step_bytes = fixed_b + ksp_per_step * matvec_b
+    step_achieved = step_bytes / (t_s / args.steps) / 1e9
     result = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_s / args.steps, "higher_is_better": True,
@@ -365,11 +446,12 @@ def run_gpu(args, world, rank, local):
         "data": "synthetic (seeded hinged plate, impulsive start)",
         "config": {"workload": WORKLOAD, "grid": "800x400", "levels": 5, "body_points": 51, "Re": 500,
                    "dt": 1e-3, "gmres_rtol": 1e-10, "fsi_tol": 1e-10, "parallelism": f"replicas{world}",
-                   "l2": "working set (~330 MB of state, tables and scratch) larger than L2 (129 MB)"},
+                   "l2": "working set (~330 MB of state, tables and scratch + 160 MB influence band) larger "
+                         "than L2 (129 MB)"},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": None,
-        "work_per_step": {"schur_matvecs": mv_per_step, "ksp_iter": ksp_sum / args.steps,
+        "gpu_launches": launches_timed,
+        "work_per_step": {"schur_matvecs": mv_per_step, "ksp_iter": ksp_per_step,
                           "fsi_iter": fsi_sum / args.steps,
                           "dst_passes": [x / args.steps for x in passes_timed]},
         "roofline": {"bound": "hbm", "kernel": "k_dst_x (DST-I along x, 399 rows of 799)", "achieved": achieved,
@@ -380,6 +462,14 @@ def run_gpu(args, world, rank, local):
         "fp64_roofline": {"kernel": "k_dst_x", "achieved": fp_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                           "frac": fp_achieved / fp64_peak, "flops_per_launch": flops_x,
                           "peak_source": "of measured FP64 FMA loop on this GPU (ib_measure_fp64_peak)"},
+        "step_roofline": {"bound": "hbm", "achieved": step_achieved, "peak": peak, "unit": "GB/s",
+                          "frac": step_achieved / peak, "bytes_per_step": step_bytes,
+                          "fixed_bytes": fixed_b, "bytes_per_krylov_iteration": matvec_b,
+                          "krylov_iterations_per_step": ksp_per_step,
+                          "note": "compulsory bytes of the reference's step (predictor on every level, two "
+                                  "vort2flux, correction, one matrix-free Schur product per Krylov iteration) "
+                                  "over the measured step time; the influence matrix replaces the per-iteration "
+                                  "work, so this is a step-level figure, not a kernel roofline"},
         "tridiagonal_pass_us": 1e3 * t_tri,
         "schur_stages_us": sim.profile_schur(20),
         "influence": sim.influence_stats(),
@@ -387,21 +477,28 @@ def run_gpu(args, world, rank, local):
         "step_phases_us": _step_phases(sim, 5),
         "step_phases_device_loop_us": _step_phases(sim, 5, device_loop=True),
     }
+    sim.close()
     if not args.no_matrix_free:
         result["matrix_free"] = _matrix_free_rate(p, bodies, args)
-    result["gpu_launches"] = launches_timed
+    if args.long_steps > 0:
+        result["long_run"] = _long_run(p, bodies, args.long_steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        t_fixed, t_mv = _oracle_sample(p, bodies, n_mv=4, workers=cores)
-        cpu_val = 1.0 / (t_fixed + mv_per_step * t_mv)
+        times, o = _oracle_steps(p, bodies, cores, budget_s=12.0, min_steps=3)
+        cpu_val = len(times) / float(np.sum(times))
         result["cpu_baseline"] = {
             "value": cpu_val, "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": f"oracle port (numpy+scipy.fft, {cores} threads): non-Krylov part of one step "
-                      f"({t_fixed:.2f} s) + 4 Schur matvecs ({t_mv * 1e3:.1f} ms each), scaled to the "
-                      f"{mv_per_step:.1f} matvecs/step measured above"}
+            "sample": f"oracle port (numpy + scipy.fft, {cores} threads; the Fortran reference cannot be built "
+                      f"here): {len(times)} whole time steps from the impulsive start (1..{len(times)}), each "
+                      f"with its own GMRES and FSI loop, {np.sum(times):.1f} s"}
+        result["speedup_vs_cpu_port"] = {
+            "e2e": e2e_value / cpu_val, "device": value / cpu_val,
+            "same_algorithm": (result["matrix_free"]["value"] / cpu_val) if "matrix_free" in result else None,
+            "note": "same_algorithm: the GPU with the matrix-free Schur operator the port runs"}
+    if rank == 0 and world == 1 and not args.no_c1:
+        result["workloads"] = {C1_WORKLOAD: _c1_workload(args)}
     if rank == 0:
         print(json.dumps(result))
-    sim.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -447,6 +544,28 @@ def _matrix_free_rate(p, bodies, args):
             "schur_matvecs_per_step": (mv1 - mv0) / args.steps}
 
 
+def run_roofline_only():
+    """The x pass of the roofline alone, 20 launches over cold inputs inside a profiler window
+    (ncu --profile-from-start off captures exactly these launches)."""
+    import torch
+    from ib_parallel_gb300 import geometry as GEO
+    from ib_parallel_gb300 import ibgpu as G
+    torch.cuda.set_device(0)
+    p, bodies = GEO.config_plate_800x400()
+    p.autotune = 0
+    sim = G.Simulation(p, bodies)
+    sim.time_pass(0, 2)
+    sim.synchronize()
+    torch.cuda.profiler.start()
+    t_x = sim.time_pass(0, 20)
+    torch.cuda.profiler.stop()
+    ns = (p.m - 1) * (p.n - 1)
+    print(json.dumps({"kernel": "k_dst_x", "avg_launch_us": 1e3 * t_x, "bytes_per_launch": 16.0 * ns,
+                      "achieved_gbs": 16.0 * ns / (t_x * 1e-3) / 1e9}))
+    sim.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -456,6 +575,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-matrix-free", action="store_true",
                     help="skip timing the matrix-free Schur operator beside the default one")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 400x200x3 rigid-cylinder workload")
+    ap.add_argument("--long-steps", type=int, default=1000,
+                    help="steps of the long run from the impulsive start with every band build timed (0: skip)")
     ap.add_argument("--profile-window", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -465,8 +587,13 @@ def main():
                     help="run the timed steps with per-phase timing on, so that the FSI iterations run from the "
                          "host and each of their kernels is a separate launch (a profiler lists kernels inside "
                          "the device loop's graph node only as the graph)")
+    ap.add_argument("--roofline-only", action="store_true",
+                    help="only time the single x pass of the roofline (inside a profiler window: the command "
+                         "the ncu traffic capture of that pass runs)")
     args = ap.parse_args()
     world, rank, local = _dist()
+    if args.roofline_only:
+        return run_roofline_only()
     if args.impl == "reference":
         return run_reference(args, world, rank)
     return run_gpu(args, world, rank, local)

@@ -767,26 +767,41 @@ int op_redistribute(Ctx* c, const double* f, double* frdst) { return redistribut
 // Device time of `reps` back-to-back launches of one full pass over the finest grid
 // (kind 0: x pass, 1: tridiagonal solve), for the roofline of a kernel timed alone.
 int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms) {
+  // Each launch reads and writes its own pair of fields, and the pairs together are more than
+  // twice L2, so every pass starts with its input in HBM, as in a step.
   cudaStream_t st = c->st;
-  auto run = [&]() -> int {
+  int dev = 0, l2 = 0;
+  IB_CUDA_CHECK(cudaGetDevice(&dev));
+  IB_CUDA_CHECK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+  const size_t field = 8 * (size_t)c->g.ns;
+  const int nbuf = std::max(2, (int)((2 * (size_t)l2 + field - 1) / field));
+  double* buf = nullptr;
+  IB_CUDA_CHECK(cudaMalloc(&buf, 2 * field * nbuf));
+  // nonzero inputs (every byte 0x3f: about 4.8e-4 in each double)
+  int rc = cudaMemsetAsync(buf, 0x3f, 2 * field * nbuf, st) == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+  auto run = [&](int i) -> int {
+    double* in = buf + (size_t)(2 * (i % nbuf)) * c->g.ns;
+    double* out = in + c->g.ns;
     if (kind == 0) {
-      DstXArgs a; a.in = c->spec2; a.out = c->spec1;
+      DstXArgs a; a.in = in; a.out = out;
       return dst_pass_x(c->px, c->g.nsy, c->g.nsx, PRE_COPY, a, c->g, c->lx, st);
     }
-    return tri_solve(c->tri_ctci, c->spec1, c->spec1, c->g.nsx, c->tl, st);
+    return tri_solve(c->tri_ctci, in, out, c->g.nsx, c->tl, st);
   };
-  RC(run());
-  cudaEvent_t e0, e1;
-  IB_CUDA_CHECK(cudaEventCreate(&e0));
-  IB_CUDA_CHECK(cudaEventCreate(&e1));
-  IB_CUDA_CHECK(cudaEventRecord(e0, st));
-  for (int r = 0; r < reps; ++r) RC(run());
-  IB_CUDA_CHECK(cudaEventRecord(e1, st));
-  IB_CUDA_CHECK(cudaEventSynchronize(e1));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (rc == IB_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = IB_ERR_CUDA;
+  for (int i = 0; i < nbuf && rc == IB_OK; ++i) rc = run(i);   // warm-up over every pair
+  if (rc == IB_OK && cudaEventRecord(e0, st) != cudaSuccess) rc = IB_ERR_CUDA;
+  for (int r = 0; r < reps && rc == IB_OK; ++r) rc = run(r);
+  if (rc == IB_OK && cudaEventRecord(e1, st) != cudaSuccess) rc = IB_ERR_CUDA;
+  if (rc == IB_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = IB_ERR_CUDA;
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (rc == IB_OK) cudaEventElapsedTime(&ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  cudaFree(buf);
+  RC(rc);
   *avg_ms = ms / reps;
   return IB_OK;
 }

@@ -170,7 +170,9 @@ int ib_schur_solve(IbCtx* ctx, const double* rhs, double* f, int* iterations);
 /* the cudaStream_t every kernel of this context runs on */
 int ib_get_stream(IbCtx* ctx, void** stream);
 /* average device time (ms) of `reps` back-to-back launches of one full pass over the finest
- * grid: kind 0 the DST-I x pass, 1 the per-mode tridiagonal solve (scratch buffers only) */
+ * grid: kind 0 the DST-I x pass, 1 the per-mode tridiagonal solve.  The launches cycle over
+ * pairs of temporary fields (allocated for the call) that together exceed twice the L2 size,
+ * so each reads its input from HBM; the context's state is not touched. */
 int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);
 /* device time (ms, summed over reps back-to-back applications) of the 8 stages of the Schur
  * operator: reg+rot, ainv, coarsify, coarse levels, finest forward, finest solve, finest
