@@ -39,8 +39,35 @@ struct DevPool {
 // vertex u, i.e. the map the matrix-free operator applies between rot and E curl.  Each
 // unknown k owns the 8 x 8 vertex patch P_k = rot(E^T e_k) (values and band indices); the
 // fluid Schur matrix is S_f = P^T K P (curl is the transpose of rot).
+// The buffers and the stream one application of the Schur operator's fluid part works in
+// (schur_fluid): the context's own, or one of the band build's concurrent sets.
+struct SchurScratch {
+  double* vort = nullptr;     // input vorticity (a unit vector during the band build)
+  double* specY = nullptr;    // ainv's modes
+  double* spec1 = nullptr;    // a level's modes
+  double* sbc = nullptr;      // ring
+  double* s0 = nullptr;       // output streamfunction rows
+  double* w[kMaxLevels] = {}; // ainv's vorticity and its coarsified levels (zero outside the centres)
+  int* rr_in = nullptr;       // row range of the input (3 ints)
+  int* prev = nullptr;        // the unit vector's last position (band build)
+  // band build: per level l, rr_lv[3l..3l+2] = the rows [lo, hi) of ainv's vorticity (l = 0)
+  // and of its coarsified levels that hold data, and the treatment of the other rows
+  int* rr_lv = nullptr;
+  cudaStream_t st = nullptr;
+};
+
 struct Influence {
   static constexpr int kTile = 8;
+  // the band's columns are computed on this many streams at once, each with its own scratch
+#ifndef IB_BAND_STREAMS
+#define IB_BAND_STREAMS 12
+#endif
+  static constexpr int kBuildStreams = IB_BAND_STREAMS;
+  std::vector<SchurScratch> bscr;
+  double* bmem = nullptr;
+  int* bint = nullptr;
+  static constexpr int kSetInts = 8 + 3 * kMaxLevels;   // prev, rr_in[3], column, rr_lv
+  int trunc_rows = 0;   // rows of ainv's response kept on each side of a unit vector's row
   bool built = false;
   bool active = false;        // S holds the operator at the current positions
   bool patch_fresh = false;   // patches and flag match the current reg weights
@@ -254,10 +281,15 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
                  const double* hat0_add = nullptr);
 int op_schur(Ctx* c, const double* x, double* y, bool with_b);
 int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out, double* s_out,
-                const double** ring0_out);
+                const double** ring0_out, const SchurScratch* sc = nullptr);
 // influence.cu
 int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
+// graph helpers (solver.cu): a while node after the capture position of st (its body graph
+// returned), the graph st is capturing, and programmatic kernel-to-kernel edges
+int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body);
+cudaGraph_t capture_graph(cudaStream_t st);
+void make_edges_programmatic(cudaGraph_t g);
 // patches + flag for the current weights (async); cleared: the band flag and the touched-vertex
 // flags are already zero (the device FSI loop clears them as it reads them)
 int inf_patch(Ctx* c, bool cleared = false);

@@ -463,6 +463,7 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
     else if (a.rowrange) {
       const int lo = max(0, a.rowrange[0] - a.row_margin), hi = min(nrows, a.rowrange[1] + a.row_margin);
       mode = (row >= lo && row < hi) ? ROW_FFT : a.rowrange[2];
+      if (a.fft_edge_rows && (row == 0 || row == nrows - 1)) mode = ROW_FFT;
       if (a.rows_used && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         a.rows_used[0] = lo;
         a.rows_used[1] = hi;

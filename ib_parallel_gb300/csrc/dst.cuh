@@ -71,6 +71,7 @@ struct DstXArgs {
   // optional device range [rr[0], rr[1]) of transformed rows; others get mode rr[2]
   const int* rowrange = nullptr;
   int row_margin = 0;            // rowrange widened by this many rows on each side (clamped)
+  int fft_edge_rows = 0;         // with rowrange: rows 0 and nrows-1 are transformed as well
   int* rows_used = nullptr;      // receives the (widened) range of transformed rows
   // optional strided row subset: line i is row row0 + i*row_step, i < nlines (0: all rows)
   int nlines = 0, row0 = 0, row_step = 0;

@@ -195,6 +195,83 @@ __global__ void k_inf_unit(int c, const int2* __restrict__ tiles, GridDims g, do
   rr_in[2] = ROW_ZERO;
 }
 
+// The band build's column loops: set i starts at column i and steps by the number of sets.
+__global__ void k_inf_col_init(int* col, int c0) {
+  IB_GRID_DEP_WAIT();
+  if (threadIdx.x == 0) *col = c0;
+}
+// Unit vector of the column *col (k_inf_unit with the column read on the device).
+// Also the rows of each level that hold data: ainv's response on rows b -+ R (the rest below
+// 1e-18 of it, written as zeros), and on each coarser level the rows coarsify fills from the
+// finer level's data rows (coarse row n/4 + (r-1)/2 from the odd fine rows r in [1, n-3]
+// whose 3-row stencil meets them); the other rows of a coarse level are zero apart from the
+// ring's first and last samples (closed form), except its two edge rows, which are transformed.
+__global__ void k_inf_unit_at(const int* col, const int2* __restrict__ tiles, GridDims g, double* vort, int* prev,
+                              int* rr_in, int* rr_lv, int L, int R) {
+  IB_GRID_DEP_WAIT();
+  if (threadIdx.x != 0) return;
+  const int c = *col;
+  const int p = *prev;
+  if (p >= 0) vort[p] = 0.0;
+  const int2 tc = tiles[c / kP];
+  const int q = c % kP;
+  const int a = tc.x * kT + (q % kT), b = tc.y * kT + q / kT;
+  int lo = 0, hi = 0;
+  if (a < g.nsx && b < g.nsy) {
+    const int o = b * g.nsx + a;
+    vort[o] = 1.0;
+    *prev = o;
+    rr_in[0] = b;
+    rr_in[1] = b + 1;
+    lo = max(0, b - R);
+    hi = min(g.nsy, b + R + 1);
+  } else {
+    *prev = -1;
+    rr_in[0] = 0;
+    rr_in[1] = 1;
+  }
+  rr_in[2] = ROW_ZERO;
+  rr_lv[0] = lo; rr_lv[1] = hi; rr_lv[2] = ROW_ZERO;
+  for (int l = 1; l < L; ++l) {
+    int r0 = max(1, lo - 1), r1 = min(g.n - 3, hi);
+    if ((r0 & 1) == 0) r0 += 1;
+    if ((r1 & 1) == 0) r1 -= 1;
+    if (lo >= hi || r0 > r1) { lo = 0; hi = 0; }
+    else { lo = g.n / 4 + (r0 - 1) / 2; hi = g.n / 4 + (r1 - 1) / 2 + 1; }
+    rr_lv[3 * l] = lo; rr_lv[3 * l + 1] = hi;
+    rr_lv[3 * l + 2] = l == L - 1 ? ROW_ZERO : ROW_EDGES;
+  }
+}
+// K[*col][v] (k_inf_gather with the column read on the device).
+__global__ void k_inf_gather_at(const int* col, int nR, const int2* __restrict__ tiles, GridDims g,
+                                const double* __restrict__ s, double* __restrict__ K) {
+  IB_GRID_DEP_WAIT();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nR) return;
+  const int c = *col;
+  const int2 tc = tiles[i / kP];
+  const int q = i % kP;
+  const int a = tc.x * kT + (q % kT), b = tc.y * kT + q / kT;
+  K[(size_t)c * nR + i] = (a < g.nsx && b < g.nsy) ? s[b * g.nsx + a] : 0.0;
+}
+// Next column of this set; the loop continues while one is left.
+__global__ void k_inf_col_next(int* col, int stride, int nR, cudaGraphConditionalHandle h) {
+  IB_GRID_DEP_WAIT();
+  if (threadIdx.x != 0) return;
+  const int c = *col + stride;
+  *col = c;
+  cudaGraphSetConditional(h, c < nR ? 1u : 0u);
+}
+
+// Clears a scratch set's unit vector after a build (prev = -1: nothing set).
+__global__ void k_inf_clear_unit(double* vort, int* prev) {
+  IB_GRID_DEP_WAIT();
+  if (threadIdx.x != 0) return;
+  const int p = *prev;
+  if (p >= 0) vort[p] = 0.0;
+  *prev = -1;
+}
+
 // K[c][v] = s(band vertex v) for every band vertex (0 for tile vertices outside the grid).
 __global__ void k_inf_gather(int c, int nR, const int2* __restrict__ tiles, GridDims g, const double* __restrict__ s,
                              double* __restrict__ K) {
@@ -240,8 +317,55 @@ static void free_band(Influence& I) {
   I.capK = I.capR = 0;
 }
 
+// The band build's scratch sets and streams (made on the first build, kept for rebuilds).
+static int build_scratch(Ctx* c) {
+  Influence& I = c->inf;
+  if (!I.bscr.empty()) return IB_OK;
+  const GridDims& g = c->g;
+  const int S = Influence::kBuildStreams, L = c->L;
+  const size_t ns = g.ns, per = (size_t)(4 + L) * ns + (size_t)g.nbc;
+  IB_CUDA_CHECK(cudaMalloc(&I.bmem, 8 * per * S));
+  IB_CUDA_CHECK(cudaMalloc(&I.bint, sizeof(int) * Influence::kSetInts * S));
+  // zero: the unit vectors start from an empty field, and the coarse levels' vorticity stays
+  // zero outside the centres coarsify writes
+  IB_CUDA_CHECK(cudaMemset(I.bmem, 0, 8 * per * S));
+  IB_CUDA_CHECK(cudaMemset(I.bint, 0xff, sizeof(int) * Influence::kSetInts * S));   // prev = -1
+  // ainv's response to a unit vector on row b, (1/c1 + lam_x + T_y)^-1 per x mode, decays
+  // away from row b at least as fast as rho^|r-b| with rho + 1/rho = 2 + 1/c1 (the slowest
+  // mode, lam_x -> 0); past trunc_rows rows it is below 1e-18 of its peak.  Only the input of
+  // the coarse levels' chain is cut there (the finest level keeps the exact modes), so the
+  // band's columns change at the 1e-18 level.
+  {
+    const double a = 2.0 + 1.0 / c->cvis[0];
+    const double rho = 0.5 * (a - std::sqrt(a * a - 4.0));
+    int R = g.nsy;
+    if (rho > 0.0 && rho < 1.0) R = (int)std::ceil(18.0 * std::log(10.0) / -std::log(rho)) + 2;
+    I.trunc_rows = std::min(R, g.nsy);
+  }
+  I.bscr.resize(S);
+  for (int i = 0; i < S; ++i) {
+    SchurScratch& sc = I.bscr[i];
+    double* b = I.bmem + per * i;
+    sc.vort = b; sc.specY = b + ns; sc.spec1 = b + 2 * ns; sc.s0 = b + 3 * ns;
+    for (int k = 0; k < L; ++k) sc.w[k] = b + (4 + k) * ns;
+    sc.sbc = b + (4 + L) * ns;
+    sc.prev = I.bint + Influence::kSetInts * i;
+    sc.rr_in = sc.prev + 1;
+    sc.rr_lv = sc.prev + 8;
+    if (cudaStreamCreateWithFlags(&sc.st, cudaStreamNonBlocking) != cudaSuccess) {
+      sc.st = nullptr;
+      return IB_ERR_CUDA;
+    }
+  }
+  return IB_OK;
+}
+
 void inf_free(Ctx* c) {
   Influence& I = c->inf;
+  for (SchurScratch& sc : I.bscr)
+    if (sc.st) cudaStreamDestroy(sc.st);
+  if (I.bmem) cudaFree(I.bmem);
+  if (I.bint) cudaFree(I.bint);
   free_band(I);
   if (I.pval) cudaFree(I.pval);
   if (I.pidx) cudaFree(I.pidx);
@@ -340,28 +464,101 @@ int inf_build(Ctx* c) {
   IB_CUDA_CHECK(cudaMemcpy(I.tile_of, tile_of.data(), sizeof(int) * tile_of.size(), cudaMemcpyHostToDevice));
   const int rr_out_h[3] = {bmin, bmax + 1, ROW_SKIP};
   IB_CUDA_CHECK(cudaMemcpy(I.rr_out, rr_out_h, sizeof(rr_out_h), cudaMemcpyHostToDevice));
-  // columns: unit vorticity at each band vertex through the fluid part of the operator
+  // columns: unit vorticity at each band vertex through the fluid part of the operator.  The
+  // columns are independent, and each is a chain of small latency-bound launches: they run on
+  // kBuildStreams streams at once, column col on set col % kBuildStreams (its own unit
+  // vector, scratch fields and output rows), after the work already on the context's stream.
+  // Each set's columns run as one captured graph: a while node whose body is one column with
+  // the column index on the device, so the host launches one graph per set.
+  RC(build_scratch(c));
   cudaStream_t st = c->st;
-  int* prev = I.flag + 2;
-  IB_CUDA_CHECK(cudaMemsetAsync(c->vort, 0, sizeof(double) * (size_t)g.ns, st));
-  const int minus1 = -1;
-  IB_CUDA_CHECK(cudaMemcpyAsync(prev, &minus1, sizeof(int), cudaMemcpyHostToDevice, st));
+  const int S = std::min(Influence::kBuildStreams, I.nR);
+  cudaEvent_t ev = nullptr;
+  IB_CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaEventRecord(ev, st);
+  for (int i = 0; i < S; ++i) cudaStreamWaitEvent(I.bscr[i].st, ev, 0);
   const bool prof = c->prof_on;
   c->prof_on = false;
   int rc = IB_OK;
-  for (int col = 0; col < I.nR && rc == IB_OK; ++col) {
-    count_launch();
-    k_inf_unit<<<1, 32, 0, st>>>(col, I.tiles, g, c->vort, prev, I.rr_in);
-    const double* ring0 = nullptr;
-    rc = schur_fluid(c, c->vort, I.rr_in, I.rr_out, c->mv_s[0], &ring0);
-    if (rc != IB_OK) break;
-    count_launch();
-    k_inf_gather<<<cdiv(I.nR, 256), 256, 0, st>>>(col, I.nR, I.tiles, g, c->mv_s[0], I.K);
-    if (cudaGetLastError() != cudaSuccess) rc = IB_ERR_CUDA;
+  long long body_launches = 0;
+  std::vector<cudaGraphExec_t> execs(S, nullptr);
+  cudaStream_t cap = nullptr;
+  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) rc = IB_ERR_CUDA;
+  const long long l0 = launch_count();
+  for (int i = 0; i < S && rc == IB_OK; ++i) {
+    const SchurScratch& sc = I.bscr[i];
+    int* col = sc.prev + 4;   // the set's fifth int (after prev and rr_in)
+    cudaGraph_t graph = nullptr;
+    do {
+      if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
+      count_launch();
+      k_inf_col_init<<<1, 32, 0, cap>>>(col, i);
+      cudaGraphConditionalHandle h = 0;
+      cudaGraph_t body = nullptr;
+      if (cudaGraphConditionalHandleCreate(&h, capture_graph(cap), 1, cudaGraphCondAssignDefault) != cudaSuccess)
+        rc = IB_ERR_CUDA;
+      if (rc == IB_OK) rc = add_while(cap, h, &body);
+      if (rc == IB_OK &&
+          cudaStreamBeginCaptureToGraph(sc.st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        rc = IB_ERR_CUDA;
+      if (rc == IB_OK) {
+        const long long b0 = launch_count();
+        count_launch();
+        k_inf_unit_at<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in, sc.rr_lv, c->L,
+                                           I.trunc_rows);
+        const double* ring0 = nullptr;
+        rc = schur_fluid(c, sc.vort, sc.rr_in, I.rr_out, sc.s0, &ring0, &sc);
+        count_launches(2);
+        k_inf_gather_at<<<cdiv(I.nR, 256), 256, 0, sc.st>>>(col, I.nR, I.tiles, g, sc.s0, I.K);
+        k_inf_col_next<<<1, 32, 0, sc.st>>>(col, S, I.nR, h);
+        body_launches = launch_count() - b0;
+        cudaGraph_t tmp;
+        if (cudaStreamEndCapture(sc.st, &tmp) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+      }
+      if (cudaStreamEndCapture(cap, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+      if (rc == IB_OK) make_edges_programmatic(body);
+      if (rc == IB_OK && cudaGraphInstantiate(&execs[i], graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+    } while (false);
+    if (graph) cudaGraphDestroy(graph);
+  }
+  count_launches(-(launch_count() - l0));   // captured, not run
+  cudaGetLastError();
+  if (rc == IB_OK) {
+    for (int i = 0; i < S && rc == IB_OK; ++i)
+      if (cudaGraphLaunch(execs[i], I.bscr[i].st) != cudaSuccess) rc = IB_ERR_CUDA;
+    if (rc == IB_OK) count_launches(S + (long long)I.nR * body_launches);
+  } else {
+    // capture unavailable: the same columns launched one by one from the host
+    rc = IB_OK;
+    for (int col = 0; col < I.nR && rc == IB_OK; ++col) {
+      SchurScratch sc = I.bscr[col % S];
+      sc.rr_lv = nullptr;   // every row transformed
+      count_launch();
+      k_inf_unit<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in);
+      const double* ring0 = nullptr;
+      rc = schur_fluid(c, sc.vort, sc.rr_in, I.rr_out, sc.s0, &ring0, &sc);
+      if (rc != IB_OK) break;
+      count_launch();
+      k_inf_gather<<<cdiv(I.nR, 256), 256, 0, sc.st>>>(col, I.nR, I.tiles, g, sc.s0, I.K);
+      if (cudaGetLastError() != cudaSuccess) rc = IB_ERR_CUDA;
+    }
   }
   c->prof_on = prof;
+  // the context's stream continues after every column; the sets' unit vectors are cleared
+  // for the next build
+  for (int i = 0; i < S; ++i) {
+    const SchurScratch& sc = I.bscr[i];
+    count_launch();
+    k_inf_clear_unit<<<1, 32, 0, sc.st>>>(sc.vort, sc.prev);
+    cudaEventRecord(ev, sc.st);
+    cudaStreamWaitEvent(st, ev, 0);
+  }
+  for (int i = 0; i < S; ++i) cudaStreamSynchronize(I.bscr[i].st);
+  for (cudaGraphExec_t e : execs)
+    if (e) cudaGraphExecDestroy(e);
+  if (cap) cudaStreamDestroy(cap);
+  cudaEventDestroy(ev);
   RC(rc);
-  IB_CUDA_CHECK(cudaMemsetAsync(c->vort, 0, sizeof(double) * (size_t)g.ns, st));
   IB_CUDA_CHECK(cudaStreamSynchronize(st));
   I.columns += I.nR;
   I.builds += 1;

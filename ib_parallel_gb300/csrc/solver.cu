@@ -643,24 +643,34 @@ static int ring_from_modes(Ctx* c, const double* spec, double* s, double* ring, 
 //  * finest level: its forward transform is 2m Y plus the boundary terms; its inverse is
 //    needed only on the rows rr_out selects.
 int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out, double* s_out,
-                const double** ring0_out) {
+                const double** ring0_out, const SchurScratch* sc) {
   const GridDims& g = c->g;
   const int L = c->L;
-  cudaStream_t st = c->st;
+  // the context's own buffers unless a scratch set (and its stream) is given
+  SchurScratch own;
+  if (!sc) {
+    own.specY = c->specY; own.spec1 = c->spec1; own.sbc = c->sbc; own.st = c->st;
+    for (int k = 0; k < L; ++k) own.w[k] = c->mv_w[k];
+    sc = &own;
+  }
+  cudaStream_t st = sc->st;
+  double* specY = sc->specY;
+  double* spec1 = sc->spec1;
   auto mark = [&](int i) { if (c->stage_on) cudaEventRecord(c->stage_ev[i], st); };
   {
     DstXArgs a;
-    a.in = vort; a.out = c->specY; a.rowrange = rr_in;
+    a.in = vort; a.out = specY; a.rowrange = rr_in;
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
   }
   {
     ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-    RC(tri_solve(c->tri_ainv, c->specY, c->specY, g.nsx, c->tl, st));
+    RC(tri_solve(c->tri_ainv, specY, specY, g.nsx, c->tl, st));
   }
   {
     DstXArgs a;
-    a.in = c->specY; a.out = c->mv_w[0];
+    a.in = specY; a.out = sc->w[0];
+    if (sc->rr_lv) a.rowrange = sc->rr_lv;   // band build: the rows of ainv's response
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx, st));
   }
@@ -668,24 +678,29 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
   const double* ring0 = c->zero_ring;
   if (L > 1) {
     // outside their centres the coarse vorticities of the operator stay zero
-    for (int k = 1; k < L; ++k) RC(launch_coarsify(g, c->mv_w[k - 1], c->mv_w[k], st));
+    for (int k = 1; k < L; ++k) RC(launch_coarsify(g, sc->w[k - 1], sc->w[k], st));
     mark(3);
     for (int k = L - 1; k >= 1; --k) {
       DstXArgs a;
-      a.in = c->mv_w[k]; a.out = c->spec1;
-      a.ring = c->sbc; a.fac = 1.0;
-      a.rowmode = k == L - 1 ? c->rm_top : c->rm_coarse;
+      a.in = sc->w[k]; a.out = spec1;
+      a.ring = sc->sbc; a.fac = 1.0;
+      if (sc->rr_lv) {   // band build: the coarsified rows holding data (and the edge rows)
+        a.rowrange = sc->rr_lv + 3 * k;
+        a.fft_edge_rows = k == L - 1 ? 0 : 1;
+      } else {
+        a.rowmode = k == L - 1 ? c->rm_top : c->rm_coarse;
+      }
       {
         ProfScope ps(c, 0, pass_bytes(c, 1, 1));
         RC(dst_pass_x(c->px, g.nsy, g.nsx, k == L - 1 ? PRE_COPY : PRE_APPLYBC, a, g, c->lx, st));
       }
       {
         ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-        RC(tri_solve(c->tri_ctci, c->spec1, c->spec1, g.nsx, c->tl, st));
+        RC(tri_solve(c->tri_ctci, spec1, spec1, g.nsx, c->tl, st));
       }
-      RC(ring_from_modes(c, c->spec1, c->mv_s[k], c->sbc));
+      RC(dst_ring_from_modes(c->px, g, spec1, g.nsx, c->wmat, 1.0, sc->sbc, st));
     }
-    ring0 = c->sbc;
+    ring0 = sc->sbc;
   } else {
     mark(3);
   }
@@ -694,17 +709,17 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
     // S_x(vort1 + apply_bc(ring0)) = 2m Y + transform of the boundary terms: the two full
     // boundary rows by dot products, the others in closed form (two nonzero samples)
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-    RC(dst_x_bc_modes(c->px, g, ring0, c->wmat, c->sk2, c->specY, 2.0 * g.m, c->spec1, st));
+    RC(dst_x_bc_modes(c->px, g, ring0, c->wmat, c->sk2, specY, 2.0 * g.m, spec1, st));
   }
   mark(5);
   {
     ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-    RC(tri_solve(c->tri_ctci, c->spec1, c->spec1, g.nsx, c->tl, st));
+    RC(tri_solve(c->tri_ctci, spec1, spec1, g.nsx, c->tl, st));
   }
   mark(6);
   {
     DstXArgs a;
-    a.in = c->spec1; a.out = s_out; a.rowrange = rr_out;
+    a.in = spec1; a.out = s_out; a.rowrange = rr_out;
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
   }
@@ -820,7 +835,7 @@ static int read_ist(Ctx* c) {
 
 // Adds a conditional (while) node after the current capture position of `st` and
 // returns its body graph.
-static int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body) {
+int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body) {
   cudaStreamCaptureStatus stat;
   cudaGraph_t capg;
   const cudaGraphNode_t* deps = nullptr;
@@ -838,7 +853,7 @@ static int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t*
   return IB_OK;
 }
 
-static cudaGraph_t capture_graph(cudaStream_t st) {
+cudaGraph_t capture_graph(cudaStream_t st) {
   cudaStreamCaptureStatus stat;
   cudaGraph_t g = nullptr;
   cudaStreamGetCaptureInfo(st, &stat, nullptr, &g, nullptr, nullptr, nullptr);
@@ -1021,7 +1036,7 @@ static void step_acc(Ctx* c, int ph, int a, int b) {
 // dependent kernel may be scheduled while its predecessor finishes (every kernel here starts
 // with IB_GRID_DEP_WAIT).  Edges to or from other nodes keep full serialisation.  An edge the
 // driver refuses to convert is put back as it was.
-static void make_edges_programmatic(cudaGraph_t g) {
+void make_edges_programmatic(cudaGraph_t g) {
   size_t n = 0;
   if (cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &n) != cudaSuccess || n == 0) {
     cudaGetLastError();
