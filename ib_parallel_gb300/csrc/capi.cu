@@ -175,6 +175,7 @@ static double* vec_ptr(Ctx* c, int which) {
     case IB_VEC_F_RDST: return c->f_rdst;
     case IB_VEC_XB: return c->xb;
     case IB_VEC_YB: return c->yb;
+    case IB_VEC_UB: return c->ub;
     default: return nullptr;
   }
 }
@@ -199,6 +200,13 @@ int ib_set_vector(IbCtx* h, int which, const double* in) {
     return fail(IB_ERR_CUDA, "copy failed");
   int rc = IB_OK;
   if (which == IB_VEC_XB || which == IB_VEC_YB) rc = ib::op_reg_prep(c);
+  if (which == IB_VEC_UB && !c->ub_on) {
+    // from now on every Schur right-hand side carries -delta u_B: the captured phases that
+    // form it are captured again
+    c->ub_on = true;
+    ib::drop_phase(&c->graph_fsi_rhs);
+    ib::drop_phase(&c->graph_fsi_loop);
+  }
   if (rc == IB_OK) rc = ib::check_err(c);
   return op_result(rc, "set_vector failed");
 }
@@ -226,6 +234,22 @@ int ib_get_body_state(IbCtx* h, double* theta, double* thetad, double* thetadd) 
       cudaStreamSynchronize(c->st) != cudaSuccess)
     return fail(IB_ERR_CUDA, "copy failed");
   return IB_OK;
+}
+
+int ib_write_variables(IbCtx* h, const char* path) {
+  CTX_OR_FAIL(h);
+  if (!path) return fail(IB_ERR_ARG, "null path");
+  std::string msg;
+  int rc = ib::op_write_variables(c, path, &msg);
+  return rc == IB_OK ? IB_OK : fail(rc, ("write_variables: " + msg).c_str());
+}
+
+int ib_read_variables(IbCtx* h, const char* path, int itime) {
+  CTX_OR_FAIL(h);
+  if (!path) return fail(IB_ERR_ARG, "null path");
+  std::string msg;
+  int rc = ib::op_read_variables(c, path, itime, &msg);
+  return rc == IB_OK ? IB_OK : fail(rc, ("read_variables: " + msg).c_str());
 }
 
 int ib_get_counters(IbCtx* h, int* ksp_iter, int* fsi_iter) {

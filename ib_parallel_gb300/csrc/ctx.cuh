@@ -172,6 +172,10 @@ struct Ctx {
   std::vector<TorsBody> tb_h;
   double *f = nullptr, *f_rdst = nullptr, *xb = nullptr, *yb = nullptr;
   double *rhsf = nullptr, *tmpf = nullptr, *tmpf2 = nullptr, *forces = nullptr;
+  // prescribed motion of rigid bodies (user.F90:137-174 compute_rhs_prescribed): the body
+  // velocity u_B; once set, -delta u_B joins the right-hand side of every Schur solve
+  double* ub = nullptr;
+  bool ub_on = false;
   int *comp = nullptr, *bid = nullptr;
   RegDev reg{};
   TorsBody* tb = nullptr;
@@ -285,6 +289,9 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
 // influence.cu
 int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
+// checkpoint.cu: the reference's restart file (variables.F90:709-913)
+int op_write_variables(Ctx* c, const char* path, std::string* msg);
+int op_read_variables(Ctx* c, const char* path, int itime, std::string* msg);
 // graph helpers (solver.cu): a while node after the capture position of st (its body graph
 // returned), the graph st is capturing, and programmatic kernel-to-kernel edges
 int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body);

@@ -44,6 +44,7 @@ int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac
 int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st);
 int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st);
 int launch_sub(int n, const double* x, const double* y, double* z, cudaStream_t st);
+int launch_sub_scaled(int n, double d, const double* x, double* z, cudaStream_t st);
 int launch_fill(int n, double v, double* z, cudaStream_t st);
 
 // ibm.cu -- fsinterface.F90, grid.F90:459-528, operators_struct.F90:711-834

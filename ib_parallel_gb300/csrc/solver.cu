@@ -216,7 +216,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += (size_t)L * ns + (size_t)L * nbc + 2 * L;       // per-level spectra and rings (vort2flux)
   dbl += (size_t)g.nsx * g.nsx + (size_t)L * (2 * (size_t)g.nsy + 2 * (size_t)g.nsx);   // edge matrix, terms
   dbl += (size_t)(L - 1) * ns + (size_t)g.nsy;           // vort2flux's coarse-level modes, row modes
-  dbl += 7 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
+  dbl += 8 * (size_t)nf + 2 * (size_t)nbody + 49 * (size_t)nf;
   dbl += 49 * (size_t)nf + (size_t)nf + 1;               // weights snapshot (+ its origins, as doubles)
   dbl += 3 * ((size_t)nt + 1) + 1;                       // fused FSI update: theta, sin, cos; ticket
   dbl += 8 * (size_t)nt + nt + 3;
@@ -264,7 +264,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   for (int k = 0; k < L; ++k) { c->sdv[k] = P.take<double>(2 * (size_t)g.nsy); c->edgev[k] = P.take<double>(2 * (size_t)g.nsx); }
   c->f = P.take<double>(nf); c->f_rdst = P.take<double>(nf); c->xb = P.take<double>(nf);
   c->yb = P.take<double>(nf); c->rhsf = P.take<double>(nf); c->tmpf = P.take<double>(nf);
-  c->tmpf2 = P.take<double>(nf); c->forces = P.take<double>(2 * nbody + 1);
+  c->tmpf2 = P.take<double>(nf); c->forces = P.take<double>(2 * nbody + 1); c->ub = P.take<double>(nf);
   c->comp = P.take<int>(nf); c->bid = P.take<int>(nf);
   c->reg.comp = c->comp; c->reg.ix = P.take<int>(nf); c->reg.iy = P.take<int>(nf);
   c->reg.w = P.take<double>(49 * (size_t)nf); c->reg.bbox = P.take<int>(16);
@@ -1166,6 +1166,7 @@ static int build_fsi_loop(Ctx* c) {
         RC(inf_assemble_b(c, s2));
         if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s2));
         RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s2));
+        if (c->ub_on) RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, s2));
         RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s2));
         IB_CUDA_CHECK(cudaEventRecord(ev_rhs, s2));
         // s3: a copy of the current origins and weights and their contribution lists
@@ -1328,7 +1329,9 @@ int op_advance(Ctx* c) {
   c->fsi_err_capped = 0.0;
   c->itime += 1;
   const int it = c->itime;
-  if (it == 1 && p.num_stat && c->nf > 0) RC(preprocess_chol(c));
+  // timestepper.F90:76 factorises at it == 1 only, so a num_stat restart (istart > 0) would
+  // solve with a matrix never factorised; here the first step of a context factorises.
+  if (p.num_stat && c->nf > 0 && !c->chol_ready) RC(preprocess_chol(c));
   step_mark(c, 0);
   // boundary values of the previous step (timestepper.F90:103-117) and the predictor, coarse
   // to fine (timestepper.F90:121-236)
@@ -1401,6 +1404,8 @@ int op_advance(Ctx* c) {
           // k_tors_rhs writes every unknown of a torsional body: rigid bodies' start at zero
           if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, c->st));
           RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, c->st));
+          // prescribed rigid-body motion (timestepper.F90:327-331): rhsf - delta u_B
+          if (c->ub_on) RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, c->st));
           return launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, c->st);
         }));
         step_mark(c, 4);
@@ -1476,7 +1481,13 @@ int op_advance(Ctx* c) {
       // fsi_tol; the reference carries on silently, this step reports it (after finishing)
       c->fsi_err_capped = err >= p.fsi_tol ? err : 0.0;
     } else {
-      RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, nullptr, c->rhsf, st));
+      if (c->ub_on) {   // -delta u_B of a prescribed motion, then E q accumulated onto it
+        RC(launch_fill(c->nf, 0.0, c->rhsf, st));
+        RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, st));
+        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, st));
+      } else {
+        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, nullptr, c->rhsf, st));
+      }
       RC(launch_chol_solve(c->nf, c->cholM, c->rhsf, c->f, st));
       RC(op_redistribute(c, c->f, c->f_rdst));
     }

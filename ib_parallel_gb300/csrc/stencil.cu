@@ -268,6 +268,13 @@ __global__ void k_sub(int n, const double* __restrict__ x, const double* __restr
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) z[t] = x[t] - y[t];
 }
+// z = z - d x, the product rounded before the difference (compute_rhs_prescribed's
+// rhsf(i) - delta*u_B, user.F90:137-174)
+__global__ void k_sub_scaled(int n, double d, const double* __restrict__ x, double* __restrict__ z) {
+  IB_GRID_DEP_WAIT();
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) z[t] = __dsub_rn(z[t], __dmul_rn(d, x[t]));
+}
 __global__ void k_fill(int n, double v, double* __restrict__ z) {
   IB_GRID_DEP_WAIT();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -341,6 +348,12 @@ int launch_axpby(int n, double a, const double* x, double b, const double* y, do
 int launch_sub(int n, const double* x, const double* y, double* z, cudaStream_t st) {
   count_launch();
   k_sub<<<blocks(n), 256, 0, st>>>(n, x, y, z);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_sub_scaled(int n, double d, const double* x, double* z, cudaStream_t st) {
+  if (n <= 0) return IB_OK;
+  count_launch();
+  k_sub_scaled<<<blocks(n), 256, 0, st>>>(n, d, x, z);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_fill(int n, double v, double* z, cudaStream_t st) {

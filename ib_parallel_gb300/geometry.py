@@ -54,3 +54,188 @@ def config_plate_800x400(seed: int = 0, npts: int = 51) -> tuple:
     p = Params(m=800, n=400, mgridlev=5, dt=1e-3, Re=500.0, len=8.0, offsetx=1.0, offsety=2.0,
                fsi_tol=1e-10, atol=1e-10, rtol=1e-10)
     return p, [torsional_plate(npts, 1.0, gamma0, itheta=0.5 / 3.0, ktheta=1e-3)]
+
+
+# ---------------------------------------------------------------------------------------------
+# The reference's input files (input/ib.inp, input/body.NNN.inp), read through the library's C
+# ABI (ib_read_namelist, ib_read_body, ib_count_bodies) and written in the same layout.
+# ---------------------------------------------------------------------------------------------
+RUN_CONTROL_KEYS = ("istart", "istop", "isave", "irestart", "compute_pressure", "dimen", "motion_prescribed",
+                    "sub_domain", "sub_domain_full_rectangular", "sub_domain_precomputed", "sdxi", "sdxe", "sdyi",
+                    "sdye", "delta_sd")
+
+
+def read_namelist(path, params: Params = None) -> tuple:
+    """input (parameters.F90:51-78): the &read_parameters group of the file at path.  Returns the
+    Params (items absent from the file keep params' values) and the run-control items."""
+    import ctypes as C
+    import dataclasses
+    import os
+
+    from . import ibgpu as G
+    base = params if params is not None else Params(m=0, n=0, mgridlev=0, dt=0.0, Re=0.0, len=0.0, offsetx=0.0,
+                                                    offsety=0.0)
+    cp = base.to_c()
+    rc = G.IbRunControl()
+    G._check(G.load().ib_read_namelist(os.fsencode(path), C.byref(cp), C.byref(rc)), "ib_read_namelist")
+    out = dataclasses.replace(base, m=cp.m, n=cp.n, mgridlev=cp.mgridlev, dt=cp.dt, Re=cp.Re, len=cp.len,
+                              offsetx=cp.offsetx, offsety=cp.offsety, fsi_tol=cp.fsi_tol, atol=cp.atol,
+                              rtol=cp.rtol, num_stat=bool(cp.num_stat))
+    return out, {k: getattr(rc, k) for k in RUN_CONTROL_KEYS}
+
+
+def read_body_file(path) -> Body:
+    """One input/body.NNN.inp (grid.F90:252-288)."""
+    import ctypes as C
+    import os
+
+    from . import ibgpu as G
+    lib = G.load()
+    b = G.IbBody()
+    cap = 0
+    x = y = np.zeros(1)
+    for _ in range(2):   # the first call reports the point count when the arrays are too small
+        rc = lib.ib_read_body(os.fsencode(path), C.byref(b), x.ctypes.data_as(C.POINTER(C.c_double)),
+                              y.ctypes.data_as(C.POINTER(C.c_double)), cap)
+        if rc == G.IB_OK:
+            break
+        if b.npts > cap:
+            cap = b.npts
+            x, y = np.zeros(cap), np.zeros(cap)
+            continue
+        G._check(rc, "ib_read_body")
+    G._check(rc, "ib_read_body")
+    return Body(x=x[:b.npts].copy(), y=y[:b.npts].copy(), fam=b.fam, gamma0_deg=b.gamma0_deg,
+                alpha0_deg=b.alpha0_deg, itheta=b.itheta, ktheta=b.ktheta, ctheta=b.ctheta)
+
+
+def load_input(directory) -> tuple:
+    """The run an input directory describes (ib.inp and body.001.inp, body.002.inp, ...)."""
+    import ctypes as C
+    import os
+    from pathlib import Path
+
+    from . import ibgpu as G
+    d = Path(directory)
+    params, rc = read_namelist(d / "ib.inp")
+    n = C.c_int(0)
+    G._check(G.load().ib_count_bodies(os.fsencode(d), C.byref(n)), "ib_count_bodies")
+    return params, rc, [read_body_file(d / f"body.{i + 1:03d}.inp") for i in range(n.value)]
+
+
+def write_body_file(path, body: Body) -> None:
+    """A body file in the layout grid.F90:252-288 reads (as input/*/build_*.m write it)."""
+    lines = [f"{body.npts:<6d} ", f"{int(body.fam):<6d} "]
+    if body.fam == 2:
+        lines += [f"{v:.16f}" for v in (body.gamma0_deg, body.alpha0_deg, body.itheta, body.ktheta, body.ctheta)]
+    lines += [f"{xv:<20.16f} {yv:<20.16f}" for xv, yv in zip(body.x, body.y)]
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+
+
+def write_namelist(path, params: Params, run_control: dict = None) -> None:
+    """An input/ib.inp for params (and the run-control items given)."""
+    def fmt(v):
+        if isinstance(v, bool):
+            return "T" if v else "F"
+        if isinstance(v, int):
+            return str(v)
+        return repr(float(v))
+    items = dict(M=params.m, N=params.n, DT=params.dt, Re=params.Re, FSI_TOL=params.fsi_tol, ATOL=params.atol,
+                 RTOL=params.rtol, LEN=params.len, OFFSETX=params.offsetx, OFFSETY=params.offsety,
+                 MGRIDLEV=params.mgridlev, num_stat=bool(params.num_stat))
+    for k, v in (run_control or {}).items():
+        items[k.upper()] = bool(v) if k in ("compute_pressure", "motion_prescribed", "sub_domain",
+                                            "sub_domain_full_rectangular", "sub_domain_precomputed") else v
+    with open(path, "w") as fh:
+        fh.write("&READ_PARAMETERS\n" + "".join(f"{k} = {fmt(v)},\n" for k, v in items.items()) + "/\n")
+
+
+# ---------------------------------------------------------------------------------------------
+# NACA 00XX airfoil with points a fixed distance apart (the method of input/airfoil*/
+# naca00_ibfm.m, restated): the half-thickness 5 t c (0.2969 sqrt(x/c) - 0.1260 (x/c)
+# - 0.3516 (x/c)^2 + 0.2843 (x/c)^3 - 0.1036 (x/c)^4) -- the last coefficient closes the
+# trailing edge -- is walked from the point where it equals ds/2 (so the two leading-edge points
+# are ds apart) in steps of straight-line distance ds, stopping where the surface, past
+# mid-chord, comes within ds/2 of the centreline; the lower surface mirrors the upper.  The
+# nominal chord is grown until the last kept point sits at the requested chord.  Points run
+# from the trailing edge over the upper surface to the leading edge and back along the lower
+# surface, then are rotated by the angle of attack (nose up for alpha > 0).
+# ---------------------------------------------------------------------------------------------
+def _naca_upper(t: float, c: float, ds: float) -> np.ndarray:
+    a = 5.0 * t * c * np.array([0.2969, -0.1260, -0.3516, 0.2843, -0.1036])
+
+    def ubd(x):
+        u = max(x, 0.0) / c
+        return a[0] * math.sqrt(u) + a[1] * u + a[2] * u * u + a[3] * u ** 3 + a[4] * u ** 4
+
+    def root(fn, lo, hi):
+        flo = fn(lo)
+        for _ in range(80):
+            mid = 0.5 * (lo + hi)
+            fm = fn(mid)
+            if (fm > 0) == (flo > 0):
+                lo, flo = mid, fm
+            else:
+                hi = mid
+            if hi - lo < 1e-15 * max(1.0, abs(hi)):
+                break
+        return 0.5 * (lo + hi)
+
+    x0 = root(lambda x: ubd(x) - ds / 2, 1e-300, ds)
+    pts = [(x0, ubd(x0))]
+    while True:
+        xp, yp = pts[-1]
+        if xp > 0.5 * c and yp < ds / 2:
+            pts.pop()   # the point that crossed into the trailing-edge gap is dropped
+            break
+        if xp >= c:
+            break
+        xn = root(lambda x: (x - xp) ** 2 + (ubd(x) - yp) ** 2 - ds * ds, xp, min(xp + ds, c))
+        pts.append((xn, ubd(xn)))
+    return np.array(pts)
+
+
+def naca00(thickness_pct: float = 12.0, ds: float = 0.01, chord: float = 1.0, alpha_deg: float = 0.0,
+           xc: float = 0.0, yc: float = 0.0) -> tuple:
+    """x, y of a NACA 00XX airfoil (leading edge at (xc, yc) before rotation about it)."""
+    t = min(abs(thickness_pct), 100.0) / 100.0
+    # the trailing-edge cut moves in steps of about ds as the nominal chord grows: scan nominal
+    # chords up to 10% longer and keep the one whose last point lies closest to `chord`
+    best = None
+    for i in range(101):
+        c = chord * (1.0 + 0.001 * i)
+        cand = _naca_upper(t, c, ds)
+        err = abs(chord - cand[-1, 0])
+        if best is None or err < best[0]:
+            best = (err, cand)
+    up = best[1]
+    xs = np.r_[up[::-1, 0], up[:, 0]]
+    ys = np.r_[up[::-1, 1], -up[:, 1]]
+    al = math.radians(alpha_deg)
+    xr = math.cos(al) * xs + math.sin(al) * ys
+    yr = -math.sin(al) * xs + math.cos(al) * ys
+    return xc + xr, yc + yr
+
+
+def pitching_motion(x_ref: np.ndarray, y_ref: np.ndarray, t: float, amp_deg: float, freq: float, phase: float = 0.0,
+                    pivot=(0.25, 0.0)) -> tuple:
+    """A rigid body pitching about `pivot` as alpha(t) = A sin(2 pi f t + phi) (nose up for
+    alpha > 0): positions and velocities of its points at time t, in the layout of the
+    body-point vectors (x-unknowns then y-unknowns, each holding every point).  Set them as
+    IB_VEC_XB, IB_VEC_YB and IB_VEC_UB before each step (the prescribed-motion hooks of
+    user.F90:87-174)."""
+    w = 2.0 * math.pi * freq
+    al = math.radians(amp_deg) * math.sin(w * t + phase)
+    ald = math.radians(amp_deg) * w * math.cos(w * t + phase)
+    dx, dy = x_ref - pivot[0], y_ref - pivot[1]
+    ca, sa = math.cos(al), math.sin(al)
+    px = pivot[0] + ca * dx + sa * dy
+    py = pivot[1] - sa * dx + ca * dy
+    # d/dt of the rotation: (-sa dx + ca dy, -ca dx - sa dy) alpha'
+    ux = ald * (-sa * dx + ca * dy)
+    uy = ald * (-ca * dx - sa * dy)
+    xb = np.r_[px, px]
+    yb = np.r_[py, py]
+    ub = np.r_[ux, uy]
+    return xb, yb, ub

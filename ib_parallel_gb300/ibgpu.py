@@ -27,7 +27,7 @@ IB_OK = 0
 ERRORS = {1: "IB_ERR_ARG", 2: "IB_ERR_CUDA", 3: "IB_ERR_NOMEM", 4: "IB_ERR_GMRES", 5: "IB_ERR_FSI",
           6: "IB_ERR_NONFINITE", 7: "IB_ERR_DOMAIN", 8: "IB_ERR_STATE"}
 FIELDS = {"omega": 0, "s": 1, "qx": 2, "qy": 3, "rhs_old": 4, "q0x": 5, "q0y": 6}
-VECTORS = {"f": 0, "f_rdst": 1, "xb": 2, "yb": 3}
+VECTORS = {"f": 0, "f_rdst": 1, "xb": 2, "yb": 3, "ub": 4}
 
 # Every symbol include/ib_gpu.h declares (checked by the CPU tests).
 EXPORTS = [
@@ -40,6 +40,7 @@ EXPORTS = [
     "ib_get_stream", "ib_profile", "ib_profile_read", "ib_get_work", "ib_measure_fp64_peak",
     "ib_launch_count", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
     "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile", "ib_get_launch_shapes",
+    "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
 ]
 
 
@@ -55,6 +56,14 @@ class IbParams(C.Structure):
                 ("num_stat", C.c_int), ("motion", C.c_double * 5),
                 ("gmres_restart", C.c_int), ("gmres_max_it", C.c_int), ("fsi_max_it", C.c_int),
                 ("autotune", C.c_int), ("schur_mode", C.c_int), ("influence_margin", C.c_int)]
+
+
+class IbRunControl(C.Structure):
+    _fields_ = [("istart", C.c_int), ("istop", C.c_int), ("isave", C.c_int), ("irestart", C.c_int),
+                ("compute_pressure", C.c_int), ("dimen", C.c_int), ("motion_prescribed", C.c_int),
+                ("sub_domain", C.c_int), ("sub_domain_full_rectangular", C.c_int),
+                ("sub_domain_precomputed", C.c_int), ("sdxi", C.c_double), ("sdxe", C.c_double),
+                ("sdyi", C.c_double), ("sdye", C.c_double), ("delta_sd", C.c_double)]
 
 
 class IbBody(C.Structure):
@@ -110,6 +119,11 @@ def load(path: Optional[os.PathLike] = None):
         "ib_step_profile": ([P, C.c_int, D, C.POINTER(C.c_longlong)], C.c_int),
         "ib_get_influence_stats": ([P, C.POINTER(C.c_longlong), D], C.c_int),
         "ib_get_launch_shapes": ([P, I], C.c_int),
+        "ib_write_variables": ([P, C.c_char_p], C.c_int),
+        "ib_read_variables": ([P, C.c_char_p, C.c_int], C.c_int),
+        "ib_read_namelist": ([C.c_char_p, C.POINTER(IbParams), C.POINTER(IbRunControl)], C.c_int),
+        "ib_read_body": ([C.c_char_p, C.POINTER(IbBody), D, D, C.c_int], C.c_int),
+        "ib_count_bodies": ([C.c_char_p, I], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -261,6 +275,14 @@ class Simulation:
         it = C.c_int()
         _check(self.lib.ib_advance(self.h, C.byref(it)), "ib_advance")
         return it.value
+
+    def write_variables(self, path) -> None:
+        """write_variables (variables.F90:709-803): the reference's restart file at path."""
+        _check(self.lib.ib_write_variables(self.h, os.fsencode(path)), "ib_write_variables")
+
+    def read_variables(self, path, itime: int) -> None:
+        """read_variables (variables.F90:807-913): restore the state; the next step is itime + 1."""
+        _check(self.lib.ib_read_variables(self.h, os.fsencode(path), int(itime)), "ib_read_variables")
 
     def get_field(self, name: str, level: int = 0) -> np.ndarray:
         out = np.empty(self.shapes[name])

@@ -72,7 +72,19 @@ typedef struct IbCtx IbCtx;
 
 enum { IB_FIELD_OMEGA = 0, IB_FIELD_S = 1, IB_FIELD_QX = 2, IB_FIELD_QY = 3, IB_FIELD_RHS_OLD = 4,
        IB_FIELD_Q0X = 5, IB_FIELD_Q0Y = 6 };
-enum { IB_VEC_F = 0, IB_VEC_F_RDST = 1, IB_VEC_XB = 2, IB_VEC_YB = 3 };
+/* IB_VEC_UB: velocity u_B of prescribed rigid-body motion at the body points (nf, per body x then
+ * y components; the reference's compute_rhs_prescribed, user.F90:137-174).  Once set it joins
+ * every Schur right-hand side as -delta u_B (timestepper.F90:327-331, 479); a host moving a rigid
+ * body sets IB_VEC_XB/YB (advance_rigidbody, user.F90:87-115) and IB_VEC_UB before each step. */
+enum { IB_VEC_F = 0, IB_VEC_F_RDST = 1, IB_VEC_XB = 2, IB_VEC_YB = 3, IB_VEC_UB = 4 };
+
+/* The namelist items of input/ib.inp that IbParams does not hold (parameters.F90:13-48). */
+typedef struct IbRunControl {
+  int istart, istop, isave, irestart;
+  int compute_pressure, dimen, motion_prescribed;
+  int sub_domain, sub_domain_full_rectangular, sub_domain_precomputed;
+  double sdxi, sdxe, sdyi, sdye, delta_sd;
+} IbRunControl;
 
 const char* ib_last_error(void);
 int ib_version(void);
@@ -101,6 +113,31 @@ int ib_set_vector(IbCtx* ctx, int which, const double* in);
 int ib_get_forces(IbCtx* ctx, double* cx, double* cy);
 /* torsional state of family-2 bodies in file order (variables.F90:31-32) */
 int ib_get_body_state(IbCtx* ctx, double* theta, double* thetad, double* thetadd);
+/* input (parameters.F90:51-78): the namelist group &read_parameters of the file at path (the
+ * reference's input/ib.inp).  Items absent from the file keep the values p and rc hold on
+ * entry, as a Fortran namelist read leaves them; an unknown item or a malformed value is an
+ * error (IB_ERR_ARG). */
+int ib_read_namelist(const char* path, IbParams* p, IbRunControl* rc);
+/* setup_geometry (grid.F90:252-288): one body file input/body.NNN.inp (npts; fam; for fam 2 the
+ * angles gamma0, alpha0 in degrees and itheta, ktheta, ctheta; then npts lines of x y), read as
+ * the reference's list-directed READs do.  x, y: arrays of capacity cap.  On return body holds
+ * the header, npts and pointers to x, y; if cap < npts nothing is copied and IB_ERR_ARG is
+ * returned with body->npts set, so a caller can size its arrays and call again. */
+int ib_read_body(const char* path, IbBody* body, double* x, double* y, int cap);
+/* The bodies of an input directory (grid.F90:252-260): body.001.inp, body.002.inp, ... up to the
+ * first number that has no file. */
+int ib_count_bodies(const char* dir, int* nbody);
+/* write_variables (variables.F90:709-803): the restart file output/dataRR_IIIIIII.var of one
+ * rank at path, in the reference's Fortran unformatted layout (4-byte record markers, 4-byte
+ * integers, 8-byte reals; the layout output/getdata.m reads). */
+int ib_write_variables(IbCtx* ctx, const char* path);
+/* read_variables (variables.F90:807-913): restores omega, s, q, q0 (= q0p + q0r), rhs_old of
+ * every level, f, xb, yb and the torsional state from a file of the same grid and bodies, and
+ * sets the step counter to itime (the reference's istart), so the next ib_advance is step
+ * itime + 1.  Like the reference it ignores the file's dt and f_rdst.  Unlike the reference
+ * (timestepper.F90:76), a num_stat context factorises its Schur matrix on its first step
+ * whatever itime is. */
+int ib_read_variables(IbCtx* ctx, const char* path, int itime);
 /* ksp_iter, fsi_iter of the last step (timestepper.F90:365-366, 456) */
 int ib_get_counters(IbCtx* ctx, int* ksp_iter, int* fsi_iter);
 int ib_get_dims(IbCtx* ctx, int* nf, int* nbc, int* ns, int* nu, int* nv);

@@ -205,6 +205,9 @@ class IBOracle:
         self.q0x, self.q0y = self.frame_flux(0)
         self.f = np.zeros(self.nf)
         self.f_rdst = np.zeros(self.nf)
+        # velocity u_B of prescribed rigid-body motion (compute_rhs_prescribed, user.F90:137-174;
+        # its body is commented out in the reference: a host sets it with the positions)
+        self.ub = np.zeros(self.nf)
         self.itime = 0
         self.ksp_iter = 0
         self.fsi_iter = 0
@@ -734,7 +737,8 @@ class IBOracle:
             self.thetadd0 = self.thetadd.copy()
             while err >= p.fsi_tol and fsi_count <= 1000:
                 fsi_count += 1
-                rhsf = self.regT(qhx, qhy, self.compute_rhs())
+                # compute_rhs, then rhsf - delta u_B (timestepper.F90:323-331), then E q on top
+                rhsf = self.regT(qhx, qhy, self.compute_rhs() - self.delta * self.ub)
                 self.f, its, _ = self.gmres(rhsf, self.f, self.a_times)
                 self.ksp_iter += its
                 self.f_rdst = self.redistribute(self.f)
@@ -742,7 +746,7 @@ class IBOracle:
                 self.setup_reg()
             self.fsi_iter = fsi_count
         else:
-            rhsf = self.regT(qhx, qhy)
+            rhsf = self.regT(qhx, qhy, 0.0 - self.delta * self.ub)
             self.f = self.chol_solve(rhsf)
             self.f_rdst = self.redistribute(self.f)
         hx, hy = self.reg(self.f) if self.nf else (np.zeros_like(self.qx[0]), np.zeros_like(self.qy[0]))
@@ -750,6 +754,113 @@ class IBOracle:
         self.omega[0] = self.omega[0] - vort
         self.s, self.qx, self.qy = self.vort2flux(self.omega)
         return it
+
+
+# ---------------------------------------------------------------------------
+# Restart file output/dataRR_IIIIIII.var (variables.F90:709-913), a Fortran unformatted
+# sequential stream as output/getdata.m reads it: each WRITE is one record framed by its byte
+# length (4-byte integer) before and after; integers are 4 bytes, reals 8.
+# ---------------------------------------------------------------------------
+def _rec(buf: bytearray, arr) -> None:
+    b = np.ascontiguousarray(arr).tobytes()
+    n = np.int32(len(b)).tobytes()
+    buf += n + b + n
+
+
+def write_variables(o: "IBOracle", path) -> None:
+    """write_variables (variables.F90:709-803) of a one-rank run."""
+    m, n, L, nf = o.m, o.n, o.L, o.nf
+    i4 = lambda *v: np.array(v, dtype="<i4")
+    f8 = lambda *v: np.array(v, dtype="<f8")
+    buf = bytearray()
+    _rec(buf, i4(m, n, L, o.nb))
+    _rec(buf, f8(o.p.Re, o.p.dt, o.p.len, o.p.offsetx, o.p.offsety))
+    _rec(buf, i4(2, m, m - 1, 2, n, n - 1))
+    _rec(buf, i4(1, m + 1, m + 1, 1, n, n))
+    _rec(buf, i4(1, m, m, 1, n + 1, n + 1))
+    uv = o.p.motion
+    for k in range(L):
+        fac = o.delta * 2.0 ** k
+        px = np.full(o.q0x[k].shape, -fac * uv[0])
+        py = np.full(o.q0y[k].shape, -fac * uv[1])
+        for a in (o.omega[k], o.s[k], o.qx[k], px, o.q0x[k] - px, o.qy[k], py, o.q0y[k] - py):
+            _rec(buf, np.asarray(a, dtype="<f8"))
+    _rec(buf, np.stack(o.rhs_old).astype("<f8"))
+    _rec(buf, f8(uv[2] * o.p.dt * o.itime, uv[3], uv[4]))
+    _rec(buf, i4(nf, 1, nf))
+    for a in (o.f, o.xb, o.yb):
+        _rec(buf, np.asarray(a, dtype="<f8"))
+    _rec(buf, i4(len(o.tors)))
+    if o.tors:
+        _rec(buf, np.concatenate([o.theta, o.thetad, o.thetadd]).astype("<f8"))
+    _rec(buf, np.asarray(o.f_rdst, dtype="<f8"))
+    with open(path, "wb") as fh:
+        fh.write(bytes(buf))
+
+
+def read_records(path) -> list:
+    """The records of a Fortran unformatted sequential file, as raw bytes."""
+    data = open(path, "rb").read()
+    out, pos = [], 0
+    while pos < len(data):
+        (nb,) = np.frombuffer(data, "<i4", 1, pos)
+        body = data[pos + 4:pos + 4 + nb]
+        (ne,) = np.frombuffer(data, "<i4", 1, pos + 4 + nb)
+        if ne != nb or len(body) != nb:
+            raise ValueError(f"bad record framing at byte {pos}")
+        out.append(body)
+        pos += 8 + nb
+    return out
+
+
+def read_variables(path) -> dict:
+    """Parse a restart file the way output/getdata.m does (one rank)."""
+    r = read_records(path)
+    i4 = lambda b: np.frombuffer(b, "<i4")
+    f8 = lambda b: np.frombuffer(b, "<f8")
+    m, n, L, nb = (int(v) for v in i4(r[0]))
+    d = dict(m=m, n=n, mgridlev=L, nb=nb)
+    d["Re"], d["dt"], d["len"], d["offsetx"], d["offsety"] = (float(v) for v in f8(r[1]))
+    d["ranges"] = [tuple(int(v) for v in i4(r[q])) for q in (2, 3, 4)]
+    names = ("omega", "s", "qx", "q0px", "q0rx", "qy", "q0py", "q0ry")
+    shapes = dict(omega=(n - 1, m - 1), s=(n - 1, m - 1), qx=(n, m + 1), q0px=(n, m + 1), q0rx=(n, m + 1),
+                  qy=(n + 1, m), q0py=(n + 1, m), q0ry=(n + 1, m))
+    i = 5
+    for nm in names:
+        d[nm] = []
+    for k in range(L):
+        for nm in names:
+            d[nm].append(f8(r[i]).reshape(shapes[nm]).copy())
+            i += 1
+    d["rhs_old"] = list(f8(r[i]).reshape(L, n - 1, m - 1).copy()); i += 1
+    d["rot_angle"], d["rox"], d["roy"] = (float(v) for v in f8(r[i])); i += 1
+    d["xfm"], d["xfi"], d["xfe"] = (int(v) for v in i4(r[i])); i += 1
+    d["f"] = f8(r[i]).copy(); d["xb"] = f8(r[i + 1]).copy(); d["yb"] = f8(r[i + 2]).copy(); i += 3
+    d["mt_body"] = int(i4(r[i])[0]); i += 1
+    if d["mt_body"] > 0:
+        t = f8(r[i]).reshape(3, d["mt_body"]); i += 1
+        d["theta"], d["thetad"], d["thetadd"] = t[0].copy(), t[1].copy(), t[2].copy()
+    d["f_rdst"] = f8(r[i]).copy() if i < len(r) else None
+    d["nrecords"] = len(r)
+    return d
+
+
+def restore(o: "IBOracle", d: dict, itime: int) -> None:
+    """read_variables (variables.F90:807-913) into an oracle of the same grid and bodies:
+    q0 = q0p + q0r, E rebuilt at the positions read, step counter istart = itime."""
+    if (d["m"], d["n"], d["mgridlev"], d["nb"]) != (o.m, o.n, o.L, o.nb):
+        raise ValueError("grid or bodies differ")
+    for k in range(o.L):
+        o.omega[k] = d["omega"][k].copy(); o.s[k] = d["s"][k].copy()
+        o.qx[k] = d["qx"][k].copy(); o.qy[k] = d["qy"][k].copy()
+        o.q0x[k] = d["q0px"][k] + d["q0rx"][k]; o.q0y[k] = d["q0py"][k] + d["q0ry"][k]
+        o.rhs_old[k] = d["rhs_old"][k].copy()
+    o.f = d["f"].copy(); o.xb = d["xb"].copy(); o.yb = d["yb"].copy()
+    if o.tors:
+        o.theta = d["theta"].copy(); o.thetad = d["thetad"].copy(); o.thetadd = d["thetadd"].copy()
+    o.itime = itime
+    if o.nf:
+        o.setup_reg()
 
 
 # ---------------------------------------------------------------------------
