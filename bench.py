@@ -497,6 +497,8 @@ def run_gpu(args, world, rank, local):
             "note": "same_algorithm: the GPU with the matrix-free Schur operator the port runs"}
     if rank == 0 and world == 1 and not args.no_c1:
         result["workloads"] = {C1_WORKLOAD: _c1_workload(args)}
+    if rank == 0 and world == 1 and args.ensemble > 0:
+        result.setdefault("workloads", {})["ensemble"] = _ensemble(args)
     if rank == 0:
         print(json.dumps(result))
     if world > 1:
@@ -544,6 +546,66 @@ def _matrix_free_rate(p, bodies, args):
             "schur_matvecs_per_step": (mv1 - mv0) / args.steps}
 
 
+def run_ensemble_only(nsim, steps, warmup):
+    """The batched ensemble (geometry.config_ensemble): nsim simulations with uneven grids and
+    bodies, advanced by ib_batch_advance for `warmup` then `steps` batch steps, and the same
+    simulations advanced one at a time through ib_advance for `steps` steps each (the plain GPU
+    path run one simulation at a time).  Host wall clock around synchronised calls (every call
+    returns with its work complete).  Prints one JSON object."""
+    import torch
+    from ib_parallel_gb300 import geometry as GEO
+    from ib_parallel_gb300 import ibgpu as G
+    torch.cuda.set_device(0)
+    runs = GEO.config_ensemble(nsim)
+    t0 = time.perf_counter()
+    batch = G.Batch(runs)
+    t_create = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(warmup):
+        batch.advance()
+    t_warm = time.perf_counter() - t0
+    launches0 = G.launch_count()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        batch.advance()
+    t_batch = time.perf_counter() - t0
+    launches = G.launch_count() - launches0
+    t0 = time.perf_counter()
+    for s in batch.sims:
+        for _ in range(steps):
+            s.advance()
+    t_seq = time.perf_counter() - t0
+    grids = {}
+    for p, b in runs:
+        grids[f"{p.m}x{p.n}"] = grids.get(f"{p.m}x{p.n}", 0) + 1
+    out = {"workload": "ensemble", "metric": "sim-steps/s, batched ensemble FP64", "nsim": nsim, "steps": steps,
+           "warmup": warmup, "value": nsim * steps / t_batch, "unit": "sim-steps/s",
+           "sequential": {"value": nsim * steps / t_seq, "unit": "sim-steps/s",
+                          "note": "the same simulations, one at a time through ib_advance"},
+           "batch_over_sequential": t_seq / t_batch, "gpu_launches_per_batch_step": launches / steps,
+           "create_s": t_create, "warmup_s": t_warm, "grids": grids,
+           "body_points": [min(len(b[0].x) for _, b in runs), max(len(b[0].x) for _, b in runs)],
+           "config": "seeded per simulation: Re U[100,500], mass ratio logU[0.1,2], stiffness logU[1e-4,1e-2], "
+                     "incidence U[0,20] deg, grid U{256x128,384x192,512x256}, 3 levels, dt 2e-3",
+           "timing": "host wall clock around synchronised calls, CUDA_DEVICE_MAX_CONNECTIONS=" +
+                     os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "default")}
+    batch.close()
+    print(json.dumps(out))
+    return 0
+
+
+def _ensemble(args):
+    """Runs the ensemble leg in its own process, with 32 hardware work queues so that the
+    simulations' streams run side by side (the variable must be set before CUDA starts)."""
+    env = dict(os.environ, CUDA_DEVICE_MAX_CONNECTIONS="32")
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--ensemble-only", str(args.ensemble),
+           "--steps", str(max(3, min(args.steps, 10))), "--warmup", "3"]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=1200)
+    if r.returncode != 0:
+        return {"error": (r.stderr or r.stdout)[-400:]}
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
 def run_roofline_only():
     """The x pass of the roofline alone, 20 launches over cold inputs inside a profiler window
     (ncu --profile-from-start off captures exactly these launches)."""
@@ -587,6 +649,9 @@ def main():
                     help="run the timed steps with per-phase timing on, so that the FSI iterations run from the "
                          "host and each of their kernels is a separate launch (a profiler lists kernels inside "
                          "the device loop's graph node only as the graph)")
+    ap.add_argument("--ensemble", type=int, default=256,
+                    help="simulations of the batched-ensemble leg (0: skip)")
+    ap.add_argument("--ensemble-only", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--roofline-only", action="store_true",
                     help="only time the single x pass of the roofline (inside a profiler window: the command "
                          "the ncu traffic capture of that pass runs)")
@@ -594,6 +659,8 @@ def main():
     world, rank, local = _dist()
     if args.roofline_only:
         return run_roofline_only()
+    if args.ensemble_only:
+        return run_ensemble_only(args.ensemble_only, args.steps, args.warmup)
     if args.impl == "reference":
         return run_reference(args, world, rank)
     return run_gpu(args, world, rank, local)

@@ -1,6 +1,7 @@
 // extern "C" entry points of include/ib_gpu.h.
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "ctx.cuh"
 
@@ -19,6 +20,7 @@ void set_last_error(const char* msg) { g_err = msg; }
 
 struct IbCtx {
   Ctx* c;
+  bool borrowed = false;   // a batch's simulation (ib_batch_context): the batch owns it
 };
 
 namespace {
@@ -106,6 +108,7 @@ int ib_create(const IbParams* p, const IbBody* bodies, int nbody, IbCtx** out) {
 
 int ib_destroy(IbCtx* h) {
   if (!h) return IB_OK;
+  if (h->borrowed) return fail(IB_ERR_ARG, "the context belongs to a batch: ib_batch_destroy frees it");
   ib::ctx_destroy(h->c);
   delete h;
   return IB_OK;
@@ -250,6 +253,82 @@ int ib_read_variables(IbCtx* h, const char* path, int itime) {
   std::string msg;
   int rc = ib::op_read_variables(c, path, itime, &msg);
   return rc == IB_OK ? IB_OK : fail(rc, ("read_variables: " + msg).c_str());
+}
+
+// ---- batches of independent simulations
+struct IbBatch {
+  std::vector<IbCtx*> sims;
+  std::vector<int> rc;
+};
+
+int ib_batch_create(const IbParams* params, const IbBody* bodies, const int* nbody, int nsim, IbBatch** out) {
+  if (!params || !nbody || !out || nsim < 1) return fail(IB_ERR_ARG, "null argument or empty batch");
+  IbBatch* b = new IbBatch();
+  int off = 0;
+  for (int i = 0; i < nsim; ++i) {
+    if (nbody[i] < 0 || (nbody[i] > 0 && !bodies)) {
+      ib_batch_destroy(b);
+      return fail(IB_ERR_ARG, "bad body count");
+    }
+    std::string msg;
+    Ctx* c = nullptr;
+    int rc = ib::ctx_create(&params[i], nbody[i] ? bodies + off : nullptr, nbody[i], &c, &msg);
+    if (rc != IB_OK) {
+      ib_batch_destroy(b);
+      return fail(rc, ("batch simulation " + std::to_string(i) + ": " + msg).c_str());
+    }
+    b->sims.push_back(new IbCtx{c, true});
+    off += nbody[i];
+  }
+  b->rc.assign(nsim, IB_OK);
+  *out = b;
+  return IB_OK;
+}
+
+int ib_batch_destroy(IbBatch* b) {
+  if (!b) return IB_OK;
+  for (IbCtx* h : b->sims) {
+    ib::ctx_destroy(h->c);
+    delete h;
+  }
+  delete b;
+  return IB_OK;
+}
+
+int ib_batch_size(IbBatch* b, int* nsim) {
+  if (!b || !nsim) return fail(IB_ERR_ARG, "null argument");
+  *nsim = (int)b->sims.size();
+  return IB_OK;
+}
+
+int ib_batch_context(IbBatch* b, int i, IbCtx** ctx) {
+  if (!b || !ctx || i < 0 || i >= (int)b->sims.size()) return fail(IB_ERR_ARG, "bad batch index");
+  *ctx = b->sims[i];
+  return IB_OK;
+}
+
+int ib_batch_advance(IbBatch* b, int* status) {
+  if (!b) return fail(IB_ERR_ARG, "null batch");
+  const int n = (int)b->sims.size();
+  // every simulation's predictor, vort2flux and device FSI loop go on the GPU first, then each
+  // simulation's counters are read and its correction launched, then each step is finished:
+  // the host waits on a simulation only after the other simulations' work is queued
+  for (int i = 0; i < n; ++i) b->rc[i] = ib::op_advance_begin(b->sims[i]->c);
+  for (int i = 0; i < n; ++i)
+    if (b->rc[i] == IB_OK) b->rc[i] = ib::op_advance_end(b->sims[i]->c);
+  for (int i = 0; i < n; ++i)
+    if (b->rc[i] == IB_OK) b->rc[i] = ib::op_advance_finish(b->sims[i]->c);
+  int first = IB_OK, where = -1;
+  for (int i = 0; i < n; ++i) {
+    if (status) status[i] = b->rc[i];
+    if (b->rc[i] != IB_OK && first == IB_OK) { first = b->rc[i]; where = i; }
+  }
+  if (first != IB_OK) {
+    cudaGetLastError();
+    return fail(first, ("batch advance: simulation " + std::to_string(where) + " returned " +
+                        std::to_string(first) + " (per-simulation codes in status)").c_str());
+  }
+  return IB_OK;
 }
 
 int ib_get_counters(IbCtx* h, int* ksp_iter, int* fsi_iter) {

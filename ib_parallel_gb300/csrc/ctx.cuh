@@ -231,6 +231,8 @@ struct Ctx {
   // if none failed), and the FSI error when the loop stopped at fsi_max_it (else 0)
   int gmres_reason = 0;
   double fsi_err_capped = 0.0;
+  // the parts of a step begun and not yet ended or finished (op_advance_begin/end/finish)
+  bool loop_pending = false, end_pending = false, finish_pending = false;
 
   // work counters (host side): Schur matvecs and DST passes by kind
   long long n_matvec = 0;
@@ -291,6 +293,10 @@ int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
 // checkpoint.cu: the reference's restart file (variables.F90:709-913)
 int op_write_variables(Ctx* c, const char* path, std::string* msg);
+// solver.cu: a time step in three parts (op_advance runs them in a row)
+int op_advance_begin(Ctx* c);
+int op_advance_end(Ctx* c);
+int op_advance_finish(Ctx* c);
 int op_read_variables(Ctx* c, const char* path, int itime, std::string* msg);
 // graph helpers (solver.cu): a while node after the capture position of st (its body graph
 // returned), the graph st is capturing, and programmatic kernel-to-kernel edges

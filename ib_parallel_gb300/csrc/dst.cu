@@ -881,9 +881,7 @@ int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, con
                    const double* post_add, double post_scale, double* out, cudaStream_t st) {
   const int N = px.N;
   const size_t smem = 2 * sizeof(double) * (size_t)N;
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_dst_bc_modes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return IB_ERR_CUDA;
+  if (allow_dyn_smem(k_dst_bc_modes, smem) != cudaSuccess) return IB_ERR_CUDA;
   const int nEdge = cdiv(N, 8);
   const int nblk = nEdge + cdiv(std::max(0, g.nsy - 2), kRowsPerCta);
   DstDev d = to_dev(px);
@@ -971,10 +969,7 @@ static int launch_cfg(K kern, size_t smem) {
   if (cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
       cudaSuccess)
     return IB_ERR_CUDA;
-  if (smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return IB_ERR_CUDA;
-  }
+  if (allow_dyn_smem(kern, smem) != cudaSuccess) return IB_ERR_CUDA;
   return IB_OK;
 }
 

@@ -417,9 +417,7 @@ int launch_cholesky(int n, double* A, int* d_err, cudaStream_t st) {
 }
 int launch_chol_solve(int n, const double* Lf, const double* b, double* x, cudaStream_t st) {
   size_t smem = sizeof(double) * n;
-  if (smem > 48 * 1024) {
-    IB_CUDA_CHECK(cudaFuncSetAttribute(k_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  }
+  IB_CUDA_CHECK(allow_dyn_smem(k_chol_solve, smem));
   count_launch();
   k_chol_solve<<<1, 512, smem, st>>>(n, Lf, b, x);
   IB_CUDA_CHECK(cudaGetLastError());
@@ -852,7 +850,7 @@ int launch_gmres_fused(const GmresDev& G, FusedPlan* plan, const double* At, con
       bytes = 8 * cs.base();
       if (bytes > limit) return IB_ERR_ARG;
     }
-    IB_CUDA_CHECK(cudaFuncSetAttribute(k_gmres_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    IB_CUDA_CHECK(allow_dyn_smem(k_gmres_cluster, bytes));
     // the cluster must fit on the device as launched
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(kSlices);

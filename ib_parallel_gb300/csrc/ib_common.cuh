@@ -12,6 +12,9 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #define IB_OK 0
 #define IB_ERR_ARG 1
@@ -119,3 +122,36 @@ long long launch_count();
       return IB_ERR_CUDA;                                                       \
     }                                                                           \
   } while (0)
+
+namespace ib {
+
+// Lets kernel `kern` take `bytes` of dynamic shared memory.  The limit is an attribute of the
+// function, shared by every context in the process, and captured graphs launch with the sizes
+// they were captured with: so it is only ever raised, once, to the most the device allows (the
+// opt-in maximum less the kernel's static shared memory), never set to one context's size.
+template <typename K>
+inline cudaError_t allow_dyn_smem(K kern, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> raised;   // (device, kernel) -> limit set
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const auto key = std::make_pair(dev, reinterpret_cast<const void*>(kern));
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = raised.find(key);
+  if (it != raised.end()) return (size_t)it->second >= bytes ? cudaSuccess : cudaErrorInvalidValue;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, kern);
+  if (e != cudaSuccess) return e;
+  const int lim = optin - (int)fa.sharedSizeBytes;
+  if (lim < 0 || (size_t)lim < bytes) return cudaErrorInvalidValue;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) raised[key] = lim;
+  return e;
+}
+
+}  // namespace ib

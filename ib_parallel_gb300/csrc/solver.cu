@@ -295,7 +295,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->stage_n = stage_n;
   for (int i = 0; i < 8; ++i) c->stage[i] = P.take<double>(stage_n);
   if (!c->stage[7] || !c->d_err) { *msg = "internal pool overflow"; ctx_destroy(c); return IB_ERR_NOMEM; }
-  if (cudaMallocHost(&c->h_ist, 8 * sizeof(int)) != cudaSuccess ||
+  if (cudaMallocHost(&c->h_ist, 16 * sizeof(int)) != cudaSuccess ||   // [12]: the step's error word
       cudaMallocHost(&c->h_scal, 4 * sizeof(double)) != cudaSuccess) {
     *msg = "pinned allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM;
   }
@@ -1319,8 +1319,20 @@ static int op_predict_levels(Ctx* c, bool seed_rhs_old) {
   return dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx_batch, st);
 }
 
-// timestepper.F90:18-556
+// timestepper.F90:18-556, in three parts so that a batch of contexts can put every context's
+// work on the GPU before it waits for any (op_batch_advance):
+//   begin:  predictor, vort2flux and, when the FSI iterations can run on the device, their
+//           captured loop, launched without waiting;
+//   end:    the loop's counters (the first wait), the host FSI iterations when needed, the
+//           correction, and the error word's copy, launched without waiting;
+//   finish: the error word and the solvers' status (the second wait).
 int op_advance(Ctx* c) {
+  RC(op_advance_begin(c));
+  RC(op_advance_end(c));
+  return op_advance_finish(c);
+}
+
+int op_advance_begin(Ctx* c) {
   const GridDims& g = c->g;
   const int L = c->L;
   const IbParams& p = c->p;
@@ -1352,8 +1364,6 @@ int op_advance(Ctx* c) {
     if (!p.num_stat) {
       if (it == 1) RC(launch_tors_initial_acc(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, st));
       RC(launch_tors_save(c->nt, c->ts, st));
-      double err = 10.0;
-      int fsi_count = 0;
       c->ksp_iter = 0;
       c->gmres_reason = 0;
       const bool moved = c->nt > 0;
@@ -1370,6 +1380,31 @@ int op_advance(Ctx* c) {
           IB_CUDA_CHECK(cudaGraphLaunch(c->graph_fsi_loop.exec, st));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st));
+          c->loop_pending = true;
+        }
+      }
+    }
+  }
+  c->end_pending = true;
+  return IB_OK;
+}
+
+int op_advance_end(Ctx* c) {
+  if (!c->end_pending) return IB_ERR_STATE;
+  c->end_pending = false;
+  const GridDims& g = c->g;
+  const int L = c->L;
+  const IbParams& p = c->p;
+  cudaStream_t st = c->st;
+  if (c->nf > 0) {
+    if (!p.num_stat) {
+      double err = 10.0;
+      int fsi_count = 0;
+      const bool moved = c->nt > 0;
+      {
+        Influence& I = c->inf;
+        if (c->loop_pending) {
+          c->loop_pending = false;
           IB_CUDA_CHECK(cudaStreamSynchronize(st));
           if (c->step_prof) {
             step_mark(c, 3);
@@ -1525,7 +1560,17 @@ int op_advance(Ctx* c) {
     return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true);
   }));
   step_mark(c, 9);
-  int rc = check_err(c);
+  IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist + 12, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  c->finish_pending = true;
+  return IB_OK;
+}
+
+int op_advance_finish(Ctx* c) {
+  if (!c->finish_pending) return IB_ERR_STATE;
+  c->finish_pending = false;
+  IB_CUDA_CHECK(cudaStreamSynchronize(c->st));
+  int rc = c->h_ist[12];
+  if (rc) IB_CUDA_CHECK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
   // the step is complete either way; a Krylov solve that stopped without converging, or an
   // FSI loop that stopped at its cap, is reported once the state is consistent
   if (rc == IB_OK && c->gmres_reason < 0) rc = IB_ERR_GMRES;

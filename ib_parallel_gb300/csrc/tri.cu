@@ -348,9 +348,7 @@ template <int S>
 static int launch_tri_reg(const TriOp& op, const double* F, double* U, int ld, int Mb, int threads, const TriBc& bc,
                           cudaStream_t st) {
   const size_t smem = tri_reg_smem(op, Mb);
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_tri_reg<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return IB_ERR_CUDA;
+  if (allow_dyn_smem(k_tri_reg<S>, smem) != cudaSuccess) return IB_ERR_CUDA;
   count_launch();
   k_tri_reg<S><<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb, bc);
   IB_CUDA_CHECK(cudaGetLastError());
@@ -383,10 +381,7 @@ int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaun
     }
   }
   size_t smem = tri_smem(op, Mb);
-  if (smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(k_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return IB_ERR_CUDA;
-  }
+  if (allow_dyn_smem(k_tri, smem) != cudaSuccess) return IB_ERR_CUDA;
   count_launch();
   k_tri<<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb, bc);
   IB_CUDA_CHECK(cudaGetLastError());

@@ -239,3 +239,31 @@ def pitching_motion(x_ref: np.ndarray, y_ref: np.ndarray, t: float, amp_deg: flo
     yb = np.r_[py, py]
     ub = np.r_[ux, uy]
     return xb, yb, ub
+
+
+def config_ensemble(nsim: int = 256, seed0: int = 0) -> list:
+    """The batched-ensemble workload: nsim independent hinged-plate simulations, simulation s
+    drawing from default_rng(seed0 + s): Re uniform in [100, 500], mass ratio log-uniform in
+    [0.1, 2] (itheta = mass ratio x length^3 / 3 about the hinge), stiffness log-uniform in
+    [1e-4, 1e-2], incidence uniform in [0, 20] degrees, fine grid one of 256x128, 384x192,
+    512x256 on [-1,7]x[-2,2], 3 levels, dt 2e-3, GMRES and FSI tolerances 1e-10.  The plate length
+    is drawn in [0.75, 1.25] and its points are two grid spacings apart (17 to 41 points by
+    grid and length): closer points make the Schur operator singular (tests/
+    test_conditioning_cpu.py), so the 50-150 points of a flexible beam's nodes are not used."""
+    grids = [(256, 128), (384, 192), (512, 256)]
+    runs = []
+    for s in range(nsim):
+        rng = np.random.default_rng(seed0 + s)
+        Re = rng.uniform(100.0, 500.0)
+        mass_ratio = math.exp(rng.uniform(math.log(0.1), math.log(2.0)))
+        stiffness = math.exp(rng.uniform(math.log(1e-4), math.log(1e-2)))
+        incidence = rng.uniform(0.0, 20.0)
+        m, n = grids[int(rng.integers(0, 3))]
+        length = rng.uniform(0.75, 1.25)
+        delta = 8.0 / m
+        npts = int(round(length / (2.0 * delta))) + 1
+        p = Params(m=m, n=n, mgridlev=3, dt=2e-3, Re=Re, len=8.0, offsetx=1.0, offsety=2.0, fsi_tol=1e-10,
+                   atol=1e-10, rtol=1e-10, autotune=False)
+        body = torsional_plate(npts, length, -incidence, itheta=mass_ratio * length ** 3 / 3.0, ktheta=stiffness)
+        runs.append((p, [body]))
+    return runs

@@ -41,6 +41,7 @@ EXPORTS = [
     "ib_launch_count", "ib_time_pass", "ib_profile_schur", "ib_ctci_static",
     "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile", "ib_get_launch_shapes",
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
+    "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
 ]
 
 
@@ -124,6 +125,10 @@ def load(path: Optional[os.PathLike] = None):
         "ib_read_namelist": ([C.c_char_p, C.POINTER(IbParams), C.POINTER(IbRunControl)], C.c_int),
         "ib_read_body": ([C.c_char_p, C.POINTER(IbBody), D, D, C.c_int], C.c_int),
         "ib_count_bodies": ([C.c_char_p, I], C.c_int),
+        "ib_batch_create": ([C.POINTER(IbParams), C.POINTER(IbBody), I, C.c_int, C.POINTER(P)], C.c_int),
+        "ib_batch_destroy": ([P], C.c_int), "ib_batch_size": ([P, I], C.c_int),
+        "ib_batch_context": ([P, C.c_int, C.POINTER(P)], C.c_int),
+        "ib_batch_advance": ([P, I], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -225,30 +230,40 @@ class Params:
         return p
 
 
+def _c_bodies(bodies: Sequence[Body], keep: list):
+    """A ctypes IbBody array of the bodies (their coordinate arrays appended to keep)."""
+    cb = (IbBody * max(1, len(bodies)))()
+    for i, b in enumerate(bodies):
+        x = np.ascontiguousarray(b.x, dtype=np.float64)
+        y = np.ascontiguousarray(b.y, dtype=np.float64)
+        keep += [x, y]
+        cb[i].npts = len(x)
+        cb[i].fam = int(b.fam)
+        cb[i].gamma0_deg = float(b.gamma0_deg)
+        cb[i].alpha0_deg = float(b.alpha0_deg)
+        cb[i].itheta = float(b.itheta)
+        cb[i].ktheta = float(b.ktheta)
+        cb[i].ctheta = float(b.ctheta)
+        cb[i].x = x.ctypes.data_as(C.POINTER(C.c_double))
+        cb[i].y = y.ctypes.data_as(C.POINTER(C.c_double))
+    return cb
+
+
 class Simulation:
     """One device-resident simulation (an ``IbCtx``)."""
 
-    def __init__(self, params: Params, bodies: Sequence[Body] = ()):
+    def __init__(self, params: Params, bodies: Sequence[Body] = (), _handle=None):
         self.lib = load()
         self.params = params
         self._keep = []
-        cb = (IbBody * max(1, len(bodies)))()
-        for i, b in enumerate(bodies):
-            x = np.ascontiguousarray(b.x, dtype=np.float64)
-            y = np.ascontiguousarray(b.y, dtype=np.float64)
-            self._keep += [x, y]
-            cb[i].npts = len(x)
-            cb[i].fam = int(b.fam)
-            cb[i].gamma0_deg = float(b.gamma0_deg)
-            cb[i].alpha0_deg = float(b.alpha0_deg)
-            cb[i].itheta = float(b.itheta)
-            cb[i].ktheta = float(b.ktheta)
-            cb[i].ctheta = float(b.ctheta)
-            cb[i].x = x.ctypes.data_as(C.POINTER(C.c_double))
-            cb[i].y = y.ctypes.data_as(C.POINTER(C.c_double))
-        h = C.c_void_p()
-        cp = params.to_c()
-        _check(self.lib.ib_create(C.byref(cp), cb, len(bodies), C.byref(h)), "ib_create")
+        self._owned = _handle is None
+        if _handle is None:
+            cb = _c_bodies(bodies, self._keep)
+            h = C.c_void_p()
+            cp = params.to_c()
+            _check(self.lib.ib_create(C.byref(cp), cb, len(bodies), C.byref(h)), "ib_create")
+        else:
+            h = _handle
         self.h = h
         self.nbody = len(bodies)
         self.ntors = sum(1 for b in bodies if b.fam == 2)
@@ -261,7 +276,8 @@ class Simulation:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.ib_destroy(self.h)
+            if self._owned:
+                self.lib.ib_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -507,3 +523,49 @@ class Simulation:
                                        C.byref(its)), "ib_schur_solve")
         return f, its.value
 
+
+
+class Batch:
+    """Independent simulations advanced together (``ib_batch_*``): each keeps its own grid,
+    bodies, device memory and stream, and a batch step queues every simulation's work before
+    waiting on any.  ``sims[i]`` is a Simulation view of simulation i (owned by the batch)."""
+
+    def __init__(self, runs: Sequence[tuple]):
+        self.lib = load()
+        self._keep = []
+        n = len(runs)
+        cps = (IbParams * n)()
+        all_bodies = [b for _, bodies in runs for b in bodies]
+        cb = _c_bodies(all_bodies, self._keep)
+        nb = (C.c_int * n)(*[len(bodies) for _, bodies in runs])
+        for i, (p, _) in enumerate(runs):
+            cps[i] = p.to_c()
+        h = C.c_void_p()
+        _check(self.lib.ib_batch_create(cps, cb, nb, n, C.byref(h)), "ib_batch_create")
+        self.h = h
+        self.status = (C.c_int * n)()
+        self.sims = []
+        for i, (p, bodies) in enumerate(runs):
+            ch = C.c_void_p()
+            _check(self.lib.ib_batch_context(self.h, i, C.byref(ch)), "ib_batch_context")
+            self.sims.append(Simulation(p, bodies, _handle=ch))
+
+    def advance(self, check: bool = True) -> list:
+        """One step of every simulation; returns the per-simulation status codes."""
+        rc = self.lib.ib_batch_advance(self.h, self.status)
+        if check:
+            _check(rc, "ib_batch_advance")
+        return list(self.status)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for s in self.sims:
+                s.h = None
+            self.lib.ib_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -142,6 +142,27 @@ int ib_read_variables(IbCtx* ctx, const char* path, int itime);
 int ib_get_counters(IbCtx* ctx, int* ksp_iter, int* fsi_iter);
 int ib_get_dims(IbCtx* ctx, int* nf, int* nbc, int* ns, int* nu, int* nv);
 
+/* ---- batches: many independent simulations advanced together (no counterpart in the
+ * reference, which runs one simulation per job) ---- */
+typedef struct IbBatch IbBatch;
+/* nsim simulations, each with its own grid and bodies: params[i], and nbody[i] bodies taken in
+ * order from `bodies` (the bodies of simulation 0, then of 1, ...).  Each is a context of its
+ * own (its own device memory and stream); set autotune = 0 for large batches, since tuning
+ * times every simulation's launch shapes at creation.  For the simulations' work to overlap on
+ * the GPU, give the process CUDA_DEVICE_MAX_CONNECTIONS=32 before CUDA starts. */
+int ib_batch_create(const IbParams* params, const IbBody* bodies, const int* nbody, int nsim, IbBatch** out);
+int ib_batch_destroy(IbBatch* batch);
+int ib_batch_size(IbBatch* batch, int* nsim);
+/* simulation i as a context handle, for every per-context entry point (fields, forces,
+ * counters, restart files); it stays the batch's: ib_destroy refuses it */
+int ib_batch_context(IbBatch* batch, int i, IbCtx** ctx);
+/* one time step of every simulation (timestepper.F90:18-556 each), with the same results as
+ * ib_advance on each alone: each simulation's predictor, vort2flux and device FSI loop are
+ * queued before the host waits on any, then their corrections, so the simulations' kernels run
+ * side by side.  status[nsim] (may be NULL) gets each simulation's ib_advance code; the call
+ * returns the first nonzero one (or IB_OK). */
+int ib_batch_advance(IbBatch* batch, int* status);
+
 /* ---- operator level (grid level 'level' is 0-based; tables of that level) ---- */
 /* operators_fluid.F90:553-587; qx, qy are the total fluxes q+q0 */
 int ib_nonlinear(IbCtx* ctx, const double* omega, const double* qx, const double* qy, const double* bc,
