@@ -331,6 +331,27 @@ int ib_batch_advance(IbBatch* b, int* status) {
   return IB_OK;
 }
 
+int ib_calculate_pressure(IbCtx* h, double* p) {
+  CTX_OR_FAIL(h);
+  if (!p) return fail(IB_ERR_ARG, "null output");
+  int rc = ib::op_pressure(c);
+  if (rc != IB_OK) return op_result(rc, "calculate_pressure failed");
+  const size_t cells = (size_t)c->g.m * c->g.n;
+  for (int k = 0; k < c->L; ++k)
+    if (cudaMemcpyAsync(p + (size_t)k * cells, c->pres.p[k], 8 * cells, cudaMemcpyDefault, c->st) != cudaSuccess)
+      return fail(IB_ERR_CUDA, "copy failed");
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "copy failed");
+  return IB_OK;
+}
+
+int ib_write_pressure(IbCtx* h, const char* path) {
+  CTX_OR_FAIL(h);
+  if (!path) return fail(IB_ERR_ARG, "null path");
+  std::string msg;
+  int rc = ib::op_write_pressure(c, path, &msg);
+  return rc == IB_OK ? IB_OK : fail(rc, ("write_pressure: " + msg).c_str());
+}
+
 int ib_get_counters(IbCtx* h, int* ksp_iter, int* fsi_iter) {
   CTX_OR_FAIL(h);
   if (ksp_iter) *ksp_iter = c->ksp_iter;
@@ -601,7 +622,8 @@ int ib_measure_fp64_peak(double* tflops) {
 
 int ib_time_pass(IbCtx* h, int kind, int reps, double* avg_ms) {
   CTX_OR_FAIL(h);
-  if (!avg_ms || reps <= 0 || kind < 0 || kind > 1) return fail(IB_ERR_ARG, "bad argument");
+  if (!avg_ms || reps <= 0 || kind < 0 || kind > 3) return fail(IB_ERR_ARG, "bad argument");
+  if (kind >= 2) return op_result(ib::op_time_pressure_transform(c, kind == 2, reps, avg_ms), "time_pass failed");
   return op_result(ib::op_time_pass(c, kind, reps, avg_ms), "time_pass failed");
 }
 

@@ -255,4 +255,26 @@ int op_read_variables(Ctx* c, const char* path, int itime, std::string* msg) {
   return IB_OK;
 }
 
+// write_pressure (operators_pressure.F90:857-879): output/pressureRR_IIIIIII.var of one rank, the
+// index range xpi, xpe, xpm, ypi, ype, ypm (1, m, m, 1, n, n) and then every level's m x n cells
+int op_write_pressure(Ctx* c, const char* path, std::string* msg) {
+  const GridDims& g = c->g;
+  if (!c->pres.computed) { *msg = "no pressure computed (ib_calculate_pressure first)"; return IB_ERR_STATE; }
+  FILE* f = std::fopen(path, "wb");
+  if (!f) { *msg = std::string("cannot open ") + path + " for writing"; return IB_ERR_ARG; }
+  RecordWriter w;
+  w.f = f;
+  w.vals<int32_t>({1, g.m, g.m, 1, g.n, g.n});
+  std::vector<double> a;
+  int rc = IB_OK;
+  for (int k = 0; k < c->L && rc == IB_OK; ++k) {
+    rc = copy_d2h(c, a, c->pres.p[k], (size_t)g.m * g.n);
+    if (rc == IB_OK) w.rec(a.data(), 8 * a.size());
+  }
+  const bool closed = std::fclose(f) == 0;
+  if (rc != IB_OK) { *msg = "device copy failed"; return rc; }
+  if (!w.ok || !closed) { *msg = std::string("write to ") + path + " failed"; return IB_ERR_ARG; }
+  return IB_OK;
+}
+
 }  // namespace ib

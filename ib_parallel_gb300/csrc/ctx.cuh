@@ -39,6 +39,17 @@ struct DevPool {
 // vertex u, i.e. the map the matrix-free operator applies between rot and E curl.  Each
 // unknown k owns the 8 x 8 vertex patch P_k = rot(E^T e_k) (values and band indices); the
 // fluid Schur matrix is S_f = P^T K P (curl is the transpose of rot).
+// Pressure recovery (pressure.cu): tables and fields, allocated on the first call.
+struct PressureOp {
+  bool ready = false, computed = false;
+  double* mem = nullptr;
+  double* W = nullptr;          // m x m DST-I matrix of the cell grid's x direction
+  TriOp tri;                    // per-mode (lx(k) + T_y)^-1 of the n cell rows
+  std::vector<double*> rhs, p, oqx, oqy, nlx, nly;   // per level
+  double *y = nullptr, *tmp = nullptr, *hx = nullptr, *hy = nullptr, *fdt = nullptr;
+  double *ubc = nullptr, *vbc = nullptr, *ring = nullptr;
+};
+
 // The buffers and the stream one application of the Schur operator's fluid part works in
 // (schur_fluid): the context's own, or one of the band build's concurrent sets.
 struct SchurScratch {
@@ -176,6 +187,7 @@ struct Ctx {
   // velocity u_B; once set, -delta u_B joins the right-hand side of every Schur solve
   double* ub = nullptr;
   bool ub_on = false;
+  PressureOp pres;
   int *comp = nullptr, *bid = nullptr;
   RegDev reg{};
   TorsBody* tb = nullptr;
@@ -293,6 +305,11 @@ int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
 // checkpoint.cu: the reference's restart file (variables.F90:709-913)
 int op_write_variables(Ctx* c, const char* path, std::string* msg);
+// pressure.cu: calculate_pressure (operators_pressure.F90:110-437) into pres.p
+int op_pressure(Ctx* c);
+void pressure_free(Ctx* c);
+int op_time_pressure_transform(Ctx* c, bool mma, int reps, double* avg_ms);
+int op_write_pressure(Ctx* c, const char* path, std::string* msg);
 // solver.cu: a time step in three parts (op_advance runs them in a row)
 int op_advance_begin(Ctx* c);
 int op_advance_end(Ctx* c);

@@ -435,6 +435,7 @@ void ctx_destroy(Ctx* c) {
     drop_phase(ph);
   if (c->solve_graph_dense) cudaGraphDestroy(c->solve_graph_dense);
   inf_free(c);
+  pressure_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);

@@ -42,6 +42,7 @@ EXPORTS = [
     "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile", "ib_get_launch_shapes",
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
+    "ib_calculate_pressure", "ib_write_pressure",
 ]
 
 
@@ -129,6 +130,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_batch_destroy": ([P], C.c_int), "ib_batch_size": ([P, I], C.c_int),
         "ib_batch_context": ([P, C.c_int, C.POINTER(P)], C.c_int),
         "ib_batch_advance": ([P, I], C.c_int),
+        "ib_calculate_pressure": ([P, P], C.c_int), "ib_write_pressure": ([P, C.c_char_p], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -291,6 +293,17 @@ class Simulation:
         it = C.c_int()
         _check(self.lib.ib_advance(self.h, C.byref(it)), "ib_advance")
         return it.value
+
+    def pressure(self) -> list:
+        """calculate_pressure (operators_pressure.F90:110-437): the pressure coefficient at the
+        cell centres of every level, a list of (n, m) arrays."""
+        L, m, n = self.params.mgridlev, self.params.m, self.params.n
+        out = np.empty((L, n, m))
+        _check(self.lib.ib_calculate_pressure(self.h, _ptr(out)), "ib_calculate_pressure")
+        return list(out)
+
+    def write_pressure(self, path) -> None:
+        _check(self.lib.ib_write_pressure(self.h, os.fsencode(path)), "ib_write_pressure")
 
     def write_variables(self, path) -> None:
         """write_variables (variables.F90:709-803): the reference's restart file at path."""

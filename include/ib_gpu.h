@@ -142,6 +142,16 @@ int ib_read_variables(IbCtx* ctx, const char* path, int itime);
 int ib_get_counters(IbCtx* ctx, int* ksp_iter, int* fsi_iter);
 int ib_get_dims(IbCtx* ctx, int* nf, int* nbc, int* ns, int* nu, int* nv);
 
+/* calculate_pressure (operators_pressure.F90:110-437, called every isave steps by main.F90:40-43
+ * when compute_pressure is set): the pressure coefficient 2 (P - |u|^2/2) of the current state
+ * at the cell centres of every level, solving D D^T P = D N(q) - D E^T f/dt coarse to fine.
+ * p: mgridlev x n x m (levels contiguous, x fastest: cell (i, j) of level k at
+ * (k*n + j-1)*m + i-1).  Zero user body forcing, as in the reference's user.F90. */
+int ib_calculate_pressure(IbCtx* ctx, double* p);
+/* write_pressure (operators_pressure.F90:857-879): the last pressure computed, written as
+ * output/pressureRR_IIIIIII.var (index range record, then one record per level). */
+int ib_write_pressure(IbCtx* ctx, const char* path);
+
 /* ---- batches: many independent simulations advanced together (no counterpart in the
  * reference, which runs one simulation per job) ---- */
 typedef struct IbBatch IbBatch;
@@ -228,7 +238,9 @@ int ib_schur_solve(IbCtx* ctx, const double* rhs, double* f, int* iterations);
 /* the cudaStream_t every kernel of this context runs on */
 int ib_get_stream(IbCtx* ctx, void** stream);
 /* average device time (ms) of `reps` back-to-back launches of one full pass over the finest
- * grid: kind 0 the DST-I x pass, 1 the per-mode tridiagonal solve.  The launches cycle over
+ * grid: kind 0 the DST-I x pass, 1 the per-mode tridiagonal solve; kinds 2 and 3 the pressure
+ * grid's x transform (n x m cells times the m x m DST-I matrix) on the FP64 tensor cores (2) or
+ * with FP64 FMAs (3).  The launches cycle over
  * pairs of temporary fields (allocated for the call) that together exceed twice the L2 size,
  * so each reads its input from HBM; the context's state is not touched. */
 int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);

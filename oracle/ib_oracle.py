@@ -678,6 +678,140 @@ class IBOracle:
                 reason = -3
         return x, its, reason
 
+    # -------------------------------------------------- operators_pressure.F90
+    # Pressure on every level (cell centres, (n, m) arrays, [j-1, i-1] <-> cell (i, j)) from the
+    # state after a step: D D^T P = D N(q) - D E^T f/dt solved coarse to fine, then the
+    # dynamic part removed and the result scaled to a pressure coefficient.
+    def ddti(self, rhs):
+        """myfft.F90:192-203: S[laminv_ddti * S[rhs]], S = RODFT00 x RODFT00 on (n, m),
+        laminv_ddti = 1 / lam_ddti / (4 (m+1)(n+1)) (myfft.F90:147-152)."""
+        m, n = self.m, self.n
+        i = np.arange(1, m + 1, dtype=np.float64)[None, :]
+        j = np.arange(1, n + 1, dtype=np.float64)[:, None]
+        lam = 2.0 * (np.cos(PI * i / float(m + 1)) + np.cos(PI * j / float(n + 1)) - 2.0)
+        laminv = 1.0 / lam / (4.0 * float((m + 1) * (n + 1)))
+        return self.dst(laminv * self.dst(rhs))
+
+    @staticmethod
+    def divergence(qx, qy):
+        """operators_pressure.F90:505-516: cell (i,j) gets qx(i+1,j)-qx(i,j)+qy(i,j+1)-qy(i,j)."""
+        return qx[:, 1:] - qx[:, :-1] + qy[1:, :] - qy[:-1, :]
+
+    def nonlinear_corner(self, omega, qx, qy):
+        """operators_pressure.F90:441-455: omega times the vertex-averaged flux."""
+        m, n = self.m, self.n
+        oqx = 0.5 * (qy[1:n, 1:m] + qy[1:n, 0:m - 1]) * omega
+        oqy = -0.5 * (qx[1:n, 1:m] + qx[0:n - 1, 1:m]) * omega
+        return oqx, oqy
+
+    def nonlinear_corner2edge(self, oqx, oqy, ubc, vbc):
+        """operators_pressure.F90:459-501: the vertex products ghosted by their rings, averaged
+        onto the faces."""
+        m, n = self.m, self.n
+        wx = self.ghost_vertex(oqx, ubc)
+        wy = self.ghost_vertex(oqy, vbc)
+        return 0.5 * (wx[1:n + 1, :] + wx[0:n, :]), 0.5 * (wy[:, 1:m + 1] + wy[:, 0:m])
+
+    def coarsify_pressure(self, fine):
+        """operators_pressure.F90:529-563 (index set :567-608, one rank): the full-weighting
+        sums at even cells, interpolated to the centres of 2x2 blocks, into coarse cells
+        (m/4+i/2+1, n/4+j/2+1); the coarse field is zero elsewhere."""
+        m, n = self.m, self.n
+        P = fine                                     # [j-1, i-1]
+        I = np.arange(2, m - 1, 2)                   # even i = 2..m-2
+        J = np.arange(2, n - 1, 2)
+        jj, ii = np.meshgrid(J - 1, I - 1, indexing="ij")
+        temp = (P[jj, ii] + 0.5 * (P[jj, ii + 1] + P[jj + 1, ii] + P[jj, ii - 1] + P[jj - 1, ii])
+                + 0.25 * (P[jj + 1, ii + 1] + P[jj - 1, ii + 1] + P[jj - 1, ii - 1] + P[jj + 1, ii - 1]))
+        coarse = np.zeros((n, m))
+        a = temp[:-1, :-1]; b = temp[:-1, 1:]; c = temp[1:, :-1]; d = temp[1:, 1:]
+        yy = (a + 3.0 * b + 3.0 * c + 9.0 * d) / 16.0   # i, j = 2..m-4, n-4 step 2
+        i2 = np.arange(2, m - 3, 2); j2 = np.arange(2, n - 3, 2)
+        coarse[np.ix_(n // 4 + j2 // 2, m // 4 + i2 // 2)] = yy
+        return coarse
+
+    def _qsq(self, qx, qy, fac):
+        """fac ((qx(i+1,j)+qx(i,j))^2 + (qy(i,j+1)+qy(i,j))^2) at every cell."""
+        a = qx[:, 1:] + qx[:, :-1]
+        b = qy[1:, :] + qy[:-1, :]
+        return fac * (a * a + b * b)
+
+    def get_bc_phi1(self, qx, qy, fac):
+        """operators_pressure.F90:731-767: the coarsest level's ring (left[n], right[n],
+        bottom[m], top[m]) from the velocity of its boundary cells."""
+        m, n = self.m, self.n
+        v = self._qsq(qx, qy, fac)
+        return np.concatenate([v[:, 0], v[:, m - 1], v[0, :], v[n - 1, :]])
+
+    def get_bc_phi2(self, p):
+        """operators_pressure.F90:771-817: a finer level's ring from the coarse cells around
+        its footprint (two ring entries per coarse cell)."""
+        m, n = self.m, self.n
+        P = lambda i, j: p[j - 1, i - 1]
+        ring = np.zeros(2 * m + 2 * n)
+        L, R, B, T = 0, n, 2 * n, 2 * n + m
+        for i in range(m // 4 + 1, 3 * m // 4 + 1):
+            j = n // 4
+            ring[B + 2 * (i - 1 - m // 4)] = 0.25 * (2 * P(i, j) + P(i, j + 1) + P(i - 1, j))
+            ring[B + 2 * (i - 1 - m // 4) + 1] = 0.25 * (2 * P(i, j) + P(i, j + 1) + P(i + 1, j))
+            j = 3 * n // 4 + 1
+            ring[T + 2 * (i - 1 - m // 4)] = 0.25 * (2 * P(i, j) + P(i, j - 1) + P(i - 1, j))
+            ring[T + 2 * (i - 1 - m // 4) + 1] = 0.25 * (2 * P(i, j) + P(i, j - 1) + P(i + 1, j))
+        for j in range(n // 4 + 1, 3 * n // 4 + 1):
+            i = m // 4
+            ring[L + 2 * (j - 1 - n // 4)] = 0.25 * (2 * P(i, j) + P(i + 1, j) + P(i, j - 1))
+            ring[L + 2 * (j - 1 - n // 4) + 1] = 0.25 * (2 * P(i, j) + P(i + 1, j) + P(i, j + 1))
+            i = 3 * m // 4 + 1
+            ring[R + 2 * (j - 1 - n // 4)] = 0.25 * (2 * P(i, j) + P(i - 1, j) + P(i, j - 1))
+            ring[R + 2 * (j - 1 - n // 4) + 1] = 0.25 * (2 * P(i, j) + P(i - 1, j) + P(i, j + 1))
+        return ring
+
+    def apply_bc_phi(self, rhs, ring):
+        """operators_pressure.F90:821-838 (in place): left, right, bottom, top subtracted."""
+        m, n = self.m, self.n
+        rhs[:, 0] = rhs[:, 0] - ring[0:n]
+        rhs[:, m - 1] = rhs[:, m - 1] - ring[n:2 * n]
+        rhs[0, :] = rhs[0, :] - ring[2 * n:2 * n + m]
+        rhs[n - 1, :] = rhs[n - 1, :] - ring[2 * n + m:2 * n + 2 * m]
+        return rhs
+
+    def calculate_pressure(self):
+        """operators_pressure.F90:110-437 (no sub-domain, zero user forcing): pressure
+        coefficient 2 (P - |u|^2/2) on every level, coarsest to finest solve."""
+        L, m, n = self.L, self.m, self.n
+        nlq = [None] * L
+        oq = [None] * L
+        for k in range(L - 1, -1, -1):
+            if k == L - 1:
+                ubc = np.zeros(self.nbc); vbc = np.zeros(self.nbc)
+            else:
+                ubc = self.get_bc(oq[k + 1][0], 1.0); vbc = self.get_bc(oq[k + 1][1], 1.0)
+            qx = self.qx[k] + self.q0x[k]; qy = self.qy[k] + self.q0y[k]
+            oq[k] = self.nonlinear_corner(self.omega[k], qx, qy)
+            nx, ny = self.nonlinear_corner2edge(oq[k][0], oq[k][1], ubc, vbc)
+            d = self.delta * float(2 ** k)
+            nlq[k] = (nx / (d * d), ny / (d * d))
+        rhs = [np.zeros((n, m)) for _ in range(L)]
+        if self.nf:
+            hx, hy = self.reg(self.f / self.p.dt)
+            rhs[0] = -self.divergence(hx, hy)
+        for k in range(1, L):
+            rhs[k] = self.coarsify_pressure(rhs[k - 1])
+        for k in range(L):
+            rhs[k] = rhs[k] + self.divergence(*nlq[k])
+        p = [None] * L
+        for k in range(L - 1, -1, -1):
+            if k == L - 1:
+                fac = 0.125 / (self.delta * 2.0 ** k) ** 2
+                ring = self.get_bc_phi1(self.qx[k] + self.q0x[k], self.qy[k] + self.q0y[k], fac)
+            else:
+                ring = self.get_bc_phi2(p[k + 1])
+            p[k] = self.ddti(self.apply_bc_phi(rhs[k], ring))
+        for k in range(L):
+            fac = 0.125 / (self.delta * 2.0 ** k) ** 2
+            p[k] = 2.0 * (p[k] - self._qsq(self.qx[k] + self.q0x[k], self.qy[k] + self.q0y[k], fac))
+        return p
+
     # ------------------------------------------------------------ stepping
     def preprocess(self):
         """timestepper.F90:560-598: dense Schur matrix, column i = a_times(e_i),
