@@ -471,6 +471,7 @@ def run_gpu(args, world, rank, local):
                                   "over the measured step time; the influence matrix replaces the per-iteration "
                                   "work, so this is a step-level figure, not a kernel roofline"},
         "tridiagonal_pass_us": 1e3 * t_tri,
+        "pressure": _pressure_leg(sim, p),
         "schur_stages_us": sim.profile_schur(20),
         "influence": sim.influence_stats(),
         "launch_shapes": sim.launch_shapes(),
@@ -505,6 +506,30 @@ def run_gpu(args, world, rank, local):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def _pressure_leg(sim, p):
+    """calculate_pressure on the current state (every level), timed with CUDA events on the
+    simulation's stream after one untimed call, and the A/B of its x transform (800 x 400 cells
+    times the 800 x 800 DST-I matrix) on the FP64 tensor cores and with FP64 FMAs."""
+    import torch
+    stream = torch.cuda.ExternalStream(sim.stream())
+    sim.pressure()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    reps = 5
+    for _ in range(reps):
+        sim.pressure()
+    e1.record(stream)
+    e1.synchronize()
+    t_mma = sim.time_pass(2, 20)
+    t_fma = sim.time_pass(3, 20)
+    flops = 2.0 * p.n * p.m * p.m
+    return {"recovery_ms": e0.elapsed_time(e1) / reps, "levels": p.mgridlev,
+            "x_transform_us": {"dmma": 1e3 * t_mma, "fma": 1e3 * t_fma},
+            "x_transform_tflops": {"dmma": flops / (t_mma * 1e-3) / 1e12, "fma": flops / (t_fma * 1e-3) / 1e12},
+            "note": "recovery_ms includes copying every level's pressure to the host"}
 
 
 def _step_phases(sim, steps, device_loop=False):

@@ -906,12 +906,13 @@ int dst_sin2_table(const DstPlan& px, double* dev_out) {
 int dst_matrix_table(const DstPlan& px, double* dev_out) {
   const long double PI_L = 3.141592653589793238462643383279502884L;
   const int N = px.N, M = px.M;
+  // entry (j, k) is 2 sin(pi r / M) with r = jk mod 2M: one table of the 2M values (long double is
+  // software-emulated on some hosts, so it is not evaluated N^2 times)
+  std::vector<double> tab(2 * (size_t)M);
+  for (long long r = 0; r < 2LL * M; ++r) tab[r] = (double)(2.0L * sinl(PI_L * (long double)r / (long double)M));
   std::vector<double> w((size_t)N * N);
   for (int j = 1; j <= N; ++j)
-    for (int k = 1; k <= N; ++k) {
-      long long num = (long long)j * k % (2LL * M);
-      w[(size_t)(j - 1) * N + (k - 1)] = (double)(2.0L * sinl(PI_L * (long double)num / (long double)M));
-    }
+    for (int k = 1; k <= N; ++k) w[(size_t)(j - 1) * N + (k - 1)] = tab[(long long)j * k % (2LL * M)];
   IB_CUDA_CHECK(cudaMemcpy(dev_out, w.data(), 8 * w.size(), cudaMemcpyHostToDevice));
   return IB_OK;
 }

@@ -7,8 +7,10 @@
 // (coarsify_pressure).  The solve on one level, ddti (myfft.F90:192-203), is the 2-D DST-I of
 // the m x n cell grid with the eigenvalues of D D^T: as for ctci, the y direction is a per-mode
 // tridiagonal solve, and the x direction -- length m, whose m + 1 (801 at 800 cells) the FFT's
-// radices 2, 3, 5 do not divide -- is a product with the DST-I matrix W (m x m), run on the FP64
-// tensor cores (mma.sync m8n8k4).  Arithmetic follows the reference's expressions: products
+// radices 2, 3, 5 do not divide -- is a product with the DST-I matrix W (m x m), with FP64 FMAs:
+// the same product on the FP64 tensor cores (mma.sync m8n8k4, kept as the measured alternative)
+// ran 686 us against 623 us at 800 x 400 on GB300, whose FP64 tensor path is no faster than its
+// FP64 pipe.  Arithmetic follows the reference's expressions: products
 // that the reference rounds before a sum are rounded separately here (no contraction).
 #include <cmath>
 #include <vector>
@@ -18,10 +20,12 @@
 namespace ib {
 
 // ------------------------------------------------------------------ x transform by GEMM
-// C (R x N) = A (R x K) B (K x N), row-major, FP64.  CTA tile 64 x 64 x 16, four warps in 2 x 2,
-// each warp 32 x 32 = 4 x 4 tiles of 8 x 8.  One mma.sync.m8n8k4.f64: lane l holds
-// A[l/4][l%4], B[l%4][l/4] and C[l/4][2(l%4) + {0,1}] of its 8 x 4, 4 x 8 and 8 x 8 tiles.
-constexpr int kPM = 64, kPN = 64, kPK = 16;
+// C (R x N) = A (R x K) B (K x N), row-major, FP64.  CTA tile 32 x 32 x 16 (325 CTAs for the
+// 400 x 800 x 800 product at 800 x 400 cells: a 64 x 64 tile left most SMs idle with 91), four
+// warps in 2 x 2, each warp 16 x 16 = 2 x 2 tiles of 8 x 8.  One mma.sync.m8n8k4.f64: lane l
+// holds A[l/4][l%4], B[l%4][l/4] and C[l/4][2(l%4) + {0,1}] of its 8 x 4, 4 x 8 and 8 x 8
+// tiles.  The FMA variant gives each thread 4 rows x 2 columns of the tile.
+constexpr int kPM = 32, kPN = 32, kPK = 16;
 
 __device__ __forceinline__ void mma_f64(double& d0, double& d1, double a, double b) {
   asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
@@ -38,11 +42,11 @@ __global__ void __launch_bounds__(128) k_pgemm(int R, int N, int K, const double
   __shared__ double Bs[kPK][kPN + 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int r0 = blockIdx.y * kPM, c0 = blockIdx.x * kPN;
-  // MMA: warp (wr, wc) owns rows wr*32.., cols wc*32..; FMA: thread owns 8 rows x 4 cols
   const int wr = warp >> 1, wc = warp & 1;
-  double acc[32];
+  const int tr = (tid >> 4) * 4, tc = (tid & 15) * 2;   // FMA: rows tr..tr+3, columns tc, tc+1
+  double acc[8];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) acc[i] = 0.0;
+  for (int i = 0; i < 8; ++i) acc[i] = 0.0;
   for (int k0 = 0; k0 < K; k0 += kPK) {
     for (int t = tid; t < kPM * kPK; t += 128) {
       const int r = t / kPK, k = t % kPK;
@@ -56,28 +60,25 @@ __global__ void __launch_bounds__(128) k_pgemm(int R, int N, int K, const double
     if (MMA) {
 #pragma unroll
       for (int kk = 0; kk < kPK; kk += 4) {
-        double a[4], b[4];
+        double a[2], b[2];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = As[wr * 32 + i * 8 + (lane >> 2)][kk + (lane & 3)];
+        for (int i = 0; i < 2; ++i) a[i] = As[wr * 16 + i * 8 + (lane >> 2)][kk + (lane & 3)];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = Bs[kk + (lane & 3)][wc * 32 + j * 8 + (lane >> 2)];
+        for (int j = 0; j < 2; ++j) b[j] = Bs[kk + (lane & 3)][wc * 16 + j * 8 + (lane >> 2)];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 2; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) mma_f64(acc[(i * 4 + j) * 2], acc[(i * 4 + j) * 2 + 1], a[i], b[j]);
+          for (int j = 0; j < 2; ++j) mma_f64(acc[(i * 2 + j) * 2], acc[(i * 2 + j) * 2 + 1], a[i], b[j]);
       }
     } else {
-      const int tr = (tid >> 4) * 8, tc = (tid & 15) * 4;
-#pragma unroll 4
+#pragma unroll
       for (int kk = 0; kk < kPK; ++kk) {
-        double b[4];
+        const double b0 = Bs[kk][tc], b1 = Bs[kk][tc + 1];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tc + j];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < 4; ++i) {
           const double a = As[tr + i][kk];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i * 4 + j] = fma(a, b[j], acc[i * 4 + j]);
+          acc[i * 2] = fma(a, b0, acc[i * 2]);
+          acc[i * 2 + 1] = fma(a, b1, acc[i * 2 + 1]);
         }
       }
     }
@@ -85,22 +86,21 @@ __global__ void __launch_bounds__(128) k_pgemm(int R, int N, int K, const double
   }
   if (MMA) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+      for (int j = 0; j < 2; ++j)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const int r = r0 + wr * 32 + i * 8 + (lane >> 2), c = c0 + wc * 32 + j * 8 + 2 * (lane & 3) + h;
-          if (r < R && c < N) C[(size_t)r * ldc + c] = acc[(i * 4 + j) * 2 + h];
+          const int r = r0 + wr * 16 + i * 8 + (lane >> 2), c = c0 + wc * 16 + j * 8 + 2 * (lane & 3) + h;
+          if (r < R && c < N) C[(size_t)r * ldc + c] = acc[(i * 2 + j) * 2 + h];
         }
   } else {
-    const int tr = (tid >> 4) * 8, tc = (tid & 15) * 4;
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < 2; ++j) {
         const int r = r0 + tr + i, c = c0 + tc + j;
-        if (r < R && c < N) C[(size_t)r * ldc + c] = acc[i * 4 + j];
+        if (r < R && c < N) C[(size_t)r * ldc + c] = acc[i * 2 + j];
       }
   }
 }
@@ -304,14 +304,13 @@ static int pressure_setup(Ctx* c) {
   P.ring = take(2 * (size_t)(m + n));
   // W[j][k] = 2 sin(pi (j+1)(k+1) / (m+1)), the DST-I matrix of length m (symmetric)
   {
-    std::vector<double> W((size_t)m * m);
+    std::vector<double> W((size_t)m * m), tab(2 * (size_t)(m + 1));
     const long double PI_L = 3.141592653589793238462643383279502884L;
     const long long M = m + 1;
+    for (long long r = 0; r < 2 * M; ++r) tab[r] = (double)(2.0L * sinl(PI_L * (long double)r / (long double)M));
     for (int j = 0; j < m; ++j)
-      for (int k = 0; k < m; ++k) {
-        const long long r = ((long long)(j + 1) * (k + 1)) % (2 * M);   // sin is 2M-periodic in r
-        W[(size_t)j * m + k] = (double)(2.0L * sinl(PI_L * (long double)r / (long double)M));
-      }
+      for (int k = 0; k < m; ++k)   // sin(pi r / M) is 2M-periodic in r
+        W[(size_t)j * m + k] = tab[((long long)(j + 1) * (k + 1)) % (2 * M)];
     IB_CUDA_CHECK(cudaMemcpy(P.W, W.data(), 8 * W.size(), cudaMemcpyHostToDevice));
   }
   // ddti = S_x S_y [1 / (lam N)] S_y S_x with lam = -(lx + ly), N = 4 (m+1)(n+1); with
@@ -404,7 +403,7 @@ int op_pressure(Ctx* c) {
     }
     count_launch();
     k_p_apply_bc<<<cdiv(cells, B), B, 0, st>>>(g, P.rhs[k], P.ring);
-    RC(ddti(c, P.rhs[k], P.p[k], true));
+    RC(ddti(c, P.rhs[k], P.p[k], false));
   }
   for (int k = 0; k < L; ++k) {
     const double d = c->delta * std::pow(2.0, k);

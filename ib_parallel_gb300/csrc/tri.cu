@@ -1,6 +1,7 @@
 // Chunked per-mode tridiagonal solver (see tri.cuh).
 #include <algorithm>
 #include <cmath>
+#include <thread>
 #include <vector>
 
 #include "tri.cuh"
@@ -50,8 +51,11 @@ int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, doub
   double* sinv = inv + S;
   double* gL = inv + 2 * S;
   double* rinv = inv + 3 * S;
+  // the modes are independent: they are split over host threads (long double arithmetic is
+  // software-emulated on some hosts and costs milliseconds per operator otherwise)
+  auto modes = [&](int k0, int k1) {
   std::vector<long double> beta(s), d(s), g(s), bp(m), z(m), x(m);
-  for (int k = 0; k < nx; ++k) {
+  for (int k = k0; k < k1; ++k) {
     long double a = 2.0L + (long double)shift[k];
     beta[0] = a;
     for (int j = 1; j < s; ++j) beta[j] = a - 1.0L / beta[j - 1];
@@ -77,6 +81,15 @@ int tri_build(TriOp* op, int nx, int ny, const double* shift, double sigma, doub
       for (int c = m - 2; c >= 0; --c) x[c] = z[c] + (B / bp[c]) * x[c + 1];
       for (int c = 0; c < m; ++c) rinv[((size_t)c * m + j) * nx + k] = (double)x[c];
     }
+  }
+  };
+  const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  if (nth == 1 || nx < 64) {
+    modes(0, nx);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t) th.emplace_back(modes, (int)((long long)nx * t / nth), (int)((long long)nx * (t + 1) / nth));
+    for (auto& x : th) x.join();
   }
   op->inv = dev;
   op->sinv = dev + S;
