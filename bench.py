@@ -190,7 +190,7 @@ def _oracle(p, bodies):
     import ib_oracle as O
     po = O.Params(**{k: getattr(p, k) for k in O.Params.__dataclass_fields__ if hasattr(p, k)})
     ob = [O.Body(x=b.x.copy(), y=b.y.copy(), fam=b.fam, gamma0_deg=b.gamma0_deg, itheta=b.itheta,
-                 ktheta=b.ktheta, ctheta=b.ctheta) for b in bodies]
+                 ktheta=b.ktheta, ctheta=b.ctheta, nelem=b.nelem) for b in bodies]
     return O.IBOracle(po, ob)
 
 
@@ -321,6 +321,34 @@ def _long_run(p, bodies, steps):
             "band_builds": st["builds"], "band_build_ms": st["build_ms"], "fallbacks": st["fallbacks"],
             "final_theta": [float(x) for x in th],
             "note": "from the impulsive start, host wall clock, every band build inside the region"}
+
+
+def _beam_workload(args):
+    """BASELINE's flexible plate as an Euler-Bernoulli beam (geometry.config_beam_800x400: 51
+    points, 25 elements, mass ratio 0.5, EI 1e-3, 800x400 x 5 levels, dt 1e-3): device-timed and
+    end-to-end steps/s.  Beams run the FSI iterations from the host each step (the captured
+    device loop is the torsional body's)."""
+    import torch
+    from ib_parallel_gb300 import geometry as GEO
+    from ib_parallel_gb300 import ibgpu as G
+    p, bodies = GEO.config_beam_800x400()
+    sim = G.Simulation(p, bodies)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    for _ in range(max(3, args.warmup)):
+        sim.advance()
+    sim.synchronize()
+    steps = max(args.steps, 20)
+    t, ksp, fsi = _timed_steps(sim, stream, steps)
+    te, h2d, d2h = _e2e_steps(sim, stream, steps)
+    q = sim.beam_state()[0]
+    sim.close()
+    return {"workload": "beam800x400", "metric": "FSI steps/s @800x400x5 FP64 (Euler-Bernoulli beam)",
+            "value": steps / t, "unit": "steps/s", "steps": steps, "ms_per_step": 1e3 * t / steps,
+            "e2e": {"value": steps / te, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "work_per_step": {"ksp_iter": ksp / steps, "fsi_iter": fsi / steps},
+            "tip_deflection": float(q[-2]) if len(q) else None,
+            "config": {"grid": "800x400", "levels": 5, "body_points": 51, "elements": 25, "mass_ratio": 0.5,
+                       "stiffness": 1e-3, "Re": 500, "dt": 1e-3}}
 
 
 def _c1_workload(args):
@@ -498,6 +526,8 @@ def run_gpu(args, world, rank, local):
             "note": "same_algorithm: the GPU with the matrix-free Schur operator the port runs"}
     if rank == 0 and world == 1 and not args.no_c1:
         result["workloads"] = {C1_WORKLOAD: _c1_workload(args)}
+    if rank == 0 and world == 1 and not args.no_c1:
+        result.setdefault("workloads", {})["beam800x400"] = _beam_workload(args)
     if rank == 0 and world == 1 and args.ensemble > 0:
         result.setdefault("workloads", {})["ensemble"] = _ensemble(args)
     if rank == 0:

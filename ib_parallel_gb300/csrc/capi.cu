@@ -352,6 +352,21 @@ int ib_write_pressure(IbCtx* h, const char* path) {
   return rc == IB_OK ? IB_OK : fail(rc, ("write_pressure: " + msg).c_str());
 }
 
+int ib_get_beam_state(IbCtx* h, double* q, double* qd, double* qdd) {
+  CTX_OR_FAIL(h);
+  size_t at = 0;
+  for (const ib::BeamDev& b : c->beams_h) {
+    const size_t n = 8 * (size_t)b.ndof;
+    if ((q && cudaMemcpyAsync(q + at, b.q, n, cudaMemcpyDefault, c->st) != cudaSuccess) ||
+        (qd && cudaMemcpyAsync(qd + at, b.qd, n, cudaMemcpyDefault, c->st) != cudaSuccess) ||
+        (qdd && cudaMemcpyAsync(qdd + at, b.qdd, n, cudaMemcpyDefault, c->st) != cudaSuccess))
+      return fail(IB_ERR_CUDA, "copy failed");
+    at += b.ndof;
+  }
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(IB_ERR_CUDA, "copy failed");
+  return IB_OK;
+}
+
 int ib_get_counters(IbCtx* h, int* ksp_iter, int* fsi_iter) {
   CTX_OR_FAIL(h);
   if (ksp_iter) *ksp_iter = c->ksp_iter;
@@ -557,6 +572,7 @@ int ib_struct_btimes(IbCtx* h, const double* x, double* y) {
   STAGE_CHECK(S);
   int rc = cudaMemsetAsync(o, 0, 8 * (size_t)c->nf, c->st) == cudaSuccess ? IB_OK : IB_ERR_CUDA;
   if (rc == IB_OK) rc = ib::launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, a, o, c->st);
+  if (rc == IB_OK) rc = ib::launch_beam_btimes(c, a, o, c->st);
   return op_result(S.finish(rc), "struct_btimes failed");
 }
 
@@ -567,6 +583,7 @@ int ib_struct_rhs(IbCtx* h, double* y) {
   STAGE_CHECK(S);
   int rc = cudaMemsetAsync(o, 0, 8 * (size_t)c->nf, c->st) == cudaSuccess ? IB_OK : IB_ERR_CUDA;
   if (rc == IB_OK) rc = ib::launch_tors_rhs(c->nt, c->tb, c->ts, c->p.dt, c->delta, o, c->st);
+  if (rc == IB_OK) rc = ib::launch_beam_rhs(c, o, c->st);
   return op_result(S.finish(rc), "struct_rhs failed");
 }
 
@@ -576,7 +593,8 @@ int ib_struct_dx(IbCtx* h, const double* f, double* err) {
   const double* a = S.in(f, c->nf);
   STAGE_CHECK(S);
   int rc = ib::launch_tors_dx(c->nt, c->tb, c->ts, c->p.dt, c->delta, a, c->xb, c->yb, c->err_fsi, c->st);
-  if (rc == IB_OK && c->nt > 0) rc = ib::op_reg_prep(c);
+  if (rc == IB_OK) rc = ib::launch_beam_dx(c, a, c->st);
+  if (rc == IB_OK && (c->nt > 0 || c->nbeam > 0)) rc = ib::op_reg_prep(c);
   rc = S.finish(rc);
   if (rc == IB_OK && err) {
     if (cudaMemcpy(err, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) rc = IB_ERR_CUDA;

@@ -188,6 +188,11 @@ struct Ctx {
   double* ub = nullptr;
   bool ub_on = false;
   PressureOp pres;
+  // family-3 beams (beam.cu)
+  int nbeam = 0;
+  BeamDev* beams = nullptr;
+  std::vector<BeamDev> beams_h;
+  std::vector<double*> beam_mem;
   int *comp = nullptr, *bid = nullptr;
   RegDev reg{};
   TorsBody* tb = nullptr;
@@ -305,6 +310,15 @@ int inf_alloc(Ctx* c);                 // fixed-size buffers (at ib_create)
 void inf_free(Ctx* c);
 // checkpoint.cu: the reference's restart file (variables.F90:709-913)
 int op_write_variables(Ctx* c, const char* path, std::string* msg);
+// beam.cu: family-3 bodies
+int beam_build(Ctx* c, const IbBody* bodies, int nbody, std::string* msg);
+void beam_free(Ctx* c);
+int launch_beam_rhs(Ctx* c, double* y, cudaStream_t st);
+int launch_beam_dx(Ctx* c, const double* f, cudaStream_t st);
+int launch_beam_btimes(Ctx* c, const double* x, double* y, cudaStream_t st);
+int launch_beam_add_b(Ctx* c, double* St, cudaStream_t st);
+int launch_beam_initial_acc(Ctx* c, const double* f, cudaStream_t st);
+int launch_beam_save(Ctx* c, cudaStream_t st);
 // pressure.cu: calculate_pressure (operators_pressure.F90:110-437) into pres.p
 int op_pressure(Ctx* c);
 void pressure_free(Ctx* c);

@@ -627,7 +627,8 @@ int inf_assemble_ptk(Ctx* c, cudaStream_t st) {
 int inf_assemble(Ctx* c) {
   RC(inf_assemble_kp(c, c->st, false));
   RC(inf_assemble_b(c, c->st));
-  return inf_assemble_ptk(c, c->st);
+  RC(inf_assemble_ptk(c, c->st));
+  return launch_beam_add_b(c, c->inf.St, c->st);   // the beams' dense blocks of B
 }
 
 // y = (S + B) x from the assembled column-major operator (B is part of it).

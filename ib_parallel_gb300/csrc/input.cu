@@ -180,14 +180,21 @@ int read_body(const char* path, IbBody* b, double* x, double* y, int cap, std::s
   if (!r.values(1, &v) || !parse_int(v[0], &npts) || npts < 1) { *msg = "bad point count"; return IB_ERR_ARG; }
   if (!r.values(1, &v) || !parse_int(v[0], &fam)) { *msg = "bad body family '" + (v.empty() ? "" : v[0]) + "'"; return IB_ERR_ARG; }
   double g0 = 0.0, a0 = 0.0, it = 0.0, kt = 0.0, ct = 0.0;
+  int nel = 0;
   if (fam == 2) {
     double* dst[5] = {&g0, &a0, &it, &kt, &ct};
     for (double* d : dst)
       if (!r.values(1, &v) || !parse_real(v[0], d)) { *msg = "bad torsion parameter"; return IB_ERR_ARG; }
+  } else if (fam == 3) {
+    // the beam family has no file layout in the reference: mass per unit length, bending
+    // stiffness EI and the number of elements, one per line, as the torsion parameters are
+    if (!r.values(1, &v) || !parse_real(v[0], &it) || !r.values(1, &v) || !parse_real(v[0], &kt) ||
+        !r.values(1, &v) || !parse_int(v[0], &nel)) { *msg = "bad beam parameter"; return IB_ERR_ARG; }
   }
   b->npts = npts;
   b->fam = fam;
   b->gamma0_deg = g0; b->alpha0_deg = a0; b->itheta = it; b->ktheta = kt; b->ctheta = ct;
+  b->nelem = nel;
   b->x = x; b->y = y;
   if (cap < npts || !x || !y) {
     *msg = "arrays hold " + std::to_string(cap) + " points, the body has " + std::to_string(npts);

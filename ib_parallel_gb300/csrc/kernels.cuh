@@ -101,6 +101,14 @@ struct TorsBody {
   // stiffness 4/dt^2 I + 2/dt C + K and its reciprocal, deltas / (4/dt^2 I + K), delta/deltas/dt
   double a44, a4, a2, keff, keff_inv, bq, bs;
 };
+// A family-3 beam (beam.cu): offset and points of its unknowns, DOFs, the cosine and sine of
+// its direction, the matrices (row-major) and the Newmark state with scratch vectors.
+struct BeamDev {
+  int off, npts, ndof;
+  double sg, cg;
+  double *M, *K, *Ke, *Ki, *Mi, *W, *phi, *B, *xy0;
+  double *q, *qd, *qdd, *q0, *qd0, *qdd0, *t1, *t2, *t3, *t4;
+};
 struct TorsState {  // device arrays of length nt
   double *theta, *thetad, *thetadd, *theta0, *thetad0, *thetadd0;
   double *sinv, *cosv;  // sin, cos (gamma0 - theta) at the current theta, kept with theta

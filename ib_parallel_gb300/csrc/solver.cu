@@ -136,8 +136,14 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   for (int i = 0; i < nbody; ++i) {
     const IbBody& b = bodies[i];
     if (b.npts < 2 || !b.x || !b.y) { *msg = "body needs >= 2 points"; return IB_ERR_ARG; }
-    if (b.fam != 1 && b.fam != 2) { *msg = "body family must be 1 (rigid) or 2 (torsional)"; return IB_ERR_ARG; }
+    if (b.fam < 1 || b.fam > 3) { *msg = "body family must be 1 (rigid), 2 (torsional) or 3 (beam)"; return IB_ERR_ARG; }
     if (b.fam == 2 && !(b.itheta > 0)) { *msg = "torsional body needs itheta > 0"; return IB_ERR_ARG; }
+    if (b.fam == 3 && (!(b.itheta > 0) || !(b.ktheta > 0))) {
+      *msg = "a beam needs mass per length (itheta) and EI (ktheta) > 0"; return IB_ERR_ARG;
+    }
+    if (b.fam == 3 && (b.nelem < 0 || (b.nelem == 0 && b.npts < 3))) {
+      *msg = "a beam needs nelem >= 1 (or at least 3 points)"; return IB_ERR_ARG;
+    }
     if (b.fam != 1) seen_nonrigid = true;
     else if (seen_nonrigid) { *msg = "rigid bodies must precede non-rigid ones (grid.F90:1226)"; return IB_ERR_ARG; }
   }
@@ -415,6 +421,10 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     if (rc != IB_OK) { *msg = "DST tuning failed"; ctx_destroy(c); return rc; }
   }
   if (nf > 0 && inf_alloc(c) != IB_OK) { *msg = "device allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM; }
+  {
+    const int rcb = beam_build(c, bodies, nbody, msg);
+    if (rcb != IB_OK) { ctx_destroy(c); return rcb; }
+  }
   rc = op_reg_prep(c);
   if (rc == IB_OK) rc = check_err(c);
   if (rc != IB_OK) { *msg = "body stencil outside the grid"; ctx_destroy(c); return rc; }
@@ -436,6 +446,7 @@ void ctx_destroy(Ctx* c) {
   if (c->solve_graph_dense) cudaGraphDestroy(c->solve_graph_dense);
   inf_free(c);
   pressure_free(c);
+  beam_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -745,6 +756,7 @@ int op_schur(Ctx* c, const double* x, double* y, bool with_b) {
   mark(7);
   RC(launch_regT_s(g, c->nf, c->mv_s[0], ring0, c->reg, nullptr, y, st));
   if (with_b) RC(launch_tors_btimes(c->nt, c->tb, c->ts, c->p.dt, c->delta, x, y, st));
+  if (with_b) RC(launch_beam_btimes(c, x, y, st));
   mark(8);
   return IB_OK;
 }
@@ -1364,17 +1376,19 @@ int op_advance_begin(Ctx* c) {
   if (c->nf > 0) {
     if (!p.num_stat) {
       if (it == 1) RC(launch_tors_initial_acc(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, st));
+      if (it == 1) RC(launch_beam_initial_acc(c, c->f, st));
       RC(launch_tors_save(c->nt, c->ts, st));
+      RC(launch_beam_save(c, st));
       c->ksp_iter = 0;
       c->gmres_reason = 0;
-      const bool moved = c->nt > 0;
+      const bool moved = c->nt > 0 || c->nbeam > 0;
       // the iterations on the device while the operator stays assembled on a valid band (the
       // host loop below takes over when a patch leaves it, and runs every step that needs the
       // band built, the matrix-free operator or per-phase timing)
       {
         Influence& I = c->inf;
         const bool device_loop = moved && p.schur_mode != 1 && c->use_step_graphs && c->use_fused && !c->prof_on &&
-                                 !c->stage_on && (!c->step_prof || c->step_prof_dev) &&
+                                 !c->stage_on && (!c->step_prof || c->step_prof_dev) && c->nbeam == 0 &&
                                  !c->graph_fsi_loop.failed &&
                                  c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
         if (device_loop && (c->graph_fsi_loop.exec || build_fsi_loop(c) == IB_OK)) {
@@ -1401,7 +1415,7 @@ int op_advance_end(Ctx* c) {
     if (!p.num_stat) {
       double err = 10.0;
       int fsi_count = 0;
-      const bool moved = c->nt > 0;
+      const bool moved = c->nt > 0 || c->nbeam > 0;
       {
         Influence& I = c->inf;
         if (c->loop_pending) {
@@ -1440,6 +1454,7 @@ int op_advance_end(Ctx* c) {
           // k_tors_rhs writes every unknown of a torsional body: rigid bodies' start at zero
           if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, c->st));
           RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, c->st));
+          RC(launch_beam_rhs(c, c->rhsf, c->st));
           // prescribed rigid-body motion (timestepper.F90:327-331): rhsf - delta u_B
           if (c->ub_on) RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, c->st));
           return launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, c->st);
@@ -1482,6 +1497,7 @@ int op_advance_end(Ctx* c) {
         RC(run_phase(c, c->graph_fsi_upd, [&]() -> int {
           RC(op_redistribute(c, c->f, c->f_rdst));
           RC(launch_tors_dx(c->nt, c->tb, c->ts, p.dt, c->delta, c->f, c->xb, c->yb, c->err_fsi, c->st));
+          RC(launch_beam_dx(c, c->f, c->st));
           if (moved) RC(op_reg_prep(c));
           if (patch) {
             RC(inf_patch(c));

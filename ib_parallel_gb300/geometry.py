@@ -31,6 +31,26 @@ def torsional_plate(npts: int = 201, length: float = 1.0, gamma0_deg: float = -1
                 itheta=itheta, ktheta=ktheta, ctheta=ctheta)
 
 
+def beam_plate(npts: int = 51, length: float = 1.0, incidence_deg: float = 10.0, mass_ratio: float = 0.5,
+               stiffness: float = 1e-3, nelem: int = 0, x0: float = 0.0, y0: float = 0.0) -> Body:
+    """Flexible plate (family 3: Euler-Bernoulli beam) clamped at (x0, y0), nose-down incidence."""
+    g = -math.radians(incidence_deg)
+    j = np.arange(npts, dtype=np.float64)
+    ds = length / (npts - 1)
+    return Body(x=x0 + j * ds * math.cos(g), y=y0 + j * ds * math.sin(g), fam=3, itheta=mass_ratio,
+                ktheta=stiffness, nelem=nelem)
+
+
+def config_beam_800x400(npts: int = 51) -> tuple:
+    """BASELINE's flexible plate as a beam: length 1 at 10 degrees, mass ratio 0.5, bending
+    stiffness 0.001, Re=500, 800x400 on [-1,7]x[-2,2], 5 levels, dt=1e-3, tolerances 1e-10;
+    51 points two grid spacings apart (25 elements) instead of 201 (half a spacing, where the
+    Schur operator is singular), no seeded tip perturbation (the beam starts straight)."""
+    p = Params(m=800, n=400, mgridlev=5, dt=1e-3, Re=500.0, len=8.0, offsetx=1.0, offsety=2.0,
+               fsi_tol=1e-10, atol=1e-10, rtol=1e-10)
+    return p, [beam_plate(npts, 1.0, 10.0, 0.5, 1e-3)]
+
+
 def config_cylinder_400x200() -> tuple:
     """Rigid cylinder, Re=100, 400x200 on [-2,6]x[-2,2], 3 levels, dt=0.004, 157 points."""
     p = Params(m=400, n=200, mgridlev=3, dt=0.004, Re=100.0, len=8.0, offsetx=2.0, offsety=2.0,
@@ -106,7 +126,7 @@ def read_body_file(path) -> Body:
         G._check(rc, "ib_read_body")
     G._check(rc, "ib_read_body")
     return Body(x=x[:b.npts].copy(), y=y[:b.npts].copy(), fam=b.fam, gamma0_deg=b.gamma0_deg,
-                alpha0_deg=b.alpha0_deg, itheta=b.itheta, ktheta=b.ktheta, ctheta=b.ctheta)
+                alpha0_deg=b.alpha0_deg, itheta=b.itheta, ktheta=b.ktheta, ctheta=b.ctheta, nelem=b.nelem)
 
 
 def load_input(directory) -> tuple:
@@ -128,6 +148,8 @@ def write_body_file(path, body: Body) -> None:
     lines = [f"{body.npts:<6d} ", f"{int(body.fam):<6d} "]
     if body.fam == 2:
         lines += [f"{v:.16f}" for v in (body.gamma0_deg, body.alpha0_deg, body.itheta, body.ktheta, body.ctheta)]
+    elif body.fam == 3:
+        lines += [repr(float(body.itheta)), repr(float(body.ktheta)), str(int(body.nelem))]
     lines += [f"{xv:<20.16f} {yv:<20.16f}" for xv, yv in zip(body.x, body.y)]
     with open(path, "w") as fh:
         fh.write("\n".join(lines) + "\n")

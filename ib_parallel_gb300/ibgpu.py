@@ -42,7 +42,7 @@ EXPORTS = [
     "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile", "ib_get_launch_shapes",
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
-    "ib_calculate_pressure", "ib_write_pressure",
+    "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state",
 ]
 
 
@@ -71,7 +71,8 @@ class IbRunControl(C.Structure):
 class IbBody(C.Structure):
     _fields_ = [("npts", C.c_int), ("fam", C.c_int), ("gamma0_deg", C.c_double),
                 ("alpha0_deg", C.c_double), ("itheta", C.c_double), ("ktheta", C.c_double),
-                ("ctheta", C.c_double), ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double))]
+                ("ctheta", C.c_double), ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("nelem", C.c_int)]
 
 
 _lib = None
@@ -131,6 +132,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_batch_context": ([P, C.c_int, C.POINTER(P)], C.c_int),
         "ib_batch_advance": ([P, I], C.c_int),
         "ib_calculate_pressure": ([P, P], C.c_int), "ib_write_pressure": ([P, C.c_char_p], C.c_int),
+        "ib_get_beam_state": ([P, P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -179,7 +181,8 @@ def measure_fp64_peak() -> float:
 
 @dataclass
 class Body:
-    """One ``input/body.NNN.inp`` (grid.F90:252-288): fam 1 rigid, 2 torsional."""
+    """One ``input/body.NNN.inp`` (grid.F90:252-288): fam 1 rigid, 2 torsional, 3 Euler-Bernoulli
+    beam (itheta = mass per unit length, ktheta = EI, nelem elements; 0: (npts - 1) / 2)."""
     x: np.ndarray
     y: np.ndarray
     fam: int = 1
@@ -188,6 +191,7 @@ class Body:
     itheta: float = 0.0
     ktheta: float = 0.0
     ctheta: float = 0.0
+    nelem: int = 0
 
     @property
     def npts(self):
@@ -248,6 +252,7 @@ def _c_bodies(bodies: Sequence[Body], keep: list):
         cb[i].ctheta = float(b.ctheta)
         cb[i].x = x.ctypes.data_as(C.POINTER(C.c_double))
         cb[i].y = y.ctypes.data_as(C.POINTER(C.c_double))
+        cb[i].nelem = int(getattr(b, "nelem", 0))
     return cb
 
 
@@ -269,6 +274,7 @@ class Simulation:
         self.h = h
         self.nbody = len(bodies)
         self.ntors = sum(1 for b in bodies if b.fam == 2)
+        self.beam_dofs = sum(2 * (b.nelem or (b.npts - 1) // 2) for b in bodies if b.fam == 3)
         nf, nbc, ns, nu, nv = (C.c_int() for _ in range(5))
         _check(self.lib.ib_get_dims(self.h, C.byref(nf), C.byref(nbc), C.byref(ns), C.byref(nu), C.byref(nv)))
         self.nf, self.nbc, self.ns, self.nu, self.nv = nf.value, nbc.value, ns.value, nu.value, nv.value
@@ -341,6 +347,13 @@ class Simulation:
         a, b, c = np.zeros(n), np.zeros(n), np.zeros(n)
         _check(self.lib.ib_get_body_state(self.h, _ptr(a), _ptr(b), _ptr(c)), "ib_get_body_state")
         return a[:self.ntors], b[:self.ntors], c[:self.ntors]
+
+    def beam_state(self):
+        """DOFs (w, dw/ds at the free nodes) of the beams, their rates and accelerations."""
+        n = max(1, self.beam_dofs)
+        a, b, c = np.zeros(n), np.zeros(n), np.zeros(n)
+        _check(self.lib.ib_get_beam_state(self.h, _ptr(a), _ptr(b), _ptr(c)), "ib_get_beam_state")
+        return a[:self.beam_dofs], b[:self.beam_dofs], c[:self.beam_dofs]
 
     def counters(self):
         k, f = C.c_int(), C.c_int()

@@ -59,13 +59,17 @@ typedef struct IbParams {
   int influence_margin; /* vertices of slack around the stencils in the band (0: 8) */
 } IbParams;
 
-/* One input/body.NNN.inp (grid.F90:252-288).  fam: 1 rigid, 2 torsional.
- * Rigid bodies must precede non-rigid ones (grid.F90:1226,1244). */
+/* One input/body.NNN.inp (grid.F90:252-288).  fam: 1 rigid, 2 torsional, 3 Euler-Bernoulli
+ * beam.  Rigid bodies must precede non-rigid ones (grid.F90:1226,1244).  Family 3 is declared
+ * and left empty in the reference; here it is a linear beam clamped at its first point along the
+ * line to its last point, nelem Hermite-cubic elements (0: (npts-1)/2), itheta = mass per unit
+ * length, ktheta = bending stiffness EI (ib_get_beam_state gives its DOFs). */
 typedef struct IbBody {
   int npts, fam;
   double gamma0_deg, alpha0_deg, itheta, ktheta, ctheta;
   const double* x;
   const double* y;
+  int nelem;
 } IbBody;
 
 typedef struct IbCtx IbCtx;
@@ -119,7 +123,8 @@ int ib_get_body_state(IbCtx* ctx, double* theta, double* thetad, double* thetadd
  * error (IB_ERR_ARG). */
 int ib_read_namelist(const char* path, IbParams* p, IbRunControl* rc);
 /* setup_geometry (grid.F90:252-288): one body file input/body.NNN.inp (npts; fam; for fam 2 the
- * angles gamma0, alpha0 in degrees and itheta, ktheta, ctheta; then npts lines of x y), read as
+ * angles gamma0, alpha0 in degrees and itheta, ktheta, ctheta; for fam 3, which has no layout in
+ * the reference, mass per length, EI and the element count; then npts lines of x y), read as
  * the reference's list-directed READs do.  x, y: arrays of capacity cap.  On return body holds
  * the header, npts and pointers to x, y; if cap < npts nothing is copied and IB_ERR_ARG is
  * returned with body->npts set, so a caller can size its arrays and call again. */
@@ -138,6 +143,9 @@ int ib_write_variables(IbCtx* ctx, const char* path);
  * (timestepper.F90:76), a num_stat context factorises its Schur matrix on its first step
  * whatever itime is. */
 int ib_read_variables(IbCtx* ctx, const char* path, int itime);
+/* state of the family-3 beams in file order, each 2 nelem DOFs (w, dw/ds at nodes 1..nelem),
+ * concatenated: deflections q, their rates and accelerations (any may be NULL) */
+int ib_get_beam_state(IbCtx* ctx, double* q, double* qd, double* qdd);
 /* ksp_iter, fsi_iter of the last step (timestepper.F90:365-366, 456) */
 int ib_get_counters(IbCtx* ctx, int* ksp_iter, int* fsi_iter);
 int ib_get_dims(IbCtx* ctx, int* nf, int* nbc, int* ns, int* nu, int* nv);

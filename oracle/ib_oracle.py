@@ -147,12 +147,13 @@ class Body:
     """One ``input/body.NNN.inp`` (grid.F90:252-288)."""
     x: np.ndarray
     y: np.ndarray
-    fam: int = 1                 # 1 rigid, 2 torsional (3 is an empty stub in the reference)
+    fam: int = 1                 # 1 rigid, 2 torsional, 3 Euler-Bernoulli beam (a stub in the reference)
     gamma0_deg: float = 0.0
     alpha0_deg: float = 0.0
-    itheta: float = 0.0
-    ktheta: float = 0.0
+    itheta: float = 0.0          # fam 3: mass per unit length
+    ktheta: float = 0.0          # fam 3: bending stiffness EI
     ctheta: float = 0.0
+    nelem: int = 0               # fam 3: finite elements (0: (npts - 1) / 2)
 
     @property
     def npts(self) -> int:
@@ -398,8 +399,8 @@ class IBOracle:
                 seen_nonrigid = True
             elif seen_nonrigid:
                 raise ValueError("rigid bodies must be numbered before non-rigid ones")
-            if b.fam not in (1, 2):
-                raise ValueError("only body families 1 (rigid) and 2 (torsional) exist in the reference")
+            if b.fam not in (1, 2, 3):
+                raise ValueError("body families are 1 (rigid), 2 (torsional) and 3 (beam)")
         self.bodies = bodies
         self.nb = sum(b.npts for b in bodies)
         self.nf = 2 * self.nb
@@ -423,6 +424,7 @@ class IBOracle:
         nt = len(self.tors)
         self.theta = np.zeros(nt); self.thetad = np.zeros(nt); self.thetadd = np.zeros(nt)
         self.theta0 = np.zeros(nt); self.thetad0 = np.zeros(nt); self.thetadd0 = np.zeros(nt)
+        self.beams = [beam_setup(bodies[i], self.body_off[i], self.p.dt) for i, b in enumerate(bodies) if b.fam == 3]
         self.tb = []
         for i in self.tors:
             b = bodies[i]
@@ -529,6 +531,9 @@ class IBOracle:
             xb_ = x[o:o + 2 * np_]
             y[o:o + 2 * np_] = br * (br @ xb_) / self._keff(t) * \
                 ((self.delta ** 2 / b['deltas'] / dt) * (2 * b['deltas'] / dt))
+        for bm in self.beams:
+            o, n2 = bm.off, 2 * bm.npts
+            y[o:o + n2] = bm.B @ x[o:o + n2] * (2.0 * self.delta * self.delta / (dt * dt))
         return y
 
     def compute_rhs(self):
@@ -544,6 +549,8 @@ class IBOracle:
                 - (4.0 / dt ** 2 * I + 2.0 / dt * C + K) * th + 0.0 + 0.0)
             o, np_ = b['off'], b['npts']
             y[o:o + 2 * np_] = self._BR(t, th) * (self.delta * (rth - jr - thd))
+        for bm in self.beams:
+            y[bm.off:bm.off + 2 * bm.npts] = bm.rhs(self.delta)
         return y
 
     def compute_dx(self, f):
@@ -570,6 +577,12 @@ class IBOracle:
             py = b['ybf0'] + j * b['deltas'] * math.sin(g)
             self.xb[o:o + np_] = px; self.xb[o + np_:o + 2 * np_] = px
             self.yb[o:o + np_] = py; self.yb[o + np_:o + 2 * np_] = py
+        for bm in self.beams:
+            err = max(err, bm.dx(f[bm.off:bm.off + 2 * bm.npts], self.delta))
+            px, py = bm.positions()
+            o, np_ = bm.off, bm.npts
+            self.xb[o:o + np_] = px; self.xb[o + np_:o + 2 * np_] = px
+            self.yb[o:o + np_] = py; self.yb[o + np_:o + 2 * np_] = py
         return err
 
     def initial_acc(self, f):
@@ -582,6 +595,8 @@ class IBOracle:
             ftint = b['ktheta'] * self.theta[t]
             self.thetadd[t] = 1.0 / b['itheta'] * (-b['ctheta'] * self.thetad[t] - ftint
                                                     + brf * b['deltas'] + 0.0 + 0.0)
+        for bm in self.beams:
+            bm.initial_acc(f[bm.off:bm.off + 2 * bm.npts], self.delta)
 
     # -------------------------------------------------------- Schur operator
     def a_times(self, x, with_b=True):
@@ -869,6 +884,8 @@ class IBOracle:
                 self.initial_acc(self.f)
             self.theta0 = self.theta.copy(); self.thetad0 = self.thetad.copy()
             self.thetadd0 = self.thetadd.copy()
+            for bm in self.beams:
+                bm.save()
             while err >= p.fsi_tol and fsi_count <= 1000:
                 fsi_count += 1
                 # compute_rhs, then rhsf - delta u_B (timestepper.F90:323-331), then E q on top
@@ -888,6 +905,112 @@ class IBOracle:
         self.omega[0] = self.omega[0] - vort
         self.s, self.qx, self.qy = self.vort2flux(self.omega)
         return it
+
+
+# ---------------------------------------------------------------------------
+# Euler-Bernoulli beam (body family 3).  The reference declares this family and leaves every
+# routine empty (operators_struct.F90:104-106, 146-148, 171-174, 285-288, 378-381, 472-474):
+# this is the library's own formulation, written from the standard finite-element mathematics
+# and coupled the way the reference couples its torsional body (operators_struct.F90:14-505),
+# with matrices in place of the hinge's scalars.  Parity against the reference is unpinned.
+#   * A linear (small-deflection) beam clamped at its first point, lying along the line from its
+#     first to its last point; transverse deflection w(s); nel Hermite-cubic elements of length
+#     h with DOFs (w, dw/ds) at the nodes, the clamped node's removed: ndof = 2 nel.
+#   * Element stiffness EI/h^3 [12 6h -12 6h; 6h 4h^2 -6h 2h^2; -12 -6h 12 -6h; 6h 2h^2 -6h 4h^2],
+#     consistent mass rho h/420 [156 22h 54 -13h; 22h 4h^2 13h -3h^2; 54 13h 156 -22h;
+#     -13h -3h^2 -22h 4h^2] (rho: mass per unit length).
+#   * Body point j (arc length j ds) has deflection Phi_j q; with the unit normal
+#     (-sin g, cos g) of the beam's direction g, its x and y unknowns move by W q,
+#     W = [-sin g Phi; cos g Phi] (the role of BR).  The point forces f act on the DOFs as
+#     F = (delta/dt) W^T f (the torque (BR . f) delta/dt of compute_dx).
+#   * Newmark (trapezoidal) with K_eff = 4/dt^2 M + K, as compute_dx does for theta:
+#     dq = K_eff^-1 (M (4/dt^2 q0 + 4/dt qd0 + qdd0) - K_eff q) + K_eff^-1 F,
+#     qd = -qd0 + 2/dt (q - q0), qdd = -qdd0 - 4/dt qd0 + 4/dt^2 (q - q0), error max |dq|;
+#     compute_rhs: delta W (r - jr - qd), r = qd0 + qd + 2/dt (q0 - q),
+#     jr = 2/dt K_eff^-1 (M a - K_eff q); b_times: (2 delta^2/dt^2) W K_eff^-1 W^T x;
+#     initial_acc: qdd = M^-1 (F - K q).
+# ---------------------------------------------------------------------------
+class BeamBody:
+    def __init__(self, b: "Body", off: int, dt: float):
+        x = np.asarray(b.x, dtype=np.float64); y = np.asarray(b.y, dtype=np.float64)
+        npts = len(x)
+        nel = int(b.nelem) if b.nelem else (npts - 1) // 2
+        if nel < 1 or npts < 2:
+            raise ValueError("a beam needs at least 2 points and 1 element")
+        dx, dy = x[-1] - x[0], y[-1] - y[0]
+        length = math.sqrt(dx * dx + dy * dy)
+        self.cg, self.sg = dx / length, dy / length          # cos, sin of the beam's direction
+        self.off, self.npts, self.nel, self.ndof, self.dt = off, npts, nel, 2 * nel, dt
+        self.x0, self.y0 = x.copy(), y.copy()
+        h = length / nel
+        rho, EI = float(b.itheta), float(b.ktheta)
+        kc = EI / (h * h * h)
+        ke = kc * np.array([[12.0, 6.0 * h, -12.0, 6.0 * h], [6.0 * h, 4.0 * h * h, -6.0 * h, 2.0 * h * h],
+                            [-12.0, -6.0 * h, 12.0, -6.0 * h], [6.0 * h, 2.0 * h * h, -6.0 * h, 4.0 * h * h]])
+        mc = rho * h / 420.0
+        me = mc * np.array([[156.0, 22.0 * h, 54.0, -13.0 * h], [22.0 * h, 4.0 * h * h, 13.0 * h, -3.0 * h * h],
+                            [54.0, 13.0 * h, 156.0, -22.0 * h], [-13.0 * h, -3.0 * h * h, -22.0 * h, 4.0 * h * h]])
+        nd = 2 * (nel + 1)
+        K = np.zeros((nd, nd)); M = np.zeros((nd, nd))
+        for e in range(nel):
+            for a in range(4):
+                for c in range(4):
+                    K[2 * e + a, 2 * e + c] += ke[a, c]
+                    M[2 * e + a, 2 * e + c] += me[a, c]
+        self.K, self.M = K[2:, 2:].copy(), M[2:, 2:].copy()
+        # deflection of body point j: element e = j nel div (npts-1), xi from the remainder
+        phi = np.zeros((npts, self.ndof))
+        for j in range(npts):
+            e = min(j * nel // (npts - 1), nel - 1)
+            xi = (j * nel - e * (npts - 1)) / float(npts - 1)
+            xi2, xi3 = xi * xi, xi * xi * xi
+            nvals = (1.0 - 3.0 * xi2 + 2.0 * xi3, h * (xi - 2.0 * xi2 + xi3), 3.0 * xi2 - 2.0 * xi3, h * (xi3 - xi2))
+            for a in range(4):
+                dof = 2 * e + a - 2
+                if dof >= 0:
+                    phi[j, dof] = nvals[a]
+        self.phi = phi
+        self.W = np.vstack([-self.sg * phi, self.cg * phi])
+        self.Keff = 4.0 / (dt * dt) * self.M + self.K
+        self.Ki = np.linalg.inv(self.Keff)
+        self.Mi = np.linalg.inv(self.M)
+        self.B = self.W @ self.Ki @ self.W.T
+        z = lambda: np.zeros(self.ndof)
+        self.q, self.qd, self.qdd, self.q0, self.qd0, self.qdd0 = z(), z(), z(), z(), z(), z()
+
+    def _a(self):
+        dt = self.dt
+        return 4.0 / (dt * dt) * self.q0 + 4.0 / dt * self.qd0 + self.qdd0
+
+    def save(self):
+        self.q0, self.qd0, self.qdd0 = self.q.copy(), self.qd.copy(), self.qdd.copy()
+
+    def rhs(self, delta):
+        dt = self.dt
+        r = self.qd0 + self.qd + 2.0 / dt * (self.q0 - self.q)
+        jr = 2.0 / dt * (self.Ki @ (self.M @ self._a() - self.Keff @ self.q))
+        return self.W @ (delta * (r - jr - self.qd))
+
+    def dx(self, f, delta):
+        dt = self.dt
+        F = delta / dt * (self.W.T @ f)
+        dq = self.Ki @ (self.M @ self._a() - self.Keff @ self.q) + self.Ki @ F
+        self.q = self.q + dq
+        self.qd = -self.qd0 + 2.0 / dt * (self.q - self.q0)
+        self.qdd = -self.qdd0 - 4.0 / dt * self.qd0 + 4.0 / (dt * dt) * (self.q - self.q0)
+        return float(np.abs(dq).max())
+
+    def initial_acc(self, f, delta):
+        F = delta / self.dt * (self.W.T @ f)
+        self.qdd = self.Mi @ (F - self.K @ self.q)
+
+    def positions(self):
+        d = self.phi @ self.q
+        return self.x0 + (-self.sg) * d, self.y0 + self.cg * d
+
+
+def beam_setup(b, off, dt):
+    return BeamBody(b, off, dt)
 
 
 # ---------------------------------------------------------------------------

@@ -11,7 +11,8 @@ def pair(p_kwargs: dict, bodies):
     po = O.Params(**{k: v for k, v in p_kwargs.items() if k in O.Params.__dataclass_fields__})
     pg = G.Params(**p_kwargs)
     ob = [O.Body(x=b.x.copy(), y=b.y.copy(), fam=b.fam, gamma0_deg=b.gamma0_deg, alpha0_deg=b.alpha0_deg,
-                 itheta=b.itheta, ktheta=b.ktheta, ctheta=b.ctheta) for b in bodies]
+                 itheta=b.itheta, ktheta=b.ktheta, ctheta=b.ctheta,
+                 nelem=getattr(b, 'nelem', 0)) for b in bodies]
     return O.IBOracle(po, ob), G.Simulation(pg, bodies)
 
 

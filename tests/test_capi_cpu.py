@@ -79,6 +79,7 @@ def _bodies(*specs):
     ("one_point", b"needs >= 2 points"),
     ("family", b"body family must be 1"),
     ("no_inertia", b"itheta > 0"),
+    ("beam_mass", b"mass per length"),
     ("rigid_after_torsional", b"rigid bodies must precede"),
 ])
 def test_create_rejects_bad_input_on_the_host(case, message):
@@ -94,6 +95,8 @@ def test_create_rejects_bad_input_on_the_host(case, message):
     elif case == "one_point":
         specs = [(1, 1, 0.0)]
     elif case == "family":
+        specs = [(5, 4, 0.0)]
+    elif case == "beam_mass":
         specs = [(5, 3, 0.0)]
     elif case == "no_inertia":
         specs = [(5, 2, 0.0)]

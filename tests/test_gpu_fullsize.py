@@ -44,7 +44,7 @@ def _pair(p, bodies, **over):
                                       "atol", "rtol", "num_stat", "motion", "gmres_restart", "gmres_max_it")}
     kw.update(over)
     ob = [O.Body(x=b.x.copy(), y=b.y.copy(), fam=b.fam, gamma0_deg=b.gamma0_deg, itheta=b.itheta,
-                 ktheta=b.ktheta, ctheta=b.ctheta) for b in bodies]
+                 ktheta=b.ktheta, ctheta=b.ctheta, nelem=b.nelem) for b in bodies]
     o = O.IBOracle(O.Params(**kw), ob)
     g = G.Simulation(G.Params(**kw, autotune=False), bodies)
     return o, g
