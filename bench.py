@@ -502,11 +502,13 @@ def run_gpu(args, world, rank, local):
         "pressure": _pressure_leg(sim, p),
         "schur_stages_us": sim.profile_schur(20),
         "influence": sim.influence_stats(),
+        "step_graph": sim.step_graph_stats(),
         "launch_shapes": sim.launch_shapes(),
         "step_phases_us": _step_phases(sim, 5),
         "step_phases_device_loop_us": _step_phases(sim, 5, device_loop=True),
     }
     sim.close()
+    result["phase_by_phase"] = _phased_rate(p, bodies, args)
     if not args.no_matrix_free:
         result["matrix_free"] = _matrix_free_rate(p, bodies, args)
     if args.long_steps > 0:
@@ -573,6 +575,31 @@ def _step_phases(sim, steps, device_loop=False):
     out = {k: v for k, v in out.items() if v > 0.0}
     out["steps"] = steps
     return out
+
+
+def _phased_rate(p, bodies, args):
+    """Steps/s of the same workload with the step run phase by phase (IB_WHOLE_STEP=0 at
+    creation: predictor, vort2flux, device FSI loop and correction as separate graphs with a
+    host readback between the loop and the correction), timed the same way."""
+    import torch
+    from ib_parallel_gb300 import ibgpu as G
+    old = os.environ.get("IB_WHOLE_STEP")
+    os.environ["IB_WHOLE_STEP"] = "0"
+    try:
+        sim = G.Simulation(p, bodies)
+    finally:
+        if old is None:
+            del os.environ["IB_WHOLE_STEP"]
+        else:
+            os.environ["IB_WHOLE_STEP"] = old
+    stream = torch.cuda.ExternalStream(sim.stream())
+    for _ in range(args.warmup):
+        sim.advance()
+    sim.synchronize()
+    t, _, _ = _timed_steps(sim, stream, args.steps)
+    stats = sim.step_graph_stats()
+    sim.close()
+    return {"value": args.steps / t, "unit": "steps/s", "steps_by_kind": stats}
 
 
 def _matrix_free_rate(p, bodies, args):

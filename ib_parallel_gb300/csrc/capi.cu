@@ -209,6 +209,7 @@ int ib_set_vector(IbCtx* h, int which, const double* in) {
     c->ub_on = true;
     ib::drop_phase(&c->graph_fsi_rhs);
     ib::drop_phase(&c->graph_fsi_loop);
+    ib::drop_phase(&c->graph_step);
   }
   if (rc == IB_OK) rc = ib::check_err(c);
   return op_result(rc, "set_vector failed");
@@ -695,6 +696,15 @@ int ib_get_influence_stats(IbCtx* h, long long* counts, double* build_ms) {
   counts[3] = I.fallbacks;
   counts[4] = I.nR;
   *build_ms = I.build_ms;
+  return IB_OK;
+}
+
+int ib_get_step_graph_stats(IbCtx* h, long long* counts) {
+  CTX_OR_FAIL(h);
+  if (!counts) return fail(IB_ERR_ARG, "bad argument");
+  counts[0] = c->n_step_graph;
+  counts[1] = c->n_step_gate_closed;
+  counts[2] = c->n_step_phased;
   return IB_OK;
 }
 

@@ -220,6 +220,18 @@ struct Ctx {
   // path; counters [0] iterations [1] Krylov iterations [2] operator products [3] band flag)
   PhaseGraph graph_fsi_loop;
   long long fsi_body_launches = 0;
+  // the whole step as one graph, from the second step on, where the forces come from the
+  // device FSI loop (mode 1) or without host decisions (mode 2: no bodies, or the direct
+  // solve): predictor, first vort2flux, forces, then the correction, in mode 1 under an if
+  // node that a gate kernel opens when the host loop has no iteration left to run.  graph_step
+  // counts what always runs (the FSI iterations come from fsi_body/post_launches), step_corr
+  // the correction's kernels and DST passes.  IB_WHOLE_STEP=0 in the environment at creation
+  // turns it off (the step then runs phase by phase with a host readback in the middle).
+  PhaseGraph graph_step, step_corr;
+  int step_mode = 0;
+  bool use_whole_step = true;
+  bool step_pending = false;       // graph_step launched: its counters arrive with the step
+  long long n_step_graph = 0, n_step_gate_closed = 0, n_step_phased = 0;
   // origins and weights of the current positions, copied at the start of a device FSI
   // iteration for its redistribution (the weights are rebuilt meanwhile)
   int* reg_ix_s = nullptr;

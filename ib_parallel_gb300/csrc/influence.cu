@@ -441,6 +441,7 @@ int inf_build(Ctx* c) {
   drop_phase(&c->graph_fsi_asm);
   drop_phase(&c->graph_fsi_upd);
   drop_phase(&c->graph_fsi_loop);
+  drop_phase(&c->graph_step);
   I.active = false;
   if (I.nR == 0) return IB_ERR_STATE;
   const size_t nK = (size_t)I.nR * I.nR;

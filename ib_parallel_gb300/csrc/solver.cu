@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "ctx.cuh"
@@ -416,6 +417,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->ly_none.B = 3; c->ly_none.NT = 384; c->ly_none.narrow_scan = 1;
   c->tl.Mb = 4;
   c->use_fused = p.schur_mode != 2;
+  if (const char* w = std::getenv("IB_WHOLE_STEP")) c->use_whole_step = std::atoi(w) != 0;
   if (p.autotune) {
     rc = tune(c);
     if (rc != IB_OK) { *msg = "DST tuning failed"; ctx_destroy(c); return rc; }
@@ -441,7 +443,7 @@ void ctx_destroy(Ctx* c) {
   if (c->solve_graph) cudaGraphDestroy(c->solve_graph);
   if (c->solve_exec_dense) cudaGraphExecDestroy(c->solve_exec_dense);
   for (PhaseGraph* ph : {&c->graph_pred, &c->graph_v2f, &c->graph_corr, &c->graph_fsi_rhs, &c->graph_fsi_asm,
-                         &c->graph_fsi_upd, &c->graph_fsi_loop})
+                         &c->graph_fsi_upd, &c->graph_fsi_loop, &c->graph_step})
     drop_phase(ph);
   if (c->solve_graph_dense) cudaGraphDestroy(c->solve_graph_dense);
   inf_free(c);
@@ -846,9 +848,10 @@ static int read_ist(Ctx* c) {
   return IB_OK;
 }
 
-// Adds a conditional (while) node after the current capture position of `st` and
-// returns its body graph.
-int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body) {
+// Adds a conditional node of the given type (while, if) after the current capture position of
+// `st` and returns its body graph.
+static int add_conditional(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                           cudaGraph_t* body) {
   cudaStreamCaptureStatus stat;
   cudaGraph_t capg;
   const cudaGraphNode_t* deps = nullptr;
@@ -857,13 +860,17 @@ int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body) 
   cudaGraphNodeParams pr = {};
   pr.type = cudaGraphNodeTypeConditional;
   pr.conditional.handle = h;
-  pr.conditional.type = cudaGraphCondTypeWhile;
+  pr.conditional.type = type;
   pr.conditional.size = 1;
   cudaGraphNode_t node;
   IB_CUDA_CHECK(cudaGraphAddNode(&node, capg, deps, nullptr, ndeps, &pr));
   IB_CUDA_CHECK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
   *body = pr.conditional.phGraph_out[0];
   return IB_OK;
+}
+
+int add_while(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body) {
+  return add_conditional(st, h, cudaGraphCondTypeWhile, body);
 }
 
 cudaGraph_t capture_graph(cudaStream_t st) {
@@ -1139,11 +1146,12 @@ __global__ void k_fsi_loop_init(int* cnt, int* band_flag, unsigned* done) {
 // them (the condition, the compaction), so the patches need no memsets; the end of the
 // iteration is one kernel (k_fsi_update).  The body's launches are counted once
 // (fsi_body_launches), the lists after the loop in fsi_post_launches.
-static int build_fsi_loop(Ctx* c) {
+// Adds the FSI iterations to the graph `st` is capturing (see build_fsi_loop).
+static int capture_fsi_loop(Ctx* c, cudaStream_t st) {
   const GridDims& g = c->g;
   const IbParams& p = c->p;
   Influence& I = c->inf;
-  cudaStream_t st = c->st, s1 = nullptr, s2 = nullptr, s3 = nullptr;
+  cudaStream_t s1 = nullptr, s2 = nullptr, s3 = nullptr;
   cudaEvent_t ev[5] = {};
   int rc = IB_OK;
   if (cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1153,11 +1161,8 @@ static int build_fsi_loop(Ctx* c) {
   for (int i = 0; i < 5 && rc == IB_OK; ++i)
     if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess) rc = IB_ERR_CUDA;
   cudaEvent_t ev_fork = ev[0], ev_rhs = ev[1], ev_lists = ev[2], ev_f = ev[3], ev_rd = ev[4];
-  cudaGraph_t graph = nullptr;
-  const long long l0 = launch_count();
   do {
     if (rc != IB_OK) break;
-    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
     count_launch();
     k_fsi_loop_init<<<1, 32, 0, st>>>(c->fsi_cnt, I.flag, c->fsi_done);
     cudaGraphConditionalHandle h = 0;
@@ -1237,22 +1242,33 @@ static int build_fsi_loop(Ctx* c) {
       rc = launch_reg_lists(c->nf, c->reg, g, st);
       c->fsi_post_launches = launch_count() - a0;
     }
-    if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
-    if (rc == IB_OK) {
-      make_edges_programmatic(body);
-      make_edges_programmatic(graph);
-    }
-    if (rc == IB_OK && cudaGraphInstantiate(&c->graph_fsi_loop.exec, graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+    if (rc == IB_OK) make_edges_programmatic(body);
   } while (false);
   c->st = st;
-  count_launches(-(launch_count() - l0));   // captured, not run
-  cudaGetLastError();
-  if (graph) cudaGraphDestroy(graph);
   for (cudaEvent_t e : ev)
     if (e) cudaEventDestroy(e);
   if (s3) cudaStreamDestroy(s3);
   if (s2) cudaStreamDestroy(s2);
   if (s1) cudaStreamDestroy(s1);
+  return rc;
+}
+
+// The FSI iterations of a step as a graph of their own.
+static int build_fsi_loop(Ctx* c) {
+  cudaStream_t st = c->st;
+  cudaGraph_t graph = nullptr;
+  const long long l0 = launch_count();
+  int rc = IB_OK;
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) rc = IB_ERR_CUDA;
+  if (rc == IB_OK) {
+    rc = capture_fsi_loop(c, st);
+    if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+  }
+  if (rc == IB_OK) make_edges_programmatic(graph);
+  if (rc == IB_OK && cudaGraphInstantiate(&c->graph_fsi_loop.exec, graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+  count_launches(-(launch_count() - l0));   // captured, not run
+  cudaGetLastError();
+  if (graph) cudaGraphDestroy(graph);
   if (rc != IB_OK) {
     if (c->graph_fsi_loop.exec) cudaGraphExecDestroy(c->graph_fsi_loop.exec);
     c->graph_fsi_loop.exec = nullptr;
@@ -1345,6 +1361,199 @@ int op_advance(Ctx* c) {
   return op_advance_finish(c);
 }
 
+// The correction on the finest grid (timestepper.F90:488-553) after the forces are known.
+static int op_correction(Ctx* c) {
+  const GridDims& g = c->g;
+  const int L = c->L;
+  if (c->nf > 0) {
+    // ainv of rot(E^T f): rot is formed as the x pass loads its rows (the face fields are
+    // read inside the stencil box only, which E^T writes wholly), and the input is zero
+    // outside the rows the stencils touch, so the forward transform runs on those rows
+    // only (the others' modes are zero).  The solve negates its right-hand side on load, so
+    // spec1 = -Y' (ainv's modes) exactly, and the inverse pass adds S_x(-Y') to omega_1 as
+    // it stores: omega_1 - vort in one pass.
+    RC(launch_reg_box(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
+    DstXArgs a;
+    a.in = c->hx; a.in2 = c->hy; a.box = c->reg.bbox; a.out = c->spec1; a.rowrange = c->reg.bbox + 4;
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_ROT, a, g, c->lx_small, c->st));
+    TriBc neg;
+    neg.post_scale = -1.0;
+    RC(tri_solve(c->tri_ainv, c->spec1, c->spec1, g.nsx, c->tl, c->st, neg));
+    DstXArgs b;
+    b.in = c->spec1; b.out = c->omega[0]; b.post_add = c->omega[0]; b.post_scale = 1.0;
+    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx, c->st));
+    // omega_1 was S_x Y (the predictor's modes, still in hat[0]): the corrected omega_1 has
+    // modes Y - Y' = hat[0] + spec1, which the finest level's solve forms as it loads them
+    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true,
+                        L >= 2 ? c->spec1 : nullptr);
+  }
+  RC(launch_reg(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
+  RC(launch_rot(g, c->hx, c->hy, c->vort, c->st));
+  RC(op_ainv(c, c->vort, c->vort));
+  RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], c->st));
+  if (L >= 2) RC(launch_sub(g.ns, c->hat[0], c->spec1, c->hat[0], c->st));
+  return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true);
+}
+
+// The stationary-body direct solve (timestepper.F90:457-490, num_stat): E q (less delta u_B
+// of a prescribed motion), the Cholesky solve and the redistribution.
+static int op_direct_solve(Ctx* c) {
+  const GridDims& g = c->g;
+  cudaStream_t st = c->st;
+  if (c->ub_on) {   // -delta u_B of a prescribed motion, then E q accumulated onto it
+    RC(launch_fill(c->nf, 0.0, c->rhsf, st));
+    RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, st));
+    RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, st));
+  } else {
+    RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, nullptr, c->rhsf, st));
+  }
+  RC(launch_chol_solve(c->nf, c->cholM, c->rhsf, c->f, st));
+  return op_redistribute(c, c->f, c->f_rdst);
+}
+
+// ------------------------------------------------------------------ the step as one graph
+// Opens the correction of a whole-step graph when the host FSI loop would add no iteration:
+// the device loop stopped at the tolerance or at the cap (timestepper.F90:318), not at a band
+// exit, and its residual is finite.  cnt[5] records the decision for the host.
+__global__ void k_step_gate(int* cnt, const double* err, double tol, int max_it, cudaGraphConditionalHandle h) {
+  IB_GRID_DEP_WAIT();
+  const double e = err[0];
+  const bool open = isfinite(e) && !(e >= tol && cnt[0] <= max_it);
+  cnt[5] = open ? 1 : 0;
+  cudaGraphSetConditional(h, open ? 1u : 0u);
+}
+
+// Which whole-step graph this step can run (0: none, the step runs phase by phase).  Mode 1
+// needs every condition of the device FSI loop; mode 2 is a step with no host decision in it.
+static int whole_step_mode(Ctx* c) {
+  const IbParams& p = c->p;
+  if (!c->use_whole_step || !c->use_step_graphs || c->prof_on || c->stage_on || c->step_prof ||
+      c->graph_step.failed || c->itime < 2)
+    return 0;
+  if (c->nf == 0 || (p.num_stat && c->chol_ready)) return 2;
+  if (p.num_stat) return 0;
+  const Influence& I = c->inf;
+  const bool loop = (c->nt > 0) && c->nbeam == 0 && p.schur_mode != 1 && c->use_fused && !c->graph_fsi_loop.failed &&
+                    c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
+  return loop ? 1 : 0;
+}
+
+// Captures graph_step for `mode`: the predictor and first vort2flux of a step after the
+// first (as graph_pred and graph_v2f), the forces, the correction (as graph_corr), and the
+// copies the host reads when the step ends: in mode 1 the FSI loop's counters, its residual
+// and the gate's decision, and the error word.
+static int build_step_graph(Ctx* c, int mode) {
+  const IbParams& p = c->p;
+  cudaStream_t st = c->st, sc = nullptr;
+  drop_phase(&c->graph_step);
+  c->step_corr = PhaseGraph{};
+  c->step_mode = mode;
+  int rc = cudaStreamCreateWithFlags(&sc, cudaStreamNonBlocking) == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+  cudaGraph_t graph = nullptr;
+  const long long l0 = launch_count();
+  long long p0[4], p1[4], l1 = l0, loop_launches = 0;
+  for (int i = 0; i < 4; ++i) p1[i] = p0[i] = c->n_pass[i];
+  const bool prof = c->prof_on;
+  do {
+    if (rc != IB_OK) break;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) { rc = IB_ERR_CUDA; break; }
+    rc = op_predict_levels(c, false);
+    if (rc == IB_OK)
+      rc = op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), false, true, true);
+    cudaGraphConditionalHandle h = 0;
+    if (rc == IB_OK && mode == 1) {
+      rc = launch_tors_save(c->nt, c->ts, st);
+      const long long b0 = launch_count();
+      Influence& I = c->inf;
+      const bool fresh = I.patch_fresh, active = I.active;
+      if (rc == IB_OK) rc = capture_fsi_loop(c, st);
+      I.patch_fresh = fresh;   // what the capture recorded on the host for an iteration it did not run
+      I.active = active;
+      loop_launches = launch_count() - b0;
+      if (rc == IB_OK &&
+          cudaGraphConditionalHandleCreate(&h, capture_graph(st), 0, cudaGraphCondAssignDefault) != cudaSuccess)
+        rc = IB_ERR_CUDA;
+      if (rc == IB_OK) {
+        count_launch();
+        k_step_gate<<<1, 1, 0, st>>>(c->fsi_cnt, c->err_fsi, p.fsi_tol, p.fsi_max_it, h);
+        if (cudaGetLastError() != cudaSuccess) rc = IB_ERR_CUDA;
+      }
+      if (rc == IB_OK &&
+          (cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 6 * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+           cudaMemcpyAsync(c->h_scal, c->err_fsi, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess))
+        rc = IB_ERR_CUDA;
+    } else if (rc == IB_OK && c->nf > 0) {
+      rc = op_direct_solve(c);
+    }
+    l1 = launch_count();
+    for (int i = 0; i < 4; ++i) p1[i] = c->n_pass[i];
+    if (rc == IB_OK && mode == 1) {
+      cudaGraph_t body = nullptr;
+      rc = add_conditional(st, h, cudaGraphCondTypeIf, &body);
+      if (rc == IB_OK && cudaStreamBeginCaptureToGraph(sc, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
+                             cudaSuccess)
+        rc = IB_ERR_CUDA;
+      if (rc == IB_OK) {
+        c->st = sc;
+        rc = op_correction(c);
+        c->st = st;
+        cudaGraph_t tmp;
+        if (cudaStreamEndCapture(sc, &tmp) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+        if (rc == IB_OK) make_edges_programmatic(body);
+      }
+    } else if (rc == IB_OK) {
+      rc = op_correction(c);
+    }
+    c->step_corr.launches = launch_count() - l1;
+    for (int i = 0; i < 4; ++i) c->step_corr.passes[i] = c->n_pass[i] - p1[i];
+    if (rc == IB_OK &&
+        cudaMemcpyAsync(c->h_ist + 12, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      rc = IB_ERR_CUDA;
+    if (cudaStreamEndCapture(st, &graph) != cudaSuccess && rc == IB_OK) rc = IB_ERR_CUDA;
+    if (rc == IB_OK) make_edges_programmatic(graph);
+    if (rc == IB_OK && cudaGraphInstantiate(&c->graph_step.exec, graph, 0) != cudaSuccess) rc = IB_ERR_CUDA;
+  } while (false);
+  c->st = st;
+  c->prof_on = prof;
+  c->graph_step.launches = (l1 - l0) - loop_launches;
+  for (int i = 0; i < 4; ++i) {
+    c->graph_step.passes[i] = p1[i] - p0[i];
+    c->n_pass[i] = p0[i];   // captured, not run
+  }
+  count_launches(-(launch_count() - l0));
+  cudaGetLastError();
+  if (graph) cudaGraphDestroy(graph);
+  if (sc) cudaStreamDestroy(sc);
+  if (rc != IB_OK) {
+    drop_phase(&c->graph_step);
+    c->graph_step.failed = true;
+  }
+  return rc;
+}
+
+// Launches graph_step when this step can run as one graph; false leaves the step to the phases.
+static bool launch_whole_step(Ctx* c) {
+  const int mode = whole_step_mode(c);
+  if (mode == 0) return false;
+  if ((!c->graph_step.exec || c->step_mode != mode) && build_step_graph(c, mode) != IB_OK) return false;
+  if (cudaGraphLaunch(c->graph_step.exec, c->st) != cudaSuccess) {
+    cudaGetLastError();
+    drop_phase(&c->graph_step);
+    c->graph_step.failed = true;
+    return false;
+  }
+  count_launches(c->graph_step.launches);
+  for (int i = 0; i < 4; ++i) c->n_pass[i] += c->graph_step.passes[i];
+  c->q0_partial = c->v2f_partial;
+  if (mode == 1) {
+    c->ksp_iter = 0;
+    c->gmres_reason = 0;
+    c->loop_pending = true;
+  }
+  c->step_pending = true;
+  return true;
+}
+
 int op_advance_begin(Ctx* c) {
   const GridDims& g = c->g;
   const int L = c->L;
@@ -1357,6 +1566,12 @@ int op_advance_begin(Ctx* c) {
   // timestepper.F90:76 factorises at it == 1 only, so a num_stat restart (istart > 0) would
   // solve with a matrix never factorised; here the first step of a context factorises.
   if (p.num_stat && c->nf > 0 && !c->chol_ready) RC(preprocess_chol(c));
+  if (launch_whole_step(c)) {
+    c->n_step_graph += 1;
+    c->end_pending = true;
+    return IB_OK;
+  }
+  c->n_step_phased += 1;
   step_mark(c, 0);
   // boundary values of the previous step (timestepper.F90:103-117) and the predictor, coarse
   // to fine (timestepper.F90:121-236)
@@ -1408,9 +1623,18 @@ int op_advance_end(Ctx* c) {
   if (!c->end_pending) return IB_ERR_STATE;
   c->end_pending = false;
   const GridDims& g = c->g;
-  const int L = c->L;
   const IbParams& p = c->p;
   cudaStream_t st = c->st;
+  const int L = c->L;
+  const bool whole = c->step_pending;
+  c->step_pending = false;
+  bool corr_done = false;
+  if (whole && c->step_mode == 2) {   // the whole step is on the stream: its error word comes at the finish
+    count_launches(c->step_corr.launches);
+    for (int i = 0; i < 4; ++i) c->n_pass[i] += c->step_corr.passes[i];
+    c->finish_pending = true;
+    return IB_OK;
+  }
   if (c->nf > 0) {
     if (!p.num_stat) {
       double err = 10.0;
@@ -1433,6 +1657,8 @@ int op_advance_end(Ctx* c) {
           I.assemblies += fsi_count;
           I.flag_h = c->h_ist[3] & 3;   // bit 4: a stencil left the rows of s computed (below)
           c->gmres_reason = std::min(c->gmres_reason, c->h_ist[4]);
+          corr_done = whole && c->h_ist[5] != 0;   // the gate opened the correction in graph_step
+          if (whole && !corr_done) c->n_step_gate_closed += 1;
           I.patch_fresh = true;
           I.active = false;
           err = c->h_scal[0];
@@ -1533,51 +1759,19 @@ int op_advance_end(Ctx* c) {
       // fsi_tol; the reference carries on silently, this step reports it (after finishing)
       c->fsi_err_capped = err >= p.fsi_tol ? err : 0.0;
     } else {
-      if (c->ub_on) {   // -delta u_B of a prescribed motion, then E q accumulated onto it
-        RC(launch_fill(c->nf, 0.0, c->rhsf, st));
-        RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, st));
-        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, st));
-      } else {
-        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, nullptr, c->rhsf, st));
-      }
-      RC(launch_chol_solve(c->nf, c->cholM, c->rhsf, c->f, st));
-      RC(op_redistribute(c, c->f, c->f_rdst));
+      RC(op_direct_solve(c));
     }
   }
   // correction on the finest grid (timestepper.F90:488-553)
   step_mark(c, 8);
-  RC(run_phase(c, c->graph_corr, [&]() -> int {
-    if (c->nf > 0) {
-      // ainv of rot(E^T f): rot is formed as the x pass loads its rows (the face fields are
-      // read inside the stencil box only, which E^T writes wholly), and the input is zero
-      // outside the rows the stencils touch, so the forward transform runs on those rows
-      // only (the others' modes are zero).  The solve negates its right-hand side on load, so
-      // spec1 = -Y' (ainv's modes) exactly, and the inverse pass adds S_x(-Y') to omega_1 as
-      // it stores: omega_1 - vort in one pass.
-      RC(launch_reg_box(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
-      DstXArgs a;
-      a.in = c->hx; a.in2 = c->hy; a.box = c->reg.bbox; a.out = c->spec1; a.rowrange = c->reg.bbox + 4;
-      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_ROT, a, g, c->lx_small, c->st));
-      TriBc neg;
-      neg.post_scale = -1.0;
-      RC(tri_solve(c->tri_ainv, c->spec1, c->spec1, g.nsx, c->tl, c->st, neg));
-      DstXArgs b;
-      b.in = c->spec1; b.out = c->omega[0]; b.post_add = c->omega[0]; b.post_scale = 1.0;
-      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx, c->st));
-      // omega_1 was S_x Y (the predictor's modes, still in hat[0]): the corrected omega_1 has
-      // modes Y - Y' = hat[0] + spec1, which the finest level's solve forms as it loads them
-      return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true,
-                          L >= 2 ? c->spec1 : nullptr);
-    }
-    RC(launch_reg(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
-    RC(launch_rot(g, c->hx, c->hy, c->vort, c->st));
-    RC(op_ainv(c, c->vort, c->vort));
-    RC(launch_sub(g.ns, c->omega[0], c->vort, c->omega[0], c->st));
-    if (L >= 2) RC(launch_sub(g.ns, c->hat[0], c->spec1, c->hat[0], c->st));
-    return op_vort2flux(c, c->omega.data(), c->s.data(), c->qx.data(), c->qy.data(), true, L >= 2, true);
-  }));
-  step_mark(c, 9);
-  IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist + 12, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (corr_done) {   // graph_step has run it and copied the error word
+    count_launches(c->step_corr.launches);
+    for (int i = 0; i < 4; ++i) c->n_pass[i] += c->step_corr.passes[i];
+  } else {
+    RC(run_phase(c, c->graph_corr, [&]() { return op_correction(c); }));
+    step_mark(c, 9);
+    IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist + 12, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  }
   c->finish_pending = true;
   return IB_OK;
 }

@@ -42,7 +42,7 @@ EXPORTS = [
     "ib_schur_matrix", "ib_get_influence_stats", "ib_step_profile", "ib_get_launch_shapes",
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
-    "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state",
+    "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state", "ib_get_step_graph_stats",
 ]
 
 
@@ -415,6 +415,13 @@ class Simulation:
         _check(self.lib.ib_get_influence_stats(self.h, counts, C.byref(ms)), "ib_get_influence_stats")
         return {"builds": counts[0], "columns": counts[1], "assemblies": counts[2], "fallbacks": counts[3],
                 "band_vertices": counts[4], "build_ms": ms.value}
+
+    def step_graph_stats(self) -> dict:
+        """How the steps ran: as one graph, of those with the FSI loop finished from the host,
+        and phase by phase."""
+        counts = (C.c_longlong * 3)()
+        _check(self.lib.ib_get_step_graph_stats(self.h, counts), "ib_get_step_graph_stats")
+        return {"graph": counts[0], "gate_closed": counts[1], "phased": counts[2]}
 
     def profile(self, enable: bool):
         _check(self.lib.ib_profile(self.h, int(bool(enable))), "ib_profile")

@@ -277,6 +277,14 @@ int ib_schur_matrix(IbCtx* ctx, double* S, int* status);
 /* influence-matrix work since creation: counts = {band builds, columns computed, assemblies,
  * matrix-free fallbacks, band vertices}, build_ms = host wall time of the builds */
 int ib_get_influence_stats(IbCtx* ctx, long long* counts, double* build_ms);
+/* How the steps since creation ran (no reference counterpart: the reference's advance,
+ * timestepper.F90:18-556, is one host routine).  counts[3] = {steps launched as one CUDA graph
+ * (predictor, first vort2flux, forces, correction: from the second step on, when the FSI
+ * iterations run in the device loop, the forces come from the direct solve, or there is no
+ * body), of those the steps whose device FSI loop left the influence band with iterations
+ * still to run (the host took over the loop and ran the correction), steps run phase by
+ * phase}.  The environment variable IB_WHOLE_STEP=0 at ib_create turns the one-graph step off. */
+int ib_get_step_graph_stats(IbCtx* ctx, long long* counts);
 /* enable (1) / disable (0) CUDA-event timing of each DST pass launch; enabling clears the totals */
 int ib_profile(IbCtx* ctx, int enable);
 /* work done since creation: Schur matvecs and DST passes by kind (0..3, see below) */
