@@ -248,6 +248,66 @@ int ib_write_variables(IbCtx* h, const char* path) {
   return rc == IB_OK ? IB_OK : fail(rc, ("write_variables: " + msg).c_str());
 }
 
+int ib_subdomain_setup(IbCtx* h, int full_rectangular, double sdxi, double sdxe, double sdyi, double sdye,
+                       double delta_sd) {
+  CTX_OR_FAIL(h);
+  std::string msg;
+  int rc = ib::sd_setup(c, full_rectangular, sdxi, sdxe, sdyi, sdye, delta_sd, &msg);
+  return rc == IB_OK ? IB_OK : fail(rc, ("subdomain_setup: " + msg).c_str());
+}
+
+int ib_subdomain_precompute(IbCtx* h) {
+  CTX_OR_FAIL(h);
+  if (!c->sd.on) return fail(IB_ERR_STATE, "subdomain_precompute: no sub-domain set up");
+  return op_result(ib::sd_precompute(c), "subdomain_precompute failed");
+}
+
+int ib_write_subdomain_matrix(IbCtx* h, const char* path) {
+  CTX_OR_FAIL(h);
+  if (!path) return fail(IB_ERR_ARG, "null path");
+  std::string msg;
+  int rc = ib::sd_write(c, path, &msg);
+  return rc == IB_OK ? IB_OK : fail(rc, ("write_subdomain_matrix: " + msg).c_str());
+}
+
+int ib_read_subdomain_matrix(IbCtx* h, const char* path) {
+  CTX_OR_FAIL(h);
+  if (!path) return fail(IB_ERR_ARG, "null path");
+  std::string msg;
+  int rc = ib::sd_read(c, path, &msg);
+  return rc == IB_OK ? IB_OK : fail(rc, ("read_subdomain_matrix: " + msg).c_str());
+}
+
+int ib_subdomain_operator(IbCtx* h, double* lumat) {
+  CTX_OR_FAIL(h);
+  if (!lumat) return fail(IB_ERR_ARG, "bad argument");
+  if (!c->sd.on) return fail(IB_ERR_STATE, "subdomain_operator: no sub-domain set up");
+  int rc = c->sd.ready ? IB_OK : ib::sd_precompute(c);
+  if (rc == IB_OK) rc = ib::sd_assemble(c, true);
+  if (rc == IB_OK) c->inf.active = true;
+  const size_t nf = (size_t)c->nf;
+  std::vector<double> St(nf * nf);
+  if (rc == IB_OK && (cudaMemcpyAsync(St.data(), c->inf.St, 8 * nf * nf, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+                      cudaStreamSynchronize(c->st) != cudaSuccess))
+    rc = IB_ERR_CUDA;
+  if (rc == IB_OK) rc = ib::check_err(c);
+  if (rc != IB_OK) return op_result(rc, "subdomain_operator failed");
+  for (size_t k = 0; k < nf; ++k)
+    for (size_t l = 0; l < nf; ++l) lumat[k * nf + l] = St[l * nf + k];
+  return IB_OK;
+}
+
+int ib_get_subdomain_stats(IbCtx* h, long long* counts, double* precompute_ms) {
+  CTX_OR_FAIL(h);
+  if (!counts || !precompute_ms) return fail(IB_ERR_ARG, "bad argument");
+  counts[0] = c->sd.nf_sd;
+  counts[1] = c->sd.candidates;
+  counts[2] = c->sd.kept;
+  counts[3] = c->sd.columns;
+  *precompute_ms = c->sd.precompute_ms;
+  return IB_OK;
+}
+
 int ib_read_variables(IbCtx* h, const char* path, int itime) {
   CTX_OR_FAIL(h);
   if (!path) return fail(IB_ERR_ARG, "null path");

@@ -121,6 +121,45 @@ inline void drop_phase(PhaseGraph* ph) {
   *ph = PhaseGraph{};
 }
 
+// The sub-domain precomputed-Schur method (sub_domain = T): a cloud of sub-domain points (the
+// stationary rigid bodies' points, then a rectangle at spacing dsd), the fluid Schur operator B
+// between them precomputed column by column on E E^T's sparsity and thinned by a drop
+// tolerance, and per FSI iteration lumat = body + P B^T P^T with P bilinear interpolation from
+// the sub-domain unknowns to the body unknowns.
+struct SubDomain {
+  bool on = false, ready = false, full_rect = true;
+  double sdxi = 0, sdxe = 0, sdyi = 0, sdye = 0, dsd = 0;
+  int nx = 0, ny = 0, nr_sd = 0, nb_sd = 0, nf_sd = 0;
+  double* ux = nullptr;          // nf_sd positions (x components, then y components)
+  double* uy = nullptr;
+  int* ucomp = nullptr;
+  RegDev reg{};                  // E_o: origins, weights, contribution lists of every unknown
+  // candidate rows of each point's columns (point indices ascending, CSR over points), and the
+  // point's own slot in its list
+  int* cptr = nullptr;
+  int* cidx = nullptr;
+  int* cself = nullptr;
+  int max_cand = 0;
+  // B column-compressed after the drop: column j holds nz[j] rows (ascending) from colptr[j]
+  long long* colptr = nullptr;
+  int* nz = nullptr;
+  int* rows = nullptr;
+  double* vals = nullptr;
+  // P of the body unknowns: 4 sub-domain unknowns and weights each; rigid[k] >= 0 maps a
+  // stationary rigid body's unknown onto its own sub-domain point exactly
+  int* rigid = nullptr;
+  int* pidx = nullptr;
+  double* pw = nullptr;
+  double* eq = nullptr;          // E_o (q + q0) on every sub-domain unknown
+  double* fsd = nullptr;         // P^T f
+  // precompute scratch per column set: the patch's 64 vertices, the candidate values
+  int* pprev = nullptr;
+  double* colbuf = nullptr;
+  void* mem = nullptr;           // the fixed-size buffers above, one allocation
+  long long candidates = 0, kept = 0, columns = 0;
+  double precompute_ms = 0;
+};
+
 struct Ctx {
   IbParams p{};
   GridDims g{};
@@ -188,6 +227,7 @@ struct Ctx {
   double* ub = nullptr;
   bool ub_on = false;
   PressureOp pres;
+  SubDomain sd;
   // family-3 beams (beam.cu)
   int nbeam = 0;
   BeamDev* beams = nullptr;
@@ -336,6 +376,18 @@ int op_pressure(Ctx* c);
 void pressure_free(Ctx* c);
 int op_time_pressure_transform(Ctx* c, bool mma, int reps, double* avg_ms);
 int op_write_pressure(Ctx* c, const char* path, std::string* msg);
+// subdomain.cu: the sub-domain method (grid.F90:572-951, timestepper.F90:368-405, 602-770,
+// operators_struct.F90:840-905)
+int sd_setup(Ctx* c, int full_rectangular, double sdxi, double sdxe, double sdyi, double sdye, double dsd,
+             std::string* msg);
+int sd_precompute(Ctx* c);
+int sd_assemble(Ctx* c, bool interp);                     // (P at the current positions,) lumat into inf.St
+int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st); // rhsf = P E_o (q + q0) + rhsf
+int launch_sd_spread(Ctx* c, const double* f, double* hx, double* hy, cudaStream_t st);   // E_o^T P^T f
+int sd_write(Ctx* c, const char* path, std::string* msg);
+int sd_read(Ctx* c, const char* path, std::string* msg);
+void sd_free(Ctx* c);
+int inf_build_scratch(Ctx* c);
 // solver.cu: a time step in three parts (op_advance runs them in a row)
 int op_advance_begin(Ctx* c);
 int op_advance_end(Ctx* c);

@@ -317,8 +317,9 @@ static void free_band(Influence& I) {
   I.capK = I.capR = 0;
 }
 
-// The band build's scratch sets and streams (made on the first build, kept for rebuilds).
-static int build_scratch(Ctx* c) {
+// The band build's scratch sets and streams (made on the first build, kept for rebuilds; the
+// sub-domain precompute runs its columns on the same sets).
+int inf_build_scratch(Ctx* c) {
   Influence& I = c->inf;
   if (!I.bscr.empty()) return IB_OK;
   const GridDims& g = c->g;
@@ -471,7 +472,7 @@ int inf_build(Ctx* c) {
   // vector, scratch fields and output rows), after the work already on the context's stream.
   // Each set's columns run as one captured graph: a while node whose body is one column with
   // the column index on the device, so the host launches one graph per set.
-  RC(build_scratch(c));
+  RC(inf_build_scratch(c));
   cudaStream_t st = c->st;
   const int S = std::min(Influence::kBuildStreams, I.nR);
   cudaEvent_t ev = nullptr;

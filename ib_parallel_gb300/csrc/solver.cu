@@ -449,6 +449,7 @@ void ctx_destroy(Ctx* c) {
   inf_free(c);
   pressure_free(c);
   beam_free(c);
+  sd_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -1372,9 +1373,12 @@ static int op_correction(Ctx* c) {
     // only (the others' modes are zero).  The solve negates its right-hand side on load, so
     // spec1 = -Y' (ainv's modes) exactly, and the inverse pass adds S_x(-Y') to omega_1 as
     // it stores: omega_1 - vort in one pass.
-    RC(launch_reg_box(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
+    // the sub-domain method spreads E_o^T P^T f instead (timestepper.F90:500-516)
+    const int* box = c->sd.on ? c->sd.reg.bbox : c->reg.bbox;
+    if (c->sd.on) RC(launch_sd_spread(c, c->f, c->hx, c->hy, c->st));
+    else RC(launch_reg_box(g, c->nf, c->f, c->reg, c->hx, c->hy, c->st));
     DstXArgs a;
-    a.in = c->hx; a.in2 = c->hy; a.box = c->reg.bbox; a.out = c->spec1; a.rowrange = c->reg.bbox + 4;
+    a.in = c->hx; a.in2 = c->hy; a.box = box; a.out = c->spec1; a.rowrange = box + 4;
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_ROT, a, g, c->lx_small, c->st));
     TriBc neg;
     neg.post_scale = -1.0;
@@ -1433,7 +1437,8 @@ static int whole_step_mode(Ctx* c) {
   if (c->nf == 0 || (p.num_stat && c->chol_ready)) return 2;
   if (p.num_stat) return 0;
   const Influence& I = c->inf;
-  const bool loop = (c->nt > 0) && c->nbeam == 0 && p.schur_mode != 1 && c->use_fused && !c->graph_fsi_loop.failed &&
+  const bool loop = (c->nt > 0) && c->nbeam == 0 && !c->sd.on && p.schur_mode != 1 && c->use_fused &&
+                    !c->graph_fsi_loop.failed &&
                     c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
   return loop ? 1 : 0;
 }
@@ -1566,6 +1571,8 @@ int op_advance_begin(Ctx* c) {
   // timestepper.F90:76 factorises at it == 1 only, so a num_stat restart (istart > 0) would
   // solve with a matrix never factorised; here the first step of a context factorises.
   if (p.num_stat && c->nf > 0 && !c->chol_ready) RC(preprocess_chol(c));
+  // preprocess_sd (timestepper.F90:79-97): B at the first step unless it was read from a file
+  if (c->sd.on && !c->sd.ready) RC(sd_precompute(c));
   if (launch_whole_step(c)) {
     c->n_step_graph += 1;
     c->end_pending = true;
@@ -1603,7 +1610,7 @@ int op_advance_begin(Ctx* c) {
       {
         Influence& I = c->inf;
         const bool device_loop = moved && p.schur_mode != 1 && c->use_step_graphs && c->use_fused && !c->prof_on &&
-                                 !c->stage_on && (!c->step_prof || c->step_prof_dev) && c->nbeam == 0 &&
+                                 !c->stage_on && (!c->step_prof || c->step_prof_dev) && c->nbeam == 0 && !c->sd.on &&
                                  !c->graph_fsi_loop.failed &&
                                  c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
         if (device_loop && (c->graph_fsi_loop.exec || build_fsi_loop(c) == IB_OK)) {
@@ -1683,6 +1690,8 @@ int op_advance_end(Ctx* c) {
           RC(launch_beam_rhs(c, c->rhsf, c->st));
           // prescribed rigid-body motion (timestepper.F90:327-331): rhsf - delta u_B
           if (c->ub_on) RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, c->st));
+          // sub-domain method (timestepper.F90:371-395): P E_o (q + q0) added to the structure's
+          if (c->sd.on) return launch_sd_rhs(c, c->rhsf, c->st);
           return launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, c->st);
         }));
         step_mark(c, 4);
@@ -1690,7 +1699,12 @@ int op_advance_end(Ctx* c) {
         // it (checked at the end of the previous iteration) -> the captured assembly; else
         // the host path (build / rebuild / matrix-free fallback)
         Influence& I = c->inf;
-        if (p.schur_mode != 1 && I.built && I.patch_fresh && I.flag_h == 0) {
+        if (c->sd.on) {
+          // compute_operator (timestepper.F90:377): lumat = body_mat + P B^T P^T, P as the
+          // right-hand side formed it (the same positions)
+          RC(sd_assemble(c, false));
+          I.active = true;
+        } else if (p.schur_mode != 1 && I.built && I.patch_fresh && I.flag_h == 0) {
           RC(run_phase(c, c->graph_fsi_asm, [&]() { return inf_assemble(c); }));
           I.assemblies += 1;
           I.active = true;

@@ -43,6 +43,8 @@ EXPORTS = [
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
     "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state", "ib_get_step_graph_stats",
+    "ib_subdomain_setup", "ib_subdomain_precompute", "ib_write_subdomain_matrix", "ib_read_subdomain_matrix",
+    "ib_subdomain_operator", "ib_get_subdomain_stats",
 ]
 
 
@@ -133,6 +135,13 @@ def load(path: Optional[os.PathLike] = None):
         "ib_batch_advance": ([P, I], C.c_int),
         "ib_calculate_pressure": ([P, P], C.c_int), "ib_write_pressure": ([P, C.c_char_p], C.c_int),
         "ib_get_beam_state": ([P, P, P, P], C.c_int),
+        "ib_get_step_graph_stats": ([P, C.POINTER(C.c_longlong)], C.c_int),
+        "ib_subdomain_setup": ([P, C.c_int] + [C.c_double] * 5, C.c_int),
+        "ib_subdomain_precompute": ([P], C.c_int),
+        "ib_write_subdomain_matrix": ([P, C.c_char_p], C.c_int),
+        "ib_read_subdomain_matrix": ([P, C.c_char_p], C.c_int),
+        "ib_subdomain_operator": ([P, P], C.c_int),
+        "ib_get_subdomain_stats": ([P, C.POINTER(C.c_longlong), D], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -415,6 +424,36 @@ class Simulation:
         _check(self.lib.ib_get_influence_stats(self.h, counts, C.byref(ms)), "ib_get_influence_stats")
         return {"builds": counts[0], "columns": counts[1], "assemblies": counts[2], "fallbacks": counts[3],
                 "band_vertices": counts[4], "build_ms": ms.value}
+
+    # ---- the sub-domain precomputed-Schur method (sub_domain = T)
+    def subdomain_setup(self, sdxi: float, sdxe: float, sdyi: float, sdye: float, delta_sd: float,
+                        full_rectangular: bool = True) -> None:
+        """Switches the context to the sub-domain method (before its first step)."""
+        _check(self.lib.ib_subdomain_setup(self.h, int(bool(full_rectangular)), C.c_double(sdxi),
+                                           C.c_double(sdxe), C.c_double(sdyi), C.c_double(sdye),
+                                           C.c_double(delta_sd)), "ib_subdomain_setup")
+
+    def subdomain_precompute(self) -> None:
+        _check(self.lib.ib_subdomain_precompute(self.h), "ib_subdomain_precompute")
+
+    def write_subdomain_matrix(self, path) -> None:
+        _check(self.lib.ib_write_subdomain_matrix(self.h, str(path).encode()), "ib_write_subdomain_matrix")
+
+    def read_subdomain_matrix(self, path) -> None:
+        _check(self.lib.ib_read_subdomain_matrix(self.h, str(path).encode()), "ib_read_subdomain_matrix")
+
+    def subdomain_operator(self) -> np.ndarray:
+        """body + P B^T P^T at the current positions (nf x nf)."""
+        out = np.zeros((self.nf, self.nf))
+        _check(self.lib.ib_subdomain_operator(self.h, _ptr(out)), "ib_subdomain_operator")
+        return out
+
+    def subdomain_stats(self) -> dict:
+        counts = (C.c_longlong * 4)()
+        ms = C.c_double()
+        _check(self.lib.ib_get_subdomain_stats(self.h, counts, C.byref(ms)), "ib_get_subdomain_stats")
+        return {"unknowns": counts[0], "candidates": counts[1], "kept": counts[2], "columns": counts[3],
+                "precompute_ms": ms.value}
 
     def step_graph_stats(self) -> dict:
         """How the steps ran: as one graph, of those with the FSI loop finished from the host,

@@ -132,6 +132,35 @@ int ib_read_body(const char* path, IbBody* body, double* x, double* y, int cap);
 /* The bodies of an input directory (grid.F90:252-260): body.001.inp, body.002.inp, ... up to the
  * first number that has no file. */
 int ib_count_bodies(const char* dir, int* nbody);
+/* The sub-domain precomputed-Schur method (sub_domain = T: grid.F90:320-352, 572-951;
+ * timestepper.F90:79-97, 368-405, 500-516, 602-770; operators_struct.F90:840-980), switched on
+ * for a context before its first step (and before ib_read_variables on a restart).  The cloud:
+ * with full_rectangular = 0 the stationary rigid bodies' points first (point p of the rigid
+ * bodies in file order is sub-domain point p; the reference assumes one such body), then the
+ * rectangle [sdxi, sdxe] x [sdyi, sdye] at spacing delta_sd, nint((sdxe-sdxi)/delta_sd + 1)
+ * points along x.  The fluid Schur operator between the cloud's unknowns, B, is computed at the
+ * first step (or read by ib_read_subdomain_matrix) on E E^T's sparsity (21 x 21 face blocks that
+ * meet) and thinned by the drop tolerance |B_ij| > 7.0e-3 B_jj; every FSI iteration then solves
+ * with body + P B^T P^T, P bilinear interpolation from the cloud to the body points.  Every
+ * cloud point's 21 x 21 block must lie inside the grid (the reference indexes it without bounds
+ * checks), num_stat must be 0, and a body that leaves the cloud ends its step with
+ * IB_ERR_DOMAIN (the reference stops). */
+int ib_subdomain_setup(IbCtx* ctx, int full_rectangular, double sdxi, double sdxe, double sdyi, double sdye,
+                       double delta_sd);
+/* preprocess_sd's column loop now rather than at the first step. */
+int ib_subdomain_precompute(IbCtx* ctx);
+/* The thinned B in the reference's input/sd_precomputed.chd layout (Fortran unformatted
+ * sequential, per column a record of its count, then one of its values and 1-based rows). */
+int ib_write_subdomain_matrix(IbCtx* ctx, const char* path);
+/* sub_domain_precomputed = T: B read from such a file (same cloud) instead of computed. */
+int ib_read_subdomain_matrix(IbCtx* ctx, const char* path);
+/* lumat = body_mat + P B^T P^T at the current body positions (nf x nf, row-major), the matrix
+ * the FSI iteration solves with (computing B first if needed). */
+int ib_subdomain_operator(IbCtx* ctx, double* lumat);
+/* counts[4] = {cloud unknowns nf_sd, candidate entries of B (E E^T's sparsity), entries kept
+ * after the drop tolerance, columns computed}; *precompute_ms = host wall time of the column
+ * loops. */
+int ib_get_subdomain_stats(IbCtx* ctx, long long* counts, double* precompute_ms);
 /* write_variables (variables.F90:709-803): the restart file output/dataRR_IIIIIII.var of one
  * rank at path, in the reference's Fortran unformatted layout (4-byte record markers, 4-byte
  * integers, 8-byte reals; the layout output/getdata.m reads). */

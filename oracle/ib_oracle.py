@@ -213,6 +213,7 @@ class IBOracle:
         self.ksp_iter = 0
         self.fsi_iter = 0
         self.cholM = None
+        self.sd = None   # ib_subdomain.SubDomain: the sub-domain method (sub_domain = T)
 
     # ----------------------------------------------------------- myfft.F90
     def _setup_fft(self):
@@ -435,53 +436,67 @@ class IBOracle:
                 xbf0=float(b.x[0]), ybf0=float(b.y[0])))
         self.setup_reg()
 
-    def setup_reg(self):
-        """grid.F90:459-528: stencil indices and weights of E for the current
-        body positions.  weight = delta*delta*d(x)*d(y), l (y offset) outer,
-        p (x offset) inner, exactly as the source loops."""
+    def reg_weights(self, xb, yb, comp):
+        """grid.F90:459-528 (and setup_pre_reg_subdomain, grid.F90:627-693, for the sub-domain
+        points): stencil face indices and weights of points at (xb, yb) with components comp
+        (1 = x on u-faces, 2 = y on v-faces).  weight = delta*delta*d(x)*d(y), l (y offset)
+        outer, p (x offset) inner, exactly as the source loops."""
         d, ox, oy, m = self.delta, self.p.offsetx, self.p.offsety, self.m
         d2 = 0.5 * d
-        ix = ((self.xb + ox) / d).astype(np.int64) + 1      # Fortran INT truncation
-        iy = ((self.yb + oy) / d).astype(np.int64) + 1
+        ix = ((xb + ox) / d).astype(np.int64) + 1      # Fortran INT truncation
+        iy = ((yb + oy) / d).astype(np.int64) + 1
         off = np.arange(-3, 4)
-        xs = (self.comp == 1)[:, None]
+        xs = (comp == 1)[:, None]
         # grid coordinates of the 7 stencil columns / rows for each unknown
         gx = d * (ix[:, None] - 1 + off[None, :]) - ox
         gx = np.where(xs, gx, gx + d2)
         gy = d * (iy[:, None] - 1 + off[None, :]) - oy
         gy = np.where(xs, gy + d2, gy)
-        dxv = deltafnc_vec(gx, self.xb[:, None], d)          # (nf, 7) over p
-        dyv = deltafnc_vec(gy, self.yb[:, None], d)          # (nf, 7) over l
+        dxv = deltafnc_vec(gx, xb[:, None], d)          # (nf, 7) over p
+        dyv = deltafnc_vec(gy, yb[:, None], d)          # (nf, 7) over l
         w = (d * d * dxv[:, None, :]) * dyv[:, :, None]      # (nf, l, p)
         fi = ix[:, None, None] + off[None, None, :]           # face i
         fj = iy[:, None, None] + off[None, :, None]           # face j
         idx = np.where(xs[:, :, None], (m + 1) * (fj - 1) + (fi - 1), m * (fj - 1) + (fi - 1))
-        self.reg_idx = idx.reshape(self.nf, 49)
-        self.reg_w = w.reshape(self.nf, 49)
+        return idx.reshape(len(xb), 49), w.reshape(len(xb), 49)
 
-    def reg(self, h0):
-        """fsinterface.F90:14-47: E^T, scatter-add in body-point order."""
+    def setup_reg(self):
+        """grid.F90:459-528: stencil indices and weights of E for the current body positions."""
+        self.reg_idx, self.reg_w = self.reg_weights(self.xb, self.yb, self.comp)
+
+    def reg_with(self, idx, w, comp, h0):
+        """fsinterface.F90:14-47 (reg_sd_sparse, fsinterface.F90:84-126, with the sub-domain's
+        weights): E^T, scatter-add in unknown order."""
         m, n = self.m, self.n
         hx = np.zeros((n, m + 1)).ravel()
         hy = np.zeros((n + 1, m)).ravel()
-        xs = self.comp == 1
-        vals = self.reg_w * h0[:, None]
-        np.add.at(hx, self.reg_idx[xs].ravel(), vals[xs].ravel())
-        np.add.at(hy, self.reg_idx[~xs].ravel(), vals[~xs].ravel())
+        xs = comp == 1
+        vals = w * h0[:, None]
+        np.add.at(hx, idx[xs].ravel(), vals[xs].ravel())
+        np.add.at(hy, idx[~xs].ravel(), vals[~xs].ravel())
         return hx.reshape(n, m + 1), hy.reshape(n + 1, m)
 
-    def regT(self, hx, hy, h0=None):
-        """fsinterface.F90:51-80: E, gathered and accumulated into h0 in stencil
-        order (slot by slot, so each unknown sees the source's summation order)."""
-        h0 = np.zeros(self.nf) if h0 is None else h0.copy()
+    def regT_with(self, idx, w, comp, hx, hy, h0=None):
+        """fsinterface.F90:51-80 (regT_sd_sparse, fsinterface.F90:130-161, with the
+        sub-domain's weights): E, gathered and accumulated into h0 in stencil order (slot by
+        slot, so each unknown sees the source's summation order)."""
+        h0 = np.zeros(len(comp)) if h0 is None else h0.copy()
         fx, fy = hx.ravel(), hy.ravel()
-        xs = self.comp == 1
+        xs = comp == 1
         acc = h0
         for t in range(49):
-            idx = self.reg_idx[:, t]
-            src = np.where(xs, fx[np.where(xs, idx, 0)], fy[np.where(xs, 0, idx)])
-            acc = acc + self.reg_w[:, t] * src
+            ix = idx[:, t]
+            src = np.where(xs, fx[np.where(xs, ix, 0)], fy[np.where(xs, 0, ix)])
+            acc = acc + w[:, t] * src
         return acc
+
+    def reg(self, h0):
+        """fsinterface.F90:14-47: E^T, scatter-add in body-point order."""
+        return self.reg_with(self.reg_idx, self.reg_w, self.comp, h0)
+
+    def regT(self, hx, hy, h0=None):
+        """fsinterface.F90:51-80: E, gathered in stencil order."""
+        return self.regT_with(self.reg_idx, self.reg_w, self.comp, hx, hy, h0)
 
     def redistribute(self, f):
         """operators_struct.F90:735-834."""
@@ -886,8 +901,21 @@ class IBOracle:
             self.thetadd0 = self.thetadd.copy()
             for bm in self.beams:
                 bm.save()
+            if self.sd is not None and self.sd.cols is None:
+                self.sd.precompute()   # preprocess_sd at the first step (timestepper.F90:79-97)
             while err >= p.fsi_tol and fsi_count <= 1000:
                 fsi_count += 1
+                if self.sd is not None:
+                    # timestepper.F90:368-405: lumat = body_mat + P B^T P^T, rhsf + P E_o q
+                    pidx, pw = self.sd.interp()
+                    rhsf = self.sd.rhs_add(self.compute_rhs() - self.delta * self.ub, qhx, qhy, pidx, pw)
+                    lu = self.sd.lumat(pidx, pw)
+                    self.f, its, _ = self.gmres(rhsf, self.f, lambda x, lu=lu: lu @ x)
+                    self.ksp_iter += its
+                    self.f_rdst = self.redistribute(self.f)
+                    err = self.compute_dx(self.f)
+                    self.setup_reg()
+                    continue
                 # compute_rhs, then rhsf - delta u_B (timestepper.F90:323-331), then E q on top
                 rhsf = self.regT(qhx, qhy, self.compute_rhs() - self.delta * self.ub)
                 self.f, its, _ = self.gmres(rhsf, self.f, self.a_times)
@@ -900,7 +928,11 @@ class IBOracle:
             rhsf = self.regT(qhx, qhy, 0.0 - self.delta * self.ub)
             self.f = self.chol_solve(rhsf)
             self.f_rdst = self.redistribute(self.f)
-        hx, hy = self.reg(self.f) if self.nf else (np.zeros_like(self.qx[0]), np.zeros_like(self.qy[0]))
+        if self.sd is not None and self.nf and not p.num_stat:
+            pidx, pw = self.sd.interp()
+            hx, hy = self.sd.spread(self.f, pidx, pw)   # timestepper.F90:500-516
+        else:
+            hx, hy = self.reg(self.f) if self.nf else (np.zeros_like(self.qx[0]), np.zeros_like(self.qy[0]))
         vort = self.ainv(self.rot(hx, hy))
         self.omega[0] = self.omega[0] - vort
         self.s, self.qx, self.qy = self.vort2flux(self.omega)

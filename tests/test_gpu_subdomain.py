@@ -1,0 +1,156 @@
+"""The sub-domain precomputed-Schur method on the GPU against the oracle's restatement
+(oracle/ib_subdomain.py): B column by column with the same pattern after the drop tolerance,
+the FSI operator lumat = body + P B^T P^T, the sd_precomputed.chd file both ways, steps
+conditional on the Krylov solve (one FSI iteration a step, the oracle handed the GPU's forces),
+free-running steps, a stationary rigid body inside the cloud, and a body leaving the cloud."""
+import numpy as np
+import pytest
+
+import ib_oracle as O
+import ib_subdomain as SD
+from helpers import PLATE, SMALL, pair, rel, small_plate
+from ib_parallel_gb300 import geometry as GEO
+from ib_parallel_gb300 import ibgpu as G
+
+pytestmark = pytest.mark.gpu
+
+CLOUD = (-0.25, 1.25, -0.25, 0.25, 0.0625)   # sdxi, sdxe, sdyi, sdye, delta_sd
+RIGID_CLOUD = (-0.75, 1.0, -0.625, 0.625, 0.125)
+
+
+def _setup(o, g, cloud, full_rect=True):
+    g.subdomain_setup(*cloud, full_rectangular=full_rect)
+    o.sd = SD.SubDomain(o, full_rect, *cloud)
+
+
+def _compare_matrices(sd_gpu_cols, sd_oracle):
+    for j, ((rg, vg), (ro, vo)) in enumerate(zip(sd_gpu_cols, sd_oracle.cols)):
+        assert np.array_equal(rg, ro), j
+        assert rel(vg, vo) < 1e-11, (j, rel(vg, vo))
+
+
+@pytest.fixture(scope="module")
+def plate_pair(tmp_path_factory):
+    o, g = pair(PLATE, [small_plate()])
+    _setup(o, g, CLOUD)
+    g.subdomain_precompute()
+    path = tmp_path_factory.mktemp("sd") / "sd_precomputed.chd"
+    g.write_subdomain_matrix(path)
+    gpu = SD.SubDomain(o, True, *CLOUD)
+    gpu.read_chd(path)
+    return o, g, gpu, path
+
+
+def test_matrix_matches_the_oracle(plate_pair):
+    o, g, gpu, _ = plate_pair
+    o.sd.precompute()
+    _compare_matrices(gpu.cols, o.sd)
+    st = g.subdomain_stats()
+    assert st["unknowns"] == o.sd.nf_sd and st["columns"] == o.sd.nf_sd
+    assert st["kept"] == sum(len(r) for r, _ in gpu.cols)
+    assert st["candidates"] == sum(len(o.sd.rows_of(j)) for j in range(o.sd.nf_sd))
+
+
+def test_operator_matches_the_oracle(plate_pair):
+    o, g, gpu, _ = plate_pair
+    o.sd.cols = gpu.cols                # the same thinned B on both sides
+    idx, w = o.sd.interp()
+    assert rel(g.subdomain_operator(), o.sd.lumat(idx, w)) < 1e-13
+
+
+def test_steps_conditional_on_the_solve(plate_pair):
+    _, _, gpu, path = plate_pair
+    o, g = pair(dict(PLATE, fsi_tol=5.0), [small_plate()])
+    _setup(o, g, CLOUD)
+    g.read_subdomain_matrix(path)
+    o.sd.cols = gpu.cols
+    for step in range(8):
+        g.advance()
+        fg = g.get_vector("f")
+        its, fsi = g.counters()
+        assert fsi == 1
+        o.gmres = lambda b, x0, op, fg=fg, its=its: (fg.copy(), its, 2)
+        o.advance()
+        tol = 1e-11 if step == 0 else 1e-10
+        for k in range(o.L):
+            assert rel(g.get_field("omega", k), o.omega[k]) < tol, (step, k)
+        assert rel(g.get_vector("xb"), o.xb) < tol and rel(g.get_vector("f_rdst"), o.f_rdst) < tol
+        assert abs(g.body_state()[0][0] - o.theta[0]) < tol * max(abs(o.theta[0]), 1e-12)
+    g.close()
+
+
+def test_free_running_steps(plate_pair):
+    _, _, gpu, path = plate_pair
+    o, g = pair(dict(PLATE, rtol=1e-12, fsi_tol=1e-11), [small_plate()])
+    _setup(o, g, CLOUD)
+    g.read_subdomain_matrix(path)
+    o.sd.cols = gpu.cols
+    for step in range(4):
+        g.advance()
+        o.advance()
+        assert rel(g.get_field("omega", 0), o.omega[0]) < 1e-7, step
+        assert abs(g.body_state()[0][0] - o.theta[0]) < 1e-7 * abs(o.theta[0]), step
+    assert g.counters()[1] >= 2
+    g.close()
+
+
+def test_computed_and_read_matrices_step_alike(plate_pair):
+    _, _, _, path = plate_pair
+    a = G.Simulation(G.Params(**PLATE), [small_plate()])
+    b = G.Simulation(G.Params(**PLATE), [small_plate()])
+    a.subdomain_setup(*CLOUD)
+    b.subdomain_setup(*CLOUD)
+    b.read_subdomain_matrix(path)      # sub_domain_precomputed = T
+    for _ in range(3):
+        a.advance()
+        b.advance()
+    assert np.array_equal(a.get_field("omega", 0), b.get_field("omega", 0))
+    assert b.subdomain_stats()["columns"] == 0 and a.subdomain_stats()["columns"] > 0
+    a.close()
+    b.close()
+
+
+def test_rigid_body_points_lead_the_cloud():
+    # a stationary cylinder whose points are the first cloud points (full_rectangular = F):
+    # its unknowns take their own points' B entries exactly
+    cyl = GEO.cylinder(npts=25)
+    o, g = pair(dict(SMALL, fsi_tol=5.0), [cyl])
+    _setup(o, g, RIGID_CLOUD, full_rect=False)
+    g.subdomain_precompute()
+    o.sd.precompute()
+    import tempfile, os
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "sd.chd")
+        g.write_subdomain_matrix(path)
+        gpu = SD.SubDomain(o, False, *RIGID_CLOUD)
+        gpu.read_chd(path)
+    _compare_matrices(gpu.cols, o.sd)
+    o.sd.cols = gpu.cols
+    idx, w = o.sd.interp()
+    assert (w[:, 0] == 1.0).all() and (w[:, 1:] == 0.0).all()
+    assert rel(g.subdomain_operator(), o.sd.lumat(idx, w)) < 1e-13
+    for step in range(3):
+        g.advance()
+        fg = g.get_vector("f")
+        its, _ = g.counters()
+        o.gmres = lambda b, x0, op, fg=fg, its=its: (fg.copy(), its, 2)
+        o.advance()
+        assert rel(g.get_field("omega", 0), o.omega[0]) < 1e-10, step
+    g.close()
+
+
+def test_setup_rejects_a_cloud_near_the_boundary():
+    g = G.Simulation(G.Params(**PLATE), [small_plate()])
+    with pytest.raises(G.IbError, match="within 11 cells"):
+        g.subdomain_setup(-0.25, 1.25, -0.40, 0.25, 0.0625)
+    g.close()
+
+
+def test_a_body_leaving_the_cloud_ends_the_step_with_a_domain_error():
+    # the stencils outside the cloud take its nearest cell (no access outside it); the solves are
+    # capped so that the step ends quickly, and the error word reports the exit
+    g = G.Simulation(G.Params(**dict(PLATE, gmres_max_it=20, fsi_max_it=1)), [small_plate()])
+    g.subdomain_setup(-0.25, 0.5, -0.25, 0.25, 0.0625)   # the plate reaches x = 0.98
+    with pytest.raises(G.IbError, match="IB_ERR_DOMAIN"):
+        g.advance()
+    g.close()
