@@ -351,6 +351,39 @@ def _beam_workload(args):
                        "stiffness": 1e-3, "Re": 500, "dt": 1e-3}}
 
 
+def _subdomain_workload(args):
+    """The 800x400 plate through the sub-domain precomputed-Schur method (the reference's
+    default, sub_domain = T): the precompute of B over the 121 x 51 cloud of
+    geometry.subdomain_800x400 (host wall clock), then device-timed and end-to-end steps/s.
+    The FSI iterations run from the host (the device loop is the influence band's)."""
+    import torch
+    from ib_parallel_gb300 import geometry as GEO
+    from ib_parallel_gb300 import ibgpu as G
+    p, bodies = GEO.config_plate_800x400()
+    sim = G.Simulation(p, bodies)
+    sim.subdomain_setup(*GEO.subdomain_800x400())
+    t0 = time.perf_counter()
+    sim.subdomain_precompute()
+    pre_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(sim.stream())
+    for _ in range(max(3, args.warmup)):
+        sim.advance()
+    sim.synchronize()
+    steps = max(args.steps, 20)
+    t, ksp, fsi = _timed_steps(sim, stream, steps)
+    te, h2d, d2h = _e2e_steps(sim, stream, steps)
+    st = sim.subdomain_stats()
+    theta = float(sim.body_state()[0][0])
+    sim.close()
+    return {"workload": "plate800x400_subdomain", "metric": "FSI steps/s @800x400x5 FP64 (sub-domain method)",
+            "value": steps / t, "unit": "steps/s", "steps": steps, "ms_per_step": 1e3 * t / steps,
+            "e2e": {"value": steps / te, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "precompute_s": pre_s, "subdomain": st,
+            "work_per_step": {"ksp_iter": ksp / steps, "fsi_iter": fsi / steps}, "theta_last": theta,
+            "config": {"grid": "800x400", "levels": 5, "body_points": 51, "cloud": "121x51 at 0.01",
+                       "droptol": "7.0e-3 (single precision)", "Re": 500, "dt": 1e-3}}
+
+
 def _c1_workload(args):
     """The rigid cylinder (400x200 x 3 levels, 157 points, Re=100, dt=0.004) through the
     stationary-body direct solve: device-timed and end-to-end steps/s, and the oracle timed on
@@ -530,6 +563,7 @@ def run_gpu(args, world, rank, local):
         result["workloads"] = {C1_WORKLOAD: _c1_workload(args)}
     if rank == 0 and world == 1 and not args.no_c1:
         result.setdefault("workloads", {})["beam800x400"] = _beam_workload(args)
+        result["workloads"]["plate800x400_subdomain"] = _subdomain_workload(args)
     if rank == 0 and world == 1 and args.ensemble > 0:
         result.setdefault("workloads", {})["ensemble"] = _ensemble(args)
     if rank == 0:

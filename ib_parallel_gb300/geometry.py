@@ -76,6 +76,13 @@ def config_plate_800x400(seed: int = 0, npts: int = 51) -> tuple:
     return p, [torsional_plate(npts, 1.0, gamma0, itheta=0.5 / 3.0, ktheta=1e-3)]
 
 
+def subdomain_800x400() -> tuple:
+    """The sub-domain cloud of the 800x400 plate (sub_domain = T, fully rectangular): the
+    rectangle [-0.1, 1.1] x [-0.35, 0.15] around the plate's swept region at the grid spacing
+    0.01, 121 x 51 points (12342 unknowns).  Returns (sdxi, sdxe, sdyi, sdye, delta_sd)."""
+    return (-0.1, 1.1, -0.35, 0.15, 0.01)
+
+
 # ---------------------------------------------------------------------------------------------
 # The reference's input files (input/ib.inp, input/body.NNN.inp), read through the library's C
 # ABI (ib_read_namelist, ib_read_body, ib_count_bodies) and written in the same layout.
