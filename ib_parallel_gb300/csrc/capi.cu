@@ -308,6 +308,24 @@ int ib_get_subdomain_stats(IbCtx* h, long long* counts, double* precompute_ms) {
   return IB_OK;
 }
 
+int ib_adjoint_forward(IbCtx* h, int nsteps, int K, const double* frames, double* forces) {
+  CTX_OR_FAIL(h);
+  if (!frames || !forces) return fail(IB_ERR_ARG, "bad argument");
+  std::string msg;
+  int rc = ib::op_adjoint_forward(c, nsteps, K, frames, forces, &msg);
+  if (rc != IB_OK && msg.empty()) return op_result(rc, "adjoint_forward failed");
+  return rc == IB_OK ? IB_OK : fail(rc, ("adjoint_forward: " + msg).c_str());
+}
+
+int ib_adjoint_backward(IbCtx* h, const double* dforces, double* dframes) {
+  CTX_OR_FAIL(h);
+  if (!dforces || !dframes) return fail(IB_ERR_ARG, "bad argument");
+  std::string msg;
+  int rc = ib::op_adjoint_backward(c, dforces, dframes, &msg);
+  if (rc != IB_OK && msg.empty()) return op_result(rc, "adjoint_backward failed");
+  return rc == IB_OK ? IB_OK : fail(rc, ("adjoint_backward: " + msg).c_str());
+}
+
 int ib_read_variables(IbCtx* h, const char* path, int itime) {
   CTX_OR_FAIL(h);
   if (!path) return fail(IB_ERR_ARG, "null path");

@@ -160,6 +160,25 @@ struct SubDomain {
   double precompute_ms = 0;
 };
 
+// The discrete adjoint (adjoint.cu): frame bases, checkpoints of the state every K steps and at
+// the end, the tape of one segment's step inputs, the adjoint state and its scratch.
+struct AdjointState {
+  bool ready = false;
+  int nsteps = 0, K = 0, nseg = 0;
+  std::vector<double> frames;          // nsteps x (u, v, W)
+  std::vector<long long> it_ckpt;      // itime at each checkpoint
+  void* mem = nullptr;                 // the fixed-size buffers below
+  double* ckpt = nullptr;              // (nseg + 1) states
+  double* tape = nullptr;              // K x levels x (omega, qx, qy)
+  double* bases = nullptr;             // 3 x levels x (u-faces, v-faces)
+  double* q0 = nullptr;                // one step's frame flux, levels x (u-faces, v-faces)
+  std::vector<double*> lom, lro, lqx, lqy, lom_n, lro_n, lqx_n, lqy_n, lw, lostar;
+  double *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *zero_v = nullptr;
+  double *hx = nullptr, *hy = nullptr, *ax = nullptr, *ay = nullptr;
+  double *ring1 = nullptr, *ring2 = nullptr, *ring3 = nullptr;
+  double *lf = nullptr, *lrhsf = nullptr, *dforce = nullptr, *dframe = nullptr;
+};
+
 struct Ctx {
   IbParams p{};
   GridDims g{};
@@ -228,6 +247,7 @@ struct Ctx {
   bool ub_on = false;
   PressureOp pres;
   SubDomain sd;
+  AdjointState adj;
   // family-3 beams (beam.cu)
   int nbeam = 0;
   BeamDev* beams = nullptr;
@@ -388,6 +408,10 @@ int sd_write(Ctx* c, const char* path, std::string* msg);
 int sd_read(Ctx* c, const char* path, std::string* msg);
 void sd_free(Ctx* c);
 int inf_build_scratch(Ctx* c);
+// adjoint.cu: the discrete adjoint for stationary rigid bodies in a moving frame
+int op_adjoint_forward(Ctx* c, int nsteps, int K, const double* frames, double* forces, std::string* msg);
+int op_adjoint_backward(Ctx* c, const double* dforces, double* dframes, std::string* msg);
+void adjoint_free(Ctx* c);
 // solver.cu: a time step in three parts (op_advance runs them in a row)
 int op_advance_begin(Ctx* c);
 int op_advance_end(Ctx* c);

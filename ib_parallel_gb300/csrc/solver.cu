@@ -450,6 +450,7 @@ void ctx_destroy(Ctx* c) {
   pressure_free(c);
   beam_free(c);
   sd_free(c);
+  adjoint_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);

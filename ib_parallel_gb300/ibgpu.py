@@ -44,7 +44,7 @@ EXPORTS = [
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
     "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state", "ib_get_step_graph_stats",
     "ib_subdomain_setup", "ib_subdomain_precompute", "ib_write_subdomain_matrix", "ib_read_subdomain_matrix",
-    "ib_subdomain_operator", "ib_get_subdomain_stats",
+    "ib_subdomain_operator", "ib_get_subdomain_stats", "ib_adjoint_forward", "ib_adjoint_backward",
 ]
 
 
@@ -142,6 +142,8 @@ def load(path: Optional[os.PathLike] = None):
         "ib_read_subdomain_matrix": ([P, C.c_char_p], C.c_int),
         "ib_subdomain_operator": ([P, P], C.c_int),
         "ib_get_subdomain_stats": ([P, C.POINTER(C.c_longlong), D], C.c_int),
+        "ib_adjoint_forward": ([P, C.c_int, C.c_int, P, P], C.c_int),
+        "ib_adjoint_backward": ([P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -454,6 +456,22 @@ class Simulation:
         _check(self.lib.ib_get_subdomain_stats(self.h, counts, C.byref(ms)), "ib_get_subdomain_stats")
         return {"unknowns": counts[0], "candidates": counts[1], "kept": counts[2], "columns": counts[3],
                 "precompute_ms": ms.value}
+
+    # ---- the discrete adjoint (stationary rigid bodies, num_stat, moving frame)
+    def adjoint_forward(self, frames, K: int = 20) -> np.ndarray:
+        """Advances len(frames) steps with per-step frame (u, v, W); returns the force
+        coefficients (nsteps, nbody, 2), keeping checkpoints for adjoint_backward."""
+        fr = np.ascontiguousarray(frames, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((fr.shape[0], max(1, self.nbody), 2))
+        _check(self.lib.ib_adjoint_forward(self.h, fr.shape[0], int(K), _ptr(fr), _ptr(out)), "ib_adjoint_forward")
+        return out[:, :self.nbody]
+
+    def adjoint_backward(self, dforces) -> np.ndarray:
+        """dJ/dframes (nsteps, 3) for J = sum(dforces * forces) of the last adjoint_forward."""
+        d = np.ascontiguousarray(dforces, dtype=np.float64)
+        out = np.zeros((d.shape[0], 3))
+        _check(self.lib.ib_adjoint_backward(self.h, _ptr(d), _ptr(out)), "ib_adjoint_backward")
+        return out
 
     def step_graph_stats(self) -> dict:
         """How the steps ran: as one graph, of those with the FSI loop finished from the host,

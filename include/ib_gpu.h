@@ -161,6 +161,20 @@ int ib_subdomain_operator(IbCtx* ctx, double* lumat);
  * after the drop tolerance, columns computed}; *precompute_ms = host wall time of the column
  * loops. */
 int ib_get_subdomain_stats(IbCtx* ctx, long long* counts, double* precompute_ms);
+/* The discrete adjoint of the step (north_star "Differentiation"; the reference has none) for
+ * stationary rigid bodies solved directly (num_stat = 1) in a moving frame.  The frame's flux
+ * (motion_potential + motion_rotation, variables.F90:299-360) is linear in its velocity (u, v)
+ * and angular velocity W about the centre (motion[3], motion[4]), so a body pitching or plunging
+ * in its own frame is given by a triple (u, v, W) per step (the reference's motion_grid of
+ * user.F90:13-31 as a function of the step).
+ * ib_adjoint_forward: advances nsteps (<= 4096) from the current state with frames[3 n..3 n+2]
+ * at step n, writes the force coefficients forces[(n nbody + b) 2 + {0, 1}] = (Cx, Cy) of body b
+ * after step n, and keeps the state every K steps and at the end on the device.
+ * ib_adjoint_backward: for J = sum dforces . forces (same layout), writes dJ/dframes (nsteps x
+ * 3): each segment of K steps is recomputed from its checkpoint and run backwards through the
+ * exact transpose of every operator of the step; the context is left as the forward left it. */
+int ib_adjoint_forward(IbCtx* ctx, int nsteps, int K, const double* frames, double* forces);
+int ib_adjoint_backward(IbCtx* ctx, const double* dforces, double* dframes);
 /* write_variables (variables.F90:709-803): the restart file output/dataRR_IIIIIII.var of one
  * rank at path, in the reference's Fortran unformatted layout (4-byte record markers, 4-byte
  * integers, 8-byte reals; the layout output/getdata.m reads). */

@@ -11,7 +11,7 @@ import ib_oracle as O
 def _oracle(L=3):
     p = O.Params(m=32, n=16, mgridlev=L, dt=0.02, Re=100.0, len=4.0, offsetx=1.0, offsety=1.0, num_stat=True,
                  motion=(-1.0, 0.0, 0.0, 0.3, 0.0))
-    return O.IBOracle(p, [O.cylinder(npts=11, diameter=0.6, xc=0.3, yc=0.0)])
+    return O.IBOracle(p, [O.cylinder(npts=10, diameter=0.8, xc=0.3, yc=0.0)])
 
 
 def _coefs(N):
