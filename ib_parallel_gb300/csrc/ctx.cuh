@@ -208,7 +208,6 @@ struct Ctx {
   // vort2flux's modes of the coarser levels (k >= 1; hat[k] keeps the predictor's meanwhile)
   std::vector<double*> v2f_modes;
   unsigned char* rm_v2f = nullptr; // the rows coarsify writes: transformed; the others: ROW_SCALE
-  unsigned char* rm_pinv = nullptr;   // the rows coarsify writes: skipped; the others: transformed
   // The step's first vort2flux transforms the finest level back only on the rows E(curl s)
   // reads (plus kFsiRowMargin) when the FSI iterations may run on the device; v2f_rows[0..1]
   // receives the rows, q0_partial says s and q of the finest level hold only those.

@@ -264,7 +264,6 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->v2f_modes.assign(L, nullptr);
   for (int k = 1; k < L; ++k) c->v2f_modes[k] = P.take<double>(ns);
   c->rm_v2f = P.take<unsigned char>(g.nsy);
-  c->rm_pinv = P.take<unsigned char>(g.nsy);
   c->v2f_rows = P.take<int>(4);
   c->v2f_partial = nf > 0 && nt > 0 && !p.num_stat;
   c->sdv.resize(L); c->edgev.resize(L);
@@ -343,12 +342,11 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   // coarsify fills coarse rows J = n/4+2 .. 3n/4; apply_bc fills rows J = 2, n wholly and
   // the first/last sample of every other row; get_bc reads rows J = n/4+1, 3n/4+1
   {
-    std::vector<unsigned char> top(g.nsy), coarse(g.nsy), fine(g.nsy), ring2(g.nsy), v2f(g.nsy), pinv(g.nsy);
+    std::vector<unsigned char> top(g.nsy), coarse(g.nsy), fine(g.nsy), ring2(g.nsy), v2f(g.nsy);
     for (int r = 0; r < g.nsy; ++r) {
       bool centre = r >= g.n / 4 && r <= 3 * g.n / 4 - 2;
       bool edge = r == 0 || r == g.nsy - 1;
       v2f[r] = centre ? ROW_FFT : ROW_SCALE;
-      pinv[r] = centre ? ROW_SKIP : ROW_FFT;
       top[r] = centre ? ROW_FFT : ROW_ZERO;
       coarse[r] = (centre || edge) ? ROW_FFT : ROW_EDGES;
       fine[r] = edge ? ROW_SKIP : ROW_EDGES;   // the edge rows come from dst_x_ring_rows
@@ -359,7 +357,6 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     IB_CUDA_CHECK(cudaMemcpy(c->rm_fine, fine.data(), g.nsy, cudaMemcpyHostToDevice));
     IB_CUDA_CHECK(cudaMemcpy(c->rm_ring2, ring2.data(), g.nsy, cudaMemcpyHostToDevice));
     IB_CUDA_CHECK(cudaMemcpy(c->rm_v2f, v2f.data(), g.nsy, cudaMemcpyHostToDevice));
-    IB_CUDA_CHECK(cudaMemcpy(c->rm_pinv, pinv.data(), g.nsy, cudaMemcpyHostToDevice));
     // points get_bc reads: rows J = n/4+1, 3n/4+1 at I = m/4+1..3m/4+1 and columns
     // I = m/4+1, 3m/4+1 at J = n/4+1..3n/4+1 (vertex row r = J-2, column c = I-2)
     std::vector<int2> pts;
@@ -1339,13 +1336,12 @@ static int op_predict_levels(Ctx* c, bool seed_rhs_old) {
     }
     if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 0.25 * c->vfac[k - 1]));
   }
-  // the coarser levels' rows that vort2flux's coarsify rewrites before anything reads them
-  // are not transformed back
+  // every row of every level back: coarsify rewrites only the centre columns of a coarser
+  // level's centre rows, the rest of those rows (the coarse grid beside the finer one) is the
+  // predictor's, read by the next step's nonlinear terms and get_bc and by vort2flux
   DstXArgs b;
   b.nlev = L;
   for (int k = 0; k < L; ++k) { b.lin[k] = c->hat[k]; b.lout[k] = c->omega[k]; }
-  b.rowmode = c->rm_pinv;
-  b.rowmode_level0 = 1;
   ProfScope ps(c, 0, pass_bytes(c, L, L));
   return dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, b, g, c->lx_batch, st);
 }

@@ -76,6 +76,18 @@ def config_plate_800x400(seed: int = 0, npts: int = 51) -> tuple:
     return p, [torsional_plate(npts, 1.0, gamma0, itheta=0.5 / 3.0, ktheta=1e-3)]
 
 
+def config_pitching_600x300(ds_cells: float = 2.0) -> tuple:
+    """The adjoint workload: a rigid NACA 0012 of chord 1 held in its own frame (leading edge at the
+    origin, pitching about the quarter chord, the frame's centre), Re=200, 600x300 on
+    [-1.5,4.5]x[-1.5,1.5], 4 levels, dt=0.002, the direct solve.  Its points are ds_cells grid
+    spacings apart (2: 101 points): at 250 points (0.8 spacings) the Schur matrix is singular to
+    working precision, as for the plate (tests/test_conditioning_cpu.py)."""
+    p = Params(m=600, n=300, mgridlev=4, dt=0.002, Re=200.0, len=6.0, offsetx=1.5, offsety=1.5, num_stat=True,
+               motion=(-1.0, 0.0, 0.0, 0.25, 0.0))
+    x, y = naca00(12.0, ds=ds_cells * p.len / p.m)
+    return p, [Body(x=x, y=y, fam=1)]
+
+
 def subdomain_800x400() -> tuple:
     """The sub-domain cloud of the 800x400 plate (sub_domain = T, fully rectangular): the
     rectangle [-0.1, 1.1] x [-0.35, 0.15] around the plate's swept region at the grid spacing

@@ -108,3 +108,27 @@ def test_plate_conditional_on_solve():
         assert rel(g.get_vector("xb"), o.xb) < tol
     g.close()
 
+
+
+@pytest.mark.parametrize("L", [2, 3])
+def test_coarse_levels_beside_the_finer_grid(L):
+    # a coarse grid spacing puts vorticity on the coarser levels beside the finer grid (their
+    # centre rows outside the centre columns, which coarsify does not rewrite) within a few
+    # steps, and over 60 steps the wake leaves the finest grid downstream: those points are the
+    # predictor's on every level, as the oracle's
+    from ib_parallel_gb300 import ibgpu as G
+    import ib_oracle as O
+    kw = dict(m=32, n=16, mgridlev=L, dt=0.05, Re=100.0, len=4.0, offsetx=1.0, offsety=1.0, num_stat=True,
+              autotune=False)
+    cyl = O.cylinder(npts=10, diameter=0.8, xc=0.3, yc=0.0)
+    o, g = pair(kw, [G.Body(x=cyl.x.copy(), y=cyl.y.copy(), fam=1)])
+    n, m = kw["n"], kw["m"]
+    for step in range(60):
+        o.advance()
+        g.advance()
+        if step in (1, 59):
+            for k in range(L):
+                assert rel(g.get_field("omega", k), o.omega[k]) < 1e-10, (step, k)
+    beside = o.omega[1][n // 4: 3 * n // 4 - 1, 3 * m // 4 - 1:]
+    assert np.abs(beside).max() > 1e-3 * np.abs(o.omega[1]).max()   # the wake has reached them
+    g.close()
