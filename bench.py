@@ -420,11 +420,11 @@ def _adjoint_workload(args):
     h = 1e-6
     jp = run(amp0 + h, 0.2, 0.0, False)
     jm = run(amp0 - h, 0.2, 0.0, False)
-    fd = (float(jp["cl"] + jp["cd"]) - float(jm["cl"] + jm["cd"])) / (2 * h)
+    fd = (float((jp["cl"] + jp["cd"]).detach()) - float((jm["cl"] + jm["cd"]).detach())) / (2 * h)
     return {"workload": "pitching600x300_adjoint", "metric": "adjoint/forward cost (reverse sweep time over forward time)",
             "value": r["t_bwd"] / r["t_fwd"], "unit": "x", "higher_is_better": False,
             "forward_s": r["t_fwd"], "backward_s": r["t_bwd"], "forward_steps_per_s": N / r["t_fwd"],
-            "mean_cl": float(r["cl"]), "mean_cd": float(r["cd"]),
+            "mean_cl": float(r["cl"].detach()), "mean_cd": float(r["cd"].detach()),
             "gradient_of_mean_cl_plus_cd": {"amplitude_rad": grads[0], "frequency": grads[1], "phase": grads[2]},
             "central_difference_amplitude": {"value": fd, "rel_err": abs(grads[0] - fd) / abs(fd)},
             "config": {"grid": "600x300", "levels": 4, "body": f"NACA 0012, {bodies[0].npts} points (2 grid spacings)",
