@@ -793,6 +793,30 @@ def run_roofline_only():
     return 0
 
 
+def run_profile_leg(which):
+    """One short leg inside a cudaProfilerStart/Stop window, for ncu --profile-from-start off:
+    'adjoint' brackets the reverse sweep of 20 steps of the pitching NACA 0012 (one segment: the
+    recompute, then the 20 reverse steps)."""
+    import torch
+    from ib_parallel_gb300 import autodiff as AD
+    from ib_parallel_gb300 import geometry as GEO
+    from ib_parallel_gb300 import ibgpu as G
+    p, bodies = GEO.config_pitching_600x300()
+    p.autotune = False
+    sim = G.Simulation(p, bodies)
+    frames = AD.pitching_frames(20, p.dt, math.radians(10.0), 0.2, 0.0).numpy()
+    forces = sim.adjoint_forward(frames, 20)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    t0 = time.perf_counter()
+    sim.adjoint_backward(np.ones_like(forces))
+    dt = time.perf_counter() - t0
+    torch.cuda.profiler.stop()
+    print(json.dumps({"leg": which + " backward, 20 steps", "seconds": dt}))
+    sim.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -820,8 +844,12 @@ def main():
     ap.add_argument("--roofline-only", action="store_true",
                     help="only time the single x pass of the roofline (inside a profiler window: the command "
                          "the ncu traffic capture of that pass runs)")
+    ap.add_argument("--profile-leg", choices=["adjoint"], default=None,
+                    help="only run one short leg inside a profiler window (the command of an ncu launch list)")
     args = ap.parse_args()
     world, rank, local = _dist()
+    if args.profile_leg:
+        return run_profile_leg(args.profile_leg)
     if args.roofline_only:
         return run_roofline_only()
     if args.ensemble_only:

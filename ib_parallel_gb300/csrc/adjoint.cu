@@ -256,23 +256,23 @@ struct DotArgs {
   const double* ay;
   const double* bases;   // [basis][level][u-faces, v-faces]
   int L, nu, nv;
-  double* out;           // 3
+  double* part;          // 3 x kDotBlocks partial sums
 };
+constexpr int kDotBlocks = 152;
 
-// out[b] = sum over levels of <lq0, B_b>: one CTA per basis, fixed-order tree
+// part[b][blk] = the block's slice of sum over levels of <lq0, B_b> (fixed-order tree)
 __global__ void k_adj_dots(DotArgs a) {
   IB_GRID_DEP_WAIT();
-  __shared__ double red[1024];
-  const int b = blockIdx.x;
+  __shared__ double red[256];
+  const int b = blockIdx.y, blk = blockIdx.x;
   const int per = a.nu + a.nv;
+  const long long total = (long long)a.L * per;
   double acc = 0.0;
-  for (int k = 0; k < a.L; ++k) {
-    const double* B = a.bases + ((size_t)b * a.L + k) * per;
-    for (int i = threadIdx.x; i < per; i += blockDim.x) {
-      double l = i < a.nu ? a.lx[k][i] : a.ly[k][i - a.nu];
-      if (k == 0) l += i < a.nu ? a.ax[i] : a.ay[i - a.nu];
-      acc = fma(l, B[i], acc);
-    }
+  for (long long t = (long long)blk * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(t / per), i = (int)(t % per);
+    double l = i < a.nu ? a.lx[k][i] : a.ly[k][i - a.nu];
+    if (k == 0) l += i < a.nu ? a.ax[i] : a.ay[i - a.nu];
+    acc = fma(l, a.bases[((size_t)b * a.L + k) * per + i], acc);
   }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -280,7 +280,16 @@ __global__ void k_adj_dots(DotArgs a) {
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) a.out[b] = red[0];
+  if (threadIdx.x == 0) a.part[b * gridDim.x + blk] = red[0];
+}
+
+__global__ void k_adj_dots_sum(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+  IB_GRID_DEP_WAIT();
+  const int b = threadIdx.x;
+  if (b >= 3) return;
+  double s = 0.0;
+  for (int i = 0; i < nblk; ++i) s += part[b * nblk + i];
+  out[b] = s;
 }
 
 int blocks(long long n) { return (int)cdiv(n, kT); }
@@ -440,9 +449,10 @@ int step_T(Adj& a, int slot, int it, const double* frame, const double* dforce_h
   // side's on level 0) against each basis
   DotArgs d;
   for (int k = 0; k < L; ++k) { d.lx[k] = A.lqx_n[k]; d.ly[k] = A.lqy_n[k]; }
-  d.ax = A.ax; d.ay = A.ay; d.bases = A.bases; d.L = L; d.nu = g.nu; d.nv = g.nv; d.out = dframe_d;
-  count_launch();
-  k_adj_dots<<<3, 1024, 0, st>>>(d);
+  d.ax = A.ax; d.ay = A.ay; d.bases = A.bases; d.L = L; d.nu = g.nu; d.nv = g.nv; d.part = A.dpart;
+  count_launches(2);
+  k_adj_dots<<<dim3(kDotBlocks, 3), 256, 0, st>>>(d);
+  k_adj_dots_sum<<<1, 32, 0, st>>>(A.dpart, kDotBlocks, dframe_d);
   IB_CUDA_CHECK(cudaGetLastError());
   std::swap(A.lom, A.lom_n);
   std::swap(A.lqx, A.lqx_n);
@@ -538,7 +548,7 @@ static int adjoint_alloc(Ctx* c) {
                    2 * (size_t)L * (g.nu + g.nv) /* lq (x2) */ + 2 * (size_t)L * g.ns /* lw, lostar */ +
                    4 * (size_t)g.ns /* t1-t3, zero */ + 3 * (size_t)(g.nu + g.nv) /* hx hy, ax ay */ +
                    3 * (size_t)g.nbc + 2 * (size_t)std::max(c->nf, 1) + 2 * (size_t)std::max(c->nbody, 1) +
-                   3 * 4096;
+                   3 * 4096 + 3 * (size_t)kDotBlocks;
   IB_CUDA_CHECK(cudaMalloc(&A.mem, 8 * n));
   IB_CUDA_CHECK(cudaMemset(A.mem, 0, 8 * n));
   double* p = (double*)A.mem;
@@ -556,6 +566,7 @@ static int adjoint_alloc(Ctx* c) {
   A.lf = take(std::max(c->nf, 1)); A.lrhsf = take(std::max(c->nf, 1));
   A.dforce = take(2 * (size_t)std::max(c->nbody, 1));
   A.dframe = take(3 * 4096);
+  A.dpart = take(3 * (size_t)kDotBlocks);
   const double cx = c->p.motion[3], cy = c->p.motion[4];
   for (int b = 0; b < 3; ++b) {
     std::vector<double> h = frame_flux_host(c, b == 0, b == 1, b == 2, cx, cy);

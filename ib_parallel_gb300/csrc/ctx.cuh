@@ -176,7 +176,7 @@ struct AdjointState {
   double *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *zero_v = nullptr;
   double *hx = nullptr, *hy = nullptr, *ax = nullptr, *ay = nullptr;
   double *ring1 = nullptr, *ring2 = nullptr, *ring3 = nullptr;
-  double *lf = nullptr, *lrhsf = nullptr, *dforce = nullptr, *dframe = nullptr;
+  double *lf = nullptr, *lrhsf = nullptr, *dforce = nullptr, *dframe = nullptr, *dpart = nullptr;
 };
 
 struct Ctx {

@@ -378,21 +378,58 @@ __global__ void k_cholesky(int n, double* A, int* err) {
   }
 }
 
+// L L^T x = b with the Cholesky factor L (row-major, lower): forward then backward substitution
+// in blocks of 32 unknowns.  Each block first subtracts what the solved unknowns contribute (one
+// warp per unknown, lanes across the solved ones, a fixed shuffle tree), then warp 0 solves the
+// block's 32 x 32 triangle with shuffles; no block-wide barrier inside the triangles.
 __global__ void k_chol_solve(int n, const double* __restrict__ L, const double* __restrict__ b, double* x) {
   IB_GRID_DEP_WAIT();
   extern __shared__ double y[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = b[i];
   __syncthreads();
-  for (int i = 0; i < n; ++i) {  // L y = b
-    if (threadIdx.x == 0) y[i] = y[i] / L[(size_t)i * n + i];
+  auto warp_sum = [](double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+  };
+  for (int b0 = 0; b0 < n; b0 += 32) {   // L y = b
+    const int nb = min(32, n - b0);
+    for (int r = b0 + warp; r < b0 + nb; r += nw) {
+      double acc = 0.0;
+      for (int c = lane; c < b0; c += 32) acc = fma(L[(size_t)r * n + c], y[c], acc);
+      acc = warp_sum(acc);
+      if (lane == 0) y[r] -= acc;
+    }
     __syncthreads();
-    for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) y[r] -= L[(size_t)r * n + i] * y[i];
+    if (warp == 0) {
+      double yr = lane < nb ? y[b0 + lane] : 0.0;
+      for (int i = 0; i < nb; ++i) {
+        if (lane == i) yr = yr / L[(size_t)(b0 + i) * n + b0 + i];
+        const double yi = __shfl_sync(0xffffffffu, yr, i);
+        if (lane > i && lane < nb) yr -= L[(size_t)(b0 + lane) * n + b0 + i] * yi;
+      }
+      if (lane < nb) y[b0 + lane] = yr;
+    }
     __syncthreads();
   }
-  for (int i = n - 1; i >= 0; --i) {  // L^T x = y
-    if (threadIdx.x == 0) y[i] = y[i] / L[(size_t)i * n + i];
+  for (int b1 = n; b1 > 0; b1 -= 32) {   // L^T x = y
+    const int b0 = max(0, b1 - 32), nb = b1 - b0;
+    for (int c = b0 + warp; c < b1; c += nw) {
+      double acc = 0.0;
+      for (int r = b1 + lane; r < n; r += 32) acc = fma(L[(size_t)r * n + c], y[r], acc);
+      acc = warp_sum(acc);
+      if (lane == 0) y[c] -= acc;
+    }
     __syncthreads();
-    for (int r = threadIdx.x; r < i; r += blockDim.x) y[r] -= L[(size_t)i * n + r] * y[i];
+    if (warp == 0) {
+      double yr = lane < nb ? y[b0 + lane] : 0.0;
+      for (int i = nb - 1; i >= 0; --i) {
+        if (lane == i) yr = yr / L[(size_t)(b0 + i) * n + b0 + i];
+        const double xi = __shfl_sync(0xffffffffu, yr, i);
+        if (lane < i) yr -= L[(size_t)(b0 + i) * n + b0 + lane] * xi;
+      }
+      if (lane < nb) y[b0 + lane] = yr;
+    }
     __syncthreads();
   }
   for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = y[i];
@@ -419,7 +456,7 @@ int launch_chol_solve(int n, const double* Lf, const double* b, double* x, cudaS
   size_t smem = sizeof(double) * n;
   IB_CUDA_CHECK(allow_dyn_smem(k_chol_solve, smem));
   count_launch();
-  k_chol_solve<<<1, 512, smem, st>>>(n, Lf, b, x);
+  k_chol_solve<<<1, 1024, smem, st>>>(n, Lf, b, x);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
