@@ -796,11 +796,23 @@ def run_roofline_only():
 def run_profile_leg(which):
     """One short leg inside a cudaProfilerStart/Stop window, for ncu --profile-from-start off:
     'adjoint' brackets the reverse sweep of 20 steps of the pitching NACA 0012 (one segment: the
-    recompute, then the 20 reverse steps)."""
+    recompute, then the 20 reverse steps); 'band' the first step of the 800x400 plate, which builds
+    the influence band (capture its first launches with ncu -c)."""
     import torch
     from ib_parallel_gb300 import autodiff as AD
     from ib_parallel_gb300 import geometry as GEO
     from ib_parallel_gb300 import ibgpu as G
+    if which == "band":
+        p, bodies = GEO.config_plate_800x400()
+        p.autotune = False
+        sim = G.Simulation(p, bodies)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        sim.advance()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"leg": "band build (first step)", "influence": sim.influence_stats()}))
+        sim.close()
+        return 0
     p, bodies = GEO.config_pitching_600x300()
     p.autotune = False
     sim = G.Simulation(p, bodies)
@@ -844,7 +856,7 @@ def main():
     ap.add_argument("--roofline-only", action="store_true",
                     help="only time the single x pass of the roofline (inside a profiler window: the command "
                          "the ncu traffic capture of that pass runs)")
-    ap.add_argument("--profile-leg", choices=["adjoint"], default=None,
+    ap.add_argument("--profile-leg", choices=["adjoint", "band"], default=None,
                     help="only run one short leg inside a profiler window (the command of an ncu launch list)")
     args = ap.parse_args()
     world, rank, local = _dist()

@@ -381,10 +381,12 @@ __global__ void k_cholesky(int n, double* A, int* err) {
 // L L^T x = b with the Cholesky factor L (row-major, lower): forward then backward substitution
 // in blocks of 32 unknowns.  Each block first subtracts what the solved unknowns contribute (one
 // warp per unknown, lanes across the solved ones, a fixed shuffle tree), then warp 0 solves the
-// block's 32 x 32 triangle with shuffles; no block-wide barrier inside the triangles.
+// block's 32 x 32 triangle, staged in shared memory, with shuffles; no block-wide barrier inside
+// the triangles.
 __global__ void k_chol_solve(int n, const double* __restrict__ L, const double* __restrict__ b, double* x) {
   IB_GRID_DEP_WAIT();
-  extern __shared__ double y[];
+  extern __shared__ double y[];   // n unknowns, then the diagonal block (32 x 33)
+  double* dg = y + n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = b[i];
   __syncthreads();
@@ -400,13 +402,14 @@ __global__ void k_chol_solve(int n, const double* __restrict__ L, const double* 
       acc = warp_sum(acc);
       if (lane == 0) y[r] -= acc;
     }
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) dg[(t / nb) * 33 + t % nb] = L[(size_t)(b0 + t / nb) * n + b0 + t % nb];
     __syncthreads();
     if (warp == 0) {
       double yr = lane < nb ? y[b0 + lane] : 0.0;
       for (int i = 0; i < nb; ++i) {
-        if (lane == i) yr = yr / L[(size_t)(b0 + i) * n + b0 + i];
+        if (lane == i) yr = yr / dg[i * 33 + i];
         const double yi = __shfl_sync(0xffffffffu, yr, i);
-        if (lane > i && lane < nb) yr -= L[(size_t)(b0 + lane) * n + b0 + i] * yi;
+        if (lane > i && lane < nb) yr -= dg[lane * 33 + i] * yi;
       }
       if (lane < nb) y[b0 + lane] = yr;
     }
@@ -420,13 +423,14 @@ __global__ void k_chol_solve(int n, const double* __restrict__ L, const double* 
       acc = warp_sum(acc);
       if (lane == 0) y[c] -= acc;
     }
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) dg[(t / nb) * 33 + t % nb] = L[(size_t)(b0 + t / nb) * n + b0 + t % nb];
     __syncthreads();
     if (warp == 0) {
       double yr = lane < nb ? y[b0 + lane] : 0.0;
       for (int i = nb - 1; i >= 0; --i) {
-        if (lane == i) yr = yr / L[(size_t)(b0 + i) * n + b0 + i];
+        if (lane == i) yr = yr / dg[i * 33 + i];
         const double xi = __shfl_sync(0xffffffffu, yr, i);
-        if (lane < i) yr -= L[(size_t)(b0 + i) * n + b0 + lane] * xi;
+        if (lane < i) yr -= dg[i * 33 + lane] * xi;
       }
       if (lane < nb) y[b0 + lane] = yr;
     }
@@ -453,7 +457,7 @@ int launch_cholesky(int n, double* A, int* d_err, cudaStream_t st) {
   return IB_OK;
 }
 int launch_chol_solve(int n, const double* Lf, const double* b, double* x, cudaStream_t st) {
-  size_t smem = sizeof(double) * n;
+  size_t smem = sizeof(double) * ((size_t)n + 32 * 33);
   IB_CUDA_CHECK(allow_dyn_smem(k_chol_solve, smem));
   count_launch();
   k_chol_solve<<<1, 1024, smem, st>>>(n, Lf, b, x);
