@@ -221,25 +221,32 @@ class SubDomain:
     # ------------------------------------------------------- FSI iteration
     def lumat(self, idx, wts):
         """compute_operator (operators_struct.F90:840-905): body_mat + P B^T P^T, where
-        lumat(k, i) = body + sum_a P(k,a) sum_b P(i,b) B(b, a), each dot product in order."""
+        lumat(k, i) = body + sum_a P(k,a) sum_b P(i,b) B(b, a), each dot product in order; B's
+        columns are read from their kept rows (zero elsewhere)."""
         o = self.o
         nf = o.nf
-        Bd = self.dense()
         body = np.zeros((nf, nf))
         for l in range(nf):
             e = np.zeros(nf); e[l] = 1.0
             body[:, l] = o.b_times(e)
-        inter = np.zeros((nf, self.nf_sd))   # inter[i, a] = sum_b B(b, a) P(i, b)
-        for i in range(nf):
-            acc = np.zeros(self.nf_sd)
-            for r in range(4):
-                acc = acc + Bd[idx[i, r], :] * wts[i, r]
-            inter[i] = acc
+        cols = {}
+        for a in np.unique(idx):
+            rows, vals = self.cols[a]
+            cols[int(a)] = dict(zip(rows.tolist(), vals.tolist()))
+        inter = {}   # inter[a][i] = sum_r B(b_r(i), a) P(i, r)
+        for a, col in cols.items():
+            v = np.zeros(nf)
+            for i in range(nf):
+                acc = 0.0
+                for r in range(4):
+                    acc = acc + col.get(int(idx[i, r]), 0.0) * wts[i, r]
+                v[i] = acc
+            inter[a] = v
         M = np.zeros((nf, nf))
         for k in range(nf):
             acc = np.zeros(nf)
             for q in range(4):
-                acc = acc + wts[k, q] * inter[:, idx[k, q]]
+                acc = acc + wts[k, q] * inter[int(idx[k, q])]
             M[k] = body[k] + acc
         return M
 

@@ -133,3 +133,25 @@ def test_autograd_binding_reaches_pitching_parameters():
         jm = float(mean_lift(*args))
         fd = (jp - jm) / (2 * h)
         assert abs(float(p.grad) - fd) <= 1e-6 * max(abs(fd), 1e-6), (i, float(p.grad), fd)
+
+
+def test_gradient_at_the_pitching_airfoil_size_matches_the_oracle():
+    # the bench's 600x300x4 NACA 0012 in its pitching frame, 4 steps (the oracle's adjoint step at
+    # this size takes about a second)
+    from ib_parallel_gb300 import autodiff as AD
+    from ib_parallel_gb300 import geometry as GEO
+    p, bodies = GEO.config_pitching_600x300()
+    p.autotune = False
+    N = 4
+    frames = AD.pitching_frames(N, p.dt, 0.1745, 0.2, 0.0).numpy()
+    W = np.random.default_rng(7).standard_normal((N, 1, 2))
+    g = G.Simulation(p, bodies)
+    Fg = g.adjoint_forward(frames, K=2)
+    gg = g.adjoint_backward(W)
+    po = O.Params(**{k: getattr(p, k) for k in O.Params.__dataclass_fields__ if hasattr(p, k)})
+    o = O.IBOracle(po, [O.Body(x=bodies[0].x.copy(), y=bodies[0].y.copy(), fam=1)])
+    ad = A.Adjoint(o)
+    Fo = ad.forward(frames)
+    go = ad.backward(W)
+    assert np.abs(Fg - Fo).max() < 1e-11 * np.abs(Fo).max()
+    assert np.abs(gg - go).max() < 1e-10 * np.abs(go).max(), np.abs(gg - go).max() / np.abs(go).max()

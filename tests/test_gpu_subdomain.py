@@ -154,3 +154,31 @@ def test_a_body_leaving_the_cloud_ends_the_step_with_a_domain_error():
     with pytest.raises(G.IbError, match="IB_ERR_DOMAIN"):
         g.advance()
     g.close()
+
+
+def test_full_size_columns_and_operator(tmp_path):
+    # the bench's 800x400x5 plate and its 121 x 51 cloud (12342 unknowns): sampled columns of B
+    # and the FSI operator lumat against the oracle
+    p, bodies = GEO.config_plate_800x400()
+    p.autotune = False
+    cloud = GEO.subdomain_800x400()
+    g = G.Simulation(p, bodies)
+    g.subdomain_setup(*cloud)
+    g.subdomain_precompute()
+    path = tmp_path / "sd_800x400.chd"
+    g.write_subdomain_matrix(path)
+    po = O.Params(**{k: getattr(p, k) for k in O.Params.__dataclass_fields__ if hasattr(p, k)})
+    ob = [O.Body(x=b.x.copy(), y=b.y.copy(), fam=b.fam, gamma0_deg=b.gamma0_deg, itheta=b.itheta,
+                 ktheta=b.ktheta, ctheta=b.ctheta) for b in bodies]
+    o = O.IBOracle(po, ob)
+    sd = SD.SubDomain(o, True, *cloud)
+    sd.read_chd(path)
+    assert sd.nf_sd == 12342
+    for j in (0, 3050, 6171 + 3050, sd.nf_sd - 1):
+        rows, vals = sd.drop(j, sd.column(j))
+        assert np.array_equal(rows, sd.cols[j][0]), j
+        assert rel(sd.cols[j][1], vals) < 1e-11, (j, rel(sd.cols[j][1], vals))
+    o.sd = sd
+    idx, w = sd.interp()
+    assert rel(g.subdomain_operator(), sd.lumat(idx, w)) < 1e-12
+    g.close()
