@@ -354,8 +354,9 @@ def _beam_workload(args):
 def _subdomain_workload(args):
     """The 800x400 plate through the sub-domain precomputed-Schur method (the reference's
     default, sub_domain = T): the precompute of B over the 121 x 51 cloud of
-    geometry.subdomain_800x400 (host wall clock), then device-timed and end-to-end steps/s.
-    The FSI iterations run from the host (the device loop is the influence band's)."""
+    geometry.subdomain_800x400 (host wall clock), then device-timed and end-to-end steps/s, the
+    FSI iterations on the device from the second step; beside it the same steps with the FSI
+    iterations run from the host (per-phase timing on), device-timed."""
     import torch
     from ib_parallel_gb300 import geometry as GEO
     from ib_parallel_gb300 import ibgpu as G
@@ -373,12 +374,19 @@ def _subdomain_workload(args):
     t, ksp, fsi = _timed_steps(sim, stream, steps)
     te, h2d, d2h = _e2e_steps(sim, stream, steps)
     st = sim.subdomain_stats()
+    graphs = sim.step_graph_stats()
     theta = float(sim.body_state()[0][0])
+    sim.step_profile(1)   # the same context on: the FSI iterations from the host
+    for _ in range(2):
+        sim.advance()
+    sim.synchronize()
+    th, _, _ = _timed_steps(sim, stream, steps)
     sim.close()
     return {"workload": "plate800x400_subdomain", "metric": "FSI steps/s @800x400x5 FP64 (sub-domain method)",
             "value": steps / t, "unit": "steps/s", "steps": steps, "ms_per_step": 1e3 * t / steps,
             "e2e": {"value": steps / te, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "precompute_s": pre_s, "subdomain": st,
+            "host_fsi_loop": {"value": steps / th, "unit": "steps/s", "ms_per_step": 1e3 * th / steps},
+            "step_graph": graphs, "precompute_s": pre_s, "subdomain": st,
             "work_per_step": {"ksp_iter": ksp / steps, "fsi_iter": fsi / steps}, "theta_last": theta,
             "config": {"grid": "800x400", "levels": 5, "body_points": 51, "cloud": "121x51 at 0.01",
                        "droptol": "7.0e-3 (single precision)", "Re": 500, "dt": 1e-3}}
@@ -797,7 +805,9 @@ def run_profile_leg(which):
     """One short leg inside a cudaProfilerStart/Stop window, for ncu --profile-from-start off:
     'adjoint' brackets the reverse sweep of 20 steps of the pitching NACA 0012 (one segment: the
     recompute, then the 20 reverse steps); 'band' the first step of the 800x400 plate, which builds
-    the influence band (capture its first launches with ncu -c)."""
+    the influence band (capture its first launches with ncu -c); 'subdomain' three steps of the
+    800x400 plate through the sub-domain method after its precompute and three warm-up steps, the
+    FSI iterations run from the host so that each kernel is a launch of its own."""
     import torch
     from ib_parallel_gb300 import autodiff as AD
     from ib_parallel_gb300 import geometry as GEO
@@ -811,6 +821,25 @@ def run_profile_leg(which):
         sim.advance()
         torch.cuda.profiler.stop()
         print(json.dumps({"leg": "band build (first step)", "influence": sim.influence_stats()}))
+        sim.close()
+        return 0
+    if which == "subdomain":
+        p, bodies = GEO.config_plate_800x400()
+        p.autotune = False
+        sim = G.Simulation(p, bodies)
+        sim.subdomain_setup(*GEO.subdomain_800x400())
+        sim.subdomain_precompute()
+        for _ in range(3):
+            sim.advance()
+        sim.step_profile(1)
+        sim.synchronize()
+        torch.cuda.profiler.start()
+        for _ in range(3):
+            sim.advance()
+        sim.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"leg": "sub-domain steps 4-6, FSI iterations from the host",
+                          "counters": sim.counters()}))
         sim.close()
         return 0
     p, bodies = GEO.config_pitching_600x300()
@@ -856,7 +885,7 @@ def main():
     ap.add_argument("--roofline-only", action="store_true",
                     help="only time the single x pass of the roofline (inside a profiler window: the command "
                          "the ncu traffic capture of that pass runs)")
-    ap.add_argument("--profile-leg", choices=["adjoint", "band"], default=None,
+    ap.add_argument("--profile-leg", choices=["adjoint", "band", "subdomain"], default=None,
                     help="only run one short leg inside a profiler window (the command of an ncu launch list)")
     args = ap.parse_args()
     world, rank, local = _dist()

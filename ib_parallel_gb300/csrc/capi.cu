@@ -777,6 +777,20 @@ int ib_get_influence_stats(IbCtx* h, long long* counts, double* build_ms) {
   return IB_OK;
 }
 
+int ib_get_coarse_stats(IbCtx* h, long long* counts, double* ms) {
+  CTX_OR_FAIL(h);
+  if (!counts || !ms) return fail(IB_ERR_ARG, "bad argument");
+  const ib::CoarseResp& cr = c->inf.cr;
+  long long held = 0;
+  for (int k = 1; k < c->L; ++k) held += cr.n[k];
+  counts[0] = cr.solves;
+  counts[1] = held;
+  counts[2] = (long long)cr.bytes;
+  counts[3] = cr.enabled ? 1 : 0;
+  *ms = cr.ms;
+  return IB_OK;
+}
+
 int ib_get_step_graph_stats(IbCtx* h, long long* counts) {
   CTX_OR_FAIL(h);
   if (!counts) return fail(IB_ERR_ARG, "bad argument");

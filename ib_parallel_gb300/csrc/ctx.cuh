@@ -64,7 +64,33 @@ struct SchurScratch {
   // band build: per level l, rr_lv[3l..3l+2] = the rows [lo, hi) of ainv's vorticity (l = 0)
   // and of its coarsified levels that hold data, and the treatment of the other rows
   int* rr_lv = nullptr;
+  // band build and sub-domain precompute: the finest-level box [box0, box1] x [box2, box3]
+  // outside which ainv's response to the column's source is below 1e-18 of its peak, and the
+  // coarse responses of level 1 (CoarseResp): with cr_R1 set the coarse levels' chain is the
+  // sum of the responses over the level-1 vertices coarsify fills from that box
+  int* box = nullptr;
+  const double* cr_R1 = nullptr;
+  const int* cr_idx1 = nullptr;
   cudaStream_t st = nullptr;
+};
+
+// The coarse levels' responses (coarse.cu).  For a level-k vertex v (k >= 1), R[k][slot(v)] is
+// the ring level k hands level k-1 when level k's vorticity is the unit vector at v and the
+// coarser levels hold its coarsified copies (the chain schur_fluid runs from level L-1 down to
+// k).  They depend on the grid alone, so they are computed once per vertex and kept for the
+// context's later builds.
+struct CoarseResp {
+  int* idx[kMaxLevels] = {};            // per level: slot of each vertex, -1 without a response
+  std::vector<int> idx_h[kMaxLevels];
+  double* R[kMaxLevels] = {};           // per level: slots x nbc ring values
+  int cap[kMaxLevels] = {}, n[kMaxLevels] = {};
+  int* items = nullptr;                 // the vertices one pass solves, level after level
+  size_t items_cap = 0;
+  int* err = nullptr;                   // a column's box met a level-1 vertex without a response
+  bool enabled = true;                  // IB_COARSE_RESP=0 at creation: the per-column chain
+  long long solves = 0;                 // level solves run
+  double ms = 0.0;                      // host wall time of the passes
+  size_t bytes = 0;
 };
 
 struct Influence {
@@ -77,7 +103,7 @@ struct Influence {
   std::vector<SchurScratch> bscr;
   double* bmem = nullptr;
   int* bint = nullptr;
-  static constexpr int kSetInts = 8 + 3 * kMaxLevels;   // prev, rr_in[3], column, rr_lv
+  static constexpr int kSetInts = 12 + 3 * kMaxLevels;   // prev, rr_in[3], column, box[4], rr_lv
   int trunc_rows = 0;   // rows of ainv's response kept on each side of a unit vector's row
   bool built = false;
   bool active = false;        // S holds the operator at the current positions
@@ -107,6 +133,7 @@ struct Influence {
   int* rr_out = nullptr;
   long long builds = 0, columns = 0, assemblies = 0, fallbacks = 0;
   double build_ms = 0.0;
+  CoarseResp cr;
 };
 
 // A fixed phase of the time step replayed as one CUDA graph.
@@ -401,6 +428,15 @@ int sd_setup(Ctx* c, int full_rectangular, double sdxi, double sdxe, double sdyi
              std::string* msg);
 int sd_precompute(Ctx* c);
 int sd_assemble(Ctx* c, bool interp);                     // (P at the current positions,) lumat into inf.St
+int launch_sd_lumat(Ctx* c, cudaStream_t st);             // lumat from P and the B rows already formed
+// coarse.cu: the coarse responses of the level-1 vertices coarsify fills from the marked
+// finest-level vertices (ns flags); IB_ERR_NOMEM when they would take more memory than allowed
+// (the callers then run the per-column chain)
+int cr_prepare(Ctx* c, const std::vector<unsigned char>& fine_mask);
+int launch_cr_ring0(Ctx* c, const SchurScratch& sc, cudaStream_t st);
+void cr_free(Ctx* c);
+// the finest-level vertices within r of a marked one, in x and in y (the boxes of the sources)
+void cr_dilate(const GridDims& g, std::vector<unsigned char>& mask, int r);
 int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st); // rhsf = P E_o (q + q0) + rhsf
 int launch_sd_spread(Ctx* c, const double* f, double* hx, double* hy, cudaStream_t st);   // E_o^T P^T f
 int sd_write(Ctx* c, const char* path, std::string* msg);

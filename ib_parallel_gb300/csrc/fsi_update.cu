@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(128) k_fsi_update(FsiUpdateArgs a) {
     const int r0 = max(0, cy - 5), r1 = min(a.g.nsy - 1, cy + 2);
     if (r0 < a.rows[0] || r1 >= a.rows[1]) atomicOr(a.flag, 4);
   }
-  for (int t = tid; t < 8 * 64; t += blockDim.x) {
+  for (int t = tid; a.pval && t < 8 * 64; t += blockDim.x) {   // no patches without a band
     const int u = t >> 6, q = t & 63;
     if (k0 + u >= kend) break;
     patch_entry(a.g, k0 + u, q, a.comp[k0 + u] == 1, org[u][0], org[u][1], wsm[u], a.tile_of, a.ntx, a.tile,

@@ -207,7 +207,7 @@ __global__ void k_inf_col_init(int* col, int c0) {
 // whose 3-row stencil meets them); the other rows of a coarse level are zero apart from the
 // ring's first and last samples (closed form), except its two edge rows, which are transformed.
 __global__ void k_inf_unit_at(const int* col, const int2* __restrict__ tiles, GridDims g, double* vort, int* prev,
-                              int* rr_in, int* rr_lv, int L, int R) {
+                              int* rr_in, int* rr_lv, int* box, int L, int R) {
   IB_GRID_DEP_WAIT();
   if (threadIdx.x != 0) return;
   const int c = *col;
@@ -225,11 +225,17 @@ __global__ void k_inf_unit_at(const int* col, const int2* __restrict__ tiles, Gr
     rr_in[1] = b + 1;
     lo = max(0, b - R);
     hi = min(g.nsy, b + R + 1);
+    box[0] = max(0, a - R);
+    box[1] = min(g.nsx - 1, a + R);
   } else {
     *prev = -1;
     rr_in[0] = 0;
     rr_in[1] = 1;
+    box[0] = 0;
+    box[1] = -1;
   }
+  box[2] = lo;
+  box[3] = hi - 1;
   rr_in[2] = ROW_ZERO;
   rr_lv[0] = lo; rr_lv[1] = hi; rr_lv[2] = ROW_ZERO;
   for (int l = 1; l < L; ++l) {
@@ -352,7 +358,8 @@ int inf_build_scratch(Ctx* c) {
     sc.sbc = b + (4 + L) * ns;
     sc.prev = I.bint + Influence::kSetInts * i;
     sc.rr_in = sc.prev + 1;
-    sc.rr_lv = sc.prev + 8;
+    sc.box = sc.prev + 8;
+    sc.rr_lv = sc.prev + 12;
     if (cudaStreamCreateWithFlags(&sc.st, cudaStreamNonBlocking) != cudaSuccess) {
       sc.st = nullptr;
       return IB_ERR_CUDA;
@@ -367,6 +374,7 @@ void inf_free(Ctx* c) {
     if (sc.st) cudaStreamDestroy(sc.st);
   if (I.bmem) cudaFree(I.bmem);
   if (I.bint) cudaFree(I.bint);
+  cr_free(c);
   free_band(I);
   if (I.pval) cudaFree(I.pval);
   if (I.pidx) cudaFree(I.pidx);
@@ -473,6 +481,25 @@ int inf_build(Ctx* c) {
   // Each set's columns run as one captured graph: a while node whose body is one column with
   // the column index on the device, so the host launches one graph per set.
   RC(inf_build_scratch(c));
+  // the coarse levels' responses for the level-1 vertices these columns reach (coarse.cu);
+  // without them (memory, or switched off) each column runs the coarse chain itself
+  bool use_cr = false;
+  if (c->L > 1 && I.cr.enabled) {
+    std::vector<unsigned char> mask(g.ns, 0);
+    for (const int2& t : I.tiles_h)
+      for (int q = 0; q < kP; ++q) {
+        const int a = t.x * kT + (q % kT), b = t.y * kT + q / kT;
+        if (a < g.nsx && b < g.nsy) mask[(size_t)b * g.nsx + a] = 1;
+      }
+    cr_dilate(g, mask, I.trunc_rows);
+    const int rcc = cr_prepare(c, mask);
+    if (rcc != IB_OK && rcc != IB_ERR_NOMEM) return rcc;
+    use_cr = rcc == IB_OK;
+  }
+  for (SchurScratch& sc : I.bscr) {
+    sc.cr_R1 = use_cr ? I.cr.R[1] : nullptr;
+    sc.cr_idx1 = use_cr ? I.cr.idx[1] : nullptr;
+  }
   cudaStream_t st = c->st;
   const int S = std::min(Influence::kBuildStreams, I.nR);
   cudaEvent_t ev = nullptr;
@@ -506,7 +533,7 @@ int inf_build(Ctx* c) {
       if (rc == IB_OK) {
         const long long b0 = launch_count();
         count_launch();
-        k_inf_unit_at<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in, sc.rr_lv, c->L,
+        k_inf_unit_at<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in, sc.rr_lv, sc.box, c->L,
                                            I.trunc_rows);
         const double* ring0 = nullptr;
         rc = schur_fluid(c, sc.vort, sc.rr_in, I.rr_out, sc.s0, &ring0, &sc);
@@ -535,6 +562,7 @@ int inf_build(Ctx* c) {
     for (int col = 0; col < I.nR && rc == IB_OK; ++col) {
       SchurScratch sc = I.bscr[col % S];
       sc.rr_lv = nullptr;   // every row transformed
+      sc.cr_R1 = nullptr;   // and the coarse chain run per column
       count_launch();
       k_inf_unit<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in);
       const double* ring0 = nullptr;
@@ -560,8 +588,14 @@ int inf_build(Ctx* c) {
     if (e) cudaGraphExecDestroy(e);
   if (cap) cudaStreamDestroy(cap);
   cudaEventDestroy(ev);
+  for (SchurScratch& sc : I.bscr) sc.cr_R1 = nullptr;
   RC(rc);
   IB_CUDA_CHECK(cudaStreamSynchronize(st));
+  if (use_cr) {
+    int err = 0;
+    IB_CUDA_CHECK(cudaMemcpy(&err, I.cr.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return IB_ERR_STATE;   // a column met a vertex without a response
+  }
   I.columns += I.nR;
   I.builds += 1;
   I.built = true;

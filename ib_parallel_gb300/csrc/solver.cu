@@ -415,6 +415,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->tl.Mb = 4;
   c->use_fused = p.schur_mode != 2;
   if (const char* w = std::getenv("IB_WHOLE_STEP")) c->use_whole_step = std::atoi(w) != 0;
+  if (const char* w = std::getenv("IB_COARSE_RESP")) c->inf.cr.enabled = std::atoi(w) != 0;
   if (p.autotune) {
     rc = tune(c);
     if (rc != IB_OK) { *msg = "DST tuning failed"; ctx_destroy(c); return rc; }
@@ -689,7 +690,13 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
   }
   mark(2);
   const double* ring0 = c->zero_ring;
-  if (L > 1) {
+  if (L > 1 && sc->cr_R1) {
+    // the coarse levels by superposition of their responses (coarse.cu)
+    RC(launch_coarsify(g, sc->w[0], sc->w[1], st));
+    mark(3);
+    RC(launch_cr_ring0(c, *sc, st));
+    ring0 = sc->sbc;
+  } else if (L > 1) {
     // outside their centres the coarse vorticities of the operator stay zero
     for (int k = 1; k < L; ++k) RC(launch_coarsify(g, sc->w[k - 1], sc->w[k], st));
     mark(3);
@@ -1184,17 +1191,23 @@ static int capture_fsi_loop(Ctx* c, cudaStream_t st) {
         if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s2));
         RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s2));
         if (c->ub_on) RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, s2));
-        RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s2));
+        if (c->sd.on) RC(launch_sd_rhs(c, c->rhsf, s2));   // P at these positions, then P E_o q
+        else RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s2));
         IB_CUDA_CHECK(cudaEventRecord(ev_rhs, s2));
         // s3: a copy of the current origins and weights and their contribution lists
         RC(launch_reg_snapshot(c->nf, c->reg, c->reg_ix_s, c->reg_iy_s, c->reg_w_s, s3));
         RC(launch_reg_lists(c->nf, c->reg, g, s3));
         IB_CUDA_CHECK(cudaMemsetAsync(c->reg.stale, 0, sizeof(int), s3));   // for the weights below
         IB_CUDA_CHECK(cudaEventRecord(ev_lists, s3));
-        // s1: assembly and solve
-        RC(inf_assemble_kp(c, s1, true));
-        IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));
-        RC(inf_assemble_ptk(c, s1));
+        // s1: assembly (the sub-domain's lumat from P and the B rows of s2) and solve
+        if (c->sd.on) {
+          IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));
+          RC(launch_sd_lumat(c, s1));
+        } else {
+          RC(inf_assemble_kp(c, s1, true));
+          IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));
+          RC(inf_assemble_ptk(c, s1));
+        }
         RC(launch_gmres_fused(c->G, &c->fused_plan, I.St, c->rhsf, c->f, p.rtol, p.atol, p.gmres_max_it, s1));
         // s2: redistribution with the copy, beside the structure update and the weights and
         // patches at the new positions on s1
@@ -1222,7 +1235,7 @@ static int capture_fsi_loop(Ctx* c, cudaStream_t st) {
         u.g = g; u.nf = c->nf; u.ox = p.offsetx; u.oy = p.offsety; u.comp = c->reg.comp;
         u.ix = c->reg.ix; u.iy = c->reg.iy; u.w = c->reg.w; u.stale = c->reg.stale; u.d_err = c->d_err;
         u.tile_of = I.tile_of; u.ntx = I.ntx; u.tile = Influence::kTile;
-        u.pval = I.pval; u.pidx = I.pidx; u.used = I.used; u.flag = I.flag;
+        u.pval = c->sd.on ? nullptr : I.pval; u.pidx = I.pidx; u.used = I.used; u.flag = I.flag;
         u.rows = c->v2f_partial ? c->v2f_rows : nullptr;
         u.cnt = c->fsi_cnt; u.ist = c->G.ist; u.tol = p.fsi_tol; u.max_it = p.fsi_max_it; u.h = h;
         u.done = c->fsi_done;
@@ -1434,9 +1447,9 @@ static int whole_step_mode(Ctx* c) {
   if (c->nf == 0 || (p.num_stat && c->chol_ready)) return 2;
   if (p.num_stat) return 0;
   const Influence& I = c->inf;
-  const bool loop = (c->nt > 0) && c->nbeam == 0 && !c->sd.on && p.schur_mode != 1 && c->use_fused &&
-                    !c->graph_fsi_loop.failed &&
-                    c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
+  const bool operator_ready = c->sd.on ? c->sd.ready : (I.built && I.patch_fresh && I.flag_h == 0);
+  const bool loop = (c->nt > 0) && c->nbeam == 0 && p.schur_mode != 1 && c->use_fused &&
+                    !c->graph_fsi_loop.failed && c->fused_plan.state == 1 && operator_ready;
   return loop ? 1 : 0;
 }
 
@@ -1606,10 +1619,10 @@ int op_advance_begin(Ctx* c) {
       // band built, the matrix-free operator or per-phase timing)
       {
         Influence& I = c->inf;
+        const bool operator_ready = c->sd.on ? c->sd.ready : (I.built && I.patch_fresh && I.flag_h == 0);
         const bool device_loop = moved && p.schur_mode != 1 && c->use_step_graphs && c->use_fused && !c->prof_on &&
-                                 !c->stage_on && (!c->step_prof || c->step_prof_dev) && c->nbeam == 0 && !c->sd.on &&
-                                 !c->graph_fsi_loop.failed &&
-                                 c->fused_plan.state == 1 && I.built && I.patch_fresh && I.flag_h == 0;
+                                 !c->stage_on && (!c->step_prof || c->step_prof_dev) && c->nbeam == 0 &&
+                                 !c->graph_fsi_loop.failed && c->fused_plan.state == 1 && operator_ready;
         if (device_loop && (c->graph_fsi_loop.exec || build_fsi_loop(c) == IB_OK)) {
           IB_CUDA_CHECK(cudaGraphLaunch(c->graph_fsi_loop.exec, st));
           IB_CUDA_CHECK(cudaMemcpyAsync(c->h_ist, c->fsi_cnt, 5 * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -64,7 +64,7 @@ __global__ void k_sd_col_next(int* col, int stride, int ncol, cudaGraphCondition
 // level the rows coarsify fills from those.
 __global__ void k_sd_source(const int* col, const int* __restrict__ comp, const int* __restrict__ ix,
                             const int* __restrict__ iy, const double* __restrict__ w, GridDims g, double* vort,
-                            int* prev, int* rr_in, int* rr_lv, int L, int R) {
+                            int* prev, int* rr_in, int* rr_lv, int* box, int L, int R) {
   IB_GRID_DEP_WAIT();
   const int q = threadIdx.x;
   const int u = *col;
@@ -94,6 +94,10 @@ __global__ void k_sd_source(const int* col, const int* __restrict__ comp, const 
   rr_in[2] = ROW_ZERO;
   int lo = max(0, b0 - R), hi = min(g.nsy, b1 + R);
   rr_lv[0] = lo; rr_lv[1] = hi; rr_lv[2] = ROW_ZERO;
+  box[0] = max(0, cx - 5 - R);
+  box[1] = min(g.nsx - 1, cx + 2 + R);
+  box[2] = lo;
+  box[3] = hi - 1;
   for (int lv = 1; lv < L; ++lv) {
     int r0 = max(1, lo - 1), r1 = min(g.n - 3, hi);
     if ((r0 & 1) == 0) r0 += 1;
@@ -292,28 +296,33 @@ __device__ __forceinline__ double b_at(const long long* __restrict__ colptr, con
 
 // compute_operator (operators_struct.F90:840-905): lumat(k, l) = body(k, l) + sum_q P(k,q)
 // inter(l, a_q(k)), inter(l, a) = sum_r B(b_r(l), a) P(l, r), each dot product in order; written
-// into the solver's column-major operator St[l][k].  body: b_times2's matrix (body_mat).
-__global__ void k_sd_lumat(int nf, const int* __restrict__ pidx, const double* __restrict__ pw,
-                           const long long* __restrict__ colptr, const int* __restrict__ nz,
-                           const int* __restrict__ rows, const double* __restrict__ vals,
-                           const double* __restrict__ brv, const double* __restrict__ bco,
-                           const int* __restrict__ bod, double* __restrict__ St) {
+// into the solver's column-major operator St[l][k].  body: b_times2's matrix (body_mat).  Sixteen
+// lanes per entry, lane 4q + r finding B(b_r(l), a_q(k)) by its own binary search (the searches
+// are the latency); the group's first lane sums the products in the order above.
+__global__ void __launch_bounds__(128) k_sd_lumat(int nf, const int* __restrict__ pidx, const double* __restrict__ pw,
+                                                  const long long* __restrict__ colptr, const int* __restrict__ nz,
+                                                  const int* __restrict__ rows, const double* __restrict__ vals,
+                                                  const double* __restrict__ brv, const double* __restrict__ bco,
+                                                  const int* __restrict__ bod, double* __restrict__ St) {
   IB_GRID_DEP_WAIT();
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane & 15, q = sub >> 2, r = sub & 3;
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;   // 8 entries of column k a CTA
   const int k = blockIdx.y;
-  if (l >= nf) return;
-  int bl[4];
-  double wl[4];
-  for (int r = 0; r < 4; ++r) {
-    bl[r] = pidx[4 * l + r];
-    wl[r] = pw[4 * l + r];
-  }
+  const bool live = l < nf;
+  double prod = 0.0;
+  if (live) prod = __dmul_rn(b_at(colptr, nz, rows, vals, pidx[4 * l + r], pidx[4 * k + q]), pw[4 * l + r]);
+  double v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __shfl_sync(0xffffffffu, prod, (lane & 16) + i);
+  if (!live || sub != 0) return;
   double dot = 0.0;
-  for (int q = 0; q < 4; ++q) {
-    const int a = pidx[4 * k + q];
+#pragma unroll
+  for (int qq = 0; qq < 4; ++qq) {
     double inter = 0.0;
-    for (int r = 0; r < 4; ++r) inter = __dadd_rn(inter, __dmul_rn(b_at(colptr, nz, rows, vals, bl[r], a), wl[r]));
-    dot = __dadd_rn(dot, __dmul_rn(pw[4 * k + q], inter));
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) inter = __dadd_rn(inter, v[4 * qq + rr]);
+    dot = __dadd_rn(dot, __dmul_rn(pw[4 * k + qq], inter));
   }
   const int bk = bod[k];
   const double body = (bk >= 0 && bod[l] == bk) ? brv[k] * brv[l] * bco[k] : 0.0;
@@ -331,19 +340,30 @@ __global__ void k_sd_rhs(int nf, const int* __restrict__ pidx, const double* __r
   rhsf[k] = __dadd_rn(dot, rhsf[k]);
 }
 
-// P^T f (timestepper.F90:502: matmul over the body unknowns in order) on every sub-domain unknown
-__global__ void k_sd_ptf(int nf, int nf_sd, const int* __restrict__ pidx, const double* __restrict__ pw,
-                         const double* __restrict__ f, double* __restrict__ fsd) {
+// P^T f (timestepper.F90:502: matmul over the body unknowns in order) on every sub-domain unknown.
+// The entries (k, q) of P pass through shared memory in chunks, each with its product
+// P(k,q) f(k); every thread scans them in order for its own cloud unknown.
+__global__ void __launch_bounds__(128) k_sd_ptf(int nf, int nf_sd, const int* __restrict__ pidx,
+                                                const double* __restrict__ pw, const double* __restrict__ f,
+                                                double* __restrict__ fsd) {
+  constexpr int kChunk = 1024;
+  __shared__ int sidx[kChunk];
+  __shared__ double sprod[kChunk];
   IB_GRID_DEP_WAIT();
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= nf_sd) return;
   double acc = 0.0;
-  for (int k = 0; k < nf; ++k) {
-    for (int q = 0; q < 4; ++q) {
-      if (pidx[4 * k + q] == a) acc = __dadd_rn(acc, __dmul_rn(pw[4 * k + q], f[k]));
+  for (int e0 = 0; e0 < 4 * nf; e0 += kChunk) {
+    const int ne = min(kChunk, 4 * nf - e0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+      sidx[e] = pidx[e0 + e];
+      sprod[e] = __dmul_rn(pw[e0 + e], f[(e0 + e) >> 2]);
     }
+    __syncthreads();
+    for (int e = 0; e < ne; ++e)
+      if (sidx[e] == a) acc = __dadd_rn(acc, sprod[e]);
   }
-  fsd[a] = acc;
+  if (a < nf_sd) fsd[a] = acc;
 }
 
 int launch_sd_interp(Ctx* c, cudaStream_t st) {
@@ -529,6 +549,9 @@ int sd_setup(Ctx* c, int full_rectangular, double sdxi, double sdxe, double sdyi
     return bad(rc, "sub-domain setup failed on the device");
   }
   c->sd = S;
+  // the cloud's stencils read the finest fluxes away from the body: the step's first vort2flux
+  // forms every row
+  c->v2f_partial = false;
   return IB_OK;
 }
 
@@ -539,6 +562,27 @@ int sd_precompute(Ctx* c) {
   Influence& I = c->inf;
   const auto t0 = std::chrono::steady_clock::now();
   RC(inf_build_scratch(c));
+  // the coarse levels' responses for the level-1 vertices the columns reach (coarse.cu)
+  bool use_cr = false;
+  if (c->L > 1 && I.cr.enabled) {
+    std::vector<int> ixh(S.nf_sd), iyh(S.nf_sd);
+    IB_CUDA_CHECK(cudaStreamSynchronize(c->st));
+    IB_CUDA_CHECK(cudaMemcpy(ixh.data(), S.reg.ix, 4 * (size_t)S.nf_sd, cudaMemcpyDeviceToHost));
+    IB_CUDA_CHECK(cudaMemcpy(iyh.data(), S.reg.iy, 4 * (size_t)S.nf_sd, cudaMemcpyDeviceToHost));
+    std::vector<unsigned char> mask(g.ns, 0);
+    for (int u = 0; u < S.nf_sd; ++u)
+      for (int b = std::max(0, iyh[u] - 5); b <= std::min(g.nsy - 1, iyh[u] + 2); ++b)
+        for (int a = std::max(0, ixh[u] - 5); a <= std::min(g.nsx - 1, ixh[u] + 2); ++a)
+          mask[(size_t)b * g.nsx + a] = 1;
+    cr_dilate(g, mask, I.trunc_rows);
+    const int rcc = cr_prepare(c, mask);
+    if (rcc != IB_OK && rcc != IB_ERR_NOMEM) return rcc;
+    use_cr = rcc == IB_OK;
+  }
+  for (SchurScratch& sc : I.bscr) {
+    sc.cr_R1 = use_cr ? I.cr.R[1] : nullptr;
+    sc.cr_idx1 = use_cr ? I.cr.idx[1] : nullptr;
+  }
   // the candidate values of every column, before the drop (freed once compacted)
   if (S.rows) cudaFree(S.rows);
   if (S.vals) cudaFree(S.vals);
@@ -590,7 +634,7 @@ int sd_precompute(Ctx* c) {
         const long long b0 = launch_count();
         count_launch();
         k_sd_source<<<1, kPatch, 0, sc.st>>>(col, S.ucomp, S.reg.ix, S.reg.iy, S.reg.w, g, sc.vort, pprev, sc.rr_in,
-                                             sc.rr_lv, c->L, I.trunc_rows);
+                                             sc.rr_lv, sc.box, c->L, I.trunc_rows);
         const double* ring0 = nullptr;
         rc = schur_fluid(c, sc.vort, sc.rr_in, S.reg.bbox + 7, sc.s0, &ring0, &sc);
         count_launches(3);
@@ -629,6 +673,12 @@ int sd_precompute(Ctx* c) {
     if (e) cudaGraphExecDestroy(e);
   if (cap) cudaStreamDestroy(cap);
   cudaEventDestroy(ev);
+  for (SchurScratch& sc : I.bscr) sc.cr_R1 = nullptr;
+  if (rc == IB_OK && use_cr) {
+    int err = 0;
+    if (cudaMemcpy(&err, I.cr.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) rc = IB_ERR_CUDA;
+    else if (err) rc = IB_ERR_STATE;   // a column met a vertex without a response
+  }
   // compaction: the kept rows of every column, back to back
   if (rc == IB_OK) {
     std::vector<int> nz(S.nf_sd);
@@ -664,17 +714,21 @@ int sd_precompute(Ctx* c) {
   return check_err(c);
 }
 
-int sd_assemble(Ctx* c, bool interp) {
+int launch_sd_lumat(Ctx* c, cudaStream_t st) {
   SubDomain& S = c->sd;
   Influence& I = c->inf;
-  cudaStream_t st = c->st;
-  if (interp) RC(launch_sd_interp(c, st));
-  RC(inf_assemble_b(c, st));
   count_launch();
-  k_sd_lumat<<<dim3(cdiv(c->nf, 128), c->nf), 128, 0, st>>>(c->nf, S.pidx, S.pw, S.colptr, S.nz, S.rows, S.vals,
+  k_sd_lumat<<<dim3(cdiv(c->nf, 8), c->nf), 128, 0, st>>>(c->nf, S.pidx, S.pw, S.colptr, S.nz, S.rows, S.vals,
                                                            I.brv, I.bco, I.bod, I.St);
   IB_CUDA_CHECK(cudaGetLastError());
   return launch_beam_add_b(c, I.St, st);
+}
+
+int sd_assemble(Ctx* c, bool interp) {
+  cudaStream_t st = c->st;
+  if (interp) RC(launch_sd_interp(c, st));
+  RC(inf_assemble_b(c, st));
+  return launch_sd_lumat(c, st);
 }
 
 int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st) {

@@ -43,6 +43,7 @@ EXPORTS = [
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
     "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state", "ib_get_step_graph_stats",
+    "ib_get_coarse_stats",
     "ib_subdomain_setup", "ib_subdomain_precompute", "ib_write_subdomain_matrix", "ib_read_subdomain_matrix",
     "ib_subdomain_operator", "ib_get_subdomain_stats", "ib_adjoint_forward", "ib_adjoint_backward",
 ]
@@ -136,6 +137,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_calculate_pressure": ([P, P], C.c_int), "ib_write_pressure": ([P, C.c_char_p], C.c_int),
         "ib_get_beam_state": ([P, P, P, P], C.c_int),
         "ib_get_step_graph_stats": ([P, C.POINTER(C.c_longlong)], C.c_int),
+        "ib_get_coarse_stats": ([P, C.POINTER(C.c_longlong), C.POINTER(C.c_double)], C.c_int),
         "ib_subdomain_setup": ([P, C.c_int] + [C.c_double] * 5, C.c_int),
         "ib_subdomain_precompute": ([P], C.c_int),
         "ib_write_subdomain_matrix": ([P, C.c_char_p], C.c_int),
@@ -479,6 +481,15 @@ class Simulation:
         counts = (C.c_longlong * 3)()
         _check(self.lib.ib_get_step_graph_stats(self.h, counts), "ib_get_step_graph_stats")
         return {"graph": counts[0], "gate_closed": counts[1], "phased": counts[2]}
+
+    def coarse_stats(self) -> dict:
+        """The coarse levels' responses behind the band build and the sub-domain precompute:
+        level solves run, responses held, their bytes, whether enabled, host milliseconds."""
+        counts = (C.c_longlong * 4)()
+        ms = C.c_double()
+        _check(self.lib.ib_get_coarse_stats(self.h, counts, C.byref(ms)), "ib_get_coarse_stats")
+        return {"solves": counts[0], "held": counts[1], "bytes": counts[2], "enabled": bool(counts[3]),
+                "ms": ms.value}
 
     def profile(self, enable: bool):
         _check(self.lib.ib_profile(self.h, int(bool(enable))), "ib_profile")

@@ -320,6 +320,13 @@ int ib_schur_matrix(IbCtx* ctx, double* S, int* status);
 /* influence-matrix work since creation: counts = {band builds, columns computed, assemblies,
  * matrix-free fallbacks, band vertices}, build_ms = host wall time of the builds */
 int ib_get_influence_stats(IbCtx* ctx, long long* counts, double* build_ms);
+/* The coarse levels' responses behind the influence-band build and the sub-domain precompute
+ * (no reference counterpart: both evaluate the reference's a_times_sd / a_times2 chain,
+ * operators_fluid.F90:14-199, column by column; here the coarse levels' part of every column is
+ * a sum of per-vertex responses computed once).  counts[4] = {coarse level solves run, responses
+ * held, bytes they take, 1 when enabled}, ms = host wall time of the passes that computed them.
+ * The environment variable IB_COARSE_RESP=0 at ib_create runs the coarse chain per column. */
+int ib_get_coarse_stats(IbCtx* ctx, long long* counts, double* ms);
 /* How the steps since creation ran (no reference counterpart: the reference's advance,
  * timestepper.F90:18-556, is one host routine).  counts[3] = {steps launched as one CUDA graph
  * (predictor, first vort2flux, forces, correction: from the second step on, when the FSI

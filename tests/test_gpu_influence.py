@@ -6,6 +6,8 @@ a_times on unit vectors; steps through the assembled operator must match steps t
 matrix-free one; moving the stencils out of the band rebuilds it; stencils that touch the
 domain boundary fall back to the matrix-free operator.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -15,6 +17,18 @@ from ib_parallel_gb300 import ibgpu as G
 pytestmark = pytest.mark.gpu
 
 TOL_MAT = 1e-11   # assembled vs matrix-free operator (FP64 round-off of ~50-term sums)
+
+
+def _without_coarse_responses(make):
+    old = os.environ.get("IB_COARSE_RESP")
+    os.environ["IB_COARSE_RESP"] = "0"
+    try:
+        return make()
+    finally:
+        if old is None:
+            del os.environ["IB_COARSE_RESP"]
+        else:
+            os.environ["IB_COARSE_RESP"] = old
 
 
 def _matrix_free(g):
@@ -138,3 +152,31 @@ def test_schur_with_points_on_grid_lines():
     So = np.stack([o.a_times(e, with_b=False) for e in np.eye(o.nf)], axis=1)
     assert rel(S, So) < TOL_MAT
     g.close()
+
+
+def test_coarse_responses_match_the_per_column_chain():
+    # the band's columns with the coarse levels summed from per-vertex responses against the same
+    # columns with each column's own coarse chain (IB_COARSE_RESP=0): round-off apart; a rebuild
+    # around moved stencils solves only the vertices it has no response for yet
+    body = small_plate()
+    a = G.Simulation(G.Params(**dict(PLATE, influence_margin=2)), [body])
+    b = _without_coarse_responses(lambda: G.Simulation(G.Params(**dict(PLATE, influence_margin=2)), [body]))
+    Sa, Sb = a.schur_matrix(), b.schur_matrix()
+    assert Sa is not None and Sb is not None
+    assert rel(Sa, Sb) < 1e-13
+    assert rel(Sa, _matrix_free(a)) < TOL_MAT
+    ca, cb = a.coarse_stats(), b.coarse_stats()
+    assert ca["enabled"] and ca["solves"] > 0 and ca["held"] == ca["solves"] and ca["bytes"] > 0
+    assert not cb["enabled"] and cb["solves"] == 0
+    d = PLATE["len"] / PLATE["m"]
+    for g in (a, b):
+        xb = g.get_vector("xb") + 12.0 * d
+        yb = g.get_vector("yb") + 3.0 * d
+        G._check(g.lib.ib_reg_prep(g.h, G._ptr(xb), G._ptr(yb)), "ib_reg_prep")
+    Sa, Sb = a.schur_matrix(), b.schur_matrix()
+    assert a.influence_stats()["builds"] == 2 and b.influence_stats()["builds"] == 2
+    assert rel(Sa, Sb) < 1e-13
+    ca2 = a.coarse_stats()
+    assert ca["solves"] < ca2["solves"] < 2 * ca["solves"] and ca2["held"] == ca2["solves"]
+    a.close()
+    b.close()

@@ -3,6 +3,8 @@
 the FSI operator lumat = body + P B^T P^T, the sd_precomputed.chd file both ways, steps
 conditional on the Krylov solve (one FSI iteration a step, the oracle handed the GPU's forces),
 free-running steps, a stationary rigid body inside the cloud, and a body leaving the cloud."""
+import os
+
 import numpy as np
 import pytest
 
@@ -85,13 +87,67 @@ def test_free_running_steps(plate_pair):
     _setup(o, g, CLOUD)
     g.read_subdomain_matrix(path)
     o.sd.cols = gpu.cols
-    for step in range(4):
+    for step in range(6):
         g.advance()
         o.advance()
         assert rel(g.get_field("omega", 0), o.omega[0]) < 1e-7, step
         assert abs(g.body_state()[0][0] - o.theta[0]) < 1e-7 * abs(o.theta[0]), step
     assert g.counters()[1] >= 2
+    assert g.step_graph_stats()["graph"] >= 3   # the later steps ran the FSI loop on the device
     g.close()
+
+
+def test_device_fsi_loop_matches_host_loop(plate_pair):
+    # from the second step the sub-domain's FSI iterations (P at the new positions, lumat, the
+    # solve, the structure update) run as the device loop inside the step's graph; with per-phase
+    # timing on they run from the host: the same kernels in the same order
+    _, _, _, path = plate_pair
+    kw = dict(PLATE, rtol=1e-12, fsi_tol=1e-11)
+    gd = G.Simulation(G.Params(**kw), [small_plate()])
+    gh = G.Simulation(G.Params(**kw), [small_plate()])
+    for g in (gd, gh):
+        g.subdomain_setup(*CLOUD)
+        g.read_subdomain_matrix(path)
+    gh.step_profile(1)
+    for _ in range(5):
+        gd.advance()
+        gh.advance()
+        assert gd.counters() == gh.counters()
+        assert np.array_equal(gd.get_vector("f"), gh.get_vector("f"))
+        assert np.array_equal(gd.get_vector("xb"), gh.get_vector("xb"))
+        assert np.array_equal(gd.body_state()[0], gh.body_state()[0])
+    for k in range(PLATE["mgridlev"]):
+        assert np.array_equal(gd.get_field("omega", k), gh.get_field("omega", k))
+    assert gd.step_graph_stats()["graph"] >= 3 and gh.step_graph_stats()["graph"] == 0
+    gd.close()
+    gh.close()
+
+
+def test_coarse_responses_match_the_per_column_chain(plate_pair, tmp_path):
+    # the precompute's columns with the coarse levels summed from per-vertex responses against
+    # the same columns with each column's own coarse chain (IB_COARSE_RESP=0)
+    o, g, gpu, _ = plate_pair
+    assert g.coarse_stats()["solves"] > 0
+    old = os.environ.get("IB_COARSE_RESP")
+    os.environ["IB_COARSE_RESP"] = "0"
+    try:
+        h = G.Simulation(G.Params(**PLATE), [small_plate()])
+    finally:
+        if old is None:
+            del os.environ["IB_COARSE_RESP"]
+        else:
+            os.environ["IB_COARSE_RESP"] = old
+    h.subdomain_setup(*CLOUD)
+    h.subdomain_precompute()
+    assert h.coarse_stats()["solves"] == 0
+    path = tmp_path / "chain.chd"
+    h.write_subdomain_matrix(path)
+    chain = SD.SubDomain(o, True, *CLOUD)
+    chain.read_chd(path)
+    for j, ((rg, vg), (rc, vc)) in enumerate(zip(gpu.cols, chain.cols)):
+        assert np.array_equal(rg, rc), j
+        assert rel(vg, vc) < 1e-13, (j, rel(vg, vc))
+    h.close()
 
 
 def test_computed_and_read_matrices_step_alike(plate_pair):
