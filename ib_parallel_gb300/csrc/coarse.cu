@@ -130,25 +130,39 @@ __global__ void k_cr_clear(double* vort, int* prev) {
 }
 
 // A column's ring0: the sum over the level-1 vertices its box reaches (rows, then vertices
-// along a row, in order) of w1[v] R_1[v], one thread per ring entry.
+// along a row, in order) of w1[v] R_1[v], one thread per ring entry.  With w0 given, every CTA
+// first forms the box's level-1 values from the finest field itself (k_coarsify's full-weighting
+// sum, the same expression) in shared memory; otherwise w1 holds them (launch_coarsify).
 __global__ void __launch_bounds__(128) k_cr_ring0(const int* __restrict__ box, GridDims g,
-                                                  const double* __restrict__ w1, const int* __restrict__ idx1,
-                                                  const double* __restrict__ R1, double* __restrict__ ring,
-                                                  int* __restrict__ err) {
+                                                  const double* __restrict__ w0, const double* __restrict__ w1,
+                                                  const int* __restrict__ idx1, const double* __restrict__ R1,
+                                                  double* __restrict__ ring, int* __restrict__ err) {
   IB_GRID_DEP_WAIT();
+  extern __shared__ double wb[];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int ca = g.m / 2 - 1, cb = g.n / 2 - 1;
   // coarse vertex a reads the fine vertices 2a .. 2a+2 (an empty box reaches none)
   const bool empty = box[1] < box[0] || box[3] < box[2];
   const int a0 = max(0, (box[0] - 1) / 2), a1 = empty ? -1 : min(ca - 1, box[1] / 2);
   const int b0 = max(0, (box[2] - 1) / 2), b1 = empty ? -1 : min(cb - 1, box[3] / 2);
+  const int na = a1 - a0 + 1;
+  if (w0) {
+    const int nq = na > 0 && b1 >= b0 ? na * (b1 - b0 + 1) : 0;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+      const int I = 2 * (a0 + q % na) + 3, J = 2 * (b0 + q / na) + 3;
+      auto F = [&](int ii, int jj) { return w0[(jj - 2) * g.nsx + (ii - 2)]; };
+      wb[q] = F(I, J) + 0.5 * (F(I + 1, J) + F(I, J + 1) + F(I - 1, J) + F(I, J - 1)) +
+              0.25 * (F(I + 1, J + 1) + F(I + 1, J - 1) + F(I - 1, J - 1) + F(I - 1, J + 1));
+    }
+    __syncthreads();
+  }
   double v = 0.0;
   for (int b = b0; b <= b1; ++b) {
     const int row = (b + g.n / 4) * g.nsx + g.m / 4;
     for (int a = a0; a <= a1; ++a) {
       const int o = row + a;
       const int s = idx1[o];
-      const double x = w1[o];
+      const double x = w0 ? wb[(b - b0) * na + (a - a0)] : w1[o];
       if (s < 0) {
         if (x != 0.0 && t == 0) atomicExch(err, 1);
         continue;
@@ -383,8 +397,14 @@ int cr_prepare(Ctx* c, const std::vector<unsigned char>& fine_mask) {
 
 int launch_cr_ring0(Ctx* c, const SchurScratch& sc, cudaStream_t st) {
   const GridDims& g = c->g;
+  // a box reaches at most trunc_rows + 6 level-1 vertices along each axis (a sub-domain patch of
+  // 8 widened by trunc_rows on both sides); past 48 KB of them coarsify runs on its own first
+  const size_t side = (size_t)c->inf.trunc_rows + 6, bytes = 8 * side * side;
+  const bool fused = bytes <= 48 * 1024;
+  if (!fused) RC(launch_coarsify(g, sc.w[0], sc.w[1], st));
   count_launch();
-  k_cr_ring0<<<cdiv(g.nbc, 128), 128, 0, st>>>(sc.box, g, sc.w[1], sc.cr_idx1, sc.cr_R1, sc.sbc, c->inf.cr.err);
+  k_cr_ring0<<<cdiv(g.nbc, 128), 128, fused ? bytes : 0, st>>>(sc.box, g, fused ? sc.w[0] : nullptr, sc.w[1],
+                                                                sc.cr_idx1, sc.cr_R1, sc.sbc, c->inf.cr.err);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -71,6 +71,11 @@ struct SchurScratch {
   int* box = nullptr;
   const double* cr_R1 = nullptr;
   const int* cr_idx1 = nullptr;
+  // band build: the column's source vertex and the rows of ainv's modes it wrote last (4 ints:
+  // a, b, the previous strip's rows [p0, p1)); with specY_ready the caller has formed ainv's
+  // modes in specY (zero outside the strip) and schur_fluid starts from them
+  int* strip = nullptr;
+  bool specY_ready = false;
   cudaStream_t st = nullptr;
 };
 
@@ -103,7 +108,12 @@ struct Influence {
   std::vector<SchurScratch> bscr;
   double* bmem = nullptr;
   int* bint = nullptr;
-  static constexpr int kSetInts = 12 + 3 * kMaxLevels;   // prev, rr_in[3], column, box[4], rr_lv
+  static constexpr int kSetInts = 16 + 3 * kMaxLevels;   // prev, rr_in[3], column, box[4], strip[4], rr_lv
+  // ainv's response to a unit vector on band row r in every x mode, rows r - trunc_rows ..
+  // r + trunc_rows, for the rows [strip_r0, strip_r0 + strip_n) (the band build)
+  double* strips = nullptr;
+  int strip_r0 = 0, strip_n = 0;
+  size_t strip_cap = 0;
   int trunc_rows = 0;   // rows of ainv's response kept on each side of a unit vector's row
   bool built = false;
   bool active = false;        // S holds the operator at the current positions

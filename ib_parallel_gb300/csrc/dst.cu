@@ -806,14 +806,41 @@ __global__ void k_dst_ring_rows(int N, GridDims g, const double* __restrict__ ri
 // per mode k reads row k of the (symmetric) DST matrix once for both dot products.  The other
 // CTAs take kRowsPerCta interior rows each, whose boundary field is zero except
 // x_1 = ring(left) and x_N = ring(right): Y_k = 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N), one FMA per
-// output from the row's two sums and the tabulated 2 sin(pi k/M).  In place allowed.
+// output from the row's two sums and the tabulated 2 sin(pi k/M).  With fft_edges the two edge
+// rows are instead transformed by the FFT line transform, one CTA each (about 2 x 700 FP64
+// instructions instead of 2 N^2 multiply-adds: for the band build's and the sub-domain
+// precompute's concurrent columns, which share the FP64 pipes).  In place allowed.
 constexpr int kRowsPerCta = 8;
 __global__ void __launch_bounds__(256) k_dst_bc_modes(DstDev pl, GridDims g, const double* __restrict__ ring,
                                                       const double* __restrict__ W, const double* __restrict__ sk2,
                                                       const double* __restrict__ post_add, double post_scale,
-                                                      double* __restrict__ out, int nEdge) {
+                                                      double* __restrict__ out, int nEdge, int fft_edges) {
   IB_GRID_DEP_WAIT();
   const int N = pl.N;
+  if (fft_edges && (int)blockIdx.x < nEdge) {
+    extern __shared__ double line[];   // the row (N, padded to N+1), then two P-point complex buffers
+    double2* zA = reinterpret_cast<double2*>(line + (N + 1));
+    double2* zB = zA + pl.P;
+    const int e = blockIdx.x;
+    const int J = e == 0 ? 2 : g.n;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      const int I = j + 2;
+      double v = 0.0;
+      if (I == 2) v = v + ring[g.left + J - 1];
+      if (I == g.m) v = v + ring[g.right + J - 1];
+      if (J == 2) v = v + ring[g.bottom + I - 1];
+      if (J == g.n) v = v + ring[g.top + I - 1];
+      line[j] = v;
+    }
+    __syncthreads();
+    dst_lines(pl, 1, line, N + 1, zA, zB, 1);
+    const size_t row = e == 0 ? 0 : (size_t)(g.nsy - 1) * g.nsx;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+      const size_t o = row + k;
+      out[o] = post_add ? fma(post_scale, post_add[o], line[k]) : line[k];
+    }
+    return;
+  }
   if ((int)blockIdx.x >= nEdge) {
     __shared__ double s_sum[kRowsPerCta][2];   // x_1 + x_N, x_1 - x_N per row
     const int r0 = 1 + ((int)blockIdx.x - nEdge) * kRowsPerCta;
@@ -878,15 +905,15 @@ __global__ void __launch_bounds__(256) k_dst_bc_modes(DstDev pl, GridDims g, con
 }
 
 int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W, const double* sk2,
-                   const double* post_add, double post_scale, double* out, cudaStream_t st) {
+                   const double* post_add, double post_scale, double* out, cudaStream_t st, bool fft_edges) {
   const int N = px.N;
-  const size_t smem = 2 * sizeof(double) * (size_t)N;
-  if (allow_dyn_smem(k_dst_bc_modes, smem) != cudaSuccess) return IB_ERR_CUDA;
-  const int nEdge = cdiv(N, 8);
+  const size_t smem = fft_edges ? sizeof(double) * 3 * ((size_t)N + 1) : 2 * sizeof(double) * (size_t)N;
+  if (allow_dyn_smem(k_dst_bc_modes, sizeof(double) * 3 * ((size_t)N + 1)) != cudaSuccess) return IB_ERR_CUDA;
+  const int nEdge = fft_edges ? 2 : cdiv(N, 8);
   const int nblk = nEdge + cdiv(std::max(0, g.nsy - 2), kRowsPerCta);
   DstDev d = to_dev(px);
   count_launch();
-  k_dst_bc_modes<<<nblk, 256, smem, st>>>(d, g, ring, W, sk2, post_add, post_scale, out, nEdge);
+  k_dst_bc_modes<<<nblk, 256, smem, st>>>(d, g, ring, W, sk2, post_add, post_scale, out, nEdge, fft_edges ? 1 : 0);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

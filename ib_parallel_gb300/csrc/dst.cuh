@@ -121,11 +121,12 @@ int dst_x_points(const DstPlan& px, const double* spec, int ld, const int2* pts,
 int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, const int* rows, int nrows,
                     const double* W, const double* post_add, double post_scale, double* out, cudaStream_t st);
 // out = post_scale*post_add + S_x(apply_bc(ring)) on every row (factor 1, zero field): the two
-// edge rows by dot products with W, the interior rows in closed form
-// 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) from sk2[k-1] = 2 sin(pi k/M) (dst_sin2_table).  In place
-// allowed (out == post_add).
+// edge rows by dot products with W (fft_edges: by the FFT line transform, fewer FP64 instructions
+// and a longer chain), the interior rows in closed form 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) from
+// sk2[k-1] = 2 sin(pi k/M) (dst_sin2_table).  In place allowed (out == post_add).
 int dst_x_bc_modes(const DstPlan& px, const GridDims& g, const double* ring, const double* W, const double* sk2,
-                   const double* post_add, double post_scale, double* out, cudaStream_t st);
+                   const double* post_add, double post_scale, double* out, cudaStream_t st,
+                   bool fft_edges = false);
 // ring = fac * get_bc of the inverse x transform of a coarser level's modes (spec, pitch ld),
 // evaluated at the points get_bc reads only (dot products with W).
 int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W, double fac,

@@ -248,6 +248,78 @@ __global__ void k_inf_unit_at(const int* col, const int2* __restrict__ tiles, Gr
     rr_lv[3 * l + 2] = l == L - 1 ? ROW_ZERO : ROW_EDGES;
   }
 }
+// The band column *col's rows (k_inf_unit_at's rr_lv for the finest level and box) without a
+// unit vector: the strip kernel below forms ainv's modes of it directly.  strip[0..1] = its
+// vertex (a, b); strip[2..3] = the rows the previous column's strip occupied.
+__global__ void k_inf_strip_rows_at(const int* col, const int2* __restrict__ tiles, GridDims g, int* strip,
+                                    int* rr_lv, int* box, int L, int R) {
+  IB_GRID_DEP_WAIT();
+  if (threadIdx.x != 0) return;
+  const int c = *col;
+  const int2 tc = tiles[c / kP];
+  const int q = c % kP;
+  const int a = tc.x * kT + (q % kT), b = tc.y * kT + q / kT;
+  strip[2] = rr_lv[0];
+  strip[3] = rr_lv[1];
+  int lo = 0, hi = 0;
+  if (a < g.nsx && b < g.nsy) {
+    lo = max(0, b - R);
+    hi = min(g.nsy, b + R + 1);
+    box[0] = max(0, a - R);
+    box[1] = min(g.nsx - 1, a + R);
+  } else {
+    box[0] = 0;
+    box[1] = -1;
+  }
+  box[2] = lo;
+  box[3] = hi - 1;
+  strip[0] = a;
+  strip[1] = b;
+  rr_lv[0] = lo; rr_lv[1] = hi; rr_lv[2] = ROW_ZERO;
+  for (int l = 1; l < L; ++l) {   // the coarse levels' rows, as k_inf_unit_at
+    int r0 = max(1, lo - 1), r1 = min(g.n - 3, hi);
+    if ((r0 & 1) == 0) r0 += 1;
+    if ((r1 & 1) == 0) r1 -= 1;
+    if (lo >= hi || r0 > r1) { lo = 0; hi = 0; }
+    else { lo = g.n / 4 + (r0 - 1) / 2; hi = g.n / 4 + (r1 - 1) / 2 + 1; }
+    rr_lv[3 * l] = lo; rr_lv[3 * l + 1] = hi;
+    rr_lv[3 * l + 2] = l == L - 1 ? ROW_ZERO : ROW_EDGES;
+  }
+}
+
+// ainv's modes of a unit vector at band vertex (a, b): the forward transform of the unit vector
+// is row a of the DST matrix W on row b, and ainv acts per mode, so on row y of the strip
+// specY[y][k] = W[a][k] A_b[y][k], A_b the tabulated response to the unit row.  The previous
+// strip's rows outside this one are cleared (specY is zero outside the current strip).
+// Grid: x over the modes, y over 2 (2R+1) row slots (the new strip's, then the old one's).
+__global__ void k_inf_strip(const int* __restrict__ strip, const int* __restrict__ rr_lv, GridDims g,
+                            const double* __restrict__ W, const double* __restrict__ A, int r0, int R,
+                            double* __restrict__ specY) {
+  IB_GRID_DEP_WAIT();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.nsx) return;
+  const int lo = rr_lv[0], hi = rr_lv[1];
+  const int sl = blockIdx.y, w = 2 * R + 1;
+  if (sl < w) {
+    const int y = lo + sl;
+    if (y >= hi) return;
+    const int a = strip[0], b = strip[1];
+    const double* Ab = A + ((size_t)(b - r0) * w + (y - (b - R))) * g.nsx;
+    specY[(size_t)y * g.nsx + k] = W[(size_t)a * g.nsx + k] * Ab[k];
+  } else {
+    const int y = strip[2] + (sl - w);
+    if (y < 0 || y >= strip[3] || (y >= lo && y < hi)) return;
+    specY[(size_t)y * g.nsx + k] = 0.0;
+  }
+}
+
+// The unit row r (every mode 1 on row r of a zeroed field) for the strip table.
+__global__ void k_inf_unit_row(GridDims g, int r, double* f) {
+  IB_GRID_DEP_WAIT();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < g.nsx) f[(size_t)r * g.nsx + k] = 1.0;
+}
+
 // K[*col][v] (k_inf_gather with the column read on the device).
 __global__ void k_inf_gather_at(const int* col, int nR, const int2* __restrict__ tiles, GridDims g,
                                 const double* __restrict__ s, double* __restrict__ K) {
@@ -313,6 +385,9 @@ int inf_alloc(Ctx* c) {
 }
 
 static void free_band(Influence& I) {
+  if (I.strips) cudaFree(I.strips);
+  I.strips = nullptr;
+  I.strip_cap = 0;
   if (I.K) cudaFree(I.K);
   if (I.used) cudaFree(I.used);
   if (I.ulist) cudaFree(I.ulist);
@@ -359,7 +434,8 @@ int inf_build_scratch(Ctx* c) {
     sc.prev = I.bint + Influence::kSetInts * i;
     sc.rr_in = sc.prev + 1;
     sc.box = sc.prev + 8;
-    sc.rr_lv = sc.prev + 12;
+    sc.strip = sc.prev + 12;
+    sc.rr_lv = sc.prev + 16;
     if (cudaStreamCreateWithFlags(&sc.st, cudaStreamNonBlocking) != cudaSuccess) {
       sc.st = nullptr;
       return IB_ERR_CUDA;
@@ -501,6 +577,44 @@ int inf_build(Ctx* c) {
     sc.cr_idx1 = use_cr ? I.cr.idx[1] : nullptr;
   }
   cudaStream_t st = c->st;
+  // ainv's response to a unit row, for every band row (the strips the columns scale by their row
+  // of W instead of transforming a unit vector and solving ainv each)
+  const int R = I.trunc_rows, wrows = 2 * R + 1;
+  bool use_strips = false;
+  {
+    const size_t need = (size_t)(bmax - bmin + 1) * wrows * g.nsx;
+    size_t freeb = 0, totalb = 0;
+    IB_CUDA_CHECK(cudaMemGetInfo(&freeb, &totalb));
+    if (need > I.strip_cap && 8 * need < freeb / 8) {
+      if (I.strips) cudaFree(I.strips);
+      I.strips = nullptr;
+      I.strip_cap = 0;
+      if (cudaMalloc(&I.strips, 8 * need) == cudaSuccess) I.strip_cap = need;
+      else cudaGetLastError();
+    }
+    use_strips = need <= I.strip_cap;
+  }
+  if (use_strips) {
+    I.strip_r0 = bmin;
+    I.strip_n = bmax - bmin + 1;
+    double* F = I.bscr[0].spec1;
+    for (int r = bmin; r <= bmax; ++r) {
+      IB_CUDA_CHECK(cudaMemsetAsync(F, 0, 8 * (size_t)g.ns, st));
+      count_launch();
+      k_inf_unit_row<<<cdiv(g.nsx, 256), 256, 0, st>>>(g, r, F);
+      RC(tri_solve(c->tri_ainv, F, F, g.nsx, c->tl, st));
+      const int lo = std::max(0, r - R), hi = std::min(g.nsy, r + R + 1);
+      IB_CUDA_CHECK(cudaMemcpyAsync(I.strips + ((size_t)(r - bmin) * wrows + (lo - (r - R))) * g.nsx,
+                                    F + (size_t)lo * g.nsx, 8 * (size_t)(hi - lo) * g.nsx,
+                                    cudaMemcpyDeviceToDevice, st));
+    }
+    // every set's ainv modes start from zero, with no strip recorded
+    for (const SchurScratch& sc : I.bscr) {
+      IB_CUDA_CHECK(cudaMemsetAsync(sc.specY, 0, 8 * (size_t)g.ns, st));
+      IB_CUDA_CHECK(cudaMemsetAsync(sc.rr_lv, 0, 2 * sizeof(int), st));
+    }
+  }
+  for (SchurScratch& sc : I.bscr) sc.specY_ready = use_strips;
   const int S = std::min(Influence::kBuildStreams, I.nR);
   cudaEvent_t ev = nullptr;
   IB_CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
@@ -532,9 +646,16 @@ int inf_build(Ctx* c) {
         rc = IB_ERR_CUDA;
       if (rc == IB_OK) {
         const long long b0 = launch_count();
-        count_launch();
-        k_inf_unit_at<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in, sc.rr_lv, sc.box, c->L,
-                                           I.trunc_rows);
+        if (use_strips) {
+          count_launches(2);
+          k_inf_strip_rows_at<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.strip, sc.rr_lv, sc.box, c->L, R);
+          k_inf_strip<<<dim3(cdiv(g.nsx, 128), 2 * wrows), 128, 0, sc.st>>>(sc.strip, sc.rr_lv, g, c->wmat,
+                                                                           I.strips, I.strip_r0, R, sc.specY);
+        } else {
+          count_launch();
+          k_inf_unit_at<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in, sc.rr_lv, sc.box, c->L,
+                                             I.trunc_rows);
+        }
         const double* ring0 = nullptr;
         rc = schur_fluid(c, sc.vort, sc.rr_in, I.rr_out, sc.s0, &ring0, &sc);
         count_launches(2);
@@ -563,6 +684,7 @@ int inf_build(Ctx* c) {
       SchurScratch sc = I.bscr[col % S];
       sc.rr_lv = nullptr;   // every row transformed
       sc.cr_R1 = nullptr;   // and the coarse chain run per column
+      sc.specY_ready = false;
       count_launch();
       k_inf_unit<<<1, 32, 0, sc.st>>>(col, I.tiles, g, sc.vort, sc.prev, sc.rr_in);
       const double* ring0 = nullptr;
@@ -588,7 +710,10 @@ int inf_build(Ctx* c) {
     if (e) cudaGraphExecDestroy(e);
   if (cap) cudaStreamDestroy(cap);
   cudaEventDestroy(ev);
-  for (SchurScratch& sc : I.bscr) sc.cr_R1 = nullptr;
+  for (SchurScratch& sc : I.bscr) {
+    sc.cr_R1 = nullptr;
+    sc.specY_ready = false;
+  }
   RC(rc);
   IB_CUDA_CHECK(cudaStreamSynchronize(st));
   if (use_cr) {

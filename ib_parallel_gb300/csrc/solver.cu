@@ -671,15 +671,17 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
   double* specY = sc->specY;
   double* spec1 = sc->spec1;
   auto mark = [&](int i) { if (c->stage_on) cudaEventRecord(c->stage_ev[i], st); };
-  {
-    DstXArgs a;
-    a.in = vort; a.out = specY; a.rowrange = rr_in;
-    ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-    RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
-  }
-  {
-    ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-    RC(tri_solve(c->tri_ainv, specY, specY, g.nsx, c->tl, st));
+  if (!sc->specY_ready) {   // else the band build has formed ainv's modes of its unit vector
+    {
+      DstXArgs a;
+      a.in = vort; a.out = specY; a.rowrange = rr_in;
+      ProfScope ps(c, 0, pass_bytes(c, 1, 1));
+      RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_small, st));
+    }
+    {
+      ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+      RC(tri_solve(c->tri_ainv, specY, specY, g.nsx, c->tl, st));
+    }
   }
   {
     DstXArgs a;
@@ -692,7 +694,6 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
   const double* ring0 = c->zero_ring;
   if (L > 1 && sc->cr_R1) {
     // the coarse levels by superposition of their responses (coarse.cu)
-    RC(launch_coarsify(g, sc->w[0], sc->w[1], st));
     mark(3);
     RC(launch_cr_ring0(c, *sc, st));
     ring0 = sc->sbc;
@@ -729,7 +730,7 @@ int schur_fluid(Ctx* c, const double* vort, const int* rr_in, const int* rr_out,
     // S_x(vort1 + apply_bc(ring0)) = 2m Y + transform of the boundary terms: the two full
     // boundary rows by dot products, the others in closed form (two nonzero samples)
     ProfScope ps(c, 0, pass_bytes(c, 1, 1));
-    RC(dst_x_bc_modes(c->px, g, ring0, c->wmat, c->sk2, specY, 2.0 * g.m, spec1, st));
+    RC(dst_x_bc_modes(c->px, g, ring0, c->wmat, c->sk2, specY, 2.0 * g.m, spec1, st, sc != &own));
   }
   mark(5);
   {
