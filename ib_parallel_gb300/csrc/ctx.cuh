@@ -443,6 +443,10 @@ int launch_sd_lumat(Ctx* c, cudaStream_t st);             // lumat from P and th
 // finest-level vertices (ns flags); IB_ERR_NOMEM when they would take more memory than allowed
 // (the callers then run the per-column chain)
 int cr_prepare(Ctx* c, const std::vector<unsigned char>& fine_mask);
+// influence.cu: ainv's strips for the rows r_lo..r_hi (inf_strip_alloc first: false when the
+// memory is not there)
+bool inf_strip_alloc(Ctx* c, int n);
+int inf_strip_table(Ctx* c, int r_lo, int r_hi);
 int launch_cr_ring0(Ctx* c, const SchurScratch& sc, cudaStream_t st);
 void cr_free(Ctx* c);
 // the finest-level vertices within r of a marked one, in x and in y (the boxes of the sources)

@@ -362,6 +362,54 @@ __global__ void k_inf_gather(int c, int nR, const int2* __restrict__ tiles, Grid
   K[(size_t)c * nR + i] = (a < g.nsx && b < g.nsy) ? s[b * g.nsx + a] : 0.0;
 }
 
+// Room for the strips of n rows (false: not available, the columns transform and solve ainv
+// themselves).
+bool inf_strip_alloc(Ctx* c, int n) {
+  Influence& I = c->inf;
+  const size_t need = (size_t)n * (2 * I.trunc_rows + 1) * c->g.nsx;
+  size_t freeb = 0, totalb = 0;
+  if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (need > I.strip_cap && 8 * need < freeb / 8) {
+    if (I.strips) cudaFree(I.strips);
+    I.strips = nullptr;
+    I.strip_cap = 0;
+    if (cudaMalloc(&I.strips, 8 * need) == cudaSuccess) I.strip_cap = need;
+    else cudaGetLastError();
+  }
+  return need <= I.strip_cap;
+}
+
+// ainv's response to a unit row r (every x mode 1 on row r), rows r - trunc_rows .. r + trunc_rows,
+// for r = r_lo .. r_hi, into the strips; then every scratch set's ainv modes are cleared, with no
+// strip recorded (the strip kernels clear only the rows they wrote last).
+int inf_strip_table(Ctx* c, int r_lo, int r_hi) {
+  Influence& I = c->inf;
+  const GridDims& g = c->g;
+  const int R = I.trunc_rows, wrows = 2 * R + 1;
+  cudaStream_t st = c->st;
+  I.strip_r0 = r_lo;
+  I.strip_n = r_hi - r_lo + 1;
+  double* F = I.bscr[0].spec1;
+  for (int r = r_lo; r <= r_hi; ++r) {
+    IB_CUDA_CHECK(cudaMemsetAsync(F, 0, 8 * (size_t)g.ns, st));
+    count_launch();
+    k_inf_unit_row<<<cdiv(g.nsx, 256), 256, 0, st>>>(g, r, F);
+    RC(tri_solve(c->tri_ainv, F, F, g.nsx, c->tl, st));
+    const int lo = std::max(0, r - R), hi = std::min(g.nsy, r + R + 1);
+    IB_CUDA_CHECK(cudaMemcpyAsync(I.strips + ((size_t)(r - r_lo) * wrows + (lo - (r - R))) * g.nsx,
+                                  F + (size_t)lo * g.nsx, 8 * (size_t)(hi - lo) * g.nsx, cudaMemcpyDeviceToDevice,
+                                  st));
+  }
+  for (const SchurScratch& sc : I.bscr) {
+    IB_CUDA_CHECK(cudaMemsetAsync(sc.specY, 0, 8 * (size_t)g.ns, st));
+    IB_CUDA_CHECK(cudaMemsetAsync(sc.rr_lv, 0, 2 * sizeof(int), st));
+  }
+  return IB_OK;
+}
+
 int inf_alloc(Ctx* c) {
   Influence& I = c->inf;
   const int nf = std::max(c->nf, 1);
@@ -580,40 +628,8 @@ int inf_build(Ctx* c) {
   // ainv's response to a unit row, for every band row (the strips the columns scale by their row
   // of W instead of transforming a unit vector and solving ainv each)
   const int R = I.trunc_rows, wrows = 2 * R + 1;
-  bool use_strips = false;
-  {
-    const size_t need = (size_t)(bmax - bmin + 1) * wrows * g.nsx;
-    size_t freeb = 0, totalb = 0;
-    IB_CUDA_CHECK(cudaMemGetInfo(&freeb, &totalb));
-    if (need > I.strip_cap && 8 * need < freeb / 8) {
-      if (I.strips) cudaFree(I.strips);
-      I.strips = nullptr;
-      I.strip_cap = 0;
-      if (cudaMalloc(&I.strips, 8 * need) == cudaSuccess) I.strip_cap = need;
-      else cudaGetLastError();
-    }
-    use_strips = need <= I.strip_cap;
-  }
-  if (use_strips) {
-    I.strip_r0 = bmin;
-    I.strip_n = bmax - bmin + 1;
-    double* F = I.bscr[0].spec1;
-    for (int r = bmin; r <= bmax; ++r) {
-      IB_CUDA_CHECK(cudaMemsetAsync(F, 0, 8 * (size_t)g.ns, st));
-      count_launch();
-      k_inf_unit_row<<<cdiv(g.nsx, 256), 256, 0, st>>>(g, r, F);
-      RC(tri_solve(c->tri_ainv, F, F, g.nsx, c->tl, st));
-      const int lo = std::max(0, r - R), hi = std::min(g.nsy, r + R + 1);
-      IB_CUDA_CHECK(cudaMemcpyAsync(I.strips + ((size_t)(r - bmin) * wrows + (lo - (r - R))) * g.nsx,
-                                    F + (size_t)lo * g.nsx, 8 * (size_t)(hi - lo) * g.nsx,
-                                    cudaMemcpyDeviceToDevice, st));
-    }
-    // every set's ainv modes start from zero, with no strip recorded
-    for (const SchurScratch& sc : I.bscr) {
-      IB_CUDA_CHECK(cudaMemsetAsync(sc.specY, 0, 8 * (size_t)g.ns, st));
-      IB_CUDA_CHECK(cudaMemsetAsync(sc.rr_lv, 0, 2 * sizeof(int), st));
-    }
-  }
+  const bool use_strips = inf_strip_alloc(c, bmax - bmin + 1);
+  if (use_strips) RC(inf_strip_table(c, bmin, bmax));
   for (SchurScratch& sc : I.bscr) sc.specY_ready = use_strips;
   const int S = std::min(Influence::kBuildStreams, I.nR);
   cudaEvent_t ev = nullptr;

@@ -64,7 +64,7 @@ __global__ void k_sd_col_next(int* col, int stride, int ncol, cudaGraphCondition
 // level the rows coarsify fills from those.
 __global__ void k_sd_source(const int* col, const int* __restrict__ comp, const int* __restrict__ ix,
                             const int* __restrict__ iy, const double* __restrict__ w, GridDims g, double* vort,
-                            int* prev, int* rr_in, int* rr_lv, int* box, int L, int R) {
+                            int* prev, int* rr_in, int* rr_lv, int* box, int* strip, int L, int R) {
   IB_GRID_DEP_WAIT();
   const int q = threadIdx.x;
   const int u = *col;
@@ -88,6 +88,10 @@ __global__ void k_sd_source(const int* col, const int* __restrict__ comp, const 
   }
   prev[q] = o;
   if (q != 0) return;
+  strip[0] = cx - 5;   // the patch's first vertex and the rows of the previous column's strip
+  strip[1] = cy - 5;
+  strip[2] = rr_lv[0];
+  strip[3] = rr_lv[1];
   const int b0 = max(0, cy - 5), b1 = min(g.nsy, cy + 3);
   rr_in[0] = b0;
   rr_in[1] = b1;
@@ -106,6 +110,52 @@ __global__ void k_sd_source(const int* col, const int* __restrict__ comp, const 
     else { lo = g.n / 4 + (r0 - 1) / 2; hi = g.n / 4 + (r1 - 1) / 2 + 1; }
     rr_lv[3 * lv] = lo; rr_lv[3 * lv + 1] = hi;
     rr_lv[3 * lv + 2] = lv == L - 1 ? ROW_ZERO : ROW_EDGES;
+  }
+}
+
+// The forward x transform of the column's patch rows, D[dj][k] = sum_di vort[b][a] W[a][k]
+// (a = strip[0] + di, b = strip[1] + dj, in order of di; zero for rows outside the grid).
+__global__ void k_sd_patch_modes(const int* __restrict__ strip, GridDims g, const double* __restrict__ vort,
+                                 const double* __restrict__ W, double* __restrict__ D) {
+  IB_GRID_DEP_WAIT();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.nsx) return;
+  const int dj = blockIdx.y, b = strip[1] + dj;
+  double v = 0.0;
+  if (b >= 0 && b < g.nsy)
+    for (int di = 0; di < 8; ++di) {
+      const int a = strip[0] + di;
+      if (a >= 0 && a < g.nsx) v = fma(vort[(size_t)b * g.nsx + a], W[(size_t)a * g.nsx + k], v);
+    }
+  D[(size_t)dj * g.nsx + k] = v;
+}
+
+// ainv's modes of the patch: per patch row b (in order), D[b] times the tabulated response A_b to
+// a unit row, on the strip's rows within trunc_rows of b; the previous strip's rows outside this
+// one cleared.  Grid: x over the modes, y over 2 (2R + 8) row slots (new strip, then old one).
+__global__ void k_sd_strip(const int* __restrict__ strip, const int* __restrict__ rr_lv, GridDims g,
+                           const double* __restrict__ D, const double* __restrict__ A, int r0, int R,
+                           double* __restrict__ specY) {
+  IB_GRID_DEP_WAIT();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.nsx) return;
+  const int lo = rr_lv[0], hi = rr_lv[1];
+  const int sl = blockIdx.y, ws = 2 * R + 8, w = 2 * R + 1;
+  if (sl < ws) {
+    const int y = lo + sl;
+    if (y >= hi) return;
+    double v = 0.0;
+    for (int dj = 0; dj < 8; ++dj) {
+      const int b = strip[1] + dj;
+      if (b < 0 || b >= g.nsy || y < b - R || y > b + R) continue;
+      const double* Ab = A + ((size_t)(b - r0) * w + (y - (b - R))) * g.nsx;
+      v = fma(D[(size_t)dj * g.nsx + k], Ab[k], v);
+    }
+    specY[(size_t)y * g.nsx + k] = v;
+  } else {
+    const int y = strip[2] + (sl - ws);
+    if (y < 0 || y >= strip[3] || (y >= lo && y < hi)) return;
+    specY[(size_t)y * g.nsx + k] = 0.0;
   }
 }
 
@@ -583,6 +633,27 @@ int sd_precompute(Ctx* c) {
     sc.cr_R1 = use_cr ? I.cr.R[1] : nullptr;
     sc.cr_idx1 = use_cr ? I.cr.idx[1] : nullptr;
   }
+  // ainv's modes of each column from the strips of its patch rows (influence.cu)
+  bool use_strips = false;
+  double* Dmodes = nullptr;
+  int strip_lo = 0, strip_hi = -1;
+  {
+    std::vector<int> iyh(S.nf_sd);
+    IB_CUDA_CHECK(cudaStreamSynchronize(c->st));
+    IB_CUDA_CHECK(cudaMemcpy(iyh.data(), S.reg.iy, 4 * (size_t)S.nf_sd, cudaMemcpyDeviceToHost));
+    strip_lo = g.nsy;
+    for (int u = 0; u < S.nf_sd; ++u) {
+      strip_lo = std::min(strip_lo, std::max(0, iyh[u] - 5));
+      strip_hi = std::max(strip_hi, std::min(g.nsy - 1, iyh[u] + 2));
+    }
+    if (strip_hi >= strip_lo && inf_strip_alloc(c, strip_hi - strip_lo + 1) &&
+        cudaMalloc(&Dmodes, 8 * 8 * (size_t)g.nsx * Influence::kBuildStreams) == cudaSuccess) {
+      RC(inf_strip_table(c, strip_lo, strip_hi));
+      use_strips = true;
+    }
+    cudaGetLastError();
+  }
+  for (SchurScratch& sc : I.bscr) sc.specY_ready = use_strips;
   // the candidate values of every column, before the drop (freed once compacted)
   if (S.rows) cudaFree(S.rows);
   if (S.vals) cudaFree(S.vals);
@@ -634,7 +705,15 @@ int sd_precompute(Ctx* c) {
         const long long b0 = launch_count();
         count_launch();
         k_sd_source<<<1, kPatch, 0, sc.st>>>(col, S.ucomp, S.reg.ix, S.reg.iy, S.reg.w, g, sc.vort, pprev, sc.rr_in,
-                                             sc.rr_lv, sc.box, c->L, I.trunc_rows);
+                                             sc.rr_lv, sc.box, sc.strip, c->L, I.trunc_rows);
+        if (use_strips) {
+          double* D = Dmodes + 8 * (size_t)g.nsx * i;
+          const int R = I.trunc_rows;
+          count_launches(2);
+          k_sd_patch_modes<<<dim3(cdiv(g.nsx, 128), 8), 128, 0, sc.st>>>(sc.strip, g, sc.vort, c->wmat, D);
+          k_sd_strip<<<dim3(cdiv(g.nsx, 128), 2 * (2 * R + 8)), 128, 0, sc.st>>>(sc.strip, sc.rr_lv, g, D, I.strips,
+                                                                                 I.strip_r0, R, sc.specY);
+        }
         const double* ring0 = nullptr;
         rc = schur_fluid(c, sc.vort, sc.rr_in, S.reg.bbox + 7, sc.s0, &ring0, &sc);
         count_launches(3);
@@ -673,7 +752,11 @@ int sd_precompute(Ctx* c) {
     if (e) cudaGraphExecDestroy(e);
   if (cap) cudaStreamDestroy(cap);
   cudaEventDestroy(ev);
-  for (SchurScratch& sc : I.bscr) sc.cr_R1 = nullptr;
+  for (SchurScratch& sc : I.bscr) {
+    sc.cr_R1 = nullptr;
+    sc.specY_ready = false;
+  }
+  if (Dmodes) cudaFree(Dmodes);
   if (rc == IB_OK && use_cr) {
     int err = 0;
     if (cudaMemcpy(&err, I.cr.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) rc = IB_ERR_CUDA;

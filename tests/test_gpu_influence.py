@@ -180,3 +180,19 @@ def test_coarse_responses_match_the_per_column_chain():
     assert ca["solves"] < ca2["solves"] < 2 * ca["solves"] and ca2["held"] == ca2["solves"]
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("levels", [2, 4])
+def test_coarse_responses_at_other_level_counts(levels):
+    # two levels (the coarsest level's responses alone) and four (two levels of sums between)
+    body = small_plate()
+    kw = dict(PLATE, mgridlev=levels)
+    a = G.Simulation(G.Params(**kw), [body])
+    b = _without_coarse_responses(lambda: G.Simulation(G.Params(**kw), [body]))
+    Sa, Sb = a.schur_matrix(), b.schur_matrix()
+    assert Sa is not None and Sb is not None
+    assert rel(Sa, _matrix_free(a)) < TOL_MAT
+    assert rel(Sa, Sb) < 1e-13
+    assert a.coarse_stats()["solves"] > 0
+    a.close()
+    b.close()
