@@ -272,27 +272,34 @@ def _timed_steps(sim, stream, steps):
     return e0.elapsed_time(e1) / 1e3, ksp_sum, fsi_sum
 
 
-def _e2e_steps(sim, stream, steps):
-    """K steps through the C ABI with host buffers: each step uploads the frame fluxes q0 of
-    all levels from pinned memory and reads the force coefficients (and hinge angles) back."""
+def _e2e_steps(sim, stream, steps, fields=False):
+    """K steps through the C ABI with host buffers: each step gives the frame's motion of that
+    step, (u, v, angular velocity) from pinned memory through ib_set_frame (the reference's
+    per-step input: motion_grid, from which motion_potential and motion_rotation form the frame
+    fluxes), or with fields=True uploads the frame fluxes q0 of all levels themselves from pinned
+    memory, and reads the force coefficients (and hinge angles) back."""
     import torch
     from ib_parallel_gb300 import ibgpu as G
     L = sim.params.mgridlev
-    q0x = [torch.from_numpy(sim.get_field("q0x", k)).pin_memory() for k in range(L)]
-    q0y = [torch.from_numpy(sim.get_field("q0y", k)).pin_memory() for k in range(L)]
+    q0x = [torch.from_numpy(sim.get_field("q0x", k)).pin_memory() for k in range(L)] if fields else []
+    q0y = [torch.from_numpy(sim.get_field("q0y", k)).pin_memory() for k in range(L)] if fields else []
+    frame = torch.tensor(list(sim.params.motion[:3]), dtype=torch.float64).pin_memory()
     cx = torch.zeros(max(1, sim.nbody), dtype=torch.float64).pin_memory()
     cy = torch.zeros_like(cx)
     th = torch.zeros(max(1, sim.ntors), dtype=torch.float64).pin_memory()
-    h2d = sum(t.numel() * 8 for t in q0x + q0y)
+    h2d = sum(t.numel() * 8 for t in q0x + q0y) if fields else frame.numel() * 8
     d2h = (2 * sim.nbody + sim.ntors) * 8
     torch.cuda.synchronize()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(steps):
-        for k in range(L):
-            sim.set_field("q0x", k, q0x[k])
-            sim.set_field("q0y", k, q0y[k])
+        if fields:
+            for k in range(L):
+                sim.set_field("q0x", k, q0x[k])
+                sim.set_field("q0y", k, q0y[k])
+        else:
+            G._check(sim.lib.ib_set_frame(sim.h, G.C.c_void_p(frame.data_ptr())), "ib_set_frame")
         sim.advance()
         G._check(sim.lib.ib_get_forces(sim.h, G.C.c_void_p(cx.data_ptr()), G.C.c_void_p(cy.data_ptr())))
         if sim.ntors:
@@ -527,6 +534,9 @@ def run_gpu(args, world, rank, local):
     e2e_local, h2d, d2h = _e2e_steps(sim, stream, args.steps)
     e2e_s = _barrier_max(e2e_local, world)
     e2e_value = world * args.steps / e2e_s
+    _barrier(world)
+    e2f_local, h2d_f, d2h_f = _e2e_steps(sim, stream, args.steps, fields=True)
+    e2f_s = _barrier_max(e2f_local, world)
 
     # ---- roofline of the dominant kernel (the DST-I x pass, the largest share of the step's
     # launch list), timed alone: 20 back-to-back full passes over the finest grid with CUDA
@@ -566,7 +576,11 @@ def run_gpu(args, world, rank, local):
                    "l2": "working set (~330 MB of state, tables and scratch + 160 MB influence band) larger "
                          "than L2 (129 MB)"},
         "clocks": clk.summary(),
-        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "input": "the step's frame motion (u, v, angular velocity) through ib_set_frame"},
+        "e2e_q0_fields": {"value": world * args.steps / e2f_s, "unit": "steps/s", "h2d_bytes_per_step": h2d_f,
+                          "d2h_bytes_per_step": d2h_f,
+                          "input": "the frame fluxes q0 of all levels uploaded by ib_set_field each step"},
         "gpu_launches": launches_timed,
         "work_per_step": {"schur_matvecs": mv_per_step, "ksp_iter": ksp_per_step,
                           "fsi_iter": fsi_sum / args.steps,

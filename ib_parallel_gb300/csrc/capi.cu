@@ -1,4 +1,5 @@
 // extern "C" entry points of include/ib_gpu.h.
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -135,6 +136,30 @@ int ib_advance(IbCtx* h, int* itime) {
     return fail(rc, m.c_str());
   }
   return op_result(rc, "advance failed");
+}
+
+int ib_set_frame(IbCtx* h, const double* uvw) {
+  CTX_OR_FAIL(h);
+  if (!uvw) return fail(IB_ERR_ARG, "bad argument");
+  if (c->end_pending) return fail(IB_ERR_STATE, "a step is in progress");
+  for (int i = 0; i < 3; ++i)
+    if (!std::isfinite(uvw[i])) return fail(IB_ERR_ARG, "frame velocity not finite");
+  ib::FrameLevels fl;
+  for (int k = 0; k < c->L; ++k) {
+    fl.q0x[k] = c->q0x[k];
+    fl.q0y[k] = c->q0y[k];
+  }
+  const auto& p = c->p;
+  if (!c->frame_lines && cudaMalloc(&c->frame_lines, 8 * (size_t)c->L * (c->g.n + c->g.m)) != cudaSuccess) {
+    c->frame_lines = nullptr;
+    cudaGetLastError();
+    return fail(IB_ERR_NOMEM, "device allocation failed");
+  }
+  const int rc = ib::launch_frame_flux(c->g, fl, c->L, c->delta, p.offsetx, p.offsety, uvw[0], uvw[1], uvw[2],
+                                       p.motion[3], p.motion[4], c->frame_lines, c->st);
+  if (rc != IB_OK) return op_result(rc, "frame fluxes failed");
+  for (int i = 0; i < 3; ++i) c->p.motion[i] = uvw[i];   // what the restart file records
+  return IB_OK;
 }
 
 static int field_ptr(Ctx* c, int field, int level, double** p, size_t* n) {

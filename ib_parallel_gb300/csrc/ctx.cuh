@@ -269,6 +269,7 @@ struct Ctx {
   double *nlx = nullptr, *nly = nullptr, *hx = nullptr, *hy = nullptr, *vort = nullptr;
   std::vector<double*> lastbc;
   double *omegabc = nullptr, *sbc = nullptr, *zero_ring = nullptr;
+  double* frame_lines = nullptr;   // ib_set_frame's per-row values (allocated on its first call)
 
   // bodies
   int nbody = 0, nb = 0, nf = 0, nt = 0;

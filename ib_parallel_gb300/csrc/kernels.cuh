@@ -19,6 +19,15 @@ struct RingBatch {
 };
 int launch_get_bc_levels(const GridDims& g, const RingBatch& rb, int nlev, double fac, cudaStream_t st);
 // curl of every level in one launch: level l from s[l] with ghosts from the ring sbc[l]
+// the frame fluxes of every level (k_frame_flux)
+struct FrameLevels {
+  double* q0x[kMaxLevels] = {};
+  double* q0y[kMaxLevels] = {};
+};
+// lines: nlev (n + m) doubles of scratch
+int launch_frame_flux(const GridDims& g, const FrameLevels& fl, int nlev, double delta, double offx, double offy,
+                      double u, double v, double w, double cx, double cy, double* lines, cudaStream_t st);
+
 struct CurlBatch {
   const double* s[kMaxLevels] = {};
   const double* sbc[kMaxLevels] = {};

@@ -448,6 +448,7 @@ void ctx_destroy(Ctx* c) {
   pressure_free(c);
   beam_free(c);
   sd_free(c);
+  if (c->frame_lines) cudaFree(c->frame_lines);
   adjoint_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);

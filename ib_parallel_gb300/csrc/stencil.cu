@@ -197,6 +197,53 @@ __global__ void k_coarsify(GridDims g, const double* __restrict__ fine, double* 
   coarse[(Jc - 2) * g.nsx + (Ic - 2)] = v;
 }
 
+// --------------------------------------------------------------- frame fluxes
+// q0 = q0p + q0r of every level for a frame moving at (u, v) and turning at w about (cx, cy)
+// (motion_potential + motion_rotation, variables.F90:299-360): on level k (1-based, spacing
+// delta 2^(k-1)) the u-face (i, j) takes -fac u + fac (0 + w (y_j - cy)) and the v-face
+// -fac v + fac (0 - w (x_i - cx)), fac = delta 2^(k-1), x_i and y_j the face centres less the
+// offsets.  A u-face's value depends on its row only and a v-face's on its column only, so
+// k_frame_lines forms the n + m values of each level and k_frame_fill writes the fields.  Every
+// operation is rounded on its own in the order written, as the context's creation forms the
+// same fluxes on the host (built without contraction), so a frame equal to the configured
+// motion gives the same fluxes bit for bit.
+__global__ void k_frame_lines(GridDims g, int nlev, double delta, double offx, double offy, double u, double v,
+                              double w, double cx, double cy, double* __restrict__ lines) {
+  IB_GRID_DEP_WAIT();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int per = g.n + g.m;
+  if (t >= nlev * per) return;
+  const int k = t / per, r = t - k * per;
+  const double pw = ldexp(1.0, k);   // 2^(level - 1), exact
+  const double fac = __dmul_rn(delta, pw);
+  if (r < g.n) {   // u-face row j = r + 1
+    double yy = __dsub_rn(__dsub_rn((double)(r + 1), 0.5), (double)(g.n / 2));
+    yy = __dmul_rn(__dmul_rn(yy, delta), pw);
+    yy = __dsub_rn(__dadd_rn(yy, __dmul_rn((double)(g.n / 2), delta)), offy);
+    const double e = __dadd_rn(0.0, __dmul_rn(w, __dsub_rn(yy, cy)));
+    lines[t] = __dadd_rn(__dmul_rn(-fac, u), __dmul_rn(fac, e));
+  } else {         // v-face column i = r - n + 1
+    double xx = __dsub_rn(__dsub_rn((double)(r - g.n + 1), 0.5), (double)(g.m / 2));
+    xx = __dmul_rn(__dmul_rn(xx, delta), pw);
+    xx = __dsub_rn(__dadd_rn(xx, __dmul_rn((double)(g.m / 2), delta)), offx);
+    const double e = __dsub_rn(0.0, __dmul_rn(w, __dsub_rn(xx, cx)));
+    lines[t] = __dadd_rn(__dmul_rn(-fac, v), __dmul_rn(fac, e));
+  }
+}
+
+// blockIdx.y = level, blockIdx.z = u-faces (0) or v-faces (1)
+__global__ void k_frame_fill(GridDims g, FrameLevels fl, const double* __restrict__ lines) {
+  IB_GRID_DEP_WAIT();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  const double* ln = lines + (size_t)k * (g.n + g.m);
+  if (blockIdx.z == 0) {
+    if (t < g.nu) fl.q0x[k][t] = ln[t / g.nux];
+  } else {
+    if (t < g.nv) fl.q0y[k][t] = ln[g.n + t % g.nvx];
+  }
+}
+
 // --------------------------------------------------------------- get_bc
 // operators_fluid.F90:475-535 with grid.F90:1091-1140: coarse values on the
 // fine boundary; coincident points copied, midpoints averaged; times fac.
@@ -317,6 +364,14 @@ int launch_coarsify(const GridDims& g, const double* fine, double* coarse, cudaS
   int n = (g.m / 2 - 1) * (g.n / 2 - 1);
   count_launch();
   k_coarsify<<<blocks(n), 256, 0, st>>>(g, fine, coarse);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_frame_flux(const GridDims& g, const FrameLevels& fl, int nlev, double delta, double offx, double offy,
+                      double u, double v, double w, double cx, double cy, double* lines, cudaStream_t st) {
+  if (nlev < 1 || nlev > kMaxLevels) return IB_ERR_ARG;
+  count_launches(2);
+  k_frame_lines<<<blocks(nlev * (g.n + g.m)), 256, 0, st>>>(g, nlev, delta, offx, offy, u, v, w, cx, cy, lines);
+  k_frame_fill<<<dim3(blocks(g.nu > g.nv ? g.nu : g.nv), nlev, 2), 256, 0, st>>>(g, fl, lines);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_get_bc(const GridDims& g, const double* s, double fac, double* ring, cudaStream_t st) {

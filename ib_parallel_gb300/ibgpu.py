@@ -43,7 +43,7 @@ EXPORTS = [
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
     "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state", "ib_get_step_graph_stats",
-    "ib_get_coarse_stats",
+    "ib_get_coarse_stats", "ib_set_frame",
     "ib_subdomain_setup", "ib_subdomain_precompute", "ib_write_subdomain_matrix", "ib_read_subdomain_matrix",
     "ib_subdomain_operator", "ib_get_subdomain_stats", "ib_adjoint_forward", "ib_adjoint_backward",
 ]
@@ -138,6 +138,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_get_beam_state": ([P, P, P, P], C.c_int),
         "ib_get_step_graph_stats": ([P, C.POINTER(C.c_longlong)], C.c_int),
         "ib_get_coarse_stats": ([P, C.POINTER(C.c_longlong), C.POINTER(C.c_double)], C.c_int),
+        "ib_set_frame": ([P, P], C.c_int),
         "ib_subdomain_setup": ([P, C.c_int] + [C.c_double] * 5, C.c_int),
         "ib_subdomain_precompute": ([P], C.c_int),
         "ib_write_subdomain_matrix": ([P, C.c_char_p], C.c_int),
@@ -336,6 +337,12 @@ class Simulation:
         out = np.empty(self.shapes[name])
         _check(self.lib.ib_get_field(self.h, FIELDS[name], level, _ptr(out)), "ib_get_field")
         return out
+
+    def set_frame(self, u: float, v: float, w: float) -> None:
+        """The frame's velocity (u, v) and angular velocity w for the steps that follow (the
+        frame fluxes q0 of every level formed on the device)."""
+        a = np.array([u, v, w], dtype=np.float64)
+        _check(self.lib.ib_set_frame(self.h, _ptr(a)), "ib_set_frame")
 
     def set_field(self, name: str, level: int, arr):
         a = np.ascontiguousarray(arr, dtype=np.float64) if not hasattr(arr, "data_ptr") else arr

@@ -108,6 +108,14 @@ int ib_synchronize(IbCtx* ctx);
  * ib_last_error() gives the reason or the final FSI error. */
 int ib_advance(IbCtx* ctx, int* itime);
 
+/* The frame's motion for the steps that follow: uvw = (u, v, angular velocity) of the grid
+ * (host memory), the centre of rotation staying motion[3], motion[4] of ib_create.  Replaces the
+ * reference's motion_potential + motion_rotation (variables.F90:299-360), which form the frame
+ * fluxes q0 from motion_grid (user.F90:13-31); here they are formed on the device, stream-ordered
+ * after the steps already launched (IB_ERR_STATE while a step of ib_advance_begin is open).  With
+ * the motion given at ib_create the fluxes are those of creation bit for bit. */
+int ib_set_frame(IbCtx* ctx, const double* uvw);
+
 /* state access (the arrays of variables.F90:10-33) */
 int ib_get_field(IbCtx* ctx, int field, int level, double* out);
 int ib_set_field(IbCtx* ctx, int field, int level, const double* in);
