@@ -1,6 +1,6 @@
 // The discrete adjoint of the time step (no reference counterpart; the reference's step is
-// timestepper.F90:18-556) for stationary rigid bodies solved directly (num_stat) in a moving
-// frame: the frame's flux is linear in its velocity (u, v) and angular velocity W about the
+// timestepper.F90:18-556) for stationary rigid bodies in a moving frame, their Schur system
+// solved directly (num_stat) or by the cluster GMRES on the assembled operator: the frame's flux is linear in its velocity (u, v) and angular velocity W about the
 // centre motion[3..4] (motion_potential + motion_rotation, variables.F90:299-360), so a
 // pitching or plunging body held fixed in its own frame takes one coefficient triple per step,
 // q0 = u Bu + v Bv + W BW on every level.
@@ -18,7 +18,10 @@
 //     and k_adj_nl_faces gather each argument's adjoint;
 //   * get_bc^T, apply_bc^T and coarsify^T are gathers (each output element sums its own
 //     contributions, so no floating-point atomics);
-//   * reg and regT are each other's transposes; the Cholesky solve is symmetric.
+//   * reg and regT are each other's transposes; the Cholesky solve is symmetric, and without
+//     num_stat the reverse solves the transposed system, S^T x = b, with the same GMRES on the
+//     assembled operator's row-major copy (which, read column-major, is S^T): the adjoint of the
+//     exact solve, which the forward's converged Krylov solve approaches (timestepper.F90:363-366).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -397,7 +400,19 @@ int step_T(Adj& a, int slot, int it, const double* frame, const double* dforce_h
   count_launch();
   k_adj_force<<<blocks(c->nf), kT, 0, st>>>(c->nf, c->nbody, c->comp, c->bid, 2.0 * c->delta / c->p.dt, A.dforce,
                                             A.lf, A.lf);
-  RC(launch_chol_solve(c->nf, c->cholM, A.lf, A.lrhsf, st));
+  if (c->p.num_stat) {
+    RC(launch_chol_solve(c->nf, c->cholM, A.lf, A.lrhsf, st));
+  } else {
+    // S^T lrhsf = lf: the band's row-major S (rigid bodies: no structure block) as the
+    // column-major operator of the cluster solver, from a zero start
+    const IbParams& p = c->p;
+    IB_CUDA_CHECK(cudaMemsetAsync(A.lrhsf, 0, 8 * (size_t)c->nf, st));
+    RC(launch_gmres_fused(c->G, &c->fused_plan, c->inf.S, A.lf, A.lrhsf, p.rtol, p.atol, p.gmres_max_it, st));
+    int ist[2] = {0, 0};
+    IB_CUDA_CHECK(cudaMemcpyAsync(ist, c->G.ist, sizeof(ist), cudaMemcpyDeviceToHost, st));
+    IB_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (ist[1] < 0) return IB_ERR_GMRES;   // the transposed solve stopped without converging
+  }
   // rhsf = regT(q*_0 + q0_0): the flux adjoint on level 0, then the first vort2flux transposed
   RC(launch_reg(g, c->nf, A.lrhsf, c->reg, A.ax, A.ay, st));
   for (int k = 0; k < L; ++k) IB_CUDA_CHECK(cudaMemcpyAsync(A.lostar[k], A.lw[k], 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, st));
@@ -462,7 +477,12 @@ int step_T(Adj& a, int slot, int it, const double* frame, const double* dforce_h
 }
 
 // the state a step starts from: omega, s, qx, qy, rhs_old of every level
-size_t state_doubles(const GridDims& g, int L) { return (size_t)L * (3 * (size_t)g.ns + g.nu + g.nv); }
+// The state a checkpoint holds: omega, s, qx, qy, rhs_old of every level, and the forces, the
+// next step's Krylov starting guess (so that a recomputed segment repeats the forward exactly).
+size_t state_doubles(const Ctx* c) {
+  const GridDims& g = c->g;
+  return (size_t)c->L * (3 * (size_t)g.ns + g.nu + g.nv) + (size_t)c->nf;
+}
 
 int save_state(Ctx* c, double* dst) {
   const GridDims& g = c->g;
@@ -474,6 +494,7 @@ int save_state(Ctx* c, double* dst) {
       p += n;
     }
   }
+  IB_CUDA_CHECK(cudaMemcpyAsync(p, c->f, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
   return IB_OK;
 }
 
@@ -487,6 +508,7 @@ int load_state(Ctx* c, const double* src) {
       p += n;
     }
   }
+  IB_CUDA_CHECK(cudaMemcpyAsync(c->f, p, 8 * (size_t)c->nf, cudaMemcpyDeviceToDevice, c->st));
   return IB_OK;
 }
 
@@ -577,8 +599,12 @@ static int adjoint_alloc(Ctx* c) {
 
 int op_adjoint_forward(Ctx* c, int nsteps, int K, const double* frames, double* forces, std::string* msg) {
   AdjointState& A = c->adj;
-  if (!c->p.num_stat || c->nt > 0 || c->nbeam > 0 || c->sd.on || c->nf == 0) {
-    *msg = "the adjoint covers stationary rigid bodies with the direct solve (num_stat)";
+  if (c->nt > 0 || c->nbeam > 0 || c->sd.on || c->nf == 0) {
+    *msg = "the adjoint covers stationary rigid bodies";
+    return IB_ERR_ARG;
+  }
+  if (!c->p.num_stat && (c->p.schur_mode != 0 || !c->use_fused)) {
+    *msg = "without num_stat the adjoint needs the assembled operator and the cluster solver (schur_mode 0)";
     return IB_ERR_ARG;
   }
   if (nsteps <= 0 || K <= 0 || nsteps > 4096) {
@@ -587,7 +613,7 @@ int op_adjoint_forward(Ctx* c, int nsteps, int K, const double* frames, double* 
   }
   RC(adjoint_alloc(c));
   const int nseg = (nsteps + K - 1) / K;
-  const size_t sd = state_doubles(c->g, c->L);
+  const size_t sd = state_doubles(c);
   if (A.ckpt) cudaFree(A.ckpt);
   if (A.tape) cudaFree(A.tape);
   A.ckpt = nullptr;
@@ -640,7 +666,7 @@ int op_adjoint_backward(Ctx* c, const double* dforces, double* dframes, std::str
   }
   const GridDims& g = c->g;
   const int L = c->L;
-  const size_t sd = state_doubles(g, L);
+  const size_t sd = state_doubles(c);
   const size_t per = (size_t)g.ns + g.nu + g.nv;
   Adj a{c, A, g, L, c->st};
   // the adjoint state after the last step: zero

@@ -1,7 +1,7 @@
 """CPU oracle of the discrete adjoint of the time step -- TEST INFRASTRUCTURE ONLY.
 
 The reference has no adjoint; this restates, for the oracle's own step (ib_oracle.IBOracle
-.advance, i.e. timestepper.F90:18-556 with num_stat = T and stationary rigid bodies), the exact
+.advance, i.e. timestepper.F90:18-556 with stationary rigid bodies), the exact
 transpose of every linear map the step applies, so that the gradient of any function of the
 per-step force coefficients with respect to the step's inputs follows by reverse accumulation.
 The kinematics enter through the moving frame's flux (motion_potential + motion_rotation,
@@ -18,7 +18,11 @@ Transposes used (each is the exact adjoint of the oracle's forward arithmetic):
   * get_bc^T scatters the ring back onto the coarse grid, apply_bc^T gathers the boundary rows,
     coarsify^T spreads the full-weighting stencil (operators_fluid.F90:381-549);
   * reg and regT are each other's transposes (fsinterface.F90:14-80); the Cholesky solve of the
-    symmetrised Schur matrix is symmetric (timestepper.F90:560-598).
+    symmetrised Schur matrix is symmetric (timestepper.F90:560-598).  Without num_stat the
+    reference solves the Schur system by GMRES (timestepper.F90:363-366); here the forward solves
+    it exactly with the dense Schur matrix (a_times on unit vectors; the bodies do not move, so it
+    is formed once) and the reverse solves with its transpose: the adjoint of the exact solve,
+    which a converged Krylov solve approaches.
 The step's state between steps is (omega, q, rhs_old) on every level.
 """
 from __future__ import annotations
@@ -28,9 +32,10 @@ import numpy as np
 
 class Adjoint:
     def __init__(self, o):
-        if not o.p.num_stat or any(b.fam != 1 for b in o.bodies):
-            raise ValueError("the adjoint covers stationary rigid bodies with the direct solve (num_stat)")
+        if any(b.fam != 1 for b in o.bodies):
+            raise ValueError("the adjoint covers stationary rigid bodies")
         self.o = o
+        self.S = None             # the dense Schur matrix without num_stat
         # frame bases: the flux of a unit u, v and W about the frame's centre (motion[3:5])
         saved = o.p.motion
         bases = []
@@ -39,6 +44,13 @@ class Adjoint:
             bases.append(o.frame_flux(0))
         o.p.motion = saved
         self.bases = bases        # [u, v, W] -> (q0x levels, q0y levels)
+
+    def schur(self):
+        """The Schur matrix a_times (operators_fluid.F90:14-120) column by column."""
+        if self.S is None:
+            eye = np.eye(self.o.nf)
+            self.S = np.stack([self.o.a_times(eye[l]) for l in range(self.o.nf)], axis=1)
+        return self.S
 
     def frame(self, c):
         qx = [c[0] * self.bases[0][0][k] + c[1] * self.bases[1][0][k] + c[2] * self.bases[2][0][k]
@@ -53,7 +65,7 @@ class Adjoint:
         coefficients (nbody, 2) and the tape of what the reverse step reads."""
         o = self.o
         L = o.L
-        if o.itime == 0 and o.cholM is None:
+        if o.p.num_stat and o.itime == 0 and o.cholM is None:
             o.preprocess()
         o.itime += 1
         it = o.itime
@@ -77,7 +89,7 @@ class Adjoint:
         s, qx, qy = o.vort2flux(ostar)          # coarsifies ostar in place
         tape["ostar_c"] = [w.copy() for w in ostar]
         rhsf = o.regT(qx[0] + q0x[0], qy[0] + q0y[0], 0.0 - o.delta * o.ub)
-        f = o.chol_solve(rhsf)
+        f = o.chol_solve(rhsf) if o.p.num_stat else np.linalg.solve(self.schur(), rhsf)
         hx, hy = o.reg(f)
         ostar[0] = ostar[0] - o.ainv(o.rot(hx, hy))
         o.omega = ostar
@@ -255,7 +267,7 @@ class Adjoint:
         scale = 2.0 * o.delta / o.p.dt
         for kf in range(o.nf):
             lf[kf] += scale * lforce[o.bid[kf], 0 if o.comp[kf] == 1 else 1]
-        lrhsf = o.chol_solve(lf)
+        lrhsf = o.chol_solve(lf) if o.p.num_stat else np.linalg.solve(self.schur().T, lf)
         # rhsf = regT(q*_0 + q0_0): the adjoint fluxes on level 0
         ax, ay = o.reg(lrhsf)
         lq0x = [np.zeros_like(b) for b in tape["q0x"]]

@@ -8,8 +8,8 @@ import ib_adjoint as A
 import ib_oracle as O
 
 
-def _oracle(L=3):
-    p = O.Params(m=32, n=16, mgridlev=L, dt=0.02, Re=100.0, len=4.0, offsetx=1.0, offsety=1.0, num_stat=True,
+def _oracle(L=3, num_stat=True):
+    p = O.Params(m=32, n=16, mgridlev=L, dt=0.02, Re=100.0, len=4.0, offsetx=1.0, offsety=1.0, num_stat=num_stat,
                  motion=(-1.0, 0.0, 0.0, 0.3, 0.0))
     return O.IBOracle(p, [O.cylinder(npts=10, diameter=0.8, xc=0.3, yc=0.0)])
 
@@ -64,14 +64,15 @@ def test_transposes_satisfy_the_dot_product_identity():
         assert np.isclose(lhs, rhs, rtol=1e-12), adj
 
 
-@pytest.mark.parametrize("L", [2, 3])
-def test_gradient_matches_central_differences(L):
+@pytest.mark.parametrize("L,num_stat", [(2, True), (3, True), (3, False)])
+def test_gradient_matches_central_differences(L, num_stat):
+    # num_stat = F: the Schur system solved with its dense matrix, the reverse with its transpose
     N = 6
     coefs = _coefs(N)
     W = np.random.default_rng(1).standard_normal((N, 1, 2))
 
     def J(c):
-        ad = A.Adjoint(_oracle(L))
+        ad = A.Adjoint(_oracle(L, num_stat))
         return float(np.sum(W * ad.forward(c))), ad
 
     J0, ad = J(coefs)

@@ -2,7 +2,8 @@
 bodies in a moving frame: its forward against plain steps, its gradient against the oracle's
 adjoint (oracle/ib_adjoint.py), against central differences of the GPU forward, for every
 checkpoint interval, the context left as the forward left it, and the torch.autograd binding
-carrying the gradient to pitching parameters."""
+carrying the gradient to pitching parameters; the same with the Schur system solved by GMRES
+(num_stat = F) and its transpose in the reverse."""
 import numpy as np
 import pytest
 
@@ -155,3 +156,63 @@ def test_gradient_at_the_pitching_airfoil_size_matches_the_oracle():
     go = ad.backward(W)
     assert np.abs(Fg - Fo).max() < 1e-11 * np.abs(Fo).max()
     assert np.abs(gg - go).max() < 1e-10 * np.abs(go).max(), np.abs(gg - go).max() / np.abs(go).max()
+
+
+# the Schur system by the cluster GMRES on the assembled operator (num_stat = F), both solves tight
+KWG = dict(KW, num_stat=False, rtol=1e-14, atol=1e-16)
+
+
+def _gpu_gmres():
+    return G.Simulation(G.Params(**KWG), [G.Body(**_cyl_kw())])
+
+
+def test_gmres_path_gradient_matches_the_oracle_adjoint():
+    # the oracle solves exactly with the dense Schur matrix and reverses with its transpose; the
+    # library solves S f = r and S^T x = b by GMRES to 1e-14
+    N = 6
+    coefs = _coefs(N)
+    W = np.random.default_rng(8).standard_normal((N, 1, 2))
+    p = O.Params(**{k: v for k, v in KWG.items() if k in O.Params.__dataclass_fields__})
+    ad = A.Adjoint(O.IBOracle(p, [O.cylinder(npts=20, diameter=0.8, xc=0.3, yc=0.0)]))
+    Fo = ad.forward(coefs)
+    go = ad.backward(W)
+    g = _gpu_gmres()
+    Fg = g.adjoint_forward(coefs, K=2)
+    gg = g.adjoint_backward(W)
+    assert np.abs(Fg - Fo).max() < 1e-10 * np.abs(Fo).max()
+    assert np.abs(gg - go).max() < 1e-8 * np.abs(go).max(), np.abs(gg - go).max() / np.abs(go).max()
+
+
+def test_gmres_path_gradient_matches_central_differences():
+    N = 6
+    coefs = _coefs(N)
+    W = np.random.default_rng(9).standard_normal((N, 1, 2))
+    g = _gpu_gmres()
+    g.adjoint_forward(coefs, K=3)
+    grad = g.adjoint_backward(W)
+
+    def J(c):
+        s = _gpu_gmres()
+        return float(np.sum(W * s.adjoint_forward(c, K=N)))
+
+    h = 1e-6
+    for (n, i) in [(0, 0), (2, 1), (5, 2), (4, 0)]:
+        cp = coefs.copy(); cp[n, i] += h
+        cm = coefs.copy(); cm[n, i] -= h
+        fd = (J(cp) - J(cm)) / (2 * h)
+        assert abs(grad[n, i] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(grad).max()), (n, i, grad[n, i], fd)
+
+
+@pytest.mark.parametrize("K", [1, 6])
+def test_gmres_path_checkpoint_interval_does_not_change_the_gradient(K):
+    # the checkpoints hold the forces too (the next solve's starting guess): a recomputed
+    # segment repeats the forward bit for bit
+    N = 6
+    coefs = _coefs(N)
+    W = np.random.default_rng(10).standard_normal((N, 1, 2))
+    ref = _gpu_gmres()
+    ref.adjoint_forward(coefs, K=2)
+    g0 = ref.adjoint_backward(W)
+    g = _gpu_gmres()
+    g.adjoint_forward(coefs, K=K)
+    assert np.array_equal(g.adjoint_backward(W), g0)
