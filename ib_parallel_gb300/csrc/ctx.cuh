@@ -187,7 +187,6 @@ struct SubDomain {
   int* rigid = nullptr;
   int* pidx = nullptr;
   double* pw = nullptr;
-  double* eq = nullptr;          // E_o (q + q0) on every sub-domain unknown
   double* fsd = nullptr;         // P^T f
   // precompute scratch per column set: the patch's 64 vertices, the candidate values
   int* pprev = nullptr;
@@ -452,7 +451,9 @@ int launch_cr_ring0(Ctx* c, const SchurScratch& sc, cudaStream_t st);
 void cr_free(Ctx* c);
 // the finest-level vertices within r of a marked one, in x and in y (the boxes of the sources)
 void cr_dilate(const GridDims& g, std::vector<unsigned char>& mask, int r);
-int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st); // rhsf = P E_o (q + q0) + rhsf
+// rhsf = P E_o (q + q0) + rhsf (P formed first at the current positions unless interp is false)
+int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st, bool interp = true);
+int launch_sd_interp(Ctx* c, cudaStream_t st);            // P at the current positions
 int launch_sd_spread(Ctx* c, const double* f, double* hx, double* hy, cudaStream_t st);   // E_o^T P^T f
 int sd_write(Ctx* c, const char* path, std::string* msg);
 int sd_read(Ctx* c, const char* path, std::string* msg);

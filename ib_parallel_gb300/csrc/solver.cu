@@ -1160,15 +1160,16 @@ static int capture_fsi_loop(Ctx* c, cudaStream_t st) {
   const IbParams& p = c->p;
   Influence& I = c->inf;
   cudaStream_t s1 = nullptr, s2 = nullptr, s3 = nullptr;
-  cudaEvent_t ev[5] = {};
+  cudaEvent_t ev[7] = {};
   int rc = IB_OK;
   if (cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking) != cudaSuccess)
     rc = IB_ERR_CUDA;
-  for (int i = 0; i < 5 && rc == IB_OK; ++i)
+  for (int i = 0; i < 7 && rc == IB_OK; ++i)
     if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess) rc = IB_ERR_CUDA;
   cudaEvent_t ev_fork = ev[0], ev_rhs = ev[1], ev_lists = ev[2], ev_f = ev[3], ev_rd = ev[4];
+  cudaEvent_t ev_p = ev[5], ev_b = ev[6];   // the sub-domain's P, and the body block's rows
   do {
     if (rc != IB_OK) break;
     count_launch();
@@ -1188,13 +1189,23 @@ static int capture_fsi_loop(Ctx* c, cudaStream_t st) {
         IB_CUDA_CHECK(cudaEventRecord(ev_fork, s1));
         IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_fork, 0));
         IB_CUDA_CHECK(cudaStreamWaitEvent(s3, ev_fork, 0));
+        // s1 (sub-domain): P at these positions, beside the B rows
+        if (c->sd.on) {
+          RC(launch_sd_interp(c, s1));
+          IB_CUDA_CHECK(cudaEventRecord(ev_p, s1));
+        }
         // s2: the B rows and the right-hand side
         RC(inf_assemble_b(c, s2));
+        IB_CUDA_CHECK(cudaEventRecord(ev_b, s2));
         if (c->nt < c->nbody) IB_CUDA_CHECK(cudaMemsetAsync(c->rhsf, 0, 8 * (size_t)c->nf, s2));
         RC(launch_tors_rhs(c->nt, c->tb, c->ts, p.dt, c->delta, c->rhsf, s2));
         if (c->ub_on) RC(launch_sub_scaled(c->nf, c->delta, c->ub, c->rhsf, s2));
-        if (c->sd.on) RC(launch_sd_rhs(c, c->rhsf, s2));   // P at these positions, then P E_o q
-        else RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s2));
+        if (c->sd.on) {   // P E_o (q + q0), P from s1
+          IB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_p, 0));
+          RC(launch_sd_rhs(c, c->rhsf, s2, false));
+        } else {
+          RC(launch_regT(g, c->nf, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], c->reg, c->rhsf, c->rhsf, s2));
+        }
         IB_CUDA_CHECK(cudaEventRecord(ev_rhs, s2));
         // s3: a copy of the current origins and weights and their contribution lists
         RC(launch_reg_snapshot(c->nf, c->reg, c->reg_ix_s, c->reg_iy_s, c->reg_w_s, s3));
@@ -1202,9 +1213,10 @@ static int capture_fsi_loop(Ctx* c, cudaStream_t st) {
         IB_CUDA_CHECK(cudaMemsetAsync(c->reg.stale, 0, sizeof(int), s3));   // for the weights below
         IB_CUDA_CHECK(cudaEventRecord(ev_lists, s3));
         // s1: assembly (the sub-domain's lumat from P and the B rows of s2) and solve
-        if (c->sd.on) {
-          IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));
+        if (c->sd.on) {   // lumat from P and the B rows, beside the right-hand side
+          IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_b, 0));
           RC(launch_sd_lumat(c, s1));
+          IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));
         } else {
           RC(inf_assemble_kp(c, s1, true));
           IB_CUDA_CHECK(cudaStreamWaitEvent(s1, ev_rhs, 0));

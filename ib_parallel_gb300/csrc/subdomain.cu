@@ -379,14 +379,38 @@ __global__ void __launch_bounds__(128) k_sd_lumat(int nf, const int* __restrict_
   St[(size_t)l * nf + k] = __dadd_rn(body, dot);
 }
 
-// timestepper.F90:390-395: rhsf(j) = P_j . (E_o (q + q0)) + rhsf(j)
-__global__ void k_sd_rhs(int nf, const int* __restrict__ pidx, const double* __restrict__ pw,
-                         const double* __restrict__ eq, double* __restrict__ rhsf) {
+// timestepper.F90:371-395: rhsf(j) = P_j . (E_o (q + q0)) + rhsf(j).  E_o (q + q0) is needed only
+// at the four sub-domain unknowns P_j reads, so each CTA (one body unknown, four warps) forms
+// those four with regT's arithmetic (k_regT: one warp per unknown, lanes over the 49 stencil
+// slots, a xor tree), then thread 0 takes the dot product in order.
+__global__ void __launch_bounds__(128) k_sd_rhs(GridDims g, const int* __restrict__ pidx,
+                                                const double* __restrict__ pw, const double* __restrict__ qx,
+                                                const double* __restrict__ qx0, const double* __restrict__ qy,
+                                                const double* __restrict__ qy0, RegDev r, double* __restrict__ rhsf) {
   IB_GRID_DEP_WAIT();
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nf) return;
+  __shared__ double eq[4];
+  const int k = blockIdx.x, q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int a = pidx[4 * k + q];
+  const bool isx = r.comp[a] == 1;
+  const double* fq = isx ? qx : qy;
+  const double* fq0 = isx ? qx0 : qy0;
+  const int ld = isx ? g.nux : g.nvx, ny = isx ? g.nuy : g.nvy;
+  const int cx = r.ix[a], cy = r.iy[a];
+  const double* wk = r.w + (size_t)a * 49;
+  double acc = 0.0;
+  for (int sl = lane; sl < 49; sl += 32) {
+    const int fi = cx + sl % 7 - 3, fj = cy + sl / 7 - 3;
+    if (fi >= 1 && fi <= ld && fj >= 1 && fj <= ny) {
+      const int idx = (fj - 1) * ld + (fi - 1);
+      acc = fma(wk[sl], fq[idx] + fq0[idx], acc);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) eq[q] = 0.0 + acc;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   double dot = 0.0;
-  for (int q = 0; q < 4; ++q) dot = __dadd_rn(dot, __dmul_rn(pw[4 * k + q], eq[pidx[4 * k + q]]));
+  for (int qq = 0; qq < 4; ++qq) dot = __dadd_rn(dot, __dmul_rn(pw[4 * k + qq], eq[qq]));
   rhsf[k] = __dadd_rn(dot, rhsf[k]);
 }
 
@@ -416,6 +440,8 @@ __global__ void __launch_bounds__(128) k_sd_ptf(int nf, int nf_sd, const int* __
   if (a < nf_sd) fsd[a] = acc;
 }
 
+}  // namespace
+
 int launch_sd_interp(Ctx* c, cudaStream_t st) {
   SubDomain& S = c->sd;
   InterpArgs a;
@@ -428,8 +454,6 @@ int launch_sd_interp(Ctx* c, cudaStream_t st) {
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
-
-}  // namespace
 
 void sd_free(Ctx* c) {
   SubDomain& S = c->sd;
@@ -545,7 +569,6 @@ int sd_setup(Ctx* c, int full_rectangular, double sdxi, double sdxe, double sdyi
   part((void**)&S.rigid, 4 * (size_t)c->nf);
   part((void**)&S.pidx, 4 * kInterp * (size_t)c->nf);
   part((void**)&S.pw, 8 * kInterp * (size_t)c->nf);
-  part((void**)&S.eq, 8 * (size_t)nfs);
   part((void**)&S.fsd, 8 * (size_t)nfs);
   part((void**)&S.pprev, 4 * kPatch * (size_t)sets);
   part((void**)&S.colbuf, 8 * 2 * (size_t)S.max_cand * sets);
@@ -814,13 +837,12 @@ int sd_assemble(Ctx* c, bool interp) {
   return launch_sd_lumat(c, st);
 }
 
-int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st) {
+int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st, bool interp) {
   SubDomain& S = c->sd;
   const GridDims& g = c->g;
-  RC(launch_sd_interp(c, st));
-  RC(launch_regT(g, S.nf_sd, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], S.reg, nullptr, S.eq, st));
+  if (interp) RC(launch_sd_interp(c, st));
   count_launch();
-  k_sd_rhs<<<cdiv(c->nf, 128), 128, 0, st>>>(c->nf, S.pidx, S.pw, S.eq, rhsf);
+  k_sd_rhs<<<c->nf, 128, 0, st>>>(g, S.pidx, S.pw, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], S.reg, rhsf);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }
