@@ -73,7 +73,13 @@ struct Staging {
   }
 };
 
+// Every entry point but the step's output getters may change the state: the pinned copy of the
+// last step's outputs stops being the state's.
 #define CTX_OR_FAIL(h)                                             \
+  if (!(h) || !(h)->c) return fail(IB_ERR_ARG, "null context");    \
+  Ctx* c = (h)->c;                                                 \
+  c->out_fresh = false;
+#define CTX_OR_FAIL_KEEP(h)                                        \
   if (!(h) || !(h)->c) return fail(IB_ERR_ARG, "null context");    \
   Ctx* c = (h)->c;
 
@@ -124,6 +130,8 @@ int ib_synchronize(IbCtx* h) {
 int ib_advance(IbCtx* h, int* itime) {
   CTX_OR_FAIL(h);
   int rc = ib::op_advance(c);
+  // the step is complete (possibly with a solver that stopped short): its outputs are in place
+  c->out_fresh = c->out_queued && (rc == IB_OK || rc == IB_ERR_GMRES || rc == IB_ERR_FSI);
   if (itime) *itime = c->itime;
   if (rc == IB_ERR_GMRES) {
     std::string m = "advance: the step is complete, but a Krylov solve stopped without converging (KSP reason " +
@@ -241,9 +249,15 @@ int ib_set_vector(IbCtx* h, int which, const double* in) {
 }
 
 int ib_get_forces(IbCtx* h, double* cx, double* cy) {
-  CTX_OR_FAIL(h);
+  CTX_OR_FAIL_KEEP(h);
   if (!cx || !cy) return fail(IB_ERR_ARG, "null output");
+  c->want_out = true;   // later steps queue their outputs' copies
   if (c->nbody == 0) return IB_OK;
+  if (c->out_fresh) {
+    std::memcpy(cx, c->h_out, 8 * (size_t)c->nbody);
+    std::memcpy(cy, c->h_out + c->nbody, 8 * (size_t)c->nbody);
+    return IB_OK;
+  }
   int rc = ib::launch_force_coeffs(c->nf, c->nbody, c->comp, c->bid, c->f, c->p.dt, c->delta, c->forces, c->st);
   if (rc) return op_result(rc, "force coefficients failed");
   if (cudaMemcpyAsync(cx, c->forces, 8 * (size_t)c->nbody, cudaMemcpyDefault, c->st) != cudaSuccess ||
@@ -254,8 +268,13 @@ int ib_get_forces(IbCtx* h, double* cx, double* cy) {
 }
 
 int ib_get_body_state(IbCtx* h, double* theta, double* thetad, double* thetadd) {
-  CTX_OR_FAIL(h);
+  CTX_OR_FAIL_KEEP(h);
+  c->want_out = true;
   if (c->nt == 0) return IB_OK;
+  if (c->out_fresh && !thetad && !thetadd) {
+    if (theta) std::memcpy(theta, c->h_out + 2 * c->nbody, 8 * (size_t)c->nt);
+    return IB_OK;
+  }
   size_t n = 8 * (size_t)c->nt;
   if ((theta && cudaMemcpyAsync(theta, c->ts.theta, n, cudaMemcpyDefault, c->st) != cudaSuccess) ||
       (thetad && cudaMemcpyAsync(thetad, c->ts.thetad, n, cudaMemcpyDefault, c->st) != cudaSuccess) ||
@@ -420,8 +439,14 @@ int ib_batch_advance(IbBatch* b, int* status) {
   for (int i = 0; i < n; ++i) b->rc[i] = ib::op_advance_begin(b->sims[i]->c);
   for (int i = 0; i < n; ++i)
     if (b->rc[i] == IB_OK) b->rc[i] = ib::op_advance_end(b->sims[i]->c);
-  for (int i = 0; i < n; ++i)
-    if (b->rc[i] == IB_OK) b->rc[i] = ib::op_advance_finish(b->sims[i]->c);
+  for (int i = 0; i < n; ++i) {
+    ib::Ctx* c = b->sims[i]->c;
+    c->out_fresh = false;
+    if (b->rc[i] == IB_OK) {
+      b->rc[i] = ib::op_advance_finish(c);
+      c->out_fresh = c->out_queued && (b->rc[i] == IB_OK || b->rc[i] == IB_ERR_GMRES || b->rc[i] == IB_ERR_FSI);
+    }
+  }
   int first = IB_OK, where = -1;
   for (int i = 0; i < n; ++i) {
     if (status) status[i] = b->rc[i];
@@ -472,7 +497,7 @@ int ib_get_beam_state(IbCtx* h, double* q, double* qd, double* qdd) {
 }
 
 int ib_get_counters(IbCtx* h, int* ksp_iter, int* fsi_iter) {
-  CTX_OR_FAIL(h);
+  CTX_OR_FAIL_KEEP(h);
   if (ksp_iter) *ksp_iter = c->ksp_iter;
   if (fsi_iter) *fsi_iter = c->fsi_iter;
   return IB_OK;

@@ -346,6 +346,14 @@ struct Ctx {
   int* d_err = nullptr;
   int* h_ist = nullptr;            // pinned mirror of G.ist
   double* h_scal = nullptr;        // pinned mirror of err_fsi[0]
+  // The step's outputs in mapped pinned memory: force coefficients (cx of every body, then cy)
+  // and hinge angles.  Once the host has asked for them, every step's coefficient kernel writes
+  // them there before the step finishes (want_out), and ib_get_forces / ib_get_body_state read
+  // them without a device round trip while out_fresh (set by ib_advance when they were written,
+  // cleared by every other entry point that may change the state).
+  double* h_out = nullptr;
+  double* d_out = nullptr;         // h_out's device address (mapped)
+  bool want_out = false, out_queued = false, out_fresh = false;
 
   // staging for host pointers passed to operator entry points
   double* stage[8] = {nullptr};

@@ -362,28 +362,42 @@ int launch_redistribute_field(const GridDims& g, int nf, const double* f, const 
   return IB_OK;
 }
 
-// write_force2: out[b] = 2 delta sum_x f/dt, out[nbody+b] = 2 delta sum_y f/dt
+// write_force2: out[b] = 2 delta sum_x f/dt, out[nbody+b] = 2 delta sum_y f/dt, each sum in the
+// order of the unknowns.  One warp per body: the lanes divide (f/dt, about ten FP64 instructions
+// each) a chunk of the unknowns at a time into shared memory, then lane 0 adds the x terms and
+// lane 1 the y terms in order.  With mirror set the coefficients, and the nt hinge angles after
+// them, are also written there (pinned host memory the device maps).
+constexpr int kForceChunk = 1024;
 __global__ void k_force_coeffs(int nf, int nbody, const int* __restrict__ comp, const int* __restrict__ bid,
-                               const double* __restrict__ f, double dt, double delta, double* out) {
+                               const double* __restrict__ f, double dt, double delta, double* out, double* mirror,
+                               const double* __restrict__ theta, int nt) {
   IB_GRID_DEP_WAIT();
-  // one thread per body, sequential in unknown order
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbody) return;
-  double fx = 0.0, fy = 0.0;
-  for (int k = 0; k < nf; ++k) {
-    if (bid[k] != b) continue;
-    if (comp[k] == 1) fx = fx + f[k] / dt;
-    else fy = fy + f[k] / dt;
+  __shared__ double q[kForceChunk];
+  const int b = blockIdx.x, lane = threadIdx.x;
+  double acc = 0.0;   // lane 0: x terms, lane 1: y terms
+  for (int k0 = 0; k0 < nf; k0 += kForceChunk) {
+    const int n = min(kForceChunk, nf - k0);
+    for (int i = lane; i < n; i += 32) q[i] = bid[k0 + i] == b ? f[k0 + i] / dt : 0.0;
+    __syncwarp();
+    if (lane < 2)
+      for (int i = 0; i < n; ++i)
+        if (bid[k0 + i] == b && (comp[k0 + i] == 1) == (lane == 0)) acc = acc + q[i];
+    __syncwarp();
   }
-  out[b] = 2.0 * delta * fx;
-  out[nbody + b] = 2.0 * delta * fy;
+  if (lane < 2) {
+    const double v = 2.0 * delta * acc;
+    out[lane * nbody + b] = v;
+    if (mirror) mirror[lane * nbody + b] = v;
+  }
+  if (mirror && b == 0)
+    for (int t = lane; t < nt; t += 32) mirror[2 * nbody + t] = theta[t];
 }
 
 int launch_force_coeffs(int nf, int nbody, const int* comp, const int* bid, const double* f, double dt,
-                        double delta, double* out, cudaStream_t st) {
+                        double delta, double* out, cudaStream_t st, double* mirror, const double* theta, int nt) {
   if (nbody == 0) return IB_OK;
   count_launch();
-  k_force_coeffs<<<cdiv(nbody, 32), 32, 0, st>>>(nf, nbody, comp, bid, f, dt, delta, out);
+  k_force_coeffs<<<nbody, 32, 0, st>>>(nf, nbody, comp, bid, f, dt, delta, out, mirror, theta, nt);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

@@ -99,8 +99,11 @@ int launch_regT_s(const GridDims& g, int nf, const double* s, const double* ring
 // finter = E^T f / E^T 1 on faces with weight > 1e-10 (operators_struct.F90:810-834)
 int launch_redistribute_field(const GridDims& g, int nf, const double* f, const RegDev& r, double* fx,
                               double* fy, cudaStream_t st);
+// mirror (optional): device address of pinned host memory that also receives the coefficients
+// and, after them, the nt values of theta
 int launch_force_coeffs(int nf, int nbody, const int* comp, const int* bid, const double* f, double dt,
-                        double delta, double* out, cudaStream_t st);
+                        double delta, double* out, cudaStream_t st, double* mirror = nullptr,
+                        const double* theta = nullptr, int nt = 0);
 
 // structure.cu -- operators_struct.F90 (family 2, torsional bodies)
 struct TorsBody {

@@ -302,7 +302,10 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   for (int i = 0; i < 8; ++i) c->stage[i] = P.take<double>(stage_n);
   if (!c->stage[7] || !c->d_err) { *msg = "internal pool overflow"; ctx_destroy(c); return IB_ERR_NOMEM; }
   if (cudaMallocHost(&c->h_ist, 16 * sizeof(int)) != cudaSuccess ||   // [12]: the step's error word
-      cudaMallocHost(&c->h_scal, 4 * sizeof(double)) != cudaSuccess) {
+      cudaMallocHost(&c->h_scal, 4 * sizeof(double)) != cudaSuccess ||
+      cudaHostAlloc(&c->h_out, sizeof(double) * (2 * (size_t)nbody + (size_t)nt + 1), cudaHostAllocMapped) !=
+          cudaSuccess ||
+      cudaHostGetDevicePointer(&c->d_out, c->h_out, 0) != cudaSuccess) {
     *msg = "pinned allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM;
   }
 
@@ -453,6 +456,7 @@ void ctx_destroy(Ctx* c) {
   if (c->pool.base) cudaFree(c->pool.base);
   if (c->h_ist) cudaFreeHost(c->h_ist);
   if (c->h_scal) cudaFreeHost(c->h_scal);
+  if (c->h_out) cudaFreeHost(c->h_out);
   for (auto& e : c->prof_ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->stage_ev)
@@ -1650,7 +1654,24 @@ int op_advance_begin(Ctx* c) {
   return IB_OK;
 }
 
+static int advance_end(Ctx* c);
+
+// The step's end, then (once the host has asked for them) the copies of its outputs into
+// pinned memory, queued before the step finishes (write_force2's values, operators_struct.F90:
+// 711-731, and the hinge angles).
 int op_advance_end(Ctx* c) {
+  c->out_queued = false;
+  RC(advance_end(c));
+  if (!c->want_out) return IB_OK;
+  // the coefficient kernel writes them, and the hinge angles, straight into the mapped buffer
+  if (c->nbody > 0)
+    RC(launch_force_coeffs(c->nf, c->nbody, c->comp, c->bid, c->f, c->p.dt, c->delta, c->forces, c->st, c->d_out,
+                           c->ts.theta, c->nt));
+  c->out_queued = true;
+  return IB_OK;
+}
+
+static int advance_end(Ctx* c) {
   if (!c->end_pending) return IB_ERR_STATE;
   c->end_pending = false;
   const GridDims& g = c->g;

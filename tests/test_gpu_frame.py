@@ -59,3 +59,32 @@ def test_steps_of_a_turning_frame_match_the_oracle(num_stat):
         ox, oy = o.force_coeffs(o.f)
         assert rel(np.r_[cx, cy], np.r_[ox, oy]) < tol, step
     g.close()
+
+
+def test_step_outputs_follow_the_state():
+    # once the host has read a step's forces, later steps copy their force coefficients and
+    # hinge angles to pinned memory before they finish, and the getters read them there; any
+    # other entry point (here the forces set directly) makes the getters go to the device again
+    from helpers import PLATE, small_plate
+    g = G.Simulation(G.Params(**PLATE), [small_plate()])
+    th = np.zeros(1)
+
+    def theta():
+        G._check(g.lib.ib_get_body_state(g.h, G._ptr(th), None, None), "ib_get_body_state")
+        return th.copy()
+
+    g.advance()
+    g.forces()
+    for _ in range(3):
+        g.advance()
+        cx, cy = g.forces()
+        t = theta()
+        g.synchronize()                      # any other call: the next reads go to the device
+        cx2, cy2 = g.forces()
+        assert np.array_equal(cx, cx2) and np.array_equal(cy, cy2)
+        assert np.array_equal(t, theta()) and np.array_equal(t, g.body_state()[0])
+    f = g.get_vector("f")
+    g.set_vector("f", 2.0 * f)
+    cx3, _ = g.forces()
+    assert np.allclose(cx3, 2.0 * cx2, rtol=1e-14, atol=0)
+    g.close()
