@@ -43,6 +43,15 @@ __global__ void k_adj_combine(int n, const double* __restrict__ b0, const double
   out[i] = __dadd_rn(__dadd_rn(__dmul_rn(c0, b0[i]), __dmul_rn(c1, b1[i])), __dmul_rn(c2, b2[i]));
 }
 
+// T[i][j] = M[j][i] (n x n)
+__global__ void k_adj_transpose(int n, const double* __restrict__ M, double* __restrict__ T) {
+  IB_GRID_DEP_WAIT();
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * n) return;
+  const int i = (int)(t / n), j = (int)(t - (long long)i * n);
+  T[t] = M[(size_t)j * n + i];
+}
+
 // out = a x + b y (y may be null)
 __global__ void k_adj_axpby(int n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
                             double* __restrict__ out) {
@@ -396,25 +405,41 @@ int step_T(Adj& a, int slot, int it, const double* frame, const double* dforce_h
   // correction omega_0 - ainv(rot(reg f)), the direct solve, the force coefficients
   RC(op_ainv(c, A.lw[0], A.t1));
   RC(launch_curl(g, A.t1, c->zero_ring, A.hx, A.hy, st));
-  RC(launch_regT(g, c->nf, A.hx, nullptr, A.hy, nullptr, c->reg, nullptr, A.lf, st));
+  // the correction spread E^T f (the sub-domain's E_o^T P^T f): its transpose, E (P E_o)
+  if (c->sd.on) RC(launch_sd_ET(c, A.hx, A.hy, A.lf, st));
+  else RC(launch_regT(g, c->nf, A.hx, nullptr, A.hy, nullptr, c->reg, nullptr, A.lf, st));
   count_launch();
   k_adj_force<<<blocks(c->nf), kT, 0, st>>>(c->nf, c->nbody, c->comp, c->bid, 2.0 * c->delta / c->p.dt, A.dforce,
                                             A.lf, A.lf);
   if (c->p.num_stat) {
     RC(launch_chol_solve(c->nf, c->cholM, A.lf, A.lrhsf, st));
   } else {
-    // S^T lrhsf = lf: the band's row-major S (rigid bodies: no structure block) as the
-    // column-major operator of the cluster solver, from a zero start
+    // S^T lrhsf = lf: the band's row-major S (rigid bodies: no structure block), or the
+    // sub-domain's lumat transposed, as the column-major operator of the cluster solver, from a
+    // zero start
     const IbParams& p = c->p;
+    const double* opT = c->inf.S;
+    if (c->sd.on) {
+      count_launch();
+      k_adj_transpose<<<(unsigned)cdiv((long long)c->nf * c->nf, kT), kT, 0, st>>>(c->nf, c->inf.St, A.opT);
+      IB_CUDA_CHECK(cudaGetLastError());
+      opT = A.opT;
+    }
     IB_CUDA_CHECK(cudaMemsetAsync(A.lrhsf, 0, 8 * (size_t)c->nf, st));
-    RC(launch_gmres_fused(c->G, &c->fused_plan, c->inf.S, A.lf, A.lrhsf, p.rtol, p.atol, p.gmres_max_it, st));
+    RC(launch_gmres_fused(c->G, &c->fused_plan, opT, A.lf, A.lrhsf, p.rtol, p.atol, p.gmres_max_it, st));
     int ist[2] = {0, 0};
     IB_CUDA_CHECK(cudaMemcpyAsync(ist, c->G.ist, sizeof(ist), cudaMemcpyDeviceToHost, st));
     IB_CUDA_CHECK(cudaStreamSynchronize(st));
     if (ist[1] < 0) return IB_ERR_GMRES;   // the transposed solve stopped without converging
   }
   // rhsf = regT(q*_0 + q0_0): the flux adjoint on level 0, then the first vort2flux transposed
-  RC(launch_reg(g, c->nf, A.lrhsf, c->reg, A.ax, A.ay, st));
+  if (c->sd.on) {   // rhsf = P E_o (q + q0): its transpose is the spread E_o^T P^T
+    IB_CUDA_CHECK(cudaMemsetAsync(A.ax, 0, 8 * (size_t)g.nu, st));
+    IB_CUDA_CHECK(cudaMemsetAsync(A.ay, 0, 8 * (size_t)g.nv, st));
+    RC(launch_sd_spread(c, A.lrhsf, A.ax, A.ay, st));
+  } else {
+    RC(launch_reg(g, c->nf, A.lrhsf, c->reg, A.ax, A.ay, st));
+  }
   for (int k = 0; k < L; ++k) IB_CUDA_CHECK(cudaMemcpyAsync(A.lostar[k], A.lw[k], 8 * (size_t)g.ns, cudaMemcpyDeviceToDevice, st));
   {
     std::vector<double*> zx(L, nullptr), zy(L, nullptr);
@@ -570,7 +595,7 @@ static int adjoint_alloc(Ctx* c) {
                    2 * (size_t)L * (g.nu + g.nv) /* lq (x2) */ + 2 * (size_t)L * g.ns /* lw, lostar */ +
                    4 * (size_t)g.ns /* t1-t3, zero */ + 3 * (size_t)(g.nu + g.nv) /* hx hy, ax ay */ +
                    3 * (size_t)g.nbc + 2 * (size_t)std::max(c->nf, 1) + 2 * (size_t)std::max(c->nbody, 1) +
-                   3 * 4096 + 3 * (size_t)kDotBlocks;
+                   3 * 4096 + 3 * (size_t)kDotBlocks + (size_t)std::max(c->nf, 1) * std::max(c->nf, 1);
   IB_CUDA_CHECK(cudaMalloc(&A.mem, 8 * n));
   IB_CUDA_CHECK(cudaMemset(A.mem, 0, 8 * n));
   double* p = (double*)A.mem;
@@ -589,6 +614,7 @@ static int adjoint_alloc(Ctx* c) {
   A.dforce = take(2 * (size_t)std::max(c->nbody, 1));
   A.dframe = take(3 * 4096);
   A.dpart = take(3 * (size_t)kDotBlocks);
+  A.opT = take((size_t)std::max(c->nf, 1) * std::max(c->nf, 1));
   const double cx = c->p.motion[3], cy = c->p.motion[4];
   for (int b = 0; b < 3; ++b) {
     std::vector<double> h = frame_flux_host(c, b == 0, b == 1, b == 2, cx, cy);
@@ -599,7 +625,7 @@ static int adjoint_alloc(Ctx* c) {
 
 int op_adjoint_forward(Ctx* c, int nsteps, int K, const double* frames, double* forces, std::string* msg) {
   AdjointState& A = c->adj;
-  if (c->nt > 0 || c->nbeam > 0 || c->sd.on || c->nf == 0) {
+  if (c->nt > 0 || c->nbeam > 0 || c->nf == 0) {
     *msg = "the adjoint covers stationary rigid bodies";
     return IB_ERR_ARG;
   }

@@ -213,6 +213,7 @@ struct AdjointState {
   double *hx = nullptr, *hy = nullptr, *ax = nullptr, *ay = nullptr;
   double *ring1 = nullptr, *ring2 = nullptr, *ring3 = nullptr;
   double *lf = nullptr, *lrhsf = nullptr, *dforce = nullptr, *dframe = nullptr, *dpart = nullptr;
+  double* opT = nullptr;   // the sub-domain's lumat transposed (column-major), for the reverse solve
 };
 
 struct Ctx {
@@ -462,6 +463,7 @@ void cr_dilate(const GridDims& g, std::vector<unsigned char>& mask, int r);
 // rhsf = P E_o (q + q0) + rhsf (P formed first at the current positions unless interp is false)
 int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st, bool interp = true);
 int launch_sd_interp(Ctx* c, cudaStream_t st);            // P at the current positions
+int launch_sd_ET(Ctx* c, const double* hx, const double* hy, double* out, cudaStream_t st);   // out = P E_o h
 int launch_sd_spread(Ctx* c, const double* f, double* hx, double* hy, cudaStream_t st);   // E_o^T P^T f
 int sd_write(Ctx* c, const char* path, std::string* msg);
 int sd_read(Ctx* c, const char* path, std::string* msg);

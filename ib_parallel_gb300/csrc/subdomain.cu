@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(128) k_sd_rhs(GridDims g, const int* __restric
     const int fi = cx + sl % 7 - 3, fj = cy + sl / 7 - 3;
     if (fi >= 1 && fi <= ld && fj >= 1 && fj <= ny) {
       const int idx = (fj - 1) * ld + (fi - 1);
-      acc = fma(wk[sl], fq[idx] + fq0[idx], acc);
+      acc = fma(wk[sl], fq0 ? fq[idx] + fq0[idx] : fq[idx], acc);
     }
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -843,6 +843,15 @@ int launch_sd_rhs(Ctx* c, double* rhsf, cudaStream_t st, bool interp) {
   if (interp) RC(launch_sd_interp(c, st));
   count_launch();
   k_sd_rhs<<<c->nf, 128, 0, st>>>(g, S.pidx, S.pw, c->qx[0], c->q0x[0], c->qy[0], c->q0y[0], S.reg, rhsf);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+int launch_sd_ET(Ctx* c, const double* hx, const double* hy, double* out, cudaStream_t st) {
+  SubDomain& S = c->sd;
+  IB_CUDA_CHECK(cudaMemsetAsync(out, 0, 8 * (size_t)c->nf, st));
+  count_launch();
+  k_sd_rhs<<<c->nf, 128, 0, st>>>(c->g, S.pidx, S.pw, hx, nullptr, hy, nullptr, S.reg, out);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
 }

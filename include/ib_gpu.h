@@ -171,8 +171,9 @@ int ib_subdomain_operator(IbCtx* ctx, double* lumat);
 int ib_get_subdomain_stats(IbCtx* ctx, long long* counts, double* precompute_ms);
 /* The discrete adjoint of the step (no reference counterpart) for stationary rigid bodies in a
  * moving frame, their Schur system solved directly (num_stat = 1) or by GMRES on the assembled
- * operator (num_stat = 0, schur_mode 0; the reverse solves the transposed system the same way
- * and returns IB_ERR_GMRES if that solve stops without converging).  The frame's flux
+ * operator or the sub-domain method's lumat (num_stat = 0, schur_mode 0; the reverse solves the
+ * transposed system the same way and returns IB_ERR_GMRES if that solve stops without
+ * converging).  The frame's flux
  * (motion_potential + motion_rotation, variables.F90:299-360) is linear in its velocity (u, v)
  * and angular velocity W about the centre (motion[3], motion[4]), so a body pitching or plunging
  * in its own frame is given by a triple (u, v, W) per step (the reference's motion_grid of

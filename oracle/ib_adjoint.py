@@ -22,7 +22,8 @@ Transposes used (each is the exact adjoint of the oracle's forward arithmetic):
     reference solves the Schur system by GMRES (timestepper.F90:363-366); here the forward solves
     it exactly with the dense Schur matrix (a_times on unit vectors; the bodies do not move, so it
     is formed once) and the reverse solves with its transpose: the adjoint of the exact solve,
-    which a converged Krylov solve approaches.
+    which a converged Krylov solve approaches.  With the sub-domain method the matrix is lumat,
+    E is P E_o and E^T is E_o^T P^T (each the other's transpose).
 The step's state between steps is (omega, q, rhs_old) on every level.
 """
 from __future__ import annotations
@@ -46,11 +47,32 @@ class Adjoint:
         self.bases = bases        # [u, v, W] -> (q0x levels, q0y levels)
 
     def schur(self):
-        """The Schur matrix a_times (operators_fluid.F90:14-120) column by column."""
+        """The Schur matrix a_times (operators_fluid.F90:14-120) column by column, or with the
+        sub-domain method lumat = body + P B^T P^T (operators_struct.F90:840-905)."""
         if self.S is None:
-            eye = np.eye(self.o.nf)
-            self.S = np.stack([self.o.a_times(eye[l]) for l in range(self.o.nf)], axis=1)
+            o = self.o
+            if o.sd is not None:
+                if o.sd.cols is None:
+                    o.sd.precompute()
+                self.S = o.sd.lumat(*o.sd.interp())
+            else:
+                eye = np.eye(o.nf)
+                self.S = np.stack([o.a_times(eye[l]) for l in range(o.nf)], axis=1)
         return self.S
+
+    # the transfers of the Schur system: E (q + q0) into its right-hand side and E^T f out of its
+    # solution; with the sub-domain method P E_o and E_o^T P^T (timestepper.F90:380-397, 500-516)
+    def E(self, qx, qy):
+        o = self.o
+        if o.sd is not None:
+            return o.sd.rhs_add(np.zeros(o.nf), qx, qy, *o.sd.interp())
+        return o.regT(qx, qy)
+
+    def ET(self, f):
+        o = self.o
+        if o.sd is not None:
+            return o.sd.spread(f, *o.sd.interp())
+        return o.reg(f)
 
     def frame(self, c):
         qx = [c[0] * self.bases[0][0][k] + c[1] * self.bases[1][0][k] + c[2] * self.bases[2][0][k]
@@ -88,9 +110,9 @@ class Adjoint:
             o.rhs_old[k] = rhs
         s, qx, qy = o.vort2flux(ostar)          # coarsifies ostar in place
         tape["ostar_c"] = [w.copy() for w in ostar]
-        rhsf = o.regT(qx[0] + q0x[0], qy[0] + q0y[0], 0.0 - o.delta * o.ub)
+        rhsf = self.E(qx[0] + q0x[0], qy[0] + q0y[0]) + (0.0 - o.delta * o.ub)
         f = o.chol_solve(rhsf) if o.p.num_stat else np.linalg.solve(self.schur(), rhsf)
-        hx, hy = o.reg(f)
+        hx, hy = self.ET(f)
         ostar[0] = ostar[0] - o.ainv(o.rot(hx, hy))
         o.omega = ostar
         o.s, o.qx, o.qy = o.vort2flux(o.omega)
@@ -263,13 +285,13 @@ class Adjoint:
         lf = np.zeros(o.nf)
         g = o.ainv(lw[0])
         hx, hy = self.rot_T(g)
-        lf -= o.regT(hx, hy)
+        lf -= self.E(hx, hy)
         scale = 2.0 * o.delta / o.p.dt
         for kf in range(o.nf):
             lf[kf] += scale * lforce[o.bid[kf], 0 if o.comp[kf] == 1 else 1]
         lrhsf = o.chol_solve(lf) if o.p.num_stat else np.linalg.solve(self.schur().T, lf)
         # rhsf = regT(q*_0 + q0_0): the adjoint fluxes on level 0
-        ax, ay = o.reg(lrhsf)
+        ax, ay = self.ET(lrhsf)
         lq0x = [np.zeros_like(b) for b in tape["q0x"]]
         lq0y = [np.zeros_like(b) for b in tape["q0y"]]
         lq0x[0] += ax

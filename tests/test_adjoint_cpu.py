@@ -95,3 +95,37 @@ def test_forward_equals_the_oracle_step():
         o2.advance()
     for k in range(o1.L):
         assert np.allclose(o1.omega[k], o2.omega[k], rtol=0, atol=1e-13 * np.abs(o2.omega[k]).max())
+
+
+def _sd_oracle(cols=None):
+    import ib_subdomain as SD
+    p = O.Params(m=64, n=32, mgridlev=3, dt=0.01, Re=100.0, len=4.0, offsetx=1.0, offsety=1.0, num_stat=False,
+                 motion=(-1.0, 0.0, 0.0, 0.3, 0.0))
+    o = O.IBOracle(p, [O.cylinder(npts=8, diameter=0.3, xc=0.1, yc=0.0)])
+    o.sd = SD.SubDomain(o, True, -0.25, 0.5, -0.25, 0.25, 0.0625)
+    if cols is None:
+        o.sd.precompute()
+    else:
+        o.sd.cols = cols
+    return o
+
+
+def test_subdomain_gradient_matches_central_differences():
+    # the sub-domain method: lumat and its transpose, P E_o and E_o^T P^T
+    N = 4
+    coefs = _coefs(N)
+    W = np.random.default_rng(2).standard_normal((N, 1, 2))
+    cols = _sd_oracle().sd.cols
+
+    def J(c):
+        ad = A.Adjoint(_sd_oracle(cols))
+        return float(np.sum(W * ad.forward(c))), ad
+
+    J0, ad = J(coefs)
+    g = ad.backward(W)
+    h = 1e-6
+    for (n, i) in [(0, 0), (1, 2), (3, 1)]:
+        cp = coefs.copy(); cp[n, i] += h
+        cm = coefs.copy(); cm[n, i] -= h
+        fd = (J(cp)[0] - J(cm)[0]) / (2 * h)
+        assert abs(g[n, i] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(g).max()), (n, i, g[n, i], fd)

@@ -3,7 +3,7 @@ bodies in a moving frame: its forward against plain steps, its gradient against 
 adjoint (oracle/ib_adjoint.py), against central differences of the GPU forward, for every
 checkpoint interval, the context left as the forward left it, and the torch.autograd binding
 carrying the gradient to pitching parameters; the same with the Schur system solved by GMRES
-(num_stat = F) and its transpose in the reverse."""
+(num_stat = F) and its transpose in the reverse, and through the sub-domain method."""
 import numpy as np
 import pytest
 
@@ -216,3 +216,70 @@ def test_gmres_path_checkpoint_interval_does_not_change_the_gradient(K):
     g = _gpu_gmres()
     g.adjoint_forward(coefs, K=K)
     assert np.array_equal(g.adjoint_backward(W), g0)
+
+
+# the sub-domain method (sub_domain = T): a small rigid cylinder inside a 13 x 9 cloud
+SD_CLOUD = (-0.25, 0.5, -0.25, 0.25, 0.0625)
+
+
+def _sd_body():
+    b = O.cylinder(npts=8, diameter=0.3, xc=0.1, yc=0.0)
+    return b, dict(x=b.x.copy(), y=b.y.copy(), fam=1)
+
+
+def _gpu_sd(path=None):
+    g = G.Simulation(G.Params(**KWG), [G.Body(**_sd_body()[1])])
+    g.subdomain_setup(*SD_CLOUD)
+    if path is not None:
+        g.read_subdomain_matrix(path)
+    return g
+
+
+def _sd_matrix(tmp_path):
+    g = _gpu_sd()
+    g.subdomain_precompute()
+    path = tmp_path / "sd_adjoint.chd"
+    g.write_subdomain_matrix(path)
+    g.close()
+    return path
+
+
+def test_subdomain_gradient_matches_the_oracle_adjoint(tmp_path):
+    import ib_subdomain as SD
+    path = _sd_matrix(tmp_path)
+    N = 5
+    coefs = _coefs(N)
+    W = np.random.default_rng(11).standard_normal((N, 1, 2))
+    p = O.Params(**{k: v for k, v in KWG.items() if k in O.Params.__dataclass_fields__})
+    o = O.IBOracle(p, [_sd_body()[0]])
+    o.sd = SD.SubDomain(o, True, *SD_CLOUD)
+    o.sd.read_chd(path)                  # the same thinned B on both sides
+    ad = A.Adjoint(o)
+    Fo = ad.forward(coefs)
+    go = ad.backward(W)
+    g = _gpu_sd(path)
+    Fg = g.adjoint_forward(coefs, K=2)
+    gg = g.adjoint_backward(W)
+    assert np.abs(Fg - Fo).max() < 1e-10 * np.abs(Fo).max()
+    assert np.abs(gg - go).max() < 1e-8 * np.abs(go).max(), np.abs(gg - go).max() / np.abs(go).max()
+
+
+def test_subdomain_gradient_matches_central_differences(tmp_path):
+    path = _sd_matrix(tmp_path)
+    N = 5
+    coefs = _coefs(N)
+    W = np.random.default_rng(12).standard_normal((N, 1, 2))
+    g = _gpu_sd(path)
+    g.adjoint_forward(coefs, K=2)
+    grad = g.adjoint_backward(W)
+
+    def J(c):
+        s = _gpu_sd(path)
+        return float(np.sum(W * s.adjoint_forward(c, K=N)))
+
+    h = 1e-6
+    for (n, i) in [(0, 0), (2, 1), (4, 2)]:
+        cp = coefs.copy(); cp[n, i] += h
+        cm = coefs.copy(); cm[n, i] -= h
+        fd = (J(cp) - J(cm)) / (2 * h)
+        assert abs(grad[n, i] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(grad).max()), (n, i, grad[n, i], fd)
