@@ -602,6 +602,10 @@ def run_gpu(args, world, rank, local):
                                   "over the measured step time; the influence matrix replaces the per-iteration "
                                   "work, so this is a step-level figure, not a kernel roofline"},
         "tridiagonal_pass_us": 1e3 * t_tri,
+        "nonlinear_stencil_us": {"plain_loads": 1e3 * sim.time_pass(4, 10), "bulk_copies": 1e3 * sim.time_pass(5, 10),
+                                 "note": "the predictor's fused nonlinear + rot stencil of all five levels, inputs "
+                                         "from HBM; bulk_copies stages the interior tiles' rows with cp.async.bulk "
+                                         "(same bits, checked)"},
         "pressure": _pressure_leg(sim, p),
         "schur_stages_us": sim.profile_schur(20),
         "influence": sim.influence_stats(),

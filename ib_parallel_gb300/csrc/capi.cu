@@ -769,8 +769,9 @@ int ib_measure_fp64_peak(double* tflops) {
 
 int ib_time_pass(IbCtx* h, int kind, int reps, double* avg_ms) {
   CTX_OR_FAIL(h);
-  if (!avg_ms || reps <= 0 || kind < 0 || kind > 3) return fail(IB_ERR_ARG, "bad argument");
-  if (kind >= 2) return op_result(ib::op_time_pressure_transform(c, kind == 2, reps, avg_ms), "time_pass failed");
+  if (!avg_ms || reps <= 0 || kind < 0 || kind > 5) return fail(IB_ERR_ARG, "bad argument");
+  if (kind == 2 || kind == 3)
+    return op_result(ib::op_time_pressure_transform(c, kind == 2, reps, avg_ms), "time_pass failed");
   return op_result(ib::op_time_pass(c, kind, reps, avg_ms), "time_pass failed");
 }
 

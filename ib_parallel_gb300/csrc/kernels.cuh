@@ -49,6 +49,8 @@ struct NlBatch {
   double* out[kMaxLevels] = {};
 };
 int launch_nonlinear_rot_levels(const GridDims& g, const NlBatch& b, int nlev, cudaStream_t st);
+// the same with the interior tiles' rows staged by bulk copies (the measured alternative)
+int launch_nonlinear_rot_levels_bulk(const GridDims& g, const NlBatch& b, int nlev, int* err, cudaStream_t st);
 int launch_apply_bc(const GridDims& g, double* v, const double* ring, double fac, cudaStream_t st);
 int launch_rhsbc(const GridDims& g, double* v, const double* ra, const double* rb, double fac, cudaStream_t st);
 int launch_axpby(int n, double a, const double* x, double b, const double* y, double* z, cudaStream_t st);

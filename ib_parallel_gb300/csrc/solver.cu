@@ -806,9 +806,83 @@ static int redistribute_with(Ctx* c, const RegDev& r, const double* f, double* f
 
 int op_redistribute(Ctx* c, const double* f, double* frdst) { return redistribute_with(c, c->reg, f, frdst); }
 
+// Kinds 4 and 5: the predictor's nonlinear-and-rot stencil over every level on the context's
+// current fields, with plain loads (4) or with the interior tiles' rows staged by bulk copies
+// (5), each launch after a write of twice the L2 size (so its inputs come from HBM).  Kind 5
+// first checks that both give the same bits.
+static int time_nonlinear(Ctx* c, bool bulk, int reps, double* avg_ms) {
+  const GridDims& g = c->g;
+  const int L = c->L;
+  cudaStream_t st = c->st;
+  int dev = 0, l2 = 0;
+  IB_CUDA_CHECK(cudaGetDevice(&dev));
+  IB_CUDA_CHECK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+  double* out = nullptr;
+  void* flush = nullptr;
+  const size_t fbytes = 2 * (size_t)l2;
+  IB_CUDA_CHECK(cudaMalloc(&out, 16 * (size_t)g.ns * L));
+  if (cudaMalloc(&flush, fbytes) != cudaSuccess) {
+    cudaFree(out);
+    return IB_ERR_NOMEM;
+  }
+  NlBatch b[2];
+  for (int v = 0; v < 2; ++v)
+    for (int k = 0; k < L; ++k) {
+      b[v].om[k] = c->omega[k];
+      b[v].bc[k] = c->lastbc[k];
+      b[v].qx[k] = c->qx[k];
+      b[v].q0x[k] = c->q0x[k];
+      b[v].qy[k] = c->qy[k];
+      b[v].q0y[k] = c->q0y[k];
+      b[v].out[k] = out + ((size_t)v * L + k) * g.ns;
+    }
+  int rc = IB_OK;
+  auto launch = [&](bool use_bulk, int v) {
+    return use_bulk ? launch_nonlinear_rot_levels_bulk(g, b[v], L, c->d_err, st)
+                    : launch_nonlinear_rot_levels(g, b[v], L, st);
+  };
+  if (bulk) {   // the two kernels' outputs, bit for bit
+    rc = launch(false, 0);
+    if (rc == IB_OK) rc = launch(true, 1);
+    if (rc == IB_OK) {
+      std::vector<double> h(2 * (size_t)g.ns * L);
+      if (cudaMemcpyAsync(h.data(), out, 8 * h.size(), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        rc = IB_ERR_CUDA;
+      else if (std::memcmp(h.data(), h.data() + (size_t)g.ns * L, 8 * (size_t)g.ns * L) != 0)
+        rc = IB_ERR_STATE;
+    }
+    if (rc == IB_OK) rc = check_err(c);
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (rc == IB_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = IB_ERR_CUDA;
+  double total = 0.0;
+  for (int r = 0; r < reps && rc == IB_OK; ++r) {
+    if (cudaMemsetAsync(flush, r & 0xff, fbytes, st) != cudaSuccess) rc = IB_ERR_CUDA;
+    if (rc == IB_OK && cudaEventRecord(e0, st) != cudaSuccess) rc = IB_ERR_CUDA;
+    if (rc == IB_OK) rc = launch(bulk, 0);
+    if (rc == IB_OK && cudaEventRecord(e1, st) != cudaSuccess) rc = IB_ERR_CUDA;
+    if (rc == IB_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = IB_ERR_CUDA;
+    float ms = 0.f;
+    if (rc == IB_OK) cudaEventElapsedTime(&ms, e0, e1);
+    total += ms;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  cudaFree(out);
+  cudaFree(flush);
+  if (rc == IB_OK) rc = check_err(c);
+  RC(rc);
+  *avg_ms = total / reps;
+  return IB_OK;
+}
+
 // Device time of `reps` back-to-back launches of one full pass over the finest grid
-// (kind 0: x pass, 1: tridiagonal solve), for the roofline of a kernel timed alone.
+// (kind 0: x pass, 1: tridiagonal solve), for the roofline of a kernel timed alone; kinds 4
+// and 5: time_nonlinear.
 int op_time_pass(Ctx* c, int kind, int reps, double* avg_ms) {
+  if (kind == 4 || kind == 5) return time_nonlinear(c, kind == 5, reps, avg_ms);
   // Each launch reads and writes its own pair of fields, and the pairs together are more than
   // twice L2, so every pass starts with its input in HBM, as in a step.
   cudaStream_t st = c->st;

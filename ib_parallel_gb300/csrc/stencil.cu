@@ -146,6 +146,203 @@ __global__ void __launch_bounds__(kNlTx * kNlTy) k_nonlinear_rot_levels(GridDims
   }
 }
 
+// The same kernel with the interior tiles' rows brought into shared memory by bulk copies
+// (cp.async.bulk, completing on an mbarrier), the measured alternative to the plain loads
+// above (op_time_pass kinds 4 and 5).  The fields keep the reference's layout, whose row pitches
+// (799, 800 and 801 doubles) are not all multiples of 16 bytes, so no tiled tensor map can
+// describe them.  Each row is copied from the even element at or before its first one, a
+// 16-byte boundary of the 256-byte-aligned fields, over an even number of elements, and read
+// from its offset in shared memory.  Tiles on the domain's edges, and any row whose rounded copy
+// would pass the end of its field, take the plain loads.  The wait on the mbarrier is bounded:
+// past the limit the CTA records IB_ERR_CUDA in err, waits (bounded again) for its copies, and
+// writes nothing.
+constexpr int kNlPitch = 40;   // doubles a staged row holds (a tile row plus the alignment slack)
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__global__ void __launch_bounds__(kNlTx * kNlTy) k_nonlinear_rot_levels_bulk(GridDims g, NlBatch b, int tiles_x,
+                                                                            int* err) {
+  IB_GRID_DEP_WAIT();
+  __shared__ double sQy[kNlTy + 2][kNlTx + 1];
+  __shared__ double sQx[kNlTy + 1][kNlTx + 2];
+  __shared__ double sW[kNlTy + 2][kNlTx + 2];
+  __shared__ double sV[kNlTy + 2][kNlTx];
+  __shared__ double sU[kNlTy][kNlTx + 2];
+  __shared__ double sNx[kNlTy + 1][kNlTx];
+  __shared__ double sNy[kNlTy][kNlTx + 1];
+  // staged rows: qy, q0y (kNlTy + 2 rows), qx, q0x (kNlTy + 1), omega (kNlTy + 2)
+  constexpr int kRows = 2 * (kNlTy + 2) + 2 * (kNlTy + 1) + (kNlTy + 2);
+  __shared__ __align__(16) double raw[kRows][kNlPitch];
+  __shared__ int s_off[kRows];
+  __shared__ __align__(8) unsigned long long mbar;
+  const int l = blockIdx.y;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int I0 = 2 + tx * kNlTx, J0 = 2 + ty * kNlTy;
+  const double* __restrict__ om = b.om[l];
+  const double* __restrict__ bc = b.bc[l];
+  const double* __restrict__ qx = b.qx[l];
+  const double* __restrict__ q0x = b.q0x[l];
+  const double* __restrict__ qy = b.qy[l];
+  const double* __restrict__ q0y = b.q0y[l];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // staged row k: its field, first element, length and the field's size
+  auto row_of = [&](int k, const double** src, long long* e0, int* len, long long* total) {
+    if (k < 2 * (kNlTy + 2)) {            // qy / q0y rows j = J0-1+r, faces i = I0-1 .. I0+kNlTx-1
+      const int r = k % (kNlTy + 2);
+      *src = k < kNlTy + 2 ? qy : q0y;
+      *e0 = (long long)(J0 - 1 + r - 1) * g.nvx + (I0 - 1 - 1);
+      *len = kNlTx + 1;
+      *total = g.nv;
+      return;
+    }
+    k -= 2 * (kNlTy + 2);
+    if (k < 2 * (kNlTy + 1)) {            // qx / q0x rows j = J0-1+r, faces i = I0-1 .. I0+kNlTx
+      const int r = k % (kNlTy + 1);
+      *src = k < kNlTy + 1 ? qx : q0x;
+      *e0 = (long long)(J0 - 1 + r - 1) * g.nux + (I0 - 1 - 1);
+      *len = kNlTx + 2;
+      *total = g.nu;
+      return;
+    }
+    k -= 2 * (kNlTy + 1);                  // omega rows J = J0-1+r, vertices I = I0-1 .. I0+kNlTx
+    *src = om;
+    *e0 = (long long)(J0 - 1 + k - 2) * g.nsx + (I0 - 1 - 2);
+    *len = kNlTx + 2;
+    *total = g.ns;
+  };
+  // an interior tile: every face and vertex it reads lies inside its field, omega's away from
+  // the ring; and every rounded row copy ends inside its field
+  bool bulk = q0x && q0y && tx >= 1 && ty >= 1 && I0 + kNlTx <= g.m && J0 + kNlTy <= g.n;
+  if (bulk)
+    for (int k = 0; k < kRows; ++k) {
+      const double* src;
+      long long e0, total;
+      int len;
+      row_of(k, &src, &e0, &len, &total);
+      const long long a = e0 & ~1LL;
+      const long long n = ((e0 + len - a) + 1) & ~1LL;
+      if (e0 < 0 || a + n > total || n > kNlPitch || ((unsigned long long)src & 15ull) != 0) bulk = false;
+    }
+  if (bulk) {
+    if (tid == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid < 32) {
+      if (tid == 0) {
+        unsigned total_bytes = 0;
+        for (int k = 0; k < kRows; ++k) {
+          const double* src;
+          long long e0, total;
+          int len;
+          row_of(k, &src, &e0, &len, &total);
+          const long long a = e0 & ~1LL;
+          total_bytes += (unsigned)(8 * (((e0 + len - a) + 1) & ~1LL));
+        }
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&mbar)),
+                     "r"(total_bytes) : "memory");
+      }
+      __syncwarp();
+      for (int k = tid; k < kRows; k += 32) {
+        const double* src;
+        long long e0, total;
+        int len;
+        row_of(k, &src, &e0, &len, &total);
+        const long long a = e0 & ~1LL;
+        const unsigned bytes = (unsigned)(8 * (((e0 + len - a) + 1) & ~1LL));
+        s_off[k] = (int)(e0 - a);
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(&raw[k][0])),
+                     "l"(src + a), "r"(bytes), "r"(smem_u32(&mbar))
+                     : "memory");
+      }
+    }
+    auto wait_bounded = [&]() -> unsigned {
+      unsigned done = 0;
+      for (int it = 0; it < (1 << 22) && !done; ++it)
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done)
+                     : "r"(smem_u32(&mbar)), "r"(0)
+                     : "memory");
+      return done;
+    };
+    const unsigned done = wait_bounded();
+    // every thread takes the same branch: the copies landed, or the CTA records the failure,
+    // waits once more for them and stops (the barrier also orders s_off)
+    if (__syncthreads_or(!done)) {
+      if (tid == 0) atomicExch(err, IB_ERR_CUDA);
+      if (!done) wait_bounded();
+      return;
+    }
+    for (int q = tid; q < (kNlTy + 2) * (kNlTx + 1); q += nt) {
+      const int r = q / (kNlTx + 1), c = q - r * (kNlTx + 1);
+      sQy[r][c] = raw[r][c + s_off[r]] + raw[kNlTy + 2 + r][c + s_off[kNlTy + 2 + r]];
+    }
+    const int bx = 2 * (kNlTy + 2), bw = bx + 2 * (kNlTy + 1);
+    for (int q = tid; q < (kNlTy + 1) * (kNlTx + 2); q += nt) {
+      const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+      sQx[r][c] = raw[bx + r][c + s_off[bx + r]] + raw[bx + kNlTy + 1 + r][c + s_off[bx + kNlTy + 1 + r]];
+    }
+    for (int q = tid; q < (kNlTy + 2) * (kNlTx + 2); q += nt) {
+      const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+      sW[r][c] = raw[bw + r][c + s_off[bw + r]];
+    }
+  } else {
+    for (int q = tid; q < (kNlTy + 2) * (kNlTx + 1); q += nt) {
+      const int r = q / (kNlTx + 1), c = q - r * (kNlTx + 1);
+      const int i = I0 - 1 + c, j = J0 - 1 + r;
+      double v = 0.0;
+      if (i >= 1 && i <= g.m && j >= 1 && j <= g.n + 1) {
+        const int idx = (j - 1) * g.nvx + (i - 1);
+        v = qy[idx] + (q0y ? q0y[idx] : 0.0);
+      }
+      sQy[r][c] = v;
+    }
+    for (int q = tid; q < (kNlTy + 1) * (kNlTx + 2); q += nt) {
+      const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+      const int i = I0 - 1 + c, j = J0 - 1 + r;
+      double v = 0.0;
+      if (i >= 1 && i <= g.m + 1 && j >= 1 && j <= g.n) {
+        const int idx = (j - 1) * g.nux + (i - 1);
+        v = qx[idx] + (q0x ? q0x[idx] : 0.0);
+      }
+      sQx[r][c] = v;
+    }
+    for (int q = tid; q < (kNlTy + 2) * (kNlTx + 2); q += nt) {
+      const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+      const int i = I0 - 1 + c, j = J0 - 1 + r;
+      sW[r][c] = (i >= 1 && i <= g.m + 1 && j >= 1 && j <= g.n + 1) ? ghost_vertex(om, bc, g, i, j) : 0.0;
+    }
+  }
+  __syncthreads();
+  for (int q = tid; q < (kNlTy + 2) * kNlTx; q += nt) {
+    const int r = q / kNlTx, c = q - r * kNlTx;
+    sV[r][c] = 0.5 * (sQy[r][c + 1] + sQy[r][c]);
+  }
+  for (int q = tid; q < kNlTy * (kNlTx + 2); q += nt) {
+    const int r = q / (kNlTx + 2), c = q - r * (kNlTx + 2);
+    sU[r][c] = 0.5 * (sQx[r + 1][c] + sQx[r][c]);
+  }
+  __syncthreads();
+  for (int q = tid; q < (kNlTy + 1) * kNlTx; q += nt) {
+    const int r = q / kNlTx, c = q - r * kNlTx;
+    const double v1 = sV[r + 1][c], v0 = sV[r][c], w1 = sW[r + 1][c + 1], w0 = sW[r][c + 1];
+    sNx[r][c] = 0.5 * (v1 * w1 + v0 * w0);
+  }
+  for (int q = tid; q < kNlTy * (kNlTx + 1); q += nt) {
+    const int r = q / (kNlTx + 1), c = q - r * (kNlTx + 1);
+    const double u1 = sU[r][c + 1], u0 = sU[r][c], w1 = sW[r + 1][c + 1], w0 = sW[r + 1][c];
+    sNy[r][c] = -0.5 * (u1 * w1 + u0 * w0);
+  }
+  __syncthreads();
+  const int cx = tid % kNlTx, cy = tid / kNlTx;
+  const int I = I0 + cx, J = J0 + cy;
+  if (cy < kNlTy && I <= g.m && J <= g.n) {
+    const double a = sNy[cy][cx + 1], bb = sNy[cy][cx], c = sNx[cy + 1][cx], d = sNx[cy][cx];
+    b.out[l][(size_t)(J - 2) * g.nsx + (I - 2)] = a - bb - c + d;
+  }
+}
+
 // ----------------------------------------------------------------- curl
 // curl_int + curl_bc (operators_fluid.F90:423-471), s ghosts from the ring.
 __global__ void k_curl(GridDims g, const double* __restrict__ s, const double* __restrict__ sbc,
@@ -342,6 +539,13 @@ int launch_nonlinear_rot_levels(const GridDims& g, const NlBatch& b, int nlev, c
   const int tiles_x = cdiv(g.nsx, kNlTx), tiles_y = cdiv(g.nsy, kNlTy);
   count_launch();
   k_nonlinear_rot_levels<<<dim3(tiles_x * tiles_y, nlev), kNlTx * kNlTy, 0, st>>>(g, b, tiles_x);
+  return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
+}
+int launch_nonlinear_rot_levels_bulk(const GridDims& g, const NlBatch& b, int nlev, int* err, cudaStream_t st) {
+  if (nlev < 1 || nlev > kMaxLevels) return IB_ERR_ARG;
+  const int tiles_x = cdiv(g.nsx, kNlTx), tiles_y = cdiv(g.nsy, kNlTy);
+  count_launch();
+  k_nonlinear_rot_levels_bulk<<<dim3(tiles_x * tiles_y, nlev), kNlTx * kNlTy, 0, st>>>(g, b, tiles_x, err);
   return cudaGetLastError() == cudaSuccess ? IB_OK : IB_ERR_CUDA;
 }
 int launch_rot(const GridDims& g, const double* hx, const double* hy, double* vort, cudaStream_t st) {

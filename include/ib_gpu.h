@@ -304,7 +304,11 @@ int ib_get_stream(IbCtx* ctx, void** stream);
  * grid's x transform (n x m cells times the m x m DST-I matrix) on the FP64 tensor cores (2) or
  * with FP64 FMAs (3).  The launches cycle over
  * pairs of temporary fields (allocated for the call) that together exceed twice the L2 size,
- * so each reads its input from HBM; the context's state is not touched. */
+ * so each reads its input from HBM; the context's state is not touched.  Kinds 4 and 5: the
+ * predictor's fused nonlinear + rot stencil of every level on the context's current fields
+ * (operators_fluid.F90:553-587, 203-233), with plain loads (4) or with its tiles' rows staged by
+ * bulk copies (5; IB_ERR_STATE if its output differs from kind 4's in any bit), each launch
+ * after a write of twice the L2 size. */
 int ib_time_pass(IbCtx* ctx, int kind, int reps, double* avg_ms);
 /* device time (ms, summed over reps back-to-back applications) of the 8 stages of the Schur
  * operator: reg+rot, ainv, coarsify, coarse levels, finest forward, finest solve, finest

@@ -4,6 +4,7 @@ import pytest
 
 import ib_oracle as O
 from helpers import PLATE, SMALL, pair, rel, small_cylinder, small_plate
+from ib_parallel_gb300 import ibgpu as G
 
 pytestmark = pytest.mark.gpu
 
@@ -141,3 +142,15 @@ def test_plate_struct_rhs_dx():
         assert rel(g.struct_rhs(), o.compute_rhs()) < 1e-13
     g.close()
 
+
+
+def test_bulk_copy_stencil_gives_the_plain_loads_bits():
+    # the predictor's nonlinear + rot stencil with its interior tiles' rows staged by bulk copies
+    # (cp.async.bulk on an mbarrier): ib_time_pass kind 5 compares its output with kind 4's bit
+    # for bit on the context's fields (256 x 128 cells: 8 x 16 tiles a level, most interior)
+    g = G.Simulation(G.Params(**dict(SMALL, m=256, n=128)), [small_cylinder()])
+    for _ in range(3):
+        g.advance()
+    assert g.time_pass(5, 2) > 0.0
+    assert g.time_pass(4, 2) > 0.0
+    g.close()
