@@ -434,8 +434,19 @@ __global__ void __launch_bounds__(128) k_sd_ptf(int nf, int nf_sd, const int* __
       sprod[e] = __dmul_rn(pw[e0 + e], f[(e0 + e) >> 2]);
     }
     __syncthreads();
-    for (int e = 0; e < ne; ++e)
-      if (sidx[e] == a) acc = __dadd_rn(acc, sprod[e]);
+    // the entries of this unknown first (integer work), then their sum in order, so that the
+    // FP64 adds are issued for the few entries that match only
+    int hit[8];
+    int nh = 0;
+    for (int e = 0; e < ne; ++e) {
+      if (sidx[e] != a) continue;
+      if (nh == 8) {   // more than eight: add the ones held, keep collecting
+        for (int h = 0; h < 8; ++h) acc = __dadd_rn(acc, sprod[hit[h]]);
+        nh = 0;
+      }
+      hit[nh++] = e;
+    }
+    for (int h = 0; h < nh; ++h) acc = __dadd_rn(acc, sprod[hit[h]]);
   }
   if (a < nf_sd) fsd[a] = acc;
 }
