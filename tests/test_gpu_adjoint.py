@@ -283,3 +283,38 @@ def test_subdomain_gradient_matches_central_differences(tmp_path):
         cm = coefs.copy(); cm[n, i] -= h
         fd = (J(cp) - J(cm)) / (2 * h)
         assert abs(grad[n, i] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(grad).max()), (n, i, grad[n, i], fd)
+
+
+def test_subdomain_gradient_at_the_pitching_airfoil_size(tmp_path):
+    # the 600x300x4 NACA 0012 in its pitching frame through the sub-domain method (a 56 x 11 cloud
+    # at two grid spacings around the chord), GMRES on lumat to 1e-13, 3 steps against the oracle
+    import dataclasses
+    import ib_subdomain as SD
+    from ib_parallel_gb300 import autodiff as AD
+    from ib_parallel_gb300 import geometry as GEO
+    p, bodies = GEO.config_pitching_600x300()
+    p = dataclasses.replace(p, autotune=False, num_stat=False, rtol=1e-13, atol=1e-15)
+    cloud = (-0.05, 1.05, -0.1, 0.1, 0.02)
+    g = G.Simulation(p, bodies)
+    g.subdomain_setup(*cloud)
+    g.subdomain_precompute()
+    path = tmp_path / "sd_airfoil.chd"
+    g.write_subdomain_matrix(path)
+    g.close()
+    N = 3
+    frames = AD.pitching_frames(N, p.dt, 0.1745, 0.2, 0.0).numpy()
+    W = np.random.default_rng(13).standard_normal((N, 1, 2))
+    g = G.Simulation(p, bodies)
+    g.subdomain_setup(*cloud)
+    g.read_subdomain_matrix(path)
+    Fg = g.adjoint_forward(frames, K=2)
+    gg = g.adjoint_backward(W)
+    po = O.Params(**{k: getattr(p, k) for k in O.Params.__dataclass_fields__ if hasattr(p, k)})
+    o = O.IBOracle(po, [O.Body(x=bodies[0].x.copy(), y=bodies[0].y.copy(), fam=1)])
+    o.sd = SD.SubDomain(o, True, *cloud)
+    o.sd.read_chd(path)
+    ad = A.Adjoint(o)
+    Fo = ad.forward(frames)
+    go = ad.backward(W)
+    assert np.abs(Fg - Fo).max() < 1e-10 * np.abs(Fo).max()
+    assert np.abs(gg - go).max() < 1e-8 * np.abs(go).max(), np.abs(gg - go).max() / np.abs(go).max()
