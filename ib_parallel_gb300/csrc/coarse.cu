@@ -385,12 +385,18 @@ int cr_prepare(Ctx* c, const std::vector<unsigned char>& fine_mask) {
     all.insert(all.end(), fresh[k].begin(), fresh[k].end());
   }
   IB_CUDA_CHECK(cudaMemcpy(cr.items, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice));
-  RC(inf_build_scratch(c));
-  for (int k = L - 1; k >= 1; --k)
-    if (!fresh[k].empty()) RC(run_level(c, k, cr.items + off[k], (int)fresh[k].size()));
+  // the slots above now claim responses: if the passes fail, the context stops using them (its
+  // later builds run the per-column chain)
+  int rc = inf_build_scratch(c);
+  for (int k = L - 1; k >= 1 && rc == IB_OK; --k)
+    if (!fresh[k].empty()) rc = run_level(c, k, cr.items + off[k], (int)fresh[k].size());
   int err = 0;
-  IB_CUDA_CHECK(cudaMemcpy(&err, cr.err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (err) return IB_ERR_STATE;
+  if (rc == IB_OK && cudaMemcpy(&err, cr.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) rc = IB_ERR_CUDA;
+  if (rc == IB_OK && err) rc = IB_ERR_STATE;
+  if (rc != IB_OK) {
+    cr.enabled = false;
+    return rc;
+  }
   cr.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return IB_OK;
 }

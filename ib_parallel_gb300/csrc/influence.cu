@@ -616,9 +616,8 @@ int inf_build(Ctx* c) {
         if (a < g.nsx && b < g.nsy) mask[(size_t)b * g.nsx + a] = 1;
       }
     cr_dilate(g, mask, I.trunc_rows);
-    const int rcc = cr_prepare(c, mask);
-    if (rcc != IB_OK && rcc != IB_ERR_NOMEM) return rcc;
-    use_cr = rcc == IB_OK;
+    use_cr = cr_prepare(c, mask) == IB_OK;   // else each column runs the coarse chain itself
+    cudaGetLastError();
   }
   for (SchurScratch& sc : I.bscr) {
     sc.cr_R1 = use_cr ? I.cr.R[1] : nullptr;

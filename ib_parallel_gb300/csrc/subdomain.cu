@@ -659,9 +659,8 @@ int sd_precompute(Ctx* c) {
         for (int a = std::max(0, ixh[u] - 5); a <= std::min(g.nsx - 1, ixh[u] + 2); ++a)
           mask[(size_t)b * g.nsx + a] = 1;
     cr_dilate(g, mask, I.trunc_rows);
-    const int rcc = cr_prepare(c, mask);
-    if (rcc != IB_OK && rcc != IB_ERR_NOMEM) return rcc;
-    use_cr = rcc == IB_OK;
+    use_cr = cr_prepare(c, mask) == IB_OK;   // else each column runs the coarse chain itself
+    cudaGetLastError();
   }
   for (SchurScratch& sc : I.bscr) {
     sc.cr_R1 = use_cr ? I.cr.R[1] : nullptr;

@@ -112,8 +112,10 @@ int ib_advance(IbCtx* ctx, int* itime);
  * (host memory), the centre of rotation staying motion[3], motion[4] of ib_create.  Replaces the
  * reference's motion_potential + motion_rotation (variables.F90:299-360), which form the frame
  * fluxes q0 from motion_grid (user.F90:13-31); here they are formed on the device, stream-ordered
- * after the steps already launched (IB_ERR_STATE while a step of ib_advance_begin is open).  With
- * the motion given at ib_create the fluxes are those of creation bit for bit. */
+ * after the steps already launched (IB_ERR_STATE if a step is still in progress).  With
+ * the motion given at ib_create the fluxes are those of creation bit for bit.  ib_write_variables
+ * then records this motion, and the frame's angle as the reference integrates it (angular
+ * velocity times time, exact for a constant one). */
 int ib_set_frame(IbCtx* ctx, const double* uvw);
 
 /* state access (the arrays of variables.F90:10-33) */
