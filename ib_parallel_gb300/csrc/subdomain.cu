@@ -346,26 +346,27 @@ __device__ __forceinline__ double b_at(const long long* __restrict__ colptr, con
 
 // compute_operator (operators_struct.F90:840-905): lumat(k, l) = body(k, l) + sum_q P(k,q)
 // inter(l, a_q(k)), inter(l, a) = sum_r B(b_r(l), a) P(l, r), each dot product in order; written
-// into the solver's column-major operator St[l][k].  body: b_times2's matrix (body_mat).  Sixteen
-// lanes per entry, lane 4q + r finding B(b_r(l), a_q(k)) by its own binary search (the searches
-// are the latency); the group's first lane sums the products in the order above.
-__global__ void __launch_bounds__(128) k_sd_lumat(int nf, const int* __restrict__ pidx, const double* __restrict__ pw,
+// into the solver's column-major operator St[l][k].  body: b_times2's matrix (body_mat).  A CTA
+// takes 32 entries l of column k: its threads find the 16 B entries of each (binary searches in
+// the columns, the latency) and their products, then one warp sums each entry in the order above.
+constexpr int kLumatRows = 32;
+__global__ void __launch_bounds__(256) k_sd_lumat(int nf, const int* __restrict__ pidx, const double* __restrict__ pw,
                                                   const long long* __restrict__ colptr, const int* __restrict__ nz,
                                                   const int* __restrict__ rows, const double* __restrict__ vals,
                                                   const double* __restrict__ brv, const double* __restrict__ bco,
                                                   const int* __restrict__ bod, double* __restrict__ St) {
   IB_GRID_DEP_WAIT();
-  const int lane = threadIdx.x & 31;
-  const int sub = lane & 15, q = sub >> 2, r = sub & 3;
-  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;   // 8 entries of column k a CTA
-  const int k = blockIdx.y;
-  const bool live = l < nf;
-  double prod = 0.0;
-  if (live) prod = __dmul_rn(b_at(colptr, nz, rows, vals, pidx[4 * l + r], pidx[4 * k + q]), pw[4 * l + r]);
-  double v[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __shfl_sync(0xffffffffu, prod, (lane & 16) + i);
-  if (!live || sub != 0) return;
+  __shared__ double prod[kLumatRows][17];
+  const int k = blockIdx.y, l0 = blockIdx.x * kLumatRows;
+  for (int t = threadIdx.x; t < kLumatRows * 16; t += blockDim.x) {
+    const int e = t >> 4, sub = t & 15, q = sub >> 2, r = sub & 3, l = l0 + e;
+    if (l < nf)
+      prod[e][sub] = __dmul_rn(b_at(colptr, nz, rows, vals, pidx[4 * l + r], pidx[4 * k + q]), pw[4 * l + r]);
+  }
+  __syncthreads();
+  const int l = l0 + (int)threadIdx.x;
+  if (threadIdx.x >= kLumatRows || l >= nf) return;
+  const double* v = prod[threadIdx.x];
   double dot = 0.0;
 #pragma unroll
   for (int qq = 0; qq < 4; ++qq) {
@@ -834,8 +835,8 @@ int launch_sd_lumat(Ctx* c, cudaStream_t st) {
   SubDomain& S = c->sd;
   Influence& I = c->inf;
   count_launch();
-  k_sd_lumat<<<dim3(cdiv(c->nf, 8), c->nf), 128, 0, st>>>(c->nf, S.pidx, S.pw, S.colptr, S.nz, S.rows, S.vals,
-                                                           I.brv, I.bco, I.bod, I.St);
+  k_sd_lumat<<<dim3(cdiv(c->nf, kLumatRows), c->nf), 256, 0, st>>>(c->nf, S.pidx, S.pw, S.colptr, S.nz, S.rows,
+                                                                   S.vals, I.brv, I.bco, I.bod, I.St);
   IB_CUDA_CHECK(cudaGetLastError());
   return launch_beam_add_b(c, I.St, st);
 }
