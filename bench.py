@@ -322,10 +322,12 @@ def _long_run(p, bodies, steps):
     sim.synchronize()
     T = time.perf_counter() - t0
     st = sim.influence_stats()
+    cr = sim.coarse_stats()
     th = sim.body_state()[0]
     sim.close()
     return {"value": steps / T, "unit": "steps/s", "steps": steps, "seconds": T,
             "band_builds": st["builds"], "band_build_ms": st["build_ms"], "fallbacks": st["fallbacks"],
+            "coarse_response_solves": cr["solves"], "coarse_response_ms": cr["ms"],
             "final_theta": [float(x) for x in th],
             "note": "from the impulsive start, host wall clock, every band build inside the region"}
 
@@ -608,7 +610,7 @@ def run_gpu(args, world, rank, local):
                                          "(same bits, checked)"},
         "pressure": _pressure_leg(sim, p),
         "schur_stages_us": sim.profile_schur(20),
-        "influence": sim.influence_stats(),
+        "influence": dict(sim.influence_stats(), coarse_responses=sim.coarse_stats()),
         "step_graph": sim.step_graph_stats(),
         "launch_shapes": sim.launch_shapes(),
         "step_phases_us": _step_phases(sim, 5),
