@@ -842,6 +842,15 @@ int ib_get_coarse_stats(IbCtx* h, long long* counts, double* ms) {
   return IB_OK;
 }
 
+int ib_get_ring_maps(IbCtx* h, long long* counts, double* ms) {
+  CTX_OR_FAIL(h);
+  if (!counts || !ms) return fail(IB_ERR_ARG, "bad argument");
+  counts[0] = c->rmap.on ? 1 : 0;
+  counts[1] = (long long)c->rmap.bytes;
+  *ms = c->rmap.ms;
+  return IB_OK;
+}
+
 int ib_get_step_graph_stats(IbCtx* h, long long* counts) {
   CTX_OR_FAIL(h);
   if (!counts) return fail(IB_ERR_ARG, "bad argument");

@@ -98,6 +98,32 @@ struct CoarseResp {
   size_t bytes = 0;
 };
 
+// The coarse-to-fine recursions of the predictor and of vort2flux with their chain of
+// dependent solves collapsed (ringmap.cu).  Level k's solve depends on level k+1 only through
+// its boundary data, which is linear in a short state of level k+1's modes: the two mode rows
+// get_bc reads (J = n/4+1, 3n/4+1) and the values at the coarse vertices of the ring's left and
+// right sides, as their sum and difference (vS, vA).  Laid out [s0 (N) | s1 (N) | vS | vA]
+// (N = m-1 modes, NQ = n/2+1 vertices a side).  The state of level k's solution is that of its
+// solution with zero boundary data plus G_k times its own boundary state, so the levels' solves
+// with zero boundary data run as one batched launch, the states follow from L-2 dense products
+// on the coarse-to-fine chain, and the final solves run as a second batched launch.  The DST's
+// mirror symmetry in x splits G_k into two blocks (even modes with vS, odd modes with vA).
+// Built only on request (IB_RING_MAPS=1): the twice-solved levels, the products and the
+// batched boundary data take more FP64 issue than the chain's latency they remove.
+struct RingMaps {
+  bool on = false;
+  int N = 0, NQ = 0, NS = 0;        // modes, coarse vertices a side, state length
+  int nb[2] = {0, 0};               // block sizes: 2 * (modes of that parity) + NQ
+  double* Gp[kMaxLevels] = {};      // the predictor's G_k, k = 1..L-2 (block 0 rows, then block 1)
+  double* Gc = nullptr;             // vort2flux's (one operator and factor on every level)
+  double* Z[kMaxLevels] = {};       // zero-boundary solutions, levels 1..L-2
+  double* Ez[kMaxLevels] = {};      // their states
+  double* R[kMaxLevels] = {};       // level k's boundary state, k = 0..L-2
+  double* mem = nullptr;
+  size_t bytes = 0;
+  double ms = 0.0;                  // host wall time of the precomputation
+};
+
 struct Influence {
   static constexpr int kTile = 8;
   // the band's columns are computed on this many streams at once, each with its own scratch
@@ -284,6 +310,7 @@ struct Ctx {
   bool ub_on = false;
   PressureOp pres;
   SubDomain sd;
+  RingMaps rmap;
   AdjointState adj;
   // family-3 beams (beam.cu)
   int nbeam = 0;
@@ -458,6 +485,13 @@ bool inf_strip_alloc(Ctx* c, int n);
 int inf_strip_table(Ctx* c, int r_lo, int r_hi);
 int launch_cr_ring0(Ctx* c, const SchurScratch& sc, cudaStream_t st);
 void cr_free(Ctx* c);
+// ringmap.cu: the ring maps of a context (IB_RING_MAPS=1 at creation, from 3 levels on; else
+// the per-level chain); rm_predict / rm_vort2flux run the recursions (the arguments as
+// op_predict_levels and op_vort2flux hold them)
+int rm_prepare(Ctx* c);
+void rm_free(Ctx* c);
+int rm_predict(Ctx* c);
+int rm_vort2flux(Ctx* c, double* const* modes, double* F0, bool all_levels, double post0, const double* add0);
 // the finest-level vertices within r of a marked one, in x and in y (the boxes of the sources)
 void cr_dilate(const GridDims& g, std::vector<unsigned char>& mask, int r);
 // rhsf = P E_o (q + q0) + rhsf (P formed first at the current positions unless interp is false)

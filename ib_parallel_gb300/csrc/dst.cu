@@ -526,29 +526,6 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
   }
 }
 
-// sum_k sr[k] wc[k] over k < N on one warp (the lane's partial sums, not yet reduced): four
-// accumulators (k = lane + 32(4t + a)) keep four loads per operand in flight.
-__device__ __forceinline__ double warp_dot_part(const double* __restrict__ sr, const double* __restrict__ wc, int N,
-                                                int lane) {
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-  int k = lane;
-  for (; k + 96 < N; k += 128) {
-    a0 = fma(sr[k], wc[k], a0);
-    a1 = fma(sr[k + 32], wc[k + 32], a1);
-    a2 = fma(sr[k + 64], wc[k + 64], a2);
-    a3 = fma(sr[k + 96], wc[k + 96], a3);
-  }
-  if (k < N) a0 = fma(sr[k], wc[k], a0);
-  if (k + 32 < N) a1 = fma(sr[k + 32], wc[k + 32], a1);
-  if (k + 64 < N) a2 = fma(sr[k + 64], wc[k + 64], a2);
-  return (a0 + a1) + (a2 + a3);
-}
-
-__device__ __forceinline__ double warp_sum(double acc) {
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  return acc;
-}
-
 // Selected points of an inverse x transform, one warp per point.
 __global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, const int2* __restrict__ pts, int npts,
                              const double* __restrict__ W, double* __restrict__ out) {

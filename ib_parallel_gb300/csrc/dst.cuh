@@ -19,6 +19,30 @@ namespace ib {
 constexpr int kMaxRadices = 16;
 constexpr int kMaxBatch = 16;   // levels one batched x pass can carry
 
+// sum_k sr[k] wc[k] over k < N on one warp (the lane's partial sums, not yet reduced): four
+// accumulators (k = lane + 32(4t + a)) keep four loads per operand in flight.  warp_sum then
+// adds the lanes' values (the same butterfly order on every lane).
+__device__ __forceinline__ double warp_dot_part(const double* __restrict__ sr, const double* __restrict__ wc, int N,
+                                                int lane) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int k = lane;
+  for (; k + 96 < N; k += 128) {
+    a0 = fma(sr[k], wc[k], a0);
+    a1 = fma(sr[k + 32], wc[k + 32], a1);
+    a2 = fma(sr[k + 64], wc[k + 64], a2);
+    a3 = fma(sr[k + 96], wc[k + 96], a3);
+  }
+  if (k < N) a0 = fma(sr[k], wc[k], a0);
+  if (k + 32 < N) a1 = fma(sr[k + 32], wc[k + 32], a1);
+  if (k + 64 < N) a2 = fma(sr[k + 64], wc[k + 64], a2);
+  return (a0 + a1) + (a2 + a3);
+}
+
+__device__ __forceinline__ double warp_sum(double acc) {
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
 struct DstPlan {
   int N = 0, M = 0, P = 0;
   int nrad = 0;

@@ -423,6 +423,8 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     rc = tune(c);
     if (rc != IB_OK) { *msg = "DST tuning failed"; ctx_destroy(c); return rc; }
   }
+  rc = rm_prepare(c);
+  if (rc != IB_OK) { *msg = "ring map precomputation failed"; ctx_destroy(c); return rc; }
   if (nf > 0 && inf_alloc(c) != IB_OK) { *msg = "device allocation failed"; ctx_destroy(c); return IB_ERR_NOMEM; }
   {
     const int rcb = beam_build(c, bodies, nbody, msg);
@@ -451,6 +453,7 @@ void ctx_destroy(Ctx* c) {
   pressure_free(c);
   beam_free(c);
   sd_free(c);
+  rm_free(c);
   if (c->frame_lines) cudaFree(c->frame_lines);
   adjoint_free(c);
   if (c->pool.base) cudaFree(c->pool.base);
@@ -599,18 +602,26 @@ int op_vort2flux(Ctx* c, double* const* w, double* const* s, double* const* qx, 
     ProfScope ps(c, 0, pass_bytes(c, L - k0, L - k0));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_COPY, a, g, c->lx_batch, st));
   }
-  for (int k = L - 1; k >= 0; --k) {
-    double* F = k == 0 ? F0 : modes(k);
-    // boundary terms of the ring of level k (get_bc of level k+1), apply_bc with fac 1, added
-    // by the solve as it loads its right-hand side
-    TriBc bc;
-    if (k < L - 1) bc = level_bc(c, k, k == 0 && skip0 ? 2.0 * g.m : 1.0);
-    if (k == 0 && skip0) bc.add2 = hat0_add;
-    {
-      ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-      RC(tri_solve(c->tri_ctci, modes(k), F, g.nsx, c->tl, st, bc));
+  if (c->rmap.on) {
+    // the same recursion with the chain of level solves collapsed (with all_levels false the
+    // coarser levels' final solves are not needed: only their boundary data is)
+    double* mk[kMaxLevels];
+    for (int k = 0; k < L; ++k) mk[k] = modes(k);
+    RC(rm_vort2flux(c, mk, F0, all_levels, skip0 ? 2.0 * g.m : 1.0, skip0 ? hat0_add : nullptr));
+  } else {
+    for (int k = L - 1; k >= 0; --k) {
+      double* F = k == 0 ? F0 : modes(k);
+      // boundary terms of the ring of level k (get_bc of level k+1), apply_bc with fac 1, added
+      // by the solve as it loads its right-hand side
+      TriBc bc;
+      if (k < L - 1) bc = level_bc(c, k, k == 0 && skip0 ? 2.0 * g.m : 1.0);
+      if (k == 0 && skip0) bc.add2 = hat0_add;
+      {
+        ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+        RC(tri_solve(c->tri_ctci, modes(k), F, g.nsx, c->tl, st, bc));
+      }
+      if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 1.0));
     }
-    if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 1.0));
   }
   if (!all_levels) {
     DstXArgs a;
@@ -1429,17 +1440,21 @@ static int op_predict_levels(Ctx* c, bool seed_rhs_old) {
     ProfScope ps(c, 0, pass_bytes(c, 4 * L, L));
     RC(dst_pass_x(c->px, g.nsy, g.nsx, PRE_PRED, a, g, c->lx_batch, st));
   }
-  for (int k = L - 1; k >= 0; --k) {
-    double* F = c->hat[k];
-    // the second ring: ringv[k] = vfac[k] * 0.25 get_bc(omega_{k+1}), left by level k+1 with
-    // its boundary terms, added by the solve
-    TriBc bc;
-    if (k < L - 1) bc = level_bc(c, k, 1.0);
-    {
-      ProfScope ps(c, 1, pass_bytes(c, 1, 1));
-      RC(tri_solve(c->tri_pred[k], F, F, g.nsx, c->tl, st, bc));
+  if (c->rmap.on) {
+    RC(rm_predict(c));   // the same recursion with the chain of level solves collapsed
+  } else {
+    for (int k = L - 1; k >= 0; --k) {
+      double* F = c->hat[k];
+      // the second ring: ringv[k] = vfac[k] * 0.25 get_bc(omega_{k+1}), left by level k+1 with
+      // its boundary terms, added by the solve
+      TriBc bc;
+      if (k < L - 1) bc = level_bc(c, k, 1.0);
+      {
+        ProfScope ps(c, 1, pass_bytes(c, 1, 1));
+        RC(tri_solve(c->tri_pred[k], F, F, g.nsx, c->tl, st, bc));
+      }
+      if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 0.25 * c->vfac[k - 1]));
     }
-    if (k > 0) RC(ring_edge_from_modes(c, F, k - 1, 0.25 * c->vfac[k - 1]));
   }
   // every row of every level back: coarsify rewrites only the centre columns of a coarser
   // level's centre rows, the rest of those rows (the coarse grid beside the finer one) is the

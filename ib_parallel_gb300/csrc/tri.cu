@@ -240,10 +240,8 @@ __global__ void k_tri(TriOp op, const double* __restrict__ F, double* U, int ld,
 // writes only the rows it read, after the CTA's barriers.
 constexpr int kTriMaxM = 31;   // interfaces (C-1) the register prefetch holds
 template <int S>
-__global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb,
-                                                 TriBc bc) {
-  IB_GRID_DEP_WAIT();
-  extern __shared__ double sm[];
+__device__ __forceinline__ void tri_reg_body(const TriOp& op, const double* __restrict__ F, double* U, int ld, int Mb,
+                                             const TriBc& bc, double* sm) {
   const int C = op.C, d = S + 1, nx = op.nx;
   const int m = C > 1 ? C - 1 : 1;
   double* t_inv = sm;                      // S x Mb
@@ -353,6 +351,24 @@ __global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restr
   }
 }
 
+template <int S>
+__global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb,
+                                                 TriBc bc) {
+  IB_GRID_DEP_WAIT();
+  extern __shared__ double sm[];
+  tri_reg_body<S>(op, F, U, ld, Mb, bc, sm);
+}
+
+// The same solve for every item of a batch, blockIdx.y picking the item (its tables, input,
+// output and boundary terms); the items share the chunking.
+template <int S>
+__global__ void __launch_bounds__(256) k_tri_reg_batch(const __grid_constant__ TriBatch b, int ld, int Mb) {
+  IB_GRID_DEP_WAIT();
+  extern __shared__ double sm[];
+  const int y = blockIdx.y;
+  tri_reg_body<S>(b.op[y], b.F[y], b.U[y], ld, Mb, b.bc[y], sm);
+}
+
 static size_t tri_reg_smem(const TriOp& op, int Mb) {
   return sizeof(double) * (size_t)Mb * (3 * (size_t)op.s + 2 * (size_t)op.C + 2 * ((size_t)op.C + 1));
 }
@@ -399,6 +415,44 @@ int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaun
   k_tri<<<cdiv(op.nx, Mb), threads, smem, st>>>(op, F, U, ld, Mb, bc);
   IB_CUDA_CHECK(cudaGetLastError());
   return IB_OK;
+}
+
+template <int S>
+static int launch_tri_reg_batch(const TriBatch& b, int ld, int Mb, int threads, cudaStream_t st) {
+  const size_t smem = tri_reg_smem(b.op[0], Mb);
+  if (allow_dyn_smem(k_tri_reg_batch<S>, smem) != cudaSuccess) return IB_ERR_CUDA;
+  count_launch();
+  k_tri_reg_batch<S><<<dim3(cdiv(b.op[0].nx, Mb), b.n), threads, smem, st>>>(b, ld, Mb);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
+}
+
+bool tri_batch_supported(const TriOp& op) {
+  if (op.C - 1 > kTriMaxM || op.C > 256) return false;
+  switch (op.s) {
+    case 1: case 2: case 3: case 4: case 5: case 6: case 7: case 8: case 9: case 11: case 12: case 14:
+    case 15: case 19: case 23: case 24: case 29: case 31: case 39: return true;
+    default: return false;
+  }
+}
+
+int tri_solve_batch(const TriBatch& b, int ld, const TriLaunch& L, cudaStream_t st) {
+  if (b.n < 1 || b.n > kTriBatch) return IB_ERR_ARG;
+  const TriOp& o = b.op[0];
+  if (!tri_batch_supported(o)) return IB_ERR_ARG;
+  for (int i = 1; i < b.n; ++i)
+    if (b.op[i].nx != o.nx || b.op[i].ny != o.ny || b.op[i].s != o.s || b.op[i].C != o.C) return IB_ERR_ARG;
+  const int Mr = std::max(1, std::min(L.Mb, 256 / o.C));
+  const int tr = ((Mr * o.C + 31) / 32) * 32;
+  switch (o.s) {
+#define IB_TRI_REG(SS) \
+    case SS: return launch_tri_reg_batch<SS>(b, ld, Mr, tr, st);
+    IB_TRI_REG(1) IB_TRI_REG(2) IB_TRI_REG(3) IB_TRI_REG(4) IB_TRI_REG(5) IB_TRI_REG(6) IB_TRI_REG(7)
+    IB_TRI_REG(8) IB_TRI_REG(9) IB_TRI_REG(11) IB_TRI_REG(12) IB_TRI_REG(14) IB_TRI_REG(15) IB_TRI_REG(19)
+    IB_TRI_REG(23) IB_TRI_REG(24) IB_TRI_REG(29) IB_TRI_REG(31) IB_TRI_REG(39)
+#undef IB_TRI_REG
+    default: return IB_ERR_ARG;
+  }
 }
 
 }  // namespace ib

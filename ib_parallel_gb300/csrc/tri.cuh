@@ -62,4 +62,18 @@ int tri_solve(const TriOp& op, const double* F, double* U, int ld, const TriLaun
               const TriBc& bc = TriBc());
 size_t tri_smem(const TriOp& op, int Mb);
 
+// Up to kTriBatch independent solves in one launch (levels of a recursion with their own
+// tables, or columns of a precomputed response), each with the arithmetic of tri_solve's
+// register-resident kernel.  The items must share nx, ny and the chunking.
+constexpr int kTriBatch = 16;
+struct TriBatch {
+  int n = 0;
+  TriOp op[kTriBatch];
+  const double* F[kTriBatch] = {};
+  double* U[kTriBatch] = {};
+  TriBc bc[kTriBatch];
+};
+bool tri_batch_supported(const TriOp& op);
+int tri_solve_batch(const TriBatch& b, int ld, const TriLaunch& L, cudaStream_t st);
+
 }  // namespace ib

@@ -43,7 +43,7 @@ EXPORTS = [
     "ib_write_variables", "ib_read_variables", "ib_read_namelist", "ib_read_body", "ib_count_bodies",
     "ib_batch_create", "ib_batch_destroy", "ib_batch_size", "ib_batch_context", "ib_batch_advance",
     "ib_calculate_pressure", "ib_write_pressure", "ib_get_beam_state", "ib_get_step_graph_stats",
-    "ib_get_coarse_stats", "ib_set_frame",
+    "ib_get_coarse_stats", "ib_get_ring_maps", "ib_set_frame",
     "ib_subdomain_setup", "ib_subdomain_precompute", "ib_write_subdomain_matrix", "ib_read_subdomain_matrix",
     "ib_subdomain_operator", "ib_get_subdomain_stats", "ib_adjoint_forward", "ib_adjoint_backward",
 ]
@@ -138,6 +138,7 @@ def load(path: Optional[os.PathLike] = None):
         "ib_get_beam_state": ([P, P, P, P], C.c_int),
         "ib_get_step_graph_stats": ([P, C.POINTER(C.c_longlong)], C.c_int),
         "ib_get_coarse_stats": ([P, C.POINTER(C.c_longlong), C.POINTER(C.c_double)], C.c_int),
+        "ib_get_ring_maps": ([P, C.POINTER(C.c_longlong), C.POINTER(C.c_double)], C.c_int),
         "ib_set_frame": ([P, P], C.c_int),
         "ib_subdomain_setup": ([P, C.c_int] + [C.c_double] * 5, C.c_int),
         "ib_subdomain_precompute": ([P], C.c_int),
@@ -497,6 +498,14 @@ class Simulation:
         _check(self.lib.ib_get_coarse_stats(self.h, counts, C.byref(ms)), "ib_get_coarse_stats")
         return {"solves": counts[0], "held": counts[1], "bytes": counts[2], "enabled": bool(counts[3]),
                 "ms": ms.value}
+
+    def ring_maps(self) -> dict:
+        """The ring maps of the predictor's and vort2flux's coarse-to-fine recursions: whether in
+        use, their bytes, host milliseconds of their precomputation."""
+        counts = (C.c_longlong * 2)()
+        ms = C.c_double()
+        _check(self.lib.ib_get_ring_maps(self.h, counts, C.byref(ms)), "ib_get_ring_maps")
+        return {"on": bool(counts[0]), "bytes": counts[1], "ms": ms.value}
 
     def profile(self, enable: bool):
         _check(self.lib.ib_profile(self.h, int(bool(enable))), "ib_profile")

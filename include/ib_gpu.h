@@ -344,6 +344,15 @@ int ib_get_influence_stats(IbCtx* ctx, long long* counts, double* build_ms);
  * held, bytes they take, 1 when enabled}, ms = host wall time of the passes that computed them.
  * The environment variable IB_COARSE_RESP=0 at ib_create runs the coarse chain per column. */
 int ib_get_coarse_stats(IbCtx* ctx, long long* counts, double* ms);
+/* The ring maps behind the coarse-to-fine recursions of the predictor and of vort2flux (no
+ * reference counterpart: fluid_predictor's and vort2flux's level loops, timestepper.F90:103-236
+ * and operators_fluid.F90:237-377, solve the levels one after another; here the levels with zero
+ * boundary data are solved together, the boundary data follow from dense products precomputed at
+ * ib_create, and the final solves again run together).  counts[2] = {1 when in use, bytes the
+ * maps take}, ms = host wall time of their precomputation.  Used only when the environment
+ * variable IB_RING_MAPS=1 at ib_create (from 3 levels on): at 800 x 400 x 5 they take more time
+ * than the level-by-level chain they replace, which runs otherwise. */
+int ib_get_ring_maps(IbCtx* ctx, long long* counts, double* ms);
 /* How the steps since creation ran (no reference counterpart: the reference's advance,
  * timestepper.F90:18-556, is one host routine).  counts[3] = {steps launched as one CUDA graph
  * (predictor, first vort2flux, forces, correction: from the second step on, when the FSI
