@@ -255,20 +255,36 @@ def _algorithmic_bytes(m, n, L, nf):
     return fixed, matvec
 
 
+class _NoGC:
+    """Python's cyclic garbage collector held off inside a timed region (a collection there
+    would stall the host between two steps, and each step waits on the host once)."""
+
+    def __enter__(self):
+        import gc
+        self.was = gc.isenabled()
+        gc.disable()
+
+    def __exit__(self, *a):
+        import gc
+        if self.was:
+            gc.enable()
+
+
 def _timed_steps(sim, stream, steps):
     """K steps of sim timed with CUDA events on its stream; returns (seconds, ksp, fsi sums)."""
     import torch
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     ksp_sum = fsi_sum = 0
-    e0.record(stream)
-    for _ in range(steps):
-        sim.advance()
-        k, f = sim.counters()
-        ksp_sum += k
-        fsi_sum += f
-    e1.record(stream)
-    e1.synchronize()
+    with _NoGC():
+        e0.record(stream)
+        for _ in range(steps):
+            sim.advance()
+            k, f = sim.counters()
+            ksp_sum += k
+            fsi_sum += f
+        e1.record(stream)
+        e1.synchronize()
     return e0.elapsed_time(e1) / 1e3, ksp_sum, fsi_sum
 
 
@@ -292,20 +308,21 @@ def _e2e_steps(sim, stream, steps, fields=False):
     torch.cuda.synchronize()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    for _ in range(steps):
-        if fields:
-            for k in range(L):
-                sim.set_field("q0x", k, q0x[k])
-                sim.set_field("q0y", k, q0y[k])
-        else:
-            G._check(sim.lib.ib_set_frame(sim.h, G.C.c_void_p(frame.data_ptr())), "ib_set_frame")
-        sim.advance()
-        G._check(sim.lib.ib_get_forces(sim.h, G.C.c_void_p(cx.data_ptr()), G.C.c_void_p(cy.data_ptr())))
-        if sim.ntors:
-            G._check(sim.lib.ib_get_body_state(sim.h, G.C.c_void_p(th.data_ptr()), None, None))
-    f1.record(stream)
-    f1.synchronize()
+    with _NoGC():
+        f0.record(stream)
+        for _ in range(steps):
+            if fields:
+                for k in range(L):
+                    sim.set_field("q0x", k, q0x[k])
+                    sim.set_field("q0y", k, q0y[k])
+            else:
+                G._check(sim.lib.ib_set_frame(sim.h, G.C.c_void_p(frame.data_ptr())), "ib_set_frame")
+            sim.advance()
+            G._check(sim.lib.ib_get_forces(sim.h, G.C.c_void_p(cx.data_ptr()), G.C.c_void_p(cy.data_ptr())))
+            if sim.ntors:
+                G._check(sim.lib.ib_get_body_state(sim.h, G.C.c_void_p(th.data_ptr()), None, None))
+        f1.record(stream)
+        f1.synchronize()
     return f0.elapsed_time(f1) / 1e3, h2d, d2h
 
 

@@ -281,7 +281,7 @@ struct Ctx {
   double* v2f_f0 = nullptr;        // the finest level's solved modes of that call
   // per level: the boundary terms its solve adds (TriBc: ring end sums, edge-row transforms)
   std::vector<double*> sdv, edgev;
-  double* emat = nullptr;          // edge matrix (dst_edge_matrix), (m-1) x (m-1)
+  double* emat = nullptr;          // edge matrix (dst_edge_matrix), its equal-parity entries: (m-1) x m/2
   // row treatments of the Schur operator's partial transforms (per vertex row)
   unsigned char *rm_top = nullptr, *rm_coarse = nullptr, *rm_fine = nullptr, *rm_ring2 = nullptr;
   double* wmat = nullptr;          // DST-I matrix of the x transform ((m-1) x (m-1))

@@ -606,45 +606,41 @@ int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec
 //    entries r+1 (closed form 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) of every row's two end values);
 //  - edge[k] and edge[N + k]: the x transform of the ring's bottom and top entries 1..m-1,
 //    which is fac E s_J, E the edge matrix and s_J the coarse modes of the row get_bc reads.
-// Every warp forms FP64 dot products of length N, so the work is spread over many CTAs of
-// kReWarps warps (an FP64 warp instruction holds its SM sub-partition's pipe for the same time
-// whatever its lanes, so a CTA's warps share four pipes): CTAs [0, nlr) take kReLrSeg entries of
-// both the left and the right side (kReLrSeg/2 + 1 coarse vertices each); [nlr, nlr + 2 nbt)
-// kReTbSeg entries of the bottom or top side; then one warp per mode k for the two edge dot
-// products.
+// The points get_bc reads come in mirror pairs about the centre column (the left and right
+// sides; a bottom or top vertex and its mirror), and each pair is one warp's dot product
+// (warp_sum_mirror); E keeps only its entries of equal parity.  CTAs of kReWarps warps:
+// [0, nlr) take kReSeg entries of both the left and the right side (kReWarps vertex pairs);
+// [nlr, nlr + 2 nbt) kReSeg entries of the left half of the bottom or top side and their
+// mirrors; then one warp per mode k for the two edge dot products.
 constexpr int kReWarps = 8;
-constexpr int kReLrSeg = kReWarps - 2;          // 2 (kReLrSeg/2 + 1) = kReWarps
-constexpr int kReTbSeg = 2 * (kReWarps - 1);    // kReTbSeg/2 + 1 = kReWarps
+constexpr int kReSeg = 2 * (kReWarps - 1);   // entries a CTA writes on a side (kReWarps vertices)
 __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, const double* __restrict__ spec,
                                                              int ld, const double* __restrict__ W,
-                                                             const double* __restrict__ E, double fac,
+                                                             const double* __restrict__ Ec, double fac,
                                                              double* __restrict__ ring, double* __restrict__ sd,
                                                              double* __restrict__ edge, int nlr, int nbt) {
   IB_GRID_DEP_WAIT();
-  __shared__ double sp[kReWarps];
+  __shared__ double sp[kReWarps], spm[kReWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int b = blockIdx.x;
   if (b < nlr) {
-    constexpr int nq = kReLrSeg / 2 + 1;   // coarse vertices per side
+    // vertex q of the left side (row J = n/4+1+q, column m/4+1) and of the right (its mirror)
     const int len = g.n + 1, qmax = (len - 1) / 2;
-    const int q0 = b * (kReLrSeg / 2);
-    const int side = warp < nq ? 0 : 1;
-    const int q = q0 + warp - side * nq;
-    double acc = 0.0;
-    if (q <= qmax) {
-      const int I = side == 0 ? g.m / 4 + 1 : 3 * g.m / 4 + 1;
-      const int J = g.n / 4 + 1 + q;
-      acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
+    const int q0 = b * (kReSeg / 2), q = q0 + warp;
+    double2 v = make_double2(0.0, 0.0);
+    if (q <= qmax)
+      v = warp_sum_mirror(warp_dot_part(spec + (size_t)(g.n / 4 - 1 + q) * ld, W + (size_t)(g.m / 4 - 1) * N, N, lane));
+    if (lane == 0) {
+      sp[warp] = v.x;
+      spm[warp] = v.y;
     }
-    acc = warp_sum(acc);
-    if (lane == 0) sp[warp] = acc;
     __syncthreads();
-    if ((int)threadIdx.x < kReLrSeg) {
-      const int p = b * kReLrSeg + (int)threadIdx.x;
+    if ((int)threadIdx.x < kReSeg) {
+      const int p = b * kReSeg + (int)threadIdx.x;
       if (p < len) {
         const int qq = p / 2 - q0;
         const double vl = (p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq];
-        const double vr = (p & 1) ? 0.5 * (sp[nq + qq] + sp[nq + qq + 1]) : sp[nq + qq];
+        const double vr = (p & 1) ? 0.5 * (spm[qq] + spm[qq + 1]) : spm[qq];
         const double xl = vl * fac, xr = vr * fac;
         ring[g.left + p] = xl;
         ring[g.right + p] = xr;
@@ -659,25 +655,26 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
   }
   b -= nlr;
   if (b < 2 * nbt) {
-    const int side = b / nbt, c = b - side * nbt;
-    const int len = g.m + 1, qmax = (len - 1) / 2;
-    const int q0 = c * (kReTbSeg / 2);
-    const int q = q0 + warp;
-    double acc = 0.0;
-    if (q <= qmax) {
-      const int J = side == 0 ? g.n / 4 + 1 : 3 * g.n / 4 + 1;
-      const int I = g.m / 4 + 1 + q;
-      acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
+    // vertex q <= m/4 of the bottom or top side (column m/4+1+q) and its mirror m/2-q
+    const int side = b / nbt, cc = b - side * nbt;
+    const int J = side == 0 ? g.n / 4 + 1 : 3 * g.n / 4 + 1;
+    const int qc = g.m / 4;   // the centre vertex, its own mirror
+    const int q0 = cc * (kReSeg / 2), q = q0 + warp;
+    double2 v = make_double2(0.0, 0.0);
+    if (q <= qc)
+      v = warp_sum_mirror(warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(g.m / 4 - 1 + q) * N, N, lane));
+    if (lane == 0) {
+      sp[warp] = v.x;
+      spm[warp] = q == qc ? v.x : v.y;
     }
-    acc = warp_sum(acc);
-    if (lane == 0) sp[warp] = acc;
     __syncthreads();
-    if ((int)threadIdx.x < kReTbSeg) {
-      const int p = c * kReTbSeg + (int)threadIdx.x;
-      if (p < len) {
+    if ((int)threadIdx.x < kReSeg) {
+      const int p = cc * kReSeg + (int)threadIdx.x;   // an entry of the left half
+      if (p <= g.m / 2) {
         const int qq = p / 2 - q0;
-        const double v = (p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq];
-        ring[(side == 0 ? g.bottom : g.top) + p] = v * fac;
+        double* rs = ring + (side == 0 ? g.bottom : g.top);
+        rs[p] = ((p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq]) * fac;
+        if (p < g.m / 2) rs[g.m - p] = ((p & 1) ? 0.5 * (spm[qq] + spm[qq + 1]) : spm[qq]) * fac;
       }
     }
     return;
@@ -685,33 +682,17 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
   b -= 2 * nbt;
   const int k = b * kReWarps + warp;
   if (k >= N) return;
-  const double* ek = E + (size_t)k * N;
-  const double* s0 = spec + (size_t)(g.n / 4 - 1) * ld;       // J = n/4 + 1
-  const double* s1 = spec + (size_t)(3 * g.n / 4 - 1) * ld;   // J = 3n/4 + 1
-  double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
-  int j = lane;
-  for (; j + 32 < N; j += 64) {
-    const double e0 = ek[j], e1 = ek[j + 32];
-    a0 = fma(e0, s0[j], a0);
-    b0 = fma(e0, s1[j], b0);
-    a1 = fma(e1, s0[j + 32], a1);
-    b1 = fma(e1, s1[j + 32], b1);
-  }
-  if (j < N) {
-    a0 = fma(ek[j], s0[j], a0);
-    b0 = fma(ek[j], s1[j], b0);
-  }
-  a0 = warp_sum(a0 + a1);
-  b0 = warp_sum(b0 + b1);
+  const double2 e = warp_edge_dot(Ec, N, k, spec + (size_t)(g.n / 4 - 1) * ld, spec + (size_t)(3 * g.n / 4 - 1) * ld,
+                                  lane);   // rows J = n/4 + 1 and 3n/4 + 1
   if (lane == 0) {
-    edge[k] = fac * a0;
-    edge[N + k] = fac * b0;
+    edge[k] = fac * e.x;
+    edge[N + k] = fac * e.y;
   }
 }
 
 int dst_ring_edge_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W,
                              const double* E, double fac, double* ring, double* sd, double* edge, cudaStream_t st) {
-  const int nlr = cdiv(g.n + 1, kReLrSeg), nbt = cdiv(g.m + 1, kReTbSeg);
+  const int nlr = cdiv(g.n + 1, kReSeg), nbt = cdiv(g.m / 2 + 1, kReSeg);
   count_launch();
   k_ring_edge<<<nlr + 2 * nbt + cdiv(px.N, kReWarps), 32 * kReWarps, 0, st>>>(px.N, g, spec, ld, W, E, fac, ring, sd,
                                                                               edge, nlr, nbt);
@@ -720,13 +701,19 @@ int dst_ring_edge_from_modes(const DstPlan& px, const GridDims& g, const double*
 }
 
 // E[k][k'] = sum_j W[k][j] P(j, k'), P(j, .) the row of W at the coarse vertex get_bc puts on
-// entry p = j+1 of a side (I = m/4 + 1 + p/2 for even p, the mean of two for odd p).  One
-// thread per entry; compensated dot product (Ogita, Rump and Oishi's Dot2: error-free product
-// by fma and Knuth's two-sum), so E is close to the exact product of the tabulated W.
+// entry p = j+1 of a side (I = m/4 + 1 + p/2 for even p, the mean of two for odd p), for k' of
+// k's parity (stored at t = k'/2 of row k, pitch (N+1)/2).  One thread per entry; compensated
+// dot product (Ogita, Rump and Oishi's Dot2: error-free product by fma and Knuth's two-sum),
+// so E is close to the exact product of the tabulated W.
 __global__ void k_edge_matrix(int N, int mq, const double* __restrict__ W, double* __restrict__ E) {
+  const int Nh = (N + 1) / 2;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)N * N) return;
-  const int k = (int)(idx / N), kp = (int)(idx - (long long)k * N);
+  if (idx >= (long long)N * Nh) return;
+  const int k = (int)(idx / Nh), kp = 2 * (int)(idx - (long long)k * Nh) + (k & 1);
+  if (kp >= N) {
+    E[idx] = 0.0;
+    return;
+  }
   const double* wk = W + (size_t)k * N;
   double sum = 0.0, comp = 0.0;
   for (int j = 0; j < N; ++j) {
@@ -742,7 +729,7 @@ __global__ void k_edge_matrix(int N, int mq, const double* __restrict__ W, doubl
 }
 
 int dst_edge_matrix(const DstPlan& px, const GridDims& g, const double* W, double* E) {
-  const long long n = (long long)px.N * px.N;
+  const long long n = (long long)px.N * ((px.N + 1) / 2);
   k_edge_matrix<<<(unsigned)cdiv(n, 256), 256>>>(px.N, g.m / 4, W, E);
   IB_CUDA_CHECK(cudaGetLastError());
   IB_CUDA_CHECK(cudaDeviceSynchronize());

@@ -43,6 +43,45 @@ __device__ __forceinline__ double warp_sum(double acc) {
   return acc;
 }
 
+// A mode row's inverse x transform at a point and at its mirror image.  W's row N-1-r is
+// (-1)^k times row r in mode k, so the two values are e + o and e - o, with e and o the row's
+// sums over even and odd modes.  A lane of warp_dot_part meets only modes of its own parity,
+// so reducing the lanes within each parity gives both at the cost of one dot product.
+// Returns (e + o, e - o) on every lane.
+__device__ __forceinline__ double2 warp_sum_mirror(double acc) {
+  for (int o = 16; o > 1; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  const double other = __shfl_xor_sync(0xffffffffu, acc, 1);
+  const bool odd = threadIdx.x & 1;
+  const double e = odd ? other : acc, o = odd ? acc : other;
+  return make_double2(e + o, e - o);
+}
+
+// (E s0)_k and (E s1)_k from the parity-compact edge matrix (dst_edge_matrix: row k holds
+// E[k][2t + (k & 1)], t < (N+1)/2), for two mode rows at once; lane-strided in t, two chains,
+// then the warp's sums.
+__device__ __forceinline__ double2 warp_edge_dot(const double* __restrict__ Ec, int N, int k,
+                                                 const double* __restrict__ s0, const double* __restrict__ s1,
+                                                 int lane) {
+  const int Nh = (N + 1) / 2, pk = k & 1, nk = pk ? N / 2 : Nh;
+  const double* ek = Ec + (size_t)k * Nh;
+  s0 += pk;
+  s1 += pk;
+  double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+  int t = lane;
+  for (; t + 32 < nk; t += 64) {
+    const double e0 = ek[t], e1 = ek[t + 32];
+    a0 = fma(e0, s0[2 * t], a0);
+    b0 = fma(e0, s1[2 * t], b0);
+    a1 = fma(e1, s0[2 * t + 64], a1);
+    b1 = fma(e1, s1[2 * t + 64], b1);
+  }
+  if (t < nk) {
+    a0 = fma(ek[t], s0[2 * t], a0);
+    b0 = fma(ek[t], s1[2 * t], b0);
+  }
+  return make_double2(warp_sum(a0 + a1), warp_sum(b0 + b1));
+}
+
 struct DstPlan {
   int N = 0, M = 0, P = 0;
   int nrad = 0;
@@ -161,9 +200,11 @@ int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec
 // edge matrix E (dst_edge_matrix) and the coarse modes of the two rows get_bc reads.
 int dst_ring_edge_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W,
                              const double* E, double fac, double* ring, double* sd, double* edge, cudaStream_t st);
-// E = W P (N x N, device): P maps the coarse modes of one row to the get_bc values on entries
-// 1..m-1 of a finer level's bottom or top side, so W P maps them to that side's x transform.
-// Computed on the device at set-up (synchronous).
+// E = W P: P maps the coarse modes of one row to the get_bc values on entries 1..m-1 of a finer
+// level's bottom or top side, so W P maps them to that side's x transform.  The side's points
+// are symmetric about the centre column, so E[k][k'] vanishes unless k and k' have the same
+// parity: only those entries are kept, row k holding E[k][2t + (k & 1)] for t < (N+1)/2 (zero
+// past N-1), N x (N+1)/2 doubles.  Computed on the device at set-up (synchronous).
 int dst_edge_matrix(const DstPlan& px, const GridDims& g, const double* W, double* E);
 // sk2[k-1] = 2 sin(pi k/M), k = 1..N, into N doubles of device memory.
 int dst_sin2_table(const DstPlan& px, double* dev_out);

@@ -149,12 +149,10 @@ __global__ void __launch_bounds__(kRmThreads) k_rm_expand(int N, GridDims g, con
   b -= 2 * nTB;
   const int k = b * kRmWarps + warp;
   if (k >= N) return;
-  const double* ek = E + (size_t)k * N;
-  const double a0 = warp_sum(warp_dot_part(ek, st, N, lane));
-  const double a1 = warp_sum(warp_dot_part(ek, st + N, N, lane));
+  const double2 e = warp_edge_dot(E, N, k, st, st + N, lane);
   if (lane == 0) {
-    it.edge[y][k] = fac * a0;
-    it.edge[y][N + k] = fac * a1;
+    it.edge[y][k] = fac * e.x;
+    it.edge[y][N + k] = fac * e.y;
   }
 }
 
