@@ -256,6 +256,17 @@ __device__ __forceinline__ void tri_reg_body(const TriOp& op, const double* __re
   const int k = min(k0 + kl, nx - 1);
   const bool chunk = c < C, store = chunk && k0 + kl < nx;
   const int r0 = c * d;
+  // the tables are constant (built at creation): fetched before the wait for the previous
+  // kernel, so that under a programmatic edge they arrive while it finishes
+  double rr[kTriMaxM];
+#pragma unroll
+  for (int j = 0; j < kTriMaxM; ++j)
+    rr[j] = (chunk && c >= 1 && j < m) ? __ldg(op.rinv + ((size_t)(c - 1) * m + j) * nx + k) : 0.0;
+  for (int q = t; q < 3 * S * Mb; q += nthr) {
+    const int row = q / Mb, kk = q - row * Mb;
+    t_inv[q] = __ldg(op.inv + (size_t)row * nx + min(k0 + kk, nx - 1));
+  }
+  IB_GRID_DEP_WAIT();
   double f[S];
 #pragma unroll
   for (int j = 0; j < S; ++j) f[j] = chunk ? F[(size_t)(r0 + j) * ld + k] : 0.0;
@@ -282,14 +293,6 @@ __device__ __forceinline__ void tri_reg_body(const TriOp& op, const double* __re
       for (int j = 0; j < S; ++j) f[j] *= ps;
       fi *= ps;
     }
-  }
-  double rr[kTriMaxM];
-#pragma unroll
-  for (int j = 0; j < kTriMaxM; ++j)
-    rr[j] = (chunk && c >= 1 && j < m) ? __ldg(op.rinv + ((size_t)(c - 1) * m + j) * nx + k) : 0.0;
-  for (int q = t; q < 3 * S * Mb; q += nthr) {
-    const int row = q / Mb, kk = q - row * Mb;
-    t_inv[q] = __ldg(op.inv + (size_t)row * nx + min(k0 + kk, nx - 1));
   }
   __syncthreads();
   // phase 1: chunk solve with zero ends (the products sigma/pivot * f are off the forward
@@ -354,16 +357,14 @@ __device__ __forceinline__ void tri_reg_body(const TriOp& op, const double* __re
 template <int S>
 __global__ void __launch_bounds__(256) k_tri_reg(TriOp op, const double* __restrict__ F, double* U, int ld, int Mb,
                                                  TriBc bc) {
-  IB_GRID_DEP_WAIT();
   extern __shared__ double sm[];
-  tri_reg_body<S>(op, F, U, ld, Mb, bc, sm);
+  tri_reg_body<S>(op, F, U, ld, Mb, bc, sm);   // waits for the previous kernel after its tables
 }
 
 // The same solve for every item of a batch, blockIdx.y picking the item (its tables, input,
 // output and boundary terms); the items share the chunking.
 template <int S>
 __global__ void __launch_bounds__(256) k_tri_reg_batch(const __grid_constant__ TriBatch b, int ld, int Mb) {
-  IB_GRID_DEP_WAIT();
   extern __shared__ double sm[];
   const int y = blockIdx.y;
   tri_reg_body<S>(b.op[y], b.F[y], b.U[y], ld, Mb, b.bc[y], sm);
