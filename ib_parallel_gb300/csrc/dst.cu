@@ -539,68 +539,8 @@ __global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, con
 }
 
 // fac * get_bc (operators_fluid.F90:475-535) of the inverse x transform of a coarser level's
-// modes, without the transform: each CTA takes kRingSeg consecutive entries of one ring side,
-// evaluates the kRingSeg/2 + 1 coarse vertices they read (one warp each, the dot product of
-// k_dst_points), then forms the entries (coincident points copied, midpoints averaged).
-constexpr int kRingSeg = 32;
-constexpr int kRingWarps = kRingSeg / 2 + 1;
-__global__ void __launch_bounds__(32 * kRingWarps) k_ring_modes(int N, GridDims g, const double* __restrict__ spec,
-                                                                 int ld, const double* __restrict__ W, double fac,
-                                                                 double* __restrict__ ring) {
-  IB_GRID_DEP_WAIT();
-  __shared__ double sp[kRingWarps];
-  const int nlr = (g.n + 1 + kRingSeg - 1) / kRingSeg, nbt = (g.m + 1 + kRingSeg - 1) / kRingSeg;
-  int b = blockIdx.x, side, c;
-  if (b < 2 * nlr) {
-    side = b / nlr;
-    c = b - side * nlr;
-  } else {
-    b -= 2 * nlr;
-    side = 2 + b / nbt;
-    c = b - (side - 2) * nbt;
-  }
-  const bool lr = side < 2;
-  const int len = lr ? g.n + 1 : g.m + 1;   // entries on this side
-  const int qmax = (len - 1) / 2;           // its last coarse vertex
-  const int q0 = c * (kRingSeg / 2);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int q = q0 + warp;
-  double acc = 0.0;
-  if (q <= qmax) {
-    int I, J;
-    if (lr) {
-      I = side == 0 ? g.m / 4 + 1 : 3 * g.m / 4 + 1;
-      J = g.n / 4 + 1 + q;
-    } else {
-      J = side == 2 ? g.n / 4 + 1 : 3 * g.n / 4 + 1;
-      I = g.m / 4 + 1 + q;
-    }
-    acc = warp_dot_part(spec + (size_t)(J - 2) * ld, W + (size_t)(I - 2) * N, N, lane);
-  }
-  acc = warp_sum(acc);
-  if (lane == 0) sp[warp] = acc;
-  __syncthreads();
-  if ((int)threadIdx.x < kRingSeg) {
-    const int p = c * kRingSeg + (int)threadIdx.x;
-    if (p < len) {
-      const int qq = p / 2 - q0;
-      const double v = (p & 1) ? 0.5 * (sp[qq] + sp[qq + 1]) : sp[qq];
-      const int t = (side == 0 ? g.left : side == 1 ? g.right : side == 2 ? g.bottom : g.top) + p;
-      ring[t] = v * fac;
-    }
-  }
-}
-
-int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W, double fac,
-                        double* ring, cudaStream_t st) {
-  const int nlr = cdiv(g.n + 1, kRingSeg), nbt = cdiv(g.m + 1, kRingSeg);
-  count_launch();
-  k_ring_modes<<<2 * (nlr + nbt), 32 * kRingWarps, 0, st>>>(px.N, g, spec, ld, W, fac, ring);
-  IB_CUDA_CHECK(cudaGetLastError());
-  return IB_OK;
-}
-
-// The same ring, and with it what the finer level's solve adds to its right-hand side modes
+// modes, without the transform (dot products with W at the points get_bc reads), and with it
+// what the finer level's solve adds to its right-hand side modes
 // (the boundary terms of apply_bc, operators_fluid.F90:539-549, transformed along x):
 //  - sd[r] = x_1 + x_N and sd[nsy + r] = x_1 - x_N of its row r, the ring's left and right
 //    entries r+1 (closed form 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) of every row's two end values);
@@ -611,7 +551,8 @@ int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec
 // (warp_sum_mirror); E keeps only its entries of equal parity.  CTAs of kReWarps warps:
 // [0, nlr) take kReSeg entries of both the left and the right side (kReWarps vertex pairs);
 // [nlr, nlr + 2 nbt) kReSeg entries of the left half of the bottom or top side and their
-// mirrors; then one warp per mode k for the two edge dot products.
+// mirrors; then one warp per mode k for the two edge dot products (dst_ring_from_modes launches
+// the first two groups alone, sd and edge null).
 constexpr int kReWarps = 8;
 constexpr int kReSeg = 2 * (kReWarps - 1);   // entries a CTA writes on a side (kReWarps vertices)
 __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, const double* __restrict__ spec,
@@ -645,7 +586,7 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
         ring[g.left + p] = xl;
         ring[g.right + p] = xr;
         const int r = p - 1;
-        if (r >= 0 && r < g.nsy) {
+        if (sd && r >= 0 && r < g.nsy) {
           sd[r] = xl + xr;
           sd[g.nsy + r] = xl - xr;
         }
@@ -688,6 +629,17 @@ __global__ void __launch_bounds__(32 * kReWarps) k_ring_edge(int N, GridDims g, 
     edge[k] = fac * e.x;
     edge[N + k] = fac * e.y;
   }
+}
+
+// The ring alone (sd and edge null): the side and bottom/top CTAs only.
+int dst_ring_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W, double fac,
+                        double* ring, cudaStream_t st) {
+  const int nlr = cdiv(g.n + 1, kReSeg), nbt = cdiv(g.m / 2 + 1, kReSeg);
+  count_launch();
+  k_ring_edge<<<nlr + 2 * nbt, 32 * kReWarps, 0, st>>>(px.N, g, spec, ld, W, nullptr, fac, ring, nullptr, nullptr,
+                                                       nlr, nbt);
+  IB_CUDA_CHECK(cudaGetLastError());
+  return IB_OK;
 }
 
 int dst_ring_edge_from_modes(const DstPlan& px, const GridDims& g, const double* spec, int ld, const double* W,
