@@ -283,12 +283,9 @@ struct Ctx {
   std::vector<double*> sdv, edgev;
   double* emat = nullptr;          // edge matrix (dst_edge_matrix), its equal-parity entries: (m-1) x m/2
   // row treatments of the Schur operator's partial transforms (per vertex row)
-  unsigned char *rm_top = nullptr, *rm_coarse = nullptr, *rm_fine = nullptr, *rm_ring2 = nullptr;
+  unsigned char *rm_top = nullptr, *rm_coarse = nullptr;
   double* wmat = nullptr;          // DST-I matrix of the x transform ((m-1) x (m-1))
   double* sk2 = nullptr;           // 2 sin(pi k/m), k = 1..m-1 (closed-form boundary-row modes)
-  int2* ring_pts = nullptr;        // (row, col) points get_bc reads
-  int n_ring_pts = 0;
-  int* edge_rows = nullptr;        // rows 0 and n-2 (apply_bc's bottom and top rows)
   double* specY = nullptr;         // ainv's mode-space solution inside the Schur operator
   // work arrays
   double *spec1 = nullptr, *spec2 = nullptr, *rhs = nullptr, *rhsbc = nullptr;

@@ -526,17 +526,6 @@ __global__ void __launch_bounds__(512) k_dst_x(DstDev pl, int nrows, int ld, con
   }
 }
 
-// Selected points of an inverse x transform, one warp per point.
-__global__ void k_dst_points(int N, const double* __restrict__ spec, int ld, const int2* __restrict__ pts, int npts,
-                             const double* __restrict__ W, double* __restrict__ out) {
-  IB_GRID_DEP_WAIT();
-  int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (gw >= npts) return;
-  int2 rc = pts[gw];
-  const double acc = warp_sum(warp_dot_part(spec + (size_t)rc.x * ld, W + (size_t)rc.y * N, N, lane));
-  if (lane == 0) out[(size_t)rc.x * ld + rc.y] = acc;
-}
 
 // fac * get_bc (operators_fluid.F90:475-535) of the inverse x transform of a coarser level's
 // modes, without the transform (dot products with W at the points get_bc reads), and with it
@@ -688,33 +677,6 @@ int dst_edge_matrix(const DstPlan& px, const GridDims& g, const double* W, doubl
   return IB_OK;
 }
 
-// Rows of the forward x transform of an apply_bc boundary field, one warp per output.
-__global__ void k_dst_ring_rows(int N, GridDims g, const double* __restrict__ ring, const int* __restrict__ rows,
-                                int nrows, const double* __restrict__ W, const double* __restrict__ post_add,
-                                double post_scale, double* __restrict__ out) {
-  IB_GRID_DEP_WAIT();
-  int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (gw >= nrows * N) return;
-  int r = rows[gw / N], k = gw % N;
-  int J = r + 2;
-  const double* wk = W + (size_t)k * N;
-  double acc = 0.0;
-  for (int j = lane; j < N; j += 32) {
-    int I = j + 2;
-    double v = 0.0;
-    if (I == 2) v = v + ring[g.left + J - 1];
-    if (I == g.m) v = v + ring[g.right + J - 1];
-    if (J == 2) v = v + ring[g.bottom + I - 1];
-    if (J == g.n) v = v + ring[g.top + I - 1];
-    acc = fma(v, wk[j], acc);
-  }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) {
-    size_t o = (size_t)r * g.nsx + k;
-    out[o] = post_add ? fma(post_scale, post_add[o], acc) : acc;
-  }
-}
 
 // out = post_scale*post_add + S_x(apply_bc(ring)) on every row (operators_fluid.F90:539-549 with
 // factor 1 on a zero field).  The first nEdge CTAs take the two edge rows 0 and n-2, whose
@@ -860,24 +822,7 @@ int dst_matrix_table(const DstPlan& px, double* dev_out) {
   return IB_OK;
 }
 
-int dst_x_points(const DstPlan& px, const double* spec, int ld, const int2* pts, int npts, const double* W,
-                 double* out, cudaStream_t st) {
-  if (npts <= 0) return IB_OK;
-  count_launch();
-  k_dst_points<<<cdiv(32LL * npts, 256), 256, 0, st>>>(px.N, spec, ld, pts, npts, W, out);
-  IB_CUDA_CHECK(cudaGetLastError());
-  return IB_OK;
-}
 
-int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, const int* rows, int nrows,
-                    const double* W, const double* post_add, double post_scale, double* out, cudaStream_t st) {
-  if (nrows <= 0) return IB_OK;
-  count_launch();
-  k_dst_ring_rows<<<cdiv(32LL * nrows * px.N, 256), 256, 0, st>>>(px.N, g, ring, rows, nrows, W, post_add,
-                                                                   post_scale, out);
-  IB_CUDA_CHECK(cudaGetLastError());
-  return IB_OK;
-}
 
 // ------------------------------------------------------------- y pass
 __global__ void __launch_bounds__(512) k_dst_y(DstDev pl, int ncols, int ld, DstYArgs a, int B, int narrow_scan) {

@@ -174,15 +174,6 @@ size_t dst_smem_x(const DstPlan& p, int B);
 
 // The DST-I matrix of the x transform, W[j][k] = 2 sin(pi (j+1)(k+1)/M), N x N (symmetric).
 int dst_matrix_table(const DstPlan& px, double* dev_out);
-// Selected points of an inverse x transform: out[r*ld + c] = sum_k spec[r*ld + k] W[c][k]
-// for each (r, c) in pts (device int2 array), one warp per point.
-int dst_x_points(const DstPlan& px, const double* spec, int ld, const int2* pts, int npts, const double* W,
-                 double* out, cudaStream_t st);
-// Selected rows of a forward x transform of an apply_bc boundary field (a zero field with the
-// ring added as operators_fluid.F90:539-549 does): out[r*ld + k] = post_scale*post_add[r*ld+k]
-// + sum_j bc(r, j) W[j][k] for rows r in rows[0..nrows), one warp per output.
-int dst_x_ring_rows(const DstPlan& px, const GridDims& g, const double* ring, const int* rows, int nrows,
-                    const double* W, const double* post_add, double post_scale, double* out, cudaStream_t st);
 // out = post_scale*post_add + S_x(apply_bc(ring)) on every row (factor 1, zero field): the two
 // edge rows by dot products with W (fft_edges: by the FFT line transform, fewer FP64 instructions
 // and a longer chain), the interior rows in closed form 2 sin(pi k/M)(x_1 + (-1)^(k+1) x_N) from

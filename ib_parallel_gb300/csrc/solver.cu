@@ -218,7 +218,6 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   dbl += 6 * ns + 2 * nu + 2 * nv;                       // work (+ ainv mode-space copy)
   dbl += (size_t)g.nsx * g.nsx + (size_t)g.nsy;          // DST matrix, row treatments
   dbl += (size_t)g.nsx;                                  // 2 sin(pi k/m) table
-  dbl += (size_t)g.m + g.n + 8;                          // get_bc points, edge rows
   dbl += (size_t)(L + 3) * nbc;                          // rings
   dbl += (size_t)L * ns + (size_t)L * nbc + 2 * L;       // per-level spectra and rings (vort2flux)
   dbl += (size_t)g.nsx * g.nsx + (size_t)L * (2 * (size_t)g.nsy + 2 * (size_t)g.nsx);   // edge matrix, terms
@@ -250,10 +249,7 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
   c->rhsbc = P.take<double>(ns); c->vort = P.take<double>(ns); c->specY = P.take<double>(ns);
   c->wmat = P.take<double>((size_t)g.nsx * g.nsx);
   c->sk2 = P.take<double>(g.nsx);
-  c->ring_pts = P.take<int2>((size_t)g.m + g.n + 8);
-  c->edge_rows = P.take<int>(2);
   c->rm_top = P.take<unsigned char>(g.nsy); c->rm_coarse = P.take<unsigned char>(g.nsy);
-  c->rm_fine = P.take<unsigned char>(g.nsy); c->rm_ring2 = P.take<unsigned char>(g.nsy);
   c->nlx = P.take<double>(nu); c->hx = P.take<double>(nu);
   c->nly = P.take<double>(nv); c->hy = P.take<double>(nv);
   lv(c->lastbc, nbc);
@@ -341,36 +337,21 @@ int ctx_create(const IbParams* pin, const IbBody* bodies, int nbody, Ctx** out, 
     }
     if (rc2 != IB_OK) { *msg = "tridiagonal table upload failed"; ctx_destroy(c); return rc2; }
   }
-  // row treatments of the Schur operator's partial transforms (vertex row r = J-2):
-  // coarsify fills coarse rows J = n/4+2 .. 3n/4; apply_bc fills rows J = 2, n wholly and
-  // the first/last sample of every other row; get_bc reads rows J = n/4+1, 3n/4+1
+  // row treatments of the partial transforms (vertex row r = J-2): coarsify fills coarse rows
+  // J = n/4+2 .. 3n/4; apply_bc fills rows J = 2, n wholly and the first/last sample of every
+  // other row
   {
-    std::vector<unsigned char> top(g.nsy), coarse(g.nsy), fine(g.nsy), ring2(g.nsy), v2f(g.nsy);
+    std::vector<unsigned char> top(g.nsy), coarse(g.nsy), v2f(g.nsy);
     for (int r = 0; r < g.nsy; ++r) {
       bool centre = r >= g.n / 4 && r <= 3 * g.n / 4 - 2;
       bool edge = r == 0 || r == g.nsy - 1;
       v2f[r] = centre ? ROW_FFT : ROW_SCALE;
       top[r] = centre ? ROW_FFT : ROW_ZERO;
       coarse[r] = (centre || edge) ? ROW_FFT : ROW_EDGES;
-      fine[r] = edge ? ROW_SKIP : ROW_EDGES;   // the edge rows come from dst_x_ring_rows
-      ring2[r] = (r == g.n / 4 - 1 || r == 3 * g.n / 4 - 1) ? ROW_FFT : ROW_SKIP;
     }
     IB_CUDA_CHECK(cudaMemcpy(c->rm_top, top.data(), g.nsy, cudaMemcpyHostToDevice));
     IB_CUDA_CHECK(cudaMemcpy(c->rm_coarse, coarse.data(), g.nsy, cudaMemcpyHostToDevice));
-    IB_CUDA_CHECK(cudaMemcpy(c->rm_fine, fine.data(), g.nsy, cudaMemcpyHostToDevice));
-    IB_CUDA_CHECK(cudaMemcpy(c->rm_ring2, ring2.data(), g.nsy, cudaMemcpyHostToDevice));
     IB_CUDA_CHECK(cudaMemcpy(c->rm_v2f, v2f.data(), g.nsy, cudaMemcpyHostToDevice));
-    // points get_bc reads: rows J = n/4+1, 3n/4+1 at I = m/4+1..3m/4+1 and columns
-    // I = m/4+1, 3m/4+1 at J = n/4+1..3n/4+1 (vertex row r = J-2, column c = I-2)
-    std::vector<int2> pts;
-    for (int r : {g.n / 4 - 1, 3 * g.n / 4 - 1})
-      for (int cc = g.m / 4 - 1; cc <= 3 * g.m / 4 - 1; ++cc) pts.push_back(make_int2(r, cc));
-    for (int cc : {g.m / 4 - 1, 3 * g.m / 4 - 1})
-      for (int r = g.n / 4; r < 3 * g.n / 4 - 1; ++r) pts.push_back(make_int2(r, cc));
-    c->n_ring_pts = (int)pts.size();
-    IB_CUDA_CHECK(cudaMemcpy(c->ring_pts, pts.data(), sizeof(int2) * pts.size(), cudaMemcpyHostToDevice));
-    int er[2] = {0, g.nsy - 1};
-    IB_CUDA_CHECK(cudaMemcpy(c->edge_rows, er, sizeof(er), cudaMemcpyHostToDevice));
     int rc3 = dst_matrix_table(c->px, c->wmat);
     if (rc3 == IB_OK) rc3 = dst_sin2_table(c->px, c->sk2);
     if (rc3 == IB_OK && L > 1) rc3 = dst_edge_matrix(c->px, g, c->wmat, c->emat);
